@@ -1,0 +1,189 @@
+"""Configuration of the CRV response engine.
+
+The dataclasses keep the field names and meanings of the reference stage configurations so that a caller's
+existing objects and knob overrides carry over:
+
+  SiPMConfig      crv/crvfastsim/response/sipm.py:26-47
+  WaveformConfig  crv/crvfastsim/reco/waveform.py:29-43
+  RecoConfig      crv/crvfastsim/reco/pulsefit.py:26-46
+  SectorCuts, FinderConfig, SectorGeom   crv/crvfastsim/reco/coinc.py:29-79
+  ChainConfig, Conditions                crv/crvfastsim/chain.py:29-84
+
+ResponseConfig replaces the reference's lookup-table photon model (crv/crvfastsim/response/photons.py:45-53) by the
+analytic one of the workload: a photon yield per MeV per SiPM and a two-exponential fibre attenuation
+frac_short e^(-d/lambda_short) + (1 - frac_short) e^(-d/lambda_long), d the distance from the step to the SiPM's
+bar end; arrival time = step time + d / signal_speed + an exponential emission delay (decay_time).
+
+Defaults are the workload's values where it names one (12.55 ns sampling, 40 PE/MeV, attenuation 100/500 cm with
+fractions 0.3/0.7, cross-talk 0.05, afterpulses 0.02, 5 PE threshold, 3 of 4 layers within 10 ns) and the
+reference's stock values otherwise.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+CHAN_MULT = 32768          # SiPM label = event key * CHAN_MULT + channel (crv/crvfastsim/chain.py:25)
+PERIOD = 12.55             # digitisation period [ns] of the workload (the reference module constant is 12.5)
+NPIX = 1600                # 40 x 40 pixel grid; the inactive 4 x 4 centre leaves 1,584 live pixels
+SPE_PEAK_VOLT = 0.0055     # single-PE peak voltage of the Gumbel template [V]
+
+
+@dataclass
+class ResponseConfig:
+    yield_per_mev: float = 40.0          # PE per MeV deposited, per SiPM, at zero attenuation
+    frac_short: float = 0.3
+    lambda_short: float = 1000.0         # mm
+    lambda_long: float = 5000.0          # mm
+    signal_speed: float = 140.0          # mm/ns along the fibre
+    decay_time: float = 7.4              # ns, exponential emission delay per photon
+    photon_yield_scale: float = 1.0
+    photon_yield_variation_scale: float = 1.0
+
+
+PIXEL_IDS = ("truncate",)
+
+
+@dataclass
+class SiPMConfig:
+    n_pixels_x: int = 40
+    n_pixels_y: int = 40
+    overvoltage: float = 3.0
+    time_constant: float = 13.3
+    capacitance: float = 8.84e-14
+    p1: float = 0.607
+    p2: float = 2.7
+    cross_talk: float = 0.05
+    thermal_rate: float = 0.0
+    trap0_prob: float = 0.02
+    trap1_prob: float = 0.0
+    trap0_lifetime: float = 5.0
+    trap1_lifetime: float = 50.0
+    inactive: tuple = field(default_factory=lambda: tuple((x, y) for x in range(18, 22) for y in range(18, 22)))
+    pixel_id: str = "truncate"
+
+    def p_fire(self, v):
+        return self.p1 * (1.0 - np.exp(-np.asarray(v) / self.p2))
+
+
+@dataclass(frozen=True)
+class WaveformConfig:
+    single_pe_file: Optional[str] = None      # (t, v) text file; None = Gumbel single-PE shape below
+    single_pe_precision: float = 0.5
+    single_pe_stretch: float = 1.0
+    single_pe_max_time: float = 100.0
+    single_pe_reference_charge: float = 2.652e-13
+    min_voltage: float = 5 * SPE_PEAK_VOLT    # readout threshold: 5 PE
+    noise: float = 4.0e-4
+    samples_zs: int = 12
+    adc_conversion: float = 2300.0
+    pedestal: int = 100
+    min_adc: int = 0
+    max_adc: int = 4095
+    gumbel_peak: float = SPE_PEAK_VOLT
+    gumbel_mu: float = 15.0
+    gumbel_beta: float = 10.0
+    period: float = PERIOD
+
+
+@dataclass(frozen=True)
+class RecoConfig:
+    min_adc_difference: float = 40.0
+    default_beta: float = 19.0
+    min_beta: float = 5.0
+    max_beta: float = 40.0
+    max_time_difference: float = 15.0
+    min_pulse_height_ratio: float = 0.7
+    max_pulse_height_ratio: float = 1.5
+    le_time_factor: float = 0.985
+    samples_before: int = 4
+    samples_after: int = 3
+    pedestal_undershoot_threshold: float = 6.0
+    use_time_offset_db: bool = True
+    time_offset_scale: float = 1.0
+    ignore_channels: bool = True
+    max_pulses: int = 8
+    lm_iterations: int = 40
+    limit_tolerance: float = 0.01
+    knife_edge_adc: float = 1.0
+    period: float = PERIOD
+
+
+@dataclass(frozen=True)
+class SectorCuts:
+    pe_threshold: float
+    max_dt_adjacent: float
+    max_dt: float
+    min_slope: float
+    max_slope: float
+    max_slope_diff: float
+    coincidence_layers: int
+    min_cluster_pes: float
+    initial_max_distance: float
+    final_max_distance: float
+
+
+# the workload's coincidence: >= 3 of 4 layers within 10 ns; other cuts as the reference's extracted-v04 EX sector
+WORKLOAD_CUTS = SectorCuts(8, 10, 10, -6, 6, 3, 3, 0, 250, 0)
+
+
+@dataclass(frozen=True)
+class FinderConfig:
+    fiber_signal_speed: float = 140.0
+    max_time_interval: float = 20.0
+    time_offset: float = 34.5
+    compensate_status_bits: tuple = (0, 1, 2)
+    ignore_secondary_pulses: bool = True
+    big_cluster_threshold: int = 50000
+    cuts: dict = field(default_factory=lambda: {"EX": WORKLOAD_CUTS})
+    add_opposite_side_pulses: bool = True
+
+
+@dataclass
+class SectorGeom:
+    sector: np.ndarray
+    layer: np.ndarray
+    counter_in_type: np.ndarray
+    x: np.ndarray
+    y: np.ndarray
+    pos: np.ndarray
+    length_dir: np.ndarray
+    sector_type: np.ndarray
+    sector_names: list
+    pos_side0: np.ndarray
+    pos_side1: np.ndarray
+    sipms_side0: np.ndarray
+    sipms_side1: np.ndarray
+
+
+@dataclass
+class Conditions:
+    pedestal: np.ndarray
+    pulsearea: np.ndarray
+    pulseheight: np.ndarray
+    timeoffset: np.ndarray
+    status: np.ndarray
+    roc: np.ndarray
+    feb: np.ndarray
+    deviation: np.ndarray
+    readout_mask: Optional[np.ndarray] = None
+
+
+PRECISIONS = ("fp64", "fp32")
+
+
+@dataclass
+class ChainConfig:
+    response: ResponseConfig = field(default_factory=ResponseConfig)
+    finder: object = None
+    sipm: SiPMConfig = field(default_factory=SiPMConfig)
+    window: tuple = (0.0, 128 * PERIOD)
+    noise: bool = True
+    waveform: object = None
+    pulse_reco: object = None
+    feb_phase_width: Optional[float] = None    # None = one digitisation period
+    feb_phase_key: str = "roc_feb"
+    backend: str = "cuda"
+    precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (FP64 LM solve and absolute times)

@@ -1,0 +1,625 @@
+/*
+ * CPU oracle for the CRV response chain: TEST INFRASTRUCTURE ONLY.
+ *
+ * Only the test suite, the smoke check and the CPU-baseline leg of the benchmark load this library, and only as
+ * the checker (never as the product path).  It restates, in plain C and serially, the stochastic stages of the
+ * reference CRV response with the project's keyed Philox draws:
+ *
+ *   - photon counts per (step, SiPM): Gauss(mean, sqrt mean) if mean > 10 else Poisson(mean), then rint and a floor
+ *     at zero  (crv/crvfastsim/response/photons.py:102-112, _draw_counts/_per_substep with one substep);
+ *   - per-SiPM mirroring of the readout end (photons.py:333-356): SiPMs 0 and 2 read the -length end, 1 and 3 the
+ *     +length end; the lookup-table probabilities are replaced by the analytic yield x two-exponential attenuation;
+ *   - SiPM pixel draw from the photon-map CDF (crv/crvfastsim/response/sipm.py:80-91, "truncate" pixel ids);
+ *   - the serial SiPM model (sipm.py:141-198): per SiPM, photons in time order; a pixel fires with
+ *     p1 (1 - exp(-v/p2)), v = Vov (1 - exp(-(t - t_last)/tau)); cross-talk breadth-first to the 4 neighbours with
+ *     multiplicity merging 1 - (1 - p)^m; trap afterpulses scheduled per firing and processed after all photons in
+ *     time order; charges sorted by time (stable).
+ *
+ * Every draw is keyed by (seed, run, subrun, event, channel, step-in-event, photon, node) through Philox4x32-10
+ * (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy as 1, 2, 3", SC'11), written from the paper.
+ * The exponential, logarithm and sin/cos(pi x) used by the draws and the SiPM recovery are this project's own
+ * (Cody-Waite reduction + Taylor series; atanh series; Taylor series of sin/cos(pi x) on [0, 1/4]), so that the
+ * FP64 device kernels, which implement the same steps with the same fused multiply-adds, agree bit for bit.
+ *
+ * Build: gcc -O2 -fPIC -shared -ffp-contract=off (no contraction: every fma below is explicit).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Philox4x32-10                                                                                                  */
+
+#define PHILOX_M0 0xD2511F53u
+#define PHILOX_M1 0xCD9E8D57u
+#define PHILOX_W0 0x9E3779B9u
+#define PHILOX_W1 0xBB67AE85u
+
+void orc_philox(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)PHILOX_M0 * c0;
+        uint64_t p1 = (uint64_t)PHILOX_M1 * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += PHILOX_W0; k1 += PHILOX_W1;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* Stage tags and counter layout (word 2): bits 0-14 channel, 15-17 call, 18-23 node index, 24-27 generation,
+ * 28-31 stage.  Word 3: step-in-event << 16 | photon (or a stage-specific id).  Word 0 = event, word 1 = subrun.
+ * Key = (seed, run). */
+enum { ST_COUNT = 1, ST_PHOTON = 2, ST_SIPM = 3, ST_TDC0 = 4, ST_NOISE = 5, ST_STEPS = 6 };
+
+static inline void keyed(uint32_t seed, uint32_t run, uint32_t event, uint32_t subrun, uint32_t w2, uint32_t w3,
+                         uint32_t out[4]) {
+    uint32_t c[4] = {event, subrun, w2, w3};
+    uint32_t k[2] = {seed, run};
+    orc_philox(c, k, out);
+}
+
+static inline uint32_t w2_of(int stage, int gen, int idx, int call, int chan) {
+    return ((uint32_t)stage << 28) | ((uint32_t)gen << 24) | ((uint32_t)idx << 18) | ((uint32_t)call << 15)
+           | ((uint32_t)chan & 0x7FFFu);
+}
+
+/* 53-bit uniforms from two words: [0, 1) and (0, 1]. */
+static inline uint64_t bits53(uint32_t a, uint32_t b) { return (((uint64_t)a << 32) | b) >> 11; }
+static inline double u01(uint32_t a, uint32_t b) { return (double)bits53(a, b) * 0x1p-53; }
+static inline double u01_open(uint32_t a, uint32_t b) { return (double)(bits53(a, b) + 1) * 0x1p-53; }
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* exp, log, sincospi                                                                                             */
+
+static const double LN2_HI = 0x1.62e42fefa39efp-1;     /* ln 2 rounded to double            */
+static const double LN2_LO = 0x1.abc9e3b39803fp-56;    /* ln 2 - LN2_HI rounded to double   */
+static const double INV_LN2 = 0x1.71547652b82fep+0;    /* 1 / ln 2 rounded to double        */
+
+static inline double pow2i(int n) {                     /* 2^n for -1022 <= n <= 1023, exact */
+    uint64_t b = (uint64_t)(n + 1023) << 52;
+    double r;
+    memcpy(&r, &b, 8);
+    return r;
+}
+
+double orc_exp(double x) {
+    if (x != x) return x;
+    if (x > 709.782712893384) return INFINITY;
+    if (x < -745.2) return 0.0;
+    double n = rint(x * INV_LN2);
+    double r = fma(-n, LN2_HI, x);
+    r = fma(-n, LN2_LO, r);
+    /* Taylor series of e^r to degree 13 (|r| <= ln2/2 + tiny: truncation < 5e-18), coefficients 1/k!. */
+    double p = 1.6059043836821613e-10;         /* 1/13! */
+    p = fma(p, r, 2.08767569878681e-09);       /* 1/12! */
+    p = fma(p, r, 2.505210838544172e-08);      /* 1/11! */
+    p = fma(p, r, 2.755731922398589e-07);      /* 1/10! */
+    p = fma(p, r, 2.7557319223985893e-06);     /* 1/9!  */
+    p = fma(p, r, 2.48015873015873e-05);       /* 1/8!  */
+    p = fma(p, r, 0.0001984126984126984);      /* 1/7!  */
+    p = fma(p, r, 0.001388888888888889);       /* 1/6!  */
+    p = fma(p, r, 0.008333333333333333);       /* 1/5!  */
+    p = fma(p, r, 0.041666666666666664);       /* 1/4!  */
+    p = fma(p, r, 0.16666666666666666);        /* 1/3!  */
+    p = fma(p, r, 0.5);
+    p = fma(p, r, 1.0);
+    p = fma(p, r, 1.0);
+    int k = (int)n;
+    if (k > 1023) return (p * pow2i(1023)) * pow2i(k - 1023);
+    if (k < -1020) return (p * pow2i(-60)) * pow2i(k + 60);
+    return p * pow2i(k);
+}
+
+double orc_log(double x) {
+    if (x != x || x < 0.0) return NAN;
+    if (x == 0.0) return -INFINITY;
+    if (isinf(x)) return x;
+    int e = 0;
+    if (x < 0x1p-1022) { x *= 0x1p54; e = -54; }       /* subnormal: scale up exactly */
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    e += (int)((b >> 52) & 0x7FF) - 1023;
+    b = (b & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull;   /* m in [1, 2) */
+    double m;
+    memcpy(&m, &b, 8);
+    if (m > 1.4142135623730951) { m *= 0.5; e += 1; }          /* m in (sqrt2/2, sqrt2] */
+    double f = m - 1.0;
+    double s = f / (2.0 + f);
+    double w = s * s;
+    /* log m = 2 atanh s = 2 s (1 + w/3 + w^2/5 + ... + w^11/23) */
+    double q = 0.043478260869565216;           /* 1/23 */
+    q = fma(q, w, 0.047619047619047616);       /* 1/21 */
+    q = fma(q, w, 0.05263157894736842);        /* 1/19 */
+    q = fma(q, w, 0.058823529411764705);       /* 1/17 */
+    q = fma(q, w, 0.06666666666666667);        /* 1/15 */
+    q = fma(q, w, 0.07692307692307693);        /* 1/13 */
+    q = fma(q, w, 0.09090909090909091);        /* 1/11 */
+    q = fma(q, w, 0.1111111111111111);         /* 1/9  */
+    q = fma(q, w, 0.14285714285714285);        /* 1/7  */
+    q = fma(q, w, 0.2);                        /* 1/5  */
+    q = fma(q, w, 0.3333333333333333);         /* 1/3  */
+    double t = 2.0 * s;
+    double lm = fma(t * w, q, t);
+    double de = (double)e;
+    return fma(de, LN2_HI, fma(de, LN2_LO, lm));
+}
+
+/* sin(pi b), cos(pi b) for b in [0, 1/4]: Taylor series in b. */
+static inline double sinpi_q(double b) {
+    double w = b * b;
+    double p = 7.952054001475513e-07;
+    p = fma(p, w, -2.1915353447830217e-05);
+    p = fma(p, w, 0.00046630280576761255);
+    p = fma(p, w, -0.0073704309457143504);
+    p = fma(p, w, 0.08214588661112823);
+    p = fma(p, w, -0.5992645293207921);
+    p = fma(p, w, 2.5501640398773455);
+    p = fma(p, w, -5.16771278004997);
+    p = fma(p, w, 3.141592653589793);
+    return p * b;
+}
+
+static inline double cospi_q(double b) {
+    double w = b * b;
+    double p = -1.3878952462213771e-07;
+    p = fma(p, w, 4.303069587032947e-06);
+    p = fma(p, w, -0.0001046381049248457);
+    p = fma(p, w, 0.0019295743094039231);
+    p = fma(p, w, -0.02580689139001406);
+    p = fma(p, w, 0.2353306303588932);
+    p = fma(p, w, -1.3352627688545895);
+    p = fma(p, w, 4.0587121264167685);
+    p = fma(p, w, -4.934802200544679);
+    p = fma(p, w, 1.0);
+    return p;
+}
+
+/* sin(pi x), cos(pi x) for x in [0, 2]. */
+void orc_sincospi(double x, double *sp, double *cp) {
+    double y = x - 2.0 * rint(0.5 * x);         /* y in [-1, 1], exact */
+    double sg = 1.0;
+    if (y < 0.0) { y = -y; sg = -1.0; }         /* sin odd, cos even */
+    double s, c;
+    if (y <= 0.25) {
+        s = sinpi_q(y); c = cospi_q(y);
+    } else if (y <= 0.75) {
+        double b = 0.5 - y;                     /* exact */
+        s = cospi_q(b); c = sinpi_q(b);
+    } else {
+        double b = 1.0 - y;                     /* exact */
+        s = sinpi_q(b); c = -cospi_q(b);
+    }
+    *sp = sg * s;
+    *cp = c;
+}
+
+/* Box-Muller pair from one Philox block (u1 in (0,1] from words 0,1; u2 in [0,1) from words 2,3). */
+static inline void normal_pair(const uint32_t w[4], double *z0, double *z1) {
+    double u1 = u01_open(w[0], w[1]);
+    double u2 = u01(w[2], w[3]);
+    double r = sqrt(-2.0 * orc_log(u1));
+    double s, c;
+    orc_sincospi(2.0 * u2, &s, &c);
+    *z0 = r * c;
+    *z1 = r * s;
+}
+
+/* Poisson(lam) by inversion for lam <= 10 (u in [0, 1)). */
+static inline int64_t poisson_inv(double lam, double u) {
+    double p = orc_exp(-lam);
+    double F = p;
+    int64_t k = 0;
+    while (u >= F && k < 200) {
+        k += 1;
+        p = p * lam / (double)k;
+        F = F + p;
+    }
+    return k;
+}
+
+/* Photon count for one (step, SiPM) row: the reference rule with one substep. */
+static inline int64_t draw_count(double avg, const uint32_t w[4]) {
+    double x;
+    if (avg > 10.0) {
+        double z0, z1;
+        normal_pair(w, &z0, &z1);
+        x = avg + sqrt(avg) * z0;
+    } else {
+        double lam = avg > 0.0 ? avg : 0.0;
+        x = (double)poisson_inv(lam, u01(w[0], w[1]));
+    }
+    x = rint(x);
+    return x > 0.0 ? (int64_t)x : 0;
+}
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Parameters                                                                                                     */
+
+typedef struct {
+    uint32_t seed;
+    uint32_t pad0;
+    /* photons */
+    double yield_per_mev;       /* PE per MeV per SiPM */
+    double frac_short;          /* attenuation: frac_short e^{-d/lambda_short} + frac_long e^{-d/lambda_long} */
+    double frac_long;
+    double lambda_short;        /* mm */
+    double lambda_long;         /* mm */
+    double signal_speed;        /* mm/ns along the fibre */
+    double decay_time;          /* ns, exponential emission delay */
+    /* SiPM */
+    double overvoltage, time_constant, capacitance, p1, p2;
+    double q_ct;                /* per-neighbour cross-talk probability per firing */
+    double q_t0, q_t1;          /* trap probability per firing */
+    double trap0_lifetime, trap1_lifetime;
+    double t_end;
+    int32_t n_pixels_x, n_pixels_y;
+} OrcParams;
+
+static inline double p_fire(const OrcParams *P, double v) { return P->p1 * (1.0 - orc_exp(-v / P->p2)); }
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Photon stage                                                                                                   */
+
+/* Readout distance of SiPM s from a step at length coordinate z (relative to the bar centre). */
+static inline double readout_distance(double z, double half, int s) {
+    double d = (s % 2 == 0) ? (z + half) : (half - z);
+    if (d < 0.0) d = 0.0;
+    if (d > 2.0 * half) d = 2.0 * half;
+    return d;
+}
+
+static inline double mean_photons(const OrcParams *P, double edep, double dev, double d) {
+    double att = P->frac_short * orc_exp(-d / P->lambda_short) + P->frac_long * orc_exp(-d / P->lambda_long);
+    return P->yield_per_mev * edep * dev * att;
+}
+
+/* Per step and SiPM s: photon count (rows = nsteps x 4, row = step * 4 + s).  zloc: length coordinate of the step
+ * relative to the bar centre, half: half length of the step's bar, dev: yield factor of the row's channel.
+ * sie: step index inside its event.  Rows with a non-finite time get 0. */
+void orc_photon_counts(const OrcParams *P, int64_t nsteps, const int32_t *bar, const double *zloc, const double *t,
+                       const double *edep, const double *half, const double *dev_chan, const uint32_t *event,
+                       const uint32_t *subrun, const uint32_t *run, const int32_t *sie, int64_t *count) {
+    for (int64_t i = 0; i < nsteps; ++i) {
+        for (int s = 0; s < 4; ++s) {
+            int64_t row = i * 4 + s;
+            if (!isfinite(t[i])) { count[row] = 0; continue; }
+            int chan = bar[i] * 4 + s;
+            double d = readout_distance(zloc[i], half[i], s);
+            double avg = mean_photons(P, edep[i], dev_chan[chan], d);
+            uint32_t w[4];
+            keyed(P->seed, run[i], event[i], subrun[i], w2_of(ST_COUNT, 0, 0, 0, chan), (uint32_t)sie[i], w);
+            count[row] = draw_count(avg, w);
+        }
+    }
+}
+
+/* Arrival time of photon j of a row. */
+static inline double photon_time(const OrcParams *P, double t, double d, uint32_t seed, uint32_t run, uint32_t ev,
+                                 uint32_t sub, int chan, int32_t sie, int64_t j) {
+    uint32_t w[4];
+    keyed(seed, run, ev, sub, w2_of(ST_PHOTON, 0, 0, 0, chan), ((uint32_t)sie << 16) | (uint32_t)(j >> 1), w);
+    int h = (int)(j & 1) * 2;
+    double u = u01_open(w[h], w[h + 1]);
+    return t + d / P->signal_speed + P->decay_time * (-orc_log(u));
+}
+
+/* Emit photons for rows with precomputed counts and offsets (row order = caller's).  Per photon: step row, channel,
+ * time, key = (step-in-event << 16) | j. */
+void orc_photon_emit(const OrcParams *P, int64_t nrows, const int64_t *row_step, const int32_t *row_s,
+                     const int64_t *row_count, const int64_t *row_off, const int32_t *bar, const double *zloc,
+                     const double *t, const double *half, const uint32_t *event, const uint32_t *subrun,
+                     const uint32_t *run, const int32_t *sie, int64_t *o_step, int64_t *o_chan, double *o_time,
+                     int64_t *o_key) {
+    for (int64_t r = 0; r < nrows; ++r) {
+        int64_t i = row_step[r];
+        int s = row_s[r];
+        int chan = bar[i] * 4 + s;
+        double d = readout_distance(zloc[i], half[i], s);
+        for (int64_t j = 0; j < row_count[r]; ++j) {
+            int64_t o = row_off[r] + j;
+            o_step[o] = i;
+            o_chan[o] = chan;
+            o_time[o] = photon_time(P, t[i], d, P->seed, run[i], event[i], subrun[i], chan, sie[i], j);
+            o_key[o] = ((int64_t)sie[i] << 16) | j;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* SiPM stage                                                                                                     */
+
+#define NPX 1600
+#define MAX_GEN 15
+#define MAX_IDX 63
+
+typedef struct { double t; int64_t key; int64_t photon; } Ph;
+typedef struct { int pix; int m; } Node;
+typedef struct { double t; int pix; int64_t photon; double u_fire; int64_t ord; } Trap;
+
+static int cmp_ph(const void *a, const void *b) {
+    const Ph *x = a, *y = b;
+    if (x->t < y->t) return -1;
+    if (x->t > y->t) return 1;
+    return (x->key < y->key) ? -1 : (x->key > y->key);
+}
+
+static int cmp_trap(const void *a, const void *b) {
+    const Trap *x = a, *y = b;
+    if (x->t < y->t) return -1;
+    if (x->t > y->t) return 1;
+    return (x->ord < y->ord) ? -1 : (x->ord > y->ord);
+}
+
+typedef struct { double t; int64_t ord; } TimeOrd;
+
+static int cmp_time_ord(const void *a, const void *b) {
+    const TimeOrd *x = a, *y = b;
+    if (x->t < y->t) return -1;
+    if (x->t > y->t) return 1;
+    return (x->ord < y->ord) ? -1 : (x->ord > y->ord);
+}
+
+static int cmp_int(const void *a, const void *b) { return *(const int *)a - *(const int *)b; }
+
+typedef struct {
+    double *t, *v;
+    int64_t *photon;
+    int64_t n, cap;
+} ChargeBuf;
+
+static void push_charge(ChargeBuf *C, double t, double v, int64_t photon) {
+    if (C->n == C->cap) {
+        C->cap = C->cap ? 2 * C->cap : 256;
+        C->t = realloc(C->t, C->cap * sizeof(double));
+        C->v = realloc(C->v, C->cap * sizeof(double));
+        C->photon = realloc(C->photon, C->cap * sizeof(int64_t));
+    }
+    C->t[C->n] = t; C->v[C->n] = v; C->photon[C->n] = photon;
+    C->n++;
+}
+
+/* Pixel of a photon from the photon-map CDF (cum: 1600 running sums over bins x * 40 + y); returns -1 for dead. */
+static inline int draw_pixel(const double *cum, const uint8_t *dead, double u) {
+    double v = u * cum[NPX - 1];
+    int lo = 0, hi = NPX;                        /* first index with cum > v (searchsorted side="right") */
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (cum[mid] <= v) lo = mid + 1; else hi = mid;
+    }
+    if (lo >= NPX) lo = NPX - 1;
+    return dead[lo] ? -1 : lo;
+}
+
+/* Simulate one SiPM.  photons sorted by (t, key) already, t <= t_end.  Returns status (0 ok, 2 limit). */
+static int sipm_one(const OrcParams *P, const double *cum, const uint8_t *dead, uint32_t run, uint32_t ev,
+                    uint32_t sub, int chan, const Ph *ph, int64_t n, ChargeBuf *out, int64_t *n_fired_pix) {
+    double last[NPX];
+    for (int i = 0; i < NPX; ++i) last[i] = -INFINITY;
+    Trap *traps = NULL;
+    int64_t ntr = 0, captr = 0;
+    int status = 0;
+    const int NX = P->n_pixels_x, NY = P->n_pixels_y;
+    for (int64_t k = 0; k < n; ++k) {
+        uint32_t w3 = (uint32_t)ph[k].key;
+        uint32_t w[4];
+        keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, 0, 0, 0, chan), w3, w);
+        int pix = draw_pixel(cum, dead, u01(w[0], w[1]));
+        if (pix < 0) continue;
+        double t = ph[k].t;
+        Node fr[MAX_IDX + 1], nx[4 * (MAX_IDX + 1)];
+        int nfr = 1;
+        fr[0].pix = pix; fr[0].m = 1;
+        int gen = 0;
+        while (nfr > 0) {
+            int fired[MAX_IDX + 1];
+            double fv[MAX_IDX + 1];
+            int nf = 0;
+            for (int i = 0; i < nfr; ++i) {
+                int p = fr[i].pix;
+                double v = P->overvoltage * (1.0 - orc_exp(-(t - last[p]) / P->time_constant));
+                double pf = p_fire(P, v);
+                double q = 1.0 - pf, qm = q;
+                for (int mm = 1; mm < fr[i].m; ++mm) qm = qm * q;
+                double pm = 1.0 - qm;
+                uint32_t wf[4];
+                if (gen == 0) { wf[2] = w[2]; wf[3] = w[3]; }
+                else keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 0, chan), w3, wf);
+                if (u01(wf[2], wf[3]) < pm) { fired[nf] = i; fv[nf] = v; nf++; }
+            }
+            for (int a = 0; a < nf; ++a) {
+                int p = fr[fired[a]].pix;
+                last[p] = t;
+                push_charge(out, t, fv[a], ph[k].photon);
+            }
+            /* traps: call 1 -> (u_trap0, u_trap0_time), call 4 -> (u_trap0_fire, u_trap1),
+             *        call 5 -> (u_trap1_time, u_trap1_fire) */
+            if (P->q_t0 > 0.0 || P->q_t1 > 0.0) {
+                for (int a = 0; a < nf; ++a) {
+                    int i = fired[a];
+                    uint32_t w1[4], w4[4], w5[4];
+                    keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 1, chan), w3, w1);
+                    keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 4, chan), w3, w4);
+                    for (int tr = 0; tr < 2; ++tr) {
+                        double q = tr ? P->q_t1 : P->q_t0;
+                        if (!(q > 0.0)) continue;
+                        double ud, ut, uf;
+                        if (tr == 0) { ud = u01(w1[0], w1[1]); ut = u01_open(w1[2], w1[3]); uf = u01(w4[0], w4[1]); }
+                        else {
+                            keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 5, chan), w3, w5);
+                            ud = u01(w4[2], w4[3]); ut = u01_open(w5[0], w5[1]); uf = u01(w5[2], w5[3]);
+                        }
+                        if (ud < q) {
+                            double life = tr ? P->trap1_lifetime : P->trap0_lifetime;
+                            if (ntr == captr) { captr = captr ? 2 * captr : 64; traps = realloc(traps, captr * sizeof(Trap)); }
+                            traps[ntr].t = t - life * orc_log(ut);
+                            traps[ntr].pix = fr[i].pix;
+                            traps[ntr].photon = ph[k].photon;
+                            traps[ntr].u_fire = uf;
+                            traps[ntr].ord = ntr;
+                            ntr++;
+                        }
+                    }
+                }
+            }
+            /* cross-talk: call 2 -> (u_ct0, u_ct1), call 3 -> (u_ct2, u_ct3); neighbours x-1, x+1, y-1, y+1 */
+            int nn = 0;
+            for (int a = 0; a < nf; ++a) {
+                int i = fired[a];
+                int p = fr[i].pix, x = p / 40, y = p % 40;
+                uint32_t c2[4], c3[4];
+                keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 2, chan), w3, c2);
+                keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 3, chan), w3, c3);
+                double u[4] = {u01(c2[0], c2[1]), u01(c2[2], c2[3]), u01(c3[0], c3[1]), u01(c3[2], c3[3])};
+                int nxp[4] = {(x - 1) * 40 + y, (x + 1) * 40 + y, x * 40 + y - 1, x * 40 + y + 1};
+                int ok[4] = {x > 0, x + 1 < NX, y > 0, y + 1 < NY};
+                for (int q = 0; q < 4; ++q)
+                    if (ok[q] && u[q] < P->q_ct) { nx[nn].pix = nxp[q]; nn++; }
+            }
+            /* next frontier: unique pixels in increasing order with multiplicity, dead removed */
+            int pl[4 * (MAX_IDX + 1)];
+            for (int a = 0; a < nn; ++a) pl[a] = nx[a].pix;
+            qsort(pl, nn, sizeof(int), cmp_int);
+            nfr = 0;
+            for (int a = 0; a < nn;) {
+                int b = a;
+                while (b < nn && pl[b] == pl[a]) b++;
+                if (!dead[pl[a]]) {
+                    if (nfr > MAX_IDX) { status = 2; break; }
+                    fr[nfr].pix = pl[a]; fr[nfr].m = b - a; nfr++;
+                }
+                a = b;
+            }
+            gen++;
+            if (nfr > 0 && gen > MAX_GEN) { status = 2; nfr = 0; }
+        }
+    }
+    /* afterpulses: after all photons, in time order, no cascades */
+    if (ntr) {
+        qsort(traps, ntr, sizeof(Trap), cmp_trap);
+        for (int64_t a = 0; a < ntr; ++a) {
+            double t1 = traps[a].t;
+            if (t1 > P->t_end) continue;
+            int p = traps[a].pix;
+            double v = P->overvoltage * (1.0 - orc_exp(-(t1 - last[p]) / P->time_constant));
+            if (traps[a].u_fire < p_fire(P, v)) {
+                last[p] = t1;
+                push_charge(out, t1, v, traps[a].photon);
+            }
+        }
+    }
+    free(traps);
+    int64_t nfp = 0;
+    for (int i = 0; i < NPX; ++i) nfp += (last[i] > -INFINITY);
+    if (n_fired_pix) *n_fired_pix = nfp;
+    return status;
+}
+
+/* Stable merge of the SiPM's charge records [a0, n) by time (records before the afterpulses are already in
+ * non-decreasing time order; afterpulses are sorted by time). */
+static void stable_time_sort(ChargeBuf *C, int64_t a0) {
+    int64_t n = C->n - a0;
+    if (n < 2) return;
+    TimeOrd *k = malloc(n * sizeof(TimeOrd));
+    for (int64_t i = 0; i < n; ++i) { k[i].t = C->t[a0 + i]; k[i].ord = i; }
+    qsort(k, n, sizeof(TimeOrd), cmp_time_ord);
+    double *t = malloc(n * sizeof(double)), *v = malloc(n * sizeof(double));
+    int64_t *ph = malloc(n * sizeof(int64_t));
+    for (int64_t i = 0; i < n; ++i) {
+        t[i] = C->t[a0 + k[i].ord]; v[i] = C->v[a0 + k[i].ord]; ph[i] = C->photon[a0 + k[i].ord];
+    }
+    memcpy(C->t + a0, t, n * sizeof(double));
+    memcpy(C->v + a0, v, n * sizeof(double));
+    memcpy(C->photon + a0, ph, n * sizeof(int64_t));
+    free(k); free(t); free(v); free(ph);
+}
+
+/* SiPM stage over photons grouped by SiPM: groups [gstart[g], gstart[g] + gcount[g]) of the photon arrays, each
+ * one SiPM (channel chan_of[g] of event (run, subrun, event)[g]).  Photons need not be sorted.  Outputs are
+ * allocated here (free with orc_free) in group order, time-sorted within a group.  Per group: charge count and
+ * fired-pixel count. */
+int orc_sipm_groups(const OrcParams *P, const double *cum, const uint8_t *dead, int64_t ngroups,
+                    const int64_t *gstart, const int64_t *gcount, const int32_t *chan_of, const uint32_t *g_event,
+                    const uint32_t *g_subrun, const uint32_t *g_run, const double *time, const int64_t *key,
+                    const int64_t *photon, int64_t *n_charges_per_group, int64_t *n_fired_pix_per_group,
+                    int64_t *n_out, double **o_time, double **o_v, int64_t **o_photon) {
+    ChargeBuf C = {0};
+    int status = 0;
+    Ph *buf = NULL;
+    int64_t capb = 0;
+    for (int64_t g = 0; g < ngroups; ++g) {
+        int64_t n = 0;
+        if (gcount[g] > capb) { capb = gcount[g]; buf = realloc(buf, capb * sizeof(Ph)); }
+        for (int64_t i = 0; i < gcount[g]; ++i) {
+            int64_t a = gstart[g] + i;
+            if (!(time[a] <= P->t_end)) continue;
+            buf[n].t = time[a]; buf[n].key = key[a]; buf[n].photon = photon[a]; n++;
+        }
+        qsort(buf, n, sizeof(Ph), cmp_ph);
+        int64_t a0 = C.n;
+        int st = sipm_one(P, cum, dead, g_run[g], g_event[g], g_subrun[g], chan_of[g], buf, n, &C,
+                          &n_fired_pix_per_group[g]);
+        if (st) status = st;
+        stable_time_sort(&C, a0);
+        n_charges_per_group[g] = C.n - a0;
+    }
+    free(buf);
+    *n_out = C.n;
+    *o_time = C.t; *o_v = C.v; *o_photon = C.photon;
+    return status;
+}
+
+void orc_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* TDC0 and electronics noise                                                                                     */
+
+/* One uniform in [0, 1) per (event, FEB key). */
+void orc_tdc0_uniform(uint32_t seed, int64_t n, const uint32_t *run, const uint32_t *event, const uint32_t *subrun,
+                      const uint32_t *febkey, double *u) {
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t w[4];
+        keyed(seed, run[i], event[i], subrun[i], (uint32_t)ST_TDC0 << 28, febkey[i], w);
+        u[i] = u01(w[0], w[1]);
+    }
+}
+
+/* Standard normal per (event, channel, tick). */
+void orc_noise_normal(uint32_t seed, int64_t n, const uint32_t *run, const uint32_t *event, const uint32_t *subrun,
+                      const int32_t *chan, const int64_t *tick, double *z) {
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t w[4];
+        int64_t tk = tick[i];
+        int64_t pair = tk >> 1;              /* arithmetic shift (floor division by 2) */
+        keyed(seed, run[i], event[i], subrun[i], ((uint32_t)ST_NOISE << 28) | ((uint32_t)chan[i] & 0x7FFFu),
+              (uint32_t)pair, w);
+        double z0, z1;
+        normal_pair(w, &z0, &z1);
+        z[i] = (tk & 1) ? z1 : z0;
+    }
+}
+
+/* Raw keyed block (for tests of the key layout). */
+void orc_keyed_block(uint32_t seed, uint32_t run, uint32_t event, uint32_t subrun, uint32_t w2, uint32_t w3,
+                     uint32_t out[4]) {
+    keyed(seed, run, event, subrun, w2, w3, out);
+}
+
+/* Vector forms of the math functions (tests against libm). */
+void orc_exp_v(int64_t n, const double *x, double *y) { for (int64_t i = 0; i < n; ++i) y[i] = orc_exp(x[i]); }
+void orc_log_v(int64_t n, const double *x, double *y) { for (int64_t i = 0; i < n; ++i) y[i] = orc_log(x[i]); }
+void orc_sincospi_v(int64_t n, const double *x, double *s, double *c) {
+    for (int64_t i = 0; i < n; ++i) orc_sincospi(x[i], s + i, c + i);
+}
+/* Photon counts from given means (distribution tests): one row per mean, keyed by (event = i). */
+void orc_counts_from_mean(uint32_t seed, int64_t n, const double *avg, int64_t *count) {
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t w[4];
+        keyed(seed, 0, (uint32_t)i, 0, w2_of(ST_COUNT, 0, 0, 0, 0), 0, w);
+        count[i] = draw_count(avg[i], w);
+    }
+}

@@ -1,0 +1,390 @@
+"""Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
+
+Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR]
+The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
+tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
+module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
+
+Fixtures (compressed .npz, a few hundred kB in total):
+  pulsefit.npz   reconstruct / reconstruct_full outputs for single-pulse, KPP-like, uneven multi-pulse and edge-case
+                 waveforms (crv/crvfastsim/reco/pulsefit.py:222-316)
+  concat.npz     concat_waveforms grouping (pulsefit.py:319-345)
+  waveform.npz   _synthesize digis with and without injected noise (crv/crvfastsim/reco/waveform.py:96-172) and the
+                 resampled Gumbel single-PE template (waveform.py:46-62)
+  coinc.npz      find_event clusters on three geometries, scalar and vectorised combination checks
+                 (crv/crvfastsim/reco/coinc.py:289-392, coinc_cpu.py:11-51)
+  stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
+"""
+import os
+import sys
+import tempfile
+from dataclasses import replace
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference/crv")
+sys.path.insert(0, str(HERE.parent / "refshim"))
+sys.path.insert(0, str(REF))
+os.environ["CRVFS_CPU_ATTACHMENT"] = "numpy"
+
+from crvfastsim.reco import coinc as C          # noqa: E402
+from crvfastsim.reco import pulsefit as PF      # noqa: E402
+from crvfastsim.reco import synth as SY         # noqa: E402
+from crvfastsim.reco import waveform as WF      # noqa: E402
+from crvfastsim.response import photons as PH   # noqa: E402
+from crvfastsim.response import sipm as SI      # noqa: E402
+
+PERIOD = 12.55
+
+
+def set_period(p):
+    PF.PERIOD = p
+    WF.PERIOD = p
+    SY.PERIOD = p
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# pulse fit
+
+def gumbel(t, A, mu, b):
+    z = (t - mu) / b
+    return A * np.exp(-z - np.exp(-z))
+
+
+def single_pulses(rng, W=160, n=24, start=10):
+    t = (start + np.arange(n)) * PERIOD
+    A = rng.uniform(300, 2000, W)
+    mu = (start + 6) * PERIOD + rng.uniform(-6, 6, W)
+    b = rng.uniform(14, 24, W)
+    y = gumbel(t[None, :], A[:, None], mu[:, None], b[:, None])
+    adc = np.round(y + 100.0 + rng.normal(0, 2.0, (W, n))).astype(np.int64)
+    return adc, np.full(W, n), np.full(W, start), np.full(W, 100.0), np.full(W, 400.0), np.full(W, 30.0)
+
+
+def uneven(rng, W=120):
+    """Uneven multi-pulse waveforms: lengths over {32, 64, 128, 256, 512}, 1-12 pulses, log-uniform 5-500 PE."""
+    lens = rng.choice([32, 64, 128, 256, 512], W)
+    L = int(lens.max())
+    area = 400.0
+    adc = np.zeros((W, L), np.int64)
+    start = rng.integers(0, 200, W)
+    for w in range(W):
+        n = lens[w]
+        t = (start[w] + np.arange(n)) * PERIOD
+        y = np.zeros(n)
+        for _ in range(rng.integers(1, 13)):
+            pe = np.exp(rng.uniform(np.log(5), np.log(500)))
+            b = rng.uniform(10, 25)
+            mu = t[0] + rng.uniform(0, n * PERIOD)
+            y += gumbel(t, pe * area / b, mu, b)
+        adc[w, :n] = np.clip(np.round(y + 100.0 + rng.normal(0, 2.0, n)), 0, 4095)
+    return adc, lens, start, np.full(W, 100.0), np.full(W, area), np.full(W, area / 15.0)
+
+
+def edge_cases():
+    rows = []
+    n = 24
+    t = (10 + np.arange(n)) * PERIOD
+    rows.append(np.full(n, 100))                                        # flat
+    rows.append(np.full(n, 4095))                                       # saturated flat
+    sat = np.clip(np.round(gumbel(t, 30000.0, 16 * PERIOD, 19.0) + 100), 0, 4095)
+    rows.append(sat)                                                     # saturated pulse (plateau)
+    rows.append(np.round(gumbel(t, 800.0, 16 * PERIOD, 19.0) + 90.0))  # pedestal undershoot
+    rows.append(np.round(gumbel(t, 30.0, 16 * PERIOD, 19.0) + 100.0))  # below threshold
+    rows.append(np.round(gumbel(t, 800.0, 11 * PERIOD, 19.0) + 100.0))  # peak at the start
+    rows.append(np.round(gumbel(t, 800.0, 33 * PERIOD, 19.0) + 100.0))  # peak at the end
+    p2 = gumbel(t, 900.0, 14 * PERIOD, 15.0) + gumbel(t, 600.0, 19 * PERIOD, 15.0)
+    rows.append(np.round(p2 + 100.0))                                   # two overlapping pulses
+    pl = np.full(n, 100.0); pl[8:12] = 400; pl[12:14] = 200            # plateau then fall
+    rows.append(pl)
+    adc = np.stack(rows).astype(np.int64)
+    W = len(adc)
+    nn = np.full(W, n)
+    extra = np.stack([np.round(gumbel(t, 800.0, 16 * PERIOD, 19.0) + 100.0)] * 4).astype(np.int64)
+    adc = np.concatenate([adc, extra])
+    nn = np.concatenate([nn, [1, 2, 3, 7]])                              # short valid lengths
+    W = len(adc)
+    return adc, nn, np.full(W, 10), np.full(W, 100.0), np.full(W, 400.0), np.full(W, 30.0)
+
+
+def run_pulsefit(tag, args, out, full=False):
+    adc, n, st, ped, area, height = args
+    f = PF.reconstruct_full if full else PF.reconstruct
+    r = f(adc, n, st, ped, area, height, PF.RecoConfig())
+    out[f"{tag}_adc"], out[f"{tag}_n"], out[f"{tag}_start"] = adc, n, st
+    out[f"{tag}_ped"], out[f"{tag}_area"], out[f"{tag}_height"] = ped, area, height
+    for k, v in r.items():
+        out[f"{tag}_out_{k}"] = v
+
+
+def make_pulsefit():
+    rng = np.random.default_rng(101)
+    out = {}
+    set_period(PERIOD)
+    run_pulsefit("single", single_pulses(rng), out)
+    adc, n, st, ped, area, height = SY.waveforms(40, seed=3, L=12)
+    run_pulsefit("kpp", (adc, n, st, ped, area, height), out)
+    run_pulsefit("uneven", uneven(rng), out, full=True)
+    run_pulsefit("edge", edge_cases(), out, full=True)
+    set_period(12.5)
+    run_pulsefit("p125", single_pulses(np.random.default_rng(7), W=40), out)
+    set_period(PERIOD)
+    out["period"] = np.array([PERIOD])
+    np.savez_compressed(HERE / "pulsefit.npz", **out)
+
+
+def make_concat():
+    rng = np.random.default_rng(5)
+    nd = 400
+    key = np.sort(rng.integers(0, 20, nd))
+    bar = rng.integers(0, 3, nd)
+    sipm = rng.integers(0, 2, nd)
+    o = np.lexsort((bar, key))
+    key, bar, sipm = key[o], bar[o], sipm[o]
+    lens = np.full(nd, 12)
+    tdc = np.zeros(nd, np.int64)
+    for i in range(1, nd):
+        same = key[i] == key[i - 1] and bar[i] == bar[i - 1] and sipm[i] == sipm[i - 1]
+        tdc[i] = tdc[i - 1] + (12 if (same and rng.random() < 0.5) else int(rng.integers(13, 40)))
+    flat = rng.integers(0, 4096, nd * 12)
+    gid, mat, n, start, first = PF.concat_waveforms(key, bar, sipm, tdc, flat, lens)
+    np.savez_compressed(HERE / "concat.npz", key=key, bar=bar, sipm=sipm, tdc=tdc, flat=flat, lens=lens, gid=gid,
+                        mat=mat, n=n, start=start, first=first)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# waveform synthesis
+
+class InjectedNormal:
+    """rng stand-in: normal(loc, scale, size) = loc + scale * Z[:size] from a fixed standard-normal matrix."""
+
+    def __init__(self, Z):
+        self.Z = Z
+        self.calls = []
+
+    def normal(self, loc, scale, size):
+        C_, L_ = size
+        self.calls.append(size)
+        return loc + scale * self.Z[:C_, :L_]
+
+
+def gumbel_template_file(path, peak=0.0055, mu=15.0, beta=10.0, precision=0.5, max_time=100.0):
+    t = np.arange(0.0, max_time + precision / 2, precision)
+    v = peak * np.e * np.exp(-(t - mu) / beta - np.exp(-(t - mu) / beta))
+    np.savetxt(path, np.c_[t, v], fmt="%.17g")
+    return t, v
+
+
+def charges_sample(rng, nchan=150):
+    chans, times, qs = [], [], []
+    qref = 2.652e-13
+    for c in range(nchan):
+        lab = 40000 + 3 * c                                              # arbitrary labels, increasing
+        ncl = rng.integers(1, 4)
+        t0s = np.sort(rng.uniform(-40.0, 1700.0, ncl))
+        tt = []
+        for t0 in t0s:
+            k = rng.integers(1, 60)
+            tt.append(t0 + np.sort(rng.exponential(8.0, k)))
+        tt = np.sort(np.concatenate(tt))
+        q = qref * rng.choice([1.0, 0.93, 0.5, 0.07, 1.0], len(tt))
+        chans.append(np.full(len(tt), lab)); times.append(tt); qs.append(q)
+    return np.concatenate(chans), np.concatenate(times), np.concatenate(qs)
+
+
+def make_waveform():
+    set_period(PERIOD)
+    rng = np.random.default_rng(11)
+    tmpdir = tempfile.mkdtemp()
+    path = os.path.join(tmpdir, "gumbel_spe.txt")
+    traw, vraw = gumbel_template_file(path)
+    cfg = WF.WaveformConfig(single_pe_file=path, single_pe_stretch=1.0, min_voltage=5 * 0.0055)
+    tmpl = WF.single_pe_template(cfg.single_pe_file, cfg.single_pe_precision, cfg.single_pe_stretch,
+                                 cfg.single_pe_max_time)
+    chan, time, charge = charges_sample(rng)
+    uch = np.unique(chan)
+    tdc0_tab = rng.uniform(0, PERIOD, len(uch))
+    lut = lambda lab: tdc0_tab[np.searchsorted(uch, lab)]              # noqa: E731
+    window = (0.0, 128 * PERIOD)
+    out = dict(template=tmpl, traw=traw, vraw=vraw, chan=chan, time=time, charge=charge, uch=uch,
+               tdc0_tab=tdc0_tab, window=np.array(window), min_voltage=np.array([cfg.min_voltage]),
+               stretch=np.array([cfg.single_pe_stretch]))
+    a = WF._synthesize(chan, time, charge, lut, cfg, window, None)
+    for k, v in a.items():
+        out[f"clean_{k}"] = v
+    Z = np.random.default_rng(12).standard_normal((4000, 600))
+    inj = InjectedNormal(Z)
+    b = WF._synthesize(chan, time, charge, lut, cfg, window, inj)
+    assert len(inj.calls) == 1
+    out["noise_shape"] = np.array(inj.calls[0])
+    out["noise_Z"] = Z[:inj.calls[0][0], :inj.calls[0][1]]
+    for k, v in b.items():
+        out[f"noisy_{k}"] = v
+    np.savez_compressed(HERE / "waveform.npz", **out)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# coincidences
+
+def module_geom(n_layers=4, n_counters=16, pitch=51.3, layer_pitch=21.1, stagger=12.8, half_length=2250.0):
+    """One module of 4 x 16 counters, lengths along z, widths along x, thickness along y (one sector EX)."""
+    layer = np.repeat(np.arange(n_layers), n_counters)
+    counter = np.tile(np.arange(n_counters), n_layers)
+    x = (counter - (n_counters - 1) / 2) * pitch + stagger * (layer % 2)
+    y = (layer - (n_layers - 1) / 2) * layer_pitch
+    nb = len(layer)
+    return C.SectorGeom(sector=np.zeros(nb, int), layer=layer, counter_in_type=counter, x=x, y=y,
+                        pos=np.column_stack([x, y, np.zeros(nb)]), length_dir=np.array([2]),
+                        sector_type=np.array([1]), sector_names=["EX"], pos_side0=np.array([-half_length]),
+                        pos_side1=np.array([half_length]), sipms_side0=np.array([True]),
+                        sipms_side1=np.array([True]))
+
+
+def two_sector_geom():
+    """Two sectors of different types and lengths, the second read out on side 0 only."""
+    a = module_geom()
+    b = module_geom(half_length=1150.0)
+    nb = len(a.layer)
+    return C.SectorGeom(sector=np.r_[np.zeros(nb, int), np.ones(nb, int)], layer=np.r_[a.layer, b.layer],
+                        counter_in_type=np.r_[a.counter_in_type, b.counter_in_type], x=np.r_[a.x, b.x + 2000.0],
+                        y=np.r_[a.y, b.y], pos=np.r_[a.pos, b.pos + [2000.0, 0, 300.0]], length_dir=np.array([2, 2]),
+                        sector_type=np.array([1, 2]), sector_names=["EX", "T1"],
+                        pos_side0=np.array([-2250.0, -850.0]), pos_side1=np.array([2250.0, 1450.0]),
+                        sipms_side0=np.array([True, True]), sipms_side1=np.array([True, False]))
+
+
+def test_geom8():
+    """The eight-bar, one-sector geometry of the reference attachment tests (two counters x four layers)."""
+    layer = np.tile(np.arange(4), 2)
+    x = np.repeat([0., 400.], 4)
+    y = layer * 10.
+    return C.SectorGeom(sector=np.zeros(8, dtype=int), layer=layer, counter_in_type=np.repeat([0, 1], 4), x=x, y=y,
+                        pos=np.column_stack([x, y, np.zeros(8)]), length_dir=np.array([2]),
+                        sector_type=np.array([1]), sector_names=["EX"], pos_side0=np.array([-700.]),
+                        pos_side1=np.array([700.]), sipms_side0=np.array([True]), sipms_side1=np.array([True]))
+
+
+def flatten_clusters(rows_per_event):
+    """Flatten per-event cluster rows into arrays (event, fields) and a member table."""
+    out = {k: [] for k in ("ev", "type", "pe", "start", "end", "slope", "avgtime", "poscalc", "pos", "sidepe",
+                           "sidetime", "sidehits", "nlayers")}
+    mem_cl, mem_idx = [], []
+    for e, rows in rows_per_event:
+        for r in rows:
+            n = len(out["ev"])
+            out["ev"].append(e); out["type"].append(r["sectortype"]); out["pe"].append(r["pe"])
+            out["start"].append(r["start"]); out["end"].append(r["end"]); out["slope"].append(r["slope"])
+            out["avgtime"].append(r["avgtime"]); out["poscalc"].append(r["poscalc"])
+            out["pos"].append(np.asarray(r["pos"], float)); out["sidepe"].append(r["sidepe"])
+            out["sidetime"].append(r["sidetime"]); out["sidehits"].append(r["sidehits"])
+            out["nlayers"].append(len(r["layers"]))
+            mem_cl += [n] * len(r["pulses"]); mem_idx += list(r["pulses"])
+    res = {k: np.asarray(v) for k, v in out.items()}
+    res["pos"] = np.asarray(out["pos"], float).reshape(-1, 3)
+    res["mem_cl"] = np.asarray(mem_cl, np.int64)
+    res["mem_idx"] = np.asarray(mem_idx, np.int64)
+    return res
+
+
+def random_small_events(rng, n_events):
+    """Small events on the eight-bar geometry with quantised times and PEs (ties, attachment, secondary pulses)."""
+    ev, idx, bar, sipm, time, pe, seq = [], [], [], [], [], [], []
+    for e in range(n_events):
+        k = rng.integers(3, 14)
+        for i in range(k):
+            ev.append(e); idx.append(i); bar.append(rng.integers(0, 8)); sipm.append(rng.integers(0, 4))
+            time.append(100.0 + 2.5 * rng.integers(0, 8)); pe.append(float(rng.choice([3.0, 5.0, 10.0, 20.0])))
+            seq.append(int(rng.random() < 0.1))
+    return dict(ev=np.array(ev), idx=np.array(idx), bar=np.array(bar), sipm=np.array(sipm), time=np.array(time),
+                pe=np.array(pe), seq=np.array(seq))
+
+
+def run_coinc(tag, P, G, cfg, status, out):
+    for vec in (False, True):
+        rows = []
+        ue = np.unique(P["ev"])
+        for e in ue:
+            m = P["ev"] == e
+            p = {k: P[k][m] for k in ("idx", "bar", "sipm", "time", "pe", "seq")}
+            rows.append((e, C.find_event(p, G, status, cfg, vectorized=vec)))
+        fl = flatten_clusters(rows)
+        for k, v in fl.items():
+            out[f"{tag}_{'vec' if vec else 'scalar'}_{k}"] = v
+    for k in ("ev", "idx", "bar", "sipm", "time", "pe", "seq"):
+        out[f"{tag}_in_{k}"] = P[k]
+    out[f"{tag}_status"] = status
+    for k in ("sector", "layer", "counter_in_type", "x", "y", "pos", "length_dir", "sector_type", "pos_side0",
+              "pos_side1", "sipms_side0", "sipms_side1"):
+        out[f"{tag}_G_{k}"] = np.asarray(getattr(G, k))
+    out[f"{tag}_G_sector_names"] = np.array(G.sector_names)
+
+
+def cuts_array(cfg, names):
+    return np.array([[getattr(cfg.cuts[n], f) for f in ("pe_threshold", "max_dt_adjacent", "max_dt", "min_slope",
+                                                          "max_slope", "max_slope_diff", "coincidence_layers",
+                                                          "min_cluster_pes", "initial_max_distance",
+                                                          "final_max_distance")] for n in names])
+
+
+def make_coinc():
+    out = {}
+    base = replace(C.EXTRACTED_V04["EX"], max_dt=10.0, coincidence_layers=3)
+    # module: synthetic track + noise events from the reference generator
+    G = module_geom()
+    cfg = C.FinderConfig(cuts={"EX": base})
+    P = SY.coinc_events(300, G, seed=4, noise_mean=10.0, shower_frac=0.1, shower_mean=30.0)
+    status = np.zeros(4 * len(G.layer), np.int64)
+    status[[5, 9, 130]] = [1, 4, 2]                                     # compensated partners
+    run_coinc("module", P, G, cfg, status, out)
+    out["module_cuts"] = cuts_array(cfg, ["EX"])
+    # two sector types, one single-sided
+    G2 = two_sector_geom()
+    cfg2 = C.FinderConfig(cuts={"EX": base, "T1": replace(base, max_dt=8.0, coincidence_layers=4)})
+    P2 = SY.coinc_events(200, G2, seed=9, noise_mean=6.0, shower_frac=0.1, shower_mean=30.0)
+    run_coinc("two", P2, G2, cfg2, np.zeros(4 * len(G2.layer), np.int64), out)
+    out["two_cuts"] = cuts_array(cfg2, ["EX", "T1"])
+    # eight bars: ties and attachment
+    G3 = test_geom8()
+    cfg3 = C.FinderConfig(cuts={"EX": replace(C.EXTRACTED_V04["EX"], max_dt=10.0)})
+    P3 = random_small_events(np.random.default_rng(21), 400)
+    run_coinc("eight", P3, G3, cfg3, np.zeros(32, np.int64), out)
+    out["eight_cuts"] = cuts_array(cfg3, ["EX"])
+    fc = C.FinderConfig()
+    out["finder"] = np.array([fc.fiber_signal_speed, fc.max_time_interval, fc.time_offset])
+    np.savez_compressed(HERE / "coinc.npz", **out)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# statistics of the stochastic reference stages
+
+def make_stats():
+    out = {}
+    rng = np.random.default_rng(31)
+    cfg = replace(SI.SiPMConfig(pixel_id="truncate"), cross_talk=0.05, trap0_prob=0.02)
+    S = 4000
+    n = rng.poisson(80, S)
+    chan = np.repeat(np.arange(S), n)
+    t = np.repeat(rng.uniform(0, 1500, S), n) + rng.exponential(7.4, len(chan))
+    r = SI.simulate(chan, t, np.arange(len(chan)), np.ones((40, 40)), cfg, np.random.default_rng(32), t_end=1606.4)
+    out["sipm_nphot"] = np.array([len(chan)])
+    out["sipm_charges"] = np.array([len(r["pe"])])
+    out["sipm_pe_sum"] = np.array([r["pe"].sum()])
+    out["sipm_frac_low"] = np.array([(r["pe"] < 0.99).mean()])
+    out["sipm_S"], out["sipm_n"] = np.array([S]), n
+    out["sipm_tspread_seed"] = np.array([31])
+    for m in (0.5, 3.0, 9.9, 10.1, 40.0, 200.0):
+        c = PH._per_substep(np.full(200_000, m), np.ones(200_000, np.int64), np.random.default_rng(int(m * 10)))
+        out[f"count_{m}"] = np.array([c.mean(), c.var()])
+    np.savez_compressed(HERE / "stats.npz", **out)
+
+
+if __name__ == "__main__":
+    make_pulsefit()
+    make_concat()
+    make_waveform()
+    make_coinc()
+    make_stats()
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)

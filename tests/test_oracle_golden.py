@@ -1,0 +1,116 @@
+"""The oracle against golden fixtures generated from the reference itself (tests/golden/make_golden.py).
+
+Integer outputs must be identical; floating outputs identical up to 1e-12 relative (the NumPy restatement performs
+the reference's operations in the reference's order, so on the generating machine they are bit-identical; the
+tolerance only covers a different libm/SIMD exp on another host).
+"""
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from crvgpu import config as CF
+
+FLOAT_RTOL = 1e-12
+
+
+def assert_same(a, b, name):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape, f"{name}: shape {a.shape} != {b.shape}"
+    if a.dtype.kind in "fc" or b.dtype.kind in "fc":
+        np.testing.assert_allclose(a, b, rtol=FLOAT_RTOL, atol=1e-300, err_msg=name)
+    else:
+        assert np.array_equal(a, b), f"{name}: values differ"
+
+
+@pytest.mark.parametrize("tag", ["single", "kpp", "uneven", "edge", "p125"])
+def test_pulsefit_matches_reference(golden, tag):
+    g = golden("pulsefit.npz")
+    period = 12.5 if tag == "p125" else float(g["period"][0])
+    cfg = CF.RecoConfig(period=period)
+    args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
+    f = O.reconstruct_full if tag in ("uneven", "edge") else O.reconstruct
+    r = f(*args, cfg, period)
+    keys = [k[len(tag) + 5:] for k in g.files if k.startswith(f"{tag}_out_")]
+    assert set(keys) == set(r)
+    for k in keys:
+        assert_same(r[k], g[f"{tag}_out_{k}"], f"{tag}.{k}")
+
+
+def test_concat_matches_reference(golden):
+    g = golden("concat.npz")
+    gid, mat, n, start, first = O.concat_waveforms(g["key"], g["bar"], g["sipm"], g["tdc"], g["flat"], g["lens"])
+    for k, v in (("gid", gid), ("mat", mat), ("n", n), ("start", start), ("first", first)):
+        assert_same(v, g[k], k)
+
+
+def _wf_cfg(g):
+    return CF.WaveformConfig(min_voltage=float(g["min_voltage"][0]), single_pe_stretch=float(g["stretch"][0]))
+
+
+def test_template_resampling_matches_reference(golden):
+    g = golden("waveform.npz")
+    t = O.resample_template(g["traw"], g["vraw"], 0.5, float(g["stretch"][0]), 100.0)
+    assert_same(t, g["template"], "template")
+    t2, v2 = O.gumbel_template_raw(CF.SPE_PEAK_VOLT, 15.0, 10.0)
+    assert np.allclose(v2, g["vraw"], rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("mode", ["clean", "noisy"])
+def test_waveform_matches_reference(golden, mode):
+    g = golden("waveform.npz")
+    cfg = _wf_cfg(g)
+    uch, tab = g["uch"], g["tdc0_tab"]
+    lut = lambda lab: tab[np.searchsorted(uch, lab)]                     # noqa: E731
+    noise = None
+    if mode == "noisy":
+        Z = g["noise_Z"]
+        noise = lambda labels, tick0, shape: Z[:shape[0], :shape[1]]      # noqa: E731
+    r = O.synthesize(g["chan"], g["time"], g["charge"], lut, g["template"], cfg, 12.55, tuple(g["window"]), noise)
+    for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc", "cluster_chan", "cluster_tstart", "cluster_keep"):
+        assert_same(r[k], g[f"{mode}_{k}"], f"{mode}.{k}")
+    if mode == "noisy":
+        assert tuple(g["noise_shape"]) == (len(r["cluster_chan"]), g["noise_Z"].shape[1])
+
+
+def _geom(g, tag):
+    G = SimpleNamespace(**{k: g[f"{tag}_G_{k}"] for k in ("sector", "layer", "counter_in_type", "x", "y", "pos",
+                                                           "length_dir", "sector_type", "pos_side0", "pos_side1",
+                                                           "sipms_side0", "sipms_side1")})
+    G.sector_names = [str(s) for s in g[f"{tag}_G_sector_names"]]
+    return G
+
+
+def _finder(g, tag):
+    cuts = {}
+    for name, row in zip(_geom(g, tag).sector_names, g[f"{tag}_cuts"]):
+        cuts[name] = CF.SectorCuts(*[int(v) if i == 6 else float(v) for i, v in enumerate(row)])
+    return CF.FinderConfig(cuts=cuts)
+
+
+@pytest.mark.parametrize("tag", ["module", "two", "eight"])
+def test_coincidences_match_reference(golden, tag):
+    g = golden("coinc.npz")
+    G, cfg, status = _geom(g, tag), _finder(g, tag), g[f"{tag}_status"]
+    P = {k: g[f"{tag}_in_{k}"] for k in ("ev", "idx", "bar", "sipm", "time", "pe", "seq")}
+    got = {k: [] for k in ("ev", "type", "pe", "start", "end", "slope", "avgtime", "poscalc", "pos", "sidepe",
+                           "sidetime", "sidehits", "nlayers")}
+    mem_cl, mem_idx = [], []
+    for e in np.unique(P["ev"]):
+        m = P["ev"] == e
+        for r in O.find_event({k: P[k][m] for k in ("idx", "bar", "sipm", "time", "pe", "seq")}, G, status, cfg):
+            n = len(got["ev"])
+            got["ev"].append(e); got["type"].append(r["sectortype"]); got["pe"].append(r["pe"])
+            got["start"].append(r["start"]); got["end"].append(r["end"]); got["slope"].append(r["slope"])
+            got["avgtime"].append(r["avgtime"]); got["poscalc"].append(r["poscalc"]); got["pos"].append(r["pos"])
+            got["sidepe"].append(r["sidepe"]); got["sidetime"].append(r["sidetime"])
+            got["sidehits"].append(r["sidehits"]); got["nlayers"].append(len(r["layers"]))
+            mem_cl += [n] * len(r["pulses"]); mem_idx += list(r["pulses"])
+    for k, v in got.items():
+        ref = g[f"{tag}_scalar_{k}"]
+        v = np.asarray(v, float).reshape(ref.shape) if k == "pos" else np.asarray(v)
+        assert_same(v, ref, f"{tag}.{k}")
+    assert_same(mem_cl, g[f"{tag}_scalar_mem_cl"], "mem_cl")
+    assert_same(mem_idx, g[f"{tag}_scalar_mem_idx"], "mem_idx")
+    assert len(got["ev"]) > 0
