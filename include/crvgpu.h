@@ -1,0 +1,198 @@
+/*
+ * crvgpu: C ABI of the GB300 CRV response engine (CrvSteps -> SiPM charges -> digis -> reco pulses -> coincidence
+ * clusters).  Plain pointers and sizes only; every array argument is a DEVICE pointer owned by the caller (the
+ * Python host allocates it with PyTorch); `stream` is a cudaStream_t; no call synchronises the host.
+ *
+ * Each entry point replaces one stage function of the reference's Python API (RobMina/mu2e-fastsim, CRV package):
+ *
+ *   crv_photon_counts / crv_photons  <- crvfastsim.response.photons.make_photons      (crv/crvfastsim/response/photons.py:359)
+ *   crv_sipm                         <- crvfastsim.response.sipm.simulate             (crv/crvfastsim/response/sipm.py:102)
+ *   crv_response                     <- crvfastsim.chain.charges                      (crv/crvfastsim/chain.py:151)
+ *   crv_digis                        <- crvfastsim.chain.digis + reco.waveform.synthesize
+ *                                                                                     (crv/crvfastsim/chain.py:234,
+ *                                                                                      crv/crvfastsim/reco/waveform.py:74)
+ *   crv_reco_waveforms               <- crvfastsim.chain.reco_waveforms + reco.pulsefit.concat_waveforms
+ *                                                                                     (crv/crvfastsim/chain.py:273,
+ *                                                                                      crv/crvfastsim/reco/pulsefit.py:319)
+ *   crv_pulses                       <- crvfastsim.reco.pulsefit.reconstruct(_full) + filter_channels
+ *                                                                                     (crv/crvfastsim/reco/pulsefit.py:222-316)
+ *   crv_coincidences                 <- crvfastsim.reco.coinc.find_event over every event, as chain.clusters
+ *                                                                                     (crv/crvfastsim/reco/coinc.py:289,
+ *                                                                                      crv/crvfastsim/chain.py:296-362)
+ *
+ * Error convention: the return value is a host error code (CRV_OK, CRV_ERR_ARG for invalid arguments, CRV_ERR_CUDA
+ * for a failed launch).  Data-dependent conditions are reported in the device status block (CrvStatus): capacity
+ * overflows carry the size they needed in need[], so the caller can re-run with larger buffers; nothing is ever
+ * silently truncated.
+ */
+#ifndef CRVGPU_H
+#define CRVGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRVGPU_VERSION 1
+
+/* host return codes */
+#define CRV_OK 0
+#define CRV_ERR_ARG 1
+#define CRV_ERR_CUDA 2
+
+/* device status flags */
+#define CRV_ST_CAPACITY 1      /* a buffer was too small; need[] has the required size */
+#define CRV_ST_LIMIT 2         /* a draw-key limit was exceeded (65,536 steps per event or photons per step row,
+                                  16 cross-talk generations, 64 nodes per generation) */
+#define CRV_ST_NONFINITE 4     /* a non-finite input where a finite one is required */
+#define CRV_ST_ORDER 8         /* input not grouped/sorted as the entry point requires */
+
+/* need[] slots */
+#define CRV_NEED_STEPS_PER_EVENT 0
+#define CRV_NEED_PHOTONS_PER_SIPM 1
+#define CRV_NEED_CHARGE_FACTOR 2   /* charges per SiPM beyond the slot: slot = factor * photons + 16 */
+#define CRV_NEED_DIGIS 3
+#define CRV_NEED_SAMPLES 4
+#define CRV_NEED_PULSES 5
+#define CRV_NEED_HITS_PER_EVENT 6
+#define CRV_NEED_CLUSTERS 7
+#define CRV_NEED_PHOTONS_TOTAL 8
+#define CRV_NEED_SLOTS_TOTAL 9
+#define CRV_NEED_CHARGES_OUT 10
+#define CRV_NEED_DIGIS_OUT 11
+#define CRV_NEED_WAVEFORMS 12
+#define CRV_NEED_PULSES_OUT 13
+#define CRV_NEED_MEMBERS 14
+
+typedef struct CrvStatus {
+    int32_t flags;
+    int32_t pad;
+    long long need[16];
+} CrvStatus;
+
+/* Physics and configuration knobs (all runtime data: no recompilation per design point). */
+typedef struct CrvParams {
+    uint32_t seed;
+    int32_t precision;           /* 0 = FP64 plain, 1 = FP32 mixed */
+    /* photons: analytic yield and two-exponential attenuation */
+    double yield_per_mev, frac_short, frac_long, lambda_short, lambda_long, signal_speed, decay_time;
+    /* SiPM */
+    double overvoltage, time_constant, capacitance, p1, p2, q_ct, q_t0, q_t1, trap0_lifetime, trap1_lifetime;
+    double t_end;
+    int32_t n_pixels_x, n_pixels_y;
+    int32_t uniform_map;         /* 1: photon map is uniform (pixel = floor(u * 1600)) */
+    int32_t charge_factor;       /* charge slots per SiPM = charge_factor * photons + 16 */
+    /* waveforms */
+    double period, spe_precision, spe_max_time, spe_ref_charge, min_voltage, noise_sigma, adc_conversion;
+    double window_lo, window_hi, feb_phase_width;
+    int32_t samples_zs, adc_pedestal, min_adc, max_adc, template_len, feb_key_mode; /* 0 roc*1000+feb, 1 feb */
+    int32_t noise_on, pad1;
+    /* pulse reconstruction */
+    double min_adc_difference, default_beta, min_beta, max_beta, max_time_difference, min_height_ratio;
+    double max_height_ratio, le_time_factor, pedestal_undershoot, time_offset_scale, limit_tolerance, knife_edge_adc;
+    int32_t samples_before, samples_after, max_pulses, lm_iterations, use_time_offset_db, ignore_channels;
+    /* coincidence finder */
+    double fiber_signal_speed, max_time_interval, time_offset;
+    int32_t compensate_mask, ignore_secondary, big_cluster_threshold, add_opposite;
+} CrvParams;
+
+/* Events: the steps of event e are rows [first_step[e], first_step[e] + nsteps[e]) of the step table. */
+typedef struct CrvEvents {
+    const uint32_t *event, *subrun, *run;
+    const int64_t *first_step;
+    const int32_t *nsteps;
+} CrvEvents;
+
+/* SoA step table: midpoint position (Mu2e frame, mm), midpoint time (ns), deposited energy (MeV), bar index.
+ * x, y, z, t, edep are float32 (real_bytes 4) or float64 (real_bytes 8). */
+typedef struct CrvSteps {
+    const void *x, *y, *z, *t, *edep;
+    const int32_t *bar;
+    int32_t real_bytes;
+    int32_t pad;
+} CrvSteps;
+
+/* Per bar: axis of the length direction (0 x, 1 y, 2 z), centre and half length along it (mm). */
+typedef struct CrvBars {
+    const int8_t *length_axis;
+    const double *center_l, *half_l;
+    int32_t nbars;
+    int32_t pad;
+} CrvBars;
+
+/* Per channel (4 * bar + SiPM): photon-yield factor, effective status, ROC, FEB, CRVCalib constants. */
+typedef struct CrvChannels {
+    const double *yield_factor;
+    const int32_t *status, *roc, *feb;
+    const double *pedestal, *pulsearea, *pulseheight, *timeoffset;
+    int32_t nchan;
+    int32_t pad;
+} CrvChannels;
+
+/* SiPM pixel model tables: photon-map running sums (1,600 bins x * 40 + y) and the dead-pixel bitmap (50 words). */
+typedef struct CrvPixels {
+    const double *cum;
+    const uint32_t *dead_bits;
+} CrvPixels;
+
+/* SiPM charges sorted by (label, time): label = event key * 32768 + channel, event key = subrun << 20 | event. */
+typedef struct CrvCharges {
+    int64_t *label;
+    double *time, *charge, *pe;
+    int64_t *photon;             /* step row of the photon that started the avalanche */
+} CrvCharges;
+
+/* ---- version / status ---- */
+int crv_version(void);
+const char *crv_status_string(int32_t flags);
+
+/* Size in bytes of the caller-provided device workspace of crv_response for the given sizes (photon_cap: photons
+ * the batch may produce; max_steps_per_event: largest event of the batch). */
+int64_t crv_response_workspace(const CrvParams *p, int64_t nevents, int64_t nsteps, int64_t photon_cap,
+                               int32_t max_steps_per_event);
+
+/*
+ * chain.charges: steps -> photons (analytic model, keyed draws) -> SiPM charges, for every unmasked channel
+ * ((status & 0b101) == 0).  Outputs (capacity out_cap) in label/time order; *n_out_dev (device int64) receives the
+ * count.  Per-SiPM diagnostics (optional, NULL to skip; capacity sipm_cap): label, photons, fired pixels; their count
+ * goes to *n_sipm_dev.
+ */
+int crv_response(const CrvParams *p, const CrvEvents *ev, int64_t nevents, const CrvSteps *st, int64_t nsteps,
+                 int32_t max_steps_per_event, const CrvBars *bars, const CrvChannels *ch, const CrvPixels *px,
+                 int64_t photon_cap, CrvCharges *out, int64_t out_cap, int64_t *n_out_dev, int64_t *sipm_label,
+                 int32_t *sipm_photons, int32_t *sipm_fired, int64_t sipm_cap, int64_t *n_sipm_dev, void *workspace,
+                 int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
+
+/*
+ * photons.make_photons, first half: photon count of every (step, SiPM) row, count[4 * step + sipm] (every channel,
+ * masked or not, as the reference stage); step_event[step] receives the step's event index.
+ */
+int crv_photon_counts(const CrvParams *p, const CrvEvents *ev, int64_t nevents, const CrvSteps *st, int64_t nsteps,
+                      const CrvBars *bars, const CrvChannels *ch, int32_t *step_event, int32_t *count, void *stream,
+                      CrvStatus *status_dev);
+
+/*
+ * photons.make_photons, second half: emit the photons of every row given row offsets (exclusive prefix of count in
+ * the reference's block order: SiPM 0..3, then step, then photon).  Outputs per photon: step row, channel, arrival
+ * time, draw key (step-in-event << 16 | photon).
+ */
+int crv_photons(const CrvParams *p, const CrvEvents *ev, int64_t nevents, const CrvSteps *st, int64_t nsteps,
+                const CrvBars *bars, const int32_t *step_event, const int32_t *count, const int64_t *row_offset,
+                int64_t *o_step, int64_t *o_chan, double *o_time, int64_t *o_key, void *stream,
+                CrvStatus *status_dev);
+
+/*
+ * sipm.simulate: photons grouped by SiPM (group g = rows [gstart[g], gstart[g] + gcount[g]), label glabel[g], run
+ * grun[g]); any order inside a group.  Charges in group order, time order inside a group (out capacity out_cap);
+ * per-group charge counts and fired-pixel counts.  key: per-photon draw key (step-in-event << 16 | photon).
+ */
+int64_t crv_sipm_workspace(const CrvParams *p, int64_t ngroups, int64_t nphotons);
+int crv_sipm(const CrvParams *p, const CrvPixels *px, int64_t ngroups, int64_t nphotons, const int64_t *gstart, const int32_t *gcount,
+             const int64_t *glabel, const uint32_t *grun, const double *time, const int64_t *key,
+             const int64_t *photon, CrvCharges *out, int64_t out_cap, int64_t *n_out_dev, int32_t *g_charges,
+             int32_t *g_fired, void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,159 @@
+"""ctypes binding of libcrvgpu.so (include/crvgpu.h).
+
+The library is the only compute path of this package: if it is missing, cannot be loaded, or no CUDA device is
+present, every entry point raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+c_i32, c_i64, c_u32, c_f64, c_p = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p
+
+CRV_OK, CRV_ERR_ARG, CRV_ERR_CUDA = 0, 1, 2
+ST_CAPACITY, ST_LIMIT, ST_NONFINITE, ST_ORDER = 1, 2, 4, 8
+NEED = dict(STEPS_PER_EVENT=0, PHOTONS_PER_SIPM=1, CHARGE_FACTOR=2, DIGIS=3, SAMPLES=4, PULSES=5, HITS_PER_EVENT=6,
+            CLUSTERS=7, PHOTONS_TOTAL=8, SLOTS_TOTAL=9, CHARGES_OUT=10, DIGIS_OUT=11, WAVEFORMS=12, PULSES_OUT=13,
+            MEMBERS=14)
+
+
+class CrvStatus(ctypes.Structure):
+    _fields_ = [("flags", c_i32), ("pad", c_i32), ("need", c_i64 * 16)]
+
+
+_PARAM_FIELDS = [
+    ("seed", c_u32), ("precision", c_i32),
+    *[(n, c_f64) for n in ("yield_per_mev", "frac_short", "frac_long", "lambda_short", "lambda_long", "signal_speed",
+                           "decay_time")],
+    *[(n, c_f64) for n in ("overvoltage", "time_constant", "capacitance", "p1", "p2", "q_ct", "q_t0", "q_t1",
+                           "trap0_lifetime", "trap1_lifetime", "t_end")],
+    ("n_pixels_x", c_i32), ("n_pixels_y", c_i32), ("uniform_map", c_i32), ("charge_factor", c_i32),
+    *[(n, c_f64) for n in ("period", "spe_precision", "spe_max_time", "spe_ref_charge", "min_voltage", "noise_sigma",
+                           "adc_conversion", "window_lo", "window_hi", "feb_phase_width")],
+    *[(n, c_i32) for n in ("samples_zs", "adc_pedestal", "min_adc", "max_adc", "template_len", "feb_key_mode",
+                           "noise_on", "pad1")],
+    *[(n, c_f64) for n in ("min_adc_difference", "default_beta", "min_beta", "max_beta", "max_time_difference",
+                           "min_height_ratio", "max_height_ratio", "le_time_factor", "pedestal_undershoot",
+                           "time_offset_scale", "limit_tolerance", "knife_edge_adc")],
+    *[(n, c_i32) for n in ("samples_before", "samples_after", "max_pulses", "lm_iterations", "use_time_offset_db",
+                           "ignore_channels")],
+    *[(n, c_f64) for n in ("fiber_signal_speed", "max_time_interval", "time_offset")],
+    *[(n, c_i32) for n in ("compensate_mask", "ignore_secondary", "big_cluster_threshold", "add_opposite")],
+]
+
+
+class CrvParams(ctypes.Structure):
+    _fields_ = _PARAM_FIELDS
+
+
+class CrvEvents(ctypes.Structure):
+    _fields_ = [("event", c_p), ("subrun", c_p), ("run", c_p), ("first_step", c_p), ("nsteps", c_p)]
+
+
+class CrvSteps(ctypes.Structure):
+    _fields_ = [("x", c_p), ("y", c_p), ("z", c_p), ("t", c_p), ("edep", c_p), ("bar", c_p), ("real_bytes", c_i32),
+                ("pad", c_i32)]
+
+
+class CrvBars(ctypes.Structure):
+    _fields_ = [("length_axis", c_p), ("center_l", c_p), ("half_l", c_p), ("nbars", c_i32), ("pad", c_i32)]
+
+
+class CrvChannels(ctypes.Structure):
+    _fields_ = [("yield_factor", c_p), ("status", c_p), ("roc", c_p), ("feb", c_p), ("pedestal", c_p),
+                ("pulsearea", c_p), ("pulseheight", c_p), ("timeoffset", c_p), ("nchan", c_i32), ("pad", c_i32)]
+
+
+class CrvPixels(ctypes.Structure):
+    _fields_ = [("cum", c_p), ("dead_bits", c_p)]
+
+
+class CrvCharges(ctypes.Structure):
+    _fields_ = [("label", c_p), ("time", c_p), ("charge", c_p), ("pe", c_p), ("photon", c_p)]
+
+
+P = ctypes.POINTER
+
+_SIGS = {
+    "crv_version": (c_i32, []),
+    "crv_status_string": (ctypes.c_char_p, [c_i32]),
+    "crv_response_workspace": (c_i64, [P(CrvParams), c_i64, c_i64, c_i64, c_i32]),
+    "crv_response": (c_i32, [P(CrvParams), P(CrvEvents), c_i64, P(CrvSteps), c_i64, c_i32, P(CrvBars), P(CrvChannels),
+                             P(CrvPixels), c_i64, P(CrvCharges), c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p, c_i64,
+                             c_p, c_p]),
+    "crv_photon_counts": (c_i32, [P(CrvParams), P(CrvEvents), c_i64, P(CrvSteps), c_i64, P(CrvBars), P(CrvChannels),
+                                  c_p, c_p, c_p, c_p]),
+    "crv_photons": (c_i32, [P(CrvParams), P(CrvEvents), c_i64, P(CrvSteps), c_i64, P(CrvBars), c_p, c_p, c_p, c_p,
+                            c_p, c_p, c_p, c_p, c_p]),
+    "crv_sipm_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
+    "crv_sipm": (c_i32, [P(CrvParams), P(CrvPixels), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, P(CrvCharges),
+                         c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
+}
+
+# symbols declared in include/crvgpu.h (the load test checks every one is exported)
+DECLARED = tuple(_SIGS)
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libcrvgpu.so (building it first if needed) and declare the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"CRV engine library missing: {path}")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(rc, what):
+    if rc == CRV_ERR_ARG:
+        raise ValueError(f"{what}: invalid arguments")
+    if rc != CRV_OK:
+        raise RuntimeError(f"{what}: CUDA launch failed (code {rc})")
+
+
+def ptr(t):
+    """Device pointer of a torch tensor (None -> NULL)."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def status_string(flags):
+    return load().crv_status_string(int(flags)).decode()
+
+
+class DeviceStatus:
+    """A device status block (CrvStatus) held in a torch tensor; read() copies it to the host."""
+
+    def __init__(self, device):
+        import torch
+        self.t = torch.zeros(ctypes.sizeof(CrvStatus) // 8, dtype=torch.int64, device=device)
+
+    def reset(self):
+        self.t.zero_()
+
+    @property
+    def ptr(self):
+        return ctypes.c_void_p(self.t.data_ptr())
+
+    def read(self):
+        a = self.t.cpu().numpy()
+        flags = int(np.int64(a[0]) & 0xFFFFFFFF)
+        return flags, a[1:17].copy()

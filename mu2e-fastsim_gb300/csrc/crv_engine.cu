@@ -1,0 +1,456 @@
+// C ABI of the CRV response engine: argument checks, workspace layout, launch orchestration.
+// The kernels of each precision live in crv_kernels_f64.cu / crv_kernels_f32.cu; this unit holds the precision-free
+// kernels (event preparation, SiPM sizing, compaction, scans).
+#define CRV_ENGINE_TU 1
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "crv_launch.h"
+#include "crv_response.cuh"
+
+namespace crv {
+
+const DeviceInfo& device_info() {
+  static DeviceInfo di{0, 0};
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int sms = 0, optin = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    di.sms = sms > 0 ? sms : 1;
+    di.smem_optin = size_t(optin > 0 ? optin : 48 * 1024);
+  });
+  return di;
+}
+
+__global__ void k_scan_parts(long long* __restrict__ part, long long nb, long long* __restrict__ total) {
+  // single block: running exclusive scan over chunks of blockDim.x
+  __shared__ long long carry;
+  __shared__ long long wsum[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (long long base = 0; base < nb; base += blockDim.x) {
+    long long i = base + threadIdx.x;
+    long long v = i < nb ? part[i] : 0;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      long long q = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+      long long qq = q;
+      for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(0xffffffffu, qq, o);
+        if (lane >= o) qq += y;
+      }
+      if (lane < (int)(blockDim.x >> 5)) wsum[lane] = qq - q;
+    }
+    __syncthreads();
+    long long ex = carry + wsum[w] + x - v;
+    if (i < nb) part[i] = ex;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = ex + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_check_caps(const long long* __restrict__ total, long long cap, int need_slot, Status* status) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && *total > cap) {
+    set_flag(status, CRV_ST_CAPACITY);
+    need_at_least(status, need_slot, *total);
+  }
+}
+
+__global__ void k_copy_i64(const long long* __restrict__ src, long long* __restrict__ dst) { *dst = *src; }
+
+__global__ void k_sipm_diag(const long long* __restrict__ nsipm_dev, long long cap, const long long* __restrict__ label,
+                            const int32_t* __restrict__ nphot, const int32_t* __restrict__ fired,
+                            int64_t* __restrict__ o_label, int32_t* __restrict__ o_phot, int32_t* __restrict__ o_fired,
+                            Status* status) {
+  long long n = *nsipm_dev;
+  if (n > cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { set_flag(status, CRV_ST_CAPACITY); }
+    return;
+  }
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+    if (o_label) o_label[g] = label[g];
+    if (o_phot) o_phot[g] = nphot[g];
+    if (o_fired) o_fired[g] = fired[g];
+  }
+}
+
+__global__ void k_slot_caps(long long ng, const int32_t* __restrict__ gcount, int factor, int32_t* __restrict__ cap) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x)
+    cap[g] = gcount[g] > 0 ? factor * gcount[g] + 16 : 0;
+}
+
+__global__ void k_fill_step_event(CrvEvents ev, long long nevents, int32_t* __restrict__ step_event) {
+  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); e < nevents; e += warps) {
+    long long f = ev.first_step[e];
+    for (int i = threadIdx.x & 31; i < ev.nsteps[e]; i += 32) step_event[f + i] = int32_t(e);
+  }
+}
+
+__global__ void k_set_i64(long long* __restrict__ dst, long long v) { *dst = v; }
+
+// ---------------------------------------------------------------------------------------------------------------------
+// workspace carving
+
+struct Carve {
+  char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(long long n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += size_t(n > 0 ? n : 1) * sizeof(T);
+    return p;
+  }
+};
+
+struct RespWs {
+  int32_t *step_event, *step_order, *count, *sipm_count;
+  long long* sipm_off;
+  int32_t *s_event, *s_chan, *s_nseg, *nphot, *slot_cap, *nmain, *nap, *fired, *ntot;
+  long long *s_seg, *id_base, *label, *ph_off, *slot_off, *out_off, *parts, *totals;
+  uint32_t* run;
+  void* ph_t;
+  uint32_t* ph_key;
+  double *slot_t, *slot_v;
+  long long* slot_id;
+  long long nb, pc, sc;
+};
+
+static RespWs resp_layout(char* base, const CrvParams& p, long long ne, long long ns, long long photon_cap, size_t* bytes) {
+  Carve c{base};
+  RespWs w;
+  w.nb = 4 * ns;
+  w.pc = photon_cap;
+  w.sc = (long long)(p.charge_factor > 0 ? p.charge_factor : 1) * photon_cap + 16 * w.nb;
+  size_t rb = p.precision == 1 ? 4 : 8;
+  w.step_event = c.take<int32_t>(ns);
+  w.step_order = c.take<int32_t>(ns);
+  w.count = c.take<int32_t>(4 * ns);
+  w.sipm_count = c.take<int32_t>(ne);
+  w.sipm_off = c.take<long long>(ne);
+  w.s_event = c.take<int32_t>(w.nb);
+  w.s_chan = c.take<int32_t>(w.nb);
+  w.s_nseg = c.take<int32_t>(w.nb);
+  w.nphot = c.take<int32_t>(w.nb);
+  w.slot_cap = c.take<int32_t>(w.nb);
+  w.nmain = c.take<int32_t>(w.nb);
+  w.nap = c.take<int32_t>(w.nb);
+  w.fired = c.take<int32_t>(w.nb);
+  w.ntot = c.take<int32_t>(w.nb);
+  w.s_seg = c.take<long long>(w.nb);
+  w.id_base = c.take<long long>(w.nb);
+  w.label = c.take<long long>(w.nb);
+  w.ph_off = c.take<long long>(w.nb);
+  w.slot_off = c.take<long long>(w.nb);
+  w.out_off = c.take<long long>(w.nb);
+  w.run = c.take<uint32_t>(w.nb);
+  long long mx = ne > w.nb ? ne : w.nb;
+  w.parts = c.take<long long>(scan_parts_len(mx) + 1);
+  w.totals = c.take<long long>(8);
+  w.ph_t = c.take<char>(photon_cap * (long long)rb);
+  w.ph_key = c.take<uint32_t>(photon_cap);
+  w.slot_t = c.take<double>(w.sc);
+  w.slot_v = c.take<double>(w.sc);
+  w.slot_id = c.take<long long>(w.sc);
+  *bytes = c.off + 256;
+  return w;
+}
+
+}  // namespace crv
+
+using namespace crv;
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) return CRV_ERR_CUDA; \
+  } while (0)
+
+static unsigned grid_for(long long n, int per_block, int mult) {
+  long long b = (n + per_block - 1) / per_block;
+  long long mx = (long long)device_info().sms * mult;
+  if (b < 1) b = 1;
+  return (unsigned)(b < mx ? b : mx);
+}
+
+extern "C" {
+
+int crv_version(void) { return CRVGPU_VERSION; }
+
+const char* crv_status_string(int32_t flags) {
+  static thread_local char buf[256];
+  if (flags == 0) return "ok";
+  buf[0] = 0;
+  const char* names[] = {"capacity", "limit", "nonfinite", "order"};
+  for (int i = 0; i < 4; ++i)
+    if (flags & (1 << i)) {
+      if (buf[0]) strncat(buf, "|", sizeof(buf) - strlen(buf) - 1);
+      strncat(buf, names[i], sizeof(buf) - strlen(buf) - 1);
+    }
+  return buf;
+}
+
+int64_t crv_response_workspace(const CrvParams* p, int64_t nevents, int64_t nsteps, int64_t photon_cap,
+                               int32_t max_steps_per_event) {
+  if (!p || nevents < 0 || nsteps < 0 || photon_cap < 0) return -1;
+  (void)max_steps_per_event;
+  size_t bytes = 0;
+  resp_layout(nullptr, *p, nevents, nsteps, photon_cap, &bytes);
+  return (int64_t)bytes;
+}
+
+int crv_photon_counts(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
+                      const CrvBars* bars, const CrvChannels* ch, int32_t* step_event, int32_t* count, void* stream,
+                      CrvStatus* status_dev) {
+  if (!p || !ev || !st || !bars || !ch || !step_event || !count || !status_dev) return CRV_ERR_ARG;
+  if (st->real_bytes != 4 && st->real_bytes != 8) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  if (nevents == 0 || nsteps == 0) return CRV_OK;
+  k_fill_step_event<<<grid_for(nevents, 8, 32), 256, 0, s>>>(*ev, nevents, step_event);
+  CK(cudaGetLastError());
+  if (p->precision == 1)
+    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, step_event, nsteps, 0, count, S, s));
+  else
+    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, step_event, nsteps, 0, count, S, s));
+  return CRV_OK;
+}
+
+int crv_photons(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
+                const CrvBars* bars, const int32_t* step_event, const int32_t* count, const int64_t* row_offset,
+                int64_t* o_step, int64_t* o_chan, double* o_time, int64_t* o_key, void* stream,
+                CrvStatus* status_dev) {
+  if (!p || !ev || !st || !bars || !step_event || !count || !row_offset || !status_dev) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nevents == 0 || nsteps == 0) return CRV_OK;
+  const long long* ro = reinterpret_cast<const long long*>(row_offset);
+  if (p->precision == 1)
+    CK(launch_photon_rows<float>(*p, *ev, *st, *bars, step_event, nsteps, count, ro, o_step, o_chan, o_time, o_key, s));
+  else
+    CK(launch_photon_rows<double>(*p, *ev, *st, *bars, step_event, nsteps, count, ro, o_step, o_chan, o_time, o_key,
+                                  s));
+  return CRV_OK;
+}
+
+int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
+                 int32_t max_steps_per_event, const CrvBars* bars, const CrvChannels* ch, const CrvPixels* px,
+                 int64_t photon_cap, CrvCharges* out, int64_t out_cap, int64_t* n_out_dev, int64_t* sipm_label,
+                 int32_t* sipm_photons, int32_t* sipm_fired, int64_t sipm_cap, int64_t* n_sipm_dev, void* workspace,
+                 int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!p || !ev || !st || !bars || !ch || !px || !out || !n_out_dev || !status_dev) return CRV_ERR_ARG;
+  if (st->real_bytes != 4 && st->real_bytes != 8) return CRV_ERR_ARG;
+  if (nevents < 0 || nsteps < 0 || photon_cap < 0 || out_cap < 0 || max_steps_per_event < 0) return CRV_ERR_ARG;
+  size_t need = 0;
+  resp_layout(nullptr, *p, nevents, nsteps, photon_cap, &need);
+  if (!workspace || (size_t)workspace_bytes < need) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  RespWs w = resp_layout(base, *p, nevents, nsteps, photon_cap, &dummy);
+  CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  if (nevents == 0 || nsteps == 0) {
+    CK(cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s));
+    if (n_sipm_dev) CK(cudaMemsetAsync(n_sipm_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  CK(cudaMemsetAsync(w.nphot, 0, sizeof(int32_t) * w.nb, s));
+  CK(cudaMemsetAsync(w.slot_cap, 0, sizeof(int32_t) * w.nb, s));
+  CK(cudaMemsetAsync(w.nmain, 0, sizeof(int32_t) * w.nb, s));
+  CK(cudaMemsetAsync(w.nap, 0, sizeof(int32_t) * w.nb, s));
+  CK(cudaMemsetAsync(w.fired, 0, sizeof(int32_t) * w.nb, s));
+  CK(cudaMemsetAsync(w.ntot, 0, sizeof(int32_t) * w.nb, s));
+  // 1. events: steps grouped by bar, SiPM counts; 2. scan; 3. SiPM table
+  int stepcap = 1;
+  while (stepcap < max_steps_per_event) stepcap <<= 1;
+  if (stepcap > 65536) stepcap = 65536;
+  size_t psmem = size_t(stepcap) * 4;
+  CK(cudaFuncSetAttribute(k_event_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  unsigned gp = grid_for(nevents, 1, 8);
+  k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, w.step_event, w.step_order,
+                                                w.sipm_count, nullptr, nullptr, nullptr, nullptr, nullptr, S, 0);
+  CK(cudaGetLastError());
+  CK(exclusive_scan(w.sipm_count, nevents, Identity(), w.sipm_off, &w.totals[0], w.parts, s));
+  k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, nullptr, nullptr, nullptr,
+                                                w.sipm_off, w.s_event, w.s_chan, w.s_seg, w.s_nseg, S, 1);
+  CK(cudaGetLastError());
+  // 4. photon counts per (step, SiPM)
+  if (p->precision == 1)
+    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, 1, w.count, S, s));
+  else
+    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, 1, w.count, S, s));
+  // 5. per-SiPM photons and charge slots; scans
+  int factor = p->charge_factor > 0 ? p->charge_factor : 1;
+  k_sipm_sizes<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
+                                                      w.step_order, w.count, *ev, factor, w.nphot, w.slot_cap,
+                                                      w.id_base, w.label, w.run);
+  CK(cudaGetLastError());
+  CK(exclusive_scan(w.nphot, w.nb, Identity(), w.ph_off, &w.totals[1], w.parts, s));
+  CK(exclusive_scan(w.slot_cap, w.nb, Identity(), w.slot_off, &w.totals[2], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], w.pc, CRV_NEED_PHOTONS_TOTAL, S);
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  CK(cudaGetLastError());
+  // 6. photons of every SiPM
+  if (p->precision == 1)
+    CK(launch_photon_emit<float>(*p, *ev, *st, *bars, w.nb, &w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
+                                 w.step_order, w.count, w.ph_off, (float*)w.ph_t, w.ph_key, &w.totals[1], w.pc, s));
+  else
+    CK(launch_photon_emit<double>(*p, *ev, *st, *bars, w.nb, &w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
+                                  w.step_order, w.count, w.ph_off, (double*)w.ph_t, w.ph_key, &w.totals[1], w.pc, s));
+  // 7. SiPM simulation
+  SipmGroups G{};
+  G.n = &w.totals[0];
+  G.guard[0] = &w.totals[1];
+  G.guard_cap[0] = w.pc;
+  G.guard[1] = &w.totals[2];
+  G.guard_cap[1] = w.sc;
+  G.start = w.ph_off;
+  G.count = w.nphot;
+  G.label = w.label;
+  G.run = w.run;
+  G.key32 = w.ph_key;
+  G.key64 = nullptr;
+  G.photon_id = nullptr;
+  G.id_base = w.id_base;
+  G.slot_off = w.slot_off;
+  G.slot_cap = w.slot_cap;
+  SipmOut O{w.slot_t, w.slot_v, w.slot_id, w.nmain, w.nap, w.fired};
+  if (p->precision == 1)
+    CK((launch_sipm<float, float>(*p, *px, G, &w.totals[0], (const float*)w.ph_t, O, S, s)));
+  else
+    CK((launch_sipm<double, double>(*p, *px, G, &w.totals[0], (const double*)w.ph_t, O, S, s)));
+  // 8. compaction into label/time order
+  k_counts_total<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  CK(cudaGetLastError());
+  CK(exclusive_scan(w.ntot, w.nb, Identity(), w.out_off, &w.totals[3], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
+  k_charge_compact<<<grid_for(w.nb, 8, 16), 256, 0, s>>>(&w.totals[0], w.label, w.slot_off, w.slot_cap, w.nmain,
+                                                          w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
+                                                          p->capacitance, p->overvoltage, *out, out_cap);
+  CK(cudaGetLastError());
+  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  if (n_sipm_dev) k_copy_i64<<<1, 1, 0, s>>>(&w.totals[0], reinterpret_cast<long long*>(n_sipm_dev));
+  if (sipm_label || sipm_photons || sipm_fired)
+    k_sipm_diag<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], sipm_cap, w.label, w.nphot, w.fired,
+                                                       sipm_label, sipm_photons, sipm_fired, S);
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+// ---- sipm.simulate over caller-grouped photons -------------------------------------------------------------------
+
+struct SipmWs {
+  long long *slot_off, *out_off, *parts, *totals, *label_dummy;
+  int32_t *slot_cap, *nmain, *nap, *ntot;
+  double *slot_t, *slot_v;
+  long long* slot_id;
+  long long sc;
+};
+
+static SipmWs sipm_layout(char* base, const CrvParams& p, long long ng, long long nph, size_t* bytes) {
+  Carve c{base};
+  SipmWs w;
+  w.sc = (long long)(p.charge_factor > 0 ? p.charge_factor : 1) * nph + 16 * ng;
+  w.slot_off = c.take<long long>(ng);
+  w.out_off = c.take<long long>(ng);
+  w.parts = c.take<long long>(scan_parts_len(ng) + 1);
+  w.totals = c.take<long long>(8);
+  w.label_dummy = nullptr;
+  w.slot_cap = c.take<int32_t>(ng);
+  w.nmain = c.take<int32_t>(ng);
+  w.nap = c.take<int32_t>(ng);
+  w.ntot = c.take<int32_t>(ng);
+  w.slot_t = c.take<double>(w.sc);
+  w.slot_v = c.take<double>(w.sc);
+  w.slot_id = c.take<long long>(w.sc);
+  *bytes = c.off + 256;
+  return w;
+}
+
+int64_t crv_sipm_workspace(const CrvParams* p, int64_t ngroups, int64_t nphotons) {
+  if (!p || ngroups < 0 || nphotons < 0) return -1;
+  size_t b = 0;
+  sipm_layout(nullptr, *p, ngroups, nphotons, &b);
+  return (int64_t)b;
+}
+
+}  // extern "C"
+
+extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups, int64_t nphotons, const int64_t* gstart,
+                        const int32_t* gcount, const int64_t* glabel, const uint32_t* grun, const double* time,
+                        const int64_t* key, const int64_t* photon, CrvCharges* out, int64_t out_cap,
+                        int64_t* n_out_dev, int32_t* g_charges, int32_t* g_fired, void* workspace,
+                        int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!p || !px || !out || !n_out_dev || !status_dev || ngroups < 0) return CRV_ERR_ARG;
+  if (ngroups > 0 && (!gstart || !gcount || !glabel || !grun || !time || !key || !photon || !g_fired)) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ngroups == 0) {
+    CK(cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  long long nph_bound = nphotons;
+  size_t need = 0;
+  sipm_layout(nullptr, *p, ngroups, nph_bound, &need);
+  if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  SipmWs w = sipm_layout(base, *p, ngroups, nph_bound, &dummy);
+  int factor = p->charge_factor > 0 ? p->charge_factor : 1;
+  CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.nmain, 0, sizeof(int32_t) * ngroups, s));
+  CK(cudaMemsetAsync(w.nap, 0, sizeof(int32_t) * ngroups, s));
+  CK(cudaMemsetAsync(g_fired, 0, sizeof(int32_t) * ngroups, s));
+  k_set_i64<<<1, 1, 0, s>>>(&w.totals[0], ngroups);
+  k_slot_caps<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(ngroups, gcount, factor, w.slot_cap);
+  CK(cudaGetLastError());
+  CK(exclusive_scan(w.slot_cap, ngroups, Identity(), w.slot_off, &w.totals[2], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  SipmGroups G{};
+  G.n = &w.totals[0];
+  G.guard[0] = &w.totals[2];
+  G.guard_cap[0] = w.sc;
+  G.guard[1] = nullptr;
+  G.start = reinterpret_cast<const long long*>(gstart);
+  G.count = gcount;
+  G.label = reinterpret_cast<const long long*>(glabel);
+  G.run = grun;
+  G.key32 = nullptr;
+  G.key64 = reinterpret_cast<const long long*>(key);
+  G.photon_id = reinterpret_cast<const long long*>(photon);
+  G.id_base = nullptr;
+  G.slot_off = w.slot_off;
+  G.slot_cap = w.slot_cap;
+  SipmOut O{w.slot_t, w.slot_v, w.slot_id, w.nmain, w.nap, g_fired};
+  if (p->precision == 1)
+    CK((launch_sipm<float, double>(*p, *px, G, &w.totals[0], time, O, S, s)));
+  else
+    CK((launch_sipm<double, double>(*p, *px, G, &w.totals[0], time, O, S, s)));
+  k_counts_total<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  CK(cudaGetLastError());
+  CK(exclusive_scan(w.ntot, ngroups, Identity(), w.out_off, &w.totals[3], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
+  k_charge_compact<<<grid_for(ngroups, 8, 16), 256, 0, s>>>(&w.totals[0], G.label, w.slot_off, w.slot_cap, w.nmain,
+                                                             w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
+                                                             p->capacitance, p->overvoltage, *out, out_cap);
+  CK(cudaGetLastError());
+  if (g_charges)
+    CK(cudaMemcpyAsync(g_charges, w.ntot, sizeof(int32_t) * ngroups, cudaMemcpyDeviceToDevice, s));
+  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  CK(cudaGetLastError());
+  return CRV_OK;
+}

@@ -1,0 +1,40 @@
+// Internal launch interface between the engine (C ABI) translation unit and the per-precision kernel units.
+#pragma once
+#include <cuda_runtime.h>
+#include "crv_device.cuh"
+
+namespace crv {
+
+struct SipmGroups;
+struct SipmOut;
+
+struct DeviceInfo {
+  int sms;
+  size_t smem_optin;
+};
+const DeviceInfo& device_info();
+
+template <typename R>
+cudaError_t launch_photon_count(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,
+                                const CrvChannels& ch, const int32_t* step_event, long long nsteps, int masked,
+                                int32_t* count, Status* status, cudaStream_t s);
+
+template <typename R>
+cudaError_t launch_photon_emit(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,
+                               long long nsipm_bound, const long long* nsipm_dev, const int32_t* s_event,
+                               const int32_t* s_chan, const long long* s_seg, const int32_t* s_nseg,
+                               const int32_t* step_order, const int32_t* count, const long long* ph_off, R* ph_t,
+                               uint32_t* ph_key, const long long* ph_total, long long ph_cap, cudaStream_t s);
+
+template <typename R>
+cudaError_t launch_photon_rows(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,
+                               const int32_t* step_event, long long nsteps, const int32_t* count,
+                               const long long* row_offset, int64_t* o_step, int64_t* o_chan, double* o_time,
+                               int64_t* o_key, cudaStream_t s);
+
+// SiPM simulation over groups; PT = storage type of the photon times (R for the chain, double for the stage API)
+template <typename R, typename PT>
+cudaError_t launch_sipm(const CrvParams& p, const CrvPixels& px, const SipmGroups& G, const long long* ngroups_dev,
+                        const PT* ph_time, const SipmOut& O, Status* status, cudaStream_t s);
+
+}  // namespace crv

@@ -61,7 +61,21 @@ def lib():
 
 
 def _p(a):
+    """Pointer of an array the caller keeps alive."""
     return ctypes.c_void_p(a.ctypes.data)
+
+
+class _Keep:
+    """Pointer factory that keeps every converted array alive until the holder is dropped (a pointer taken from a
+    temporary array would dangle as soon as the temporary is freed)."""
+
+    def __init__(self):
+        self.arrays = []
+
+    def __call__(self, a, dtype=None):
+        a = np.ascontiguousarray(a, dtype)
+        self.arrays.append(a)
+        return ctypes.c_void_p(a.ctypes.data)
 
 
 class OrcParams(ctypes.Structure):
@@ -77,7 +91,8 @@ class OrcParams(ctypes.Structure):
 
 
 def p_fire(sc, v):
-    return sc.p1 * (1.0 - lib().orc_exp(-v / sc.p2))
+    """Host-side p_fire for derived constants (NumPy exp, as the reference's SiPMConfig.p_fire)."""
+    return sc.p1 * (1.0 - np.exp(-v / sc.p2))
 
 
 def params(rc, sc, seed, t_end):
@@ -93,7 +108,7 @@ def params(rc, sc, seed, t_end):
     P.decay_time = rc.decay_time
     P.overvoltage, P.time_constant, P.capacitance = sc.overvoltage, sc.time_constant, sc.capacitance
     P.p1, P.p2 = sc.p1, sc.p2
-    pf = p_fire(sc, sc.overvoltage)
+    pf = float(p_fire(sc, sc.overvoltage))
     P.q_ct = (1.0 - (1.0 - sc.cross_talk) ** 0.25) / pf
     P.q_t0 = sc.trap0_prob / pf
     P.q_t1 = sc.trap1_prob / pf
@@ -123,18 +138,18 @@ def dead_table(sc):
 def tdc0_uniform(seed, run, event, subrun, febkey):
     n = len(event)
     u = np.empty(n)
-    a = [np.ascontiguousarray(x, np.uint32) for x in (run, event, subrun, febkey)]
-    lib().orc_tdc0_uniform(ctypes.c_uint32(seed), ctypes.c_int64(n), *[_p(x) for x in a], _p(u))
+    k = _Keep()
+    lib().orc_tdc0_uniform(ctypes.c_uint32(seed), ctypes.c_int64(n), *[k(x, np.uint32) for x in (run, event, subrun,
+                                                                                             febkey)], k(u))
     return u
 
 
 def noise_normal(seed, run, event, subrun, chan, tick):
     n = len(event)
     z = np.empty(n)
-    a = [np.ascontiguousarray(x, np.uint32) for x in (run, event, subrun)]
-    c = np.ascontiguousarray(chan, np.int32)
-    tk = np.ascontiguousarray(tick, np.int64)
-    lib().orc_noise_normal(ctypes.c_uint32(seed), ctypes.c_int64(n), *[_p(x) for x in a], _p(c), _p(tk), _p(z))
+    k = _Keep()
+    lib().orc_noise_normal(ctypes.c_uint32(seed), ctypes.c_int64(n), *[k(x, np.uint32) for x in (run, event, subrun)],
+                           k(chan, np.int32), k(tick, np.int64), k(z))
     return z
 
 
@@ -181,11 +196,10 @@ def photon_counts(steps, geom, rc, deviation, seed):
     n = len(bar)
     cnt = np.zeros(4 * n, np.int64)
     P = params(rc, _NullSiPM, seed, 1e5)
-    lib().orc_photon_counts(ctypes.byref(P), ctypes.c_int64(n), _p(np.ascontiguousarray(bar, np.int32)),
-                            _p(np.ascontiguousarray(z)), _p(np.ascontiguousarray(t)), _p(np.ascontiguousarray(edep)),
-                            _p(np.ascontiguousarray(half)), _p(dev), _p(np.ascontiguousarray(ev, np.uint32)),
-                            _p(np.ascontiguousarray(sub, np.uint32)), _p(np.ascontiguousarray(run, np.uint32)),
-                            _p(np.ascontiguousarray(sie, np.int32)), _p(cnt))
+    k = _Keep()
+    lib().orc_photon_counts(ctypes.byref(P), ctypes.c_int64(n), k(bar, np.int32), k(z, np.float64), k(t, np.float64),
+                            k(edep, np.float64), k(half, np.float64), k(dev, np.float64), k(ev, np.uint32),
+                            k(sub, np.uint32), k(run, np.uint32), k(sie, np.int32), k(cnt))
     return cnt.reshape(n, 4)
 
 
@@ -209,13 +223,11 @@ def make_photons(steps, geom, rc, deviation, seed):
     tot = int(rc_.sum())
     o = [np.empty(tot, np.int64), np.empty(tot, np.int64), np.empty(tot), np.empty(tot, np.int64)]
     P = params(rc, _NullSiPM, seed, 1e5)
-    lib().orc_photon_emit(ctypes.byref(P), ctypes.c_int64(4 * n), _p(np.ascontiguousarray(rows_step, np.int64)),
-                          _p(np.ascontiguousarray(rows_s, np.int32)), _p(np.ascontiguousarray(rc_, np.int64)), _p(off),
-                          _p(np.ascontiguousarray(bar, np.int32)), _p(np.ascontiguousarray(z)),
-                          _p(np.ascontiguousarray(t)), _p(np.ascontiguousarray(half)),
-                          _p(np.ascontiguousarray(ev, np.uint32)), _p(np.ascontiguousarray(sub, np.uint32)),
-                          _p(np.ascontiguousarray(run, np.uint32)), _p(np.ascontiguousarray(sie, np.int32)),
-                          *[_p(x) for x in o])
+    k = _Keep()
+    lib().orc_photon_emit(ctypes.byref(P), ctypes.c_int64(4 * n), k(rows_step, np.int64), k(rows_s, np.int32),
+                          k(rc_, np.int64), k(off, np.int64), k(bar, np.int32), k(z, np.float64), k(t, np.float64),
+                          k(half, np.float64), k(ev, np.uint32), k(sub, np.uint32), k(run, np.uint32),
+                          k(sie, np.int32), *[k(x) for x in o])
     return o[0], o[1], o[2], o[3]
 
 
@@ -241,12 +253,11 @@ def sipm_groups(label, time, photon, key, run_of_label, sc, seed, t_end, pmap=No
     tm = np.ascontiguousarray(np.asarray(time, float)[o])
     ky = np.ascontiguousarray(np.asarray(key, np.int64)[o])
     ph = np.ascontiguousarray(np.asarray(photon, np.int64)[o])
-    st = lib().orc_sipm_groups(ctypes.byref(P), _p(cum), _p(dead), ctypes.c_int64(G),
-                               _p(np.ascontiguousarray(start, np.int64)), _p(np.ascontiguousarray(cnt, np.int64)),
-                               _p(np.ascontiguousarray(chan, np.int32)), _p(np.ascontiguousarray(ev, np.uint32)),
-                               _p(np.ascontiguousarray(sub, np.uint32)), _p(np.ascontiguousarray(run, np.uint32)),
-                               _p(tm), _p(ky), _p(ph), _p(nq), _p(nfp), ctypes.byref(nout), ctypes.byref(pt),
-                               ctypes.byref(pv), ctypes.byref(pp))
+    k = _Keep()
+    st = lib().orc_sipm_groups(ctypes.byref(P), k(cum), k(dead), ctypes.c_int64(G), k(start, np.int64),
+                               k(cnt, np.int64), k(chan, np.int32), k(ev, np.uint32), k(sub, np.uint32),
+                               k(run, np.uint32), k(tm), k(ky), k(ph), k(nq), k(nfp), ctypes.byref(nout),
+                               ctypes.byref(pt), ctypes.byref(pv), ctypes.byref(pp))
     n = nout.value
     if n:
         t = np.ctypeslib.as_array(pt, (n,)).copy()

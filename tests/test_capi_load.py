@@ -1,0 +1,47 @@
+"""The engine library builds, loads and exports every entry point include/crvgpu.h declares (no GPU needed)."""
+import os
+import re
+
+from crvgpu import _capi, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_in_header():
+    text = open(os.path.join(ROOT, "include", "crvgpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(crv_\w+)\s*\(", text))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = build.build()
+    assert os.path.exists(path)
+    L = _capi.load()
+    header = declared_in_header()
+    assert header, "no entry points found in the header"
+    assert header == set(_capi.DECLARED), header ^ set(_capi.DECLARED)
+    for name in header:
+        assert hasattr(L, name), name
+    assert L.crv_version() == 1
+    assert _capi.status_string(0) == "ok"
+    assert _capi.status_string(3) == "capacity|limit"
+
+
+def test_struct_sizes_match_header_layout():
+    import ctypes
+    # CrvStatus: flags, pad, need[16]
+    assert ctypes.sizeof(_capi.CrvStatus) == 8 + 16 * 8
+    # every double field of CrvParams is 8-byte aligned (no implicit padding surprises between int pairs)
+    for name, typ in _capi.CrvParams._fields_:
+        off = getattr(_capi.CrvParams, name).offset
+        assert off % ctypes.sizeof(typ) == 0, name
+
+
+def test_workspace_query_without_gpu():
+    import ctypes
+    from crvgpu.params import make_params
+    L = _capi.load()
+    P = make_params()
+    assert L.crv_response_workspace(ctypes.byref(P), 10, 400, 100000, 64) > 0
+    assert L.crv_response_workspace(ctypes.byref(P), -1, 400, 100000, 64) == -1
+    assert L.crv_sipm_workspace(ctypes.byref(P), 10, 1000) > 0
