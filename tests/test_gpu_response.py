@@ -47,7 +47,8 @@ def test_sipm_stage_bit_exact_and_fired_pixels(R):
     label = evk[so] * 32768 + co
     run = np.asarray(steps["run"], np.int64)[so]
     G = R.simulate(label, to, so, None, cfg.sipm, None, t_end=cfg.window[1], key=5, draw_key=ko, run=run)
-    Qo, u, nq, nfp, st = O.sipm_groups(label, to, so, ko, run_of(steps), cfg.sipm, 5, cfg.window[1])
+    rof = run_of(steps)
+    Qo, u, nq, nfp, st = O.sipm_groups(label, to, so, ko, lambda L: rof(L // 32768), cfg.sipm, 5, cfg.window[1])
     assert st == 0
     for k in ("chan", "time", "charge", "pe", "photon"):
         assert np.array_equal(G[k], Qo[k]), k
