@@ -142,6 +142,15 @@ typedef struct CrvCharges {
     int64_t *photon;             /* step row of the photon that started the avalanche */
 } CrvCharges;
 
+/* Zero-suppressed digis sorted by (label, start): label, start (ns), TDC0 (ns), start TDC, volt[n][12], adc[n][12]. */
+typedef struct CrvDigis {
+    int64_t *chan;
+    double *start, *tdc0;
+    int64_t *starttdc;
+    double *volt;
+    int16_t *adc;
+} CrvDigis;
+
 /* ---- version / status ---- */
 int crv_version(void);
 const char *crv_status_string(int32_t flags);
@@ -191,6 +200,19 @@ int crv_sipm(const CrvParams *p, const CrvPixels *px, int64_t ngroups, int64_t n
              const int64_t *glabel, const uint32_t *grun, const double *time, const int64_t *key,
              const int64_t *photon, CrvCharges *out, int64_t out_cap, int64_t *n_out_dev, int32_t *g_charges,
              int32_t *g_fired, void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
+
+/*
+ * chain.digis / waveform.synthesize: SiPM charges sorted by (label, time) -> digis.  TDC0 is one keyed uniform x
+ * feb_phase_width per (event, FEB); electronics noise is keyed by (event, channel, sample tick).  tmpl: the single-PE
+ * template (tlen samples at spe_precision).  ev_keys/ev_runs (optional, n_events sorted event keys and their runs)
+ * give the run of each event for the keys; without them run 0 is used.  slot_cap: digi slots of the workspace
+ * (an upper bound is computed on the device; CRV_NEED_DIGIS reports the bound when it exceeds slot_cap).
+ */
+int64_t crv_digis_workspace(const CrvParams *p, int64_t ncharges, int64_t slot_cap);
+int crv_digis(const CrvParams *p, const CrvChannels *ch, int64_t ncharges, const int64_t *label, const double *time,
+              const double *charge, const double *tmpl, int32_t tlen, const int64_t *ev_keys, const uint32_t *ev_runs,
+              int64_t n_events, int64_t slot_cap, CrvDigis *out, int64_t out_cap, int64_t *n_out_dev, void *workspace,
+              int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
 
 #ifdef __cplusplus
 }

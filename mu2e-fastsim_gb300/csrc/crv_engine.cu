@@ -8,6 +8,7 @@
 
 #include "crv_launch.h"
 #include "crv_response.cuh"
+#include "crv_waveform.cuh"
 
 namespace crv {
 
@@ -101,6 +102,12 @@ __global__ void k_fill_step_event(CrvEvents ev, long long nevents, int32_t* __re
 }
 
 __global__ void k_set_i64(long long* __restrict__ dst, long long v) { *dst = v; }
+
+// *out = (*total <= cap) ? *n : 0  (downstream kernels then see no groups)
+__global__ void k_guard_groups(const long long* __restrict__ total, long long cap, const long long* __restrict__ n,
+                               long long* __restrict__ out) {
+  *out = (*total <= cap) ? *n : 0;
+}
 
 // ---------------------------------------------------------------------------------------------------------------------
 // workspace carving
@@ -450,6 +457,114 @@ extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups
   CK(cudaGetLastError());
   if (g_charges)
     CK(cudaMemcpyAsync(g_charges, w.ntot, sizeof(int32_t) * ngroups, cudaMemcpyDeviceToDevice, s));
+  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+// ---- chain.digis ---------------------------------------------------------------------------------------------------
+
+namespace crv {
+struct DigiWs {
+  int32_t *head, *gcount, *g_bound, *g_maxlen, *dn;
+  long long *gidx, *gstart, *glabel, *slot_off, *out_off, *parts, *totals;
+  uint32_t* grun;
+  double* g_tdc0;
+  DigiSlots D;
+  long long sc;
+};
+
+static DigiWs digi_layout(char* base, long long nq, long long slot_cap, int zs, size_t* bytes) {
+  Carve c{base};
+  DigiWs w;
+  w.sc = slot_cap;
+  w.head = c.take<int32_t>(nq);
+  w.gidx = c.take<long long>(nq);
+  w.gstart = c.take<long long>(nq);
+  w.glabel = c.take<long long>(nq);
+  w.gcount = c.take<int32_t>(nq);
+  w.grun = c.take<uint32_t>(nq);
+  w.g_tdc0 = c.take<double>(nq);
+  w.g_bound = c.take<int32_t>(nq);
+  w.g_maxlen = c.take<int32_t>(nq);
+  w.slot_off = c.take<long long>(nq);
+  w.dn = c.take<int32_t>(nq);
+  w.out_off = c.take<long long>(nq);
+  w.parts = c.take<long long>(scan_parts_len(nq) + 1);
+  w.totals = c.take<long long>(8);
+  w.D.off = w.slot_off;
+  w.D.cap = w.g_bound;
+  w.D.n = w.dn;
+  w.D.chan = c.take<long long>(slot_cap);
+  w.D.start = c.take<double>(slot_cap);
+  w.D.tdc0 = c.take<double>(slot_cap);
+  w.D.starttdc = c.take<long long>(slot_cap);
+  w.D.volt = c.take<double>(slot_cap * zs);
+  w.D.adc = c.take<int16_t>(slot_cap * zs);
+  *bytes = c.off + 256;
+  return w;
+}
+}  // namespace crv
+
+extern "C" int64_t crv_digis_workspace(const CrvParams* p, int64_t ncharges, int64_t slot_cap) {
+  if (!p || ncharges < 0 || slot_cap < 0 || p->samples_zs <= 0 || p->samples_zs > 32) return -1;
+  size_t b = 0;
+  digi_layout(nullptr, ncharges, slot_cap, p->samples_zs, &b);
+  return (int64_t)b;
+}
+
+extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const int64_t* label,
+                         const double* time, const double* charge, const double* tmpl, int32_t tlen,
+                         const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
+                         CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
+                         void* stream, CrvStatus* status_dev) {
+  if (!p || !ch || !out || !n_out_dev || !status_dev || ncharges < 0 || slot_cap < 0 || out_cap < 0) return CRV_ERR_ARG;
+  if (p->samples_zs <= 0 || p->samples_zs > 32 || tlen <= 0 || !tmpl) return CRV_ERR_ARG;
+  if (ncharges > 0 && (!label || !time || !charge)) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ncharges == 0) {
+    CK(cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  size_t need = 0;
+  digi_layout(nullptr, ncharges, slot_cap, p->samples_zs, &need);
+  if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  DigiWs w = digi_layout(base, ncharges, slot_cap, p->samples_zs, &dummy);
+  const long long* lab = reinterpret_cast<const long long*>(label);
+  CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.g_maxlen, 0, sizeof(int32_t) * ncharges, s));
+  CK(cudaMemsetAsync(w.g_bound, 0, sizeof(int32_t) * ncharges, s));
+  CK(cudaMemsetAsync(w.dn, 0, sizeof(int32_t) * ncharges, s));
+  unsigned gq = grid_for(ncharges, 256, 8);
+  k_label_heads<<<gq, 256, 0, s>>>(ncharges, lab, w.head);
+  CK(exclusive_scan(w.head, ncharges, Identity(), w.gidx, &w.totals[0], w.parts, s));
+  k_label_groups<<<gq, 256, 0, s>>>(ncharges, lab, w.head, w.gidx, w.gstart, w.glabel);
+  k_group_counts<<<gq, 256, 0, s>>>(&w.totals[0], ncharges, w.gstart, w.glabel, w.gcount,
+                                    reinterpret_cast<const long long*>(ev_keys), ev_runs, n_events, w.grun, S);
+  CK(cudaGetLastError());
+  WfGroups G{&w.totals[0], w.gstart, w.gcount, w.glabel, w.grun};
+  if (p->precision == 1)
+    CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen, s));
+  else
+    CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen, s));
+  CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, CRV_NEED_DIGIS, S);
+  // synthesis only when the slots fit: guard by zeroing the group count otherwise
+  k_guard_groups<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, &w.totals[0], &w.totals[2]);
+  CK(cudaGetLastError());
+  G.n = &w.totals[2];
+  if (p->precision == 1)
+    CK(launch_wf_synth<float>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.D, S, s));
+  else
+    CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.D, S, s));
+  CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_DIGIS_OUT, S);
+  Digis O{reinterpret_cast<long long*>(out->chan), out->start, out->tdc0, reinterpret_cast<long long*>(out->starttdc),
+          out->volt, out->adc};
+  k_digi_compact<<<grid_for(ncharges, 8, 16), 256, 0, s>>>(&w.totals[2], w.D, w.out_off, p->samples_zs, O, out_cap);
   k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
   CK(cudaGetLastError());
   return CRV_OK;

@@ -7,6 +7,8 @@ namespace crv {
 
 struct SipmGroups;
 struct SipmOut;
+struct WfGroups;
+struct DigiSlots;
 
 struct DeviceInfo {
   int sms;
@@ -36,5 +38,15 @@ cudaError_t launch_photon_rows(const CrvParams& p, const CrvEvents& ev, const Cr
 template <typename R, typename PT>
 cudaError_t launch_sipm(const CrvParams& p, const CrvPixels& px, const SipmGroups& G, const long long* ngroups_dev,
                         const PT* ph_time, const SipmOut& O, Status* status, cudaStream_t s);
+
+template <typename R>
+cudaError_t launch_wf_prepass(const CrvParams& p, const CrvChannels& ch, const WfGroups& G, long long ng_bound,
+                              const double* time, const double* tmpl, int tlen, double* g_tdc0, int32_t* g_bound,
+                              int32_t* g_maxlen, cudaStream_t s);
+
+template <typename R>
+cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_bound, const double* time,
+                            const double* charge, const double* tmpl, int tlen, const double* g_tdc0,
+                            const int32_t* g_maxlen, const DigiSlots& D, Status* status, cudaStream_t s);
 
 }  // namespace crv

@@ -1,0 +1,410 @@
+// Waveform stage: SiPM charges -> zero-suppressed 12-sample digis.
+//
+// Semantics of the reference synthesis (crv/crvfastsim/reco/waveform.py:65-172, chain.py:219-270):
+//   * TDC0 per (event, FEB): one uniform x width (keyed by event and FEB key, so no global order is needed);
+//   * charges of a SiPM split into clusters where consecutive times differ by more than max_time + 4 periods; a
+//     cluster is kept if n_charges * max(template) >= min_voltage;
+//   * the cluster waveform starts at t_start = ceil((t_first - P - TDC0) / P) P + TDC0 and is
+//     max(floor((t_last - t_first + max_time) / P), last reached sample + 1) samples long;
+//   * every charge adds template[rint((J P + t_start - t) / precision)] * charge / q_ref to samples J >= ceil((t -
+//     t_start)/P) within ceil(max_time/P) + 2 samples; electronics noise sigma * z(event, channel, tick) is added to
+//     every sample (keyed normals);
+//   * zero suppression: a digi starts at sample i if a sample in i-2..i+2 exceeds min_voltage, i >= the end of the
+//     previous digi and t_start + i P lies in the window; ADC = clip(int16(V * conv + pedestal + 0.5), min, max);
+//     startTDC = rint((start - TDC0) / P).
+//
+// GPU mapping: one warp per SiPM; the cluster waveform is a shared-memory tile (lanes own samples); each sample sums
+// the charges that reach it in charge order (a contiguous range found by binary search), so FP64 sums round exactly
+// as the reference's scatter-add; the zero-suppression scan proceeds 32 samples per ballot.
+#pragma once
+#include "crv_device.cuh"
+
+namespace crv {
+
+struct WfGroups {
+  const long long* n;            // device: number of SiPM groups
+  const long long* start;        // first charge row of the group
+  const int32_t* count;          // charges in the group
+  const long long* label;        // SiPM label
+  const uint32_t* run;           // run per group (keys), may be null (run 0)
+};
+
+struct DigiSlots {
+  const long long* off;          // first slot of the group
+  const int32_t* cap;            // slots of the group
+  int32_t* n;                    // digis written
+  long long* chan;
+  double* start;
+  double* tdc0;
+  long long* starttdc;
+  double* volt;                  // [slots, 12]
+  int16_t* adc;                  // [slots, 12]
+};
+
+__device__ __forceinline__ int32_t feb_key(const CrvParams& p, const CrvChannels& ch, int c) {
+  return p.feb_key_mode == 1 ? ch.feb[c] : ch.roc[c] * 1000 + ch.feb[c];
+}
+
+__device__ __forceinline__ double tdc0_of(const CrvParams& p, const CrvChannels& ch, long long label, uint32_t run) {
+  long long evk = label / 32768;
+  int c = int(label % 32768);
+  EvKey ek{uint32_t(evk & 0xFFFFF), uint32_t(evk >> 20), run};
+  U4 w = keyed(p.seed, ek, ST_TDC0 << 28, uint32_t(feb_key(p, ch, c)));
+  return u01(w.x, w.y) * p.feb_phase_width;
+}
+
+__device__ __forceinline__ int reach_samples(const CrvParams& p) { return int(ceil(p.spe_max_time / p.period)) + 2; }
+
+// first sample a charge at time t reaches in a cluster starting at ts
+template <typename R>
+__device__ __forceinline__ long long first_sample(const CrvParams& p, double t, double ts) {
+  if (sizeof(R) == 8) {
+    double v = ceil((t - ts) / p.period);
+    return v > 0.0 ? (long long)v : 0;
+  }
+  float v = ceilf(float(t - ts) / float(p.period));
+  return v > 0.0f ? (long long)v : 0;
+}
+
+// template index of sample J for a charge at t (returns -1 when the pair does not contribute)
+template <typename R>
+__device__ __forceinline__ int tmpl_index(const CrvParams& p, long long J, double t, double ts, int tlen) {
+  if (sizeof(R) == 8) {
+    double st = double(J) * p.period + ts - t;
+    if (!(st >= 0.0)) return -1;
+    double ti = rint(st / p.spe_precision);
+    return ti < double(tlen) ? int(ti) : -1;
+  }
+  float st = float(J) * float(p.period) - float(t - ts);
+  if (!(st >= 0.0f)) return -1;
+  float ti = rintf(st / float(p.spe_precision));
+  return ti < float(tlen) ? int(ti) : -1;
+}
+
+struct ClusterInfo {
+  int a, b;                      // charge rows [a, b) relative to the group start
+  double ts;                     // t_start
+  long long tick0;
+  int length;
+  bool keep;
+};
+
+// Length of a kept cluster: max(est, last contributing sample + 1); lanes split the charges.
+template <typename R>
+__device__ int cluster_length(const CrvParams& p, const double* t, int a, int b, double ts, int tlen, bool keep) {
+  long long est = (long long)floor((t[b - 1] - t[a] + p.spe_max_time) / p.period);
+  long long used = 0;
+  if (keep) {
+    int nr = reach_samples(p);
+    for (int q = a + lane_id(); q < b; q += 32) {
+      long long j0 = first_sample<R>(p, t[q], ts);
+      for (int k = nr - 1; k >= 0; --k) {
+        if (tmpl_index<R>(p, j0 + k, t[q], ts, tlen) >= 0) {
+          if (j0 + k + 1 > used) used = j0 + k + 1;
+          break;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      long long y = __shfl_xor_sync(0xffffffffu, used, o);
+      used = y > used ? y : used;
+    }
+  }
+  long long L = est > used ? est : used;
+  return int(L);
+}
+
+// Next cluster [a, b) of the group from charge a (warp-uniform); returns b.
+__device__ inline int next_cluster_end(const CrvParams& p, const double* t, int a, int n) {
+  double gap = p.spe_max_time + 4.0 * p.period;
+  int b = a + 1;
+  while (b < n) {
+    int i = b + lane_id();
+    bool brk = i < n && (t[i] - t[i - 1] > gap);
+    unsigned m = __ballot_sync(0xffffffffu, brk);
+    if (m) return b + __ffs(m) - 1;
+    int adv = n - b < 32 ? n - b : 32;
+    b += adv;
+  }
+  return n;
+}
+
+// Per group: TDC0, digi bound (sum over kept clusters of ceil(length / 12)), longest kept cluster.
+template <typename R>
+__global__ void k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G, const double* __restrict__ time,
+                             const double* __restrict__ tmpl, int tlen, double* __restrict__ g_tdc0,
+                             int32_t* __restrict__ g_bound, int32_t* __restrict__ g_maxlen) {
+  __shared__ double vmax_s;
+  if (threadIdx.x < 32) {
+    double v = -1e300;
+    for (int i = threadIdx.x; i < tlen; i += 32) v = fmax(v, tmpl[i]);
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) vmax_s = v;
+  }
+  __syncthreads();
+  double vmax = vmax_s;
+  long long ng = *G.n;
+  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
+    int n = G.count[g];
+    const double* t = time + G.start[g];
+    long long lab = G.label[g];
+    double tdc0 = tdc0_of(p, ch, lab, G.run ? G.run[g] : 0u);
+    long long bound = 0;
+    int maxlen = 0;
+    for (int a = 0; a < n;) {
+      int b = next_cluster_end(p, t, a, n);
+      bool keep = double(b - a) * vmax >= p.min_voltage;
+      if (keep) {
+        double ts = ceil((t[a] - p.period - tdc0) / p.period) * p.period + tdc0;
+        int L = cluster_length<R>(p, t, a, b, ts, tlen, true);
+        bound += (L + p.samples_zs - 1) / p.samples_zs;
+        maxlen = L > maxlen ? L : maxlen;
+      }
+      a = b;
+    }
+    if (lane_id() == 0) {
+      g_tdc0[g] = tdc0;
+      g_bound[g] = int32_t(bound);
+      g_maxlen[g] = maxlen;
+    }
+  }
+}
+
+__device__ __forceinline__ int16_t adc_of(const CrvParams& p, double v) {
+  double x = v * p.adc_conversion + double(p.adc_pedestal) + 0.5;
+  long long i;
+  if (!(x == x)) i = (long long)-2147483648ll;
+  else if (x >= 2147483647.0) i = 2147483647ll;
+  else if (x <= -2147483648.0) i = -2147483648ll;
+  else i = (long long)trunc(x);
+  int16_t s = int16_t(uint16_t(uint32_t(int32_t(i)) & 0xFFFFu));
+  int r = s;
+  if (r < p.min_adc) r = p.min_adc;
+  if (r > p.max_adc) r = p.max_adc;
+  return int16_t(r);
+}
+
+// Synthesis + zero suppression of the groups whose longest kept cluster is in (lo, cap].
+template <typename R>
+__global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
+                                                  const double* __restrict__ charge, const double* __restrict__ tmpl,
+                                                  int tlen, const double* __restrict__ g_tdc0,
+                                                  const int32_t* __restrict__ g_maxlen, int lo, int cap,
+                                                  int last_pass, DigiSlots D, Status* status) {
+  extern __shared__ __align__(16) char smem[];
+  R* wave = reinterpret_cast<R*>(smem) + size_t(warp_in_block()) * cap;
+  __shared__ double vmax_s;
+  if (threadIdx.x < 32) {
+    double v = -1e300;
+    for (int i = threadIdx.x; i < tlen; i += 32) v = fmax(v, tmpl[i]);
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) vmax_s = v;
+  }
+  __syncthreads();
+  const double vmax = vmax_s;
+  const int nr = reach_samples(p);
+  const int zs = p.samples_zs;
+  long long ng = *G.n;
+  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
+    int ml = g_maxlen[g];
+    if (ml <= lo) continue;
+    if (ml > cap) {
+      if (last_pass && lane_id() == 0) {
+        set_flag(status, CRV_ST_CAPACITY);
+        need_at_least(status, CRV_NEED_SAMPLES, ml);
+      }
+      continue;
+    }
+    int n = G.count[g];
+    long long q0 = G.start[g];
+    const double* t = time + q0;
+    const double* qc = charge + q0;
+    long long lab = G.label[g];
+    uint32_t run = G.run ? G.run[g] : 0u;
+    long long evk = lab / 32768;
+    EvKey ek{uint32_t(evk & 0xFFFFF), uint32_t(evk >> 20), run};
+    uint32_t chan = uint32_t(lab % 32768);
+    double tdc0 = g_tdc0[g];
+    long long slot = D.off[g];
+    int scap = D.cap[g];
+    int nd = 0;
+    for (int a = 0; a < n;) {
+      int b = next_cluster_end(p, t, a, n);
+      bool keep = double(b - a) * vmax >= p.min_voltage;
+      if (!keep) { a = b; continue; }
+      double k0 = ceil((t[a] - p.period - tdc0) / p.period);
+      double ts = k0 * p.period + tdc0;
+      int L = cluster_length<R>(p, t, a, b, ts, tlen, true);
+      // samples: sum of the charges reaching each sample, in charge order
+      for (int j = lane_id(); j < L; j += 32) {
+        // charges with first_sample in (j - nr, j]: first_sample is non-decreasing along the cluster
+        int lo_q = a, hi_q = b;                      // first charge with first_sample > j - nr
+        while (lo_q < hi_q) {
+          int m = (lo_q + hi_q) >> 1;
+          if (first_sample<R>(p, t[m], ts) > (long long)j - nr) hi_q = m; else lo_q = m + 1;
+        }
+        int q1 = lo_q;
+        int lo2 = q1, hi2 = b;                       // first charge with first_sample > j
+        while (lo2 < hi2) {
+          int m = (lo2 + hi2) >> 1;
+          if (first_sample<R>(p, t[m], ts) > (long long)j) hi2 = m; else lo2 = m + 1;
+        }
+        R acc = R(0);
+        for (int q = q1; q < lo2; ++q) {
+          int ti = tmpl_index<R>(p, j, t[q], ts, tlen);
+          if (ti >= 0) acc += R(tmpl[ti]) * R(qc[q] / p.spe_ref_charge);
+        }
+        if (p.noise_on) {
+          long long tk = (long long)k0 + j;
+          U4 w = keyed(p.seed, ek, (ST_NOISE << 28) | (chan & 0x7FFFu), uint32_t(tk >> 1));
+          R z0, z1;
+          Math<R>::normal_pair(w, &z0, &z1);
+          acc = acc + R(p.noise_sigma) * ((tk & 1) ? z1 : z0);
+        }
+        wave[j] = acc;
+      }
+      __syncwarp();
+      // zero suppression over chunks of 32 samples
+      int next_i = 0;
+      for (int base = 0; base < L; base += 32) {
+        int i = base + lane_id();
+        bool w = false;
+        if (i < L) {
+          for (int d = -2; d <= 2 && !w; ++d) {
+            int k = i + d;
+            if (k >= 0 && k < L && wave[k] > R(p.min_voltage)) w = true;
+          }
+        }
+        double tstart = ts + double(i) * p.period;
+        bool inwin = (tstart >= p.window_lo) && (tstart <= p.window_hi);
+        unsigned cand = __ballot_sync(0xffffffffu, w && inwin);
+        while (true) {
+          unsigned m = cand;
+          if (next_i > base) m &= (next_i - base >= 32) ? 0u : ~((1u << (next_i - base)) - 1u);
+          if (!m) break;
+          int i0 = base + __ffs(m) - 1;
+          // emit digi at i0
+          if (nd < scap) {
+            long long o = slot + nd;
+            double st0 = ts + double(i0) * p.period;
+            if (lane_id() < zs) {
+              int c = i0 + lane_id();
+              double v = c < L ? double(wave[c]) : 0.0;
+              D.volt[o * zs + lane_id()] = v;
+              D.adc[o * zs + lane_id()] = adc_of(p, v);
+            }
+            if (lane_id() == 0) {
+              D.chan[o] = lab;
+              D.start[o] = st0;
+              D.tdc0[o] = tdc0;
+              D.starttdc[o] = (long long)rint((st0 - tdc0) / p.period);
+            }
+          }
+          ++nd;
+          next_i = i0 + zs;
+        }
+      }
+      __syncwarp();
+      a = b;
+    }
+    if (lane_id() == 0) {
+      D.n[g] = nd;
+      if (nd > scap) set_flag(status, CRV_ST_CAPACITY);
+    }
+  }
+}
+
+}  // namespace crv
+
+namespace crv {
+
+struct Digis {
+  long long* chan;
+  double* start;
+  double* tdc0;
+  long long* starttdc;
+  double* volt;
+  int16_t* adc;
+};
+
+#ifdef CRV_ENGINE_TU
+// Move each group's digis from its slots to the output, ordered by start (stable) within the group.
+__global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D, const long long* __restrict__ out_off,
+                               int zs, Digis O, long long out_cap) {
+  long long ng = *ng_dev;
+  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
+    int nd = D.n[g];
+    if (nd > D.cap[g]) continue;
+    long long s0 = D.off[g], o0 = out_off[g];
+    if (o0 + nd > out_cap) continue;
+    for (int i = 0; i < nd; ++i) {
+      // rank of digi i among the group's digis by start, ties by production order
+      double si = D.start[s0 + i];
+      int r = 0;
+      for (int j = lane_id(); j < nd; j += 32) {
+        double sj = D.start[s0 + j];
+        r += (sj < si) || (sj == si && j < i);
+      }
+      r = warp_sum(r);
+      long long o = o0 + r, s = s0 + i;
+      if (lane_id() == 0) {
+        O.chan[o] = D.chan[s];
+        O.start[o] = D.start[s];
+        O.tdc0[o] = D.tdc0[s];
+        O.starttdc[o] = D.starttdc[s];
+      }
+      if (lane_id() < zs) {
+        O.volt[o * zs + lane_id()] = D.volt[s * zs + lane_id()];
+        O.adc[o * zs + lane_id()] = D.adc[s * zs + lane_id()];
+      }
+    }
+  }
+}
+
+// Segments of equal labels in a label-sorted array: heads, then group start/label/count.
+__global__ void k_label_heads(long long n, const long long* __restrict__ label, int32_t* __restrict__ head) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    head[i] = (i == 0 || label[i] != label[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_label_groups(long long n, const long long* __restrict__ label, const int32_t* __restrict__ head,
+                               const long long* __restrict__ gidx, long long* __restrict__ gstart,
+                               long long* __restrict__ glabel) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (head[i]) {
+      long long g = gidx[i];
+      gstart[g] = i;
+      glabel[g] = label[i];
+    }
+}
+
+// counts from consecutive starts; run per group from a sorted (event key -> run) table (run 0 if absent)
+__global__ void k_group_counts(const long long* __restrict__ ng_dev, long long n, const long long* __restrict__ gstart,
+                               const long long* __restrict__ glabel, int32_t* __restrict__ gcount,
+                               const long long* __restrict__ ev_keys, const uint32_t* __restrict__ ev_runs,
+                               long long n_ev, uint32_t* __restrict__ grun, Status* status) {
+  long long ng = *ng_dev;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+    long long e = (g + 1 < ng ? gstart[g + 1] : n) - gstart[g];
+    gcount[g] = int32_t(e);
+    uint32_t r = 0;
+    if (ev_keys && n_ev > 0) {
+      long long k = glabel[g] / 32768;
+      long long lo = 0, hi = n_ev;
+      while (lo < hi) {
+        long long m = (lo + hi) >> 1;
+        if (ev_keys[m] < k) lo = m + 1; else hi = m;
+      }
+      if (lo < n_ev && ev_keys[lo] == k) r = ev_runs[lo];
+      else set_flag(status, CRV_ST_ORDER);
+    }
+    grun[g] = r;
+  }
+}
+#endif
+
+}  // namespace crv
