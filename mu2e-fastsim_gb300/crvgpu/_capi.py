@@ -76,6 +76,19 @@ class CrvCharges(ctypes.Structure):
     _fields_ = [("label", c_p), ("time", c_p), ("charge", c_p), ("pe", c_p), ("photon", c_p)]
 
 
+class CrvDigis(ctypes.Structure):
+    _fields_ = [("chan", c_p), ("start", c_p), ("tdc0", c_p), ("starttdc", c_p), ("volt", c_p), ("adc", c_p)]
+
+
+PULSE_INT = ("wf", "seq")
+PULSE_FLOAT = ("pe", "peph", "time", "height", "beta", "chi2", "letime", "ped", "fit_A", "fit_mu", "fit_b")
+PULSE_BOOL = ("failed", "zerondf", "pedfromdb")
+
+
+class CrvPulses(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in PULSE_INT + PULSE_FLOAT + PULSE_BOOL]
+
+
 P = ctypes.POINTER
 
 _SIGS = {
@@ -90,6 +103,12 @@ _SIGS = {
     "crv_photons": (c_i32, [P(CrvParams), P(CrvEvents), c_i64, P(CrvSteps), c_i64, P(CrvBars), c_p, c_p, c_p, c_p,
                             c_p, c_p, c_p, c_p, c_p]),
     "crv_sipm_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
+    "crv_digis_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
+    "crv_digis": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64, c_i64,
+                          P(CrvDigis), c_i64, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
+    "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, c_i64, P(CrvPulses),
+                           c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_sipm": (c_i32, [P(CrvParams), P(CrvPixels), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, P(CrvCharges),
                          c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
 }

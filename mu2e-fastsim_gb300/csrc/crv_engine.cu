@@ -9,6 +9,7 @@
 #include "crv_launch.h"
 #include "crv_response.cuh"
 #include "crv_waveform.cuh"
+#include "crv_pulsefit.cuh"
 
 namespace crv {
 
@@ -566,6 +567,98 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
           out->volt, out->adc};
   k_digi_compact<<<grid_for(ncharges, 8, 16), 256, 0, s>>>(&w.totals[2], w.D, w.out_off, p->samples_zs, O, out_cap);
   k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+// ---- pulsefit.reconstruct -----------------------------------------------------------------------------------------
+
+namespace crv {
+struct PulseWs {
+  PulseRec* rec;
+  long long *base, *out_off, *parts, *totals;
+  int32_t *count, *deferred;
+  long long rc;
+};
+
+static PulseWs pulse_layout(char* base, long long nw, long long rec_cap, size_t* bytes) {
+  Carve c{base};
+  PulseWs w;
+  w.rc = rec_cap;
+  w.base = c.take<long long>(nw);
+  w.out_off = c.take<long long>(nw);
+  w.parts = c.take<long long>(scan_parts_len(nw) + 1);
+  w.totals = c.take<long long>(8);
+  w.count = c.take<int32_t>(nw);
+  w.deferred = c.take<int32_t>(nw);
+  w.rec = c.take<PulseRec>(rec_cap);
+  *bytes = c.off + 256;
+  return w;
+}
+
+__global__ void k_pulse_compact(long long nw, const long long* __restrict__ base, const int32_t* __restrict__ count,
+                                const long long* __restrict__ out_off, const PulseRec* __restrict__ rec,
+                                CrvPulses O, long long out_cap) {
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+    int c = count[w];
+    long long o0 = out_off[w], b0 = base[w];
+    if (o0 + c > out_cap) continue;
+    for (int k = 0; k < c; ++k) {
+      const PulseRec& r = rec[b0 + k];
+      long long o = o0 + k;
+      O.wf[o] = w; O.seq[o] = r.seq;
+      O.pe[o] = r.pe; O.peph[o] = r.peph; O.time[o] = r.time; O.height[o] = r.height; O.beta[o] = r.beta;
+      O.chi2[o] = r.chi2; O.letime[o] = r.letime; O.ped[o] = r.ped;
+      O.fit_A[o] = r.A; O.fit_mu[o] = r.mu; O.fit_b[o] = r.b;
+      O.failed[o] = r.failed; O.zerondf[o] = r.zerondf; O.pedfromdb[o] = r.pedfromdb;
+    }
+  }
+}
+}  // namespace crv
+
+extern "C" int64_t crv_pulses_workspace(const CrvParams* p, int64_t nw, int64_t rec_cap) {
+  if (!p || nw < 0 || rec_cap < 0) return -1;
+  size_t b = 0;
+  pulse_layout(nullptr, nw, rec_cap, &b);
+  return (int64_t)b;
+}
+
+extern "C" int crv_pulses(const CrvParams* p, int64_t nw, const int64_t* off, const int32_t* n,
+                          const int64_t* start_tdc, const double* ped_db, const double* area, const double* height,
+                          const int16_t* adc16, const int64_t* adc64, int32_t max_pulses, int64_t rec_cap,
+                          CrvPulses* out, int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
+                          int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!p || !out || !n_out_dev || !status_dev || nw < 0 || rec_cap < 0 || out_cap < 0 || max_pulses < 0)
+    return CRV_ERR_ARG;
+  if (nw > 0 && (!off || !n || !start_tdc || !ped_db || !area || !height || !wf_near || (!adc16 == !adc64)))
+    return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nw == 0) {
+    CK(cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  size_t need = 0;
+  pulse_layout(nullptr, nw, rec_cap, &need);
+  if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  PulseWs w = pulse_layout(base, nw, rec_cap, &dummy);
+  CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.count, 0, sizeof(int32_t) * nw, s));
+  CK(cudaMemsetAsync(w.deferred, 0, sizeof(int32_t) * nw, s));
+  CK(cudaMemsetAsync(wf_near, 0, nw, s));
+  WaveIn W{nw, reinterpret_cast<const long long*>(off), n, reinterpret_cast<const long long*>(start_tdc), ped_db,
+           area, height, adc16, reinterpret_cast<const long long*>(adc64)};
+  PulseOut O{w.rec, w.base, w.count, wf_near, &w.totals[0], rec_cap};
+  if (p->precision == 1)
+    CK(launch_pulsefit<float>(*p, W, max_pulses, O, w.deferred, S, s));
+  else
+    CK(launch_pulsefit<double>(*p, W, max_pulses, O, w.deferred, S, s));
+  CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s));
+  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], out_cap, CRV_NEED_PULSES_OUT, S);
+  k_pulse_compact<<<grid_for(nw, 256, 8), 256, 0, s>>>(nw, w.base, w.count, w.out_off, w.rec, *out, out_cap);
+  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[1], reinterpret_cast<long long*>(n_out_dev));
   CK(cudaGetLastError());
   return CRV_OK;
 }

@@ -9,6 +9,8 @@ struct SipmGroups;
 struct SipmOut;
 struct WfGroups;
 struct DigiSlots;
+struct WaveIn;
+struct PulseOut;
 
 struct DeviceInfo {
   int sms;
@@ -48,5 +50,9 @@ template <typename R>
 cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_bound, const double* time,
                             const double* charge, const double* tmpl, int tlen, const double* g_tdc0,
                             const int32_t* g_maxlen, const DigiSlots& D, Status* status, cudaStream_t s);
+
+template <typename R>
+cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, int max_pulses, const PulseOut& O, int32_t* deferred,
+                            Status* status, cudaStream_t s);
 
 }  // namespace crv

@@ -1,0 +1,68 @@
+"""GPU pulse reconstruction against the reference's own outputs (golden fixtures) and the oracle.
+
+FP64: pulse counts, sequence numbers and flags identical; fitted PE and time within 1e-9 relative (exp differs in the
+last bit between libm/NumPy and CUDA, so the LM iterations agree to ~1e-12, not bit for bit).  FP32-mixed: mean PE
+within 0.3 % and time within 0.05 ns of FP64 on the non-failed fits.
+"""
+import numpy as np
+import pytest
+
+from crvgpu import config as CF
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+EXACT = ("wf", "seq", "failed", "zerondf", "pedfromdb", "wf_near_threshold")
+CLOSE = ("pe", "peph", "time", "height", "beta", "chi2", "letime", "ped", "fit_A", "fit_mu", "fit_b")
+
+
+def compare(got, ref, tag):
+    for k in EXACT:
+        assert np.array_equal(np.asarray(got[k]).astype(np.int64), np.asarray(ref[k]).astype(np.int64)), (tag, k)
+    worst = {}
+    for k in CLOSE:
+        a, b = np.asarray(got[k], float), np.asarray(ref[k], float)
+        rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+        rel[(a == b)] = 0.0
+        worst[k] = float(rel.max()) if len(rel) else 0.0
+        assert worst[k] <= RTOL, (tag, k, worst[k])
+    return worst
+
+
+@pytest.mark.parametrize("tag", ["single", "kpp", "uneven", "edge", "p125"])
+def test_pulsefit_matches_reference_fixtures(golden, tag):
+    from crvgpu import pulsefit as PF
+    g = golden("pulsefit.npz")
+    period = 12.5 if tag == "p125" else float(g["period"][0])
+    cfg = CF.RecoConfig(period=period)
+    args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
+    f = PF.reconstruct_full if tag in ("uneven", "edge") else PF.reconstruct
+    r = f(*args, cfg)
+    ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f"{tag}_out_")}
+    worst = compare(r, ref, tag)
+    print(tag, "max rel diff", {k: f"{v:.1e}" for k, v in worst.items()})
+
+
+def cfg2_like(n_wf=3000, seed=5):
+    """Uneven waveforms of the batched-fit workload: 1-12 pulses, lengths over {32..512}, pedestal 100, noise 2 ADC,
+    PE log-uniform 5-500, beta U(10, 25)."""
+    from tests.helpers import uneven_waveforms
+    return uneven_waveforms(np.random.default_rng(seed), n_wf)
+
+
+def test_pulsefit_fp32_mixed_accuracy():
+    from crvgpu import pulsefit as PF
+    adc, n, st, ped, area, height = cfg2_like(1500)
+    cfg = CF.RecoConfig()
+    r64 = PF.reconstruct_full(adc, n, st, ped, area, height, cfg)
+    r32 = PF.reconstruct_full(adc, n, st, ped, area, height, cfg, precision="fp32")
+    # same pulse list except for rare knife-edge flips; compare on common (wf, seq) with both fits good
+    k64 = r64["wf"] * 4096 + r64["seq"]
+    k32 = r32["wf"] * 4096 + r32["seq"]
+    common, i64, i32 = np.intersect1d(k64, k32, return_indices=True)
+    assert len(common) > 0.98 * len(k64)
+    good = ~r64["failed"][i64] & ~r32["failed"][i32]
+    pe64, pe32 = r64["pe"][i64][good], r32["pe"][i32][good]
+    assert abs(pe32.mean() / pe64.mean() - 1) < 3e-3
+    dt = np.abs(r32["time"][i32][good] - r64["time"][i64][good])
+    assert np.median(dt) < 0.05
