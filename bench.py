@@ -1,0 +1,353 @@
+"""Benchmark of the GB300 CRV response engine: CRV events/s steps -> coincidence clusters.
+
+Workload (default): 1,048,576 events of the workload's one-module geometry (4 layers x 16 counters of 450 cm),
+Poisson(40) synthetic steps per event (~42 M steps, SoA float32 x/y/z/t/edep + int32 bar, resident in HBM), the full
+chain (photons, SiPM, waveforms + zero suppression, pulse fit, coincidences) in event batches.  One benchmark step =
+one pass over all events.  The FP32-mixed engine is the headline (value); the FP64 plain chain is timed beside it.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Multi-GPU: events are independent, so each rank processes its own event range (weak scaling, no collective on the
+data path; a barrier brackets the timed region and the time is the max over ranks).
+--impl reference: the reference algorithm on the host cores (the CPU oracle's restatement of the reference NumPy
+path: keyed C photons/SiPM + NumPy waveforms/pulse fit + Python coincidence finder), one process per core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "mu2e-fastsim_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "CRV events/s steps→coincidences, FP32 vs FP64 plain, 1 GB300; p99 job latency"
+UNIT = "events/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# CPU reference arm (oracle port of the reference NumPy path)
+
+def _cpu_worker(args):
+    n_events, first_event, seed = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "mu2e-fastsim_gb300")]
+    from oracle import oracle as O
+    from crvgpu import config as CF
+    from crvgpu import geometry as GM
+    from crvgpu import waveform as WV
+    geom = GM.module_geometry()
+    cond = GM.default_conditions(geom)
+    cfg = CF.ChainConfig()
+    G = GM.sector_geom(geom)
+    steps = GM.synthetic_steps(n_events, geom, seed=seed, first_event=first_event)
+    t0 = time.perf_counter()
+    Q, _ = O.charges(steps, geom, cond, cfg.response, cfg.sipm, seed, cfg.window[1])
+    wc = CF.WaveformConfig()
+    run_of = lambda keys: np.ones(len(np.asarray(keys).ravel()), np.int64)  # noqa: E731
+    tdc0 = lambda labels: O.tdc0_of_labels(labels, cond, seed, wc.period, "roc_feb", run_of)  # noqa: E731
+    D = O.synthesize(Q["chan"], Q["time"], Q["charge"], tdc0, WV.single_pe_template(wc), wc, wc.period, cfg.window,
+                     O.keyed_noise(seed, run_of))
+    W = O.reco_waveforms(D, cond)
+    rc = CF.RecoConfig()
+    P = O.pulses_from_waveforms(W, cond, rc, rc.period)
+    out = O.clusters_from_pulses(W, P, G, cond.status, CF.FinderConfig())
+    return time.perf_counter() - t0, n_events, len(out["cl_event"])
+
+
+def cpu_reference(n_events_per_proc, procs, seed=7):
+    """Events/s of the CPU reference path on `procs` processes (spawned), each on its own event range."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    jobs = [(n_events_per_proc, 1_000_000 + i * n_events_per_proc, seed) for i in range(procs)]
+    t0 = time.perf_counter()
+    if procs == 1:
+        res = [_cpu_worker(jobs[0])]
+    else:
+        with ctx.Pool(procs) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    ev = sum(r[1] for r in res)
+    busy = max(r[0] for r in res)
+    return ev / busy, ev, busy, wall
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    procs = max(1, min(os.cpu_count() or 1, 64))
+    per = args.ref_events
+    vals = []
+    for _ in range(max(1, args.warmup_ref)):
+        cpu_reference(max(8, per // 8), procs)
+    for _ in range(args.steps):
+        v, ev, busy, wall = cpu_reference(per, procs)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * per * procs / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"one 4x16 module, Poisson(40) steps/event, full chain; bounded sample of "
+                                   f"{per} events per process x {procs} processes", "events_per_step": per * procs},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": f"{per} events per process on {procs} processes"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# GPU arm
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--events", type=int, default=1 << 20)
+    ap.add_argument("--batch", type=int, default=1 << 16)
+    ap.add_argument("--ref-events", type=int, default=96)
+    ap.add_argument("--warmup-ref", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    from crvgpu import _capi, chain as CH, config as CF, geometry as GM
+    from crvgpu.response import upload_steps
+
+    geom = GM.module_geometry()
+    cond = GM.default_conditions(geom)
+    # this rank's events (weak scaling: every rank its own event range)
+    first = rank * args.events
+    t_gen = time.perf_counter()
+    batches = []
+    host_batches = []
+    nsteps_total = 0
+    for b0 in range(0, args.events, args.batch):
+        nb = min(args.batch, args.events - b0)
+        st = GM.synthetic_steps(nb, geom, seed=11, first_event=first + b0)
+        host_batches.append(st)
+        batches.append(upload_steps(st, nbars=geom.nbars))
+        nsteps_total += len(st)
+    t_gen = time.perf_counter() - t_gen
+    step_bytes = sum(b.x.numel() * 4 * 5 + b.bar.numel() * 4 for b in batches)
+
+    cfg32 = CF.ChainConfig(precision="fp32")
+    cfg64 = CF.ChainConfig(precision="fp64")
+    eng32 = CH.ChainEngine(geom, cond, cfg32)
+    eng64 = CH.ChainEngine(geom, cond, cfg64)
+
+    def one_pass(eng, seed):
+        tot = dict(clusters=0, pulses=0, charges=0, digis=0)
+        for ds in batches:
+            r = eng.run(ds, seed)
+            tot["clusters"] += r.n_clusters
+            tot["pulses"] += r.n_pulses
+            tot["charges"] += r.n_charges
+            tot["digis"] += r.n_digis
+        return tot
+
+    def timed(eng, k, w):
+        for _ in range(w):
+            one_pass(eng, 5)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clocks = Clocks(local)
+        clocks.start()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = _capi.launch_count()
+        e0.record(st)
+        tot = None
+        for _ in range(k):
+            tot = one_pass(eng, 5)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        launches = _capi.launch_count() - n0
+        ck = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, tot, ck, launches
+
+    ms32, tot32, clk, launches = timed(eng32, args.steps, args.warmup)
+    ev_total = args.events * world * args.steps
+    value = ev_total / (ms32 / 1000.0)
+    fp64 = None
+    if not args.no_fp64:
+        ms64, tot64, clk64, _ = timed(eng64, max(1, args.steps // 2), 1)
+        fp64 = args.events * world * max(1, args.steps // 2) / (ms64 / 1000.0)
+
+    # per-kernel device time of one FP32 pass (profiling events; not the timed number)
+    torch.cuda.synchronize()
+    _capi.profile(True)
+    one_pass(eng32, 5)
+    torch.cuda.synchronize()
+    prof = _capi.profile_read()
+    _capi.profile(False)
+    per_kernel = {}
+    for name, t in prof:
+        a = per_kernel.setdefault(name, [0, 0.0])
+        a[0] += 1
+        a[1] += t
+    top = max(per_kernel.items(), key=lambda kv: kv[1][1])
+    # algorithmic bytes of the dominant kernels (per launch, averaged over the pass)
+    tot_ms = sum(v[1] for v in per_kernel.values())
+
+    # e2e: host step arrays -> device -> chain -> cluster table back to the host, one pass
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h2d = d2h = 0
+    e0.record()
+    for st in host_batches:
+        ds = upload_steps(st, nbars=geom.nbars)
+        h2d += sum(int(np.asarray(st[k]).nbytes) for k in ("x", "y", "z", "t", "edep", "bar"))
+        r = eng32.run(ds, 5)
+        host_cl = {k: v.cpu().numpy() for k, v in r.clusters.items()}
+        d2h += sum(a.nbytes for a in host_cl.values())
+    e1.record()
+    torch.cuda.synchronize()
+    e2e = args.events / (e0.elapsed_time(e1) / 1000.0)
+
+    # FP32-mixed accuracy vs FP64 on the first batch
+    acc = {}
+    try:
+        r64 = eng64.run(batches[0], 5, keep=True)
+        r32 = eng32.run(batches[0], 5, keep=True)
+        pe64, pe32 = r64.pulses["pe"], r32.pulses["pe"]
+        acc["pulses_fp64"], acc["pulses_fp32"] = int(pe64.numel()), int(pe32.numel())
+        acc["mean_pe_rel"] = float((pe32.mean() / pe64.mean() - 1).item())
+        acc["clusters_fp64"], acc["clusters_fp32"] = r64.n_clusters, r32.n_clusters
+        if r64.n_digis == r32.n_digis:
+            acc["adc_mismatch_rate"] = float((r64.digis["adc"] != r32.digis["adc"]).double().mean().item())
+        k64 = r64.pulses["wf"] * 100000 + r64.pulses["seq"]
+        k32 = r32.pulses["wf"] * 100000 + r32.pulses["seq"]
+        if r64.n_waveforms == r32.n_waveforms:
+            a64, a32 = k64.cpu().numpy(), k32.cpu().numpy()
+            com, i64, i32 = np.intersect1d(a64, a32, return_indices=True)
+            t64 = r64.pulses["time"].cpu().numpy()[i64]
+            t32 = r32.pulses["time"].cpu().numpy()[i32]
+            acc["pulse_time_median_abs_ns"] = float(np.median(np.abs(t64 - t32))) if len(com) else None
+    except Exception as exc:  # accuracy report is informative only
+        acc["error"] = str(exc)[:200]
+
+    hbm, peak_kind = peaks()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        procs = 1
+        v, ev, busy, wall = cpu_reference(48, procs)
+        cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"{ev} events of the same workload through the oracle chain on 1 core ({busy:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32-mixed", "data": "synthetic",
+                "config": {"workload": f"{args.events} events/GPU, one 4x16 module of 450 cm counters, Poisson(40) "
+                                       f"steps/event ({nsteps_total} steps, SoA f32 resident), full chain "
+                                       f"steps->coincidences in batches of {args.batch} events",
+                           "precision": "fp32-mixed (FP64 LM solve and absolute times)",
+                           "l2": f"inputs larger than L2 ({step_bytes / 1e9:.2f} GB of steps)"},
+                "fp64_plain_events_per_s": fp64,
+                "fp32_over_fp64": (value / fp64) if fp64 else None,
+                "fp32_vs_fp64": acc,
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": int(launches),
+                "clocks": clk,
+                "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}
+                            for k, v in sorted(per_kernel.items(), key=lambda kv: -kv[1][1])[:12]},
+                "dominant_kernel": top[0],
+                "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

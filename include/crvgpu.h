@@ -158,9 +158,51 @@ typedef struct CrvPulses {
     uint8_t *failed, *zerondf, *pedfromdb;
 } CrvPulses;
 
-/* ---- version / status ---- */
+/* Coincidence-finder geometry and cuts (SectorGeom + FinderConfig cuts, flattened).  cuts: per cut set 10 values
+ * (pe_threshold, max_dt_adjacent, max_dt, min_slope, max_slope, max_slope_diff, coincidence_layers, min_cluster_pes,
+ * initial_max_distance, final_max_distance); sec_cut = -1 for sectors without cuts.  Types ascending, with their
+ * readout-end extremes p0/p1, half length, largest max_dt and instrumented sides. */
+typedef struct CrvFinderGeom {
+    const int32_t *bar_sector, *bar_layer, *bar_counter;
+    const double *bar_x, *bar_y, *bar_pos;
+    const int32_t *sec_type, *sec_cut, *sec_length_dir;
+    const double *sec_pos0, *sec_pos1;
+    const double *cuts;
+    const int32_t *type_id;
+    const double *type_p0, *type_p1, *type_half, *type_maxdt;
+    const int32_t *type_side0, *type_side1;
+    int32_t ntypes;
+    int32_t pad;
+} CrvFinderGeom;
+
+/* Coincidence clusters (event order, then sector type, then cluster order) and their member pulses. */
+typedef struct CrvClusters {
+    int64_t *event;
+    int32_t *type;
+    double *pe, *start, *end, *slope, *avgtime;
+    uint8_t *poscalc;
+    double *pos;                 /* [n][3] */
+    double *sidepe, *sidetime;   /* [n][2] */
+    int32_t *sidehits;           /* [n][2] */
+    int32_t *nlayers;
+} CrvClusters;
+
+typedef struct CrvMembers {
+    int64_t *cl;                 /* cluster row */
+    int32_t *idx;                /* pulse index inside its event */
+    int64_t *event;
+} CrvMembers;
+
+/* ---- version / status / accounting ---- */
 int crv_version(void);
 const char *crv_status_string(int32_t flags);
+/* Kernel launches issued by this library since load (every entry point's launches). */
+long long crv_launch_count(void);
+/* Profiling: crv_profile(1) clears the record and records CUDA events around every later launch (on its stream);
+ * crv_profile_read synchronises on the recorded events and returns their count, with up to cap kernel names (64 bytes
+ * each) and durations in ms.  crv_profile(0) stops recording. */
+void crv_profile(int on);
+int crv_profile_read(int cap, char *names, float *ms);
 
 /* Size in bytes of the caller-provided device workspace of crv_response for the given sizes (photon_cap: photons
  * the batch may produce; max_steps_per_event: largest event of the batch). */
@@ -233,6 +275,44 @@ int crv_pulses(const CrvParams *p, int64_t nw, const int64_t *off, const int32_t
                const int64_t *adc64, int32_t max_pulses, int64_t rec_cap, CrvPulses *out, int64_t out_cap,
                int64_t *n_out_dev, uint8_t *wf_near, void *workspace, int64_t workspace_bytes, void *stream,
                CrvStatus *status_dev);
+
+/*
+ * coinc.find_event over every event (chain.clusters' loop): pulses sorted by (event, waveform, sequence); event e owns
+ * pulse rows [ev_start[e], ev_start[e] + ev_count[e]) and reports ev_key[e].  Per pulse: bar, SiPM, sequence, time,
+ * PE; status: per-channel status (compensated-partner bits).
+ */
+int64_t crv_coincidences_workspace(int64_t nevents, int64_t npulses);
+int crv_coincidences(const CrvParams *p, const CrvFinderGeom *g, int64_t nevents, const int64_t *ev_start,
+                     const int32_t *ev_count, const int64_t *ev_key, int64_t npulses, const int32_t *bar,
+                     const int32_t *sipm, const int32_t *seq, const double *time, const double *pe,
+                     const int32_t *status, CrvClusters *out, int64_t cl_cap, int64_t *n_cl_dev, CrvMembers *mem,
+                     int64_t mem_cap, int64_t *n_mem_dev, void *workspace, int64_t workspace_bytes, void *stream,
+                     CrvStatus *status_dev);
+
+/*
+ * chain.reco_waveforms: digis sorted by (label, start) -> reco waveforms (consecutive digis of one channel whose TDCs
+ * continue, pulsefit.concat_waveforms' rule).  Waveform w: label, first sample row (digi row * samples_zs) of the digi
+ * ADC array, valid samples, start TDC, and the channel's pedestal / pulse area / pulse height / time offset.
+ */
+int64_t crv_reco_waveforms_workspace(int64_t ndigis);
+int crv_reco_waveforms(const CrvParams *p, const CrvChannels *ch, int64_t ndigis, const int64_t *label,
+                       const int64_t *starttdc, int64_t *w_label, int64_t *w_off, int32_t *w_n, int64_t *w_start,
+                       double *w_ped, double *w_area, double *w_height, double *w_toff, int64_t *n_w_dev,
+                       void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
+
+/*
+ * chain.clusters' pulse glue: pulses in (waveform, sequence) order of waveforms grouped by event -> finder input.
+ * Drops pulses of status-bit-1 channels (ignore_channels), adds the DB time offset x time_offset_scale
+ * (use_time_offset_db) and the optional per-waveform event_t0, and segments the kept pulses by event
+ * (ev_start / ev_count / ev_key; idx inside the event is the position in the segment).
+ */
+int64_t crv_pulse_hits_workspace(int64_t npulses);
+int crv_pulse_hits(const CrvParams *p, const int32_t *status, int64_t nw, const int64_t *w_label,
+                   const double *w_toff, const double *event_t0, int64_t npulses, const int64_t *p_wf,
+                   const int64_t *p_seq, const double *p_time, const double *p_pe, int64_t *ev_start,
+                   int32_t *ev_count, int64_t *ev_key, int32_t *bar, int32_t *sipm, int32_t *seq, double *time,
+                   double *pe, int64_t *n_ev_dev, int64_t *n_hit_dev, void *workspace, int64_t workspace_bytes,
+                   void *stream, CrvStatus *status_dev);
 
 #ifdef __cplusplus
 }

@@ -89,11 +89,30 @@ class CrvPulses(ctypes.Structure):
     _fields_ = [(k, c_p) for k in PULSE_INT + PULSE_FLOAT + PULSE_BOOL]
 
 
+class CrvFinderGeom(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("bar_sector", "bar_layer", "bar_counter", "bar_x", "bar_y", "bar_pos", "sec_type",
+                                   "sec_cut", "sec_length_dir", "sec_pos0", "sec_pos1", "cuts", "type_id", "type_p0",
+                                   "type_p1", "type_half", "type_maxdt", "type_side0", "type_side1")] + \
+        [("ntypes", c_i32), ("pad", c_i32)]
+
+
+class CrvClusters(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("event", "type", "pe", "start", "end", "slope", "avgtime", "poscalc", "pos",
+                                   "sidepe", "sidetime", "sidehits", "nlayers")]
+
+
+class CrvMembers(ctypes.Structure):
+    _fields_ = [("cl", c_p), ("idx", c_p), ("event", c_p)]
+
+
 P = ctypes.POINTER
 
 _SIGS = {
     "crv_version": (c_i32, []),
     "crv_status_string": (ctypes.c_char_p, [c_i32]),
+    "crv_launch_count": (ctypes.c_longlong, []),
+    "crv_profile": (None, [c_i32]),
+    "crv_profile_read": (c_i32, [c_i32, ctypes.c_char_p, P(ctypes.c_float)]),
     "crv_response_workspace": (c_i64, [P(CrvParams), c_i64, c_i64, c_i64, c_i32]),
     "crv_response": (c_i32, [P(CrvParams), P(CrvEvents), c_i64, P(CrvSteps), c_i64, c_i32, P(CrvBars), P(CrvChannels),
                              P(CrvPixels), c_i64, P(CrvCharges), c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p, c_i64,
@@ -109,6 +128,15 @@ _SIGS = {
     "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
     "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, c_i64, P(CrvPulses),
                            c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_coincidences_workspace": (c_i64, [c_i64, c_i64]),
+    "crv_coincidences": (c_i32, [P(CrvParams), P(CrvFinderGeom), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_p, c_p,
+                                 c_p, P(CrvClusters), c_i64, c_p, P(CrvMembers), c_i64, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_reco_waveforms_workspace": (c_i64, [c_i64]),
+    "crv_reco_waveforms": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p,
+                                   c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_pulse_hits_workspace": (c_i64, [c_i64]),
+    "crv_pulse_hits": (c_i32, [P(CrvParams), c_p, c_i64, c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p,
+                               c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_sipm": (c_i32, [P(CrvParams), P(CrvPixels), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, P(CrvCharges),
                          c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
 }
@@ -176,3 +204,21 @@ class DeviceStatus:
         a = self.t.cpu().numpy()
         flags = int(np.int64(a[0]) & 0xFFFFFFFF)
         return flags, a[1:17].copy()
+
+
+def launch_count():
+    return int(load().crv_launch_count())
+
+
+def profile(on):
+    load().crv_profile(1 if on else 0)
+
+
+def profile_read(cap=100000):
+    """[(kernel name, ms)] of the launches recorded since profile(True) (synchronises on their events)."""
+    L = load()
+    names = ctypes.create_string_buffer(64 * cap)
+    ms = (ctypes.c_float * cap)()
+    n = L.crv_profile_read(cap, names, ms)
+    raw = names.raw
+    return [(raw[64 * i:64 * i + 64].split(b"\0", 1)[0].decode(), float(ms[i])) for i in range(min(n, cap))]

@@ -1,5 +1,205 @@
-"""Chain glue with the reference's entry points (crv/crvfastsim/chain.py): charges, digis, reco_waveforms, clusters."""
+"""Chain glue with the reference's entry points (crv/crvfastsim/chain.py): charges (:151), digis (:234),
+reco_waveforms (:273), clusters (:296); plus ChainEngine, the device-resident chain steps -> coincidence clusters
+used by the benchmark (every stage a CUDA launch sequence behind the C ABI; host syncs only to read sizes).
+
+Event key = (subrun << 20) | event; SiPM label = event key * CHAN_MULT + channel (CHAN_MULT 32768).
+"""
 from __future__ import annotations
 
-from .config import CHAN_MULT, PERIOD, ChainConfig, Conditions  # noqa: F401
-from .response import charges  # noqa: F401
+import ctypes
+import time as _time
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from . import _capi
+from .coinc import CoincEngine, FinderTables, rows_of  # noqa: F401
+from .config import CHAN_MULT, PERIOD, ChainConfig, Conditions, FinderConfig, RecoConfig, WaveformConfig  # noqa: F401
+from .params import make_params, validate_sipm, validate_window
+from .pulsefit import PulseEngine, filter_channels, concat_waveforms
+from .pulsefit import reconstruct_full as _reconstruct_full
+from .response import (DeviceSteps, DeviceTables, ResponseEngine, _stream, _torch, charges, raise_status,  # noqa: F401
+                       seed_of, upload_steps)
+from .waveform import DigiEngine, digis, single_pe_template  # noqa: F401
+
+
+def reco_waveforms(D, cond):
+    """Digis -> reco waveform rows with calibration, sorted by (event, channel, start) (pulsefit.concat_waveforms'
+    grouping; host glue as in the reference)."""
+    ev, ch = D["chan"] // CHAN_MULT, D["chan"] % CHAN_MULT
+    o = np.lexsort((D["starttdc"], ch, ev))
+    ev, ch, st = ev[o], ch[o], D["starttdc"][o]
+    adc = np.asarray(D["adc"])[o]
+    lens = np.full(len(o), adc.shape[1] if adc.ndim == 2 else 12, np.int64)
+    gid, mat, n, start, first = concat_waveforms(ev, ch // 4, ch % 4, st, adc.ravel(), lens)
+    c0 = ch[first]
+    return {"ev": ev[first], "bar": c0 // 4, "sipm": c0 % 4, "chan": c0, "adc": mat, "n": n, "start": start,
+            "ped": cond.pedestal[c0], "area": cond.pulsearea[c0], "height": cond.pulseheight[c0],
+            "toff": cond.timeoffset[c0]}
+
+
+def clusters(W, cond, geom, counters_cfg, cfg: ChainConfig, timers=None, detail=False, rng=None, caps=None):
+    """Reco waveforms -> pulses (GPU) -> coincidence clusters (GPU).  counters_cfg: the SectorGeom of the geometry (or
+    None to build it from geom).  Returns ([dict of cl_* arrays (+ members with detail)], timers)."""
+    from . import coinc as CO
+    from .geometry import sector_geom
+    timers = timers if timers is not None else {}
+    if caps is not None:
+        raise ValueError("capacities are managed by the engine")
+    if getattr(cfg, "background", None) is not None:
+        raise NotImplementedError("background pulse overlays are not part of the GPU chain")
+    if "toff" not in W:
+        W = {**W, "toff": cond.timeoffset[W["bar"] * 4 + W["sipm"]]}
+    G = counters_cfg if counters_cfg is not None and hasattr(counters_cfg, "sector_type") else sector_geom(geom)
+    fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
+    rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
+    t0 = _time.perf_counter()
+    P = _reconstruct_full(W["adc"], W["n"], W["start"], W["ped"], W["area"], W["height"], rcfg,
+                          precision=cfg.precision)
+    P = filter_channels(P, W["bar"] * 4 + W["sipm"], cond.status, rcfg)
+    if rcfg.use_time_offset_db:
+        P["time"] = P["time"] + W["toff"][P["wf"]] * rcfg.time_offset_scale
+    if "event_t0" in W:
+        P["time"] = P["time"] + W["event_t0"][P["wf"]]
+    timers["pulses_s"] = timers.get("pulses_s", 0.0) + _time.perf_counter() - t0
+    wf = P["wf"]
+    ev = W["ev"][wf]
+    o = np.lexsort((P["seq"], wf, ev))
+    ev, wf = ev[o], wf[o]
+    idx = np.arange(len(ev)) - np.searchsorted(ev, ev)
+    bar, sipm, time, pe, seq = W["bar"][wf], W["sipm"][wf], P["time"][o], P["pe"][o], P["seq"][o]
+    t0 = _time.perf_counter()
+    cl, mem = CO.find_events(ev, idx, bar, sipm, time, pe, seq, G, cond.status, fcfg)
+    timers["coinc_s"] = timers.get("coinc_s", 0.0) + _time.perf_counter() - t0
+    timers["pulses"] = timers.get("pulses", 0) + len(ev)
+    out = {"cl_event": cl["event"], "cl_type": cl["type"].astype(np.int64), "cl_pe": cl["pe"], "cl_start": cl["start"],
+           "cl_end": cl["end"], "cl_slope": cl["slope"], "cl_avgtime": cl["avgtime"],
+           "cl_poscalc": cl["poscalc"].astype(bool)}
+    if detail:
+        out.update({"mem_cl": mem["cl"], "mem_idx": mem["idx"].astype(np.int64), "mem_event": mem["event"],
+                    "cl_pos": cl["pos"], "pulses": dict(ev=ev, idx=idx, bar=bar, sipm=sipm, seq=seq, pe=pe,
+                                                          time=time)})
+    return [out], timers
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# device-resident chain
+
+class _Ws:
+    """Grow-only device workspace."""
+
+    def __init__(self, device):
+        self.device, self.t = device, None
+
+    def get(self, nbytes):
+        torch = _torch()
+        if self.t is None or self.t.numel() < nbytes:
+            self.t = torch.empty(int(nbytes * 1.1) + 1024, dtype=torch.uint8, device=self.device)
+        return self.t
+
+
+@dataclass
+class ChainResult:
+    n_events: int
+    n_charges: int
+    n_digis: int
+    n_waveforms: int
+    n_pulses: int
+    n_hits: int
+    n_clusters: int
+    n_members: int
+    clusters: dict
+    members: dict
+    charges: object = None
+    digis: dict = None
+    waveforms: dict = None
+    pulses: dict = None
+    hits: dict = None
+
+
+class ChainEngine:
+    """steps (DeviceSteps) -> charges -> digis -> reco waveforms -> pulses -> coincidence clusters, on the device."""
+
+    def __init__(self, geom, cond, cfg: ChainConfig, G=None, device="cuda", pmap=None):
+        from .coinc import FinderTables
+        from .geometry import sector_geom
+        torch = _torch()
+        validate_sipm(cfg.sipm)
+        validate_window(cfg.window)
+        self.cfg = cfg
+        self.device = device
+        self.wcfg = cfg.waveform if cfg.waveform is not None else WaveformConfig()
+        self.rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
+        self.fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
+        self.ccfg = replace(cfg, waveform=self.wcfg, pulse_reco=self.rcfg, finder=self.fcfg)
+        self.tabs = DeviceTables(geom, cond, self.ccfg, device, pmap)
+        self.fin = FinderTables(G if G is not None else sector_geom(geom), self.fcfg, device)
+        tm = single_pe_template(self.wcfg)
+        self.tmpl = torch.from_numpy(tm).to(device)
+        self.tlen = len(tm)
+        self.resp, self.dig, self.pul, self.coi = (ResponseEngine(device), DigiEngine(device), PulseEngine(device),
+                                                   CoincEngine(device))
+        self.ws_w, self.ws_h = _Ws(device), _Ws(device)
+        self.status = _capi.DeviceStatus(device)
+
+    def params(self, seed):
+        P = make_params(self.ccfg, seed, template_len=self.tlen, uniform_map=self.tabs.uniform_map)
+        P.period = self.wcfg.period
+        return P
+
+    def run(self, ds: DeviceSteps, seed, keep=False):
+        torch = _torch()
+        L = _capi.load()
+        dev = self.device
+        P = self.params(seed)
+        R = self.resp.run(P, ds, self.tabs, diagnostics=False)
+        evk = ((ds.ev_subrun.to(torch.int64) & 0xFFFFFFFF) << 20) | (ds.ev_event.to(torch.int64) & 0xFFFFFFFF)
+        D = self.dig.run(P, self.tabs, R.label, R.time, R.charge, self.tmpl, evk, ds.ev_run)
+        nd = int(D["chan"].numel())
+        # reco waveforms
+        W = {k: torch.empty(max(nd, 1), dtype=dt, device=dev) for k, dt in
+             (("label", torch.int64), ("off", torch.int64), ("n", torch.int32), ("start", torch.int64),
+              ("ped", torch.float64), ("area", torch.float64), ("height", torch.float64), ("toff", torch.float64))}
+        nw_t = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.status.reset()
+        ws = self.ws_w.get(L.crv_reco_waveforms_workspace(nd))
+        _capi.check(L.crv_reco_waveforms(ctypes.byref(P), ctypes.byref(self.tabs.c_channels()), nd,
+                                         _capi.ptr(D["chan"]), _capi.ptr(D["starttdc"]),
+                                         *[_capi.ptr(W[k]) for k in ("label", "off", "n", "start", "ped", "area",
+                                                                      "height", "toff")],
+                                         _capi.ptr(nw_t), _capi.ptr(ws), ws.numel(), _stream(), self.status.ptr),
+                    "crv_reco_waveforms")
+        nw = int(nw_t.item())
+        W = {k: v[:nw] for k, v in W.items()}
+        adc16 = D["adc"].reshape(-1)
+        Pu = self.pul.run(P, W["off"], W["n"], W["start"], W["ped"], W["area"], W["height"], adc16=adc16,
+                          max_pulses=1 << 30)
+        npu = int(Pu["wf"].numel())
+        # finder input
+        H = dict(ev_start=torch.empty(max(npu, 1), dtype=torch.int64, device=dev),
+                 ev_count=torch.empty(max(npu, 1), dtype=torch.int32, device=dev),
+                 ev_key=torch.empty(max(npu, 1), dtype=torch.int64, device=dev),
+                 bar=torch.empty(max(npu, 1), dtype=torch.int32, device=dev),
+                 sipm=torch.empty(max(npu, 1), dtype=torch.int32, device=dev),
+                 seq=torch.empty(max(npu, 1), dtype=torch.int32, device=dev),
+                 time=torch.empty(max(npu, 1), dtype=torch.float64, device=dev),
+                 pe=torch.empty(max(npu, 1), dtype=torch.float64, device=dev))
+        nn = torch.zeros(2, dtype=torch.int64, device=dev)
+        ws = self.ws_h.get(L.crv_pulse_hits_workspace(npu))
+        _capi.check(L.crv_pulse_hits(ctypes.byref(P), _capi.ptr(self.tabs.status), nw, _capi.ptr(W["label"]),
+                                     _capi.ptr(W["toff"]), None, npu, _capi.ptr(Pu["wf"]), _capi.ptr(Pu["seq"]),
+                                     _capi.ptr(Pu["time"]), _capi.ptr(Pu["pe"]),
+                                     *[_capi.ptr(H[k]) for k in ("ev_start", "ev_count", "ev_key", "bar", "sipm",
+                                                                  "seq", "time", "pe")],
+                                     _capi.ptr(nn[0:1]), _capi.ptr(nn[1:2]), _capi.ptr(ws), ws.numel(), _stream(),
+                                     self.status.ptr), "crv_pulse_hits")
+        flags, need = self.status.read()
+        raise_status(flags, need, "chain glue")
+        nev, nh = (int(v) for v in nn.cpu().numpy())
+        H = {k: (v[:nev] if k.startswith("ev_") else v[:nh]) for k, v in H.items()}
+        cl, mem = self.coi.run(P, self.fin, H["ev_start"], H["ev_count"], H["ev_key"], H["bar"], H["sipm"],
+                               H["seq"], H["time"], H["pe"], self.tabs.status)
+        res = ChainResult(ds.nevents, R.n, nd, nw, npu, nh, int(cl["pe"].numel()), int(mem["cl"].numel()), cl, mem)
+        if keep:
+            res.charges, res.digis, res.waveforms, res.pulses, res.hits = R, D, W, Pu, H
+        return res

@@ -1,0 +1,579 @@
+// Coincidence finder: reco pulses of each event -> coincidence clusters (crv/crvfastsim/reco/coinc.py:112-392,
+// crv/crvfastsim/reco/coinc_cpu.py:11-51; per-event loop of crv/crvfastsim/chain.py:325-362).
+//
+// Per event and sector type (ascending): hits = first pulses (secondary pulses dropped) with the fibre-length time
+// correction to the type's outermost readout end and PE doubled when the same-end partner SiPM has a compensated
+// status bit; per readout side: filterHits (same + one adjacent counter in the layer, |dt| <= max_dt_adjacent, PE sum
+// >= threshold, sums in list order), greedy single-linkage clustering in list order (|dx| <= max(maxd), |dt| < max_dt),
+// the 2/3/4-layer combination check (time window, slope window and pairwise slope differences; passing combinations
+// widen maxd to the gaps to their x-neighbours); then clustering of the coincidence hits of both sides (opposite sides
+// get + 2 half-length / v), attachment of filtered first pulses on missing opposite counter ends, PE-weighted
+// properties.
+//
+// GPU mapping: one warp per event; hits and work lists in shared memory; the O(H^2) filter, the link tests and the
+// combination enumeration are spread over the lanes; list-order decisions (greedy joins, attachment order) are taken
+// in order with ballots.  All arithmetic is FP64.
+#pragma once
+#include "crv_device.cuh"
+
+namespace crv {
+
+struct CoincGeom {
+  const int32_t *bar_sector, *bar_layer, *bar_counter;
+  const double *bar_x, *bar_y, *bar_pos;           // pos: [nbars][3]
+  const int32_t *sec_type, *sec_cut, *sec_length_dir;
+  const double *sec_pos0, *sec_pos1;
+  const double* cuts;                              // [ncuts][10]
+  const int32_t* type_id;                          // [ntypes], ascending
+  const double *type_p0, *type_p1, *type_half, *type_maxdt;
+  const int32_t *type_side0, *type_side1;
+  int32_t ntypes;
+  int32_t pad;
+};
+
+struct CoincIn {
+  long long nev;
+  const long long* ev_start;                       // first pulse row of event e
+  const int32_t* ev_count;                         // pulses of event e
+  const int32_t *bar, *sipm, *seq;
+  const double *time, *pe;
+  const int32_t* status;                           // per channel
+};
+
+struct ClusterRec {
+  double pe, start, end, slope, avgtime, pos[3], sidepe[2], sidetime[2];
+  int32_t type, sidehits[2], nlayers, poscalc, mem_begin, mem_count, pad;
+};
+
+struct CoincOut {
+  ClusterRec* rec;                                 // slots: event e uses rows [ev_start[e], ev_start[e] + ev_count[e])
+  int32_t* mem_idx;                                // member slots, same rows
+  int32_t* ncl;                                    // clusters per event
+  int32_t* nmem;                                   // members per event
+};
+
+enum { CUT_PE = 0, CUT_DTADJ, CUT_DT, CUT_SMIN, CUT_SMAX, CUT_SDIFF, CUT_LAYERS, CUT_MINPE, CUT_D0, CUT_D1 };
+
+struct CoincShared {
+  // hits of the event (all types)
+  int32_t *idx, *bar, *layer, *counter, *side, *sipm, *seq, *sector, *cut, *type;
+  double *x, *y, *t, *pe, *maxd;
+  // work lists (indices into hits or into the coincidence list)
+  int32_t *list, *pool, *clus, *filt, *coinc, *cl_of, *order, *tmp;
+  double *cmaxd;                                   // maxd of the coincidence copies
+  unsigned long long* wid;                         // widened maxd (non-negative doubles as ordered integers)
+  uint8_t* kept;
+};
+
+__host__ __device__ inline size_t coinc_smem_per_warp(int hcap) {
+  return (size_t(hcap) * (10 * 4 + 5 * 8 + 8 * 4 + 8 + 8 + 1) + 64 + 15) & ~size_t(15);
+}
+
+__device__ inline CoincShared coinc_carve(char* b, int hcap) {
+  CoincShared S;
+  double* d = reinterpret_cast<double*>(b);
+  S.x = d; S.y = d + hcap; S.t = d + 2 * hcap; S.pe = d + 3 * hcap; S.maxd = d + 4 * hcap; S.cmaxd = d + 5 * hcap;
+  S.wid = reinterpret_cast<unsigned long long*>(d + 6 * hcap);
+  int32_t* q = reinterpret_cast<int32_t*>(d + 7 * hcap);
+  int32_t** f[] = {&S.idx, &S.bar, &S.layer, &S.counter, &S.side, &S.sipm, &S.seq, &S.sector, &S.cut, &S.type,
+                   &S.list, &S.pool, &S.clus, &S.filt, &S.coinc, &S.cl_of, &S.order, &S.tmp};
+  for (int k = 0; k < 18; ++k) *f[k] = q + k * hcap;
+  S.kept = reinterpret_cast<uint8_t*>(q + 18 * hcap);
+  return S;
+}
+
+__device__ __forceinline__ double cutv(const CoincGeom& G, int c, int k) { return G.cuts[c * 10 + k]; }
+
+// link test of hit/copy a and b (maxd taken from ma, mb)
+__device__ __forceinline__ bool linked(const CoincShared& S, int a, int b, double ma, double mb, double max_dt,
+                                       bool opposite, double dt_opp) {
+  double md = ma > mb ? ma : mb;
+  double mt = max_dt + ((opposite && S.side[a] != S.side[b]) ? dt_opp : 0.0);
+  return fabs(S.x[a] - S.x[b]) <= md && fabs(S.t[a] - S.t[b]) < mt;
+}
+
+// Greedy clustering of items 0..n-1 in list order: item k is hit ids[k] with maxd mds[k].  Writes the cluster of
+// every item into cl_of[k], the items grouped by cluster in join order into out[], and cluster starts into
+// clstart[0..ncl].  Returns the number of clusters.  S.pool is scratch.
+__device__ int greedy(const CoincShared& S, const int32_t* ids, const double* mds, int n, double max_dt, bool opposite,
+                      double dt_opp, int32_t* cl_of, int32_t* out, int32_t* clstart) {
+  for (int i = lane_id(); i < n; i += 32) S.pool[i] = i;
+  __syncwarp();
+  int npool = n, nout = 0, ncl = 0;
+  while (npool > 0) {
+    int first = S.pool[0];
+    __syncwarp();
+    if (lane_id() == 0) {
+      for (int i = 1; i < npool; ++i) S.pool[i - 1] = S.pool[i];
+      out[nout] = first;
+      cl_of[first] = ncl;
+      clstart[ncl] = nout;
+    }
+    __syncwarp();
+    --npool;
+    int c0 = nout;
+    ++nout;
+    bool grew = true;
+    while (grew) {
+      grew = false;
+      int i = 0;
+      while (i < npool) {
+        int cand = S.pool[i];
+        int hc = ids[cand];
+        double mc = mds[cand];
+        bool link = false;
+        for (int m = c0 + lane_id(); m < nout; m += 32) {
+          int it = out[m];
+          link = link || linked(S, hc, ids[it], mc, mds[it], max_dt, opposite, dt_opp);
+        }
+        bool any = __any_sync(0xffffffffu, link);
+        __syncwarp();
+        if (any) {
+          if (lane_id() == 0) {
+            out[nout] = cand;
+            cl_of[cand] = ncl;
+            for (int k = i + 1; k < npool; ++k) S.pool[k - 1] = S.pool[k];
+          }
+          __syncwarp();
+          ++nout;
+          --npool;
+          grew = true;
+        } else {
+          ++i;
+        }
+      }
+    }
+    ++ncl;
+  }
+  if (lane_id() == 0) clstart[ncl] = nout;
+  __syncwarp();
+  return ncl;
+}
+
+// combination check of one cluster (members: hit ids in mem[0..m)); kept hits get kept=1 and wid widened.
+__device__ void check_coincidence(const CoincGeom& G, const CoincShared& S, const int32_t* mem, int m,
+                                  int big_threshold) {
+  int cnt[4] = {0, 0, 0, 0};
+  int nmin = 1 << 30, nmax = -1;
+  for (int k = 0; k < m; ++k) {
+    int h = mem[k];
+    cnt[S.layer[h]]++;
+    int cl = int(cutv(G, S.cut[h], CUT_LAYERS));
+    nmin = cl < nmin ? cl : nmin;
+    nmax = cl > nmax ? cl : nmax;
+  }
+  for (int k = lane_id(); k < m; k += 32) {
+    int h = mem[k];
+    S.wid[h] = (unsigned long long)__double_as_longlong(cutv(G, S.cut[h], CUT_D1));
+    S.kept[h] = 0;
+  }
+  __syncwarp();
+  int nonempty = (cnt[0] > 0) + (cnt[1] > 0) + (cnt[2] > 0) + (cnt[3] > 0);
+  if (m > big_threshold && nonempty >= nmin) {
+    for (int k = lane_id(); k < m; k += 32) S.kept[mem[k]] = 1;
+    __syncwarp();
+    return;
+  }
+  // bucket lists: offsets
+  int off[5] = {0, cnt[0], cnt[0] + cnt[1], cnt[0] + cnt[1] + cnt[2], m};
+  if (lane_id() == 0) {
+    int fill[4] = {off[0], off[1], off[2], off[3]};
+    for (int k = 0; k < m; ++k) { int h = mem[k]; S.tmp[fill[S.layer[h]]++] = h; }
+  }
+  __syncwarp();
+  for (int nl = 2; nl <= 4; ++nl) {
+    bool need = (nl == 2 && nmin == 2) || (nl == 3 && nmin <= 3 && 3 <= nmax) || (nl == 4 && nmax == 4);
+    if (!need) continue;
+    for (int mask = 0; mask < 16; ++mask) {
+      if (__popc(mask) != nl) continue;
+      int ls[4], sz[4], k = 0;
+      long long total = 1;
+      for (int l = 0; l < 4; ++l)
+        if (mask & (1 << l)) { ls[k] = l; sz[k] = cnt[l]; total *= cnt[l]; ++k; }
+      if (total == 0) continue;
+      for (long long c = lane_id(); c < total; c += 32) {
+        int hs[4];
+        long long r = c;
+        for (int q = nl - 1; q >= 0; --q) {         // mixed radix, first layer slowest
+          hs[q] = S.tmp[off[ls[q]] + int(r % sz[q])];
+          r /= sz[q];
+        }
+        bool skip = true;
+        for (int q = 0; q < nl; ++q) skip = skip && (cutv(G, S.cut[hs[q]], CUT_LAYERS) > nl);
+        if (skip) continue;
+        double mdt = -1e300, lo = 1e300, hi = -1e300, msd = -1e300, tmin = 1e300, tmax = -1e300;
+        for (int q = 0; q < nl; ++q) {
+          int c_ = S.cut[hs[q]];
+          mdt = fmax(mdt, cutv(G, c_, CUT_DT));
+          lo = fmin(lo, cutv(G, c_, CUT_SMIN));
+          hi = fmax(hi, cutv(G, c_, CUT_SMAX));
+          msd = fmax(msd, cutv(G, c_, CUT_SDIFF));
+          tmin = fmin(tmin, S.t[hs[q]]);
+          tmax = fmax(tmax, S.t[hs[q]]);
+        }
+        if (tmax - tmin > mdt) continue;
+        double sl[3];
+        bool ok = true;
+        for (int q = 0; q + 1 < nl; ++q) {
+          double s = (S.x[hs[q + 1]] - S.x[hs[q]]) / (S.y[hs[q + 1]] - S.y[hs[q]]);
+          if (s < lo || s > hi) { ok = false; break; }
+          sl[q] = s;
+        }
+        if (!ok) continue;
+        if (nl > 2 && fabs(sl[0] - sl[1]) > msd) continue;
+        if (nl > 3 && (fabs(sl[0] - sl[2]) > msd || fabs(sl[1] - sl[2]) > msd)) continue;
+        // widen: x-sorted neighbours (stable)
+        int srt[4];
+        for (int q = 0; q < nl; ++q) srt[q] = hs[q];
+        for (int a = 1; a < nl; ++a) {
+          int v = srt[a];
+          int b = a - 1;
+          while (b >= 0 && S.x[srt[b]] > S.x[v]) { srt[b + 1] = srt[b]; --b; }
+          srt[b + 1] = v;
+        }
+        for (int q = 0; q < nl; ++q) {
+          double w = -1e300;
+          if (q > 0) w = fmax(w, S.x[srt[q]] - S.x[srt[q - 1]]);
+          if (q + 1 < nl) w = fmax(w, S.x[srt[q + 1]] - S.x[srt[q]]);
+          // gaps are >= 0; maxd starts at final_max_distance: order non-negative doubles as integers
+          if (w >= 0.0) atomicMax(&S.wid[srt[q]], (unsigned long long)__double_as_longlong(w));
+          S.kept[srt[q]] = 1;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+}
+
+// scratch of the per-type lists beyond CoincShared (carved after it)
+struct CoincWork {
+  int32_t *clstart, *ccl, *cstart, *att_c, *att_cl, *att_bar, *att_sipm;
+  double *cmd, *att_dt, *fmd;
+};
+
+__host__ __device__ inline size_t coinc_work_per_warp(int hcap) {
+  return (size_t(hcap + 1) * 4 * 3 + size_t(hcap) * 4 * 4 + size_t(hcap) * 8 * 3 + 64 + 15) & ~size_t(15);
+}
+
+__device__ inline CoincWork work_carve(char* b, int hcap) {
+  CoincWork W;
+  double* d = reinterpret_cast<double*>(b);
+  W.cmd = d; W.att_dt = d + hcap; W.fmd = d + 2 * hcap;
+  int32_t* q = reinterpret_cast<int32_t*>(d + 3 * hcap);
+  W.clstart = q; W.ccl = q + (hcap + 1); W.cstart = q + 2 * (hcap + 1);
+  W.att_c = q + 3 * (hcap + 1); W.att_cl = W.att_c + hcap; W.att_bar = W.att_cl + hcap; W.att_sipm = W.att_bar + hcap;
+  return W;
+}
+
+// properties of one cluster (members: hit ids mem[0..m)); returns false when the cluster is below min_cluster_pes
+__device__ bool cluster_props(const CoincGeom& G, const CoincShared& S, const CrvParams& p, int ti, int type,
+                              const int32_t* mem, int m, ClusterRec& R) {
+  double tot = 0.0, minpe = 1e300;
+  for (int k = 0; k < m; ++k) {
+    tot += S.pe[mem[k]];
+    minpe = fmin(minpe, cutv(G, S.cut[mem[k]], CUT_MINPE));
+  }
+  if (tot < minpe) return false;
+  double pos[3] = {0, 0, 0}, sx = 0, sy = 0, sxy = 0, syy = 0;
+  for (int c = 0; c < 3; ++c) {
+    double a = 0.0;
+    for (int k = 0; k < m; ++k) a += G.bar_pos[S.bar[mem[k]] * 3 + c] * S.pe[mem[k]];
+    pos[c] = a / tot;
+  }
+  for (int k = 0; k < m; ++k) {
+    int h = mem[k];
+    double pe = S.pe[h], x = S.x[h], y = S.y[h];
+    sxy += pe * x * y; sx += pe * x; sy += pe * y; syy += pe * y * y;
+  }
+  double slope = (tot * sxy - sx * sy) / (tot * syy - sy * sy);
+  int nh[2] = {0, 0};
+  double spe[2] = {0, 0}, stp[2] = {0, 0}, st[2], tmin[2] = {1e300, 1e300}, tmax[2] = {-1e300, -1e300};
+  double t0 = 1e300, t1 = -1e300;
+  unsigned layers = 0;
+  for (int k = 0; k < m; ++k) {
+    int h = mem[k];
+    double t = S.t[h];
+    t0 = fmin(t0, t); t1 = fmax(t1, t);
+    layers |= 1u << S.layer[h];
+    if (S.pe[h] > 0.0) {
+      int sd = S.side[h];
+      nh[sd] += 1; spe[sd] += S.pe[h]; stp[sd] += t * S.pe[h];
+      tmin[sd] = fmin(tmin[sd], t); tmax[sd] = fmax(tmax[sd], t);
+    }
+  }
+  for (int sd = 0; sd < 2; ++sd) {
+    st[sd] = spe[sd] > 0.0 ? stp[sd] / spe[sd] : 0.0;
+    if (!nh[sd]) { tmin[sd] = 0.0; tmax[sd] = 0.0; }
+  }
+  int ld = G.sec_length_dir[S.sector[mem[0]]];
+  double v = p.fiber_signal_speed, P0 = G.type_p0[ti], P1 = G.type_p1[ti];
+  bool calc = false;
+  double avg;
+  if (nh[0] && nh[1]) {
+    double org = 0.5 * (v * (st[0] - st[1]) + (P0 + P1));
+    if (P0 < org && org < P1 && tmax[0] - tmin[0] < p.max_time_interval && tmax[1] - tmin[1] < p.max_time_interval) {
+      calc = true;
+      pos[ld] = org;
+      avg = st[0] - (org - P0) / v;
+    } else {
+      org = pos[ld];
+      avg = 0.5 * ((st[0] - (org - P0) / v) + (st[1] - (P1 - org) / v));
+    }
+  } else {
+    double org = pos[ld];
+    avg = nh[0] ? (st[0] - (org - P0) / v) : (st[1] - (P1 - org) / v);
+  }
+  R.pe = tot; R.start = t0; R.end = t1; R.slope = slope; R.avgtime = avg - p.time_offset;
+  for (int c = 0; c < 3; ++c) R.pos[c] = pos[c];
+  R.sidepe[0] = spe[0]; R.sidepe[1] = spe[1]; R.sidetime[0] = st[0]; R.sidetime[1] = st[1];
+  R.type = type; R.sidehits[0] = nh[0]; R.sidehits[1] = nh[1]; R.nlayers = __popc(layers); R.poscalc = calc;
+  return true;
+}
+
+constexpr int CO_WARPS_MAX = 8;
+
+// second_pass == 0: events with at most hcap hits (others deferred); second_pass == 1: deferred events only.
+__global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincGeom G, CoincIn I, int hcap,
+                                                           int second_pass, CoincOut O, int32_t* __restrict__ deferred,
+                                                           Status* status) {
+  extern __shared__ __align__(16) char smem[];
+  size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
+  char* wb = smem + size_t(warp_in_block()) * per;
+  CoincShared S = coinc_carve(wb, hcap);
+  CoincWork W = work_carve(wb + coinc_smem_per_warp(hcap), hcap);
+  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); e < I.nev; e += warps) {
+    if (second_pass && !deferred[e]) continue;
+    long long r0 = I.ev_start[e];
+    int np_ = I.ev_count[e];
+    // hits in pulse order
+    int H = 0;
+    for (int base = 0; base < np_; base += 32) {
+      int i = base + lane_id();
+      bool ok = false;
+      int bar = 0, sec = 0, cut = -1, ti = -1;
+      if (i < np_) {
+        long long r = r0 + i;
+        bar = I.bar[r];
+        sec = G.bar_sector[bar];
+        cut = G.sec_cut[sec];
+        ok = cut >= 0 && !(p.ignore_secondary && I.seq[r] > 0);
+        if (ok) {
+          int ty = G.sec_type[sec];
+          for (int k = 0; k < G.ntypes; ++k) if (G.type_id[k] == ty) ti = k;
+          ok = ti >= 0;
+        }
+      }
+      unsigned m = __ballot_sync(0xffffffffu, ok);
+      int pos = H + __popc(m & ((1u << lane_id()) - 1u));
+      if (ok && pos < hcap) {
+        long long r = r0 + i;
+        int sipm = I.sipm[r];
+        int side = sipm % 2;
+        double t = I.time[r];
+        t += (side == 0 ? (G.sec_pos0[sec] - G.type_p0[ti]) : (G.type_p1[ti] - G.sec_pos1[sec])) / p.fiber_signal_speed;
+        double pe = I.pe[r];
+        int partner = bar * 4 + sipm + (sipm < 2 ? 2 : -2);
+        if (I.status[partner] & p.compensate_mask) pe *= 2.0;
+        S.idx[pos] = i; S.bar[pos] = bar; S.layer[pos] = G.bar_layer[bar]; S.counter[pos] = G.bar_counter[bar];
+        S.side[pos] = side; S.sipm[pos] = sipm; S.seq[pos] = I.seq[r]; S.sector[pos] = sec; S.cut[pos] = cut;
+        S.type[pos] = ti; S.x[pos] = G.bar_x[bar]; S.y[pos] = G.bar_y[bar]; S.t[pos] = t; S.pe[pos] = pe;
+        S.maxd[pos] = cutv(G, cut, CUT_D0);
+      }
+      H += __popc(m);
+    }
+    if (H > hcap) {
+      if (lane_id() == 0) {
+        if (second_pass) {
+          set_flag(status, CRV_ST_CAPACITY);
+          need_at_least(status, CRV_NEED_HITS_PER_EVENT, H);
+          O.ncl[e] = 0; O.nmem[e] = 0;
+        } else {
+          deferred[e] = 1;
+        }
+      }
+      continue;
+    }
+    __syncwarp();
+    int ncl_ev = 0, nmem_ev = 0;
+    for (int ti = 0; ti < G.ntypes; ++ti) {
+      // hits of this type, in order
+      int nt = 0;
+      for (int base = 0; base < H; base += 32) {
+        int h = base + lane_id();
+        bool in = h < H && S.type[h] == ti;
+        unsigned m = __ballot_sync(0xffffffffu, in);
+        if (in) S.list[nt + __popc(m & ((1u << lane_id()) - 1u))] = h;
+        nt += __popc(m);
+      }
+      __syncwarp();
+      if (nt == 0) continue;
+      int nf = 0, nc = 0;
+      for (int side = 0; side < 2; ++side) {
+        // filterHits over the side's hits (list order sums)
+        int f0 = nf;
+        for (int base = 0; base < nt; base += 32) {
+          int k = base + lane_id();
+          bool pass = false;
+          if (k < nt) {
+            int h = S.list[k];
+            if (S.side[h] == side) {
+              double same = 0.0, a1 = 0.0, a2 = 0.0;
+              double dadj = cutv(G, S.cut[h], CUT_DTADJ);
+              for (int q = 0; q < nt; ++q) {
+                int a = S.list[q];
+                if (S.side[a] != side || S.layer[a] != S.layer[h] || fabs(S.t[a] - S.t[h]) > dadj) continue;
+                int d = S.counter[a] - S.counter[h];
+                same += d == 0 ? S.pe[a] : 0.0;
+                a1 += d == -1 ? S.pe[a] : 0.0;
+                a2 += d == 1 ? S.pe[a] : 0.0;
+              }
+              double thr = cutv(G, S.cut[h], CUT_PE);
+              pass = (same + a1 >= thr) || (same + a2 >= thr);
+            }
+          }
+          unsigned m = __ballot_sync(0xffffffffu, pass);
+          if (pass) S.filt[nf + __popc(m & ((1u << lane_id()) - 1u))] = S.list[k];
+          nf += __popc(m);
+        }
+        __syncwarp();
+        int nfs = nf - f0;
+        if (nfs == 0) continue;
+        for (int k = lane_id(); k < nfs; k += 32) W.fmd[k] = S.maxd[S.filt[f0 + k]];
+        __syncwarp();
+        int ncl1 = greedy(S, S.filt + f0, W.fmd, nfs, G.type_maxdt[ti], false, 0.0, S.cl_of, S.clus, W.clstart);
+        for (int c = 0; c < ncl1; ++c) {
+          int a = W.clstart[c], b = W.clstart[c + 1];
+          for (int k = lane_id(); k < b - a; k += 32) S.order[k] = S.filt[f0 + S.clus[a + k]];
+          __syncwarp();
+          check_coincidence(G, S, S.order, b - a, p.big_cluster_threshold);
+          // kept members sorted by pulse idx -> coincidence list
+          int mk = b - a;
+          for (int k = lane_id(); k < mk; k += 32) {
+            int h = S.order[k];
+            if (!S.kept[h]) continue;
+            int r = 0;
+            for (int q = 0; q < mk; ++q) {
+              int o = S.order[q];
+              r += S.kept[o] && S.idx[o] < S.idx[h];
+            }
+            S.coinc[nc + r] = h;
+            double w = __longlong_as_double((long long)S.wid[h]);
+            double f = cutv(G, S.cut[h], CUT_D1);
+            W.cmd[nc + r] = w > f ? w : f;
+          }
+          int nk = 0;
+          for (int k = lane_id(); k < mk; k += 32) nk += S.kept[S.order[k]];
+          nk = warp_sum(nk);
+          __syncwarp();
+          nc += nk;
+        }
+      }
+      if (nc == 0) continue;
+      bool both = G.type_side0[ti] && G.type_side1[ti];
+      double dt_opp = 2.0 * G.type_half[ti] / p.fiber_signal_speed;
+      int ncl2 = greedy(S, S.coinc, W.cmd, nc, G.type_maxdt[ti], both, dt_opp, W.ccl, S.clus, W.cstart);
+      // attachment of filtered first pulses on missing opposite counter ends
+      int natt = 0;
+      if (both && p.add_opposite) {
+        double mdt = G.type_maxdt[ti] + dt_opp;
+        for (int base = 0; base < nf; base += 32) {
+          int k = base + lane_id();
+          bool got = false;
+          int bestc = 0;
+          double bestdt = 0.0;
+          int h = -1;
+          if (k < nf) {
+            h = S.filt[k];
+            bool member = false;
+            for (int q = 0; q < nc && !member; ++q) member = S.coinc[q] == h;
+            if (S.seq[h] == 0 && !member) {
+              for (int q = 0; q < nc; ++q) {
+                int a = S.coinc[q];
+                if (S.seq[a] != 0 || S.bar[a] != S.bar[h] || S.side[h] != 1 - S.side[a]) continue;
+                double dt = fabs(S.t[h] - S.t[a]);
+                if (!(dt < mdt)) continue;
+                int cl = W.ccl[q];
+                bool occ = false;
+                for (int z = W.cstart[cl]; z < W.cstart[cl + 1] && !occ; ++z) {
+                  int o = S.coinc[S.clus[z]];
+                  occ = S.bar[o] == S.bar[h] && S.side[o] == S.side[h];
+                }
+                if (occ) continue;
+                if (!got || dt < bestdt || (dt == bestdt && cl < bestc)) { got = true; bestdt = dt; bestc = cl; }
+              }
+            }
+          }
+          unsigned m = __ballot_sync(0xffffffffu, got);
+          if (got) {
+            int o = natt + __popc(m & ((1u << lane_id()) - 1u));
+            W.att_c[o] = k; W.att_cl[o] = bestc; W.att_dt[o] = bestdt;
+            W.att_bar[o] = S.bar[h]; W.att_sipm[o] = S.sipm[h];
+          }
+          natt += __popc(m);
+        }
+        __syncwarp();
+        if (lane_id() == 0 && natt > 1) {     // sort by (cluster, bar, sipm, dt, candidate)
+          for (int a = 1; a < natt; ++a) {
+            int c = W.att_c[a], cl = W.att_cl[a], br = W.att_bar[a], sp = W.att_sipm[a];
+            double dt = W.att_dt[a];
+            int b = a - 1;
+            while (b >= 0) {
+              bool gt = W.att_cl[b] != cl ? W.att_cl[b] > cl : W.att_bar[b] != br ? W.att_bar[b] > br
+                      : W.att_sipm[b] != sp ? W.att_sipm[b] > sp : W.att_dt[b] != dt ? W.att_dt[b] > dt
+                      : W.att_c[b] > c;
+              if (!gt) break;
+              W.att_c[b + 1] = W.att_c[b]; W.att_cl[b + 1] = W.att_cl[b]; W.att_bar[b + 1] = W.att_bar[b];
+              W.att_sipm[b + 1] = W.att_sipm[b]; W.att_dt[b + 1] = W.att_dt[b];
+              --b;
+            }
+            W.att_c[b + 1] = c; W.att_cl[b + 1] = cl; W.att_bar[b + 1] = br; W.att_sipm[b + 1] = sp;
+            W.att_dt[b + 1] = dt;
+          }
+          // keep the first per (cluster, bar, sipm): mark duplicates with cluster -1
+          for (int a = 1; a < natt; ++a) {
+            int b = a - 1;
+            while (b >= 0 && W.att_cl[b] < 0) --b;
+            if (b >= 0 && W.att_cl[b] == W.att_cl[a] && W.att_bar[b] == W.att_bar[a] && W.att_sipm[b] == W.att_sipm[a])
+              W.att_cl[a] = -1 - W.att_cl[a];
+          }
+        }
+        __syncwarp();
+      }
+      // clusters -> records (lane 0), members into the event's member slots
+      if (lane_id() == 0) {
+        for (int c = 0; c < ncl2; ++c) {
+          int m = 0;
+          int a = W.cstart[c], b = W.cstart[c + 1];
+          for (int z = a; z < b; ++z) S.order[m++] = S.coinc[S.clus[z]];
+          for (int z = 0; z < natt; ++z)
+            if (W.att_cl[z] == c) S.order[m++] = S.filt[W.att_c[z]];
+          ClusterRec R;
+          if (!cluster_props(G, S, p, ti, G.type_id[ti], S.order, m, R)) continue;
+          R.mem_begin = nmem_ev;
+          R.mem_count = m;
+          R.pad = 0;
+          if (ncl_ev < np_ && nmem_ev + m <= np_) {
+            O.rec[r0 + ncl_ev] = R;
+            for (int z = 0; z < m; ++z) O.mem_idx[r0 + nmem_ev + z] = S.idx[S.order[z]];
+          }
+          ++ncl_ev;
+          nmem_ev += m;
+        }
+      }
+      ncl_ev = __shfl_sync(0xffffffffu, ncl_ev, 0);
+      nmem_ev = __shfl_sync(0xffffffffu, nmem_ev, 0);
+      __syncwarp();
+    }
+    if (lane_id() == 0) {
+      O.ncl[e] = ncl_ev;
+      O.nmem[e] = nmem_ev;
+      if (second_pass) deferred[e] = 0;
+      if (ncl_ev > np_ || nmem_ev > np_) set_flag(status, CRV_ST_LIMIT);
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace crv

@@ -2,14 +2,17 @@
 // The kernels of each precision live in crv_kernels_f64.cu / crv_kernels_f32.cu; this unit holds the precision-free
 // kernels (event preparation, SiPM sizing, compaction, scans).
 #define CRV_ENGINE_TU 1
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "crv_launch.h"
 #include "crv_response.cuh"
 #include "crv_waveform.cuh"
 #include "crv_pulsefit.cuh"
+#include "crv_coinc.cuh"
 
 namespace crv {
 
@@ -26,6 +29,46 @@ const DeviceInfo& device_info() {
     di.smem_optin = size_t(optin > 0 ? optin : 48 * 1024);
   });
   return di;
+}
+
+// ---- launch accounting / profiling ---------------------------------------------------------------------------------
+
+namespace {
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof;
+std::vector<cudaEvent_t> g_pool;
+size_t g_pool_used = 0;
+std::atomic<long long> g_launches{0};
+
+cudaEvent_t pool_event() {
+  if (g_pool_used == g_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    g_pool.push_back(e);
+  }
+  return g_pool[g_pool_used++];
+}
+}  // namespace
+
+Mark::Mark(const char* name, cudaStream_t s) : slot(-1), stream(s) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  if (!g_prof_on) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  ProfRec r{name, pool_event(), pool_event()};
+  cudaEventRecord(r.a, s);
+  slot = int(g_prof.size());
+  g_prof.push_back(r);
+}
+
+Mark::~Mark() {
+  if (slot < 0) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEventRecord(g_prof[slot].b, stream);
 }
 
 __global__ void k_scan_parts(long long* __restrict__ part, long long nb, long long* __restrict__ total) {
@@ -199,6 +242,29 @@ extern "C" {
 
 int crv_version(void) { return CRVGPU_VERSION; }
 
+long long crv_launch_count(void) { return g_launches.load(); }
+
+void crv_profile(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.clear();
+  g_pool_used = 0;
+  g_prof_on = on != 0;
+}
+
+int crv_profile_read(int cap, char* names, float* ms) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  int n = int(g_prof.size());
+  for (int i = 0; i < n && i < cap; ++i) {
+    cudaEventSynchronize(g_prof[i].b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, g_prof[i].a, g_prof[i].b);
+    ms[i] = t;
+    strncpy(names + size_t(i) * 64, g_prof[i].name, 63);
+    names[size_t(i) * 64 + 63] = 0;
+  }
+  return n;
+}
+
 const char* crv_status_string(int32_t flags) {
   static thread_local char buf[256];
   if (flags == 0) return "ok";
@@ -229,7 +295,10 @@ int crv_photon_counts(const CrvParams* p, const CrvEvents* ev, int64_t nevents, 
   cudaStream_t s = (cudaStream_t)stream;
   Status* S = reinterpret_cast<Status*>(status_dev);
   if (nevents == 0 || nsteps == 0) return CRV_OK;
-  k_fill_step_event<<<grid_for(nevents, 8, 32), 256, 0, s>>>(*ev, nevents, step_event);
+  {
+    crv::Mark mark_("k_fill_step_event", s);
+    k_fill_step_event<<<grid_for(nevents, 8, 32), 256, 0, s>>>(*ev, nevents, step_event);
+  }
   CK(cudaGetLastError());
   if (p->precision == 1)
     CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, step_event, nsteps, 0, count, S, s));
@@ -289,12 +358,18 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
   size_t psmem = size_t(stepcap) * 4;
   CK(cudaFuncSetAttribute(k_event_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
   unsigned gp = grid_for(nevents, 1, 8);
-  k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, w.step_event, w.step_order,
-                                                w.sipm_count, nullptr, nullptr, nullptr, nullptr, nullptr, S, 0);
+  {
+    crv::Mark mark_("k_event_prep", s);
+    k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, w.step_event, w.step_order,
+                                                  w.sipm_count, nullptr, nullptr, nullptr, nullptr, nullptr, S, 0);
+  }
   CK(cudaGetLastError());
   CK(exclusive_scan(w.sipm_count, nevents, Identity(), w.sipm_off, &w.totals[0], w.parts, s));
-  k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, nullptr, nullptr, nullptr,
-                                                w.sipm_off, w.s_event, w.s_chan, w.s_seg, w.s_nseg, S, 1);
+  {
+    crv::Mark mark_("k_event_prep", s);
+    k_event_prep<<<gp, PREP_THREADS, psmem, s>>>(*ev, nevents, *st, *ch, 1, stepcap, nullptr, nullptr, nullptr,
+                                                  w.sipm_off, w.s_event, w.s_chan, w.s_seg, w.s_nseg, S, 1);
+  }
   CK(cudaGetLastError());
   // 4. photon counts per (step, SiPM)
   if (p->precision == 1)
@@ -303,14 +378,23 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
     CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, 1, w.count, S, s));
   // 5. per-SiPM photons and charge slots; scans
   int factor = p->charge_factor > 0 ? p->charge_factor : 1;
-  k_sipm_sizes<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
-                                                      w.step_order, w.count, *ev, factor, w.nphot, w.slot_cap,
-                                                      w.id_base, w.label, w.run);
+  {
+    crv::Mark mark_("k_sipm_sizes", s);
+    k_sipm_sizes<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
+                                                        w.step_order, w.count, *ev, factor, w.nphot, w.slot_cap,
+                                                        w.id_base, w.label, w.run);
+  }
   CK(cudaGetLastError());
   CK(exclusive_scan(w.nphot, w.nb, Identity(), w.ph_off, &w.totals[1], w.parts, s));
   CK(exclusive_scan(w.slot_cap, w.nb, Identity(), w.slot_off, &w.totals[2], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], w.pc, CRV_NEED_PHOTONS_TOTAL, S);
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], w.pc, CRV_NEED_PHOTONS_TOTAL, S);
+  }
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  }
   CK(cudaGetLastError());
   // 6. photons of every SiPM
   if (p->precision == 1)
@@ -342,19 +426,37 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
   else
     CK((launch_sipm<double, double>(*p, *px, G, &w.totals[0], (const double*)w.ph_t, O, S, s)));
   // 8. compaction into label/time order
-  k_counts_total<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  {
+    crv::Mark mark_("k_counts_total", s);
+    k_counts_total<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  }
   CK(cudaGetLastError());
   CK(exclusive_scan(w.ntot, w.nb, Identity(), w.out_off, &w.totals[3], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
-  k_charge_compact<<<grid_for(w.nb, 8, 16), 256, 0, s>>>(&w.totals[0], w.label, w.slot_off, w.slot_cap, w.nmain,
-                                                          w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
-                                                          p->capacitance, p->overvoltage, *out, out_cap);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
+  }
+  {
+    crv::Mark mark_("k_charge_compact", s);
+    k_charge_compact<<<grid_for(w.nb, 8, 16), 256, 0, s>>>(&w.totals[0], w.label, w.slot_off, w.slot_cap, w.nmain,
+                                                            w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
+                                                            p->capacitance, p->overvoltage, *out, out_cap);
+  }
   CK(cudaGetLastError());
-  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
-  if (n_sipm_dev) k_copy_i64<<<1, 1, 0, s>>>(&w.totals[0], reinterpret_cast<long long*>(n_sipm_dev));
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  }
+  if (n_sipm_dev) {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[0], reinterpret_cast<long long*>(n_sipm_dev));
+  }
   if (sipm_label || sipm_photons || sipm_fired)
-    k_sipm_diag<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], sipm_cap, w.label, w.nphot, w.fired,
-                                                       sipm_label, sipm_photons, sipm_fired, S);
+    {
+      crv::Mark mark_("k_sipm_diag", s);
+      k_sipm_diag<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], sipm_cap, w.label, w.nphot, w.fired,
+                                                         sipm_label, sipm_photons, sipm_fired, S);
+    }
   CK(cudaGetLastError());
   return CRV_OK;
 }
@@ -423,11 +525,20 @@ extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups
   CK(cudaMemsetAsync(w.nmain, 0, sizeof(int32_t) * ngroups, s));
   CK(cudaMemsetAsync(w.nap, 0, sizeof(int32_t) * ngroups, s));
   CK(cudaMemsetAsync(g_fired, 0, sizeof(int32_t) * ngroups, s));
-  k_set_i64<<<1, 1, 0, s>>>(&w.totals[0], ngroups);
-  k_slot_caps<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(ngroups, gcount, factor, w.slot_cap);
+  {
+    crv::Mark mark_("k_set_i64", s);
+    k_set_i64<<<1, 1, 0, s>>>(&w.totals[0], ngroups);
+  }
+  {
+    crv::Mark mark_("k_slot_caps", s);
+    k_slot_caps<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(ngroups, gcount, factor, w.slot_cap);
+  }
   CK(cudaGetLastError());
   CK(exclusive_scan(w.slot_cap, ngroups, Identity(), w.slot_off, &w.totals[2], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
+  }
   SipmGroups G{};
   G.n = &w.totals[0];
   G.guard[0] = &w.totals[2];
@@ -448,17 +559,29 @@ extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups
     CK((launch_sipm<float, double>(*p, *px, G, &w.totals[0], time, O, S, s)));
   else
     CK((launch_sipm<double, double>(*p, *px, G, &w.totals[0], time, O, S, s)));
-  k_counts_total<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  {
+    crv::Mark mark_("k_counts_total", s);
+    k_counts_total<<<grid_for(ngroups, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
+  }
   CK(cudaGetLastError());
   CK(exclusive_scan(w.ntot, ngroups, Identity(), w.out_off, &w.totals[3], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
-  k_charge_compact<<<grid_for(ngroups, 8, 16), 256, 0, s>>>(&w.totals[0], G.label, w.slot_off, w.slot_cap, w.nmain,
-                                                             w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
-                                                             p->capacitance, p->overvoltage, *out, out_cap);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
+  }
+  {
+    crv::Mark mark_("k_charge_compact", s);
+    k_charge_compact<<<grid_for(ngroups, 8, 16), 256, 0, s>>>(&w.totals[0], G.label, w.slot_off, w.slot_cap, w.nmain,
+                                                               w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
+                                                               p->capacitance, p->overvoltage, *out, out_cap);
+  }
   CK(cudaGetLastError());
   if (g_charges)
     CK(cudaMemcpyAsync(g_charges, w.ntot, sizeof(int32_t) * ngroups, cudaMemcpyDeviceToDevice, s));
-  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  }
   CK(cudaGetLastError());
   return CRV_OK;
 }
@@ -540,11 +663,20 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   CK(cudaMemsetAsync(w.g_bound, 0, sizeof(int32_t) * ncharges, s));
   CK(cudaMemsetAsync(w.dn, 0, sizeof(int32_t) * ncharges, s));
   unsigned gq = grid_for(ncharges, 256, 8);
-  k_label_heads<<<gq, 256, 0, s>>>(ncharges, lab, w.head);
+  {
+    crv::Mark mark_("k_label_heads", s);
+    k_label_heads<<<gq, 256, 0, s>>>(ncharges, lab, w.head);
+  }
   CK(exclusive_scan(w.head, ncharges, Identity(), w.gidx, &w.totals[0], w.parts, s));
-  k_label_groups<<<gq, 256, 0, s>>>(ncharges, lab, w.head, w.gidx, w.gstart, w.glabel);
-  k_group_counts<<<gq, 256, 0, s>>>(&w.totals[0], ncharges, w.gstart, w.glabel, w.gcount,
-                                    reinterpret_cast<const long long*>(ev_keys), ev_runs, n_events, w.grun, S);
+  {
+    crv::Mark mark_("k_label_groups", s);
+    k_label_groups<<<gq, 256, 0, s>>>(ncharges, lab, w.head, w.gidx, w.gstart, w.glabel);
+  }
+  {
+    crv::Mark mark_("k_group_counts", s);
+    k_group_counts<<<gq, 256, 0, s>>>(&w.totals[0], ncharges, w.gstart, w.glabel, w.gcount,
+                                      reinterpret_cast<const long long*>(ev_keys), ev_runs, n_events, w.grun, S);
+  }
   CK(cudaGetLastError());
   WfGroups G{&w.totals[0], w.gstart, w.gcount, w.glabel, w.grun};
   if (p->precision == 1)
@@ -552,9 +684,15 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   else
     CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen, s));
   CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, CRV_NEED_DIGIS, S);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, CRV_NEED_DIGIS, S);
+  }
   // synthesis only when the slots fit: guard by zeroing the group count otherwise
-  k_guard_groups<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, &w.totals[0], &w.totals[2]);
+  {
+    crv::Mark mark_("k_guard_groups", s);
+    k_guard_groups<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, &w.totals[0], &w.totals[2]);
+  }
   CK(cudaGetLastError());
   G.n = &w.totals[2];
   if (p->precision == 1)
@@ -562,11 +700,20 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   else
     CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.D, S, s));
   CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_DIGIS_OUT, S);
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_DIGIS_OUT, S);
+  }
   Digis O{reinterpret_cast<long long*>(out->chan), out->start, out->tdc0, reinterpret_cast<long long*>(out->starttdc),
           out->volt, out->adc};
-  k_digi_compact<<<grid_for(ncharges, 8, 16), 256, 0, s>>>(&w.totals[2], w.D, w.out_off, p->samples_zs, O, out_cap);
-  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  {
+    crv::Mark mark_("k_digi_compact", s);
+    k_digi_compact<<<grid_for(ncharges, 8, 16), 256, 0, s>>>(&w.totals[2], w.D, w.out_off, p->samples_zs, O, out_cap);
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[3], reinterpret_cast<long long*>(n_out_dev));
+  }
   CK(cudaGetLastError());
   return CRV_OK;
 }
@@ -656,9 +803,374 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, const int64_t* off, co
   else
     CK(launch_pulsefit<double>(*p, W, max_pulses, O, w.deferred, S, s));
   CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s));
-  k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], out_cap, CRV_NEED_PULSES_OUT, S);
-  k_pulse_compact<<<grid_for(nw, 256, 8), 256, 0, s>>>(nw, w.base, w.count, w.out_off, w.rec, *out, out_cap);
-  k_copy_i64<<<1, 1, 0, s>>>(&w.totals[1], reinterpret_cast<long long*>(n_out_dev));
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], out_cap, CRV_NEED_PULSES_OUT, S);
+  }
+  {
+    crv::Mark mark_("k_pulse_compact", s);
+    k_pulse_compact<<<grid_for(nw, 256, 8), 256, 0, s>>>(nw, w.base, w.count, w.out_off, w.rec, *out, out_cap);
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[1], reinterpret_cast<long long*>(n_out_dev));
+  }
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+// ---- coincidences ---------------------------------------------------------------------------------------------------
+
+namespace crv {
+static_assert(sizeof(CrvFinderGeom) == sizeof(CoincGeom), "finder geometry layout");
+
+struct CoincWs {
+  ClusterRec* rec;
+  int32_t *mem_idx, *ncl, *nmem, *deferred;
+  long long *cl_off, *mem_off, *parts, *totals;
+};
+
+static CoincWs coinc_layout(char* base, long long nev, long long np, size_t* bytes) {
+  Carve c{base};
+  CoincWs w;
+  w.rec = c.take<ClusterRec>(np);
+  w.mem_idx = c.take<int32_t>(np);
+  w.ncl = c.take<int32_t>(nev);
+  w.nmem = c.take<int32_t>(nev);
+  w.deferred = c.take<int32_t>(nev);
+  w.cl_off = c.take<long long>(nev);
+  w.mem_off = c.take<long long>(nev);
+  w.parts = c.take<long long>(scan_parts_len(nev) + 1);
+  w.totals = c.take<long long>(8);
+  *bytes = c.off + 256;
+  return w;
+}
+
+__global__ void k_coinc_compact(long long nev, const long long* __restrict__ ev_start, const long long* __restrict__ ev_key,
+                                const int32_t* __restrict__ ncl, const long long* __restrict__ cl_off,
+                                const long long* __restrict__ mem_off, const ClusterRec* __restrict__ rec,
+                                const int32_t* __restrict__ mem_idx, CrvClusters O, long long cl_cap, CrvMembers M,
+                                long long mem_cap) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nev; e += (long long)gridDim.x * blockDim.x) {
+    long long r0 = ev_start[e];
+    for (int k = 0; k < ncl[e]; ++k) {
+      const ClusterRec& R = rec[r0 + k];
+      long long o = cl_off[e] + k;
+      if (o >= cl_cap) break;
+      O.event[o] = ev_key[e];
+      O.type[o] = R.type;
+      O.pe[o] = R.pe; O.start[o] = R.start; O.end[o] = R.end; O.slope[o] = R.slope; O.avgtime[o] = R.avgtime;
+      O.poscalc[o] = uint8_t(R.poscalc);
+      for (int c = 0; c < 3; ++c) O.pos[o * 3 + c] = R.pos[c];
+      for (int sd = 0; sd < 2; ++sd) {
+        O.sidepe[o * 2 + sd] = R.sidepe[sd];
+        O.sidetime[o * 2 + sd] = R.sidetime[sd];
+        O.sidehits[o * 2 + sd] = R.sidehits[sd];
+      }
+      O.nlayers[o] = R.nlayers;
+      for (int z = 0; z < R.mem_count; ++z) {
+        long long q = mem_off[e] + R.mem_begin + z;
+        if (q >= mem_cap) break;
+        M.cl[q] = o;
+        M.idx[q] = mem_idx[r0 + R.mem_begin + z];
+        M.event[q] = ev_key[e];
+      }
+    }
+  }
+}
+}  // namespace crv
+
+extern "C" int64_t crv_coincidences_workspace(int64_t nevents, int64_t npulses) {
+  if (nevents < 0 || npulses < 0) return -1;
+  size_t b = 0;
+  coinc_layout(nullptr, nevents, npulses, &b);
+  return (int64_t)b;
+}
+
+extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int64_t nevents, const int64_t* ev_start,
+                                const int32_t* ev_count, const int64_t* ev_key, int64_t npulses, const int32_t* bar,
+                                const int32_t* sipm, const int32_t* seq, const double* time, const double* pe,
+                                const int32_t* status, CrvClusters* out, int64_t cl_cap, int64_t* n_cl_dev,
+                                CrvMembers* mem, int64_t mem_cap, int64_t* n_mem_dev, void* workspace,
+                                int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!p || !g || !out || !mem || !n_cl_dev || !n_mem_dev || !status_dev || nevents < 0 || npulses < 0) return CRV_ERR_ARG;
+  if (nevents > 0 && (!ev_start || !ev_count || !ev_key)) return CRV_ERR_ARG;
+  if (npulses > 0 && (!bar || !sipm || !seq || !time || !pe || !status)) return CRV_ERR_ARG;
+  if (g->ntypes < 0) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nevents == 0) {
+    CK(cudaMemsetAsync(n_cl_dev, 0, sizeof(long long), s));
+    CK(cudaMemsetAsync(n_mem_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  size_t need = 0;
+  coinc_layout(nullptr, nevents, npulses, &need);
+  if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
+  Status* S = reinterpret_cast<Status*>(status_dev);
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  CoincWs w = coinc_layout(base, nevents, npulses, &dummy);
+  CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.ncl, 0, sizeof(int32_t) * nevents, s));
+  CK(cudaMemsetAsync(w.nmem, 0, sizeof(int32_t) * nevents, s));
+  CK(cudaMemsetAsync(w.deferred, 0, sizeof(int32_t) * nevents, s));
+  CoincGeom G;
+  memcpy(&G, g, sizeof(G));
+  CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
+  CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
+  const DeviceInfo& di = device_info();
+  struct Pass { int hcap, warps; } passes[2] = {{256, 6}, {1280, 1}};
+  for (int k = 0; k < 2; ++k) {
+    size_t per = coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap);
+    size_t smem = per * passes[k].warps;
+    if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
+    CK(cudaFuncSetAttribute(k_coinc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
+    long long maxb = (long long)di.sms * (k == 0 ? 8 : 2);
+    {
+      crv::Mark mark_("k_coinc", s);
+      k_coinc<<<(unsigned)(blocks < maxb ? blocks : maxb), passes[k].warps * 32, smem, s>>>(*p, G, I, passes[k].hcap, k,
+                                                                                            O, w.deferred, S);
+    }
+    CK(cudaGetLastError());
+  }
+  CK(exclusive_scan(w.ncl, nevents, Identity(), w.cl_off, &w.totals[0], w.parts, s));
+  CK(exclusive_scan(w.nmem, nevents, Identity(), w.mem_off, &w.totals[1], w.parts, s));
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[0], cl_cap, CRV_NEED_CLUSTERS, S);
+  }
+  {
+    crv::Mark mark_("k_check_caps", s);
+    k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], mem_cap, CRV_NEED_MEMBERS, S);
+  }
+  {
+    crv::Mark mark_("k_coinc_compact", s);
+    k_coinc_compact<<<grid_for(nevents, 256, 8), 256, 0, s>>>(nevents, reinterpret_cast<const long long*>(ev_start),
+                                                            reinterpret_cast<const long long*>(ev_key), w.ncl, w.cl_off,
+                                                            w.mem_off, w.rec, w.mem_idx, *out, cl_cap, *mem, mem_cap);
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[0], reinterpret_cast<long long*>(n_cl_dev));
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&w.totals[1], reinterpret_cast<long long*>(n_mem_dev));
+  }
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+// ---- reco waveforms and pulse glue ---------------------------------------------------------------------------------
+
+namespace crv {
+__global__ void k_wf_heads(long long nd, const long long* __restrict__ label, const long long* __restrict__ tdc, int zs,
+                           int32_t* __restrict__ head) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
+    head[i] = (i == 0 || label[i] != label[i - 1] || tdc[i] != tdc[i - 1] + zs) ? 1 : 0;
+}
+
+__global__ void k_wf_fill(long long nd, const long long* __restrict__ label, const long long* __restrict__ tdc, int zs,
+                          const int32_t* __restrict__ head, const long long* __restrict__ gidx, const long long* n_dev,
+                          CrvChannels ch, long long* __restrict__ w_label, long long* __restrict__ w_off,
+                          int32_t* __restrict__ w_n, long long* __restrict__ w_start, double* __restrict__ w_ped,
+                          double* __restrict__ w_area, double* __restrict__ w_height, double* __restrict__ w_toff) {
+  long long G = *n_dev;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x) {
+    if (!head[i]) continue;
+    long long g = gidx[i];
+    long long j = i + 1;
+    while (j < nd && !head[j]) ++j;
+    int c = int(label[i] % 32768);
+    w_label[g] = label[i];
+    w_off[g] = i * zs;
+    w_n[g] = int32_t((j - i) * zs);
+    w_start[g] = tdc[i];
+    w_ped[g] = ch.pedestal[c];
+    w_area[g] = ch.pulsearea[c];
+    w_height[g] = ch.pulseheight[c];
+    w_toff[g] = ch.timeoffset[c];
+    (void)G;
+  }
+}
+
+__global__ void k_hit_keep(const CrvParams p, const int32_t* __restrict__ status, const long long* __restrict__ w_label,
+                           long long np, const long long* __restrict__ p_wf, int32_t* __restrict__ keep) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
+    int c = int(w_label[p_wf[i]] % 32768);
+    keep[i] = (p.ignore_channels && (status[c] & 0b010)) ? 0 : 1;
+  }
+}
+
+__global__ void k_hit_fill(const CrvParams p, const long long* __restrict__ w_label, const double* __restrict__ w_toff,
+                           const double* __restrict__ event_t0, long long np, const long long* __restrict__ p_wf,
+                           const long long* __restrict__ p_seq, const double* __restrict__ p_time,
+                           const double* __restrict__ p_pe, const int32_t* __restrict__ keep,
+                           const long long* __restrict__ kidx, int32_t* __restrict__ bar, int32_t* __restrict__ sipm,
+                           int32_t* __restrict__ seq, double* __restrict__ time, double* __restrict__ pe,
+                           long long* __restrict__ hev) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
+    if (!keep[i]) continue;
+    long long k = kidx[i];
+    long long w = p_wf[i];
+    long long lab = w_label[w];
+    int c = int(lab % 32768);
+    double t = p_time[i];
+    if (p.use_time_offset_db) t = t + w_toff[w] * p.time_offset_scale;
+    if (event_t0) t = t + event_t0[w];
+    bar[k] = c / 4;
+    sipm[k] = c % 4;
+    seq[k] = int32_t(p_seq[i]);
+    time[k] = t;
+    pe[k] = p_pe[i];
+    hev[k] = lab / 32768;
+  }
+}
+
+__global__ void k_ev_heads(const long long* __restrict__ n_dev, const long long* __restrict__ hev,
+                           int32_t* __restrict__ head) {
+  long long n = *n_dev;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    head[i] = (i == 0 || hev[i] != hev[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_ev_fill(const long long* __restrict__ n_dev, const long long* __restrict__ hev,
+                          const int32_t* __restrict__ head, const long long* __restrict__ eidx,
+                          long long* __restrict__ ev_start, int32_t* __restrict__ ev_count,
+                          long long* __restrict__ ev_key) {
+  long long n = *n_dev;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (!head[i]) continue;
+    long long e = eidx[i];
+    long long j = i + 1;
+    while (j < n && !head[j]) ++j;
+    ev_start[e] = i;
+    ev_count[e] = int32_t(j - i);
+    ev_key[e] = hev[i];
+  }
+}
+}  // namespace crv
+
+extern "C" int64_t crv_reco_waveforms_workspace(int64_t nd) {
+  if (nd < 0) return -1;
+  Carve c{nullptr};
+  c.take<int32_t>(nd);
+  c.take<long long>(nd);
+  c.take<long long>(scan_parts_len(nd) + 1);
+  c.take<long long>(8);
+  return (int64_t)(c.off + 256);
+}
+
+extern "C" int crv_reco_waveforms(const CrvParams* p, const CrvChannels* ch, int64_t nd, const int64_t* label,
+                                  const int64_t* starttdc, int64_t* w_label, int64_t* w_off, int32_t* w_n,
+                                  int64_t* w_start, double* w_ped, double* w_area, double* w_height, double* w_toff,
+                                  int64_t* n_w_dev, void* workspace, int64_t workspace_bytes, void* stream,
+                                  CrvStatus* status_dev) {
+  if (!p || !ch || !n_w_dev || !status_dev || nd < 0) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nd == 0) {
+    CK(cudaMemsetAsync(n_w_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  if (crv_reco_waveforms_workspace(nd) > workspace_bytes || !workspace) return CRV_ERR_ARG;
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  Carve c{base};
+  int32_t* head = c.take<int32_t>(nd);
+  long long* gidx = c.take<long long>(nd);
+  long long* parts = c.take<long long>(scan_parts_len(nd) + 1);
+  long long* totals = c.take<long long>(8);
+  const long long* lab = reinterpret_cast<const long long*>(label);
+  const long long* tdc = reinterpret_cast<const long long*>(starttdc);
+  unsigned g = grid_for(nd, 256, 8);
+  {
+    crv::Mark mark_("k_wf_heads", s);
+    k_wf_heads<<<g, 256, 0, s>>>(nd, lab, tdc, p->samples_zs, head);
+  }
+  CK(exclusive_scan(head, nd, Identity(), gidx, &totals[0], parts, s));
+  {
+    crv::Mark mark_("k_wf_fill", s);
+    k_wf_fill<<<g, 256, 0, s>>>(nd, lab, tdc, p->samples_zs, head, gidx, &totals[0], *ch,
+                                reinterpret_cast<long long*>(w_label), reinterpret_cast<long long*>(w_off), w_n,
+                                reinterpret_cast<long long*>(w_start), w_ped, w_area, w_height, w_toff);
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&totals[0], reinterpret_cast<long long*>(n_w_dev));
+  }
+  CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+extern "C" int64_t crv_pulse_hits_workspace(int64_t np) {
+  if (np < 0) return -1;
+  Carve c{nullptr};
+  c.take<int32_t>(np);
+  c.take<long long>(np);
+  c.take<long long>(np);
+  c.take<int32_t>(np);
+  c.take<long long>(np);
+  c.take<long long>(scan_parts_len(np) + 1);
+  c.take<long long>(8);
+  return (int64_t)(c.off + 256);
+}
+
+extern "C" int crv_pulse_hits(const CrvParams* p, const int32_t* status, int64_t nw, const int64_t* w_label,
+                              const double* w_toff, const double* event_t0, int64_t np, const int64_t* p_wf,
+                              const int64_t* p_seq, const double* p_time, const double* p_pe, int64_t* ev_start,
+                              int32_t* ev_count, int64_t* ev_key, int32_t* bar, int32_t* sipm, int32_t* seq,
+                              double* time, double* pe, int64_t* n_ev_dev, int64_t* n_hit_dev, void* workspace,
+                              int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!p || !status || !n_ev_dev || !n_hit_dev || !status_dev || np < 0 || nw < 0) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (np == 0) {
+    CK(cudaMemsetAsync(n_ev_dev, 0, sizeof(long long), s));
+    CK(cudaMemsetAsync(n_hit_dev, 0, sizeof(long long), s));
+    return CRV_OK;
+  }
+  if (crv_pulse_hits_workspace(np) > workspace_bytes || !workspace) return CRV_ERR_ARG;
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  Carve c{base};
+  int32_t* keep = c.take<int32_t>(np);
+  long long* kidx = c.take<long long>(np);
+  long long* hev = c.take<long long>(np);
+  int32_t* head = c.take<int32_t>(np);
+  long long* eidx = c.take<long long>(np);
+  long long* parts = c.take<long long>(scan_parts_len(np) + 1);
+  long long* totals = c.take<long long>(8);
+  unsigned g = grid_for(np, 256, 8);
+  const long long* wl = reinterpret_cast<const long long*>(w_label);
+  {
+    crv::Mark mark_("k_hit_keep", s);
+    k_hit_keep<<<g, 256, 0, s>>>(*p, status, wl, np, reinterpret_cast<const long long*>(p_wf), keep);
+  }
+  CK(exclusive_scan(keep, np, Identity(), kidx, &totals[0], parts, s));
+  {
+    crv::Mark mark_("k_hit_fill", s);
+    k_hit_fill<<<g, 256, 0, s>>>(*p, wl, w_toff, event_t0, np, reinterpret_cast<const long long*>(p_wf),
+                                 reinterpret_cast<const long long*>(p_seq), p_time, p_pe, keep, kidx, bar, sipm, seq,
+                                 time, pe, hev);
+  }
+  // rows beyond the kept count stay 0 so the event scan counts kept pulses only
+  CK(cudaMemsetAsync(head, 0, sizeof(int32_t) * np, s));
+  {
+    crv::Mark mark_("k_ev_heads", s);
+    k_ev_heads<<<g, 256, 0, s>>>(&totals[0], hev, head);
+  }
+  CK(exclusive_scan(head, np, Identity(), eidx, &totals[1], parts, s));
+  {
+    crv::Mark mark_("k_ev_fill", s);
+    k_ev_fill<<<g, 256, 0, s>>>(&totals[0], hev, head, eidx, reinterpret_cast<long long*>(ev_start), ev_count,
+                                reinterpret_cast<long long*>(ev_key));
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&totals[1], reinterpret_cast<long long*>(n_ev_dev));
+  }
+  {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(&totals[0], reinterpret_cast<long long*>(n_hit_dev));
+  }
   CK(cudaGetLastError());
   return CRV_OK;
 }

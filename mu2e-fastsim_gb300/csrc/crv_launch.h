@@ -18,6 +18,15 @@ struct DeviceInfo {
 };
 const DeviceInfo& device_info();
 
+// Launch accounting: every kernel launch of the library is wrapped in a Mark, which counts it and, while profiling
+// is enabled (crv_profile), records CUDA events around it on its stream.
+struct Mark {
+  int slot;
+  cudaStream_t stream;
+  Mark(const char* name, cudaStream_t s);
+  ~Mark();
+};
+
 template <typename R>
 cudaError_t launch_photon_count(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,
                                 const CrvChannels& ch, const int32_t* step_event, long long nsteps, int masked,

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "crv_launch.h"
 
 namespace crv {
 
@@ -97,9 +98,18 @@ cudaError_t exclusive_scan(const T* in, long long n, F f, long long* out, long l
     cudaMemsetAsync(total, 0, sizeof(long long), s);
     return cudaGetLastError();
   }
-  k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part);
-  k_scan_parts<<<1, 1024, 0, s>>>(part, nb, total);
-  k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part, out);
+  {
+    crv::Mark mark_("k_scan_reduce", s);
+    k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part);
+  }
+  {
+    crv::Mark mark_("k_scan_parts", s);
+    k_scan_parts<<<1, 1024, 0, s>>>(part, nb, total);
+  }
+  {
+    crv::Mark mark_("k_scan_down", s);
+    k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part, out);
+  }
   return cudaGetLastError();
 }
 
