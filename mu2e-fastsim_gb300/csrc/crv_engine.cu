@@ -919,7 +919,7 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
   CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
   const DeviceInfo& di = device_info();
-  struct Pass { int hcap, warps; } passes[2] = {{256, 6}, {1280, 1}};
+  struct Pass { int hcap, warps; } passes[2] = {{256, 4}, {1024, 1}};
   for (int k = 0; k < 2; ++k) {
     size_t per = coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap);
     size_t smem = per * passes[k].warps;
