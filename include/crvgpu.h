@@ -265,14 +265,14 @@ int crv_digis(const CrvParams *p, const CrvChannels *ch, int64_t ncharges, const
 
 /*
  * pulsefit.reconstruct: nw waveforms; waveform w has n[w] valid samples at sample rows [off[w], off[w] + n[w]) of
- * adc16 (int16) or adc64 (int64; exactly one is non-null), start TDC, DB pedestal, calibration area and height.
- * max_pulses: rounds per waveform (reconstruct_full passes max(cfg max, longest waveform)).  rec_cap: pulse records of
- * the workspace.  Outputs: pulses (capacity out_cap) and per-waveform wf_near_threshold.
+ * adc16 (int16) or adc64 (int64; exactly one is non-null), start TDC, DB pedestal, calibration area and height;
+ * nsamples: rows of the sample array.  max_pulses: rounds per waveform (reconstruct_full passes max(cfg max, longest
+ * waveform)).  Outputs: pulses (capacity out_cap) and per-waveform wf_near_threshold.
  */
-int64_t crv_pulses_workspace(const CrvParams *p, int64_t nw, int64_t rec_cap);
-int crv_pulses(const CrvParams *p, int64_t nw, const int64_t *off, const int32_t *n, const int64_t *start_tdc,
-               const double *ped_db, const double *area, const double *height, const int16_t *adc16,
-               const int64_t *adc64, int32_t max_pulses, int64_t rec_cap, CrvPulses *out, int64_t out_cap,
+int64_t crv_pulses_workspace(const CrvParams *p, int64_t nw, int64_t nsamples);
+int crv_pulses(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *off, const int32_t *n,
+               const int64_t *start_tdc, const double *ped_db, const double *area, const double *height,
+               const int16_t *adc16, const int64_t *adc64, int32_t max_pulses, CrvPulses *out, int64_t out_cap,
                int64_t *n_out_dev, uint8_t *wf_near, void *workspace, int64_t workspace_bytes, void *stream,
                CrvStatus *status_dev);
 

@@ -126,7 +126,7 @@ _SIGS = {
     "crv_digis": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64, c_i64,
                           P(CrvDigis), c_i64, c_p, c_p, c_i64, c_p, c_p]),
     "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
-    "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, c_i64, P(CrvPulses),
+    "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, P(CrvPulses),
                            c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_coincidences_workspace": (c_i64, [c_i64, c_i64]),
     "crv_coincidences": (c_i32, [P(CrvParams), P(CrvFinderGeom), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_p, c_p,

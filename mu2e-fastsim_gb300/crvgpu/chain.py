@@ -173,7 +173,7 @@ class ChainEngine:
         W = {k: v[:nw] for k, v in W.items()}
         adc16 = D["adc"].reshape(-1)
         Pu = self.pul.run(P, W["off"], W["n"], W["start"], W["ped"], W["area"], W["height"], adc16=adc16,
-                          max_pulses=1 << 30)
+                          max_pulses=2 ** 31 - 1, nsamples=adc16.numel())
         npu = int(Pu["wf"].numel())
         # finder input
         H = dict(ev_start=torch.empty(max(npu, 1), dtype=torch.int64, device=dev),

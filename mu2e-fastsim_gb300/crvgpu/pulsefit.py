@@ -22,35 +22,37 @@ class PulseEngine:
     def __init__(self, device="cuda"):
         self.device = device
         self.ws = None
-        self.rec_factor = 4.0
+        self.out_factor = 2.0
         self.status = _capi.DeviceStatus(device)
 
-    def run(self, P, off, n, start_tdc, ped, area, height, adc16=None, adc64=None, max_pulses=8, max_tries=4):
+    def run(self, P, off, n, start_tdc, ped, area, height, adc16=None, adc64=None, max_pulses=8, nsamples=None,
+            max_tries=4):
         torch = _torch()
         L = _capi.load()
         dev = self.device
         nw = int(n.numel())
+        ns = int(nsamples if nsamples is not None else (adc16 if adc16 is not None else adc64).numel())
         for _ in range(max_tries):
-            rc_ = int(max(1024, self.rec_factor * nw))
-            wsb = L.crv_pulses_workspace(ctypes.byref(P), nw, rc_)
+            cap = int(max(1024, self.out_factor * nw))
+            wsb = L.crv_pulses_workspace(ctypes.byref(P), nw, ns)
             if self.ws is None or self.ws.numel() < wsb:
                 self.ws = torch.empty(int(wsb * 1.1) + 1024, dtype=torch.uint8, device=dev)
-            out = {k: torch.empty(rc_, dtype=torch.int64, device=dev) for k in _capi.PULSE_INT}
-            out.update({k: torch.empty(rc_, dtype=torch.float64, device=dev) for k in _capi.PULSE_FLOAT})
-            out.update({k: torch.empty(rc_, dtype=torch.uint8, device=dev) for k in _capi.PULSE_BOOL})
+            out = {k: torch.empty(cap, dtype=torch.int64, device=dev) for k in _capi.PULSE_INT}
+            out.update({k: torch.empty(cap, dtype=torch.float64, device=dev) for k in _capi.PULSE_FLOAT})
+            out.update({k: torch.empty(cap, dtype=torch.uint8, device=dev) for k in _capi.PULSE_BOOL})
             near = torch.empty(max(nw, 1), dtype=torch.uint8, device=dev)
             n_out = torch.zeros(1, dtype=torch.int64, device=dev)
             self.status.reset()
             O = _capi.CrvPulses(*[_capi.ptr(out[k]) for k in _capi.PULSE_INT + _capi.PULSE_FLOAT + _capi.PULSE_BOOL])
-            r = L.crv_pulses(ctypes.byref(P), nw, _capi.ptr(off), _capi.ptr(n), _capi.ptr(start_tdc), _capi.ptr(ped),
-                             _capi.ptr(area), _capi.ptr(height), _capi.ptr(adc16), _capi.ptr(adc64), int(max_pulses),
-                             rc_, ctypes.byref(O), rc_, _capi.ptr(n_out), _capi.ptr(near), _capi.ptr(self.ws),
-                             self.ws.numel(), _stream(), self.status.ptr)
+            r = L.crv_pulses(ctypes.byref(P), nw, ns, _capi.ptr(off), _capi.ptr(n), _capi.ptr(start_tdc),
+                             _capi.ptr(ped), _capi.ptr(area), _capi.ptr(height), _capi.ptr(adc16), _capi.ptr(adc64),
+                             int(min(max_pulses, 2 ** 31 - 1)), ctypes.byref(O), cap, _capi.ptr(n_out),
+                             _capi.ptr(near), _capi.ptr(self.ws), self.ws.numel(), _stream(), self.status.ptr)
             _capi.check(r, "crv_pulses")
             flags, need = self.status.read()
             npo = need[_capi.NEED["PULSES_OUT"]]
-            if flags == _capi.ST_CAPACITY and npo and not need[_capi.NEED["SAMPLES"]] and not need[_capi.NEED["PULSES"]]:
-                self.rec_factor = 1.3 * npo / max(nw, 1)
+            if flags == _capi.ST_CAPACITY and npo:
+                self.out_factor = 1.3 * npo / max(nw, 1)
                 continue
             raise_status(flags, need, "crv_pulses")
             m = int(n_out.item())

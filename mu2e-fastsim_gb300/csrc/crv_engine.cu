@@ -722,33 +722,45 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
 
 namespace crv {
 struct PulseWs {
+  double* yscr;
   PulseRec* rec;
-  long long *base, *out_off, *parts, *totals;
-  int32_t *count, *deferred;
+  long long *slot_off, *out_off, *parts, *totals;
+  int32_t *cap, *count;
   long long rc;
 };
 
-static PulseWs pulse_layout(char* base, long long nw, long long rec_cap, size_t* bytes) {
+// record slots of waveform w: min(max_pulses, n/2 + 1) (every round advances the search by at least two samples)
+static long long pulse_slot_bound(long long nw, long long nsamples) { return nsamples / 2 + nw + 1; }
+
+static PulseWs pulse_layout(char* base, long long nw, long long nsamples, size_t* bytes) {
   Carve c{base};
   PulseWs w;
-  w.rc = rec_cap;
-  w.base = c.take<long long>(nw);
+  w.rc = pulse_slot_bound(nw, nsamples);
+  w.yscr = c.take<double>(nsamples);
+  w.rec = c.take<PulseRec>(w.rc);
+  w.slot_off = c.take<long long>(nw);
   w.out_off = c.take<long long>(nw);
   w.parts = c.take<long long>(scan_parts_len(nw) + 1);
   w.totals = c.take<long long>(8);
+  w.cap = c.take<int32_t>(nw);
   w.count = c.take<int32_t>(nw);
-  w.deferred = c.take<int32_t>(nw);
-  w.rec = c.take<PulseRec>(rec_cap);
   *bytes = c.off + 256;
   return w;
 }
 
-__global__ void k_pulse_compact(long long nw, const long long* __restrict__ base, const int32_t* __restrict__ count,
+__global__ void k_pulse_caps(long long nw, const int32_t* __restrict__ n, int max_pulses, int32_t* __restrict__ cap) {
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+    int b = n[w] / 2 + 1;
+    cap[w] = b < max_pulses ? b : max_pulses;
+  }
+}
+
+__global__ void k_pulse_compact(long long nw, const long long* __restrict__ slot_off, const int32_t* __restrict__ count,
                                 const long long* __restrict__ out_off, const PulseRec* __restrict__ rec,
                                 CrvPulses O, long long out_cap) {
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
     int c = count[w];
-    long long o0 = out_off[w], b0 = base[w];
+    long long o0 = out_off[w], b0 = slot_off[w];
     if (o0 + c > out_cap) continue;
     for (int k = 0; k < c; ++k) {
       const PulseRec& r = rec[b0 + k];
@@ -763,19 +775,19 @@ __global__ void k_pulse_compact(long long nw, const long long* __restrict__ base
 }
 }  // namespace crv
 
-extern "C" int64_t crv_pulses_workspace(const CrvParams* p, int64_t nw, int64_t rec_cap) {
-  if (!p || nw < 0 || rec_cap < 0) return -1;
+extern "C" int64_t crv_pulses_workspace(const CrvParams* p, int64_t nw, int64_t nsamples) {
+  if (!p || nw < 0 || nsamples < 0) return -1;
   size_t b = 0;
-  pulse_layout(nullptr, nw, rec_cap, &b);
+  pulse_layout(nullptr, nw, nsamples, &b);
   return (int64_t)b;
 }
 
-extern "C" int crv_pulses(const CrvParams* p, int64_t nw, const int64_t* off, const int32_t* n,
+extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, const int64_t* off, const int32_t* n,
                           const int64_t* start_tdc, const double* ped_db, const double* area, const double* height,
-                          const int16_t* adc16, const int64_t* adc64, int32_t max_pulses, int64_t rec_cap,
-                          CrvPulses* out, int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
+                          const int16_t* adc16, const int64_t* adc64, int32_t max_pulses, CrvPulses* out,
+                          int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
                           int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
-  if (!p || !out || !n_out_dev || !status_dev || nw < 0 || rec_cap < 0 || out_cap < 0 || max_pulses < 0)
+  if (!p || !out || !n_out_dev || !status_dev || nw < 0 || nsamples < 0 || out_cap < 0 || max_pulses < 0)
     return CRV_ERR_ARG;
   if (nw > 0 && (!off || !n || !start_tdc || !ped_db || !area || !height || !wf_near || (!adc16 == !adc64)))
     return CRV_ERR_ARG;
@@ -785,23 +797,26 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, const int64_t* off, co
     return CRV_OK;
   }
   size_t need = 0;
-  pulse_layout(nullptr, nw, rec_cap, &need);
+  pulse_layout(nullptr, nw, nsamples, &need);
   if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
   Status* S = reinterpret_cast<Status*>(status_dev);
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
   size_t dummy;
-  PulseWs w = pulse_layout(base, nw, rec_cap, &dummy);
+  PulseWs w = pulse_layout(base, nw, nsamples, &dummy);
   CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
-  CK(cudaMemsetAsync(w.count, 0, sizeof(int32_t) * nw, s));
-  CK(cudaMemsetAsync(w.deferred, 0, sizeof(int32_t) * nw, s));
-  CK(cudaMemsetAsync(wf_near, 0, nw, s));
+  unsigned g = grid_for(nw, 256, 8);
+  {
+    crv::Mark mark_("k_pulse_caps", s);
+    k_pulse_caps<<<g, 256, 0, s>>>(nw, n, max_pulses, w.cap);
+  }
+  CK(exclusive_scan(w.cap, nw, Identity(), w.slot_off, &w.totals[0], w.parts, s));
   WaveIn W{nw, reinterpret_cast<const long long*>(off), n, reinterpret_cast<const long long*>(start_tdc), ped_db,
            area, height, adc16, reinterpret_cast<const long long*>(adc64)};
-  PulseOut O{w.rec, w.base, w.count, wf_near, &w.totals[0], rec_cap};
+  PulseSlots PS{w.slot_off, w.cap, w.count, wf_near, w.rec};
   if (p->precision == 1)
-    CK(launch_pulsefit<float>(*p, W, max_pulses, O, w.deferred, S, s));
+    CK(launch_pulsefit<float>(*p, W, w.yscr, max_pulses, PS, S, s));
   else
-    CK(launch_pulsefit<double>(*p, W, max_pulses, O, w.deferred, S, s));
+    CK(launch_pulsefit<double>(*p, W, w.yscr, max_pulses, PS, S, s));
   CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s));
   {
     crv::Mark mark_("k_check_caps", s);
@@ -809,7 +824,7 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, const int64_t* off, co
   }
   {
     crv::Mark mark_("k_pulse_compact", s);
-    k_pulse_compact<<<grid_for(nw, 256, 8), 256, 0, s>>>(nw, w.base, w.count, w.out_off, w.rec, *out, out_cap);
+    k_pulse_compact<<<g, 256, 0, s>>>(nw, w.slot_off, w.count, w.out_off, w.rec, *out, out_cap);
   }
   {
     crv::Mark mark_("k_copy_i64", s);

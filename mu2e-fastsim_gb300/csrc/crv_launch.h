@@ -10,7 +10,7 @@ struct SipmOut;
 struct WfGroups;
 struct DigiSlots;
 struct WaveIn;
-struct PulseOut;
+struct PulseSlots;
 
 struct DeviceInfo {
   int sms;
@@ -61,7 +61,7 @@ cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_
                             const int32_t* g_maxlen, const DigiSlots& D, Status* status, cudaStream_t s);
 
 template <typename R>
-cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, int max_pulses, const PulseOut& O, int32_t* deferred,
+cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses, const PulseSlots& S,
                             Status* status, cudaStream_t s);
 
 }  // namespace crv

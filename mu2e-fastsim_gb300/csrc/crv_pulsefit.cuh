@@ -7,11 +7,13 @@
 // (40 Levenberg-Marquardt steps, then 8 Gauss-Newton steps with halving, EDM and Hessian checks), the failed-fit
 // fallback, then the rounded fit is subtracted from every sample and the search resumes at the window end.
 //
-// GPU mapping: one warp per waveform; the waveform lives in shared memory; the peak search runs on lane 0; fit points
-// are spread over the lanes and the normal equations are warp reductions; the 3x3 solve (LU with partial pivoting)
-// and the symmetric eigenvalues (cyclic Jacobi) are FP64 on every lane.  R = double: every step in FP64; R = float
-// (mixed): residuals and Jacobians in FP32 relative to the window's first sample time, normal equations accumulated
-// in FP32, solve / acceptance / parameters / absolute times in FP64.
+// GPU mapping: one thread per waveform (FP64 throughput is scarce on this GPU, so no lane repeats another's uniform
+// work): the waveform's samples sit in a global scratch mirror (L1-resident while the lane works on it), the peak
+// search, the fit (sums sequential over the window, as the reference's contractions), the 3x3 solve (LU with partial
+// pivoting) and the symmetric eigenvalues (cyclic Jacobi) run in the lane; pulses go to per-waveform record slots
+// (rounds are bounded by half the samples).  R = double: every step in FP64; R = float (mixed): parameter mapping,
+// residuals, Jacobians and sums in FP32 relative to the window's first sample, solve / acceptance / absolute times in
+// FP64.
 #pragma once
 #include "crv_device.cuh"
 
@@ -33,15 +35,6 @@ struct WaveIn {
   const double* height;
   const int16_t* adc16;      // samples (one of adc16 / adc64)
   const long long* adc64;
-};
-
-struct PulseOut {            // per-pulse scratch records + per-waveform counts
-  PulseRec* rec;
-  long long* base;           // per waveform: first record in rec
-  int32_t* count;            // per waveform: pulses
-  uint8_t* near;             // per waveform: wf_near_threshold
-  long long* cursor;         // device record cursor
-  long long cap;             // records available
 };
 
 __device__ __forceinline__ double round_half_away(double x) {
@@ -119,85 +112,94 @@ __device__ __forceinline__ void eig3(const double M[3][3], double e[3]) {
 
 struct Fit3 {
   double lo[3], hi[3], half[3];
-  double t0;                 // time origin of the FP32 evaluation
+  double t0;                 // time origin of the FP32 evaluation (first window sample)
 };
 
-// residuals + normal equations at internal parameters u over the P window points yw[0..P) whose times are
-// (tdc_fs + i) * period (lanes split the points)
+// One lane's fit: residuals / normal equations at internal parameters u over the window points yw[0..P), times
+// (tdc_fs + i) * period.  Sums are sequential over the points (the reference's contractions are sequential).
+// R = double: every operation in FP64; R = float: mapping, residuals and sums in FP32 relative to the window start.
 template <typename R>
-__device__ __forceinline__ void evaluate(const Fit3& F, const double u[3], const double* yw, long long tdc_fs,
-                                         double period, int P, double* chi2, double H[3][3], double g[3]) {
-  double p[3], d[3];
-  for (int k = 0; k < 3; ++k) {
-    p[k] = F.lo[k] + (F.hi[k] - F.lo[k]) * (sin(u[k]) + 1.0) * 0.5;
-    d[k] = F.half[k] * cos(u[k]);
+__device__ __forceinline__ void eval_lane(const Fit3& F, const double u[3], const double* yw, long long tdc_fs,
+                                          double period, int P, double* chi2, double H[6], double g[3]) {
+  R A, mu, b, d0, d1, d2;
+  if (sizeof(R) == 8) {
+    double p0 = F.lo[0] + (F.hi[0] - F.lo[0]) * (sin(u[0]) + 1.0) * 0.5;
+    double p1 = F.lo[1] + (F.hi[1] - F.lo[1]) * (sin(u[1]) + 1.0) * 0.5;
+    double p2 = F.lo[2] + (F.hi[2] - F.lo[2]) * (sin(u[2]) + 1.0) * 0.5;
+    A = R(p0); mu = R(p1); b = R(p2);
+    d0 = R(F.half[0] * cos(u[0])); d1 = R(F.half[1] * cos(u[1])); d2 = R(F.half[2] * cos(u[2]));
+  } else {
+    float s0, c0, s1, c1, s2, c2;
+    sincosf(float(u[0]), &s0, &c0);
+    sincosf(float(u[1]), &s1, &c1);
+    sincosf(float(u[2]), &s2, &c2);
+    A = R(F.lo[0]) + R(F.hi[0] - F.lo[0]) * (s0 + 1.0f) * 0.5f;
+    mu = R(F.lo[1] - F.t0) + R(F.hi[1] - F.lo[1]) * (s1 + 1.0f) * 0.5f;
+    b = R(F.lo[2]) + R(F.hi[2] - F.lo[2]) * (s2 + 1.0f) * 0.5f;
+    d0 = R(F.half[0]) * c0; d1 = R(F.half[1]) * c1; d2 = R(F.half[2]) * c2;
   }
-  R A = R(p[0]), b = R(p[2]);
-  R mu = sizeof(R) == 8 ? R(p[1]) : R(p[1] - F.t0);
-  R s_c = 0, s00 = 0, s01 = 0, s02 = 0, s11 = 0, s12 = 0, s22 = 0, s0 = 0, s1 = 0, s2 = 0;
-  for (int i = lane_id(); i < P; i += 32) {
-    R t = sizeof(R) == 8 ? R(double(tdc_fs + i) * period) : R(double(i) * period);
+  R c = 0, h00 = 0, h01 = 0, h02 = 0, h11 = 0, h12 = 0, h22 = 0, g0 = 0, g1 = 0, g2 = 0;
+  for (int i = 0; i < P; ++i) {
+    R t = sizeof(R) == 8 ? R(double(tdc_fs + i) * period) : R(float(i) * float(period));
     R z = (t - mu) / b;
-    R ez = sizeof(R) == 8 ? R(exp(double(-z))) : R(__expf(float(-z)));
-    R gg = sizeof(R) == 8 ? R(exp(double(-z - ez))) : R(__expf(float(-z - ez)));
+    R ez, gg;
+    if (sizeof(R) == 8) { ez = R(exp(double(-z))); gg = R(exp(double(-z - ez))); }
+    else { ez = R(__expf(float(-z))); gg = R(__expf(float(-z - ez))); }
     R f = A * gg;
     R r = R(yw[i]) - f;
     R fz = f * (ez - R(1));
-    R j0 = gg * R(d[0]);
-    R j1 = fz * (R(-1) / b) * R(d[1]);
-    R j2 = fz * (-z / b) * R(d[2]);
-    s_c += r * r;
-    s00 += j0 * j0; s01 += j0 * j1; s02 += j0 * j2;
-    s11 += j1 * j1; s12 += j1 * j2; s22 += j2 * j2;
-    s0 += j0 * r; s1 += j1 * r; s2 += j2 * r;
+    R j0 = gg * d0;
+    R j1 = fz * (R(-1) / b) * d1;
+    R j2 = fz * (-z / b) * d2;
+    c += r * r;
+    h00 += j0 * j0; h01 += j0 * j1; h02 += j0 * j2;
+    h11 += j1 * j1; h12 += j1 * j2; h22 += j2 * j2;
+    g0 += j0 * r; g1 += j1 * r; g2 += j2 * r;
   }
-  double v[10] = {double(s_c), double(s00), double(s01), double(s02), double(s11), double(s12), double(s22),
-                  double(s0), double(s1), double(s2)};
-#pragma unroll
-  for (int k = 0; k < 10; ++k) v[k] = warp_sum(v[k]);
-  *chi2 = v[0];
-  H[0][0] = v[1]; H[0][1] = H[1][0] = v[2]; H[0][2] = H[2][0] = v[3];
-  H[1][1] = v[4]; H[1][2] = H[2][1] = v[5]; H[2][2] = v[6];
-  g[0] = v[7]; g[1] = v[8]; g[2] = v[9];
+  *chi2 = double(c);
+  H[0] = double(h00); H[1] = double(h01); H[2] = double(h02); H[3] = double(h11); H[4] = double(h12);
+  H[5] = double(h22);
+  g[0] = double(g0); g[1] = double(g1); g[2] = double(g2);
 }
 
-// bounded Gumbel fit; returns params, chi2, converged, hessian_ok
+__device__ __forceinline__ void sym3(const double H[6], double M[3][3]) {
+  M[0][0] = H[0]; M[0][1] = M[1][0] = H[1]; M[0][2] = M[2][0] = H[2];
+  M[1][1] = H[3]; M[1][2] = M[2][1] = H[4]; M[2][2] = H[5];
+}
+
+// bounded Gumbel fit of one lane (40 LM steps, 8 Gauss-Newton steps with halving, EDM + Hessian checks)
 template <typename R>
-__device__ void fit_gumbel(const Fit3& F, const double p0[3], const double* yw, long long tdc_fs, double period, int P,
-                           int iters, double par[3], double* chi2_out, bool* conv, bool* hok) {
+__device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, long long tdc_fs, double period, int P,
+                         int iters, double par[3], double* chi2_out, bool* conv, bool* hok) {
   double u[3];
   for (int k = 0; k < 3; ++k) {
     double c = 2.0 * (p0[k] - F.lo[k]) / (F.hi[k] - F.lo[k]) - 1.0;
-    c = fmin(fmax(c, -1.0), 1.0);
-    u[k] = asin(c);
+    u[k] = asin(fmin(fmax(c, -1.0), 1.0));
   }
-  double chi2, H[3][3], g[3];
-  evaluate<R>(F, u, yw, tdc_fs, period, P, &chi2, H, g);
+  double chi2, H[6], g[3];
+  eval_lane<R>(F, u, yw, tdc_fs, period, P, &chi2, H, g);
   double lam = 1e-3;
   for (int it = 0; it < iters; ++it) {
-    double Aug[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) Aug[i][j] = H[i][j];
-    for (int i = 0; i < 3; ++i) Aug[i][i] = H[i][i] + lam * (H[i][i] + 1e-12);
+    double M[3][3];
+    sym3(H, M);
+    for (int i = 0; i < 3; ++i) M[i][i] = M[i][i] + lam * (M[i][i] + 1e-12);
     double du[3];
-    if (!solve3(Aug, g, du)) du[0] = du[1] = du[2] = 0.0;
+    if (!solve3(M, g, du)) du[0] = du[1] = du[2] = 0.0;
     double un[3] = {u[0] + du[0], u[1] + du[1], u[2] + du[2]};
-    double c2, Hn[3][3], gn[3];
-    evaluate<R>(F, un, yw, tdc_fs, period, P, &c2, Hn, gn);
+    double c2, Hn[6], gn[3];
+    eval_lane<R>(F, un, yw, tdc_fs, period, P, &c2, Hn, gn);
     bool better = c2 < chi2;
     if (better) {
       for (int k = 0; k < 3; ++k) { u[k] = un[k]; g[k] = gn[k]; }
-      for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) H[i][j] = Hn[i][j];
+      for (int k = 0; k < 6; ++k) H[k] = Hn[k];
       chi2 = c2;
     }
-    lam = better ? lam * 0.3 : lam * 10.0;
-    lam = fmin(fmax(lam, 1e-9), 1e9);
+    lam = fmin(fmax(better ? lam * 0.3 : lam * 10.0, 1e-9), 1e9);
   }
   for (int it = 0; it < 8; ++it) {
     double M[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) M[i][j] = H[i][j] + (i == j ? 1e-12 : 0.0);
+    sym3(H, M);
+    for (int i = 0; i < 3; ++i) M[i][i] += 1e-12;
     double du[3];
     if (!solve3(M, g, du)) break;
     for (int k = 0; k < 3; ++k)
@@ -205,27 +207,27 @@ __device__ void fit_gumbel(const Fit3& F, const double p0[3], const double* yw, 
     for (int sc = 0; sc < 4; ++sc) {
       double s = sc == 0 ? 1.0 : (sc == 1 ? 0.5 : (sc == 2 ? 0.25 : 0.125));
       double un[3] = {u[0] + s * du[0], u[1] + s * du[1], u[2] + s * du[2]};
-      double c2, Hn[3][3], gn[3];
-      evaluate<R>(F, un, yw, tdc_fs, period, P, &c2, Hn, gn);
+      double c2, Hn[6], gn[3];
+      eval_lane<R>(F, un, yw, tdc_fs, period, P, &c2, Hn, gn);
       if (c2 < chi2) {
         for (int k = 0; k < 3; ++k) { u[k] = un[k]; g[k] = gn[k]; }
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j) H[i][j] = Hn[i][j];
+        for (int k = 0; k < 6; ++k) H[k] = Hn[k];
         chi2 = c2;
-        break;                 // the accepted step zeroes du: later scales re-evaluate the same point
+        break;                 // the accepted step zeroes du: later scales would re-evaluate the same point
       }
     }
   }
   double M[3][3];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) M[i][j] = H[i][j] + (i == j ? 1e-12 : 0.0);
+  sym3(H, M);
+  for (int i = 0; i < 3; ++i) M[i][i] += 1e-12;
   double st[3];
   double edm;
   bool okh;
   if (solve3(M, g, st)) {
     edm = 0.5 * (g[0] * st[0] + g[1] * st[1] + g[2] * st[2]);
-    double e[3];
-    eig3(H, e);
+    double Hm[3][3], e[3];
+    sym3(H, Hm);
+    eig3(Hm, e);
     okh = e[0] > 1e-12 * fmax(e[2], 1e-300);
   } else {
     edm = INFINITY;
@@ -237,117 +239,113 @@ __device__ void fit_gumbel(const Fit3& F, const double p0[3], const double* yw, 
   *chi2_out = chi2;
 }
 
-// near-threshold local maximum among samples [a, b] (inclusive range of candidate positions)
-__device__ __forceinline__ bool near_threshold_any(const double* y, int n, int a, int b, double thr, double edge) {
-  bool any = false;
+// near-threshold local maximum among positions [a, b]
+__device__ __forceinline__ bool near_lane(const double* y, int n, int a, int b, double thr, double edge) {
   if (a < 0) a = 0;
   if (b > n - 1) b = n - 1;
-  for (int base = a; base <= b; base += 32) {
-    int i = base + lane_id();
-    bool hit = false;
-    if (i <= b) {
-      double left = i > 0 ? y[i - 1] : -1e9;
-      double right = i + 1 < n ? y[i + 1] : -1e9;
-      hit = (y[i] >= left) && (y[i] > right) && (fabs(y[i] - thr) <= edge);
-    }
-    any |= __any_sync(0xffffffffu, hit);
+  for (int i = a; i <= b; ++i) {
+    double left = i > 0 ? y[i - 1] : -1e9;
+    double right = i + 1 < n ? y[i + 1] : -1e9;
+    if (y[i] >= left && y[i] > right && fabs(y[i] - thr) <= edge) return true;
   }
-  return any;
+  return false;
 }
 
-// FindNextPeak (lane 0) + fit window; results broadcast to the warp
-__device__ __forceinline__ bool next_peak(const CrvParams& p, const double* y, int n, int start, int* ps_o, int* pe_o,
+// FindNextPeak + fit window of one lane
+__device__ __forceinline__ bool peak_lane(const CrvParams& p, const double* y, int n, int start, int* ps_o, int* pe_o,
                                           int* fs_o, int* fe_o) {
-  int found = 0, ps = 0, pe = 0, fs = 0, fe = 0;
-  if (lane_id() == 0) {
-    bool rising = false;
-    for (int b = (start + 1 > 1 ? start + 1 : 1); b < n; ++b) {
-      double prev = y[b - 1], cur = y[b];
-      if (prev < cur) { rising = true; ps = b; pe = b; }
-      else if (prev == cur) { if (rising) pe = b; }
-      else if (rising) {
-        if (y[pe] > p.min_adc_difference) { found = 1; break; }
-        rising = false;
-      }
-    }
-    if (found) {
-      fs = ps - 1;
-      fe = pe + 1;
-      for (int k = 1; k <= p.samples_before; ++k) {
-        int i = ps - k;
-        if (i < 0) break;
-        if (!(y[i] <= y[i + 1])) break;
-        fs = i;
-        if (i == 0) break;
-      }
-      for (int k = 1; k <= p.samples_after; ++k) {
-        int i = pe + k;
-        if (i >= n) break;
-        if (!(y[i - 1] >= y[i])) break;
-        fe = i;
-      }
-      if (ps - fs > 1) fs += 1;
-      if (fe - pe > 1) fe -= 1;
+  bool rising = false, found = false;
+  int ps = 0, pe = 0;
+  for (int b = (start + 1 > 1 ? start + 1 : 1); b < n; ++b) {
+    double prev = y[b - 1], cur = y[b];
+    if (prev < cur) { rising = true; ps = b; pe = b; }
+    else if (prev == cur) { if (rising) pe = b; }
+    else if (rising) {
+      if (y[pe] > p.min_adc_difference) { found = true; break; }
+      rising = false;
     }
   }
-  found = __shfl_sync(0xffffffffu, found, 0);
-  *ps_o = __shfl_sync(0xffffffffu, ps, 0);
-  *pe_o = __shfl_sync(0xffffffffu, pe, 0);
-  *fs_o = __shfl_sync(0xffffffffu, fs, 0);
-  *fe_o = __shfl_sync(0xffffffffu, fe, 0);
-  return found != 0;
+  if (!found) return false;
+  int fs = ps - 1, fe = pe + 1;
+  for (int k = 1; k <= p.samples_before; ++k) {
+    int i = ps - k;
+    if (i < 0 || !(y[i] <= y[i + 1])) break;
+    fs = i;
+    if (i == 0) break;
+  }
+  for (int k = 1; k <= p.samples_after; ++k) {
+    int i = pe + k;
+    if (i >= n || !(y[i - 1] >= y[i])) break;
+    fe = i;
+  }
+  if (ps - fs > 1) fs += 1;
+  if (fe - pe > 1) fe -= 1;
+  *ps_o = ps; *pe_o = pe; *fs_o = fs; *fe_o = fe;
+  return true;
 }
 
-constexpr int PF_WARPS = 8;
+struct PulseSlots {
+  const long long* off;      // per waveform: first record slot
+  const int32_t* cap;        // per waveform: slots (rounds bound)
+  int32_t* count;            // per waveform: pulses
+  uint8_t* near;             // per waveform: wf_near_threshold
+  PulseRec* rec;
+};
 
-__host__ __device__ inline size_t pulsefit_smem_per_warp(int cap, int pcap) {
-  return size_t(cap) * 8 + size_t(pcap) * sizeof(PulseRec);
-}
-
-// second_pass == 0: every waveform with n <= cap whose pulses fit pcap records; others are deferred.
-// second_pass == 1: only deferred waveforms; what still does not fit is reported (CRV_ST_CAPACITY).
+// subtract round(fit) from the samples it reaches: walk out from the mode while the rounded value can be non-zero
 template <typename R>
-__global__ void __launch_bounds__(PF_WARPS * 32) k_pulsefit(CrvParams p, WaveIn W, int cap, int pcap, int second_pass,
-                                                          int max_pulses, PulseOut O, int32_t* __restrict__ deferred,
-                                                          Status* status) {
-  extern __shared__ __align__(16) char smem[];
-  char* base = smem + size_t(warp_in_block()) * pulsefit_smem_per_warp(cap, pcap);
-  double* y = reinterpret_cast<double*>(base);
-  PulseRec* rec = reinterpret_cast<PulseRec*>(base + size_t(cap) * 8);
-  const double E = 2.718281828459045;
-  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long w = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); w < W.nw; w += warps) {
-    if (second_pass && !deferred[w]) continue;
-    int n = W.n[w];
-    if (n > cap) {
-      if (lane_id() == 0) {
-        if (second_pass) {
-          set_flag(status, CRV_ST_CAPACITY);
-          need_at_least(status, CRV_NEED_SAMPLES, n);
-          O.count[w] = 0;
-        } else {
-          deferred[w] = 1;
-        }
+__device__ __forceinline__ void subtract_lane(const CrvParams& p, double* y, int n, long long st_tdc, double A,
+                                              double mu, double b, int* lo_o, int* hi_o) {
+  long long im = (long long)floor(mu / p.period) - st_tdc;
+  if (im < 0) im = 0;
+  if (im > n - 1) im = n - 1;
+  int lo = int(im), hi = int(im);
+  for (int dir = -1; dir <= 1; dir += 2) {
+    for (int i = int(im) + (dir > 0 ? 1 : 0); i >= 0 && i < n; i += dir) {
+      double gv;
+      if (sizeof(R) == 8) {
+        double t = double(st_tdc + i) * p.period;
+        double z = (t - mu) / b;
+        gv = A * exp(-z - exp(-z));
+      } else {
+        float z = float(double(st_tdc + i) * p.period - mu) / float(b);
+        gv = double(float(A) * __expf(-z - __expf(-z)));
       }
-      continue;
+      y[i] -= round_half_away(gv);
+      if (dir < 0) lo = i; else hi = i;
+      // unimodal: past the mode the value only shrinks; stop well below the rounding threshold
+      if (fabs(gv) < 0.25 && ((dir < 0 && double(st_tdc + i) * p.period < mu) ||
+                              (dir > 0 && double(st_tdc + i) * p.period > mu)))
+        break;
     }
+  }
+  *lo_o = lo;
+  *hi_o = hi;
+}
+
+// one thread per waveform
+template <typename R>
+__global__ void __launch_bounds__(128) k_pulsefit(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
+                                                 PulseSlots S, Status* status) {
+  const double E = 2.718281828459045;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < W.nw;
+       w += (long long)gridDim.x * blockDim.x) {
+    int n = W.n[w];
     long long off = W.off[w];
+    double* y = yscr + off;
     double pdb = W.ped_db[w];
     double x0 = n > 0 ? (W.adc16 ? double(W.adc16[off]) : double(W.adc64[off])) : 0.0;
     bool under = (n > 0) && (pdb - x0 > p.pedestal_undershoot);
     double ped = under ? x0 : pdb;
-    for (int i = lane_id(); i < n; i += 32) {
-      double a = W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i]);
-      y[i] = a - ped;
-    }
-    __syncwarp();
-    bool near = near_threshold_any(y, n, 0, n - 1, p.min_adc_difference, p.knife_edge_adc);
+    for (int i = 0; i < n; ++i) y[i] = (W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i])) - ped;
+    bool near = near_lane(y, n, 0, n - 1, p.min_adc_difference, p.knife_edge_adc);
     long long st_tdc = W.start_tdc[w];
-    int start = 0, npulse = 0;
+    int start = 0, cnt = 0, cap = S.cap[w];
+    long long slot = S.off[w];
     bool failed_before = false;
     for (int seq = 0; seq < max_pulses; ++seq) {
       int ps, pe, fs, fe;
-      if (!next_peak(p, y, n, start, &ps, &pe, &fs, &fe)) break;
+      if (!peak_lane(p, y, n, start, &ps, &pe, &fs, &fe)) break;
       int P = fe - fs + 1;
       double yps = y[ps];
       double t_ps = double(st_tdc + ps) * p.period;
@@ -362,7 +360,7 @@ __global__ void __launch_bounds__(PF_WARPS * 32) k_pulsefit(CrvParams p, WaveIn 
       double p0[3] = {yps * E, t_peak, p.default_beta};
       double par[3], chi2;
       bool conv, hok;
-      fit_gumbel<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
+      fit_lane<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
       int ndf = P - 3;
       bool nearlim = false;
       for (int k = 0; k < 3; ++k) {
@@ -376,8 +374,8 @@ __global__ void __launch_bounds__(PF_WARPS * 32) k_pulsefit(CrvParams p, WaveIn 
       double beta = failed ? p.default_beta : b;
       double tp = failed ? t_peak : mu;
       bool fseq = failed || failed_before;
-      if (lane_id() == 0 && npulse < pcap) {
-        PulseRec& r = rec[npulse];
+      if (cnt < cap) {
+        PulseRec& r = S.rec[slot + cnt];
         r.pe = (failed ? yps * E * p.default_beta : A * b) / W.area[w];
         r.peph = height / W.height[w];
         r.time = tp;
@@ -390,53 +388,16 @@ __global__ void __launch_bounds__(PF_WARPS * 32) k_pulsefit(CrvParams p, WaveIn 
         r.seq = seq;
         r.failed = fseq; r.zerondf = ndf <= 0; r.pedfromdb = !under; r.pad = 0;
       }
-      ++npulse;
+      ++cnt;
       failed_before = fseq;
-      for (int i = lane_id(); i < n; i += 32) {
-        double t = double(st_tdc + i) * p.period;
-        double z = (t - mu) / b;
-        double gv = A * exp(-z - exp(-z));
-        y[i] -= round_half_away(gv);
-      }
-      __syncwarp();
-      near = near_threshold_any(y, n, 0, n - 1, p.min_adc_difference, p.knife_edge_adc) || near;
+      int lo, hi;
+      subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
+      near = near || near_lane(y, n, lo - 1, hi + 1, p.min_adc_difference, p.knife_edge_adc);
       start = fe;
     }
-    if (npulse > pcap) {
-      if (lane_id() == 0) {
-        if (second_pass) {
-          set_flag(status, CRV_ST_CAPACITY);
-          need_at_least(status, CRV_NEED_PULSES, npulse);
-          O.count[w] = 0;
-        } else {
-          deferred[w] = 1;
-        }
-      }
-      __syncwarp();
-      continue;
-    }
-    long long bse = 0;
-    if (lane_id() == 0) bse = (long long)atomicAdd(reinterpret_cast<unsigned long long*>(O.cursor),
-                                                  (unsigned long long)npulse);
-    bse = __shfl_sync(0xffffffffu, bse, 0);
-    if (bse + npulse > O.cap) {
-      if (lane_id() == 0) {
-        set_flag(status, CRV_ST_CAPACITY);
-        need_at_least(status, CRV_NEED_PULSES_OUT, bse + npulse);
-        O.count[w] = 0;
-        O.near[w] = near;
-        if (second_pass) deferred[w] = 0;
-      }
-      continue;
-    }
-    for (int k = lane_id(); k < npulse; k += 32) O.rec[bse + k] = rec[k];
-    if (lane_id() == 0) {
-      O.base[w] = bse;
-      O.count[w] = npulse;
-      O.near[w] = near;
-      if (second_pass) deferred[w] = 0;
-    }
-    __syncwarp();
+    S.count[w] = cnt;
+    S.near[w] = near;
+    if (cnt > cap) set_flag(status, CRV_ST_LIMIT);
   }
 }
 
