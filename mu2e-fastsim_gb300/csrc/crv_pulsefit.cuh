@@ -76,6 +76,41 @@ __device__ __forceinline__ bool solve3(const double M[3][3], const double r[3], 
   return true;
 }
 
+// FP64 reciprocal from an FP32 seed and two Newton steps (24 -> 48 -> 96 bits): one FP32 MUFU op and four FP64
+// FMAs instead of an FP64 division
+__device__ __forceinline__ double rcp64(double d) {
+  double r = double(__frcp_rn(float(d)));
+  if (!(fabs(r) < 1e300) || r == 0.0) return 1.0 / d;       // outside the FP32 range: plain division
+  r = r * (2.0 - d * r);
+  r = r * (2.0 - d * r);
+  return r;
+}
+
+// 3x3 solve by the adjugate (FP32-mixed fits): one reciprocal of the determinant
+__device__ __forceinline__ bool solve3_adj(const double M[3][3], const double b[3], double x[3]) {
+  double c00 = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+  double c01 = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+  double c02 = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+  double det = M[0][0] * c00 + M[0][1] * c01 + M[0][2] * c02;
+  if (det == 0.0 || !isfinite(det)) return false;
+  double c10 = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+  double c11 = M[0][0] * M[2][2] - M[0][2] * M[2][0];
+  double c12 = M[0][1] * M[2][0] - M[0][0] * M[2][1];
+  double c20 = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+  double c21 = M[0][2] * M[1][0] - M[0][0] * M[1][2];
+  double c22 = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+  double inv = rcp64(det);
+  x[0] = (c00 * b[0] + c10 * b[1] + c20 * b[2]) * inv;
+  x[1] = (c01 * b[0] + c11 * b[1] + c21 * b[2]) * inv;
+  x[2] = (c02 * b[0] + c12 * b[1] + c22 * b[2]) * inv;
+  return true;
+}
+
+template <typename R>
+__device__ __forceinline__ bool solve3_p(const double M[3][3], const double b[3], double x[3]) {
+  return sizeof(R) == 8 ? solve3(M, b, x) : solve3_adj(M, b, x);
+}
+
 // eigenvalues of a symmetric 3x3 matrix (cyclic Jacobi), ascending
 __device__ __forceinline__ void eig3(const double M[3][3], double e[3]) {
   double a[3][3];
@@ -184,7 +219,7 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, lo
     sym3(H, M);
     for (int i = 0; i < 3; ++i) M[i][i] = M[i][i] + lam * (M[i][i] + 1e-12);
     double du[3];
-    if (!solve3(M, g, du)) du[0] = du[1] = du[2] = 0.0;
+    if (!solve3_p<R>(M, g, du)) du[0] = du[1] = du[2] = 0.0;
     double un[3] = {u[0] + du[0], u[1] + du[1], u[2] + du[2]};
     double c2, Hn[6], gn[3];
     eval_lane<R>(F, un, yw, tdc_fs, period, P, &c2, Hn, gn);
@@ -201,7 +236,7 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, lo
     sym3(H, M);
     for (int i = 0; i < 3; ++i) M[i][i] += 1e-12;
     double du[3];
-    if (!solve3(M, g, du)) break;
+    if (!solve3_p<R>(M, g, du)) break;
     for (int k = 0; k < 3; ++k)
       if (!isfinite(du[k])) du[k] = 0.0;
     for (int sc = 0; sc < 4; ++sc) {
@@ -223,7 +258,7 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, lo
   double st[3];
   double edm;
   bool okh;
-  if (solve3(M, g, st)) {
+  if (solve3_p<R>(M, g, st)) {
     edm = 0.5 * (g[0] * st[0] + g[1] * st[1] + g[2] * st[2]);
     double Hm[3][3], e[3];
     sym3(H, Hm);

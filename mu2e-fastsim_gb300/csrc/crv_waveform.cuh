@@ -66,13 +66,20 @@ __device__ __forceinline__ long long first_sample(const CrvParams& p, double t, 
   return v > 0.0f ? (long long)v : 0;
 }
 
+// x / d, exactly: a multiplication by 1/d when d is a power of two (the quotient rounds identically), else a division
+__device__ __forceinline__ double exact_div(double x, double d) {
+  int e;
+  double m = frexp(d, &e);
+  return m == 0.5 ? x * ldexp(1.0, 1 - e) : x / d;
+}
+
 // template index of sample J for a charge at t (returns -1 when the pair does not contribute)
 template <typename R>
 __device__ __forceinline__ int tmpl_index(const CrvParams& p, long long J, double t, double ts, int tlen) {
   if (sizeof(R) == 8) {
     double st = double(J) * p.period + ts - t;
     if (!(st >= 0.0)) return -1;
-    double ti = rint(st / p.spe_precision);
+    double ti = rint(exact_div(st, p.spe_precision));
     return ti < double(tlen) ? int(ti) : -1;
   }
   float st = float(J) * float(p.period) - float(t - ts);
@@ -172,6 +179,13 @@ __global__ void k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G, const doub
   }
 }
 
+constexpr int WF_QSTAGE = 512;    // charges of a cluster staged in shared memory (larger clusters: on the fly)
+
+template <typename R>
+__host__ __device__ inline size_t wf_smem_per_warp(int cap) {
+  return (size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * (sizeof(R) + 4) + 15) & ~size_t(15);
+}
+
 __device__ __forceinline__ int16_t adc_of(const CrvParams& p, double v) {
   double x = v * p.adc_conversion + double(p.adc_pedestal) + 0.5;
   long long i;
@@ -194,7 +208,10 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
                                                   const int32_t* __restrict__ g_maxlen, int lo, int cap,
                                                   int last_pass, DigiSlots D, Status* status) {
   extern __shared__ __align__(16) char smem[];
-  R* wave = reinterpret_cast<R*>(smem) + size_t(warp_in_block()) * cap;
+  char* wbase = smem + size_t(warp_in_block()) * wf_smem_per_warp<R>(cap);
+  R* wave = reinterpret_cast<R*>(wbase);
+  R* qn_s = reinterpret_cast<R*>(wbase + size_t(cap) * sizeof(R));
+  int32_t* j0_s = reinterpret_cast<int32_t*>(wbase + size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * sizeof(R));
   __shared__ double vmax_s;
   if (threadIdx.x < 32) {
     double v = -1e300;
@@ -238,24 +255,36 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
       double k0 = ceil((t[a] - p.period - tdc0) / p.period);
       double ts = k0 * p.period + tdc0;
       int L = cluster_length<R>(p, t, a, b, ts, tlen, true);
+      // stage each charge's first reached sample and normalised charge (once per charge, not per sample)
+      const bool staged = (b - a) <= WF_QSTAGE;
+      if (staged) {
+        const R inv_q = R(1.0 / p.spe_ref_charge);
+        for (int q = a + lane_id(); q < b; q += 32) {
+          j0_s[q - a] = int32_t(first_sample<R>(p, t[q], ts));
+          qn_s[q - a] = sizeof(R) == 8 ? R(qc[q] / p.spe_ref_charge) : R(qc[q]) * inv_q;
+        }
+        __syncwarp();
+      }
       // samples: sum of the charges reaching each sample, in charge order
       for (int j = lane_id(); j < L; j += 32) {
         // charges with first_sample in (j - nr, j]: first_sample is non-decreasing along the cluster
         int lo_q = a, hi_q = b;                      // first charge with first_sample > j - nr
         while (lo_q < hi_q) {
           int m = (lo_q + hi_q) >> 1;
-          if (first_sample<R>(p, t[m], ts) > (long long)j - nr) hi_q = m; else lo_q = m + 1;
+          long long fm = staged ? (long long)j0_s[m - a] : first_sample<R>(p, t[m], ts);
+          if (fm > (long long)j - nr) hi_q = m; else lo_q = m + 1;
         }
         int q1 = lo_q;
         int lo2 = q1, hi2 = b;                       // first charge with first_sample > j
         while (lo2 < hi2) {
           int m = (lo2 + hi2) >> 1;
-          if (first_sample<R>(p, t[m], ts) > (long long)j) hi2 = m; else lo2 = m + 1;
+          long long fm = staged ? (long long)j0_s[m - a] : first_sample<R>(p, t[m], ts);
+          if (fm > (long long)j) hi2 = m; else lo2 = m + 1;
         }
         R acc = R(0);
         for (int q = q1; q < lo2; ++q) {
           int ti = tmpl_index<R>(p, j, t[q], ts, tlen);
-          if (ti >= 0) acc += R(tmpl[ti]) * R(qc[q] / p.spe_ref_charge);
+          if (ti >= 0) acc += R(tmpl[ti]) * (staged ? qn_s[q - a] : R(qc[q] / p.spe_ref_charge));
         }
         if (p.noise_on) {
           long long tk = (long long)k0 + j;
