@@ -154,7 +154,7 @@ struct Fit3 {
 // (tdc_fs + i) * period.  Sums are sequential over the points (the reference's contractions are sequential).
 // R = double: every operation in FP64; R = float: mapping, residuals and sums in FP32 relative to the window start.
 template <typename R>
-__device__ __forceinline__ void eval_lane(const Fit3& F, const double u[3], const double* yw, long long tdc_fs,
+__device__ __forceinline__ void eval_lane(const Fit3& F, const double u[3], const R* yw, long long tdc_fs,
                                           double period, int P, double* chi2, double H[6], double g[3]) {
   R A, mu, b, d0, d1, d2;
   if (sizeof(R) == 8) {
@@ -204,7 +204,7 @@ __device__ __forceinline__ void sym3(const double H[6], double M[3][3]) {
 
 // bounded Gumbel fit of one lane (40 LM steps, 8 Gauss-Newton steps with halving, EDM + Hessian checks)
 template <typename R>
-__device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, long long tdc_fs, double period, int P,
+__device__ void fit_lane(const Fit3& F, const double p0[3], const R* yw, long long tdc_fs, double period, int P,
                          int iters, double par[3], double* chi2_out, bool* conv, bool* hok) {
   double u[3];
   for (int k = 0; k < 3; ++k) {
@@ -275,28 +275,32 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const double* yw, lo
 }
 
 // near-threshold local maximum among positions [a, b]
-__device__ __forceinline__ bool near_lane(const double* y, int n, int a, int b, double thr, double edge) {
+template <typename Y>
+__device__ __forceinline__ bool near_lane(const Y* y, int n, int a, int b, Y thr, Y edge) {
   if (a < 0) a = 0;
   if (b > n - 1) b = n - 1;
   for (int i = a; i <= b; ++i) {
-    double left = i > 0 ? y[i - 1] : -1e9;
-    double right = i + 1 < n ? y[i + 1] : -1e9;
-    if (y[i] >= left && y[i] > right && fabs(y[i] - thr) <= edge) return true;
+    Y left = i > 0 ? y[i - 1] : Y(-1e9);
+    Y right = i + 1 < n ? y[i + 1] : Y(-1e9);
+    Y d = y[i] - thr;
+    if (y[i] >= left && y[i] > right && (d < Y(0) ? -d : d) <= edge) return true;
   }
   return false;
 }
 
 // FindNextPeak + fit window of one lane
-__device__ __forceinline__ bool peak_lane(const CrvParams& p, const double* y, int n, int start, int* ps_o, int* pe_o,
+template <typename Y>
+__device__ __forceinline__ bool peak_lane(const CrvParams& p, const Y* y, int n, int start, int* ps_o, int* pe_o,
                                           int* fs_o, int* fe_o) {
   bool rising = false, found = false;
   int ps = 0, pe = 0;
+  const Y thr = Y(p.min_adc_difference);
   for (int b = (start + 1 > 1 ? start + 1 : 1); b < n; ++b) {
-    double prev = y[b - 1], cur = y[b];
+    Y prev = y[b - 1], cur = y[b];
     if (prev < cur) { rising = true; ps = b; pe = b; }
     else if (prev == cur) { if (rising) pe = b; }
     else if (rising) {
-      if (y[pe] > p.min_adc_difference) { found = true; break; }
+      if (y[pe] > thr) { found = true; break; }
       rising = false;
     }
   }
@@ -327,31 +331,40 @@ struct PulseSlots {
   PulseRec* rec;
 };
 
+__device__ __forceinline__ float round_half_away_f(float x) {
+  float a = floorf(fabsf(x) + 0.5f);
+  return x < 0.0f ? -a : (x > 0.0f ? a : 0.0f * x);
+}
+
 // subtract round(fit) from the samples it reaches: walk out from the mode while the rounded value can be non-zero
 template <typename R>
-__device__ __forceinline__ void subtract_lane(const CrvParams& p, double* y, int n, long long st_tdc, double A,
+__device__ __forceinline__ void subtract_lane(const CrvParams& p, R* y, int n, long long st_tdc, double A,
                                               double mu, double b, int* lo_o, int* hi_o) {
   long long im = (long long)floor(mu / p.period) - st_tdc;
   if (im < 0) im = 0;
   if (im > n - 1) im = n - 1;
   int lo = int(im), hi = int(im);
+  // FP32: sample times relative to the mode's sample (exact small multiples of the period)
+  const float mu_rel = float(mu - double(st_tdc + im) * p.period);
+  const float inv_b = 1.0f / float(b), Af = float(A), Pf = float(p.period);
   for (int dir = -1; dir <= 1; dir += 2) {
     for (int i = int(im) + (dir > 0 ? 1 : 0); i >= 0 && i < n; i += dir) {
-      double gv;
       if (sizeof(R) == 8) {
         double t = double(st_tdc + i) * p.period;
         double z = (t - mu) / b;
-        gv = A * exp(-z - exp(-z));
+        double gv = A * exp(-z - exp(-z));
+        y[i] -= R(round_half_away(gv));
+        if (dir < 0) lo = i; else hi = i;
+        // unimodal: past the mode the value only shrinks; stop well below the rounding threshold
+        if (fabs(gv) < 0.25 && ((dir < 0 && t < mu) || (dir > 0 && t > mu))) break;
       } else {
-        float z = float(double(st_tdc + i) * p.period - mu) / float(b);
-        gv = double(float(A) * __expf(-z - __expf(-z)));
+        float tr = float(i - int(im)) * Pf;
+        float z = (tr - mu_rel) * inv_b;
+        float gv = Af * __expf(-z - __expf(-z));
+        y[i] -= R(round_half_away_f(gv));
+        if (dir < 0) lo = i; else hi = i;
+        if (fabsf(gv) < 0.25f && ((dir < 0 && tr < mu_rel) || (dir > 0 && tr > mu_rel))) break;
       }
-      y[i] -= round_half_away(gv);
-      if (dir < 0) lo = i; else hi = i;
-      // unimodal: past the mode the value only shrinks; stop well below the rounding threshold
-      if (fabs(gv) < 0.25 && ((dir < 0 && double(st_tdc + i) * p.period < mu) ||
-                              (dir > 0 && double(st_tdc + i) * p.period > mu)))
-        break;
     }
   }
   *lo_o = lo;
@@ -367,22 +380,28 @@ __global__ void __launch_bounds__(128) k_pulsefit(CrvParams p, WaveIn W, double*
        w += (long long)gridDim.x * blockDim.x) {
     int n = W.n[w];
     long long off = W.off[w];
-    double* y = yscr + off;
+    R* y = reinterpret_cast<R*>(yscr) + off;
     double pdb = W.ped_db[w];
     double x0 = n > 0 ? (W.adc16 ? double(W.adc16[off]) : double(W.adc64[off])) : 0.0;
     bool under = (n > 0) && (pdb - x0 > p.pedestal_undershoot);
     double ped = under ? x0 : pdb;
-    for (int i = 0; i < n; ++i) y[i] = (W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i])) - ped;
-    bool near = near_lane(y, n, 0, n - 1, p.min_adc_difference, p.knife_edge_adc);
+    if (sizeof(R) == 8) {
+      for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i])) - ped);
+    } else {
+      const float pf = float(ped);
+      for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? float(W.adc16[off + i]) : float(W.adc64[off + i])) - pf);
+    }
+    const R thr = R(p.min_adc_difference), edge = R(p.knife_edge_adc);
+    bool near = near_lane<R>(y, n, 0, n - 1, thr, edge);
     long long st_tdc = W.start_tdc[w];
     int start = 0, cnt = 0, cap = S.cap[w];
     long long slot = S.off[w];
     bool failed_before = false;
     for (int seq = 0; seq < max_pulses; ++seq) {
       int ps, pe, fs, fe;
-      if (!peak_lane(p, y, n, start, &ps, &pe, &fs, &fe)) break;
+      if (!peak_lane<R>(p, y, n, start, &ps, &pe, &fs, &fe)) break;
       int P = fe - fs + 1;
-      double yps = y[ps];
+      double yps = double(y[ps]);
       double t_ps = double(st_tdc + ps) * p.period;
       double t_pe = double(st_tdc + pe) * p.period;
       double t_peak = 0.5 * (t_ps + t_pe);
@@ -427,7 +446,7 @@ __global__ void __launch_bounds__(128) k_pulsefit(CrvParams p, WaveIn W, double*
       failed_before = fseq;
       int lo, hi;
       subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
-      near = near || near_lane(y, n, lo - 1, hi + 1, p.min_adc_difference, p.knife_edge_adc);
+      near = near || near_lane<R>(y, n, lo - 1, hi + 1, thr, edge);
       start = fe;
     }
     S.count[w] = cnt;

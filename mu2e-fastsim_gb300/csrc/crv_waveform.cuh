@@ -88,6 +88,19 @@ __device__ __forceinline__ int tmpl_index(const CrvParams& p, long long J, doubl
   return ti < float(tlen) ? int(ti) : -1;
 }
 
+// FP32-mixed forms on dt = t - t_start (one FP64 subtraction per charge, then FP32)
+__device__ __forceinline__ int first_sample_f(float dt, float P) {
+  float v = ceilf(dt / P);
+  return v > 0.0f ? int(v) : 0;
+}
+
+__device__ __forceinline__ int tmpl_index_f(int J, float dt, float P, float inv_prec, int tlen) {
+  float st = float(J) * P - dt;
+  if (!(st >= 0.0f)) return -1;
+  float ti = rintf(st * inv_prec);
+  return ti < float(tlen) ? int(ti) : -1;
+}
+
 struct ClusterInfo {
   int a, b;                      // charge rows [a, b) relative to the group start
   double ts;                     // t_start
@@ -103,12 +116,24 @@ __device__ int cluster_length(const CrvParams& p, const double* t, int a, int b,
   long long used = 0;
   if (keep) {
     int nr = reach_samples(p);
+    const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
     for (int q = a + lane_id(); q < b; q += 32) {
-      long long j0 = first_sample<R>(p, t[q], ts);
-      for (int k = nr - 1; k >= 0; --k) {
-        if (tmpl_index<R>(p, j0 + k, t[q], ts, tlen) >= 0) {
-          if (j0 + k + 1 > used) used = j0 + k + 1;
-          break;
+      if (sizeof(R) == 8) {
+        long long j0 = first_sample<R>(p, t[q], ts);
+        for (int k = nr - 1; k >= 0; --k) {
+          if (tmpl_index<R>(p, j0 + k, t[q], ts, tlen) >= 0) {
+            if (j0 + k + 1 > used) used = j0 + k + 1;
+            break;
+          }
+        }
+      } else {
+        float dt = float(t[q] - ts);
+        int j0 = first_sample_f(dt, Pf);
+        for (int k = nr - 1; k >= 0; --k) {
+          if (tmpl_index_f(j0 + k, dt, Pf, ip, tlen) >= 0) {
+            if (j0 + k + 1 > used) used = j0 + k + 1;
+            break;
+          }
         }
       }
     }
@@ -183,7 +208,7 @@ constexpr int WF_QSTAGE = 512;    // charges of a cluster staged in shared memor
 
 template <typename R>
 __host__ __device__ inline size_t wf_smem_per_warp(int cap) {
-  return (size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * (sizeof(R) + 4) + 15) & ~size_t(15);
+  return (size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * (sizeof(R) + 8) + 15) & ~size_t(15);
 }
 
 __device__ __forceinline__ int16_t adc_of(const CrvParams& p, double v) {
@@ -212,6 +237,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
   R* wave = reinterpret_cast<R*>(wbase);
   R* qn_s = reinterpret_cast<R*>(wbase + size_t(cap) * sizeof(R));
   int32_t* j0_s = reinterpret_cast<int32_t*>(wbase + size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * sizeof(R));
+  float* dt_s = reinterpret_cast<float*>(wbase + size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * (sizeof(R) + 4));
   __shared__ double vmax_s;
   if (threadIdx.x < 32) {
     double v = -1e300;
@@ -219,6 +245,9 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     if (threadIdx.x == 0) vmax_s = v;
   }
+  __shared__ float tmpl_f[1024];
+  if (sizeof(R) == 4)
+    for (int i = threadIdx.x; i < tlen && i < 1024; i += blockDim.x) tmpl_f[i] = float(tmpl[i]);
   __syncthreads();
   const double vmax = vmax_s;
   const int nr = reach_samples(p);
@@ -260,8 +289,15 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
       if (staged) {
         const R inv_q = R(1.0 / p.spe_ref_charge);
         for (int q = a + lane_id(); q < b; q += 32) {
-          j0_s[q - a] = int32_t(first_sample<R>(p, t[q], ts));
-          qn_s[q - a] = sizeof(R) == 8 ? R(qc[q] / p.spe_ref_charge) : R(qc[q]) * inv_q;
+          if (sizeof(R) == 8) {
+            j0_s[q - a] = int32_t(first_sample<R>(p, t[q], ts));
+            qn_s[q - a] = R(qc[q] / p.spe_ref_charge);
+          } else {
+            float dt = float(t[q] - ts);
+            dt_s[q - a] = dt;
+            j0_s[q - a] = first_sample_f(dt, float(p.period));
+            qn_s[q - a] = R(qc[q]) * inv_q;
+          }
         }
         __syncwarp();
       }
@@ -282,9 +318,17 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
           if (fm > (long long)j) hi2 = m; else lo2 = m + 1;
         }
         R acc = R(0);
-        for (int q = q1; q < lo2; ++q) {
-          int ti = tmpl_index<R>(p, j, t[q], ts, tlen);
-          if (ti >= 0) acc += R(tmpl[ti]) * (staged ? qn_s[q - a] : R(qc[q] / p.spe_ref_charge));
+        if (sizeof(R) == 4 && staged) {
+          const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
+          for (int q = q1; q < lo2; ++q) {
+            int ti = tmpl_index_f(j, dt_s[q - a], Pf, ip, tlen);
+            if (ti >= 0) acc += R(tmpl_f[ti]) * qn_s[q - a];
+          }
+        } else {
+          for (int q = q1; q < lo2; ++q) {
+            int ti = tmpl_index<R>(p, j, t[q], ts, tlen);
+            if (ti >= 0) acc += R(tmpl[ti]) * (staged ? qn_s[q - a] : R(qc[q] / p.spe_ref_charge));
+          }
         }
         if (p.noise_on) {
           long long tk = (long long)k0 + j;
@@ -296,6 +340,20 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         wave[j] = acc;
       }
       __syncwarp();
+      // samples whose start lies in the window: [i_lo, i_hi] (monotone predicates, found once per cluster)
+      int i_lo = 0, i_hi = -1;
+      {
+        double a0 = ceil((p.window_lo - ts) / p.period);
+        long long c = (long long)fmax(a0 - 1.0, 0.0);
+        while (c < L && !(ts + double(c) * p.period >= p.window_lo)) ++c;
+        while (c > 0 && ts + double(c - 1) * p.period >= p.window_lo) --c;
+        i_lo = int(c);
+        double b0 = floor((p.window_hi - ts) / p.period);
+        long long d = (long long)fmin(b0 + 1.0, double(L - 1));
+        while (d >= 0 && !(ts + double(d) * p.period <= p.window_hi)) --d;
+        while (d + 1 < L && ts + double(d + 1) * p.period <= p.window_hi) ++d;
+        i_hi = int(d);
+      }
       // zero suppression over chunks of 32 samples
       int next_i = 0;
       for (int base = 0; base < L; base += 32) {
@@ -307,8 +365,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
             if (k >= 0 && k < L && wave[k] > R(p.min_voltage)) w = true;
           }
         }
-        double tstart = ts + double(i) * p.period;
-        bool inwin = (tstart >= p.window_lo) && (tstart <= p.window_hi);
+        bool inwin = i >= i_lo && i <= i_hi;
         unsigned cand = __ballot_sync(0xffffffffu, w && inwin);
         while (true) {
           unsigned m = cand;
