@@ -217,13 +217,15 @@ def main():
     eng64 = CH.ChainEngine(geom, cond, cfg64)
 
     def one_pass(eng, seed):
-        tot = dict(clusters=0, pulses=0, charges=0, digis=0)
+        tot = dict(clusters=0, pulses=0, charges=0, digis=0, waveforms=0, groups=0, hits=0)
         for ds in batches:
             r = eng.run(ds, seed)
             tot["clusters"] += r.n_clusters
             tot["pulses"] += r.n_pulses
             tot["charges"] += r.n_charges
             tot["digis"] += r.n_digis
+            tot["waveforms"] += r.n_waveforms
+            tot["hits"] += r.n_hits
         return tot
 
     def timed(eng, k, w):
@@ -265,7 +267,7 @@ def main():
     # per-kernel device time of one FP32 pass (profiling events; not the timed number)
     torch.cuda.synchronize()
     _capi.profile(True)
-    one_pass(eng32, 5)
+    counts = one_pass(eng32, 5)
     torch.cuda.synchronize()
     prof = _capi.profile_read()
     _capi.profile(False)
@@ -275,8 +277,35 @@ def main():
         a[0] += 1
         a[1] += t
     top = max(per_kernel.items(), key=lambda kv: kv[1][1])
-    # algorithmic bytes of the dominant kernels (per launch, averaged over the pass)
     tot_ms = sum(v[1] for v in per_kernel.values())
+    hbm, peak_kind = peaks()
+    nb = len(batches)
+
+    # Algorithmic bytes per launch (one launch per event batch), from the stage counts of the pass:
+    #   k_pulsefit: int16 samples in (12 per digi) + per waveform 44 B in (sample row 8, length 4, start TDC 8,
+    #               pedestal / area / height 24) + per pulse 104 B out (11 FP64 columns, wf, seq, 3 flags)
+    #   k_wf_synth: per charge 16 B in (time, charge) + per SiPM group 28 B in (start 8, count 4, label 8, TDC0 8)
+    #               + per digi 152 B out (label, start, TDC0, start TDC, 12 volts, 12 ADC)
+    def alg_bytes(name):
+        if name == "k_pulsefit":
+            return (counts["digis"] * 12 * 2 + counts["waveforms"] * 44 + counts["pulses"] * 104) / nb
+        if name == "k_wf_synth":
+            return (counts["charges"] * 16 + counts["charges"] * 0 + counts["digis"] * 152) / nb
+        return None
+
+    def roofline_of(name):
+        if name not in per_kernel:
+            return None
+        launches, ms = per_kernel[name]
+        # the second pass of a two-pass kernel only picks up oversized items: time per batch = sum over passes
+        per_batch_ms = ms / nb
+        b = alg_bytes(name)
+        if b is None or per_batch_ms <= 0:
+            return None
+        ach = b / (per_batch_ms / 1000.0) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                "kernel": name, "algorithmic_bytes_per_launch": b, "ms_per_launch": per_batch_ms,
+                "peak_kind": f"{peak_kind} (copy bandwidth)"}
 
     # e2e: host step arrays -> device -> chain -> cluster table back to the host, one pass
     torch.cuda.synchronize()
@@ -315,7 +344,6 @@ def main():
     except Exception as exc:  # accuracy report is informative only
         acc["error"] = str(exc)[:200]
 
-    hbm, peak_kind = peaks()
     cpu = None
     if rank == 0 and not args.no_cpu:
         procs = 1
@@ -341,6 +369,8 @@ def main():
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}
                             for k, v in sorted(per_kernel.items(), key=lambda kv: -kv[1][1])[:12]},
                 "dominant_kernel": top[0],
+                "roofline": roofline_of(top[0]),
+                "roofline_waveform": roofline_of("k_wf_synth"),
                 "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
                 "cpu_baseline": cpu}
         print(json.dumps(line))

@@ -14,7 +14,8 @@ import numpy as np
 
 from . import _capi
 from .coinc import CoincEngine, FinderTables, rows_of  # noqa: F401
-from .config import CHAN_MULT, PERIOD, ChainConfig, Conditions, FinderConfig, RecoConfig, WaveformConfig  # noqa: F401
+from .config import (CHAN_MULT, PERIOD, ChainConfig, Conditions, FinderConfig, RecoConfig, WaveformConfig,  # noqa: F401
+                     from_reference)
 from .params import make_params, validate_sipm, validate_window
 from .pulsefit import PulseEngine, filter_channels, concat_waveforms
 from .pulsefit import reconstruct_full as _reconstruct_full

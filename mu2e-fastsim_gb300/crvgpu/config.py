@@ -187,3 +187,32 @@ class ChainConfig:
     feb_phase_key: str = "roc_feb"
     backend: str = "cuda"
     precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (FP64 LM solve and absolute times)
+
+
+def _fields_of(cls, obj, **over):
+    """cls(**{same-named attributes of obj that cls has}) with overrides; obj None -> None."""
+    if obj is None:
+        return None
+    from dataclasses import fields
+    kw = {f.name: getattr(obj, f.name) for f in fields(cls) if hasattr(obj, f.name)}
+    kw.update(over)
+    return cls(**kw)
+
+
+def from_reference(cfg, precision="fp64"):
+    """ChainConfig of this engine from a reference ChainConfig (crv/crvfastsim/chain.py:62-84) or any object with its
+    field names: same-named fields of the chain, SiPM, waveform, reco and finder blocks are carried over; the reference's
+    lookup-table response block contributes its yield scales only (the photon model here is the analytic one); JAX
+    switches have no meaning here and are dropped."""
+    resp = getattr(cfg, "response", None)
+    rc = ResponseConfig(**{k: getattr(resp, k) for k in ("photon_yield_scale", "photon_yield_variation_scale")
+                           if hasattr(resp, k)})
+    kw = dict(response=rc, precision=precision,
+              sipm=_fields_of(SiPMConfig, getattr(cfg, "sipm", None)) or SiPMConfig(),
+              waveform=_fields_of(WaveformConfig, getattr(cfg, "waveform", None)),
+              pulse_reco=_fields_of(RecoConfig, getattr(cfg, "pulse_reco", None)),
+              finder=_fields_of(FinderConfig, getattr(cfg, "finder", None)))
+    for k in ("window", "noise", "feb_phase_width", "feb_phase_key"):
+        if hasattr(cfg, k):
+            kw[k] = getattr(cfg, k)
+    return ChainConfig(**kw)

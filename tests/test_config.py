@@ -1,0 +1,51 @@
+"""Host-side configuration: validation rules (crv/crvfastsim/response/contract.py:5-29 semantics: invalid settings are
+refused before any work) and the reference-config converter.  CPU only."""
+import types
+
+import pytest
+
+from crvgpu import config as C
+from crvgpu.chain import from_reference
+from crvgpu.params import make_params, validate_sipm, validate_window
+
+
+def test_thermal_noise_is_refused():
+    with pytest.raises(ValueError, match="thermal_rate"):
+        validate_sipm(C.SiPMConfig(thermal_rate=1e-3))
+
+
+@pytest.mark.parametrize("kw", [dict(pixel_id="square"), dict(n_pixels_x=30)])
+def test_unsupported_pixel_layouts_are_refused(kw):
+    with pytest.raises(ValueError):
+        validate_sipm(C.SiPMConfig(**kw))
+
+
+@pytest.mark.parametrize("w", [(10.0, 5.0), (0.0, float("inf")), (0.0,), (float("nan"), 1.0)])
+def test_bad_windows_are_refused(w):
+    with pytest.raises(ValueError):
+        validate_window(w)
+
+
+def test_defaults_are_the_workload_values():
+    P = make_params(C.ChainConfig(), 7)
+    assert P.seed == 7
+    assert C.WaveformConfig().period == 12.55 and C.RecoConfig().period == 12.55
+    assert C.WaveformConfig().min_voltage == pytest.approx(5 * 0.0055)
+    assert C.WORKLOAD_CUTS.coincidence_layers == 3 and C.WORKLOAD_CUTS.max_dt == 10
+    assert C.SiPMConfig().cross_talk == 0.05 and C.SiPMConfig().trap0_prob == 0.02
+
+
+def test_from_reference_carries_same_named_fields():
+    ref = types.SimpleNamespace(
+        sipm=types.SimpleNamespace(cross_talk=0.1, time_constant=12.0, jax_only=1),
+        window=(0.0, 1e5), noise=False, jax=True, rounds=3, feb_phase_width=12.5, feb_phase_key="feb",
+        waveform=types.SimpleNamespace(noise=1e-3, samples_zs=10),
+        pulse_reco=types.SimpleNamespace(max_pulses=4, min_beta=4.0),
+        finder=None,
+        response=types.SimpleNamespace(photon_yield_scale=1.2, tables="v6"))
+    c = from_reference(ref, precision="fp32")
+    assert c.sipm.cross_talk == 0.1 and c.sipm.time_constant == 12.0 and c.sipm.trap0_prob == 0.02
+    assert c.window == (0.0, 1e5) and c.noise is False and c.feb_phase_key == "feb"
+    assert c.waveform.noise == 1e-3 and c.waveform.samples_zs == 10 and c.waveform.period == 12.55
+    assert c.pulse_reco.max_pulses == 4 and c.pulse_reco.min_beta == 4.0
+    assert c.finder is None and c.response.photon_yield_scale == 1.2 and c.precision == "fp32"
