@@ -39,6 +39,7 @@ extern "C" {
 #define CRV_OK 0
 #define CRV_ERR_ARG 1
 #define CRV_ERR_CUDA 2
+#define CRV_ERR_TOO_LARGE 3 /* crv_pulses_static: the call needs more scratch than CRV_PULSES_STATIC_MAX_BYTES */
 
 /* device status flags */
 #define CRV_ST_CAPACITY 1      /* a buffer was too small; need[] has the required size */
@@ -275,6 +276,21 @@ int crv_pulses(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *
                const int16_t *adc16, const int64_t *adc64, int32_t max_pulses, CrvPulses *out, int64_t out_cap,
                int64_t *n_out_dev, uint8_t *wf_near, void *workspace, int64_t workspace_bytes, void *stream,
                CrvStatus *status_dev);
+
+/*
+ * crv_pulses without a caller workspace (no counterpart in the reference): the scratch is a file-scope device array of
+ * CRV_PULSES_STATIC_MAX_BYTES per device, so the call allocates nothing (launch profiler off).  For callers that must
+ * not allocate once running: cudaMalloc/cudaFree synchronise the device and stall other streams sharing it, and plain
+ * C FFI hosts have no caching allocator.  Limits: crv_pulses_workspace(p, nw, nsamples) must not exceed the maximum
+ * (else CRV_ERR_TOO_LARGE, nothing launched); the first call on a device (that device current) sets up the scratch
+ * address and should precede any stream capture; the scratch needs no zeroing; calls overlapping in time on one
+ * device share the scratch and race, so serialise them.  Arguments and results as crv_pulses.
+ */
+#define CRV_PULSES_STATIC_MAX_BYTES (64ll << 20)
+int crv_pulses_static(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *off, const int32_t *n,
+                      const int64_t *start_tdc, const double *ped_db, const double *area, const double *height,
+                      const int16_t *adc16, const int64_t *adc64, int32_t max_pulses, CrvPulses *out, int64_t out_cap,
+                      int64_t *n_out_dev, uint8_t *wf_near, void *stream, CrvStatus *status_dev);
 
 /*
  * coinc.find_event over every event (chain.clusters' loop): pulses sorted by (event, waveform, sequence); event e owns

@@ -14,7 +14,8 @@ from . import build as _build
 
 c_i32, c_i64, c_u32, c_f64, c_p = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32, ctypes.c_double, ctypes.c_void_p
 
-CRV_OK, CRV_ERR_ARG, CRV_ERR_CUDA = 0, 1, 2
+CRV_OK, CRV_ERR_ARG, CRV_ERR_CUDA, CRV_ERR_TOO_LARGE = 0, 1, 2, 3
+PULSES_STATIC_MAX_BYTES = 64 << 20
 ST_CAPACITY, ST_LIMIT, ST_NONFINITE, ST_ORDER = 1, 2, 4, 8
 NEED = dict(STEPS_PER_EVENT=0, PHOTONS_PER_SIPM=1, CHARGE_FACTOR=2, DIGIS=3, SAMPLES=4, PULSES=5, HITS_PER_EVENT=6,
             CLUSTERS=7, PHOTONS_TOTAL=8, SLOTS_TOTAL=9, CHARGES_OUT=10, DIGIS_OUT=11, WAVEFORMS=12, PULSES_OUT=13,
@@ -128,6 +129,8 @@ _SIGS = {
     "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
     "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, P(CrvPulses),
                            c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_pulses_static": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32,
+                                  P(CrvPulses), c_i64, c_p, c_p, c_p, c_p]),
     "crv_coincidences_workspace": (c_i64, [c_i64, c_i64]),
     "crv_coincidences": (c_i32, [P(CrvParams), P(CrvFinderGeom), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_p, c_p,
                                  c_p, P(CrvClusters), c_i64, c_p, P(CrvMembers), c_i64, c_p, c_p, c_i64, c_p, c_p]),
@@ -173,6 +176,8 @@ def load(build_if_missing=True):
 def check(rc, what):
     if rc == CRV_ERR_ARG:
         raise ValueError(f"{what}: invalid arguments")
+    if rc == CRV_ERR_TOO_LARGE:
+        raise ValueError(f"{what}: the call needs more scratch than the static maximum ({PULSES_STATIC_MAX_BYTES} bytes)")
     if rc != CRV_OK:
         raise RuntimeError(f"{what}: CUDA launch failed (code {rc})")
 

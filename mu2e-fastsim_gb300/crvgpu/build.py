@@ -22,6 +22,7 @@ UNITS = {
     "crv_engine.cu": [],
     "crv_kernels_f64.cu": ["-fmad=false"],
     "crv_kernels_f32.cu": [],
+    "crv_static.cu": [],
 }
 
 
