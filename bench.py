@@ -217,7 +217,7 @@ def main():
     eng64 = CH.ChainEngine(geom, cond, cfg64)
 
     def one_pass(eng, seed):
-        tot = dict(clusters=0, pulses=0, charges=0, digis=0, waveforms=0, groups=0, hits=0)
+        tot = dict(clusters=0, pulses=0, charges=0, digis=0, waveforms=0, groups=0, hits=0, members=0, events=0)
         for ds in batches:
             r = eng.run(ds, seed)
             tot["clusters"] += r.n_clusters
@@ -226,6 +226,8 @@ def main():
             tot["digis"] += r.n_digis
             tot["waveforms"] += r.n_waveforms
             tot["hits"] += r.n_hits
+            tot["members"] += r.n_members
+            tot["events"] += r.n_events
         return tot
 
     def timed(eng, k, w):
@@ -276,36 +278,52 @@ def main():
         a = per_kernel.setdefault(name, [0, 0.0])
         a[0] += 1
         a[1] += t
-    top = max(per_kernel.items(), key=lambda kv: kv[1][1])
     tot_ms = sum(v[1] for v in per_kernel.values())
     hbm, peak_kind = peaks()
     nb = len(batches)
 
-    # Algorithmic bytes per launch (one launch per event batch), from the stage counts of the pass:
-    #   k_pulsefit: int16 samples in (12 per digi) + per waveform 44 B in (sample row 8, length 4, start TDC 8,
+    # Algorithmic bytes per event batch, from the stage counts of the pass.  The pulse fit is one group of launches
+    # per batch (k_pf_begin + the round launches k_pf_round), timed together:
+    #   pulse fit:  int16 samples in (12 per digi) + per waveform 44 B in (sample row 8, length 4, start TDC 8,
     #               pedestal / area / height 24) + per pulse 104 B out (11 FP64 columns, wf, seq, 3 flags)
-    #   k_wf_synth: per charge 16 B in (time, charge) + per SiPM group 28 B in (start 8, count 4, label 8, TDC0 8)
-    #               + per digi 152 B out (label, start, TDC0, start TDC, 12 volts, 12 ADC)
-    def alg_bytes(name):
-        if name == "k_pulsefit":
+    #   k_wf_synth: per charge 16 B in (time, charge) + per digi 152 B out (label, start, TDC0, start TDC, 12 volts,
+    #               12 ADC)
+    #   k_coinc:    per hit 28 B in (bar, SiPM, sequence, time, PE) + per event 20 B in (first hit, count, key)
+    #               + per cluster 120 B out (event, type, PE, start, end, slope, average time, position, flags) + 4 B
+    #               per member index
+    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth",), "k_coinc": ("k_coinc",)}
+
+    def alg_bytes(group):
+        if group == "pulse fit":
             return (counts["digis"] * 12 * 2 + counts["waveforms"] * 44 + counts["pulses"] * 104) / nb
-        if name == "k_wf_synth":
-            return (counts["charges"] * 16 + counts["charges"] * 0 + counts["digis"] * 152) / nb
+        if group == "k_wf_synth":
+            return (counts["charges"] * 16 + counts["digis"] * 152) / nb
+        if group == "k_coinc":
+            return (counts["hits"] * 28 + counts["events"] * 20 + counts["clusters"] * 120
+                    + counts["members"] * 4) / nb
         return None
 
-    def roofline_of(name):
-        if name not in per_kernel:
+    def group_of(name):
+        return next((g for g, ks in groups.items() if name in ks), name)
+
+    by_group = {}
+    for name, (_, ms_k) in per_kernel.items():
+        by_group[group_of(name)] = by_group.get(group_of(name), 0.0) + ms_k
+    top_group = max(by_group.items(), key=lambda kv: kv[1])[0]
+
+    def roofline_of(group):
+        ks = groups.get(group, (group,))
+        if not any(k in per_kernel for k in ks):
             return None
-        launches, ms = per_kernel[name]
-        # the second pass of a two-pass kernel only picks up oversized items: time per batch = sum over passes
+        ms = sum(per_kernel[k][1] for k in ks if k in per_kernel)
         per_batch_ms = ms / nb
-        b = alg_bytes(name)
+        b = alg_bytes(group)
         if b is None or per_batch_ms <= 0:
             return None
         ach = b / (per_batch_ms / 1000.0) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
-                "kernel": name, "algorithmic_bytes_per_launch": b, "ms_per_launch": per_batch_ms,
-                "peak_kind": f"{peak_kind} (copy bandwidth)"}
+                "kernel": "+".join(ks), "algorithmic_bytes_per_launch": b, "ms_per_launch": per_batch_ms,
+                "launch": "one event batch", "peak_kind": f"{peak_kind} (copy bandwidth)"}
 
     # e2e: host step arrays -> device -> chain -> cluster table back to the host, one pass
     torch.cuda.synchronize()
@@ -368,9 +386,10 @@ def main():
                 "clocks": clk,
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}
                             for k, v in sorted(per_kernel.items(), key=lambda kv: -kv[1][1])[:12]},
-                "dominant_kernel": top[0],
-                "roofline": roofline_of(top[0]),
+                "dominant_kernel": top_group,
+                "roofline": roofline_of(top_group),
                 "roofline_waveform": roofline_of("k_wf_synth"),
+                "roofline_pulse_fit": roofline_of("pulse fit"),
                 "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
                 "cpu_baseline": cpu}
         print(json.dumps(line))

@@ -727,7 +727,11 @@ struct PulseWs {
   long long *slot_off, *out_off, *parts, *totals;
   int32_t *cap, *count;
   long long rc;
+  PfQueue q;
 };
+
+// round launches over the task list before the tail launch finishes what is left lane by lane
+constexpr int kPulseRounds = 16;
 
 // record slots of waveform w: min(max_pulses, n/2 + 1) (every round advances the search by at least two samples)
 static long long pulse_slot_bound(long long nw, long long nsamples) { return nsamples / 2 + nw + 1; }
@@ -744,6 +748,11 @@ static PulseWs pulse_layout(char* base, long long nw, long long nsamples, size_t
   w.totals = c.take<long long>(8);
   w.cap = c.take<int32_t>(nw);
   w.count = c.take<int32_t>(nw);
+  w.q.st = c.take<PfState>(nw);
+  w.q.list[0] = c.take<long long>(nw);
+  w.q.list[1] = c.take<long long>(nw);
+  w.q.counts = c.take<long long>(kPulseRounds + 2);
+  w.q.rounds = kPulseRounds;
   *bytes = c.off + 256;
   return w;
 }
@@ -804,6 +813,7 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, cons
   size_t dummy;
   PulseWs w = pulse_layout(base, nw, nsamples, &dummy);
   CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.q.counts, 0, (kPulseRounds + 2) * sizeof(long long), s));
   unsigned g = grid_for(nw, 256, 8);
   {
     crv::Mark mark_("k_pulse_caps", s);
@@ -814,9 +824,9 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, cons
            area, height, adc16, reinterpret_cast<const long long*>(adc64)};
   PulseSlots PS{w.slot_off, w.cap, w.count, wf_near, w.rec};
   if (p->precision == 1)
-    CK(launch_pulsefit<float>(*p, W, w.yscr, max_pulses, PS, S, s));
+    CK(launch_pulsefit<float>(*p, W, w.yscr, max_pulses, PS, w.q, S, s));
   else
-    CK(launch_pulsefit<double>(*p, W, w.yscr, max_pulses, PS, S, s));
+    CK(launch_pulsefit<double>(*p, W, w.yscr, max_pulses, PS, w.q, S, s));
   CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s));
   {
     crv::Mark mark_("k_check_caps", s);

@@ -11,6 +11,7 @@ struct WfGroups;
 struct DigiSlots;
 struct WaveIn;
 struct PulseSlots;
+struct PfQueue;
 
 struct DeviceInfo {
   int sms;
@@ -62,6 +63,6 @@ cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_
 
 template <typename R>
 cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses, const PulseSlots& S,
-                            Status* status, cudaStream_t s);
+                            const PfQueue& Q, Status* status, cudaStream_t s);
 
 }  // namespace crv

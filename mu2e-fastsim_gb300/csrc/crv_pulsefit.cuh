@@ -7,13 +7,14 @@
 // (40 Levenberg-Marquardt steps, then 8 Gauss-Newton steps with halving, EDM and Hessian checks), the failed-fit
 // fallback, then the rounded fit is subtracted from every sample and the search resumes at the window end.
 //
-// GPU mapping: one thread per waveform (FP64 throughput is scarce on this GPU, so no lane repeats another's uniform
-// work): the waveform's samples sit in a global scratch mirror (L1-resident while the lane works on it), the peak
-// search, the fit (sums sequential over the window, as the reference's contractions), the 3x3 solve (LU with partial
-// pivoting) and the symmetric eigenvalues (cyclic Jacobi) run in the lane; pulses go to per-waveform record slots
-// (rounds are bounded by half the samples).  R = double: every step in FP64; R = float (mixed): parameter mapping,
-// residuals, Jacobians and sums in FP32 relative to the window's first sample, solve / acceptance / absolute times in
-// FP64.
+// GPU mapping: one lane per fit (FP64 throughput is scarce on this GPU, so no lane repeats another's uniform work).
+// Pulses are found in rounds over a device task list (one pulse per pending waveform per round, see k_pf_round), so
+// the lanes of a warp run the same fit schedule; the waveform's samples sit in a global scratch mirror, the peak
+// search, the fit (sums sequential over the window, as the reference's contractions), the 3x3 solve and the symmetric
+// eigenvalues (cyclic Jacobi) run in the lane; pulses go to per-waveform record slots (rounds are bounded by half the
+// samples).  R = double: every step in FP64, the solve by LU with partial pivoting.  R = float (mixed): parameter
+// mapping, residuals, Jacobians, sums and the fit state in FP32 relative to the window's first sample; the
+// normal-equation solve in FP64; absolute pulse times in FP64.
 #pragma once
 #include "crv_device.cuh"
 
@@ -239,6 +240,7 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const R* yw, long lo
     if (!solve3_p<R>(M, g, du)) break;
     for (int k = 0; k < 3; ++k)
       if (!isfinite(du[k])) du[k] = 0.0;
+    bool moved = false;
     for (int sc = 0; sc < 4; ++sc) {
       double s = sc == 0 ? 1.0 : (sc == 1 ? 0.5 : (sc == 2 ? 0.25 : 0.125));
       double un[3] = {u[0] + s * du[0], u[1] + s * du[1], u[2] + s * du[2]};
@@ -248,9 +250,11 @@ __device__ void fit_lane(const Fit3& F, const double p0[3], const R* yw, long lo
         for (int k = 0; k < 3; ++k) { u[k] = un[k]; g[k] = gn[k]; }
         for (int k = 0; k < 6; ++k) H[k] = Hn[k];
         chi2 = c2;
+        moved = true;
         break;                 // the accepted step zeroes du: later scales would re-evaluate the same point
       }
     }
+    if (!moved) break;         // state unchanged: every remaining Gauss-Newton step would repeat this one exactly
   }
   double M[3][3];
   sym3(H, M);
@@ -371,87 +375,342 @@ __device__ __forceinline__ void subtract_lane(const CrvParams& p, R* y, int n, l
   *hi_o = hi;
 }
 
-// one thread per waveform
+// ---- FP32-mixed fit: evaluation, mapping and state in FP32, the normal-equation solve in FP64 -----------------------
+
+struct Fit3f {
+  float lo[3], w[3], half[3];   // lower bound (time: relative to the window's first sample), span, half span
+};
+
+// residuals / normal equations at internal parameters u; window sample i at time i * period
+__device__ __forceinline__ void eval_f32(const Fit3f& F, const float u[3], const float* yw, float period, int P,
+                                         float* chi2, float H[6], float g[3]) {
+  float s0, c0, s1, c1, s2, c2;
+  sincosf(u[0], &s0, &c0);
+  sincosf(u[1], &s1, &c1);
+  sincosf(u[2], &s2, &c2);
+  const float A = F.lo[0] + F.w[0] * (s0 + 1.0f) * 0.5f;
+  const float mu = F.lo[1] + F.w[1] * (s1 + 1.0f) * 0.5f;
+  const float b = F.lo[2] + F.w[2] * (s2 + 1.0f) * 0.5f;
+  const float d0 = F.half[0] * c0, d1 = F.half[1] * c1, d2 = F.half[2] * c2;
+  const float ib = 1.0f / b;
+  float c = 0, h00 = 0, h01 = 0, h02 = 0, h11 = 0, h12 = 0, h22 = 0, g0 = 0, g1 = 0, g2 = 0;
+  for (int i = 0; i < P; ++i) {
+    const float z = (float(i) * period - mu) * ib;
+    // e^-z overflows FP32 beyond 88; at 80 the Gumbel factor e^(-z - e^-z) is already exactly 0
+    const float mz = fminf(-z, 80.0f);
+    const float ez = __expf(mz);
+    const float gg = __expf(mz - ez);
+    const float f = A * gg;
+    const float r = yw[i] - f;
+    const float fz = f * (ez - 1.0f);
+    const float j0 = gg * d0;
+    const float j1 = -fz * ib * d1;
+    const float j2 = -fz * z * ib * d2;
+    c += r * r;
+    h00 += j0 * j0; h01 += j0 * j1; h02 += j0 * j2;
+    h11 += j1 * j1; h12 += j1 * j2; h22 += j2 * j2;
+    g0 += j0 * r; g1 += j1 * r; g2 += j2 * r;
+  }
+  *chi2 = c;
+  H[0] = h00; H[1] = h01; H[2] = h02; H[3] = h11; H[4] = h12; H[5] = h22;
+  g[0] = g0; g[1] = g1; g[2] = g2;
+}
+
+// symmetric 3x3 solve M x = b (M packed 00 01 02 11 12 22): cofactors, determinant and adjugate product in FP64
+// (products of FP32 inputs are exact there), the final division by the determinant in FP32
+__device__ __forceinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {
+  const double m00 = M[0], m01 = M[1], m02 = M[2], m11 = M[3], m12 = M[4], m22 = M[5];
+  const double c00 = m11 * m22 - m12 * m12;
+  const double c01 = m12 * m02 - m01 * m22;
+  const double c02 = m01 * m12 - m11 * m02;
+  const double det = m00 * c00 + m01 * c01 + m02 * c02;
+  if (!(det != 0.0) || !(fabs(det) < 1e300)) return false;
+  const double c11 = m00 * m22 - m02 * m02;
+  const double c12 = m01 * m02 - m00 * m12;
+  const double c22 = m00 * m11 - m01 * m01;
+  const double b0 = b[0], b1 = b[1], b2 = b[2];
+  const double y0 = c00 * b0 + c01 * b1 + c02 * b2;
+  const double y1 = c01 * b0 + c11 * b1 + c12 * b2;
+  const double y2 = c02 * b0 + c12 * b1 + c22 * b2;
+  const float df = float(det);
+  if (fabsf(df) < 1e-30f || !(fabsf(df) < 1e30f)) {          // outside the comfortable FP32 range: FP64 division
+    const double r = 1.0 / det;
+    x[0] = float(y0 * r); x[1] = float(y1 * r); x[2] = float(y2 * r);
+    return true;
+  }
+  const float r = 1.0f / df;
+  x[0] = float(y0) * r; x[1] = float(y1) * r; x[2] = float(y2) * r;
+  return true;
+}
+
+__device__ __forceinline__ bool same3(const float a[3], const float b[3]) {
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2];
+}
+
+// the reference's schedule (40 LM steps, 8 Gauss-Newton steps with halving, EDM and Hessian checks) on FP32 state.
+// Skipped work is exactly work whose outcome is known: a step that leaves the FP32 parameters unchanged evaluates to
+// the same chi2 and is rejected; a rejected step at the clamped damping, or a Gauss-Newton step that no scale
+// improves, leaves the state as it was, so every later step would repeat it.
+__device__ inline void fit_f32(const Fit3& F64, const double p0[3], const float* yw, double period, int P, int iters,
+                        double par[3], double* chi2_out, bool* conv, bool* hok) {
+  Fit3f F;
+  for (int k = 0; k < 3; ++k) {
+    F.lo[k] = float(k == 1 ? F64.lo[k] - F64.t0 : F64.lo[k]);
+    F.w[k] = float(F64.hi[k] - F64.lo[k]);
+    F.half[k] = float(F64.half[k]);
+  }
+  float u[3];
+  for (int k = 0; k < 3; ++k) {
+    float c = 2.0f * float(p0[k] - F64.lo[k]) / F.w[k] - 1.0f;
+    u[k] = asinf(fminf(fmaxf(c, -1.0f), 1.0f));
+  }
+  const float Pf = float(period);
+  float chi2, H[6], g[3];
+  eval_f32(F, u, yw, Pf, P, &chi2, H, g);
+  float lam = 1e-3f;
+  for (int it = 0; it < iters; ++it) {
+    float M[6] = {H[0] + lam * (H[0] + 1e-12f), H[1], H[2], H[3] + lam * (H[3] + 1e-12f), H[4],
+                  H[5] + lam * (H[5] + 1e-12f)};
+    float du[3];
+    if (!solve_sym64(M, g, du)) du[0] = du[1] = du[2] = 0.0f;
+    float un[3] = {u[0] + du[0], u[1] + du[1], u[2] + du[2]};
+    bool better = false;
+    if (!same3(un, u)) {
+      float c2, Hn[6], gn[3];
+      eval_f32(F, un, yw, Pf, P, &c2, Hn, gn);
+      if (c2 < chi2) {
+        better = true;
+        for (int k = 0; k < 3; ++k) { u[k] = un[k]; g[k] = gn[k]; }
+        for (int k = 0; k < 6; ++k) H[k] = Hn[k];
+        chi2 = c2;
+      }
+    }
+    const float ln = fminf(fmaxf(better ? lam * 0.3f : lam * 10.0f, 1e-9f), 1e9f);
+    if (!better && ln == lam) break;
+    lam = ln;
+  }
+  for (int it = 0; it < 8; ++it) {
+    float M[6] = {H[0] + 1e-12f, H[1], H[2], H[3] + 1e-12f, H[4], H[5] + 1e-12f};
+    float du[3];
+    if (!solve_sym64(M, g, du)) break;
+    for (int k = 0; k < 3; ++k)
+      if (!isfinite(du[k])) du[k] = 0.0f;
+    bool moved = false;
+    for (int sc = 0; sc < 4 && !moved; ++sc) {
+      const float s = sc == 0 ? 1.0f : (sc == 1 ? 0.5f : (sc == 2 ? 0.25f : 0.125f));
+      float un[3] = {u[0] + s * du[0], u[1] + s * du[1], u[2] + s * du[2]};
+      if (same3(un, u)) continue;
+      float c2, Hn[6], gn[3];
+      eval_f32(F, un, yw, Pf, P, &c2, Hn, gn);
+      if (c2 < chi2) {
+        for (int k = 0; k < 3; ++k) { u[k] = un[k]; g[k] = gn[k]; }
+        for (int k = 0; k < 6; ++k) H[k] = Hn[k];
+        chi2 = c2;
+        moved = true;
+      }
+    }
+    if (!moved) break;
+  }
+  float M[6] = {H[0] + 1e-12f, H[1], H[2], H[3] + 1e-12f, H[4], H[5] + 1e-12f};
+  float st[3];
+  float edm;
+  bool okh;
+  if (solve_sym64(M, g, st)) {
+    edm = 0.5f * (g[0] * st[0] + g[1] * st[1] + g[2] * st[2]);
+    const double Hd[6] = {H[0], H[1], H[2], H[3], H[4], H[5]};
+    double Hm[3][3], e[3];
+    sym3(Hd, Hm);
+    eig3(Hm, e);
+    okh = e[0] > 1e-12 * fmax(e[2], 1e-300);
+  } else {
+    edm = INFINITY;
+    okh = false;
+  }
+  *conv = isfinite(edm) && (edm <= 1e-3f * fmaxf(chi2, 1.0f));
+  *hok = okh;
+  for (int k = 0; k < 3; ++k) par[k] = F64.lo[k] + (F64.hi[k] - F64.lo[k]) * (double(sinf(u[k])) + 1.0) * 0.5;
+  *chi2_out = double(chi2);
+}
+
 template <typename R>
-__global__ void __launch_bounds__(128) k_pulsefit(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
-                                                 PulseSlots S, Status* status) {
+__device__ __forceinline__ void fit_any(const Fit3& F, const double p0[3], const R* yw, long long tdc_fs,
+                                        double period, int P, int iters, double par[3], double* chi2, bool* conv,
+                                        bool* hok) {
+  if constexpr (sizeof(R) == 4)
+    fit_f32(F, p0, reinterpret_cast<const float*>(yw), period, P, iters, par, chi2, conv, hok);
+  else
+    fit_lane<R>(F, p0, yw, tdc_fs, period, P, iters, par, chi2, conv, hok);
+}
+
+// ---- rounds over a device task list -----------------------------------------------------------------------------
+//
+// A waveform's pulses are found one per round.  Round 0 (k_pf_begin) prepares every waveform and finds its first
+// peak; each later launch (k_pf_round) fits one pulse of every waveform still pending, records it, subtracts it and
+// searches the next peak, appending the waveform to the next round's list.  Lanes of a warp therefore run the same
+// fit schedule on different waveforms instead of one lane per waveform for all its rounds.  After a fixed number of
+// rounds a tail launch finishes the few waveforms left, one lane each.  Results depend only on the waveform, so the
+// (atomic) order of the lists does not matter.
+
+struct PfState {             // per waveform, carried between rounds
+  double ped;
+  int32_t start, cnt, ps, pe, fs, fe;
+  uint8_t under, fb, near, pad[5];
+};
+
+struct PfQueue {
+  PfState* st;               // [nw]
+  long long* list[2];        // [nw] each: waveforms pending in even / odd rounds
+  long long* counts;         // [rounds + 2]: tasks per round (zeroed before round 0)
+  int rounds;                // round launches before the tail launch
+};
+
+__device__ __forceinline__ void push_task(long long* list, long long* count, long long w, bool pend) {
+  const unsigned m = __ballot_sync(0xffffffffu, pend);
+  if (!m) return;
+  const int lane = lane_id();
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(reinterpret_cast<unsigned long long*>(count), (unsigned long long)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (pend) list[base + __popc(m & ((1u << lane) - 1u))] = w;
+}
+
+// pedestal, sample copy, near-threshold scan and the first peak; true when a pulse is pending
+template <typename R>
+__device__ __forceinline__ bool pf_begin(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses,
+                                         long long w, PfState& st) {
+  const int n = W.n[w];
+  const long long off = W.off[w];
+  R* y = reinterpret_cast<R*>(yscr) + off;
+  const double pdb = W.ped_db[w];
+  const double x0 = n > 0 ? (W.adc16 ? double(W.adc16[off]) : double(W.adc64[off])) : 0.0;
+  const bool under = (n > 0) && (pdb - x0 > p.pedestal_undershoot);
+  const double ped = under ? x0 : pdb;
+  if (sizeof(R) == 8) {
+    for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i])) - ped);
+  } else {
+    const float pf = float(ped);
+    for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? float(W.adc16[off + i]) : float(W.adc64[off + i])) - pf);
+  }
+  st.ped = ped;
+  st.under = under;
+  st.start = 0;
+  st.cnt = 0;
+  st.fb = 0;
+  st.near = near_lane<R>(y, n, 0, n - 1, R(p.min_adc_difference), R(p.knife_edge_adc));
+  if (max_pulses <= 0) return false;
+  return peak_lane<R>(p, y, n, 0, &st.ps, &st.pe, &st.fs, &st.fe);
+}
+
+// fit, record and subtract the pending pulse, then search the next one; true when another pulse is pending
+template <typename R>
+__device__ __forceinline__ bool pf_step(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses,
+                                        const PulseSlots& S, long long w, PfState& st) {
   const double E = 2.718281828459045;
-  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < W.nw;
-       w += (long long)gridDim.x * blockDim.x) {
-    int n = W.n[w];
-    long long off = W.off[w];
-    R* y = reinterpret_cast<R*>(yscr) + off;
-    double pdb = W.ped_db[w];
-    double x0 = n > 0 ? (W.adc16 ? double(W.adc16[off]) : double(W.adc64[off])) : 0.0;
-    bool under = (n > 0) && (pdb - x0 > p.pedestal_undershoot);
-    double ped = under ? x0 : pdb;
-    if (sizeof(R) == 8) {
-      for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? double(W.adc16[off + i]) : double(W.adc64[off + i])) - ped);
-    } else {
-      const float pf = float(ped);
-      for (int i = 0; i < n; ++i) y[i] = R((W.adc16 ? float(W.adc16[off + i]) : float(W.adc64[off + i])) - pf);
+  const int n = W.n[w];
+  R* y = reinterpret_cast<R*>(yscr) + W.off[w];
+  const long long st_tdc = W.start_tdc[w];
+  const int ps = st.ps, pe = st.pe, fs = st.fs, fe = st.fe;
+  const int P = fe - fs + 1;
+  const double yps = double(y[ps]);
+  const double t_ps = double(st_tdc + ps) * p.period;
+  const double t_pe = double(st_tdc + pe) * p.period;
+  const double t_peak = 0.5 * (t_ps + t_pe);
+  Fit3 F;
+  F.lo[0] = yps * E * p.min_height_ratio; F.hi[0] = yps * E * p.max_height_ratio;
+  F.lo[1] = t_ps - p.max_time_difference; F.hi[1] = t_pe + p.max_time_difference;
+  F.lo[2] = p.min_beta; F.hi[2] = p.max_beta;
+  for (int k = 0; k < 3; ++k) F.half[k] = (F.hi[k] - F.lo[k]) * 0.5;
+  F.t0 = double(st_tdc + fs) * p.period;
+  const double p0[3] = {yps * E, t_peak, p.default_beta};
+  double par[3], chi2;
+  bool conv, hok;
+  fit_any<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
+  const int ndf = P - 3;
+  bool nearlim = false;
+  for (int k = 0; k < 3; ++k) {
+    const double span = F.hi[k] - F.lo[k];
+    if ((par[k] - F.lo[k]) / span < p.limit_tolerance || (F.hi[k] - par[k]) / span < p.limit_tolerance)
+      nearlim = true;
+  }
+  const bool failed = !conv || !hok || nearlim;
+  const double A = par[0], mu = par[1], b = par[2];
+  const double height = failed ? yps : A / E;
+  const double beta = failed ? p.default_beta : b;
+  const double tp = failed ? t_peak : mu;
+  const bool fseq = failed || st.fb;
+  const int seq = st.cnt;
+  if (seq < S.cap[w]) {
+    PulseRec& r = S.rec[S.off[w] + seq];
+    r.pe = (failed ? yps * E * p.default_beta : A * b) / W.area[w];
+    r.peph = height / W.height[w];
+    r.time = tp;
+    r.height = height;
+    r.beta = beta;
+    r.chi2 = (failed || ndf <= 0) ? -1.0 : chi2 / double(ndf > 1 ? ndf : 1);
+    r.letime = tp - p.le_time_factor * beta;
+    r.ped = st.ped;
+    r.A = A; r.mu = mu; r.b = b;
+    r.seq = seq;
+    r.failed = fseq; r.zerondf = ndf <= 0; r.pedfromdb = !st.under; r.pad = 0;
+  }
+  st.cnt = seq + 1;
+  st.fb = fseq;
+  int lo, hi;
+  subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
+  st.near = st.near || near_lane<R>(y, n, lo - 1, hi + 1, R(p.min_adc_difference), R(p.knife_edge_adc));
+  st.start = fe;
+  if (st.cnt >= max_pulses) return false;
+  return peak_lane<R>(p, y, n, st.start, &st.ps, &st.pe, &st.fs, &st.fe);
+}
+
+__device__ __forceinline__ void pf_finish(const PulseSlots& S, Status* status, long long w, const PfState& st) {
+  S.count[w] = st.cnt;
+  S.near[w] = st.near;
+  if (st.cnt > S.cap[w]) set_flag(status, CRV_ST_LIMIT);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_pf_begin(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
+                                                 PulseSlots S, PfQueue Q, Status* status) {
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; base < W.nw;
+       base += nwarps * 32) {
+    const long long w = base + lane_id();
+    bool pend = false;
+    if (w < W.nw) {
+      PfState st;
+      pend = pf_begin<R>(p, W, yscr, max_pulses, w, st);
+      if (pend) Q.st[w] = st;
+      else pf_finish(S, status, w, st);
     }
-    const R thr = R(p.min_adc_difference), edge = R(p.knife_edge_adc);
-    bool near = near_lane<R>(y, n, 0, n - 1, thr, edge);
-    long long st_tdc = W.start_tdc[w];
-    int start = 0, cnt = 0, cap = S.cap[w];
-    long long slot = S.off[w];
-    bool failed_before = false;
-    for (int seq = 0; seq < max_pulses; ++seq) {
-      int ps, pe, fs, fe;
-      if (!peak_lane<R>(p, y, n, start, &ps, &pe, &fs, &fe)) break;
-      int P = fe - fs + 1;
-      double yps = double(y[ps]);
-      double t_ps = double(st_tdc + ps) * p.period;
-      double t_pe = double(st_tdc + pe) * p.period;
-      double t_peak = 0.5 * (t_ps + t_pe);
-      Fit3 F;
-      F.lo[0] = yps * E * p.min_height_ratio; F.hi[0] = yps * E * p.max_height_ratio;
-      F.lo[1] = t_ps - p.max_time_difference; F.hi[1] = t_pe + p.max_time_difference;
-      F.lo[2] = p.min_beta; F.hi[2] = p.max_beta;
-      for (int k = 0; k < 3; ++k) F.half[k] = (F.hi[k] - F.lo[k]) * 0.5;
-      F.t0 = double(st_tdc + fs) * p.period;
-      double p0[3] = {yps * E, t_peak, p.default_beta};
-      double par[3], chi2;
-      bool conv, hok;
-      fit_lane<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
-      int ndf = P - 3;
-      bool nearlim = false;
-      for (int k = 0; k < 3; ++k) {
-        double span = F.hi[k] - F.lo[k];
-        if ((par[k] - F.lo[k]) / span < p.limit_tolerance || (F.hi[k] - par[k]) / span < p.limit_tolerance)
-          nearlim = true;
-      }
-      bool failed = !conv || !hok || nearlim;
-      double A = par[0], mu = par[1], b = par[2];
-      double height = failed ? yps : A / E;
-      double beta = failed ? p.default_beta : b;
-      double tp = failed ? t_peak : mu;
-      bool fseq = failed || failed_before;
-      if (cnt < cap) {
-        PulseRec& r = S.rec[slot + cnt];
-        r.pe = (failed ? yps * E * p.default_beta : A * b) / W.area[w];
-        r.peph = height / W.height[w];
-        r.time = tp;
-        r.height = height;
-        r.beta = beta;
-        r.chi2 = (failed || ndf <= 0) ? -1.0 : chi2 / double(ndf > 1 ? ndf : 1);
-        r.letime = tp - p.le_time_factor * beta;
-        r.ped = ped;
-        r.A = A; r.mu = mu; r.b = b;
-        r.seq = seq;
-        r.failed = fseq; r.zerondf = ndf <= 0; r.pedfromdb = !under; r.pad = 0;
-      }
-      ++cnt;
-      failed_before = fseq;
-      int lo, hi;
-      subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
-      near = near || near_lane<R>(y, n, lo - 1, hi + 1, thr, edge);
-      start = fe;
+    push_task(Q.list[0], &Q.counts[0], w, pend);
+  }
+}
+
+// round r: the tasks of list r & 1 (count counts[r]); tail != 0: finish every task in the lane
+template <typename R>
+__global__ void __launch_bounds__(128) k_pf_round(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
+                                                 PulseSlots S, PfQueue Q, int r, int tail, Status* status) {
+  const long long* in = Q.list[r & 1];
+  const long long n_in = Q.counts[r];
+  long long* out = Q.list[(r + 1) & 1];
+  long long* n_out = &Q.counts[r + 1];
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; base < n_in;
+       base += nwarps * 32) {
+    const long long i = base + lane_id();
+    long long w = -1;
+    bool pend = false;
+    if (i < n_in) {
+      w = in[i];
+      PfState st = Q.st[w];
+      pend = pf_step<R>(p, W, yscr, max_pulses, S, w, st);
+      if (tail)
+        while (pend) pend = pf_step<R>(p, W, yscr, max_pulses, S, w, st);
+      if (pend) Q.st[w] = st;
+      else pf_finish(S, status, w, st);
     }
-    S.count[w] = cnt;
-    S.near[w] = near;
-    if (cnt > cap) set_flag(status, CRV_ST_LIMIT);
+    if (!tail) push_task(out, n_out, w, pend);
   }
 }
 
