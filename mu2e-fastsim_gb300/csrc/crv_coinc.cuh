@@ -94,58 +94,73 @@ __device__ __forceinline__ bool linked(const CoincShared& S, int a, int b, doubl
 
 // Greedy clustering of items 0..n-1 in list order: item k is hit ids[k] with maxd mds[k].  Writes the cluster of
 // every item into cl_of[k], the items grouped by cluster in join order into out[], and cluster starts into
-// clstart[0..ncl].  Returns the number of clusters.  S.pool is scratch.
+// clstart[0..ncl].  Returns the number of clusters.
+//
+// The reference seeds a cluster with the first item left, then scans the remaining items in order, adding every
+// item linked to a member (including members added earlier in the same scan), and repeats the scan until it adds
+// nothing.  Here the scan goes over 32 items at a time, one per lane: each lane tests its item against the members;
+// the lowest linked lane joins first, the lanes after it re-test against that new member, and so on, which is the
+// sequential scan's order exactly.
 __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* mds, int n, double max_dt, bool opposite,
                       double dt_opp, int32_t* cl_of, int32_t* out, int32_t* clstart) {
-  for (int i = lane_id(); i < n; i += 32) S.pool[i] = i;
+  const int lane = lane_id();
+  for (int k = lane; k < n; k += 32) cl_of[k] = -1;
   __syncwarp();
-  int npool = n, nout = 0, ncl = 0;
-  while (npool > 0) {
-    int first = S.pool[0];
-    __syncwarp();
-    if (lane_id() == 0) {
-      for (int i = 1; i < npool; ++i) S.pool[i - 1] = S.pool[i];
-      out[nout] = first;
-      cl_of[first] = ncl;
-      clstart[ncl] = nout;
+  int nout = 0, ncl = 0, first = 0;
+  while (true) {
+    int seed = -1;
+    for (int base = first; base < n && seed < 0; base += 32) {
+      const int k = base + lane;
+      const unsigned m = __ballot_sync(0xffffffffu, k < n && cl_of[k] < 0);
+      if (m) seed = base + __ffs(m) - 1;
     }
+    if (seed < 0) break;
+    first = seed + 1;
     __syncwarp();
-    --npool;
-    int c0 = nout;
+    if (lane == 0) { out[nout] = seed; cl_of[seed] = ncl; clstart[ncl] = nout; }
+    __syncwarp();
+    const int c0 = nout;
     ++nout;
     bool grew = true;
     while (grew) {
       grew = false;
-      int i = 0;
-      while (i < npool) {
-        int cand = S.pool[i];
-        int hc = ids[cand];
-        double mc = mds[cand];
+      for (int base = first; base < n; base += 32) {
+        const int k = base + lane;
+        const bool cand = k < n && cl_of[k] < 0;
+        int hc = 0;
+        double mc = 0.0;
         bool link = false;
-        for (int m = c0 + lane_id(); m < nout; m += 32) {
-          int it = out[m];
-          link = link || linked(S, hc, ids[it], mc, mds[it], max_dt, opposite, dt_opp);
-        }
-        bool any = __any_sync(0xffffffffu, link);
-        __syncwarp();
-        if (any) {
-          if (lane_id() == 0) {
-            out[nout] = cand;
-            cl_of[cand] = ncl;
-            for (int k = i + 1; k < npool; ++k) S.pool[k - 1] = S.pool[k];
+        if (cand) {
+          hc = ids[k];
+          mc = mds[k];
+          for (int m = c0; m < nout && !link; ++m) {
+            const int it = out[m];
+            link = linked(S, hc, ids[it], mc, mds[it], max_dt, opposite, dt_opp);
           }
-          __syncwarp();
-          ++nout;
-          --npool;
-          grew = true;
-        } else {
-          ++i;
         }
+        unsigned L = __ballot_sync(0xffffffffu, link);
+        while (L) {
+          const int b = __ffs(L) - 1;
+          const int nk = base + b;
+          __syncwarp();
+          if (lane == 0) { out[nout] = nk; cl_of[nk] = ncl; }
+          ++nout;
+          grew = true;
+          L &= L - 1u;
+          bool t = false;
+          if (cand && !link && lane > b) {
+            t = linked(S, hc, ids[nk], mc, mds[nk], max_dt, opposite, dt_opp);
+            link = t;
+          }
+          L |= __ballot_sync(0xffffffffu, t);
+        }
+        __syncwarp();
       }
     }
     ++ncl;
   }
-  if (lane_id() == 0) clstart[ncl] = nout;
+  __syncwarp();
+  if (lane == 0) clstart[ncl] = nout;
   __syncwarp();
   return ncl;
 }
