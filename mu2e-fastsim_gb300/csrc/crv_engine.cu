@@ -590,7 +590,8 @@ extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups
 
 namespace crv {
 struct DigiWs {
-  int32_t *head, *gcount, *g_bound, *g_maxlen, *dn;
+  int32_t *head, *gcount, *g_bound, *g_maxlen, *g_nkept, *dn;
+  WfCluster* cl;                 // kept clusters by charge row (shares the group index memory, free after grouping)
   long long *gidx, *gstart, *glabel, *slot_off, *out_off, *parts, *totals;
   uint32_t* grun;
   double* g_tdc0;
@@ -603,7 +604,9 @@ static DigiWs digi_layout(char* base, long long nq, long long slot_cap, int zs, 
   DigiWs w;
   w.sc = slot_cap;
   w.head = c.take<int32_t>(nq);
-  w.gidx = c.take<long long>(nq);
+  static_assert(sizeof(WfCluster) == 2 * sizeof(long long), "cluster record size");
+  w.gidx = c.take<long long>(2 * nq);
+  w.cl = reinterpret_cast<WfCluster*>(w.gidx);
   w.gstart = c.take<long long>(nq);
   w.glabel = c.take<long long>(nq);
   w.gcount = c.take<int32_t>(nq);
@@ -611,6 +614,7 @@ static DigiWs digi_layout(char* base, long long nq, long long slot_cap, int zs, 
   w.g_tdc0 = c.take<double>(nq);
   w.g_bound = c.take<int32_t>(nq);
   w.g_maxlen = c.take<int32_t>(nq);
+  w.g_nkept = c.take<int32_t>(nq);
   w.slot_off = c.take<long long>(nq);
   w.dn = c.take<int32_t>(nq);
   w.out_off = c.take<long long>(nq);
@@ -680,9 +684,11 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   CK(cudaGetLastError());
   WfGroups G{&w.totals[0], w.gstart, w.gcount, w.glabel, w.grun};
   if (p->precision == 1)
-    CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen, s));
+    CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen,
+                                w.g_nkept, w.cl, s));
   else
-    CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen, s));
+    CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen,
+                                 w.g_nkept, w.cl, s));
   CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s));
   {
     crv::Mark mark_("k_check_caps", s);
@@ -696,9 +702,11 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   CK(cudaGetLastError());
   G.n = &w.totals[2];
   if (p->precision == 1)
-    CK(launch_wf_synth<float>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.D, S, s));
+    CK(launch_wf_synth<float>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.g_nkept, w.cl,
+                              w.D, S, s));
   else
-    CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.D, S, s));
+    CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.g_nkept, w.cl,
+                               w.D, S, s));
   CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s));
   {
     crv::Mark mark_("k_check_caps", s);

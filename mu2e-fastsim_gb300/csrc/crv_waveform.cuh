@@ -101,72 +101,56 @@ __device__ __forceinline__ int tmpl_index_f(int J, float dt, float P, float inv_
   return ti < float(tlen) ? int(ti) : -1;
 }
 
-struct ClusterInfo {
-  int a, b;                      // charge rows [a, b) relative to the group start
-  double ts;                     // t_start
-  long long tick0;
-  int length;
-  bool keep;
+// A kept cluster: t_start = k0 P + TDC0; first charge row (relative to the group start); length in samples.
+struct WfCluster {
+  long long k0;
+  int32_t a, L;
 };
 
-// Length of a kept cluster: max(est, last contributing sample + 1); lanes split the charges.
+// t_start of a cluster, rounded the same way wherever it is formed (no contraction into an FMA)
+__device__ __forceinline__ double cluster_ts(long long k0, double period, double tdc0) {
+  return __dadd_rn(__dmul_rn(double(k0), period), tdc0);
+}
+
+// cluster_length for one thread (charges a..b-1 in turn); nr = reach_samples(p), ip = 1 / template precision
 template <typename R>
-__device__ int cluster_length(const CrvParams& p, const double* t, int a, int b, double ts, int tlen, bool keep) {
+__device__ __forceinline__ int cluster_length_serial(const CrvParams& p, const double* t, int a, int b, double ts,
+                                                     int tlen, int nr, float ip) {
   long long est = (long long)floor((t[b - 1] - t[a] + p.spe_max_time) / p.period);
   long long used = 0;
-  if (keep) {
-    int nr = reach_samples(p);
-    const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
-    for (int q = a + lane_id(); q < b; q += 32) {
-      if (sizeof(R) == 8) {
-        long long j0 = first_sample<R>(p, t[q], ts);
-        for (int k = nr - 1; k >= 0; --k) {
-          if (tmpl_index<R>(p, j0 + k, t[q], ts, tlen) >= 0) {
-            if (j0 + k + 1 > used) used = j0 + k + 1;
-            break;
-          }
+  const float Pf = float(p.period);
+  for (int q = a; q < b; ++q) {
+    if (sizeof(R) == 8) {
+      long long j0 = first_sample<R>(p, t[q], ts);
+      for (int k = nr - 1; k >= 0; --k) {
+        if (tmpl_index<R>(p, j0 + k, t[q], ts, tlen) >= 0) {
+          if (j0 + k + 1 > used) used = j0 + k + 1;
+          break;
         }
-      } else {
-        float dt = float(t[q] - ts);
-        int j0 = first_sample_f(dt, Pf);
-        for (int k = nr - 1; k >= 0; --k) {
-          if (tmpl_index_f(j0 + k, dt, Pf, ip, tlen) >= 0) {
-            if (j0 + k + 1 > used) used = j0 + k + 1;
-            break;
-          }
+      }
+    } else {
+      float dt = float(t[q] - ts);
+      int j0 = first_sample_f(dt, Pf);
+      for (int k = nr - 1; k >= 0; --k) {
+        if (tmpl_index_f(j0 + k, dt, Pf, ip, tlen) >= 0) {
+          if (j0 + k + 1 > used) used = j0 + k + 1;
+          break;
         }
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      long long y = __shfl_xor_sync(0xffffffffu, used, o);
-      used = y > used ? y : used;
-    }
   }
-  long long L = est > used ? est : used;
-  return int(L);
+  return int(est > used ? est : used);
 }
 
-// Next cluster [a, b) of the group from charge a (warp-uniform); returns b.
-__device__ inline int next_cluster_end(const CrvParams& p, const double* t, int a, int n) {
-  double gap = p.spe_max_time + 4.0 * p.period;
-  int b = a + 1;
-  while (b < n) {
-    int i = b + lane_id();
-    bool brk = i < n && (t[i] - t[i - 1] > gap);
-    unsigned m = __ballot_sync(0xffffffffu, brk);
-    if (m) return b + __ffs(m) - 1;
-    int adv = n - b < 32 ? n - b : 32;
-    b += adv;
-  }
-  return n;
-}
-
-// Per group: TDC0, digi bound (sum over kept clusters of ceil(length / 12)), longest kept cluster.
+// Per group, one thread each (the per-cluster FP64 scalars are then computed once per cluster, not by a whole
+// warp): TDC0, the kept clusters (into cl[group start + k]), the digi bound (sum over kept clusters of
+// ceil(length / samples_zs)) and the longest kept cluster.
 template <typename R>
-__global__ void k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G, const double* __restrict__ time,
-                             const double* __restrict__ tmpl, int tlen, double* __restrict__ g_tdc0,
-                             int32_t* __restrict__ g_bound, int32_t* __restrict__ g_maxlen) {
+__global__ void __launch_bounds__(256) k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G,
+                                                    const double* __restrict__ time, const double* __restrict__ tmpl,
+                                                    int tlen, double* __restrict__ g_tdc0, int32_t* __restrict__ g_bound,
+                                                    int32_t* __restrict__ g_maxlen, int32_t* __restrict__ g_nkept,
+                                                    WfCluster* __restrict__ cl) {
   __shared__ double vmax_s;
   if (threadIdx.x < 32) {
     double v = -1e300;
@@ -175,33 +159,57 @@ __global__ void k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G, const doub
     if (threadIdx.x == 0) vmax_s = v;
   }
   __syncthreads();
-  double vmax = vmax_s;
-  long long ng = *G.n;
-  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
-    int n = G.count[g];
-    const double* t = time + G.start[g];
-    long long lab = G.label[g];
-    double tdc0 = tdc0_of(p, ch, lab, G.run ? G.run[g] : 0u);
+  const double vmax = vmax_s;
+  const double gap = p.spe_max_time + 4.0 * p.period;
+  const int nr = reach_samples(p);
+  const float ip = float(1.0 / p.spe_precision);
+  const int zs = p.samples_zs;
+  const long long ng = *G.n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
+    const int n = G.count[g];
+    const long long q0 = G.start[g];
+    const double* t = time + q0;
+    const double tdc0 = tdc0_of(p, ch, G.label[g], G.run ? G.run[g] : 0u);
     long long bound = 0;
-    int maxlen = 0;
+    int maxlen = 0, nk = 0;
     for (int a = 0; a < n;) {
-      int b = next_cluster_end(p, t, a, n);
-      bool keep = double(b - a) * vmax >= p.min_voltage;
-      if (keep) {
-        double ts = ceil((t[a] - p.period - tdc0) / p.period) * p.period + tdc0;
-        int L = cluster_length<R>(p, t, a, b, ts, tlen, true);
-        bound += (L + p.samples_zs - 1) / p.samples_zs;
+      int b = a + 1;
+      while (b < n && !(t[b] - t[b - 1] > gap)) ++b;
+      if (double(b - a) * vmax >= p.min_voltage) {
+        const long long k0 = (long long)ceil((t[a] - p.period - tdc0) / p.period);
+        const double ts = cluster_ts(k0, p.period, tdc0);
+        const int L = cluster_length_serial<R>(p, t, a, b, ts, tlen, nr, ip);
+        bound += (L + zs - 1) / zs;
         maxlen = L > maxlen ? L : maxlen;
+        cl[q0 + nk] = WfCluster{k0, a, L};
+        ++nk;
       }
       a = b;
     }
-    if (lane_id() == 0) {
-      g_tdc0[g] = tdc0;
-      g_bound[g] = int32_t(bound);
-      g_maxlen[g] = maxlen;
-    }
+    g_tdc0[g] = tdc0;
+    g_bound[g] = int32_t(bound);
+    g_maxlen[g] = maxlen;
+    g_nkept[g] = nk;
   }
+}
+
+// samples of a cluster whose start lies in the window: [i_lo, i_hi] (monotone predicates)
+__device__ __forceinline__ void window_bounds(const CrvParams& p, double ts, int L, int* lo_o, int* hi_o) {
+  if (ts >= p.window_lo && __dadd_rn(ts, __dmul_rn(double(L - 1), p.period)) <= p.window_hi) {
+    *lo_o = 0;
+    *hi_o = L - 1;
+    return;
+  }
+  double a0 = ceil((p.window_lo - ts) / p.period);
+  long long c = (long long)fmax(a0 - 1.0, 0.0);
+  while (c < L && !(__dadd_rn(ts, __dmul_rn(double(c), p.period)) >= p.window_lo)) ++c;
+  while (c > 0 && __dadd_rn(ts, __dmul_rn(double(c - 1), p.period)) >= p.window_lo) --c;
+  double b0 = floor((p.window_hi - ts) / p.period);
+  long long d = (long long)fmin(b0 + 1.0, double(L - 1));
+  while (d >= 0 && !(__dadd_rn(ts, __dmul_rn(double(d), p.period)) <= p.window_hi)) --d;
+  while (d + 1 < L && __dadd_rn(ts, __dmul_rn(double(d + 1), p.period)) <= p.window_hi) ++d;
+  *lo_o = int(c);
+  *hi_o = int(d);
 }
 
 constexpr int WF_QSTAGE = 512;    // charges of a cluster staged in shared memory (larger clusters: on the fly)
@@ -230,28 +238,26 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
                                                   const double* __restrict__ charge, const double* __restrict__ tmpl,
                                                   int tlen, const double* __restrict__ g_tdc0,
-                                                  const int32_t* __restrict__ g_maxlen, int lo, int cap,
-                                                  int last_pass, DigiSlots D, Status* status) {
+                                                  const int32_t* __restrict__ g_maxlen,
+                                                  const int32_t* __restrict__ g_nkept,
+                                                  const WfCluster* __restrict__ cl, int lo, int cap, int last_pass,
+                                                  DigiSlots D, Status* status) {
   extern __shared__ __align__(16) char smem[];
   char* wbase = smem + size_t(warp_in_block()) * wf_smem_per_warp<R>(cap);
   R* wave = reinterpret_cast<R*>(wbase);
   R* qn_s = reinterpret_cast<R*>(wbase + size_t(cap) * sizeof(R));
   int32_t* j0_s = reinterpret_cast<int32_t*>(wbase + size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * sizeof(R));
   float* dt_s = reinterpret_cast<float*>(wbase + size_t(cap) * sizeof(R) + size_t(WF_QSTAGE) * (sizeof(R) + 4));
-  __shared__ double vmax_s;
-  if (threadIdx.x < 32) {
-    double v = -1e300;
-    for (int i = threadIdx.x; i < tlen; i += 32) v = fmax(v, tmpl[i]);
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (threadIdx.x == 0) vmax_s = v;
-  }
   __shared__ float tmpl_f[1024];
   if (sizeof(R) == 4)
     for (int i = threadIdx.x; i < tlen && i < 1024; i += blockDim.x) tmpl_f[i] = float(tmpl[i]);
   __syncthreads();
-  const double vmax = vmax_s;
   const int nr = reach_samples(p);
   const int zs = p.samples_zs;
+  const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
+  const R inv_q = R(1.0 / p.spe_ref_charge);
+  const R vthr = R(p.min_voltage);
+  const double gap = p.spe_max_time + 4.0 * p.period;
   long long ng = *G.n;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
@@ -277,17 +283,23 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
     long long slot = D.off[g];
     int scap = D.cap[g];
     int nd = 0;
-    for (int a = 0; a < n;) {
-      int b = next_cluster_end(p, t, a, n);
-      bool keep = double(b - a) * vmax >= p.min_voltage;
-      if (!keep) { a = b; continue; }
-      double k0 = ceil((t[a] - p.period - tdc0) / p.period);
-      double ts = k0 * p.period + tdc0;
-      int L = cluster_length<R>(p, t, a, b, ts, tlen, true);
+    const int nk = g_nkept[g];
+    for (int kc = 0; kc < nk; ++kc) {
+      const WfCluster C = cl[q0 + kc];
+      const int a = C.a;
+      int b = a + 1;                                 // cluster end: first gap > max_time + 4 periods
+      while (b < n) {
+        int i = b + lane_id();
+        unsigned m = __ballot_sync(0xffffffffu, i < n && (t[i] - t[i - 1] > gap));
+        if (m) { b += __ffs(m) - 1; break; }
+        b += n - b < 32 ? n - b : 32;
+      }
+      const long long k0 = C.k0;
+      const double ts = cluster_ts(k0, p.period, tdc0);
+      const int L = C.L;
       // stage each charge's first reached sample and normalised charge (once per charge, not per sample)
       const bool staged = (b - a) <= WF_QSTAGE;
       if (staged) {
-        const R inv_q = R(1.0 / p.spe_ref_charge);
         for (int q = a + lane_id(); q < b; q += 32) {
           if (sizeof(R) == 8) {
             j0_s[q - a] = int32_t(first_sample<R>(p, t[q], ts));
@@ -295,7 +307,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
           } else {
             float dt = float(t[q] - ts);
             dt_s[q - a] = dt;
-            j0_s[q - a] = first_sample_f(dt, float(p.period));
+            j0_s[q - a] = first_sample_f(dt, Pf);
             qn_s[q - a] = R(qc[q]) * inv_q;
           }
         }
@@ -319,7 +331,6 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         }
         R acc = R(0);
         if (sizeof(R) == 4 && staged) {
-          const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
           for (int q = q1; q < lo2; ++q) {
             int ti = tmpl_index_f(j, dt_s[q - a], Pf, ip, tlen);
             if (ti >= 0) acc += R(tmpl_f[ti]) * qn_s[q - a];
@@ -331,7 +342,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
           }
         }
         if (p.noise_on) {
-          long long tk = (long long)k0 + j;
+          long long tk = k0 + j;
           U4 w = keyed(p.seed, ek, (ST_NOISE << 28) | (chan & 0x7FFFu), uint32_t(tk >> 1));
           R z0, z1;
           Math<R>::normal_pair(w, &z0, &z1);
@@ -340,20 +351,8 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         wave[j] = acc;
       }
       __syncwarp();
-      // samples whose start lies in the window: [i_lo, i_hi] (monotone predicates, found once per cluster)
-      int i_lo = 0, i_hi = -1;
-      {
-        double a0 = ceil((p.window_lo - ts) / p.period);
-        long long c = (long long)fmax(a0 - 1.0, 0.0);
-        while (c < L && !(ts + double(c) * p.period >= p.window_lo)) ++c;
-        while (c > 0 && ts + double(c - 1) * p.period >= p.window_lo) --c;
-        i_lo = int(c);
-        double b0 = floor((p.window_hi - ts) / p.period);
-        long long d = (long long)fmin(b0 + 1.0, double(L - 1));
-        while (d >= 0 && !(ts + double(d) * p.period <= p.window_hi)) --d;
-        while (d + 1 < L && ts + double(d + 1) * p.period <= p.window_hi) ++d;
-        i_hi = int(d);
-      }
+      int i_lo, i_hi;
+      window_bounds(p, ts, L, &i_lo, &i_hi);
       // zero suppression over chunks of 32 samples
       int next_i = 0;
       for (int base = 0; base < L; base += 32) {
@@ -362,7 +361,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         if (i < L) {
           for (int d = -2; d <= 2 && !w; ++d) {
             int k = i + d;
-            if (k >= 0 && k < L && wave[k] > R(p.min_voltage)) w = true;
+            if (k >= 0 && k < L && wave[k] > vthr) w = true;
           }
         }
         bool inwin = i >= i_lo && i <= i_hi;
@@ -372,10 +371,9 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
           if (next_i > base) m &= (next_i - base >= 32) ? 0u : ~((1u << (next_i - base)) - 1u);
           if (!m) break;
           int i0 = base + __ffs(m) - 1;
-          // emit digi at i0
+          // emit digi at i0; its start TDC (start - TDC0) / P is the integer tick k0 + i0
           if (nd < scap) {
             long long o = slot + nd;
-            double st0 = ts + double(i0) * p.period;
             if (lane_id() < zs) {
               int c = i0 + lane_id();
               double v = c < L ? double(wave[c]) : 0.0;
@@ -384,9 +382,9 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
             }
             if (lane_id() == 0) {
               D.chan[o] = lab;
-              D.start[o] = st0;
+              D.start[o] = __dadd_rn(ts, __dmul_rn(double(i0), p.period));
               D.tdc0[o] = tdc0;
-              D.starttdc[o] = (long long)rint((st0 - tdc0) / p.period);
+              D.starttdc[o] = k0 + i0;
             }
           }
           ++nd;
@@ -394,7 +392,6 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         }
       }
       __syncwarp();
-      a = b;
     }
     if (lane_id() == 0) {
       D.n[g] = nd;
