@@ -325,6 +325,9 @@ struct SipmShared {
   R* ph_t;
   uint32_t* ph_key;
   uint32_t* ph_loc;
+  R* ph_uf;                      // firing uniform of the photon (call 0), drawn once
+  uint16_t* ph_pix;              // its pixel (0xFFFF: inactive pixel), drawn once
+  uint8_t* ph_ct;                // its cross-talk mask once drawn (0xFF: not drawn yet)
   R* last;
   uint32_t* bm;
   R* tr_t;
@@ -340,7 +343,7 @@ struct SipmShared {
 template <typename R>
 __host__ __device__ inline size_t sipm_smem_per_warp(int cap) {
   size_t b = 0;
-  b += size_t(cap) * (sizeof(R) + 8);          // ph_t, ph_key, ph_loc
+  b += size_t(cap) * (2 * sizeof(R) + 8 + 2 + 1);   // ph_t, ph_key, ph_loc, ph_uf, ph_pix, ph_ct
   b += NPX * sizeof(R);                        // last
   b += 64 * 4;                                 // bm (50 used)
   b += TCAP * (2 * sizeof(R) + 8 + 2);         // traps
@@ -354,6 +357,7 @@ __device__ SipmShared<R> carve(char* base, int cap) {
   char* q = base;
   S.last = reinterpret_cast<R*>(q); q += NPX * sizeof(R);
   S.ph_t = reinterpret_cast<R*>(q); q += size_t(cap) * sizeof(R);
+  S.ph_uf = reinterpret_cast<R*>(q); q += size_t(cap) * sizeof(R);
   S.tr_t = reinterpret_cast<R*>(q); q += TCAP * sizeof(R);
   S.tr_uf = reinterpret_cast<R*>(q); q += TCAP * sizeof(R);
   S.tr_id = reinterpret_cast<long long*>(q); q += TCAP * 8;
@@ -365,6 +369,8 @@ __device__ SipmShared<R> carve(char* base, int cap) {
   S.fr_pix = reinterpret_cast<uint16_t*>(q); q += 64 * 2;
   S.fr_m = reinterpret_cast<uint16_t*>(q); q += 64 * 2;
   S.cand = reinterpret_cast<uint16_t*>(q); q += 256 * 2;
+  S.ph_pix = reinterpret_cast<uint16_t*>(q); q += size_t(cap) * 2;
+  S.ph_ct = reinterpret_cast<uint8_t*>(q); q += size_t(cap);
   return S;
 }
 
@@ -390,24 +396,45 @@ __device__ __forceinline__ int draw_pixel(const CrvParams& p, const CrvPixels& p
   return ((dead[b >> 5] >> (b & 31)) & 1u) ? -1 : b;
 }
 
+// SiPM constants in the compute type, converted once per block (held in shared memory: in the FP32 kernels a
+// conversion from the FP64 parameters inside the per-photon code would issue on the narrow FP64 pipe every time)
+template <typename R>
+struct SipmK {
+  R vov, tau, p1, p2, q_ct, q_t0, q_t1, life0, life1, t_end;
+  float t_end_dn;                // largest float <= t_end: float times compare with it exactly as with t_end
+  int ct_on, t0_on, t1_on, npx, npy;
+};
+
+template <typename R>
+__device__ __forceinline__ SipmK<R> sipm_consts(const CrvParams& p) {
+  SipmK<R> K;
+  K.vov = R(p.overvoltage); K.tau = R(p.time_constant); K.p1 = R(p.p1); K.p2 = R(p.p2);
+  K.q_ct = R(p.q_ct); K.q_t0 = R(p.q_t0); K.q_t1 = R(p.q_t1);
+  K.life0 = R(p.trap0_lifetime); K.life1 = R(p.trap1_lifetime); K.t_end = R(p.t_end);
+  K.t_end_dn = __double2float_rd(p.t_end);
+  K.ct_on = p.q_ct > 0.0; K.t0_on = p.q_t0 > 0.0; K.t1_on = p.q_t1 > 0.0;
+  K.npx = p.n_pixels_x; K.npy = p.n_pixels_y;
+  return K;
+}
+
 // recovered overvoltage of pixel q at time t (Vov if it never fired)
 template <typename R>
-__device__ __forceinline__ R recovered(const CrvParams& p, const SipmShared<R>& S, int q, R t) {
+__device__ __forceinline__ R recovered(const SipmK<R>& K, const SipmShared<R>& S, int q, R t) {
   using M = Math<R>;
-  if (!bm_test(S.bm, q)) return R(p.overvoltage);
-  return R(p.overvoltage) * (R(1) - M::exp(-(t - S.last[q]) / R(p.time_constant)));
+  if (!bm_test(S.bm, q)) return K.vov;
+  return K.vov * (R(1) - M::exp(-(t - S.last[q]) / K.tau));
 }
 
 template <typename R>
-__device__ __forceinline__ R pfire(const CrvParams& p, R v) {
+__device__ __forceinline__ R pfire(const SipmK<R>& K, R v) {
   using M = Math<R>;
-  return R(p.p1) * (R(1) - M::exp(-v / R(p.p2)));
+  return K.p1 * (R(1) - M::exp(-v / K.p2));
 }
 
 // probability that a node hit m times fires: 1 - (1 - pfire)^m
 template <typename R>
-__device__ __forceinline__ R pfire_m(const CrvParams& p, R v, int m) {
-  R q = R(1) - pfire<R>(p, v);
+__device__ __forceinline__ R pfire_m(const SipmK<R>& K, R v, int m) {
+  R q = R(1) - pfire<R>(K, v);
   R qm = q;
   for (int i = 1; i < m; ++i) qm = qm * q;
   return R(1) - qm;
@@ -427,21 +454,23 @@ struct SipmCtx {
 // Schedule the afterpulses of a fired node (trap0: call 1 (u, u_time), call 4 word 0-1 (u_fire);
 // trap1: call 4 word 2-3 (u), call 5 (u_time, u_fire)).  Returns how many were scheduled into (t, uf).
 template <typename R>
-__device__ __forceinline__ int node_traps(const CrvParams& p, const SipmCtx& C, uint32_t gen, uint32_t idx,
-                                          uint32_t key, R t, R* tt, R* uf) {
+__device__ __forceinline__ int node_traps(const CrvParams& p, const SipmK<R>& K, const SipmCtx& C, uint32_t gen,
+                                          uint32_t idx, uint32_t key, R t, R* tt, R* uf) {
   using M = Math<R>;
-  if (!(p.q_t0 > 0.0) && !(p.q_t1 > 0.0)) return 0;
+  if (!K.t0_on && !K.t1_on) return 0;
   U4 a = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 1, C.chan), key);
+  const bool trap0 = K.t0_on && M::uni(a, 0) < K.q_t0;
+  if (!trap0 && !K.t1_on) return 0;              // call 4 is only read by a trap-0 afterpulse or the trap-1 draw
   U4 b = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 4, C.chan), key);
   int n = 0;
-  if (p.q_t0 > 0.0 && M::uni(a, 0) < R(p.q_t0)) {
-    tt[n] = t - R(p.trap0_lifetime) * M::log(M::uni_open(a, 1));
+  if (trap0) {
+    tt[n] = t - K.life0 * M::log(M::uni_open(a, 1));
     uf[n] = M::uni(b, 0);
     ++n;
   }
-  if (p.q_t1 > 0.0 && M::uni(b, 1) < R(p.q_t1)) {
+  if (K.t1_on && M::uni(b, 1) < K.q_t1) {
     U4 c = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 5, C.chan), key);
-    tt[n] = t - R(p.trap1_lifetime) * M::log(M::uni_open(c, 0));
+    tt[n] = t - K.life1 * M::log(M::uni_open(c, 0));
     uf[n] = M::uni(c, 1);
     ++n;
   }
@@ -450,19 +479,19 @@ __device__ __forceinline__ int node_traps(const CrvParams& p, const SipmCtx& C, 
 
 // cross-talk candidates of a fired node: bit q set for neighbour q (x-1, x+1, y-1, y+1) when it is drawn
 template <typename R>
-__device__ __forceinline__ unsigned node_crosstalk(const CrvParams& p, const SipmCtx& C, uint32_t gen, uint32_t idx,
-                                                   uint32_t key, int pix) {
+__device__ __forceinline__ unsigned node_crosstalk(const CrvParams& p, const SipmK<R>& K, const SipmCtx& C,
+                                                   uint32_t gen, uint32_t idx, uint32_t key, int pix) {
   using M = Math<R>;
-  if (!(p.q_ct > 0.0)) return 0;
+  if (!K.ct_on) return 0;
   U4 a = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 2, C.chan), key);
   U4 b = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 3, C.chan), key);
   int x = pix / 40, y = pix % 40;
-  R q = R(p.q_ct);
+  const R q = K.q_ct;
   unsigned m = 0;
   if (x > 0 && M::uni(a, 0) < q) m |= 1u;
-  if (x + 1 < p.n_pixels_x && M::uni(a, 1) < q) m |= 2u;
+  if (x + 1 < K.npx && M::uni(a, 1) < q) m |= 2u;
   if (y > 0 && M::uni(b, 0) < q) m |= 4u;
-  if (y + 1 < p.n_pixels_y && M::uni(b, 1) < q) m |= 8u;
+  if (y + 1 < K.npy && M::uni(b, 1) < q) m |= 8u;
   return m;
 }
 
@@ -515,8 +544,8 @@ __device__ __forceinline__ int make_frontier(const SipmShared<R>& S, int nc, con
 
 // Cross-talk cascade of one fired primary (generation 1 onwards), frontier spread over the lanes.
 template <typename R>
-__device__ void run_cascade(const CrvParams& p, const SipmShared<R>& S, const uint32_t* dead, SipmCtx& C,
-                            const SipmOut& O, unsigned cand0, int pix0, R t, uint32_t key, long long id) {
+__device__ void run_cascade(const CrvParams& p, const SipmK<R>& K, const SipmShared<R>& S, const uint32_t* dead,
+                            SipmCtx& C, const SipmOut& O, unsigned cand0, int pix0, R t, uint32_t key, long long id) {
   // generation-1 candidates from the primary
   int nc = 0;
   if (lane_id() == 0) {
@@ -540,8 +569,8 @@ __device__ void run_cascade(const CrvParams& p, const SipmShared<R>& S, const ui
       R v = R(0);
       bool fire = false;
       if (act) {
-        v = recovered<R>(p, S, q, t);
-        R pm = pfire_m<R>(p, v, S.fr_m[i]);
+        v = recovered<R>(K, S, q, t);
+        R pm = pfire_m<R>(K, v, S.fr_m[i]);
         U4 w = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, uint32_t(i), 0, C.chan), key);
         fire = Math<R>::uni(w, 1) < pm;
       }
@@ -554,8 +583,8 @@ __device__ void run_cascade(const CrvParams& p, const SipmShared<R>& S, const ui
         put_charge(O, C, pos, double(t), double(v), id);
         S.last[q] = t;
         bm_set(S.bm, q);
-        ntr = node_traps<R>(p, C, gen, uint32_t(i), key, t, tt, uf);
-        ct = node_crosstalk<R>(p, C, gen, uint32_t(i), key, q);
+        ntr = node_traps<R>(p, K, C, gen, uint32_t(i), key, t, tt, uf);
+        ct = node_crosstalk<R>(p, K, C, gen, uint32_t(i), key, q);
       }
       C.nq += __popc(fm);
       // traps in node order
@@ -589,11 +618,20 @@ __device__ void run_cascade(const CrvParams& p, const SipmShared<R>& S, const ui
 
 // Serial-semantics simulation of one SiPM whose sorted photons (n <= cap) sit in S.ph_*.
 template <typename R>
-__device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const SipmShared<R>& S, const uint32_t* dead,
-                              SipmCtx& C, const SipmOut& O, int n, const long long* photon_id, long long gstart,
-                              long long id_base) {
+__device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPixels& px, const SipmShared<R>& S,
+                              const uint32_t* dead, SipmCtx& C, const SipmOut& O, int n, const long long* photon_id,
+                              long long gstart, long long id_base) {
   using M = Math<R>;
   for (int w = lane_id(); w < 64; w += 32) S.bm[w] = 0u;
+  // The draws of a photon do not depend on the pixel state: take them once here.  A 32-photon step below commits
+  // only up to the first collision or cascade, and the photons after that are evaluated again in the next step.
+  for (int i = lane_id(); i < n; i += 32) {
+    U4 w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), S.ph_key[i]);
+    int pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0));
+    S.ph_pix[i] = pix < 0 ? uint16_t(0xFFFF) : uint16_t(pix);
+    S.ph_uf[i] = M::uni(w0, 1);
+    S.ph_ct[i] = uint8_t(0xFF);
+  }
   __syncwarp();
   int k = 0;
   while (k < n) {
@@ -602,10 +640,9 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
     R t = has ? S.ph_t[i] : R(0);
     uint32_t key = has ? S.ph_key[i] : 0u;
     int pix = -1;
-    U4 w0{0, 0, 0, 0};
     if (has) {
-      w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), key);
-      pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0));
+      const uint16_t pp = S.ph_pix[i];
+      pix = pp == 0xFFFF ? -1 : int(pp);
     }
     bool live = pix >= 0;
     unsigned same = __match_any_sync(FULL, live ? pix : -1 - lane_id());
@@ -614,10 +651,17 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
     unsigned ct = 0;
     R v = R(0);
     if (live && !collide) {
-      v = recovered<R>(p, S, pix, t);
-      R pm = pfire_m<R>(p, v, 1);
-      fire = M::uni(w0, 1) < pm;
-      if (fire) ct = node_crosstalk<R>(p, C, 0, 0, key, pix);
+      v = recovered<R>(K, S, pix, t);
+      R pm = pfire_m<R>(K, v, 1);
+      fire = S.ph_uf[i] < pm;
+      if (fire) {
+        uint8_t c = S.ph_ct[i];
+        if (c == 0xFF) {
+          c = uint8_t(node_crosstalk<R>(p, K, C, 0, 0, key, pix));
+          S.ph_ct[i] = c;
+        }
+        ct = c;
+      }
     }
     int nv = min(n - k, 32);
     unsigned cm = __ballot_sync(FULL, collide);
@@ -627,7 +671,7 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
     int ncommit = (g < f) ? g + 1 : min(f, nv);
     bool commit = lane_id() < ncommit && fire;
     long long id = 0;
-    if (has) id = photon_id ? photon_id[gstart + S.ph_loc[i]] : id_base + (long long)(key >> 16);
+    if (commit) id = photon_id ? photon_id[gstart + S.ph_loc[i]] : id_base + (long long)(key >> 16);
     unsigned fm = __ballot_sync(FULL, commit);
     R tt[2], uf[2];
     int ntr = 0;
@@ -635,7 +679,7 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
       put_charge(O, C, __popc(fm & lanemask_lt()), double(t), double(v), id);
       S.last[pix] = t;
       bm_set(S.bm, pix);
-      ntr = node_traps<R>(p, C, 0, 0, key, t, tt, uf);
+      ntr = node_traps<R>(p, K, C, 0, 0, key, t, tt, uf);
     }
     C.nq += __popc(fm);
     int tot;
@@ -652,7 +696,7 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
       R tg = __shfl_sync(FULL, t, g);
       uint32_t kg = __shfl_sync(FULL, key, g);
       long long idg = __shfl_sync(FULL, id, g);
-      run_cascade<R>(p, S, dead, C, O, c0, p0, tg, kg, idg);
+      run_cascade<R>(p, K, S, dead, C, O, c0, p0, tg, kg, idg);
     }
     k += ncommit;
   }
@@ -661,7 +705,7 @@ __device__ void simulate_sipm(const CrvParams& p, const CrvPixels& px, const Sip
 
 // Afterpulses after all photons, in (time, schedule order); stored after the main records.  Returns the count.
 template <typename R>
-__device__ int run_afterpulses(const CrvParams& p, const SipmShared<R>& S, SipmCtx& C, const SipmOut& O) {
+__device__ int run_afterpulses(const SipmK<R>& K, const SipmShared<R>& S, SipmCtx& C, const SipmOut& O) {
   int ntr = min(C.ntr, TCAP);
   int nap = 0;
   if (lane_id() == 0 && ntr > 0) {
@@ -680,10 +724,10 @@ __device__ int run_afterpulses(const CrvParams& p, const SipmShared<R>& S, SipmC
     }
     for (int a = 0; a < ntr; ++a) {
       R t1 = S.tr_t[a];
-      if (t1 > R(p.t_end)) continue;
+      if (t1 > K.t_end) continue;
       int q = S.tr_pix[a];
-      R v = recovered<R>(p, S, q, t1);
-      if (S.tr_uf[a] < pfire<R>(p, v)) {
+      R v = recovered<R>(K, S, q, t1);
+      if (S.tr_uf[a] < pfire<R>(K, v)) {
         S.last[q] = t1;
         S.bm[q >> 5] |= 1u << (q & 31);
         long long id = S.tr_id[a];
@@ -742,7 +786,9 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
                                                  SipmOut O, Status* status) {
   extern __shared__ __align__(16) char smem[];
   __shared__ uint32_t dead[64];
+  __shared__ SipmK<R> K;
   for (int i = threadIdx.x; i < 64; i += blockDim.x) dead[i] = i < 50 ? px.dead_bits[i] : 0u;
+  if (threadIdx.x == 0) K = sipm_consts<R>(p);
   __syncthreads();
   SipmShared<R> S = carve<R>(smem + size_t(warp_in_block()) * sipm_smem_per_warp<R>(cap), cap);
   for (int q = 0; q < 2; ++q)
@@ -777,7 +823,9 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
       int i = base + lane_id();
       bool in = i < cnt;
       R t = in ? R(ph_time[a + i]) : R(0);
-      bool keep = in && (double(ph_time[a + i]) <= p.t_end);
+      bool keep;
+      if constexpr (sizeof(PT) == 4) keep = in && (float(ph_time[a + i]) <= K.t_end_dn);
+      else keep = in && (double(ph_time[a + i]) <= p.t_end);
       unsigned km = __ballot_sync(FULL, keep);
       if (keep) {
         int o = n + __popc(km & lanemask_lt());
@@ -790,8 +838,8 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
     __syncwarp();
     sort_photons<R>(S, n);
     const long long idb = G.id_base ? G.id_base[g] : 0;
-    simulate_sipm<R>(p, px, S, dead, C, O, n, G.photon_id, a, idb);
-    int nap = run_afterpulses<R>(p, S, C, O);
+    simulate_sipm<R>(p, K, px, S, dead, C, O, n, G.photon_id, a, idb);
+    int nap = run_afterpulses<R>(K, S, C, O);
     int fired = 0;
     for (int w = lane_id(); w < 50; w += 32) fired += __popc(S.bm[w]);
     fired = warp_sum(fired);
