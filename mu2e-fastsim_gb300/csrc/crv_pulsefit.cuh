@@ -416,31 +416,71 @@ __device__ __forceinline__ void eval_f32(const Fit3f& F, const float u[3], const
   g[0] = g0; g[1] = g1; g[2] = g2;
 }
 
+// FP32 <-> FP64 moves by integer bit arithmetic.  On this GPU a conversion instruction issues on the FP64 pipe, as
+// slowly as an FP64 multiply; these forms run on the integer pipe and fall back to the instruction only outside the
+// normal range.  f2d is exact; d2f_trunc truncates the mantissa (at most one FP32 ulp below round-to-nearest).
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if ((u & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+__device__ __forceinline__ float d2f_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = int((b >> 52) & 0x7FFu);
+  if (E < 897 || E > 1150) return (float)x;
+  const uint32_t u = uint32_t((b >> 32) & 0x80000000ull) | (uint32_t(E - 896) << 23) | uint32_t((b >> 29) & 0x7FFFFFull);
+  return __uint_as_float(u);
+}
+
+// finite and non-zero, tested on the bits
+__device__ __forceinline__ bool finite_nonzero(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x7FFFFFFFFFFFFFFFull) != 0ull && ((b >> 52) & 0x7FFull) != 0x7FFull;
+}
+
 // symmetric 3x3 solve M x = b (M packed 00 01 02 11 12 22): cofactors, determinant and adjugate product in FP64
 // (products of FP32 inputs are exact there), the final division by the determinant in FP32
 __device__ __forceinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {
-  const double m00 = M[0], m01 = M[1], m02 = M[2], m11 = M[3], m12 = M[4], m22 = M[5];
+  const double m00 = f2d(M[0]), m01 = f2d(M[1]), m02 = f2d(M[2]), m11 = f2d(M[3]), m12 = f2d(M[4]), m22 = f2d(M[5]);
   const double c00 = m11 * m22 - m12 * m12;
   const double c01 = m12 * m02 - m01 * m22;
   const double c02 = m01 * m12 - m11 * m02;
   const double det = m00 * c00 + m01 * c01 + m02 * c02;
-  if (!(det != 0.0) || !(fabs(det) < 1e300)) return false;
+  if (!finite_nonzero(det)) return false;
   const double c11 = m00 * m22 - m02 * m02;
   const double c12 = m01 * m02 - m00 * m12;
   const double c22 = m00 * m11 - m01 * m01;
-  const double b0 = b[0], b1 = b[1], b2 = b[2];
+  const double b0 = f2d(b[0]), b1 = f2d(b[1]), b2 = f2d(b[2]);
   const double y0 = c00 * b0 + c01 * b1 + c02 * b2;
   const double y1 = c01 * b0 + c11 * b1 + c12 * b2;
   const double y2 = c02 * b0 + c12 * b1 + c22 * b2;
-  const float df = float(det);
-  if (fabsf(df) < 1e-30f || !(fabsf(df) < 1e30f)) {          // outside the comfortable FP32 range: FP64 division
-    const double r = 1.0 / det;
-    x[0] = float(y0 * r); x[1] = float(y1 * r); x[2] = float(y2 * r);
+  const float df = d2f_trunc(det);
+  const float r = 1.0f / df;
+  if (!(fabsf(r) < 1e30f) || !(fabsf(r) > 1e-30f)) {       // determinant outside the comfortable FP32 range
+    const double rd = 1.0 / det;
+    x[0] = float(y0 * rd); x[1] = float(y1 * rd); x[2] = float(y2 * rd);
     return true;
   }
-  const float r = 1.0f / df;
-  x[0] = float(y0) * r; x[1] = float(y1) * r; x[2] = float(y2) * r;
+  x[0] = d2f_trunc(y0) * r; x[1] = d2f_trunc(y1) * r; x[2] = d2f_trunc(y2) * r;
   return true;
+}
+
+// Hessian check of the FP32-mixed fit: the smallest eigenvalue above 1e-12 of the matrix's scale, as H - tau I
+// positive definite (Sylvester: every leading principal minor positive), tau = 1e-12 max(trace, 1e-300); the trace
+// stands in for the largest eigenvalue (within a factor 3 of it for a positive semi-definite H).
+__device__ __forceinline__ bool hessian_ok(const float H[6]) {
+  const double h00 = f2d(H[0]), h01 = f2d(H[1]), h02 = f2d(H[2]), h11 = f2d(H[3]), h12 = f2d(H[4]), h22 = f2d(H[5]);
+  const double tr = h00 + h11 + h22;
+  const double tau = 1e-12 * (tr > 1e-300 ? tr : 1e-300);
+  const double a = h00 - tau, d = h11 - tau, f = h22 - tau;
+  const double m2 = a * d - h01 * h01;
+  const double m3 = a * (d * f - h12 * h12) - h01 * (h01 * f - h12 * h02) + h02 * (h01 * h12 - d * h02);
+  return a > 0.0 && m2 > 0.0 && m3 > 0.0;
 }
 
 __device__ __forceinline__ bool same3(const float a[3], const float b[3]) {
@@ -451,20 +491,13 @@ __device__ __forceinline__ bool same3(const float a[3], const float b[3]) {
 // Skipped work is exactly work whose outcome is known: a step that leaves the FP32 parameters unchanged evaluates to
 // the same chi2 and is rejected; a rejected step at the clamped damping, or a Gauss-Newton step that no scale
 // improves, leaves the state as it was, so every later step would repeat it.
-__device__ inline void fit_f32(const Fit3& F64, const double p0[3], const float* yw, double period, int P, int iters,
-                        double par[3], double* chi2_out, bool* conv, bool* hok) {
-  Fit3f F;
-  for (int k = 0; k < 3; ++k) {
-    F.lo[k] = float(k == 1 ? F64.lo[k] - F64.t0 : F64.lo[k]);
-    F.w[k] = float(F64.hi[k] - F64.lo[k]);
-    F.half[k] = float(F64.half[k]);
-  }
+__device__ inline void fit_f32(const Fit3f& F, const float p0[3], const float* yw, float Pf, int P, int iters,
+                               float u_out[3], float* chi2_out, bool* conv, bool* hok) {
   float u[3];
   for (int k = 0; k < 3; ++k) {
-    float c = 2.0f * float(p0[k] - F64.lo[k]) / F.w[k] - 1.0f;
+    float c = 2.0f * (p0[k] - F.lo[k]) / F.w[k] - 1.0f;
     u[k] = asinf(fminf(fmaxf(c, -1.0f), 1.0f));
   }
-  const float Pf = float(period);
   float chi2, H[6], g[3];
   eval_f32(F, u, yw, Pf, P, &chi2, H, g);
   float lam = 1e-3f;
@@ -517,29 +550,15 @@ __device__ inline void fit_f32(const Fit3& F64, const double p0[3], const float*
   bool okh;
   if (solve_sym64(M, g, st)) {
     edm = 0.5f * (g[0] * st[0] + g[1] * st[1] + g[2] * st[2]);
-    const double Hd[6] = {H[0], H[1], H[2], H[3], H[4], H[5]};
-    double Hm[3][3], e[3];
-    sym3(Hd, Hm);
-    eig3(Hm, e);
-    okh = e[0] > 1e-12 * fmax(e[2], 1e-300);
+    okh = hessian_ok(H);
   } else {
     edm = INFINITY;
     okh = false;
   }
   *conv = isfinite(edm) && (edm <= 1e-3f * fmaxf(chi2, 1.0f));
   *hok = okh;
-  for (int k = 0; k < 3; ++k) par[k] = F64.lo[k] + (F64.hi[k] - F64.lo[k]) * (double(sinf(u[k])) + 1.0) * 0.5;
-  *chi2_out = double(chi2);
-}
-
-template <typename R>
-__device__ __forceinline__ void fit_any(const Fit3& F, const double p0[3], const R* yw, long long tdc_fs,
-                                        double period, int P, int iters, double par[3], double* chi2, bool* conv,
-                                        bool* hok) {
-  if constexpr (sizeof(R) == 4)
-    fit_f32(F, p0, reinterpret_cast<const float*>(yw), period, P, iters, par, chi2, conv, hok);
-  else
-    fit_lane<R>(F, p0, yw, tdc_fs, period, P, iters, par, chi2, conv, hok);
+  for (int k = 0; k < 3; ++k) u_out[k] = u[k];
+  *chi2_out = chi2;
 }
 
 // ---- rounds over a device task list -----------------------------------------------------------------------------
@@ -601,66 +620,155 @@ __device__ __forceinline__ bool pf_begin(const CrvParams& p, const WaveIn& W, do
   return peak_lane<R>(p, y, n, 0, &st.ps, &st.pe, &st.fs, &st.fe);
 }
 
-// fit, record and subtract the pending pulse, then search the next one; true when another pulse is pending
-template <typename R>
-__device__ __forceinline__ bool pf_step(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses,
-                                        const PulseSlots& S, long long w, PfState& st) {
-  const double E = 2.718281828459045;
+// FP32-mixed pulse step: the fit window, bounds and fitted values relative to the window's first sample in FP32;
+// FP64 for the window's absolute time and the absolute pulse times derived from it
+__device__ __forceinline__ bool pf_step_f32(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses,
+                                           const PulseSlots& S, long long w, PfState& st) {
+  const float E = 2.718281828459045f;
   const int n = W.n[w];
-  R* y = reinterpret_cast<R*>(yscr) + W.off[w];
+  float* y = reinterpret_cast<float*>(yscr) + W.off[w];
   const long long st_tdc = W.start_tdc[w];
   const int ps = st.ps, pe = st.pe, fs = st.fs, fe = st.fe;
   const int P = fe - fs + 1;
-  const double yps = double(y[ps]);
-  const double t_ps = double(st_tdc + ps) * p.period;
-  const double t_pe = double(st_tdc + pe) * p.period;
-  const double t_peak = 0.5 * (t_ps + t_pe);
-  Fit3 F;
-  F.lo[0] = yps * E * p.min_height_ratio; F.hi[0] = yps * E * p.max_height_ratio;
-  F.lo[1] = t_ps - p.max_time_difference; F.hi[1] = t_pe + p.max_time_difference;
-  F.lo[2] = p.min_beta; F.hi[2] = p.max_beta;
-  for (int k = 0; k < 3; ++k) F.half[k] = (F.hi[k] - F.lo[k]) * 0.5;
-  F.t0 = double(st_tdc + fs) * p.period;
-  const double p0[3] = {yps * E, t_peak, p.default_beta};
-  double par[3], chi2;
+  const float Pf = float(p.period);
+  const float yps = y[ps];
+  const float mtd = float(p.max_time_difference);
+  Fit3f F;
+  F.lo[0] = yps * E * float(p.min_height_ratio);
+  F.w[0] = yps * E * float(p.max_height_ratio) - F.lo[0];
+  F.lo[1] = float(ps - fs) * Pf - mtd;
+  F.w[1] = float(pe - ps) * Pf + 2.0f * mtd;
+  F.lo[2] = float(p.min_beta);
+  F.w[2] = float(p.max_beta) - F.lo[2];
+  for (int k = 0; k < 3; ++k) F.half[k] = F.w[k] * 0.5f;
+  const float tpk_rel = 0.5f * float(ps + pe - 2 * fs) * Pf;      // peak time relative to the window start
+  const float p0[3] = {yps * E, tpk_rel, float(p.default_beta)};
+  float u[3], chi2;
   bool conv, hok;
-  fit_any<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
+  fit_f32(F, p0, y + fs, Pf, P, p.lm_iterations, u, &chi2, &conv, &hok);
   const int ndf = P - 3;
   bool nearlim = false;
+  float par[3];
+  const float tol = float(p.limit_tolerance);
   for (int k = 0; k < 3; ++k) {
-    const double span = F.hi[k] - F.lo[k];
-    if ((par[k] - F.lo[k]) / span < p.limit_tolerance || (F.hi[k] - par[k]) / span < p.limit_tolerance)
-      nearlim = true;
+    const float fr = (sinf(u[k]) + 1.0f) * 0.5f;                   // (par - lo) / span
+    par[k] = F.lo[k] + F.w[k] * fr;
+    if (fr < tol || 1.0f - fr < tol) nearlim = true;
   }
   const bool failed = !conv || !hok || nearlim;
-  const double A = par[0], mu = par[1], b = par[2];
-  const double height = failed ? yps : A / E;
-  const double beta = failed ? p.default_beta : b;
-  const double tp = failed ? t_peak : mu;
+  const double t0 = double(st_tdc + fs) * p.period;               // absolute time of the window's first sample
+  const float A = par[0], b = par[2];
+  const double mu = t0 + f2d(par[1]);
+  const float height = failed ? yps : A / E;
+  const float beta = failed ? float(p.default_beta) : b;
+  const double tp = failed ? t0 + f2d(tpk_rel) : mu;
   const bool fseq = failed || st.fb;
   const int seq = st.cnt;
   if (seq < S.cap[w]) {
     PulseRec& r = S.rec[S.off[w] + seq];
-    r.pe = (failed ? yps * E * p.default_beta : A * b) / W.area[w];
-    r.peph = height / W.height[w];
+    r.pe = f2d((failed ? yps * E * float(p.default_beta) : A * b) / d2f_trunc(W.area[w]));
+    r.peph = f2d(height / d2f_trunc(W.height[w]));
     r.time = tp;
-    r.height = height;
-    r.beta = beta;
-    r.chi2 = (failed || ndf <= 0) ? -1.0 : chi2 / double(ndf > 1 ? ndf : 1);
-    r.letime = tp - p.le_time_factor * beta;
+    r.height = f2d(height);
+    r.beta = f2d(beta);
+    r.chi2 = (failed || ndf <= 0) ? -1.0 : f2d(chi2 / float(ndf > 1 ? ndf : 1));
+    r.letime = tp - p.le_time_factor * f2d(beta);
     r.ped = st.ped;
-    r.A = A; r.mu = mu; r.b = b;
+    r.A = f2d(A); r.mu = mu; r.b = f2d(b);
     r.seq = seq;
     r.failed = fseq; r.zerondf = ndf <= 0; r.pedfromdb = !st.under; r.pad = 0;
   }
   st.cnt = seq + 1;
   st.fb = fseq;
-  int lo, hi;
-  subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
-  st.near = st.near || near_lane<R>(y, n, lo - 1, hi + 1, R(p.min_adc_difference), R(p.knife_edge_adc));
+  // subtract round(fit) walking out from the mode's sample
+  int im = fs + int(floorf(par[1] / Pf));
+  if (im < 0) im = 0;
+  if (im > n - 1) im = n - 1;
+  int lo = im, hi = im;
+  {
+    const float mu_rel = par[1] - float(im - fs) * Pf;             // mode relative to sample im
+    const float inv_b = 1.0f / b;
+    for (int dir = -1; dir <= 1; dir += 2) {
+      for (int i = im + (dir > 0 ? 1 : 0); i >= 0 && i < n; i += dir) {
+        const float tr = float(i - im) * Pf;
+        const float z = (tr - mu_rel) * inv_b;
+        const float gv = A * __expf(-z - __expf(-z));
+        y[i] -= round_half_away_f(gv);
+        if (dir < 0) lo = i; else hi = i;
+        if (fabsf(gv) < 0.25f && ((dir < 0 && tr < mu_rel) || (dir > 0 && tr > mu_rel))) break;
+      }
+    }
+  }
+  st.near = st.near || near_lane<float>(y, n, lo - 1, hi + 1, float(p.min_adc_difference), float(p.knife_edge_adc));
   st.start = fe;
   if (st.cnt >= max_pulses) return false;
-  return peak_lane<R>(p, y, n, st.start, &st.ps, &st.pe, &st.fs, &st.fe);
+  return peak_lane<float>(p, y, n, st.start, &st.ps, &st.pe, &st.fs, &st.fe);
+}
+
+// fit, record and subtract the pending pulse, then search the next one; true when another pulse is pending
+template <typename R>
+__device__ __forceinline__ bool pf_step(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses,
+                                        const PulseSlots& S, long long w, PfState& st) {
+  if constexpr (sizeof(R) == 4) {
+    return pf_step_f32(p, W, yscr, max_pulses, S, w, st);
+  } else {
+    const double E = 2.718281828459045;
+    const int n = W.n[w];
+    R* y = reinterpret_cast<R*>(yscr) + W.off[w];
+    const long long st_tdc = W.start_tdc[w];
+    const int ps = st.ps, pe = st.pe, fs = st.fs, fe = st.fe;
+    const int P = fe - fs + 1;
+    const double yps = double(y[ps]);
+    const double t_ps = double(st_tdc + ps) * p.period;
+    const double t_pe = double(st_tdc + pe) * p.period;
+    const double t_peak = 0.5 * (t_ps + t_pe);
+    Fit3 F;
+    F.lo[0] = yps * E * p.min_height_ratio; F.hi[0] = yps * E * p.max_height_ratio;
+    F.lo[1] = t_ps - p.max_time_difference; F.hi[1] = t_pe + p.max_time_difference;
+    F.lo[2] = p.min_beta; F.hi[2] = p.max_beta;
+    for (int k = 0; k < 3; ++k) F.half[k] = (F.hi[k] - F.lo[k]) * 0.5;
+    F.t0 = double(st_tdc + fs) * p.period;
+    const double p0[3] = {yps * E, t_peak, p.default_beta};
+    double par[3], chi2;
+    bool conv, hok;
+    fit_lane<R>(F, p0, y + fs, st_tdc + fs, p.period, P, p.lm_iterations, par, &chi2, &conv, &hok);
+    const int ndf = P - 3;
+    bool nearlim = false;
+    for (int k = 0; k < 3; ++k) {
+      const double span = F.hi[k] - F.lo[k];
+      if ((par[k] - F.lo[k]) / span < p.limit_tolerance || (F.hi[k] - par[k]) / span < p.limit_tolerance)
+        nearlim = true;
+    }
+    const bool failed = !conv || !hok || nearlim;
+    const double A = par[0], mu = par[1], b = par[2];
+    const double height = failed ? yps : A / E;
+    const double beta = failed ? p.default_beta : b;
+    const double tp = failed ? t_peak : mu;
+    const bool fseq = failed || st.fb;
+    const int seq = st.cnt;
+    if (seq < S.cap[w]) {
+      PulseRec& r = S.rec[S.off[w] + seq];
+      r.pe = (failed ? yps * E * p.default_beta : A * b) / W.area[w];
+      r.peph = height / W.height[w];
+      r.time = tp;
+      r.height = height;
+      r.beta = beta;
+      r.chi2 = (failed || ndf <= 0) ? -1.0 : chi2 / double(ndf > 1 ? ndf : 1);
+      r.letime = tp - p.le_time_factor * beta;
+      r.ped = st.ped;
+      r.A = A; r.mu = mu; r.b = b;
+      r.seq = seq;
+      r.failed = fseq; r.zerondf = ndf <= 0; r.pedfromdb = !st.under; r.pad = 0;
+    }
+    st.cnt = seq + 1;
+    st.fb = fseq;
+    int lo, hi;
+    subtract_lane<R>(p, y, n, st_tdc, A, mu, b, &lo, &hi);
+    st.near = st.near || near_lane<R>(y, n, lo - 1, hi + 1, R(p.min_adc_difference), R(p.knife_edge_adc));
+    st.start = fe;
+    if (st.cnt >= max_pulses) return false;
+    return peak_lane<R>(p, y, n, st.start, &st.ps, &st.pe, &st.fs, &st.fe);
+  }
 }
 
 __device__ __forceinline__ void pf_finish(const PulseSlots& S, Status* status, long long w, const PfState& st) {
