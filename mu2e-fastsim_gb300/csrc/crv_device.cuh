@@ -160,6 +160,33 @@ __device__ __forceinline__ void dsincospi(double x, double* sp, double* cp) {
 // Precision policy: the FP64 path uses the project's functions above (bit-exact with the oracle); the FP32-mixed path
 // uses 24-bit uniforms and hardware float transcendentals.
 
+// FP32 <-> FP64 moves by integer bit arithmetic.  On this GPU a conversion instruction issues on the FP64 pipe, as
+// slowly as an FP64 multiply; these forms run on the integer pipe and fall back to the instruction only outside the
+// normal range.  f2d is exact; d2f_trunc truncates the mantissa (at most one FP32 ulp below round-to-nearest).
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if ((u & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+__device__ __forceinline__ float d2f_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = int((b >> 52) & 0x7FFu);
+  if (E < 897 || E > 1150) return (float)x;
+  const uint32_t u = uint32_t((b >> 32) & 0x80000000ull) | (uint32_t(E - 896) << 23) | uint32_t((b >> 29) & 0x7FFFFFull);
+  return __uint_as_float(u);
+}
+
+// finite and non-zero, tested on the bits
+__device__ __forceinline__ bool finite_nonzero(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x7FFFFFFFFFFFFFFFull) != 0ull && ((b >> 52) & 0x7FFull) != 0x7FFull;
+}
+
 template <typename R> struct Math;
 
 template <> struct Math<double> {

@@ -416,33 +416,6 @@ __device__ __forceinline__ void eval_f32(const Fit3f& F, const float u[3], const
   g[0] = g0; g[1] = g1; g[2] = g2;
 }
 
-// FP32 <-> FP64 moves by integer bit arithmetic.  On this GPU a conversion instruction issues on the FP64 pipe, as
-// slowly as an FP64 multiply; these forms run on the integer pipe and fall back to the instruction only outside the
-// normal range.  f2d is exact; d2f_trunc truncates the mantissa (at most one FP32 ulp below round-to-nearest).
-__device__ __forceinline__ double f2d(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  if ((u & 0x7FFFFFFFu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
-  if (e == 0u || e == 0xFFu) return (double)f;
-  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
-                               ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
-
-__device__ __forceinline__ float d2f_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int E = int((b >> 52) & 0x7FFu);
-  if (E < 897 || E > 1150) return (float)x;
-  const uint32_t u = uint32_t((b >> 32) & 0x80000000ull) | (uint32_t(E - 896) << 23) | uint32_t((b >> 29) & 0x7FFFFFull);
-  return __uint_as_float(u);
-}
-
-// finite and non-zero, tested on the bits
-__device__ __forceinline__ bool finite_nonzero(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return (b & 0x7FFFFFFFFFFFFFFFull) != 0ull && ((b >> 52) & 0x7FFull) != 0x7FFull;
-}
-
 // symmetric 3x3 solve M x = b (M packed 00 01 02 11 12 22): cofactors, determinant and adjugate product in FP64
 // (products of FP32 inputs are exact there), the final division by the determinant in FP32
 __device__ __forceinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {

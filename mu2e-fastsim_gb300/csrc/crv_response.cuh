@@ -500,13 +500,17 @@ __device__ __forceinline__ int neighbour(int pix, int q) {
 }
 
 // Append a charge record (lane-ordered position pos relative to C.nq) if it fits.
-__device__ __forceinline__ void put_charge(const SipmOut& O, const SipmCtx& C, int pos, double t, double v,
-                                           long long id) {
+// widening to the FP64 output columns (FP32: by integer bit arithmetic, off the FP64 pipe)
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) { return f2d(x); }
+
+template <typename R>
+__device__ __forceinline__ void put_charge(const SipmOut& O, const SipmCtx& C, int pos, R t, R v, long long id) {
   int k = C.nq + pos;
   if (k < C.cap) {
     long long o = C.slot + k;
-    O.t[o] = t;
-    O.v[o] = v;
+    O.t[o] = widen(t);
+    O.v[o] = widen(v);
     O.id[o] = id;
   }
 }
@@ -580,7 +584,7 @@ __device__ void run_cascade(const CrvParams& p, const SipmK<R>& K, const SipmSha
       int ntr = 0;
       unsigned ct = 0;
       if (fire) {
-        put_charge(O, C, pos, double(t), double(v), id);
+        put_charge<R>(O, C, pos, t, v, id);
         S.last[q] = t;
         bm_set(S.bm, q);
         ntr = node_traps<R>(p, K, C, gen, uint32_t(i), key, t, tt, uf);
@@ -676,7 +680,7 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     R tt[2], uf[2];
     int ntr = 0;
     if (commit) {
-      put_charge(O, C, __popc(fm & lanemask_lt()), double(t), double(v), id);
+      put_charge<R>(O, C, __popc(fm & lanemask_lt()), t, v, id);
       S.last[pix] = t;
       bm_set(S.bm, pix);
       ntr = node_traps<R>(p, K, C, 0, 0, key, t, tt, uf);
@@ -734,8 +738,8 @@ __device__ int run_afterpulses(const SipmK<R>& K, const SipmShared<R>& S, SipmCt
         int kk = C.nq + nap;
         if (kk < C.cap) {
           long long o = C.slot + kk;
-          O.t[o] = double(t1);
-          O.v[o] = double(v);
+          O.t[o] = widen(t1);
+          O.v[o] = widen(v);
           O.id[o] = id;
         }
         ++nap;
@@ -745,6 +749,23 @@ __device__ int run_afterpulses(const SipmK<R>& K, const SipmShared<R>& S, SipmCt
   nap = __shfl_sync(FULL, nap, 0);
   __syncwarp();
   return nap;
+}
+
+// Order-preserving integer image of an FP64 time, -0 taken as +0 (as the numeric comparison does): FP64 sort
+// comparisons on the integer pipe instead of the FP64 pipe.
+__device__ __forceinline__ unsigned long long ord_time(double t) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(t);
+  if (u == 0x8000000000000000ull) u = 0ull;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// (ta, ka) > (tb, kb) in (time, key) order
+__device__ __forceinline__ bool after(float ta, uint32_t ka, float tb, uint32_t kb) {
+  return (ta > tb) || (ta == tb && ka > kb);
+}
+__device__ __forceinline__ bool after(double ta, uint32_t ka, double tb, uint32_t kb) {
+  const unsigned long long a = ord_time(ta), b = ord_time(tb);
+  return (a > b) || (a == b && ka > kb);
 }
 
 // sort the staged photons by (time, key) (warp bitonic over the next power of two)
@@ -761,13 +782,12 @@ __device__ void sort_photons(const SipmShared<R>& S, int n) {
   for (int size = 2; size <= P; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
       for (int q = lane_id(); q < (P >> 1); q += 32) {
-        int lo = 2 * stride * (q / stride) + (q % stride);
-        int hi = lo + stride;
-        bool up = (lo & size) == 0;
-        R ta = S.ph_t[lo], tb = S.ph_t[hi];
-        uint32_t ka = S.ph_key[lo], kb = S.ph_key[hi];
-        bool gt = (ta > tb) || (ta == tb && ka > kb);
-        if (gt == up) {
+        const int lo = ((q & ~(stride - 1)) << 1) | (q & (stride - 1));   // stride is a power of two
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const R ta = S.ph_t[lo], tb = S.ph_t[hi];
+        const uint32_t ka = S.ph_key[lo], kb = S.ph_key[hi];
+        if (after(ta, ka, tb, kb) == up) {
           S.ph_t[lo] = tb; S.ph_t[hi] = ta;
           S.ph_key[lo] = kb; S.ph_key[hi] = ka;
           uint32_t la = S.ph_loc[lo];
