@@ -161,6 +161,108 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def uneven_chunk(n_wf, seed, device, period=12.55, area=400.0):
+    """Device-generated waveforms of the uneven batched-fit workload: length uniform over {32, 64, 128, 256, 512},
+    1-12 Gumbel pulses of log-uniform 5-500 PE and beta U(10, 25) ns at uniform times in the window, pedestal 100
+    with N(0, 2) ADC noise, int16 samples clipped to [0, 4095]."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    lens = torch.tensor([32, 64, 128, 256, 512], device=device)[torch.randint(0, 5, (n_wf,), generator=g,
+                                                                               device=device)]
+    off = torch.cumsum(lens, 0) - lens
+    ns = int(lens.sum().item())
+    start = torch.randint(0, 200, (n_wf,), generator=g, device=device)
+    wf_of = torch.repeat_interleave(torch.arange(n_wf, device=device), lens)
+    t = ((start[wf_of] + torch.arange(ns, device=device) - off[wf_of]) * period).float()
+    y = torch.full((ns,), 100.0, device=device) + 2.0 * torch.randn(ns, generator=g, device=device)
+    npul = torch.randint(1, 13, (n_wf,), generator=g, device=device)
+    t0 = (start * period).float()
+    span = (lens * period).float()
+    for k in range(12):
+        u = torch.rand((4, n_wf), generator=g, device=device)
+        pe = torch.exp(np.log(5.0) + u[0] * (np.log(500.0) - np.log(5.0)))
+        beta = 10.0 + 15.0 * u[1]
+        mu = t0 + u[2] * span
+        amp = torch.where(npul > k, pe * area / beta, torch.zeros_like(pe))
+        z = (t - mu[wf_of]) / beta[wf_of]
+        y += amp[wf_of] * torch.exp(-z - torch.exp(-z))
+    adc = torch.clamp(torch.round(y), 0, 4095).to(torch.int16)
+    return dict(off=off, n=lens.to(torch.int32), start=start.to(torch.int64), adc=adc, ns=ns,
+                ped=torch.full((n_wf,), 100.0, dtype=torch.float64, device=device),
+                area=torch.full((n_wf,), area, dtype=torch.float64, device=device),
+                height=torch.full((n_wf,), area / 15.0, dtype=torch.float64, device=device), true=int(npul.sum()))
+
+
+def uneven_pulse_fit(total, chunk, device="cuda"):
+    """Waveforms/s of the batched pulse fit (reconstruct_full: rounds bounded by the waveform length) over `total`
+    device-generated uneven waveforms, FP32-mixed and FP64 plain; device time of the fit calls only."""
+    import torch
+    from crvgpu import config as CF
+    from crvgpu.params import make_params
+    from crvgpu.pulsefit import PulseEngine
+    out = {"waveforms": total, "chunk": chunk}
+    chunks = [uneven_chunk(min(chunk, total - c0), 1000 + c0, device) for c0 in range(0, total, chunk)]
+    out["samples"] = sum(c["ns"] for c in chunks)
+    out["true_pulses"] = sum(c["true"] for c in chunks)
+    for prec in ("fp32", "fp64"):
+        eng = PulseEngine(device)
+        eng.out_factor = 16.0
+        P = make_params(reco=CF.RecoConfig(), precision=prec)
+        P.period = CF.PERIOD
+
+        def run(c):
+            return eng.run(P, c["off"], c["n"], c["start"], c["ped"], c["area"], c["height"], adc16=c["adc"],
+                           max_pulses=2 ** 31 - 1, nsamples=c["ns"])
+        run(chunks[0])                                            # warm-up: workspace and capacities
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        found = 0
+        e0.record()
+        for c in chunks:
+            found += int(run(c)["wf"].numel())
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {"waveforms_per_s": total / (ms / 1000.0), "ms": ms, "pulses": found}
+    if out["fp64"]["waveforms_per_s"]:
+        out["fp32_over_fp64"] = out["fp32"]["waveforms_per_s"] / out["fp64"]["waveforms_per_s"]
+    return out
+
+
+def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=2048):
+    """Serving loop over a resident step pool: isolated run time model, saturated capacity, then Poisson arrivals at
+    `load` of capacity (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
+    import torch
+    from crvgpu import geometry as GM
+    from crvgpu.response import upload_steps
+    from crvgpu.serve import Job, ServeEngine, latency_stats, random_jobs
+    pool = upload_steps(GM.synthetic_steps(pool_events, geom, seed=77), nbars=geom.nbars)
+    free, _ = torch.cuda.mem_get_info()
+    srv = ServeEngine(geom, cond, pool, hbm_budget=int(0.6 * free), max_slots=max_slots, chunk_events=chunk)
+    # isolated run time: alone on an idle device, a small and a large job
+    iso = []
+    for n in (4096, min(131072, pool_events)):
+        t0 = time.perf_counter()
+        srv.run([Job(0, n, seed=3)], realtime=False)
+        iso.append((n, time.perf_counter() - t0))
+    (n1, t1), (n2, t2) = iso
+    rate = (n2 - n1) / max(t2 - t1, 1e-9)
+    overhead = max(0.0, t1 - n1 / rate)
+    rng = np.random.default_rng(seed)
+    burst = random_jobs(n_jobs, rng, max_events=pool_events, pool_events=pool_events)
+    res = srv.run(burst, realtime=False)
+    cap = latency_stats(res, rate, overhead)["events_per_s"]
+    mean_ev = np.mean([j.n_events for j in burst])
+    jobs = random_jobs(n_jobs, np.random.default_rng(seed + 1), max_events=pool_events, pool_events=pool_events,
+                       rate=load * cap / mean_ev)
+    st = latency_stats(srv.run(jobs, realtime=True), rate, overhead)
+    return {"jobs": n_jobs, "slots": len(srv.slots), "slot_footprint_gb": srv.footprint / 1e9,
+            "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",
+            "isolated_events_per_s": rate, "isolated_overhead_s": overhead, "capacity_events_per_s": cap,
+            "offered_load": load, **{k: v for k, v in st.items() if k != "jobs"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -173,6 +275,11 @@ def main():
     ap.add_argument("--warmup-ref", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
+    ap.add_argument("--serve-load", type=float, default=0.8)
+    ap.add_argument("--uneven-waveforms", type=int, default=1 << 22,
+                    help="waveforms of the uneven batched pulse-fit measurement (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -216,10 +323,11 @@ def main():
     eng32 = CH.ChainEngine(geom, cond, cfg32)
     eng64 = CH.ChainEngine(geom, cond, cfg64)
 
-    def one_pass(eng, seed):
-        tot = dict(clusters=0, pulses=0, charges=0, digis=0, waveforms=0, groups=0, hits=0, members=0, events=0)
+    def one_pass(eng, seed, diagnostics=False):
+        tot = dict(clusters=0, pulses=0, charges=0, digis=0, waveforms=0, groups=0, hits=0, members=0, events=0,
+                   photons=0, sipms=0)
         for ds in batches:
-            r = eng.run(ds, seed)
+            r = eng.run(ds, seed, diagnostics=diagnostics)
             tot["clusters"] += r.n_clusters
             tot["pulses"] += r.n_pulses
             tot["charges"] += r.n_charges
@@ -228,6 +336,8 @@ def main():
             tot["hits"] += r.n_hits
             tot["members"] += r.n_members
             tot["events"] += r.n_events
+            tot["photons"] += r.n_photons
+            tot["sipms"] += r.n_sipms
         return tot
 
     def timed(eng, k, w):
@@ -269,7 +379,7 @@ def main():
     # per-kernel device time of one FP32 pass (profiling events; not the timed number)
     torch.cuda.synchronize()
     _capi.profile(True)
-    counts = one_pass(eng32, 5)
+    counts = one_pass(eng32, 5, diagnostics=True)
     torch.cuda.synchronize()
     prof = _capi.profile_read()
     _capi.profile(False)
@@ -288,16 +398,21 @@ def main():
     #               pedestal / area / height 24) + per pulse 104 B out (11 FP64 columns, wf, seq, 3 flags)
     #   k_wf_synth: per charge 16 B in (time, charge) + per digi 152 B out (label, start, TDC0, start TDC, 12 volts,
     #               12 ADC)
+    #   k_sipm_sim: per photon 8 B in (FP32 time, key) + per SiPM 32 B in (first photon, count, label, run, slots)
+    #               + per charge 24 B out (time, voltage, photon id)
     #   k_coinc:    per hit 28 B in (bar, SiPM, sequence, time, PE) + per event 20 B in (first hit, count, key)
     #               + per cluster 120 B out (event, type, PE, start, end, slope, average time, position, flags) + 4 B
     #               per member index
-    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth",), "k_coinc": ("k_coinc",)}
+    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth",), "k_coinc": ("k_coinc",),
+              "k_sipm_sim": ("k_sipm_sim",)}
 
     def alg_bytes(group):
         if group == "pulse fit":
             return (counts["digis"] * 12 * 2 + counts["waveforms"] * 44 + counts["pulses"] * 104) / nb
         if group == "k_wf_synth":
             return (counts["charges"] * 16 + counts["digis"] * 152) / nb
+        if group == "k_sipm_sim":
+            return (counts["photons"] * 8 + counts["sipms"] * 32 + counts["charges"] * 24) / nb
         if group == "k_coinc":
             return (counts["hits"] * 28 + counts["events"] * 20 + counts["clusters"] * 120
                     + counts["members"] * 4) / nb
@@ -369,6 +484,20 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{ev} events of the same workload through the oracle chain on 1 core ({busy:.1f} s)"}
 
+    # the extra measurements below start from a device without the benchmark's own chain engines and batches
+    eng32 = eng64 = batches = r = ds = r64 = r32 = pe64 = pe32 = None
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+    uneven = None
+    if rank == 0 and args.uneven_waveforms > 0:
+        uneven = uneven_pulse_fit(args.uneven_waveforms, 1 << 19)
+        torch.cuda.empty_cache()
+
+    serve = None
+    if rank == 0 and args.serve_jobs > 0:
+        serve = serving(geom, cond, args.serve_jobs, args.serve_pool, args.serve_load)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -391,6 +520,8 @@ def main():
                 "roofline_waveform": roofline_of("k_wf_synth"),
                 "roofline_pulse_fit": roofline_of("pulse fit"),
                 "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
+                "uneven_pulse_fit": uneven,
+                "serving": serve,
                 "cpu_baseline": cpu}
         print(json.dumps(line))
     if dist is not None:

@@ -111,6 +111,8 @@ class ChainResult:
     n_members: int
     clusters: dict
     members: dict
+    n_photons: int = 0
+    n_sipms: int = 0
     charges: object = None
     digis: dict = None
     waveforms: dict = None
@@ -133,8 +135,10 @@ class ChainEngine:
         self.rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
         self.fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
         self.ccfg = replace(cfg, waveform=self.wcfg, pulse_reco=self.rcfg, finder=self.fcfg)
+        self.geom, self.cond, self.pmap = geom, cond, pmap
+        self.G = G if G is not None else sector_geom(geom)
         self.tabs = DeviceTables(geom, cond, self.ccfg, device, pmap)
-        self.fin = FinderTables(G if G is not None else sector_geom(geom), self.fcfg, device)
+        self.fin = FinderTables(self.G, self.fcfg, device)
         tm = single_pe_template(self.wcfg)
         self.tmpl = torch.from_numpy(tm).to(device)
         self.tlen = len(tm)
@@ -143,17 +147,44 @@ class ChainEngine:
         self.ws_w, self.ws_h = _Ws(device), _Ws(device)
         self.status = _capi.DeviceStatus(device)
 
+    def configure(self, cfg: ChainConfig):
+        """Switch to another design point: knobs carried in the launch parameters change freely; the finder tables
+        and the single-PE template are rebuilt when their settings change, the channel tables when the response
+        scales or SiPM settings do."""
+        from .coinc import FinderTables
+        torch = _torch()
+        validate_sipm(cfg.sipm)
+        validate_window(cfg.window)
+        wcfg = cfg.waveform if cfg.waveform is not None else WaveformConfig()
+        rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
+        fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
+        ccfg = replace(cfg, waveform=wcfg, pulse_reco=rcfg, finder=fcfg)
+        old = self.ccfg
+        if (cfg.sipm != old.sipm or cfg.response.photon_yield_scale != old.response.photon_yield_scale
+                or cfg.response.photon_yield_variation_scale != old.response.photon_yield_variation_scale):
+            self.tabs = DeviceTables(self.geom, self.cond, ccfg, self.device, self.pmap)
+        if fcfg != self.fcfg:
+            self.fin = FinderTables(self.G, fcfg, self.device)
+        shape = ("single_pe_file", "single_pe_precision", "single_pe_stretch", "single_pe_max_time", "gumbel_peak",
+                 "gumbel_mu", "gumbel_beta")
+        if any(getattr(wcfg, k) != getattr(self.wcfg, k) for k in shape):
+            tm = single_pe_template(wcfg)
+            self.tmpl = torch.from_numpy(tm).to(self.device)
+            self.tlen = len(tm)
+        self.cfg, self.ccfg, self.wcfg, self.rcfg, self.fcfg = cfg, ccfg, wcfg, rcfg, fcfg
+
     def params(self, seed):
         P = make_params(self.ccfg, seed, template_len=self.tlen, uniform_map=self.tabs.uniform_map)
         P.period = self.wcfg.period
         return P
 
-    def run(self, ds: DeviceSteps, seed, keep=False):
+    def run(self, ds: DeviceSteps, seed, keep=False, diagnostics=False):
+        """One pass of the chain over ds.  diagnostics: also count photons and hit SiPMs (n_photons, n_sipms)."""
         torch = _torch()
         L = _capi.load()
         dev = self.device
         P = self.params(seed)
-        R = self.resp.run(P, ds, self.tabs, diagnostics=False)
+        R = self.resp.run(P, ds, self.tabs, diagnostics=diagnostics)
         evk = ((ds.ev_subrun.to(torch.int64) & 0xFFFFFFFF) << 20) | (ds.ev_event.to(torch.int64) & 0xFFFFFFFF)
         D = self.dig.run(P, self.tabs, R.label, R.time, R.charge, self.tmpl, evk, ds.ev_run)
         nd = int(D["chan"].numel())
@@ -200,7 +231,9 @@ class ChainEngine:
         H = {k: (v[:nev] if k.startswith("ev_") else v[:nh]) for k, v in H.items()}
         cl, mem = self.coi.run(P, self.fin, H["ev_start"], H["ev_count"], H["ev_key"], H["bar"], H["sipm"],
                                H["seq"], H["time"], H["pe"], self.tabs.status)
-        res = ChainResult(ds.nevents, R.n, nd, nw, npu, nh, int(cl["pe"].numel()), int(mem["cl"].numel()), cl, mem)
+        res = ChainResult(ds.nevents, R.n, nd, nw, npu, nh, int(cl["pe"].numel()), int(mem["cl"].numel()), cl, mem,
+                          int(R.sipm_photons.sum().item()) if diagnostics and R.nsipm else 0,
+                          R.nsipm if diagnostics else 0)
         if keep:
             res.charges, res.digis, res.waveforms, res.pulses, res.hits = R, D, W, Pu, H
         return res

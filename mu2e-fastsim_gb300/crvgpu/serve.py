@@ -1,0 +1,249 @@
+"""Serving loop: design-point jobs through the device-resident chain with continuous batching.
+
+The reference runs one design-point job per process (a knob set over a step sample).  Here jobs arrive as a
+stream and are served by slots: a slot is a ChainEngine with its own CUDA stream, workspaces and host thread, and the
+number of slots follows from the HBM budget (the footprint of one slot, measured on a chunk).  Jobs are cut into chunks
+of events; free slots take the next chunk of the arrived job with the least work left, so a job that arrives while
+others run joins the mix at the next chunk boundary and its chunks overlap with theirs on the device.  Step tables
+stay resident: a job names a range of events of a device step pool, which it reads through views.
+
+Per-job knobs (the design point): photon yield [PE/MeV], long attenuation length [mm], readout threshold [PE] and
+coincidence window [ns].  Every draw is keyed by (job seed, run, subrun, event, SiPM, draw), so a job's result does not
+depend on what else runs: alone and in a mix it is the same, bit for bit.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from .config import SPE_PEAK_VOLT, WORKLOAD_CUTS, ChainConfig, FinderConfig, ResponseConfig, WaveformConfig
+from .response import DeviceSteps, _torch
+
+
+@dataclass
+class Job:
+    id: int
+    n_events: int
+    first: int = 0                   # first event of the job in the step pool
+    seed: int = 1
+    yield_per_mev: float = 40.0
+    lambda_long: float = 5000.0      # mm
+    threshold_pe: float = 5.0
+    window_ns: float = 10.0
+    arrival: float = 0.0             # seconds after the start of the run
+
+
+@dataclass
+class JobResult:
+    id: int
+    n_events: int
+    clusters: dict                   # host cluster columns (event, type, pe, start, end, slope, avgtime, ...)
+    n_clusters: int
+    arrival: float
+    start: float
+    finish: float
+    slot: int
+
+    @property
+    def latency(self):
+        return self.finish - self.arrival
+
+
+def job_config(job: Job, precision="fp32", sector="EX") -> ChainConfig:
+    """ChainConfig of a design point (the serving knobs of the workload)."""
+    return ChainConfig(response=ResponseConfig(yield_per_mev=job.yield_per_mev, lambda_long=job.lambda_long),
+                       waveform=WaveformConfig(min_voltage=job.threshold_pe * SPE_PEAK_VOLT),
+                       finder=FinderConfig(cuts={sector: replace(WORKLOAD_CUTS, max_dt=job.window_ns)}),
+                       precision=precision)
+
+
+def random_jobs(n, rng, min_events=1000, max_events=1_000_000, pool_events=None, rate=None):
+    """Jobs of the serving workload: events log-uniform in [min_events, max_events], knobs uniform (yield 30-50
+    PE/MeV, long attenuation 350-650 cm, threshold 3-8 PE, coincidence window 5-20 ns), Poisson arrivals at `rate`
+    jobs/s (all at 0 when rate is None)."""
+    ev = np.exp(rng.uniform(np.log(min_events), np.log(max_events), n)).astype(np.int64)
+    gaps = rng.exponential(1.0 / rate, n) if rate else np.zeros(n)
+    arr = np.cumsum(gaps) - (gaps[0] if rate else 0.0)
+    jobs = []
+    for i in range(n):
+        first = int(rng.integers(0, max(1, pool_events - ev[i] + 1))) if pool_events else 0
+        jobs.append(Job(id=i, n_events=int(ev[i]), first=first, seed=int(rng.integers(1, 2 ** 31)),
+                        yield_per_mev=float(rng.uniform(30, 50)), lambda_long=float(rng.uniform(3500, 6500)),
+                        threshold_pe=float(rng.uniform(3, 8)), window_ns=float(rng.uniform(5, 20)),
+                        arrival=float(arr[i])))
+    return jobs
+
+
+def slice_events(ds: DeviceSteps, a: int, b: int) -> DeviceSteps:
+    """Events [a, b) of a device step table as views of its columns (event table rebased to the slice)."""
+    torch = _torch()
+    first = ds.ev_first[a:b]
+    r0 = int(first[0].item()) if b > a else 0
+    cnt = ds.ev_nsteps[a:b]
+    n = int(cnt.sum().item()) if b > a else 0
+    sl = slice(r0, r0 + n)
+    return DeviceSteps(x=ds.x[sl], y=ds.y[sl], z=ds.z[sl], t=ds.t[sl], edep=ds.edep[sl], bar=ds.bar[sl],
+                       ev_event=ds.ev_event[a:b], ev_subrun=ds.ev_subrun[a:b], ev_run=ds.ev_run[a:b],
+                       ev_first=(first - r0).to(torch.int64), ev_nsteps=cnt, nsteps=n, nevents=b - a,
+                       max_steps=int(cnt.max().item()) if b > a else 0)
+
+
+@dataclass
+class _Slot:
+    index: int
+    engine: object
+    stream: object
+    footprint: int = 0
+    job_id: object = None            # design point the engine is configured for
+
+
+class ServeEngine:
+    """Continuous-batching job server over a resident step pool.
+
+    pool: DeviceSteps with the events jobs refer to.  hbm_budget: bytes the slots may hold (the number of slots is
+    min(max_slots, budget // footprint of one slot)).  chunk_events: events per chain call (bounds a slot's
+    footprint and the granularity at which jobs interleave)."""
+
+    def __init__(self, geom, cond, pool: DeviceSteps, hbm_budget: int, max_slots=8, chunk_events=4096,
+                 precision="fp32", device="cuda"):
+        from .chain import ChainEngine
+        from .geometry import sector_geom
+        torch = _torch()
+        self.geom, self.cond, self.pool = geom, cond, pool
+        self.G = sector_geom(geom)
+        self.sector = str(self.G.sector_names[0])
+        self.precision = precision
+        self.device = device
+        self.chunk = int(chunk_events)
+        base = job_config(Job(0, 1), precision, self.sector)
+        # The first slot measures its footprint on a full chunk at the most demanding design point of the knob ranges
+        # (largest yield and attenuation length, lowest threshold, widest window), with a margin for the event-to-event
+        # spread of later chunks.
+        heavy = job_config(Job(0, 1, yield_per_mev=50.0, lambda_long=6500.0, threshold_pe=3.0, window_ns=20.0),
+                           precision, self.sector)
+        torch.cuda.synchronize()
+        torch.cuda.reset_peak_memory_stats()
+        m0 = torch.cuda.memory_allocated()
+        s0 = _Slot(0, ChainEngine(geom, cond, base, G=self.G, device=device), torch.cuda.Stream())
+        with torch.cuda.stream(s0.stream):
+            s0.engine.configure(heavy)
+            s0.engine.run(slice_events(pool, 0, min(self.chunk, pool.nevents)), 1)
+        torch.cuda.synchronize()
+        s0.footprint = int(1.25 * max(1, torch.cuda.max_memory_allocated() - m0))
+        n = int(max(1, min(max_slots, hbm_budget // s0.footprint)))
+        self.slots = [s0] + [_Slot(i, ChainEngine(geom, cond, base, G=self.G, device=device), torch.cuda.Stream(),
+                                   s0.footprint) for i in range(1, n)]
+        self.footprint = s0.footprint
+
+    def _run_chunk(self, slot: _Slot, job: Job, a: int, b: int) -> dict:
+        torch = _torch()
+        eng = slot.engine
+        if slot.job_id != job.id:
+            eng.configure(job_config(job, self.precision, self.sector))
+            slot.job_id = job.id
+        with torch.cuda.stream(slot.stream):
+            r = eng.run(slice_events(self.pool, a, b), job.seed)
+            out = {k: v.clone() for k, v in r.clusters.items()}
+            slot.stream.synchronize()
+        return out
+
+    def run(self, jobs, realtime=True):
+        """Serve `jobs` (arrival times in seconds from now when realtime, else all at once).  Returns JobResults in
+        job order.
+
+        Scheduling: a job is split into chunks of chunk_events events; whenever a slot is free it takes the next
+        chunk of the arrived job with the fewest events left (shortest remaining work first), so small jobs that
+        arrive during large ones are not queued behind them, and an otherwise idle device works on one job's chunks
+        on every slot.  Chunk results are kept per job and joined in event order when its last chunk is done."""
+        torch = _torch()
+        t0 = time.perf_counter()
+        cv = threading.Condition()
+        state = {"pending": sorted(jobs, key=lambda j: j.arrival), "active": [], "done": 0, "stop": False}
+        info = {}
+        results = {}
+        errors = []
+        total = len(jobs)
+
+        def admit_arrived(now):
+            # caller holds cv
+            while state["pending"] and (not realtime or state["pending"][0].arrival <= now):
+                job = state["pending"].pop(0)
+                bounds = [(a, min(a + self.chunk, job.first + job.n_events))
+                          for a in range(job.first, job.first + job.n_events, self.chunk)]
+                info[job.id] = {"job": job, "next": 0, "bounds": bounds, "parts": [None] * len(bounds),
+                                "left": job.n_events, "ndone": 0, "start": None}
+                state["active"].append(job.id)
+
+        def finish(jid):
+            rec = info[jid]
+            parts = [p for p in rec["parts"] if p is not None]
+            cl = {k: torch.cat([p[k] for p in parts]).cpu().numpy() for k in parts[0]} if parts else {}
+            job = rec["job"]
+            fin = time.perf_counter() - t0
+            results[jid] = JobResult(jid, job.n_events, cl, len(cl.get("pe", ())),
+                                     job.arrival if realtime else 0.0, rec["start"], fin, rec.get("slot", -1))
+
+        def worker(slot):
+            while True:
+                with cv:
+                    while True:
+                        if errors or state["done"] == total:
+                            return
+                        admit_arrived(time.perf_counter() - t0)
+                        cand = [jid for jid in state["active"] if info[jid]["next"] < len(info[jid]["bounds"])]
+                        if cand:
+                            jid = min(cand, key=lambda j: (info[j]["left"], info[j]["job"].arrival, j))
+                            rec = info[jid]
+                            k = rec["next"]
+                            rec["next"] += 1
+                            a, b = rec["bounds"][k]
+                            rec["left"] -= b - a
+                            if rec["start"] is None:
+                                rec["start"] = time.perf_counter() - t0
+                                rec["slot"] = slot.index
+                            break
+                        wait = None
+                        if realtime and state["pending"]:
+                            wait = max(0.0, state["pending"][0].arrival - (time.perf_counter() - t0))
+                        cv.wait(timeout=wait if wait is not None else 0.05)
+                try:
+                    out = self._run_chunk(slot, rec["job"], a, b)
+                except Exception as exc:                    # reported to the caller after the run
+                    with cv:
+                        errors.append(exc)
+                        cv.notify_all()
+                    return
+                with cv:
+                    rec["parts"][k] = out
+                    rec["ndone"] += 1
+                    if rec["ndone"] == len(rec["bounds"]):
+                        state["active"].remove(jid)
+                        finish(jid)
+                        state["done"] += 1
+                    cv.notify_all()
+
+        for s_ in self.slots:
+            s_.job_id = None
+        threads = [threading.Thread(target=worker, args=(s_,), daemon=True) for s_ in self.slots]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
+        return [results[j.id] for j in jobs]
+
+
+def latency_stats(results, iso_rate, iso_overhead=0.0):
+    """p50 / p99 job latency [s] and p99 of latency / isolated run time (isolated time modelled as
+    iso_overhead + events / iso_rate)."""
+    lat = np.array([r.latency for r in results])
+    iso = np.array([iso_overhead + r.n_events / iso_rate for r in results])
+    span = max(r.finish for r in results) - min(r.arrival for r in results) if results else 0.0
+    ev = sum(r.n_events for r in results)
+    return {"jobs": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "p99_over_isolated": float(np.percentile(lat / iso, 99)),
+            "events_per_s": float(ev / span) if span > 0 else None}

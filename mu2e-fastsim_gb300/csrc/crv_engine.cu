@@ -356,7 +356,8 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
   while (stepcap < max_steps_per_event) stepcap <<= 1;
   if (stepcap > 65536) stepcap = 65536;
   size_t psmem = size_t(stepcap) * 4;
-  CK(cudaFuncSetAttribute(k_event_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+  if (psmem > device_info().smem_optin) return CRV_ERR_ARG;
+  CK(allow_dynamic_smem(k_event_prep));
   unsigned gp = grid_for(nevents, 1, 8);
   {
     crv::Mark mark_("k_event_prep", s);
@@ -957,7 +958,7 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
     size_t per = coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap);
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
-    CK(cudaFuncSetAttribute(k_coinc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(allow_dynamic_smem(k_coinc));
     long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
     long long maxb = (long long)di.sms * (k == 0 ? 8 : 2);
     {

@@ -20,6 +20,18 @@ struct DeviceInfo {
 };
 const DeviceInfo& device_info();
 
+// Allow a kernel the device's whole opt-in shared memory as dynamic shared memory (less its static part).  The
+// limit is a per-kernel setting shared by every thread of the process; setting it to the same value in every call
+// keeps concurrent callers (serving slots on other host threads) from lowering it under each other's launches.
+template <typename K>
+inline cudaError_t allow_dynamic_smem(K kern) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kern);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(device_info().smem_optin - a.sharedSizeBytes));
+}
+
 // Launch accounting: every kernel launch of the library is wrapped in a Mark, which counts it and, while profiling
 // is enabled (crv_profile), records CUDA events around it on its stream.
 struct Mark {
