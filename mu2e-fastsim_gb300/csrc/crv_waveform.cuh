@@ -233,6 +233,18 @@ __device__ __forceinline__ int16_t adc_of(const CrvParams& p, double v) {
   return int16_t(r);
 }
 
+// ADC of an FP32 sample: v * conversion + pedestal + 0.5 is exact in FP64 for an FP32 v (a 24-bit by 12-bit
+// product plus a small offset), so one FP32 FMA (one rounding) truncates to the same integer unless it lands on an
+// integer itself; only then, or out of range, is the FP64 form evaluated.
+__device__ __forceinline__ int16_t adc_of_f(const CrvParams& p, float v, float conv, float off) {
+  const float x = fmaf(v, conv, off);
+  if (!(fabsf(x) < 1e9f) || x == truncf(x)) return adc_of(p, f2d(v));
+  int r = int16_t(uint16_t(uint32_t(int32_t(truncf(x))) & 0xFFFFu));
+  if (r < p.min_adc) r = p.min_adc;
+  if (r > p.max_adc) r = p.max_adc;
+  return int16_t(r);
+}
+
 // Synthesis + zero suppression of the groups whose longest kept cluster is in (lo, cap].
 template <typename R>
 __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
@@ -257,6 +269,8 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
   const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
   const R inv_q = R(1.0 / p.spe_ref_charge);
   const R vthr = R(p.min_voltage);
+  const R sigma = R(p.noise_sigma);
+  const float conv_f = float(p.adc_conversion), off_f = float(double(p.adc_pedestal) + 0.5);
   const double gap = p.spe_max_time + 4.0 * p.period;
   long long ng = *G.n;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -308,26 +322,42 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
             float dt = float(t[q] - ts);
             dt_s[q - a] = dt;
             j0_s[q - a] = first_sample_f(dt, Pf);
-            qn_s[q - a] = R(qc[q]) * inv_q;
+            qn_s[q - a] = R(d2f_trunc(qc[q])) * inv_q;        // FP32-stage charges: exact FP32 values
           }
         }
         __syncwarp();
       }
       // samples: sum of the charges reaching each sample, in charge order
       for (int j = lane_id(); j < L; j += 32) {
-        // charges with first_sample in (j - nr, j]: first_sample is non-decreasing along the cluster
-        int lo_q = a, hi_q = b;                      // first charge with first_sample > j - nr
-        while (lo_q < hi_q) {
-          int m = (lo_q + hi_q) >> 1;
-          long long fm = staged ? (long long)j0_s[m - a] : first_sample<R>(p, t[m], ts);
-          if (fm > (long long)j - nr) hi_q = m; else lo_q = m + 1;
-        }
-        int q1 = lo_q;
-        int lo2 = q1, hi2 = b;                       // first charge with first_sample > j
-        while (lo2 < hi2) {
-          int m = (lo2 + hi2) >> 1;
-          long long fm = staged ? (long long)j0_s[m - a] : first_sample<R>(p, t[m], ts);
-          if (fm > (long long)j) hi2 = m; else lo2 = m + 1;
+        // charges with first_sample in (j - nr, j]: first_sample is non-decreasing along the cluster.  The staged
+        // and the on-the-fly searches are separate loops, so the staged one carries no FP64 work.
+        int q1, lo2;
+        if (staged) {
+          int lo_q = a, hi_q = b;                    // first charge with first_sample > j - nr
+          while (lo_q < hi_q) {
+            int m = (lo_q + hi_q) >> 1;
+            if (j0_s[m - a] > j - nr) hi_q = m; else lo_q = m + 1;
+          }
+          q1 = lo_q;
+          int hi2 = b;                               // first charge with first_sample > j
+          lo2 = q1;
+          while (lo2 < hi2) {
+            int m = (lo2 + hi2) >> 1;
+            if (j0_s[m - a] > j) hi2 = m; else lo2 = m + 1;
+          }
+        } else {
+          int lo_q = a, hi_q = b;
+          while (lo_q < hi_q) {
+            int m = (lo_q + hi_q) >> 1;
+            if (first_sample<R>(p, t[m], ts) > (long long)j - nr) hi_q = m; else lo_q = m + 1;
+          }
+          q1 = lo_q;
+          int hi2 = b;
+          lo2 = q1;
+          while (lo2 < hi2) {
+            int m = (lo2 + hi2) >> 1;
+            if (first_sample<R>(p, t[m], ts) > (long long)j) hi2 = m; else lo2 = m + 1;
+          }
         }
         R acc = R(0);
         if (sizeof(R) == 4 && staged) {
@@ -346,7 +376,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
           U4 w = keyed(p.seed, ek, (ST_NOISE << 28) | (chan & 0x7FFFu), uint32_t(tk >> 1));
           R z0, z1;
           Math<R>::normal_pair(w, &z0, &z1);
-          acc = acc + R(p.noise_sigma) * ((tk & 1) ? z1 : z0);
+          acc = acc + sigma * ((tk & 1) ? z1 : z0);
         }
         wave[j] = acc;
       }
@@ -376,9 +406,15 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
             long long o = slot + nd;
             if (lane_id() < zs) {
               int c = i0 + lane_id();
-              double v = c < L ? double(wave[c]) : 0.0;
-              D.volt[o * zs + lane_id()] = v;
-              D.adc[o * zs + lane_id()] = adc_of(p, v);
+              if constexpr (sizeof(R) == 4) {
+                const float v = c < L ? float(wave[c]) : 0.0f;
+                D.volt[o * zs + lane_id()] = f2d(v);
+                D.adc[o * zs + lane_id()] = adc_of_f(p, v, conv_f, off_f);
+              } else {
+                double v = c < L ? double(wave[c]) : 0.0;
+                D.volt[o * zs + lane_id()] = v;
+                D.adc[o * zs + lane_id()] = adc_of(p, v);
+              }
             }
             if (lane_id() == 0) {
               D.chan[o] = lab;
