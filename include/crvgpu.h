@@ -295,7 +295,8 @@ int crv_pulses_static(const CrvParams *p, int64_t nw, int64_t nsamples, const in
 /*
  * coinc.find_event over every event (chain.clusters' loop): pulses sorted by (event, waveform, sequence); event e owns
  * pulse rows [ev_start[e], ev_start[e] + ev_count[e]) and reports ev_key[e].  Per pulse: bar, SiPM, sequence, time,
- * PE; status: per-channel status (compensated-partner bits).
+ * PE; status: per-channel status (compensated-partner bits).  Limits of the geometry tables: fewer than 65536 bars and
+ * counters per sector type, at most 255 cut sets and 255 sector types.
  */
 int64_t crv_coincidences_workspace(int64_t nevents, int64_t npulses);
 int crv_coincidences(const CrvParams *p, const CrvFinderGeom *g, int64_t nevents, const int64_t *ev_start,

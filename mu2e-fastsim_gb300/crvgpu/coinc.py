@@ -48,6 +48,9 @@ class FinderTables:
             if cfg.cuts[n].final_max_distance < 0 or cfg.cuts[n].initial_max_distance < 0:
                 raise ValueError("coincidence max distances must be non-negative")
         cut_index = {n: i for i, n in enumerate(cut_names)}
+        # the device keeps bar and counter indices in 16 bits, cut-set and type indices in 8 bits
+        if len(G.sector) > 65535 or int(np.max(G.counter_in_type, initial=0)) > 65535 or len(cut_names) > 255:
+            raise ValueError("coincidence finder: more than 65535 bars or counters per type, or 255 cut sets")
         cuts = np.array([[float(getattr(cfg.cuts[n], f)) for f in CUT_FIELDS] for n in cut_names], float)
         lim = type_limits(G, cfg)
         types = sorted(lim)
@@ -67,6 +70,8 @@ class FinderTables:
         self.type_side0 = i32([lim[t]["side0"] for t in types] or [0])
         self.type_side1 = i32([lim[t]["side1"] for t in types] or [0])
         self.ntypes = len(types)
+        if self.ntypes > 255:
+            raise ValueError("coincidence finder: more than 255 sector types")
 
     def c_geom(self):
         keys = ("bar_sector", "bar_layer", "bar_counter", "bar_x", "bar_y", "bar_pos", "sec_type", "sec_cut",

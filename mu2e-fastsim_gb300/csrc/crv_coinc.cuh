@@ -54,31 +54,36 @@ struct CoincOut {
 
 enum { CUT_PE = 0, CUT_DTADJ, CUT_DT, CUT_SMIN, CUT_SMAX, CUT_SDIFF, CUT_LAYERS, CUT_MINPE, CUT_D0, CUT_D1 };
 
+// Per-warp shared memory, per hit of the event (narrow types; y, sector and the initial maxd are read from the bar and
+// cut tables when needed).
 struct CoincShared {
   // hits of the event (all types)
-  int32_t *idx, *bar, *layer, *counter, *side, *sipm, *seq, *sector, *cut, *type;
-  double *x, *y, *t, *pe, *maxd;
-  // work lists (indices into hits or into the coincidence list)
-  int32_t *list, *pool, *clus, *filt, *coinc, *cl_of, *order, *tmp;
-  double *cmaxd;                                   // maxd of the coincidence copies
+  double *x, *t, *pe;
   unsigned long long* wid;                         // widened maxd (non-negative doubles as ordered integers)
-  uint8_t* kept;
+  int32_t* idx;                                    // pulse row within the event
+  uint16_t *bar, *counter;
+  uint8_t *cut, *layer, *side, *sipm, *seq0, *type, *kept;   // seq0: first pulse of its waveform
+  // work lists (indices into hits or into the coincidence list)
+  int32_t *list, *clus, *filt, *coinc, *cl_of, *order, *tmp;
 };
 
 __host__ __device__ inline size_t coinc_smem_per_warp(int hcap) {
-  return (size_t(hcap) * (10 * 4 + 5 * 8 + 8 * 4 + 8 + 8 + 1) + 64 + 15) & ~size_t(15);
+  return (size_t(hcap) * (4 * 8 + 8 * 4 + 2 * 2 + 7) + 64 + 15) & ~size_t(15);
 }
 
 __device__ inline CoincShared coinc_carve(char* b, int hcap) {
   CoincShared S;
   double* d = reinterpret_cast<double*>(b);
-  S.x = d; S.y = d + hcap; S.t = d + 2 * hcap; S.pe = d + 3 * hcap; S.maxd = d + 4 * hcap; S.cmaxd = d + 5 * hcap;
-  S.wid = reinterpret_cast<unsigned long long*>(d + 6 * hcap);
-  int32_t* q = reinterpret_cast<int32_t*>(d + 7 * hcap);
-  int32_t** f[] = {&S.idx, &S.bar, &S.layer, &S.counter, &S.side, &S.sipm, &S.seq, &S.sector, &S.cut, &S.type,
-                   &S.list, &S.pool, &S.clus, &S.filt, &S.coinc, &S.cl_of, &S.order, &S.tmp};
-  for (int k = 0; k < 18; ++k) *f[k] = q + k * hcap;
-  S.kept = reinterpret_cast<uint8_t*>(q + 18 * hcap);
+  S.x = d; S.t = d + hcap; S.pe = d + 2 * hcap;
+  S.wid = reinterpret_cast<unsigned long long*>(d + 3 * hcap);
+  int32_t* q = reinterpret_cast<int32_t*>(d + 4 * hcap);
+  int32_t** f[] = {&S.idx, &S.list, &S.clus, &S.filt, &S.coinc, &S.cl_of, &S.order, &S.tmp};
+  for (int k = 0; k < 8; ++k) *f[k] = q + k * hcap;
+  uint16_t* h = reinterpret_cast<uint16_t*>(q + 8 * hcap);
+  S.bar = h; S.counter = h + hcap;
+  uint8_t* c = reinterpret_cast<uint8_t*>(h + 2 * hcap);
+  uint8_t** g[] = {&S.cut, &S.layer, &S.side, &S.sipm, &S.seq0, &S.type, &S.kept};
+  for (int k = 0; k < 7; ++k) *g[k] = c + k * hcap;
   return S;
 }
 
@@ -230,7 +235,7 @@ __device__ void check_coincidence(const CoincGeom& G, const CoincShared& S, cons
         double sl[3];
         bool ok = true;
         for (int q = 0; q + 1 < nl; ++q) {
-          double s = (S.x[hs[q + 1]] - S.x[hs[q]]) / (S.y[hs[q + 1]] - S.y[hs[q]]);
+          double s = (S.x[hs[q + 1]] - S.x[hs[q]]) / (G.bar_y[S.bar[hs[q + 1]]] - G.bar_y[S.bar[hs[q]]]);
           if (s < lo || s > hi) { ok = false; break; }
           sl[q] = s;
         }
@@ -262,22 +267,24 @@ __device__ void check_coincidence(const CoincGeom& G, const CoincShared& S, cons
 }
 
 // scratch of the per-type lists beyond CoincShared (carved after it)
+// scratch of the per-type lists beyond CoincShared; the attachment lists reuse lists that are dead by then (the
+// type's hit list, the combination buckets, the first clustering's starts, cluster ids and maxd)
 struct CoincWork {
   int32_t *clstart, *ccl, *cstart, *att_c, *att_cl, *att_bar, *att_sipm;
   double *cmd, *att_dt, *fmd;
 };
 
 __host__ __device__ inline size_t coinc_work_per_warp(int hcap) {
-  return (size_t(hcap + 1) * 4 * 3 + size_t(hcap) * 4 * 4 + size_t(hcap) * 8 * 3 + 64 + 15) & ~size_t(15);
+  return (size_t(hcap + 1) * 4 * 3 + size_t(hcap) * 8 * 2 + 64 + 15) & ~size_t(15);
 }
 
-__device__ inline CoincWork work_carve(char* b, int hcap) {
+__device__ inline CoincWork work_carve(char* b, int hcap, const CoincShared& S) {
   CoincWork W;
   double* d = reinterpret_cast<double*>(b);
-  W.cmd = d; W.att_dt = d + hcap; W.fmd = d + 2 * hcap;
-  int32_t* q = reinterpret_cast<int32_t*>(d + 3 * hcap);
+  W.cmd = d; W.fmd = d + hcap;
+  int32_t* q = reinterpret_cast<int32_t*>(d + 2 * hcap);
   W.clstart = q; W.ccl = q + (hcap + 1); W.cstart = q + 2 * (hcap + 1);
-  W.att_c = q + 3 * (hcap + 1); W.att_cl = W.att_c + hcap; W.att_bar = W.att_cl + hcap; W.att_sipm = W.att_bar + hcap;
+  W.att_c = S.list; W.att_cl = S.tmp; W.att_bar = W.clstart; W.att_sipm = S.cl_of; W.att_dt = W.fmd;
   return W;
 }
 
@@ -298,7 +305,7 @@ __device__ bool cluster_props(const CoincGeom& G, const CoincShared& S, const Cr
   }
   for (int k = 0; k < m; ++k) {
     int h = mem[k];
-    double pe = S.pe[h], x = S.x[h], y = S.y[h];
+    double pe = S.pe[h], x = S.x[h], y = G.bar_y[S.bar[h]];
     sxy += pe * x * y; sx += pe * x; sy += pe * y; syy += pe * y * y;
   }
   double slope = (tot * sxy - sx * sy) / (tot * syy - sy * sy);
@@ -321,7 +328,7 @@ __device__ bool cluster_props(const CoincGeom& G, const CoincShared& S, const Cr
     st[sd] = spe[sd] > 0.0 ? stp[sd] / spe[sd] : 0.0;
     if (!nh[sd]) { tmin[sd] = 0.0; tmax[sd] = 0.0; }
   }
-  int ld = G.sec_length_dir[S.sector[mem[0]]];
+  int ld = G.sec_length_dir[G.bar_sector[S.bar[mem[0]]]];
   double v = p.fiber_signal_speed, P0 = G.type_p0[ti], P1 = G.type_p1[ti];
   bool calc = false;
   double avg;
@@ -356,7 +363,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
   size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
   char* wb = smem + size_t(warp_in_block()) * per;
   CoincShared S = coinc_carve(wb, hcap);
-  CoincWork W = work_carve(wb + coinc_smem_per_warp(hcap), hcap);
+  CoincWork W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); e < I.nev; e += warps) {
     if (second_pass && !deferred[e]) continue;
@@ -391,10 +398,10 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
         double pe = I.pe[r];
         int partner = bar * 4 + sipm + (sipm < 2 ? 2 : -2);
         if (I.status[partner] & p.compensate_mask) pe *= 2.0;
-        S.idx[pos] = i; S.bar[pos] = bar; S.layer[pos] = G.bar_layer[bar]; S.counter[pos] = G.bar_counter[bar];
-        S.side[pos] = side; S.sipm[pos] = sipm; S.seq[pos] = I.seq[r]; S.sector[pos] = sec; S.cut[pos] = cut;
-        S.type[pos] = ti; S.x[pos] = G.bar_x[bar]; S.y[pos] = G.bar_y[bar]; S.t[pos] = t; S.pe[pos] = pe;
-        S.maxd[pos] = cutv(G, cut, CUT_D0);
+        S.idx[pos] = i; S.bar[pos] = uint16_t(bar); S.layer[pos] = uint8_t(G.bar_layer[bar]);
+        S.counter[pos] = uint16_t(G.bar_counter[bar]); S.side[pos] = uint8_t(side); S.sipm[pos] = uint8_t(sipm);
+        S.seq0[pos] = I.seq[r] == 0; S.cut[pos] = uint8_t(cut); S.type[pos] = uint8_t(ti);
+        S.x[pos] = G.bar_x[bar]; S.t[pos] = t; S.pe[pos] = pe;
       }
       H += __popc(m);
     }
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
               for (int q = 0; q < nt; ++q) {
                 int a = S.list[q];
                 if (S.side[a] != side || S.layer[a] != S.layer[h] || fabs(S.t[a] - S.t[h]) > dadj) continue;
-                int d = S.counter[a] - S.counter[h];
+                int d = int(S.counter[a]) - int(S.counter[h]);
                 same += d == 0 ? S.pe[a] : 0.0;
                 a1 += d == -1 ? S.pe[a] : 0.0;
                 a2 += d == 1 ? S.pe[a] : 0.0;
@@ -455,7 +462,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
         __syncwarp();
         int nfs = nf - f0;
         if (nfs == 0) continue;
-        for (int k = lane_id(); k < nfs; k += 32) W.fmd[k] = S.maxd[S.filt[f0 + k]];
+        for (int k = lane_id(); k < nfs; k += 32) W.fmd[k] = cutv(G, S.cut[S.filt[f0 + k]], CUT_D0);
         __syncwarp();
         int ncl1 = greedy(S, S.filt + f0, W.fmd, nfs, G.type_maxdt[ti], false, 0.0, S.cl_of, S.clus, W.clstart);
         for (int c = 0; c < ncl1; ++c) {
@@ -503,10 +510,10 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
             h = S.filt[k];
             bool member = false;
             for (int q = 0; q < nc && !member; ++q) member = S.coinc[q] == h;
-            if (S.seq[h] == 0 && !member) {
+            if (S.seq0[h] && !member) {
               for (int q = 0; q < nc; ++q) {
                 int a = S.coinc[q];
-                if (S.seq[a] != 0 || S.bar[a] != S.bar[h] || S.side[h] != 1 - S.side[a]) continue;
+                if (!S.seq0[a] || S.bar[a] != S.bar[h] || S.side[h] != 1 - S.side[a]) continue;
                 double dt = fabs(S.t[h] - S.t[a]);
                 if (!(dt < mdt)) continue;
                 int cl = W.ccl[q];

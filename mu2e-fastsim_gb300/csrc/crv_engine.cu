@@ -953,14 +953,15 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
   CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
   const DeviceInfo& di = device_info();
-  struct Pass { int hcap, warps; } passes[2] = {{256, 4}, {1024, 1}};
+  // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM), larger ones in a second pass
+  struct Pass { int hcap, warps; } passes[2] = {{192, 1}, {1024, 1}};
   for (int k = 0; k < 2; ++k) {
     size_t per = coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap);
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
     CK(allow_dynamic_smem(k_coinc));
     long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
-    long long maxb = (long long)di.sms * (k == 0 ? 8 : 2);
+    long long maxb = (long long)di.sms * (k == 0 ? 16 : 2);
     {
       crv::Mark mark_("k_coinc", s);
       k_coinc<<<(unsigned)(blocks < maxb ? blocks : maxb), passes[k].warps * 32, smem, s>>>(*p, G, I, passes[k].hcap, k,
