@@ -15,7 +15,7 @@ import numpy as np
 from . import _capi
 from .coinc import CoincEngine, FinderTables, rows_of  # noqa: F401
 from .config import (CHAN_MULT, PERIOD, ChainConfig, Conditions, FinderConfig, RecoConfig, WaveformConfig,  # noqa: F401
-                     from_reference)
+                     from_reference, workload_finder)
 from .params import make_params, validate_sipm, validate_window
 from .pulsefit import PulseEngine, filter_channels, concat_waveforms
 from .pulsefit import reconstruct_full as _reconstruct_full
@@ -52,7 +52,7 @@ def clusters(W, cond, geom, counters_cfg, cfg: ChainConfig, timers=None, detail=
     if "toff" not in W:
         W = {**W, "toff": cond.timeoffset[W["bar"] * 4 + W["sipm"]]}
     G = counters_cfg if counters_cfg is not None and hasattr(counters_cfg, "sector_type") else sector_geom(geom)
-    fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
+    fcfg = cfg.finder if cfg.finder is not None else workload_finder(G.sector_names)
     rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
     t0 = _time.perf_counter()
     P = _reconstruct_full(W["adc"], W["n"], W["start"], W["ped"], W["area"], W["height"], rcfg,
@@ -131,12 +131,12 @@ class ChainEngine:
         validate_window(cfg.window)
         self.cfg = cfg
         self.device = device
-        self.wcfg = cfg.waveform if cfg.waveform is not None else WaveformConfig()
-        self.rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
-        self.fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
-        self.ccfg = replace(cfg, waveform=self.wcfg, pulse_reco=self.rcfg, finder=self.fcfg)
         self.geom, self.cond, self.pmap = geom, cond, pmap
         self.G = G if G is not None else sector_geom(geom)
+        self.wcfg = cfg.waveform if cfg.waveform is not None else WaveformConfig()
+        self.rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
+        self.fcfg = cfg.finder if cfg.finder is not None else workload_finder(self.G.sector_names)
+        self.ccfg = replace(cfg, waveform=self.wcfg, pulse_reco=self.rcfg, finder=self.fcfg)
         self.tabs = DeviceTables(geom, cond, self.ccfg, device, pmap)
         self.fin = FinderTables(self.G, self.fcfg, device)
         tm = single_pe_template(self.wcfg)
@@ -157,7 +157,7 @@ class ChainEngine:
         validate_window(cfg.window)
         wcfg = cfg.waveform if cfg.waveform is not None else WaveformConfig()
         rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
-        fcfg = cfg.finder if cfg.finder is not None else FinderConfig()
+        fcfg = cfg.finder if cfg.finder is not None else workload_finder(self.G.sector_names)
         ccfg = replace(cfg, waveform=wcfg, pulse_reco=rcfg, finder=fcfg)
         old = self.ccfg
         if (cfg.sipm != old.sipm or cfg.response.photon_yield_scale != old.response.photon_yield_scale

@@ -20,7 +20,7 @@ reference's stock values otherwise.
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 from typing import Optional
 
 import numpy as np
@@ -216,3 +216,9 @@ def from_reference(cfg, precision="fp64"):
         if hasattr(cfg, k):
             kw[k] = getattr(cfg, k)
     return ChainConfig(**kw)
+
+
+def workload_finder(sector_names, base: FinderConfig = None) -> FinderConfig:
+    """FinderConfig with the workload's coincidence cuts (3 of 4 layers within 10 ns) for every sector name."""
+    base = base or FinderConfig()
+    return replace(base, cuts={str(n): WORKLOAD_CUTS for n in sector_names})

@@ -355,20 +355,36 @@ __device__ bool cluster_props(const CoincGeom& G, const CoincShared& S, const Cr
 
 constexpr int CO_WARPS_MAX = 8;
 
-// second_pass == 0: events with at most hcap hits (others deferred); second_pass == 1: deferred events only.
+// Per-event scratch of the global-memory pass: event e's lists start at byte (ev_start[e] + 16 e) * COINC_GBYTES, room
+// for the per-warp layout of its pulse count rounded up to 16 (coinc_smem_per_warp + coinc_work_per_warp), so the
+// regions of different events are disjoint.
+constexpr size_t COINC_GBYTES = 112;
+
+// pass 0: events with at most hcap hits (others deferred); pass 1: deferred events with at most hcap hits (others stay
+// deferred); pass 2: the remaining deferred events, lists in global memory (gscratch) sized by the event.
 __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincGeom G, CoincIn I, int hcap,
-                                                           int second_pass, CoincOut O, int32_t* __restrict__ deferred,
-                                                           Status* status) {
+                                                           int pass, CoincOut O, int32_t* __restrict__ deferred,
+                                                           char* __restrict__ gscratch, Status* status) {
   extern __shared__ __align__(16) char smem[];
-  size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
-  char* wb = smem + size_t(warp_in_block()) * per;
-  CoincShared S = coinc_carve(wb, hcap);
-  CoincWork W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
+  CoincShared S;
+  CoincWork W;
+  if (pass < 2) {
+    size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
+    char* wb = smem + size_t(warp_in_block()) * per;
+    S = coinc_carve(wb, hcap);
+    W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
+  }
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); e < I.nev; e += warps) {
-    if (second_pass && !deferred[e]) continue;
+    if (pass > 0 && !deferred[e]) continue;
     long long r0 = I.ev_start[e];
     int np_ = I.ev_count[e];
+    if (pass == 2) {
+      hcap = (np_ + 15) & ~15;
+      char* wb = gscratch + size_t(r0 + 16 * e) * COINC_GBYTES;
+      S = coinc_carve(wb, hcap);
+      W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
+    }
     // hits in pulse order
     int H = 0;
     for (int base = 0; base < np_; base += 32) {
@@ -407,7 +423,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
     }
     if (H > hcap) {
       if (lane_id() == 0) {
-        if (second_pass) {
+        if (pass == 2) {                             // cannot happen: the global lists hold every pulse of the event
           set_flag(status, CRV_ST_CAPACITY);
           need_at_least(status, CRV_NEED_HITS_PER_EVENT, H);
           O.ncl[e] = 0; O.nmem[e] = 0;
@@ -591,7 +607,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
     if (lane_id() == 0) {
       O.ncl[e] = ncl_ev;
       O.nmem[e] = nmem_ev;
-      if (second_pass) deferred[e] = 0;
+      if (pass > 0) deferred[e] = 0;
       if (ncl_ev > np_ || nmem_ev > np_) set_flag(status, CRV_ST_LIMIT);
     }
     __syncwarp();

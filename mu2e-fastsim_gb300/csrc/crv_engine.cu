@@ -862,6 +862,7 @@ struct CoincWs {
   ClusterRec* rec;
   int32_t *mem_idx, *ncl, *nmem, *deferred;
   long long *cl_off, *mem_off, *parts, *totals;
+  char* gscratch;                // per-event lists of the global-memory pass
 };
 
 static CoincWs coinc_layout(char* base, long long nev, long long np, size_t* bytes) {
@@ -876,6 +877,9 @@ static CoincWs coinc_layout(char* base, long long nev, long long np, size_t* byt
   w.mem_off = c.take<long long>(nev);
   w.parts = c.take<long long>(scan_parts_len(nev) + 1);
   w.totals = c.take<long long>(8);
+  // event e's region of the global pass: (ev_count + 16) * COINC_GBYTES bytes, at least the per-warp layout of
+  // hcap = ev_count rounded up to 16 (103 B per hit plus under 250 B of alignment and counters)
+  w.gscratch = c.take<char>((np + 16 * nev + 1) * (long long)COINC_GBYTES);
   *bytes = c.off + 256;
   return w;
 }
@@ -953,19 +957,20 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
   CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
   const DeviceInfo& di = device_info();
-  // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM), larger ones in a second pass
-  struct Pass { int hcap, warps; } passes[2] = {{192, 1}, {1024, 1}};
-  for (int k = 0; k < 2; ++k) {
-    size_t per = coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap);
+  // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM), up to 1024 hits in a second
+  // pass; larger events (full-scale detector) in a third pass with their lists in global memory
+  struct Pass { int hcap, warps; } passes[3] = {{192, 1}, {1024, 1}, {0, 1}};
+  for (int k = 0; k < 3; ++k) {
+    size_t per = k < 2 ? coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap) : 0;
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
     CK(allow_dynamic_smem(k_coinc));
     long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
-    long long maxb = (long long)di.sms * (k == 0 ? 16 : 2);
+    long long maxb = (long long)di.sms * (k == 0 ? 16 : (k == 1 ? 2 : 8));
     {
       crv::Mark mark_("k_coinc", s);
-      k_coinc<<<(unsigned)(blocks < maxb ? blocks : maxb), passes[k].warps * 32, smem, s>>>(*p, G, I, passes[k].hcap, k,
-                                                                                            O, w.deferred, S);
+      k_coinc<<<(unsigned)(blocks < maxb ? blocks : maxb), passes[k].warps * 32, smem, s>>>(
+          *p, G, I, passes[k].hcap, k, O, w.deferred, w.gscratch, S);
     }
     CK(cudaGetLastError());
   }
