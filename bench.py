@@ -263,6 +263,42 @@ def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=20
             "offered_load": load, **{k: v for k, v in st.items() if k != "jobs"}}
 
 
+def fullscale(n_events, batch, seed=13):
+    """Full-scale detector (86 modules of 4 x 16 counters, bar lengths over {230, 300, 450, 560, 660} cm, Poisson(60)
+    steps plus 0.5 noise steps per counter per event): events/s of the chain on a resident subset, FP32-mixed and
+    FP64 plain, device time over the batches."""
+    import torch
+    from crvgpu import chain as CH, config as CF, geometry as GM
+    from crvgpu.response import upload_steps
+    geom = GM.module_geometry(86)
+    cond = GM.default_conditions(geom)
+    batches, nsteps = [], 0
+    for b0 in range(0, n_events, batch):
+        st = GM.synthetic_steps(min(batch, n_events - b0), geom, seed=seed, mean_steps=60.0, noise_per_counter=0.5,
+                                first_event=b0)
+        nsteps += len(st)
+        batches.append(upload_steps(st, nbars=geom.nbars))
+    out = {"events": n_events, "batch": batch, "steps": nsteps, "counters": geom.nbars}
+    for prec in ("fp32", "fp64"):
+        eng = CH.ChainEngine(geom, cond, CF.ChainConfig(precision=prec))
+        eng.run(batches[0], 3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ncl = 0
+        e0.record()
+        for ds in batches:
+            ncl += eng.run(ds, 3).n_clusters
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {"events_per_s": n_events / (ms / 1000.0), "ms": ms, "clusters": ncl}
+        eng = None
+        torch.cuda.empty_cache()
+    out["fp32_over_fp64"] = out["fp32"]["events_per_s"] / out["fp64"]["events_per_s"]
+    out["projected_s_16777216_events_fp32"] = 16777216 / out["fp32"]["events_per_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -276,6 +312,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--fullscale-events", type=int, default=2048, help="events of the full-scale measurement (0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
     ap.add_argument("--serve-load", type=float, default=0.8)
     ap.add_argument("--uneven-waveforms", type=int, default=1 << 22,
@@ -501,6 +538,11 @@ def main():
         uneven = uneven_pulse_fit(args.uneven_waveforms, 1 << 19)
         torch.cuda.empty_cache()
 
+    full = None
+    if rank == 0 and args.fullscale_events > 0:
+        full = fullscale(args.fullscale_events, 1024)
+        torch.cuda.empty_cache()
+
     serve = None
     if rank == 0 and args.serve_jobs > 0:
         serve = serving(geom, cond, args.serve_jobs, args.serve_pool, args.serve_load)
@@ -529,6 +571,7 @@ def main():
                 "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
                 "uneven_pulse_fit": uneven,
                 "serving": serve,
+                "fullscale": full,
                 "cpu_baseline": cpu}
         print(json.dumps(line))
     if dist is not None:

@@ -358,7 +358,26 @@ constexpr int CO_WARPS_MAX = 8;
 // Per-event scratch of the global-memory pass: event e's lists start at byte (ev_start[e] + 16 e) * COINC_GBYTES, room
 // for the per-warp layout of its pulse count rounded up to 16 (coinc_smem_per_warp + coinc_work_per_warp), so the
 // regions of different events are disjoint.
-constexpr size_t COINC_GBYTES = 112;
+constexpr size_t COINC_GBYTES = 128;
+
+// warp bitonic sort of a[0..n) ascending over the next power of two (a has room for it; padding with ~0)
+__device__ inline void warp_sort_u64(unsigned long long* a, int n) {
+  int P = 1;
+  while (P < n) P <<= 1;
+  for (int i = n + lane_id(); i < P; i += 32) a[i] = ~0ull;
+  __syncwarp();
+  for (int size = 2; size <= P; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int q = lane_id(); q < (P >> 1); q += 32) {
+        const int lo = ((q & ~(stride - 1)) << 1) | (q & (stride - 1));
+        const int hi = lo + stride;
+        const bool up = (lo & size) == 0;
+        const unsigned long long x = a[lo], y = a[hi];
+        if ((x > y) == up) { a[lo] = y; a[hi] = x; }
+      }
+      __syncwarp();
+    }
+}
 
 // pass 0: events with at most hcap hits (others deferred); pass 1: deferred events with at most hcap hits (others stay
 // deferred); pass 2: the remaining deferred events, lists in global memory (gscratch) sized by the event.
@@ -368,6 +387,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
   extern __shared__ __align__(16) char smem[];
   CoincShared S;
   CoincWork W;
+  unsigned long long* sk = nullptr;                // global pass: (layer, counter, order) sort words
   if (pass < 2) {
     size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
     char* wb = smem + size_t(warp_in_block()) * per;
@@ -384,6 +404,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
       char* wb = gscratch + size_t(r0 + 16 * e) * COINC_GBYTES;
       S = coinc_carve(wb, hcap);
       W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
+      sk = reinterpret_cast<unsigned long long*>(wb + coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap));
     }
     // hits in pulse order
     int H = 0;
@@ -451,6 +472,59 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
       for (int side = 0; side < 2; ++side) {
         // filterHits over the side's hits (list order sums)
         int f0 = nf;
+        if (pass == 2) {
+          // large events: the side's hits sorted by (layer, counter, list order); each hit sums the entries of its own
+          // and the two adjacent counters, which are contiguous there and, per counter, in list order
+          int ns = 0;
+          for (int base = 0; base < nt; base += 32) {
+            const int k = base + lane_id();
+            const bool on = k < nt && S.side[S.list[k]] == side;
+            const unsigned m = __ballot_sync(0xffffffffu, on);
+            if (on) {
+              const int j = ns + __popc(m & ((1u << lane_id()) - 1u));
+              const int h = S.list[k];
+              const uint32_t key = uint32_t(S.layer[h]) * 65536u + S.counter[h];
+              sk[j] = ((unsigned long long)key << 32) | uint32_t(j);
+              S.tmp[j] = h;
+            }
+            ns += __popc(m);
+          }
+          __syncwarp();
+          warp_sort_u64(sk, ns);
+          for (int base = 0; base < ns; base += 32) {
+            const int j = base + lane_id();
+            bool pass_ = false;
+            int h = -1;
+            if (j < ns) {
+              h = S.tmp[j];
+              const uint32_t K = uint32_t(S.layer[h]) * 65536u + S.counter[h];
+              const unsigned long long first = K > 0 ? (unsigned long long)(K - 1) << 32 : 0ull;
+              int lo = 0, hi = ns;
+              while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (sk[mid] < first) lo = mid + 1; else hi = mid;
+              }
+              double same = 0.0, a1 = 0.0, a2 = 0.0;
+              const double dadj = cutv(G, S.cut[h], CUT_DTADJ);
+              for (int q = lo; q < ns; ++q) {
+                const unsigned long long w = sk[q];
+                const uint32_t kq = uint32_t(w >> 32);
+                if (kq > K + 1) break;
+                const int a = S.tmp[uint32_t(w)];
+                if (fabs(S.t[a] - S.t[h]) > dadj) continue;
+                const int d = int(kq) - int(K);
+                same += d == 0 ? S.pe[a] : 0.0;
+                a1 += d == -1 ? S.pe[a] : 0.0;
+                a2 += d == 1 ? S.pe[a] : 0.0;
+              }
+              const double thr = cutv(G, S.cut[h], CUT_PE);
+              pass_ = (same + a1 >= thr) || (same + a2 >= thr);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, pass_);
+            if (pass_) S.filt[nf + __popc(m & ((1u << lane_id()) - 1u))] = h;
+            nf += __popc(m);
+          }
+        } else
         for (int base = 0; base < nt; base += 32) {
           int k = base + lane_id();
           bool pass = false;
