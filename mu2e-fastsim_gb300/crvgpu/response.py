@@ -122,6 +122,39 @@ def upload_steps(steps, device="cuda", dtype=None, nbars=None):
                        max_steps=int(cnt.max()) if len(cnt) else 0, order=order)
 
 
+@dataclass
+class PinnedSteps:
+    """A step table staged in pinned host memory with its event table (see pin_steps); to_device copies it with
+    asynchronous copies on the current stream."""
+    cols: dict
+    nsteps: int
+    nevents: int
+    max_steps: int
+
+    def to_device(self, device="cuda") -> DeviceSteps:
+        c = {k: v.to(device, non_blocking=True) for k, v in self.cols.items()}
+        return DeviceSteps(x=c["x"], y=c["y"], z=c["z"], t=c["t"], edep=c["edep"], bar=c["bar"],
+                           ev_event=c["ev_event"], ev_subrun=c["ev_subrun"], ev_run=c["ev_run"],
+                           ev_first=c["ev_first"], ev_nsteps=c["ev_nsteps"], nsteps=self.nsteps,
+                           nevents=self.nevents, max_steps=self.max_steps)
+
+    @property
+    def nbytes(self):
+        return sum(v.numel() * v.element_size() for v in self.cols.values())
+
+
+def pin_steps(steps, nbars=None) -> PinnedSteps:
+    """Host step table -> the device layout of upload_steps, in pinned host memory (events grouped and keyed once
+    on the host, so a later transfer is a set of plain copies)."""
+    torch = _torch()
+    ds = upload_steps(steps, device="cpu", nbars=nbars)
+    if ds.order is not None:
+        raise ValueError("pin_steps: events must be contiguous and in increasing key order")
+    cols = {k: getattr(ds, k).pin_memory() for k in ("x", "y", "z", "t", "edep", "bar", "ev_event", "ev_subrun",
+                                                       "ev_run", "ev_first", "ev_nsteps")}
+    return PinnedSteps(cols, ds.nsteps, ds.nevents, ds.max_steps)
+
+
 class PixelTables:
     """Photon-map running sums and dead-pixel bitmap of a SiPM configuration on the device."""
 
