@@ -380,7 +380,9 @@ __device__ inline void warp_sort_u64(unsigned long long* a, int n) {
 }
 
 // pass 0: events with at most hcap hits (others deferred); pass 1: deferred events with at most hcap hits (others stay
-// deferred); pass 2: the remaining deferred events, lists in global memory (gscratch) sized by the event.
+// deferred); pass 2 (GLOBAL): the remaining deferred events, lists in global memory (gscratch) sized by the event.
+// The global pass is its own instantiation, so the shared-memory passes do not carry its code and registers.
+template <bool GLOBAL>
 __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincGeom G, CoincIn I, int hcap,
                                                            int pass, CoincOut O, int32_t* __restrict__ deferred,
                                                            char* __restrict__ gscratch, Status* status) {
@@ -388,7 +390,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
   CoincShared S;
   CoincWork W;
   unsigned long long* sk = nullptr;                // global pass: (layer, counter, order) sort words
-  if (pass < 2) {
+  if (!GLOBAL) {
     size_t per = coinc_smem_per_warp(hcap) + coinc_work_per_warp(hcap);
     char* wb = smem + size_t(warp_in_block()) * per;
     S = coinc_carve(wb, hcap);
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
     if (pass > 0 && !deferred[e]) continue;
     long long r0 = I.ev_start[e];
     int np_ = I.ev_count[e];
-    if (pass == 2) {
+    if (GLOBAL) {
       hcap = (np_ + 15) & ~15;
       char* wb = gscratch + size_t(r0 + 16 * e) * COINC_GBYTES;
       S = coinc_carve(wb, hcap);
@@ -444,7 +446,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
     }
     if (H > hcap) {
       if (lane_id() == 0) {
-        if (pass == 2) {                             // cannot happen: the global lists hold every pulse of the event
+        if (GLOBAL) {                                // cannot happen: the global lists hold every pulse of the event
           set_flag(status, CRV_ST_CAPACITY);
           need_at_least(status, CRV_NEED_HITS_PER_EVENT, H);
           O.ncl[e] = 0; O.nmem[e] = 0;
@@ -472,7 +474,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
       for (int side = 0; side < 2; ++side) {
         // filterHits over the side's hits (list order sums)
         int f0 = nf;
-        if (pass == 2) {
+        if constexpr (GLOBAL) {
           // large events: the side's hits sorted by (layer, counter, list order); each hit sums the entries of its own
           // and the two adjacent counters, which are contiguous there and, per counter, in list order
           int ns = 0;

@@ -964,13 +964,17 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
     size_t per = k < 2 ? coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap) : 0;
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
-    CK(allow_dynamic_smem(k_coinc));
     long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
     long long maxb = (long long)di.sms * (k == 0 ? 16 : (k == 1 ? 2 : 8));
-    {
+    const unsigned grid = (unsigned)(blocks < maxb ? blocks : maxb);
+    if (k < 2) {
+      CK(allow_dynamic_smem(k_coinc<false>));
       crv::Mark mark_("k_coinc", s);
-      k_coinc<<<(unsigned)(blocks < maxb ? blocks : maxb), passes[k].warps * 32, smem, s>>>(
-          *p, G, I, passes[k].hcap, k, O, w.deferred, w.gscratch, S);
+      k_coinc<false><<<grid, passes[k].warps * 32, smem, s>>>(*p, G, I, passes[k].hcap, k, O, w.deferred, w.gscratch,
+                                                             S);
+    } else {
+      crv::Mark mark_("k_coinc_global", s);
+      k_coinc<true><<<grid, passes[k].warps * 32, 0, s>>>(*p, G, I, 0, k, O, w.deferred, w.gscratch, S);
     }
     CK(cudaGetLastError());
   }

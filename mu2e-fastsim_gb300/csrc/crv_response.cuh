@@ -292,7 +292,9 @@ __global__ void k_photon_emit(CrvParams p, CrvEvents ev, CrvSteps st, CrvBars ba
 // ---------------------------------------------------------------------------------------------------------------------
 // SiPM simulation: one warp per SiPM
 
-constexpr int TCAP = 128;        // scheduled afterpulses per SiPM
+// scheduled afterpulses per SiPM: a SiPM of at most 256 photons fires at most a few hundred pixels, with trap-0
+// probabilities of a few percent; beyond the queue the SiPM reports CRV_ST_LIMIT
+__host__ __device__ constexpr int sipm_tcap(int cap) { return cap <= 256 ? 32 : 128; }
 constexpr int SIPM_WARPS = 8;    // warps per block
 
 struct SipmGroups {
@@ -325,9 +327,6 @@ struct SipmShared {
   R* ph_t;
   uint32_t* ph_key;
   uint32_t* ph_loc;
-  R* ph_uf;                      // firing uniform of the photon (call 0), drawn once
-  uint16_t* ph_pix;              // its pixel (0xFFFF: inactive pixel), drawn once
-  uint8_t* ph_ct;                // its cross-talk mask once drawn (0xFF: not drawn yet)
   R* last;
   uint32_t* bm;
   R* tr_t;
@@ -338,15 +337,16 @@ struct SipmShared {
   uint16_t* fr_m;
   uint16_t* cand;
   int* misc;                     // [0] n candidates
+  int tcap;                      // afterpulse queue length
 };
 
 template <typename R>
 __host__ __device__ inline size_t sipm_smem_per_warp(int cap) {
   size_t b = 0;
-  b += size_t(cap) * (2 * sizeof(R) + 8 + 2 + 1);   // ph_t, ph_key, ph_loc, ph_uf, ph_pix, ph_ct
+  b += size_t(cap) * (sizeof(R) + 8);          // ph_t, ph_key, ph_loc
   b += NPX * sizeof(R);                        // last
   b += 64 * 4;                                 // bm (50 used)
-  b += TCAP * (2 * sizeof(R) + 8 + 2);         // traps
+  b += size_t(sipm_tcap(cap)) * (2 * sizeof(R) + 8 + 2);   // traps
   b += 64 * 2 + 64 * 2 + 256 * 2 + 16;         // frontier, candidates, misc
   return (b + 15) & ~size_t(15);
 }
@@ -357,20 +357,19 @@ __device__ SipmShared<R> carve(char* base, int cap) {
   char* q = base;
   S.last = reinterpret_cast<R*>(q); q += NPX * sizeof(R);
   S.ph_t = reinterpret_cast<R*>(q); q += size_t(cap) * sizeof(R);
-  S.ph_uf = reinterpret_cast<R*>(q); q += size_t(cap) * sizeof(R);
-  S.tr_t = reinterpret_cast<R*>(q); q += TCAP * sizeof(R);
-  S.tr_uf = reinterpret_cast<R*>(q); q += TCAP * sizeof(R);
-  S.tr_id = reinterpret_cast<long long*>(q); q += TCAP * 8;
+  const int tcap = sipm_tcap(cap);
+  S.tcap = tcap;
+  S.tr_t = reinterpret_cast<R*>(q); q += tcap * sizeof(R);
+  S.tr_uf = reinterpret_cast<R*>(q); q += tcap * sizeof(R);
+  S.tr_id = reinterpret_cast<long long*>(q); q += tcap * 8;
   S.ph_key = reinterpret_cast<uint32_t*>(q); q += size_t(cap) * 4;
   S.ph_loc = reinterpret_cast<uint32_t*>(q); q += size_t(cap) * 4;
   S.bm = reinterpret_cast<uint32_t*>(q); q += 64 * 4;
   S.misc = reinterpret_cast<int*>(q); q += 16;
-  S.tr_pix = reinterpret_cast<uint16_t*>(q); q += TCAP * 2;
+  S.tr_pix = reinterpret_cast<uint16_t*>(q); q += tcap * 2;
   S.fr_pix = reinterpret_cast<uint16_t*>(q); q += 64 * 2;
   S.fr_m = reinterpret_cast<uint16_t*>(q); q += 64 * 2;
   S.cand = reinterpret_cast<uint16_t*>(q); q += 256 * 2;
-  S.ph_pix = reinterpret_cast<uint16_t*>(q); q += size_t(cap) * 2;
-  S.ph_ct = reinterpret_cast<uint8_t*>(q); q += size_t(cap);
   return S;
 }
 
@@ -596,7 +595,7 @@ __device__ void run_cascade(const CrvParams& p, const SipmK<R>& K, const SipmSha
       int tpos = warp_excl(ntr, &tot);
       for (int a = 0; a < ntr; ++a) {
         int k = C.ntr + tpos + a;
-        if (k < TCAP) { S.tr_t[k] = tt[a]; S.tr_uf[k] = uf[a]; S.tr_pix[k] = uint16_t(q); S.tr_id[k] = id; }
+        if (k < S.tcap) { S.tr_t[k] = tt[a]; S.tr_uf[k] = uf[a]; S.tr_pix[k] = uint16_t(q); S.tr_id[k] = id; }
       }
       C.ntr += tot;
       // candidates
@@ -627,15 +626,6 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
                               long long gstart, long long id_base) {
   using M = Math<R>;
   for (int w = lane_id(); w < 64; w += 32) S.bm[w] = 0u;
-  // The draws of a photon do not depend on the pixel state: take them once here.  A 32-photon step below commits
-  // only up to the first collision or cascade, and the photons after that are evaluated again in the next step.
-  for (int i = lane_id(); i < n; i += 32) {
-    U4 w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), S.ph_key[i]);
-    int pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0));
-    S.ph_pix[i] = pix < 0 ? uint16_t(0xFFFF) : uint16_t(pix);
-    S.ph_uf[i] = M::uni(w0, 1);
-    S.ph_ct[i] = uint8_t(0xFF);
-  }
   __syncwarp();
   int k = 0;
   while (k < n) {
@@ -644,9 +634,10 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     R t = has ? S.ph_t[i] : R(0);
     uint32_t key = has ? S.ph_key[i] : 0u;
     int pix = -1;
+    U4 w0{0, 0, 0, 0};
     if (has) {
-      const uint16_t pp = S.ph_pix[i];
-      pix = pp == 0xFFFF ? -1 : int(pp);
+      w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), key);
+      pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0));
     }
     bool live = pix >= 0;
     unsigned same = __match_any_sync(FULL, live ? pix : -1 - lane_id());
@@ -657,15 +648,8 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     if (live && !collide) {
       v = recovered<R>(K, S, pix, t);
       R pm = pfire_m<R>(K, v, 1);
-      fire = S.ph_uf[i] < pm;
-      if (fire) {
-        uint8_t c = S.ph_ct[i];
-        if (c == 0xFF) {
-          c = uint8_t(node_crosstalk<R>(p, K, C, 0, 0, key, pix));
-          S.ph_ct[i] = c;
-        }
-        ct = c;
-      }
+      fire = M::uni(w0, 1) < pm;
+      if (fire) ct = node_crosstalk<R>(p, K, C, 0, 0, key, pix);
     }
     int nv = min(n - k, 32);
     unsigned cm = __ballot_sync(FULL, collide);
@@ -690,7 +674,7 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     int tpos = warp_excl(ntr, &tot);
     for (int a = 0; a < ntr; ++a) {
       int kk = C.ntr + tpos + a;
-      if (kk < TCAP) { S.tr_t[kk] = tt[a]; S.tr_uf[kk] = uf[a]; S.tr_pix[kk] = uint16_t(pix); S.tr_id[kk] = id; }
+      if (kk < S.tcap) { S.tr_t[kk] = tt[a]; S.tr_uf[kk] = uf[a]; S.tr_pix[kk] = uint16_t(pix); S.tr_id[kk] = id; }
     }
     C.ntr += tot;
     __syncwarp();
@@ -704,13 +688,13 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     }
     k += ncommit;
   }
-  if (C.ntr > TCAP) C.limit = 1;
+  if (C.ntr > S.tcap) C.limit = 1;
 }
 
 // Afterpulses after all photons, in (time, schedule order); stored after the main records.  Returns the count.
 template <typename R>
 __device__ int run_afterpulses(const SipmK<R>& K, const SipmShared<R>& S, SipmCtx& C, const SipmOut& O) {
-  int ntr = min(C.ntr, TCAP);
+  int ntr = min(C.ntr, S.tcap);
   int nap = 0;
   if (lane_id() == 0 && ntr > 0) {
     // insertion sort by time (stable: equal times keep schedule order)
