@@ -386,8 +386,8 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
                                                         w.id_base, w.label, w.run);
   }
   CK(cudaGetLastError());
-  CK(exclusive_scan(w.nphot, w.nb, Identity(), w.ph_off, &w.totals[1], w.parts, s));
-  CK(exclusive_scan(w.slot_cap, w.nb, Identity(), w.slot_off, &w.totals[2], w.parts, s));
+  CK(exclusive_scan(w.nphot, w.nb, Identity(), w.ph_off, &w.totals[1], w.parts, s, &w.totals[0]));
+  CK(exclusive_scan(w.slot_cap, w.nb, Identity(), w.slot_off, &w.totals[2], w.parts, s, &w.totals[0]));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], w.pc, CRV_NEED_PHOTONS_TOTAL, S);
@@ -432,7 +432,7 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
     k_counts_total<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.nmain, w.nap, w.ntot);
   }
   CK(cudaGetLastError());
-  CK(exclusive_scan(w.ntot, w.nb, Identity(), w.out_off, &w.totals[3], w.parts, s));
+  CK(exclusive_scan(w.ntot, w.nb, Identity(), w.out_off, &w.totals[3], w.parts, s, &w.totals[0]));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_CHARGES_OUT, S);
@@ -690,7 +690,7 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   else
     CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen,
                                  w.g_nkept, w.cl, s));
-  CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s));
+  CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s, &w.totals[0]));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], slot_cap, CRV_NEED_DIGIS, S);
@@ -708,7 +708,7 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   else
     CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.g_nkept, w.cl,
                                w.D, S, s));
-  CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s));
+  CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s, &w.totals[2]));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[3], out_cap, CRV_NEED_DIGIS_OUT, S);

@@ -11,15 +11,26 @@ constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_ITEMS = 8;                        // items per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
+// effective length: the host bound n, or the device count *n_dev when it is smaller (arrays sized by an upper bound)
+__device__ __forceinline__ long long scan_len(long long n, const long long* n_dev) {
+  if (!n_dev) return n;
+  long long m = *n_dev;
+  return m < n ? m : n;
+}
+
 template <typename T, typename F>
-__global__ void k_scan_reduce(const T* __restrict__ in, long long n, F f, long long* __restrict__ part) {
+__global__ void k_scan_reduce(const T* __restrict__ in, long long n, const long long* __restrict__ n_dev, F f,
+                              long long* __restrict__ part) {
   __shared__ long long red[SCAN_THREADS / 32];
+  n = scan_len(n, n_dev);
   long long base = (long long)blockIdx.x * SCAN_TILE;
   long long s = 0;
+  if (base < n) {
 #pragma unroll
-  for (int j = 0; j < SCAN_ITEMS; ++j) {
-    long long i = base + (long long)j * SCAN_THREADS + threadIdx.x;
-    if (i < n) s += f(in[i]);
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+      long long i = base + (long long)j * SCAN_THREADS + threadIdx.x;
+      if (i < n) s += f(in[i]);
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -36,23 +47,31 @@ __global__ void k_scan_reduce(const T* __restrict__ in, long long n, F f, long l
 // exclusive scan of part[0..nb) in place by one block; total -> *total (device)
 __global__ void k_scan_parts(long long* __restrict__ part, long long nb, long long* __restrict__ total);
 
+// Tile of SCAN_TILE items: coalesced loads into shared memory, each thread scans SCAN_ITEMS consecutive items there,
+// coalesced stores of the results.
 template <typename T, typename F>
-__global__ void k_scan_down(const T* __restrict__ in, long long n, F f, const long long* __restrict__ part,
-                            long long* __restrict__ out) {
+__global__ void k_scan_down(const T* __restrict__ in, long long n, const long long* __restrict__ n_dev, F f,
+                            const long long* __restrict__ part, long long* __restrict__ out) {
+  __shared__ long long tile[SCAN_TILE];
   __shared__ long long wsum[SCAN_THREADS / 32];
+  n = scan_len(n, n_dev);
   long long base = (long long)blockIdx.x * SCAN_TILE;
+  if (base >= n) return;                                      // the whole block: uniform
   long long off = part[blockIdx.x];
-  // each thread owns SCAN_ITEMS consecutive items
-  long long v[SCAN_ITEMS];
-  long long s = 0;
-  long long t0 = base + (long long)threadIdx.x * SCAN_ITEMS;
 #pragma unroll
   for (int j = 0; j < SCAN_ITEMS; ++j) {
-    long long i = t0 + j;
-    v[j] = i < n ? f(in[i]) : 0;
+    int k = j * SCAN_THREADS + threadIdx.x;
+    long long i = base + k;
+    tile[k] = i < n ? f(in[i]) : 0;
+  }
+  __syncthreads();
+  long long v[SCAN_ITEMS];
+  long long s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    v[j] = tile[threadIdx.x * SCAN_ITEMS + j];
     s += v[j];
   }
-  // block exclusive scan of s
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   long long x = s;
 #pragma unroll
@@ -76,9 +95,15 @@ __global__ void k_scan_down(const T* __restrict__ in, long long n, F f, const lo
   long long run = off + wsum[w] + (x - s);
 #pragma unroll
   for (int j = 0; j < SCAN_ITEMS; ++j) {
-    long long i = t0 + j;
-    if (i < n) out[i] = run;
+    tile[threadIdx.x * SCAN_ITEMS + j] = run;
     run += v[j];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    int k = j * SCAN_THREADS + threadIdx.x;
+    long long i = base + k;
+    if (i < n) out[i] = tile[k];
   }
 }
 
@@ -89,10 +114,11 @@ struct Identity {
 
 inline long long scan_parts_len(long long n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
 
-// out[i] = sum_{j<i} f(in[j]); *total = sum f(in).  part: scratch of scan_parts_len(n) + 1 entries.
+// out[i] = sum_{j<i} f(in[j]); *total = sum f(in).  part: scratch of scan_parts_len(n) + 1 entries.  n_dev (may be
+// null): device count of valid items when n is only an upper bound; items beyond it are neither read nor written.
 template <typename T, typename F>
 cudaError_t exclusive_scan(const T* in, long long n, F f, long long* out, long long* total, long long* part,
-                           cudaStream_t s) {
+                           cudaStream_t s, const long long* n_dev = nullptr) {
   long long nb = scan_parts_len(n);
   if (nb == 0) {
     cudaMemsetAsync(total, 0, sizeof(long long), s);
@@ -100,7 +126,7 @@ cudaError_t exclusive_scan(const T* in, long long n, F f, long long* out, long l
   }
   {
     crv::Mark mark_("k_scan_reduce", s);
-    k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part);
+    k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, n_dev, f, part);
   }
   {
     crv::Mark mark_("k_scan_parts", s);
@@ -108,7 +134,7 @@ cudaError_t exclusive_scan(const T* in, long long n, F f, long long* out, long l
   }
   {
     crv::Mark mark_("k_scan_down", s);
-    k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, f, part, out);
+    k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, n_dev, f, part, out);
   }
   return cudaGetLastError();
 }

@@ -460,6 +460,23 @@ __global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D
     if (nd > D.cap[g]) continue;
     long long s0 = D.off[g], o0 = out_off[g];
     if (o0 + nd > out_cap) continue;
+    // digis come out of the synthesis in start order (clusters in time order, digis in sample order): then the stable
+    // order by start is the production order and the copy runs over all lanes
+    bool sorted = true;
+    for (int j = lane_id() + 1; j < nd; j += 32) sorted = sorted && !(D.start[s0 + j] < D.start[s0 + j - 1]);
+    if (__all_sync(0xffffffffu, sorted)) {
+      for (int i = lane_id(); i < nd; i += 32) {
+        O.chan[o0 + i] = D.chan[s0 + i];
+        O.start[o0 + i] = D.start[s0 + i];
+        O.tdc0[o0 + i] = D.tdc0[s0 + i];
+        O.starttdc[o0 + i] = D.starttdc[s0 + i];
+      }
+      for (long long f = lane_id(); f < (long long)nd * zs; f += 32) {
+        O.volt[o0 * zs + f] = D.volt[s0 * zs + f];
+        O.adc[o0 * zs + f] = D.adc[s0 * zs + f];
+      }
+      continue;
+    }
     for (int i = 0; i < nd; ++i) {
       // rank of digi i among the group's digis by start, ties by production order
       double si = D.start[s0 + i];
