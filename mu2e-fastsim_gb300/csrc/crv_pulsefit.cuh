@@ -45,7 +45,7 @@ __device__ __forceinline__ double round_half_away(double x) {
 
 // LU with partial pivoting (largest |a| in the column, first on ties), then substitution.  Returns false on a zero
 // pivot (singular).
-__device__ __forceinline__ bool solve3(const double M[3][3], const double r[3], double x[3]) {
+static __device__ __noinline__ bool solve3(const double M[3][3], const double r[3], double x[3]) {
   double a[3][3], b[3];
   for (int i = 0; i < 3; ++i) {
     b[i] = r[i];
@@ -113,7 +113,7 @@ __device__ __forceinline__ bool solve3_p(const double M[3][3], const double b[3]
 }
 
 // eigenvalues of a symmetric 3x3 matrix (cyclic Jacobi), ascending
-__device__ __forceinline__ void eig3(const double M[3][3], double e[3]) {
+static __device__ __noinline__ void eig3(const double M[3][3], double e[3]) {
   double a[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) a[i][j] = M[i][j];
@@ -155,8 +155,8 @@ struct Fit3 {
 // (tdc_fs + i) * period.  Sums are sequential over the points (the reference's contractions are sequential).
 // R = double: every operation in FP64; R = float: mapping, residuals and sums in FP32 relative to the window start.
 template <typename R>
-__device__ __forceinline__ void eval_lane(const Fit3& F, const double u[3], const R* yw, long long tdc_fs,
-                                          double period, int P, double* chi2, double H[6], double g[3]) {
+static __device__ __noinline__ void eval_lane(const Fit3& F, const double u[3], const R* yw, long long tdc_fs,
+                                              double period, int P, double* chi2, double H[6], double g[3]) {
   R A, mu, b, d0, d1, d2;
   if (sizeof(R) == 8) {
     double p0 = F.lo[0] + (F.hi[0] - F.lo[0]) * (sin(u[0]) + 1.0) * 0.5;
@@ -376,13 +376,16 @@ __device__ __forceinline__ void subtract_lane(const CrvParams& p, R* y, int n, l
 }
 
 // ---- FP32-mixed fit: evaluation, mapping and state in FP32, the normal-equation solve in FP64 -----------------------
+//
+// The evaluation and the solves are called, not inlined: inlined at each call site they made the round kernel large
+// enough to stall on instruction fetch (1.7x faster as calls).
 
 struct Fit3f {
   float lo[3], w[3], half[3];   // lower bound (time: relative to the window's first sample), span, half span
 };
 
 // residuals / normal equations at internal parameters u; window sample i at time i * period
-__device__ __forceinline__ void eval_f32(const Fit3f& F, const float u[3], const float* yw, float period, int P,
+static __device__ __noinline__ void eval_f32(const Fit3f& F, const float u[3], const float* yw, float period, int P,
                                          float* chi2, float H[6], float g[3]) {
   float s0, c0, s1, c1, s2, c2;
   sincosf(u[0], &s0, &c0);
@@ -418,7 +421,7 @@ __device__ __forceinline__ void eval_f32(const Fit3f& F, const float u[3], const
 
 // symmetric 3x3 solve M x = b (M packed 00 01 02 11 12 22): cofactors, determinant and adjugate product in FP64
 // (products of FP32 inputs are exact there), the final division by the determinant in FP32
-__device__ __forceinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {
+static __device__ __noinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {
   const double m00 = f2d(M[0]), m01 = f2d(M[1]), m02 = f2d(M[2]), m11 = f2d(M[3]), m12 = f2d(M[4]), m22 = f2d(M[5]);
   const double c00 = m11 * m22 - m12 * m12;
   const double c01 = m12 * m02 - m01 * m22;
