@@ -957,10 +957,11 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
   CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
   const DeviceInfo& di = device_info();
-  // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM), up to 1024 hits in a second
-  // pass; larger events (full-scale detector) in a third pass with their lists in global memory
+  // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM); the larger ones in a pass
+  // with their lists in global memory (many warps per SM, where a 1024-hit shared-memory pass fits two)
   struct Pass { int hcap, warps; } passes[3] = {{192, 1}, {1024, 1}, {0, 1}};
   for (int k = 0; k < 3; ++k) {
+    if (k == 1) continue;
     size_t per = k < 2 ? coinc_smem_per_warp(passes[k].hcap) + coinc_work_per_warp(passes[k].hcap) : 0;
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
