@@ -605,8 +605,8 @@ static DigiWs digi_layout(char* base, long long nq, long long slot_cap, int zs, 
   DigiWs w;
   w.sc = slot_cap;
   w.head = c.take<int32_t>(nq);
-  static_assert(sizeof(WfCluster) == 2 * sizeof(long long), "cluster record size");
-  w.gidx = c.take<long long>(2 * nq);
+  static_assert(sizeof(WfCluster) == 4 * sizeof(long long), "cluster record size");
+  w.gidx = c.take<long long>(4 * nq);
   w.cl = reinterpret_cast<WfCluster*>(w.gidx);
   w.gstart = c.take<long long>(nq);
   w.glabel = c.take<long long>(nq);

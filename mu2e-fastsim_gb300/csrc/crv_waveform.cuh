@@ -101,15 +101,38 @@ __device__ __forceinline__ int tmpl_index_f(int J, float dt, float P, float inv_
   return ti < float(tlen) ? int(ti) : -1;
 }
 
-// A kept cluster: t_start = k0 P + TDC0; first charge row (relative to the group start); length in samples.
+// A kept cluster, computed once per cluster by the prepass (one thread per SiPM): t_start = k0 P + TDC0, charge rows
+// [a, b) relative to the group start, length in samples, and the samples whose start lies in the window [ilo, ihi]
+// (valid while the length fits a synthesis pass, at most 16,384 samples).
 struct WfCluster {
+  double ts;
   long long k0;
-  int32_t a, L;
+  int32_t a, b, L;
+  int16_t ilo, ihi;
 };
 
 // t_start of a cluster, rounded the same way wherever it is formed (no contraction into an FMA)
 __device__ __forceinline__ double cluster_ts(long long k0, double period, double tdc0) {
   return __dadd_rn(__dmul_rn(double(k0), period), tdc0);
+}
+
+// samples of a cluster whose start lies in the window: [i_lo, i_hi] (monotone predicates)
+__device__ __forceinline__ void window_bounds(const CrvParams& p, double ts, int L, int* lo_o, int* hi_o) {
+  if (ts >= p.window_lo && __dadd_rn(ts, __dmul_rn(double(L - 1), p.period)) <= p.window_hi) {
+    *lo_o = 0;
+    *hi_o = L - 1;
+    return;
+  }
+  double a0 = ceil((p.window_lo - ts) / p.period);
+  long long c = (long long)fmax(a0 - 1.0, 0.0);
+  while (c < L && !(__dadd_rn(ts, __dmul_rn(double(c), p.period)) >= p.window_lo)) ++c;
+  while (c > 0 && __dadd_rn(ts, __dmul_rn(double(c - 1), p.period)) >= p.window_lo) --c;
+  double b0 = floor((p.window_hi - ts) / p.period);
+  long long d = (long long)fmin(b0 + 1.0, double(L - 1));
+  while (d >= 0 && !(__dadd_rn(ts, __dmul_rn(double(d), p.period)) <= p.window_hi)) --d;
+  while (d + 1 < L && __dadd_rn(ts, __dmul_rn(double(d + 1), p.period)) <= p.window_hi) ++d;
+  *lo_o = int(c);
+  *hi_o = int(d);
 }
 
 // cluster_length for one thread (charges a..b-1 in turn); nr = reach_samples(p), ip = 1 / template precision
@@ -181,7 +204,9 @@ __global__ void __launch_bounds__(256) k_wf_prepass(CrvParams p, CrvChannels ch,
         const int L = cluster_length_serial<R>(p, t, a, b, ts, tlen, nr, ip);
         bound += (L + zs - 1) / zs;
         maxlen = L > maxlen ? L : maxlen;
-        cl[q0 + nk] = WfCluster{k0, a, L};
+        int ilo = 0, ihi = -1;
+        if (L <= 16384) window_bounds(p, ts, L, &ilo, &ihi);
+        cl[q0 + nk] = WfCluster{ts, k0, a, b, L, int16_t(ilo), int16_t(ihi)};
         ++nk;
       }
       a = b;
@@ -193,24 +218,6 @@ __global__ void __launch_bounds__(256) k_wf_prepass(CrvParams p, CrvChannels ch,
   }
 }
 
-// samples of a cluster whose start lies in the window: [i_lo, i_hi] (monotone predicates)
-__device__ __forceinline__ void window_bounds(const CrvParams& p, double ts, int L, int* lo_o, int* hi_o) {
-  if (ts >= p.window_lo && __dadd_rn(ts, __dmul_rn(double(L - 1), p.period)) <= p.window_hi) {
-    *lo_o = 0;
-    *hi_o = L - 1;
-    return;
-  }
-  double a0 = ceil((p.window_lo - ts) / p.period);
-  long long c = (long long)fmax(a0 - 1.0, 0.0);
-  while (c < L && !(__dadd_rn(ts, __dmul_rn(double(c), p.period)) >= p.window_lo)) ++c;
-  while (c > 0 && __dadd_rn(ts, __dmul_rn(double(c - 1), p.period)) >= p.window_lo) --c;
-  double b0 = floor((p.window_hi - ts) / p.period);
-  long long d = (long long)fmin(b0 + 1.0, double(L - 1));
-  while (d >= 0 && !(__dadd_rn(ts, __dmul_rn(double(d), p.period)) <= p.window_hi)) --d;
-  while (d + 1 < L && __dadd_rn(ts, __dmul_rn(double(d + 1), p.period)) <= p.window_hi) ++d;
-  *lo_o = int(c);
-  *hi_o = int(d);
-}
 
 constexpr int WF_QSTAGE = 512;    // charges of a cluster staged in shared memory (larger clusters: on the fly)
 
@@ -247,7 +254,7 @@ __device__ __forceinline__ int16_t adc_of_f(const CrvParams& p, float v, float c
 
 // Synthesis + zero suppression of the groups whose longest kept cluster is in (lo, cap].
 template <typename R>
-__global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
+__global__ void __launch_bounds__(256, 3) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
                                                   const double* __restrict__ charge, const double* __restrict__ tmpl,
                                                   int tlen, const double* __restrict__ g_tdc0,
                                                   const int32_t* __restrict__ g_maxlen,
@@ -271,7 +278,6 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
   const R vthr = R(p.min_voltage);
   const R sigma = R(p.noise_sigma);
   const float conv_f = float(p.adc_conversion), off_f = float(double(p.adc_pedestal) + 0.5);
-  const double gap = p.spe_max_time + 4.0 * p.period;
   long long ng = *G.n;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
@@ -284,7 +290,6 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
       }
       continue;
     }
-    int n = G.count[g];
     long long q0 = G.start[g];
     const double* t = time + q0;
     const double* qc = charge + q0;
@@ -300,17 +305,9 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
     const int nk = g_nkept[g];
     for (int kc = 0; kc < nk; ++kc) {
       const WfCluster C = cl[q0 + kc];
-      const int a = C.a;
-      int b = a + 1;                                 // cluster end: first gap > max_time + 4 periods
-      while (b < n) {
-        int i = b + lane_id();
-        unsigned m = __ballot_sync(0xffffffffu, i < n && (t[i] - t[i - 1] > gap));
-        if (m) { b += __ffs(m) - 1; break; }
-        b += n - b < 32 ? n - b : 32;
-      }
+      const int a = C.a, b = C.b, L = C.L;
       const long long k0 = C.k0;
-      const double ts = cluster_ts(k0, p.period, tdc0);
-      const int L = C.L;
+      const double ts = C.ts;
       // stage each charge's first reached sample and normalised charge (once per charge, not per sample)
       const bool staged = (b - a) <= WF_QSTAGE;
       if (staged) {
@@ -381,8 +378,7 @@ __global__ void __launch_bounds__(256) k_wf_synth(CrvParams p, WfGroups G, const
         wave[j] = acc;
       }
       __syncwarp();
-      int i_lo, i_hi;
-      window_bounds(p, ts, L, &i_lo, &i_hi);
+      const int i_lo = C.ilo, i_hi = C.ihi;
       // zero suppression over chunks of 32 samples
       int next_i = 0;
       for (int base = 0; base < L; base += 32) {
