@@ -441,7 +441,8 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
     crv::Mark mark_("k_charge_compact", s);
     k_charge_compact<<<grid_for(w.nb, 8, 16), 256, 0, s>>>(&w.totals[0], w.label, w.slot_off, w.slot_cap, w.nmain,
                                                             w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
-                                                            p->capacitance, p->overvoltage, *out, out_cap);
+                                                            p->capacitance, p->overvoltage, p->precision == 1,
+                                                            *out, out_cap);
   }
   CK(cudaGetLastError());
   {
@@ -574,7 +575,8 @@ extern "C" int crv_sipm(const CrvParams* p, const CrvPixels* px, int64_t ngroups
     crv::Mark mark_("k_charge_compact", s);
     k_charge_compact<<<grid_for(ngroups, 8, 16), 256, 0, s>>>(&w.totals[0], G.label, w.slot_off, w.slot_cap, w.nmain,
                                                                w.nap, w.out_off, w.slot_t, w.slot_v, w.slot_id,
-                                                               p->capacitance, p->overvoltage, *out, out_cap);
+                                                               p->capacitance, p->overvoltage, p->precision == 1,
+                                                            *out, out_cap);
   }
   CK(cudaGetLastError());
   if (g_charges)

@@ -869,7 +869,9 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
                                  const int32_t* __restrict__ nmain, const int32_t* __restrict__ nap,
                                  const long long* __restrict__ out_off, const double* __restrict__ st,
                                  const double* __restrict__ sv, const long long* __restrict__ sid, double capacitance,
-                                 double overvoltage, CrvCharges out, long long out_cap) {
+                                 double overvoltage, int fp32, CrvCharges out, long long out_cap) {
+  // FP32-mixed: voltages are FP32 values; charge and PE in FP32 (no FP64 multiply and division per charge)
+  const float cap_f = float(capacitance), inv_vov_f = 1.0f / float(overvoltage);
   long long ngroups = *ngroups_dev;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ngroups; g += warps) {
@@ -900,8 +902,14 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
       double v = sv[src];
       out.label[o] = lab;
       out.time[o] = t;
-      out.charge[o] = capacitance * v;
-      out.pe[o] = v / overvoltage;
+      if (fp32) {
+        const float vf = d2f_trunc(v);
+        out.charge[o] = f2d(cap_f * vf);
+        out.pe[o] = f2d(vf * inv_vov_f);
+      } else {
+        out.charge[o] = capacitance * v;
+        out.pe[o] = v / overvoltage;
+      }
       out.photon[o] = sid[src];
     }
   }
