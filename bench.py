@@ -205,6 +205,8 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
     chunks = [uneven_chunk(min(chunk, total - c0), 1000 + c0, device) for c0 in range(0, total, chunk)]
     out["samples"] = sum(c["ns"] for c in chunks)
     out["true_pulses"] = sum(c["true"] for c in chunks)
+    from crvgpu.pulsefit import DEFAULT_SHAPE, GraphFitter, ShapeTuner, set_shape
+    set_shape(DEFAULT_SHAPE)
     for prec in ("fp32", "fp64"):
         eng = PulseEngine(device)
         eng.out_factor = 16.0
@@ -225,6 +227,37 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         out[prec] = {"waveforms_per_s": total / (ms / 1000.0), "ms": ms, "pulses": found}
+    # FP32-mixed with the launch shape tuned for the batch size and every batch a replay of one captured CUDA graph
+    eng = PulseEngine(device)
+    eng.out_factor = 16.0
+    P = make_params(reco=CF.RecoConfig(), precision="fp32")
+    P.period = CF.PERIOD
+    kw = lambda c: dict(off=c["off"], n=c["n"], start_tdc=c["start"], ped=c["ped"], area=c["area"],  # noqa: E731
+                        height=c["height"], adc16=c["adc"], max_pulses=2 ** 31 - 1, nsamples=c["ns"])
+    tuner = ShapeTuner()
+    shape = tuner.shape_for(eng, P, kw(chunks[0]))
+    set_shape(shape)
+    gf = GraphFitter(P, max(int(c["n"].numel()) for c in chunks), max(c["ns"] for c in chunks), 16 * chunk)
+    first = gf.fit(chunks[0]["off"], chunks[0]["n"], chunks[0]["start"], chunks[0]["ped"], chunks[0]["area"],
+                   chunks[0]["height"], chunks[0]["adc"])
+    plain = eng.run(P, **kw(chunks[0]))
+    same = all(torch.equal(first[k], plain[k]) for k in plain)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    found = 0
+    e0.record()
+    for c in chunks:
+        found += int(gf.fit(c["off"], c["n"], c["start"], c["ped"], c["area"], c["height"], c["adc"])["wf"].numel())
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out["fp32_tuned_graph"] = {"waveforms_per_s": total / (ms / 1000.0), "ms": ms, "pulses": found,
+                               "shape": {"threads": shape[0], "blocks_per_sm": shape[1], "rounds": shape[2]},
+                               "tuning_ms": {f"{a}/{b}/{c}": round(v, 3) for (a, b, c), v in
+                                             tuner.best[tuner.bucket(int(chunks[0]['n'].numel()))][1].items()},
+                               "matches_plain": bool(same)}
+    set_shape(DEFAULT_SHAPE)
+    gf = None
     if out["fp64"]["waveforms_per_s"]:
         out["fp32_over_fp64"] = out["fp32"]["waveforms_per_s"] / out["fp64"]["waveforms_per_s"]
     return out

@@ -278,6 +278,14 @@ int crv_pulses(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *
                CrvStatus *status_dev);
 
 /*
+ * Launch shape of the pulse-fit rounds for later crv_pulses calls of this process (no counterpart in the reference;
+ * chosen per size bucket by the host's autotuner): threads per block 64 or 128, blocks per SM 1..32, round
+ * launches before the tail launch 1..32.  Results do not depend on the shape.  Returns CRV_ERR_ARG outside those
+ * ranges.  Default 128 / 16 / 16.
+ */
+int crv_pulses_shape(int32_t threads, int32_t blocks_per_sm, int32_t rounds);
+
+/*
  * crv_pulses without a caller workspace (no counterpart in the reference): the scratch is a file-scope device array of
  * CRV_PULSES_STATIC_MAX_BYTES per device, so the call allocates nothing (launch profiler off).  For callers that must
  * not allocate once running: cudaMalloc/cudaFree synchronise the device and stall other streams sharing it, and plain

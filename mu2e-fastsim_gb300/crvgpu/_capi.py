@@ -129,6 +129,7 @@ _SIGS = {
     "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
     "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, P(CrvPulses),
                            c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_pulses_shape": (c_i32, [c_i32, c_i32, c_i32]),
     "crv_pulses_static": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32,
                                   P(CrvPulses), c_i64, c_p, c_p, c_p, c_p]),
     "crv_coincidences_workspace": (c_i64, [c_i64, c_i64]),

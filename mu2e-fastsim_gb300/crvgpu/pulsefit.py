@@ -62,6 +62,117 @@ class PulseEngine:
         raise RuntimeError("crv_pulses: capacities did not converge")
 
 
+DEFAULT_SHAPE = (128, 16, 16)          # threads per block, blocks per SM, round launches before the tail
+
+
+def set_shape(shape):
+    """Launch shape of the fit rounds for later calls (threads 64 or 128, blocks per SM 1..32, rounds 1..32)."""
+    _capi.check(_capi.load().crv_pulses_shape(*[int(v) for v in shape]), "crv_pulses_shape")
+
+
+SHAPES = tuple((t, b, r) for t in (64, 128) for b in (8, 16, 32) for r in (8, 16))
+
+
+class ShapeTuner:
+    """Picks the launch shape of the fit rounds per size bucket (waveforms rounded up to a power of two) by timing
+    every candidate once on the first batch of that bucket; results do not depend on the shape."""
+
+    def __init__(self, shapes=SHAPES):
+        self.shapes = tuple(shapes)
+        self.best = {}                 # bucket -> (shape, {shape: ms})
+
+    @staticmethod
+    def bucket(nw):
+        return max(0, int(nw - 1).bit_length())
+
+    def shape_for(self, eng, P, batch):
+        """Shape for this batch's bucket, tuning it first when unseen; batch = the keyword arguments of eng.run."""
+        torch = _torch()
+        b = self.bucket(int(batch["n"].numel()))
+        if b not in self.best:
+            times = {}
+            for sh in self.shapes:
+                set_shape(sh)
+                eng.run(P, **batch)                           # warm (workspace, capacities)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                eng.run(P, **batch)
+                e1.record()
+                torch.cuda.synchronize()
+                times[sh] = e0.elapsed_time(e1)
+            self.best[b] = (min(times, key=times.get), times)
+        return self.best[b][0]
+
+
+class GraphFitter:
+    """Fits batches of up to nw_cap waveforms / ns_cap samples (int16) by replaying one captured CUDA graph of
+    crv_pulses: each batch is copied into static device buffers and padded with zero-length waveforms (which find no
+    pulses), so every replay has the captured shape.  The launch shape is the one in force at capture."""
+
+    def __init__(self, P, nw_cap, ns_cap, out_cap, max_pulses=2 ** 31 - 1, device="cuda"):
+        torch = _torch()
+        L = _capi.load()
+        self.P, self.nw_cap, self.ns_cap, self.out_cap, self.device = P, int(nw_cap), int(ns_cap), int(out_cap), device
+        i64, i32, f64 = torch.int64, torch.int32, torch.float64
+        self.inp = dict(off=torch.zeros(self.nw_cap, dtype=i64, device=device),
+                        n=torch.zeros(self.nw_cap, dtype=i32, device=device),
+                        start=torch.zeros(self.nw_cap, dtype=i64, device=device),
+                        ped=torch.zeros(self.nw_cap, dtype=f64, device=device),
+                        area=torch.ones(self.nw_cap, dtype=f64, device=device),
+                        height=torch.ones(self.nw_cap, dtype=f64, device=device),
+                        adc=torch.zeros(self.ns_cap, dtype=torch.int16, device=device))
+        self.out = {k: torch.empty(self.out_cap, dtype=i64, device=device) for k in _capi.PULSE_INT}
+        self.out.update({k: torch.empty(self.out_cap, dtype=f64, device=device) for k in _capi.PULSE_FLOAT})
+        self.out.update({k: torch.empty(self.out_cap, dtype=torch.uint8, device=device) for k in _capi.PULSE_BOOL})
+        self.near = torch.empty(self.nw_cap, dtype=torch.uint8, device=device)
+        self.n_out = torch.zeros(1, dtype=i64, device=device)
+        self.status = _capi.DeviceStatus(device)
+        wsb = L.crv_pulses_workspace(ctypes.byref(P), self.nw_cap, self.ns_cap)
+        self.ws = torch.empty(int(wsb) + 1024, dtype=torch.uint8, device=device)
+        self.O = _capi.CrvPulses(*[_capi.ptr(self.out[k]) for k in _capi.PULSE_INT + _capi.PULSE_FLOAT +
+                                   _capi.PULSE_BOOL])
+        self.max_pulses = int(min(max_pulses, 2 ** 31 - 1))
+        self._call()                                          # warm-up outside the capture
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(self.graph, stream=side):
+                self.status.t.zero_()
+                self._call()
+        torch.cuda.current_stream().wait_stream(side)
+
+    def _call(self):
+        L = _capi.load()
+        x = self.inp
+        _capi.check(L.crv_pulses(ctypes.byref(self.P), self.nw_cap, self.ns_cap, _capi.ptr(x["off"]),
+                                 _capi.ptr(x["n"]), _capi.ptr(x["start"]), _capi.ptr(x["ped"]), _capi.ptr(x["area"]),
+                                 _capi.ptr(x["height"]), _capi.ptr(x["adc"]), None, self.max_pulses,
+                                 ctypes.byref(self.O), self.out_cap, _capi.ptr(self.n_out), _capi.ptr(self.near),
+                                 _capi.ptr(self.ws), self.ws.numel(), _stream(), self.status.ptr), "crv_pulses")
+
+    def fit(self, off, n, start_tdc, ped, area, height, adc16):
+        """Pulses of one batch (device tensors as PulseEngine.run takes them); returns the same dict."""
+        adc16 = adc16.reshape(-1)
+        nw, ns = int(n.numel()), int(adc16.numel())
+        if nw > self.nw_cap or ns > self.ns_cap:
+            raise ValueError(f"GraphFitter: batch of {nw} waveforms / {ns} samples exceeds its capacity")
+        x = self.inp
+        x["n"][nw:].zero_()
+        for k, v in (("off", off), ("n", n), ("start", start_tdc), ("ped", ped), ("area", area), ("height", height)):
+            x[k][:nw].copy_(v)
+        x["adc"][:ns].copy_(adc16)
+        self.graph.replay()
+        flags, need = self.status.read()
+        raise_status(flags, need, "crv_pulses (graph)")
+        m = int(self.n_out.item())
+        res = {k: v[:m] for k, v in self.out.items()}
+        res["wf_near_threshold"] = self.near[:nw]
+        return res
+
+
 _ENGINE = {}
 
 

@@ -741,8 +741,15 @@ struct PulseWs {
   PfQueue q;
 };
 
-// round launches over the task list before the tail launch finishes what is left lane by lane
-constexpr int kPulseRounds = 16;
+// round launches over the task list before the tail launch finishes what is left lane by lane (the counts array
+// has room for the largest setting)
+constexpr int kPulseRoundsMax = 32;
+
+// launch shape of the fit rounds for later crv_pulses calls of this process (crv_pulses_shape)
+struct PulseShape {
+  std::atomic<int> threads{128}, blocks_per_sm{16}, rounds{16};
+};
+static PulseShape g_pulse_shape;
 
 // record slots of waveform w: min(max_pulses, n/2 + 1) (every round advances the search by at least two samples)
 static long long pulse_slot_bound(long long nw, long long nsamples) { return nsamples / 2 + nw + 1; }
@@ -762,8 +769,10 @@ static PulseWs pulse_layout(char* base, long long nw, long long nsamples, size_t
   w.q.st = c.take<PfState>(nw);
   w.q.list[0] = c.take<long long>(nw);
   w.q.list[1] = c.take<long long>(nw);
-  w.q.counts = c.take<long long>(kPulseRounds + 2);
-  w.q.rounds = kPulseRounds;
+  w.q.counts = c.take<long long>(kPulseRoundsMax + 2);
+  w.q.rounds = g_pulse_shape.rounds.load();
+  w.q.threads = g_pulse_shape.threads.load();
+  w.q.blocks_per_sm = g_pulse_shape.blocks_per_sm.load();
   *bytes = c.off + 256;
   return w;
 }
@@ -795,6 +804,16 @@ __global__ void k_pulse_compact(long long nw, const long long* __restrict__ slot
 }
 }  // namespace crv
 
+extern "C" int crv_pulses_shape(int32_t threads, int32_t blocks_per_sm, int32_t rounds) {
+  if ((threads != 64 && threads != 128) || blocks_per_sm < 1 || blocks_per_sm > 32 || rounds < 1 ||
+      rounds > kPulseRoundsMax)
+    return CRV_ERR_ARG;
+  g_pulse_shape.threads.store(threads);
+  g_pulse_shape.blocks_per_sm.store(blocks_per_sm);
+  g_pulse_shape.rounds.store(rounds);
+  return CRV_OK;
+}
+
 extern "C" int64_t crv_pulses_workspace(const CrvParams* p, int64_t nw, int64_t nsamples) {
   if (!p || nw < 0 || nsamples < 0) return -1;
   size_t b = 0;
@@ -824,7 +843,7 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, cons
   size_t dummy;
   PulseWs w = pulse_layout(base, nw, nsamples, &dummy);
   CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
-  CK(cudaMemsetAsync(w.q.counts, 0, (kPulseRounds + 2) * sizeof(long long), s));
+  CK(cudaMemsetAsync(w.q.counts, 0, (kPulseRoundsMax + 2) * sizeof(long long), s));
   unsigned g = grid_for(nw, 256, 8);
   {
     crv::Mark mark_("k_pulse_caps", s);

@@ -557,6 +557,8 @@ struct PfQueue {
   long long* list[2];        // [nw] each: waveforms pending in even / odd rounds
   long long* counts;         // [rounds + 2]: tasks per round (zeroed before round 0)
   int rounds;                // round launches before the tail launch
+  int threads;               // launch shape of the round kernels: threads per block
+  int blocks_per_sm;         //   and blocks per SM (grid = min(needed, SMs x blocks_per_sm))
 };
 
 __device__ __forceinline__ void push_task(long long* list, long long* count, long long w, bool pend) {

@@ -45,3 +45,12 @@ def test_workspace_query_without_gpu():
     assert L.crv_response_workspace(ctypes.byref(P), 10, 400, 100000, 64) > 0
     assert L.crv_response_workspace(ctypes.byref(P), -1, 400, 100000, 64) == -1
     assert L.crv_sipm_workspace(ctypes.byref(P), 10, 1000) > 0
+
+
+def test_pulse_launch_shape_is_validated():
+    import pytest
+    from crvgpu.pulsefit import DEFAULT_SHAPE, set_shape
+    for bad in ((96, 16, 16), (128, 0, 16), (128, 16, 40), (256, 16, 16)):
+        with pytest.raises(ValueError):
+            set_shape(bad)
+    set_shape(DEFAULT_SHAPE)

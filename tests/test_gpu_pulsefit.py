@@ -76,3 +76,34 @@ def test_pulsefit_fp32_mixed_accuracy():
     assert abs(pe32.mean() / pe64.mean() - 1) < 3e-3
     dt = np.abs(r32["time"][i32][good] - r64["time"][i64][good])
     assert np.median(dt) < 0.05
+
+
+def test_graph_fitter_and_launch_shapes_match_the_engine():
+    import torch
+    from crvgpu import config as CF
+    from crvgpu.params import make_params
+    from crvgpu.pulsefit import DEFAULT_SHAPE, GraphFitter, PulseEngine, set_shape
+    from tests.helpers import uneven_waveforms
+    adc, n, start, ped, area, height = uneven_waveforms(np.random.default_rng(8), 300)
+    W, L = adc.shape
+    d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a).astype(dt))).cuda()  # noqa: E731
+    args = dict(off=d(np.arange(W) * L, np.int64), n=d(n, np.int32), start_tdc=d(start, np.int64),
+                ped=d(ped, np.float64), area=d(area, np.float64), height=d(height, np.float64))
+    adc16 = d(adc, np.int16)
+    for prec in ("fp32", "fp64"):
+        P = make_params(reco=CF.RecoConfig(), precision=prec)
+        eng = PulseEngine()
+        eng.out_factor = 16.0
+        ref = eng.run(P, **args, adc16=adc16, max_pulses=2 ** 31 - 1, nsamples=W * L)
+        try:
+            set_shape((64, 8, 4))                      # another launch shape: same results
+            other = eng.run(P, **args, adc16=adc16, max_pulses=2 ** 31 - 1, nsamples=W * L)
+            gf = GraphFitter(P, W + 37, W * L + 1000, 16 * W)   # padded capacity, replayed graph
+            got = gf.fit(args["off"], args["n"], args["start_tdc"], args["ped"], args["area"], args["height"], adc16)
+            got2 = gf.fit(args["off"], args["n"], args["start_tdc"], args["ped"], args["area"], args["height"], adc16)
+        finally:
+            set_shape(DEFAULT_SHAPE)
+        for k in ref:
+            assert torch.equal(other[k], ref[k]), (prec, k)
+            assert torch.equal(got[k], ref[k]), (prec, k)
+            assert torch.equal(got2[k], ref[k]), (prec, k)
