@@ -410,9 +410,21 @@ def main():
             tot["sipms"] += r.n_sipms
         return tot
 
-    def timed(eng, k, w):
+    def resident_pass(rc, seed):
+        tot = dict(clusters=0, pulses=0, charges=0, digis=0, events=0)
+        for ds in batches:
+            r = rc.run(ds, seed)
+            tot["clusters"] += r.counts["clusters"]
+            tot["pulses"] += r.counts["pulses"]
+            tot["charges"] += r.counts["charges"]
+            tot["digis"] += r.counts["digis"]
+            tot["events"] += r.n_events
+        return tot
+
+    def timed(eng, k, w, pass_fn=None):
+        pass_fn = pass_fn or one_pass
         for _ in range(w):
-            one_pass(eng, 5)
+            pass_fn(eng, 5)
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
@@ -421,15 +433,17 @@ def main():
         st = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         n0 = _capi.launch_count()
+        r0 = getattr(eng, "replays", 0)
         e0.record(st)
         tot = None
         for _ in range(k):
-            tot = one_pass(eng, 5)
+            tot = pass_fn(eng, 5)
         e1.record(st)
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
-        launches = _capi.launch_count() - n0
+        # library launches outside graphs, plus the kernels of every graph replay
+        launches = _capi.launch_count() - n0 + (getattr(eng, "replays", 0) - r0) * getattr(eng, "launches_per_run", 0)
         ck = clocks.stop()
         ms = e0.elapsed_time(e1)
         if dist is not None:
@@ -438,9 +452,71 @@ def main():
             ms = float(t.item())
         return ms, tot, ck, launches
 
-    ms32, tot32, clk, launches = timed(eng32, args.steps, args.warmup)
+    # per-stage engine (every stage reads its sizes back to the host)
+    ms_st, tot_st, clk_st, launches_st = timed(eng32, args.steps, args.warmup)
     ev_total = args.events * world * args.steps
+    stage_value = ev_total / (ms_st / 1000.0)
+    # resident engine: one crv_chain call per batch, replayed as a CUDA graph, explicit capacities sized by a trial
+    # batch (batches that need more grow them during the warm-up)
+    from crvgpu.resident import ChainCaps, ResidentChain, caps_for
+    from crvgpu.serve import slice_events
+    sample = slice_events(batches[0], 0, min(8192, batches[0].nevents))
+    trial = ResidentChain(eng32, caps_for(eng32, [sample]), graph=False, grow=True, max_grow=8)
+    trial.run(sample, 5)
+    scale = max(b.nevents for b in batches) / sample.nevents
+    res_caps = ChainCaps.from_counts({k: v * scale for k, v in trial.last_counts.items()},
+                                     events=max(b.nevents for b in batches), steps=max(b.nsteps for b in batches),
+                                     max_steps_per_event=max(b.max_steps for b in batches), margin=1.1)
+    trial = None
+    torch.cuda.empty_cache()
+    rchain = ResidentChain(eng32, res_caps, graph=True, grow=True)
+    ms32, tot32, clk, launches = timed(rchain, args.steps, args.warmup, pass_fn=resident_pass)
     value = ev_total / (ms32 / 1000.0)
+    resident = {"caps": rchain.caps.as_dict(), "launches_per_batch": rchain.launches_per_run,
+                "device_bytes": rchain.nbytes, "clusters_per_pass": tot32["clusters"],
+                "stage_engine_clusters_per_pass": tot_st["clusters"]}
+
+    # e2e: step tables in pinned host memory -> device (asynchronous copies on a second stream, the next batch while
+    # the current one computes) -> chain -> cluster table back to the host, one pass
+    from crvgpu.response import pin_steps
+    pinned = [pin_steps(st, nbars=geom.nbars) for st in host_batches]
+    copy_stream = torch.cuda.Stream()
+    ready = [torch.cuda.Event() for _ in pinned]
+
+    def prefetch(i):
+        with torch.cuda.stream(copy_stream):
+            d = pinned[i].to_device()
+            ready[i].record(copy_stream)
+        return d
+
+    def e2e_pass():
+        h2d = d2h = 0
+        nxt = prefetch(0)
+        for i in range(len(pinned)):
+            cur = nxt
+            torch.cuda.current_stream().wait_event(ready[i])
+            h2d += pinned[i].nbytes
+            if i + 1 < len(pinned):
+                nxt = prefetch(i + 1)
+            r_ = rchain.run(cur, 5, copy=False)
+            host_cl = {k: v.cpu().numpy() for k, v in r_.clusters.items()}
+            d2h += sum(a.nbytes for a in host_cl.values())
+        return h2d, d2h
+
+    e2e_pass()                                            # warm-up (pinned buffers, allocator)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    h2d, d2h = e2e_pass()
+    e1.record()
+    torch.cuda.synchronize()
+    e2e = args.events / (e0.elapsed_time(e1) / 1000.0)
+    r = None
+    pinned = None
+    rchain = None
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
     fp64 = None
     if not args.no_fp64:
         ms64, tot64, clk64, _ = timed(eng64, max(1, args.steps // 2), 1)
@@ -517,44 +593,6 @@ def main():
                 "kernel": "+".join(ks), "algorithmic_bytes_per_launch": b, "ms_per_launch": per_batch_ms,
                 "launch": "one event batch", "peak_kind": f"{peak_kind} (copy bandwidth)"}
 
-    # e2e: step tables in pinned host memory -> device (asynchronous copies on a second stream, the next batch while
-    # the current one computes) -> chain -> cluster table back to the host, one pass
-    from crvgpu.response import pin_steps
-    pinned = [pin_steps(st, nbars=geom.nbars) for st in host_batches]
-    copy_stream = torch.cuda.Stream()
-    ready = [torch.cuda.Event() for _ in pinned]
-
-    def prefetch(i):
-        with torch.cuda.stream(copy_stream):
-            d = pinned[i].to_device()
-            ready[i].record(copy_stream)
-        return d
-
-    def e2e_pass():
-        h2d = d2h = 0
-        nxt = prefetch(0)
-        for i in range(len(pinned)):
-            cur = nxt
-            torch.cuda.current_stream().wait_event(ready[i])
-            h2d += pinned[i].nbytes
-            if i + 1 < len(pinned):
-                nxt = prefetch(i + 1)
-            r_ = eng32.run(cur, 5)
-            host_cl = {k: v.cpu().numpy() for k, v in r_.clusters.items()}
-            d2h += sum(a.nbytes for a in host_cl.values())
-        return h2d, d2h
-
-    e2e_pass()                                            # warm-up (pinned buffers, allocator)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    h2d, d2h = e2e_pass()
-    e1.record()
-    torch.cuda.synchronize()
-    e2e = args.events / (e0.elapsed_time(e1) / 1000.0)
-    r = None
-    pinned = None
-
     # FP32-mixed accuracy vs FP64 on the first batch
     acc = {}
     try:
@@ -609,9 +647,12 @@ def main():
                 "vs_baseline": None, "dtype": "f32-mixed", "data": "synthetic",
                 "config": {"workload": f"{args.events} events/GPU, one 4x16 module of 450 cm counters, Poisson(40) "
                                        f"steps/event ({nsteps_total} steps, SoA f32 resident), full chain "
-                                       f"steps->coincidences in batches of {args.batch} events",
+                                       f"steps->coincidences in batches of {args.batch} events, resident engine "
+                                       f"(one CUDA graph replay per batch)",
                            "precision": "fp32-mixed (FP64 LM solve and absolute times)",
                            "l2": f"inputs larger than L2 ({step_bytes / 1e9:.2f} GB of steps)"},
+                "stage_engine_events_per_s": stage_value,
+                "resident": resident,
                 "fp64_plain_events_per_s": fp64,
                 "fp32_over_fp64": (value / fp64) if fp64 else None,
                 "fp32_vs_fp64": acc,

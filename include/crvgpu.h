@@ -19,6 +19,9 @@
  *   crv_coincidences                 <- crvfastsim.reco.coinc.find_event over every event, as chain.clusters
  *                                                                                     (crv/crvfastsim/reco/coinc.py:289,
  *                                                                                      crv/crvfastsim/chain.py:296-362)
+ *   crv_chain                        <- the chain above in one resident call with explicit capacities, as the
+ *                                       mixing adapter's resident CRV chain (mixing/device_crv.py:127-573,
+ *                                       mixing/DEVICE_CRV.md "Explicit capacities")
  *
  * Error convention: the return value is a host error code (CRV_OK, CRV_ERR_ARG for invalid arguments, CRV_ERR_CUDA
  * for a failed launch).  Data-dependent conditions are reported in the device status block (CrvStatus): capacity
@@ -338,6 +341,53 @@ int crv_pulse_hits(const CrvParams *p, const int32_t *status, int64_t nw, const 
                    int32_t *ev_count, int64_t *ev_key, int32_t *bar, int32_t *sipm, int32_t *seq, double *time,
                    double *pe, int64_t *n_ev_dev, int64_t *n_hit_dev, void *workspace, int64_t workspace_bytes,
                    void *stream, CrvStatus *status_dev);
+
+/*
+ * The whole chain, steps -> clusters, in one call that reads no size back to the host, so a stream capture of it is a
+ * CUDA graph that can be replayed batch after batch.  Capacities are explicit static bounds, not physics cuts
+ * (CrvChainCaps, every entry positive); every intermediate lives in the workspace.  Inputs:
+ *   - the event table has caps->events rows; a batch with fewer events fills the rest with nsteps 0;
+ *   - ev_keys / ev_runs: the event keys (subrun << 20 | event) of those rows in ascending order and their runs (rows
+ *     past the batch: keys above every real key, e.g. INT64_MAX);
+ *   - the step table has caps->steps rows, of which the first *nsteps_dev (device int64) are the batch's;
+ *   - tmpl / tlen: the single-PE template; g: the finder tables; per-channel status in ch.
+ * Outputs: clusters and members (capacity caps->pulses each) as crv_coincidences; counts_dev[10] (device int64): the
+ * CRV_CHAIN_* counts of the stages, which may exceed a capacity when the status says so (a trial batch with ample
+ * capacities gives every figure the capacities are sized from).
+ * A capacity overflow sets CRV_ST_CAPACITY with the size needed; later stages then see no items, so the outputs of a
+ * batch with any status flag set are not a result and the batch is to be rejected (re-run with larger capacities).
+ * Pulse reconstruction runs as the chain's (every pulse of a waveform, reconstruct_full's bound).  The caller zeroes the
+ * status block before the call (or inside the captured graph).
+ */
+typedef struct CrvChainCaps {
+    int64_t events;              /* rows of the event table */
+    int64_t steps;               /* rows of the step table */
+    int64_t photons;             /* photons of a batch */
+    int64_t charges;             /* SiPM charges of a batch */
+    int64_t slots;               /* digi slots before zero suppression */
+    int64_t digis;               /* digis; also bounds the reco waveforms (samples = digis * samples_zs) */
+    int64_t pulses;              /* pulses; also bounds the finder hits, clusters and members */
+    int32_t max_steps_per_event; /* largest event of any batch run with these capacities */
+    int32_t pad;
+} CrvChainCaps;
+
+#define CRV_CHAIN_CHARGES 0
+#define CRV_CHAIN_DIGIS 1
+#define CRV_CHAIN_WAVEFORMS 2
+#define CRV_CHAIN_PULSES 3
+#define CRV_CHAIN_EVENTS 4           /* events with finder hits */
+#define CRV_CHAIN_HITS 5
+#define CRV_CHAIN_CLUSTERS 6
+#define CRV_CHAIN_MEMBERS 7
+#define CRV_CHAIN_PHOTONS 8
+#define CRV_CHAIN_SLOTS 9            /* digi slots before zero suppression */
+
+int64_t crv_chain_workspace(const CrvParams *p, const CrvChainCaps *caps);
+int crv_chain(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev, const int64_t *ev_keys,
+              const uint32_t *ev_runs, const CrvSteps *st, const int64_t *nsteps_dev, const CrvBars *bars,
+              const CrvChannels *ch, const CrvPixels *px, const double *tmpl, int32_t tlen, const CrvFinderGeom *g,
+              CrvClusters *out, CrvMembers *mem, int64_t *counts_dev, void *workspace, int64_t workspace_bytes,
+              void *stream, CrvStatus *status_dev);
 
 #ifdef __cplusplus
 }

@@ -106,6 +106,15 @@ class CrvMembers(ctypes.Structure):
     _fields_ = [("cl", c_p), ("idx", c_p), ("event", c_p)]
 
 
+CHAIN_CAPS = ("events", "steps", "photons", "charges", "slots", "digis", "pulses", "max_steps_per_event")
+CHAIN_COUNTS = ("charges", "digis", "waveforms", "pulses", "events", "hits", "clusters", "members", "photons",
+                "slots")
+
+
+class CrvChainCaps(ctypes.Structure):
+    _fields_ = [(k, c_i64) for k in CHAIN_CAPS[:-1]] + [("max_steps_per_event", c_i32), ("pad", c_i32)]
+
+
 P = ctypes.POINTER
 
 _SIGS = {
@@ -143,6 +152,10 @@ _SIGS = {
                                c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_sipm": (c_i32, [P(CrvParams), P(CrvPixels), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, P(CrvCharges),
                          c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_chain_workspace": (c_i64, [P(CrvParams), P(CrvChainCaps)]),
+    "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
+                          P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters), P(CrvMembers),
+                          c_p, c_p, c_i64, c_p, c_p]),
 }
 
 # symbols declared in include/crvgpu.h (the load test checks every one is exported)

@@ -32,7 +32,8 @@ struct CoincGeom {
 };
 
 struct CoincIn {
-  long long nev;
+  long long nev;                                   // events (an upper bound when nev_dev is set)
+  const long long* nev_dev;                        // device count of events, or null
   const long long* ev_start;                       // first pulse row of event e
   const int32_t* ev_count;                         // pulses of event e
   const int32_t *bar, *sipm, *seq;
@@ -397,7 +398,8 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
     W = work_carve(wb + coinc_smem_per_warp(hcap), hcap, S);
   }
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); e < I.nev; e += warps) {
+  const long long nev = bounded_count(I.nev, I.nev_dev);
+  for (long long e = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); e < nev; e += warps) {
     if (pass > 0 && !deferred[e]) continue;
     long long r0 = I.ev_start[e];
     int np_ = I.ev_count[e];

@@ -235,6 +235,14 @@ __device__ __forceinline__ void need_at_least(Status* s, int slot, long long v) 
   atomicMax(reinterpret_cast<unsigned long long*>(&s->need[slot]), (unsigned long long)v);
 }
 
+// Item count of an array sized by an upper bound: the host bound n, or the device count *n_dev when that is smaller
+// (n_dev null: n itself).  Entry points that run inside a captured graph take their counts this way.
+__device__ __forceinline__ long long bounded_count(long long n, const long long* n_dev) {
+  if (!n_dev) return n;
+  long long m = *n_dev;
+  return m < n ? m : n;
+}
+
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ int warp_in_block() { return threadIdx.x >> 5; }
 

@@ -301,9 +301,9 @@ int crv_photon_counts(const CrvParams* p, const CrvEvents* ev, int64_t nevents, 
   }
   CK(cudaGetLastError());
   if (p->precision == 1)
-    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, step_event, nsteps, 0, count, S, s));
+    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, step_event, nsteps, nullptr, 0, count, S, s));
   else
-    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, step_event, nsteps, 0, count, S, s));
+    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, step_event, nsteps, nullptr, 0, count, S, s));
   return CRV_OK;
 }
 
@@ -323,11 +323,14 @@ int crv_photons(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const 
   return CRV_OK;
 }
 
-int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
-                 int32_t max_steps_per_event, const CrvBars* bars, const CrvChannels* ch, const CrvPixels* px,
-                 int64_t photon_cap, CrvCharges* out, int64_t out_cap, int64_t* n_out_dev, int64_t* sipm_label,
-                 int32_t* sipm_photons, int32_t* sipm_fired, int64_t sipm_cap, int64_t* n_sipm_dev, void* workspace,
-                 int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+// Stage bodies take an optional device count beside each host count (the host count is then a capacity), so that a
+// whole chain can run without reading sizes back: the public entry points pass null.
+static int response_run(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
+                        const long long* nsteps_dev, int32_t max_steps_per_event, const CrvBars* bars,
+                        const CrvChannels* ch, const CrvPixels* px, int64_t photon_cap, CrvCharges* out,
+                        int64_t out_cap, int64_t* n_out_dev, int64_t* sipm_label, int32_t* sipm_photons,
+                        int32_t* sipm_fired, int64_t sipm_cap, int64_t* n_sipm_dev, void* workspace,
+                        int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
   if (!p || !ev || !st || !bars || !ch || !px || !out || !n_out_dev || !status_dev) return CRV_ERR_ARG;
   if (st->real_bytes != 4 && st->real_bytes != 8) return CRV_ERR_ARG;
   if (nevents < 0 || nsteps < 0 || photon_cap < 0 || out_cap < 0 || max_steps_per_event < 0) return CRV_ERR_ARG;
@@ -374,9 +377,9 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
   CK(cudaGetLastError());
   // 4. photon counts per (step, SiPM)
   if (p->precision == 1)
-    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, 1, w.count, S, s));
+    CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, nsteps_dev, 1, w.count, S, s));
   else
-    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, 1, w.count, S, s));
+    CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, nsteps_dev, 1, w.count, S, s));
   // 5. per-SiPM photons and charge slots; scans
   int factor = p->charge_factor > 0 ? p->charge_factor : 1;
   {
@@ -461,6 +464,16 @@ int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const
     }
   CK(cudaGetLastError());
   return CRV_OK;
+}
+
+int crv_response(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
+                 int32_t max_steps_per_event, const CrvBars* bars, const CrvChannels* ch, const CrvPixels* px,
+                 int64_t photon_cap, CrvCharges* out, int64_t out_cap, int64_t* n_out_dev, int64_t* sipm_label,
+                 int32_t* sipm_photons, int32_t* sipm_fired, int64_t sipm_cap, int64_t* n_sipm_dev, void* workspace,
+                 int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  return response_run(p, ev, nevents, st, nsteps, nullptr, max_steps_per_event, bars, ch, px, photon_cap, out, out_cap,
+                      n_out_dev, sipm_label, sipm_photons, sipm_fired, sipm_cap, n_sipm_dev, workspace,
+                      workspace_bytes, stream, status_dev);
 }
 
 // ---- sipm.simulate over caller-grouped photons -------------------------------------------------------------------
@@ -644,11 +657,11 @@ extern "C" int64_t crv_digis_workspace(const CrvParams* p, int64_t ncharges, int
   return (int64_t)b;
 }
 
-extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const int64_t* label,
-                         const double* time, const double* charge, const double* tmpl, int32_t tlen,
-                         const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
-                         CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
-                         void* stream, CrvStatus* status_dev) {
+static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const long long* nq_dev,
+                     const int64_t* label, const double* time, const double* charge, const double* tmpl, int32_t tlen,
+                     const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
+                     CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
+                     void* stream, CrvStatus* status_dev) {
   if (!p || !ch || !out || !n_out_dev || !status_dev || ncharges < 0 || slot_cap < 0 || out_cap < 0) return CRV_ERR_ARG;
   if (p->samples_zs <= 0 || p->samples_zs > 32 || tlen <= 0 || !tmpl) return CRV_ERR_ARG;
   if (ncharges > 0 && (!label || !time || !charge)) return CRV_ERR_ARG;
@@ -672,16 +685,16 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   unsigned gq = grid_for(ncharges, 256, 8);
   {
     crv::Mark mark_("k_label_heads", s);
-    k_label_heads<<<gq, 256, 0, s>>>(ncharges, lab, w.head);
+    k_label_heads<<<gq, 256, 0, s>>>(ncharges, nq_dev, lab, w.head);
   }
-  CK(exclusive_scan(w.head, ncharges, Identity(), w.gidx, &w.totals[0], w.parts, s));
+  CK(exclusive_scan(w.head, ncharges, Identity(), w.gidx, &w.totals[0], w.parts, s, nq_dev));
   {
     crv::Mark mark_("k_label_groups", s);
-    k_label_groups<<<gq, 256, 0, s>>>(ncharges, lab, w.head, w.gidx, w.gstart, w.glabel);
+    k_label_groups<<<gq, 256, 0, s>>>(ncharges, nq_dev, lab, w.head, w.gidx, w.gstart, w.glabel);
   }
   {
     crv::Mark mark_("k_group_counts", s);
-    k_group_counts<<<gq, 256, 0, s>>>(&w.totals[0], ncharges, w.gstart, w.glabel, w.gcount,
+    k_group_counts<<<gq, 256, 0, s>>>(&w.totals[0], ncharges, nq_dev, w.gstart, w.glabel, w.gcount,
                                       reinterpret_cast<const long long*>(ev_keys), ev_runs, n_events, w.grun, S);
   }
   CK(cudaGetLastError());
@@ -727,6 +740,15 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
   }
   CK(cudaGetLastError());
   return CRV_OK;
+}
+
+extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const int64_t* label,
+                         const double* time, const double* charge, const double* tmpl, int32_t tlen,
+                         const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
+                         CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
+                         void* stream, CrvStatus* status_dev) {
+  return digis_run(p, ch, ncharges, nullptr, label, time, charge, tmpl, tlen, ev_keys, ev_runs, n_events, slot_cap,
+                   out, out_cap, n_out_dev, workspace, workspace_bytes, stream, status_dev);
 }
 
 // ---- pulsefit.reconstruct -----------------------------------------------------------------------------------------
@@ -777,16 +799,20 @@ static PulseWs pulse_layout(char* base, long long nw, long long nsamples, size_t
   return w;
 }
 
-__global__ void k_pulse_caps(long long nw, const int32_t* __restrict__ n, int max_pulses, int32_t* __restrict__ cap) {
+__global__ void k_pulse_caps(long long nw, const long long* __restrict__ nw_dev, const int32_t* __restrict__ n,
+                             int max_pulses, int32_t* __restrict__ cap) {
+  nw = bounded_count(nw, nw_dev);
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
     int b = n[w] / 2 + 1;
     cap[w] = b < max_pulses ? b : max_pulses;
   }
 }
 
-__global__ void k_pulse_compact(long long nw, const long long* __restrict__ slot_off, const int32_t* __restrict__ count,
+__global__ void k_pulse_compact(long long nw, const long long* __restrict__ nw_dev,
+                                const long long* __restrict__ slot_off, const int32_t* __restrict__ count,
                                 const long long* __restrict__ out_off, const PulseRec* __restrict__ rec,
                                 CrvPulses O, long long out_cap) {
+  nw = bounded_count(nw, nw_dev);
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
     int c = count[w];
     long long o0 = out_off[w], b0 = slot_off[w];
@@ -821,11 +847,11 @@ extern "C" int64_t crv_pulses_workspace(const CrvParams* p, int64_t nw, int64_t 
   return (int64_t)b;
 }
 
-extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, const int64_t* off, const int32_t* n,
-                          const int64_t* start_tdc, const double* ped_db, const double* area, const double* height,
-                          const int16_t* adc16, const int64_t* adc64, int32_t max_pulses, CrvPulses* out,
-                          int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
-                          int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+static int pulses_run(const CrvParams* p, int64_t nw, const long long* nw_dev, int64_t nsamples, const int64_t* off,
+                      const int32_t* n, const int64_t* start_tdc, const double* ped_db, const double* area,
+                      const double* height, const int16_t* adc16, const int64_t* adc64, int32_t max_pulses,
+                      CrvPulses* out, int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
+                      int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
   if (!p || !out || !n_out_dev || !status_dev || nw < 0 || nsamples < 0 || out_cap < 0 || max_pulses < 0)
     return CRV_ERR_ARG;
   if (nw > 0 && (!off || !n || !start_tdc || !ped_db || !area || !height || !wf_near || (!adc16 == !adc64)))
@@ -847,24 +873,24 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, cons
   unsigned g = grid_for(nw, 256, 8);
   {
     crv::Mark mark_("k_pulse_caps", s);
-    k_pulse_caps<<<g, 256, 0, s>>>(nw, n, max_pulses, w.cap);
+    k_pulse_caps<<<g, 256, 0, s>>>(nw, nw_dev, n, max_pulses, w.cap);
   }
-  CK(exclusive_scan(w.cap, nw, Identity(), w.slot_off, &w.totals[0], w.parts, s));
-  WaveIn W{nw, reinterpret_cast<const long long*>(off), n, reinterpret_cast<const long long*>(start_tdc), ped_db,
+  CK(exclusive_scan(w.cap, nw, Identity(), w.slot_off, &w.totals[0], w.parts, s, nw_dev));
+  WaveIn W{nw, nw_dev, reinterpret_cast<const long long*>(off), n, reinterpret_cast<const long long*>(start_tdc), ped_db,
            area, height, adc16, reinterpret_cast<const long long*>(adc64)};
   PulseSlots PS{w.slot_off, w.cap, w.count, wf_near, w.rec};
   if (p->precision == 1)
     CK(launch_pulsefit<float>(*p, W, w.yscr, max_pulses, PS, w.q, S, s));
   else
     CK(launch_pulsefit<double>(*p, W, w.yscr, max_pulses, PS, w.q, S, s));
-  CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s));
+  CK(exclusive_scan(w.count, nw, Identity(), w.out_off, &w.totals[1], w.parts, s, nw_dev));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[1], out_cap, CRV_NEED_PULSES_OUT, S);
   }
   {
     crv::Mark mark_("k_pulse_compact", s);
-    k_pulse_compact<<<g, 256, 0, s>>>(nw, w.slot_off, w.count, w.out_off, w.rec, *out, out_cap);
+    k_pulse_compact<<<g, 256, 0, s>>>(nw, nw_dev, w.slot_off, w.count, w.out_off, w.rec, *out, out_cap);
   }
   {
     crv::Mark mark_("k_copy_i64", s);
@@ -872,6 +898,15 @@ extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, cons
   }
   CK(cudaGetLastError());
   return CRV_OK;
+}
+
+extern "C" int crv_pulses(const CrvParams* p, int64_t nw, int64_t nsamples, const int64_t* off, const int32_t* n,
+                          const int64_t* start_tdc, const double* ped_db, const double* area, const double* height,
+                          const int16_t* adc16, const int64_t* adc64, int32_t max_pulses, CrvPulses* out,
+                          int64_t out_cap, int64_t* n_out_dev, uint8_t* wf_near, void* workspace,
+                          int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  return pulses_run(p, nw, nullptr, nsamples, off, n, start_tdc, ped_db, area, height, adc16, adc64, max_pulses, out,
+                    out_cap, n_out_dev, wf_near, workspace, workspace_bytes, stream, status_dev);
 }
 
 // ---- coincidences ---------------------------------------------------------------------------------------------------
@@ -905,11 +940,13 @@ static CoincWs coinc_layout(char* base, long long nev, long long np, size_t* byt
   return w;
 }
 
-__global__ void k_coinc_compact(long long nev, const long long* __restrict__ ev_start, const long long* __restrict__ ev_key,
+__global__ void k_coinc_compact(long long nev, const long long* __restrict__ nev_dev,
+                                const long long* __restrict__ ev_start, const long long* __restrict__ ev_key,
                                 const int32_t* __restrict__ ncl, const long long* __restrict__ cl_off,
                                 const long long* __restrict__ mem_off, const ClusterRec* __restrict__ rec,
                                 const int32_t* __restrict__ mem_idx, CrvClusters O, long long cl_cap, CrvMembers M,
                                 long long mem_cap) {
+  nev = bounded_count(nev, nev_dev);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nev; e += (long long)gridDim.x * blockDim.x) {
     long long r0 = ev_start[e];
     for (int k = 0; k < ncl[e]; ++k) {
@@ -946,12 +983,12 @@ extern "C" int64_t crv_coincidences_workspace(int64_t nevents, int64_t npulses) 
   return (int64_t)b;
 }
 
-extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int64_t nevents, const int64_t* ev_start,
-                                const int32_t* ev_count, const int64_t* ev_key, int64_t npulses, const int32_t* bar,
-                                const int32_t* sipm, const int32_t* seq, const double* time, const double* pe,
-                                const int32_t* status, CrvClusters* out, int64_t cl_cap, int64_t* n_cl_dev,
-                                CrvMembers* mem, int64_t mem_cap, int64_t* n_mem_dev, void* workspace,
-                                int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+static int coinc_run(const CrvParams* p, const CrvFinderGeom* g, int64_t nevents, const long long* nev_dev,
+                     const int64_t* ev_start, const int32_t* ev_count, const int64_t* ev_key, int64_t npulses,
+                     const int32_t* bar, const int32_t* sipm, const int32_t* seq, const double* time, const double* pe,
+                     const int32_t* status, CrvClusters* out, int64_t cl_cap, int64_t* n_cl_dev, CrvMembers* mem,
+                     int64_t mem_cap, int64_t* n_mem_dev, void* workspace, int64_t workspace_bytes, void* stream,
+                     CrvStatus* status_dev) {
   if (!p || !g || !out || !mem || !n_cl_dev || !n_mem_dev || !status_dev || nevents < 0 || npulses < 0) return CRV_ERR_ARG;
   if (nevents > 0 && (!ev_start || !ev_count || !ev_key)) return CRV_ERR_ARG;
   if (npulses > 0 && (!bar || !sipm || !seq || !time || !pe || !status)) return CRV_ERR_ARG;
@@ -975,7 +1012,7 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   CK(cudaMemsetAsync(w.deferred, 0, sizeof(int32_t) * nevents, s));
   CoincGeom G;
   memcpy(&G, g, sizeof(G));
-  CoincIn I{nevents, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
+  CoincIn I{nevents, nev_dev, reinterpret_cast<const long long*>(ev_start), ev_count, bar, sipm, seq, time, pe, status};
   CoincOut O{w.rec, w.mem_idx, w.ncl, w.nmem};
   const DeviceInfo& di = device_info();
   // events up to 192 hits (nearly all) at one warp per block (~11 resident warps per SM); the larger ones in a pass
@@ -1000,8 +1037,8 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
     }
     CK(cudaGetLastError());
   }
-  CK(exclusive_scan(w.ncl, nevents, Identity(), w.cl_off, &w.totals[0], w.parts, s));
-  CK(exclusive_scan(w.nmem, nevents, Identity(), w.mem_off, &w.totals[1], w.parts, s));
+  CK(exclusive_scan(w.ncl, nevents, Identity(), w.cl_off, &w.totals[0], w.parts, s, nev_dev));
+  CK(exclusive_scan(w.nmem, nevents, Identity(), w.mem_off, &w.totals[1], w.parts, s, nev_dev));
   {
     crv::Mark mark_("k_check_caps", s);
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[0], cl_cap, CRV_NEED_CLUSTERS, S);
@@ -1012,7 +1049,8 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   }
   {
     crv::Mark mark_("k_coinc_compact", s);
-    k_coinc_compact<<<grid_for(nevents, 256, 8), 256, 0, s>>>(nevents, reinterpret_cast<const long long*>(ev_start),
+    k_coinc_compact<<<grid_for(nevents, 256, 8), 256, 0, s>>>(nevents, nev_dev,
+                                                            reinterpret_cast<const long long*>(ev_start),
                                                             reinterpret_cast<const long long*>(ev_key), w.ncl, w.cl_off,
                                                             w.mem_off, w.rec, w.mem_idx, *out, cl_cap, *mem, mem_cap);
   }
@@ -1028,21 +1066,33 @@ extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int6
   return CRV_OK;
 }
 
+extern "C" int crv_coincidences(const CrvParams* p, const CrvFinderGeom* g, int64_t nevents, const int64_t* ev_start,
+                                const int32_t* ev_count, const int64_t* ev_key, int64_t npulses, const int32_t* bar,
+                                const int32_t* sipm, const int32_t* seq, const double* time, const double* pe,
+                                const int32_t* status, CrvClusters* out, int64_t cl_cap, int64_t* n_cl_dev,
+                                CrvMembers* mem, int64_t mem_cap, int64_t* n_mem_dev, void* workspace,
+                                int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  return coinc_run(p, g, nevents, nullptr, ev_start, ev_count, ev_key, npulses, bar, sipm, seq, time, pe, status, out,
+                   cl_cap, n_cl_dev, mem, mem_cap, n_mem_dev, workspace, workspace_bytes, stream, status_dev);
+}
+
 // ---- reco waveforms and pulse glue ---------------------------------------------------------------------------------
 
 namespace crv {
-__global__ void k_wf_heads(long long nd, const long long* __restrict__ label, const long long* __restrict__ tdc, int zs,
-                           int32_t* __restrict__ head) {
+__global__ void k_wf_heads(long long nd, const long long* __restrict__ nd_dev, const long long* __restrict__ label,
+                           const long long* __restrict__ tdc, int zs, int32_t* __restrict__ head) {
+  nd = bounded_count(nd, nd_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x)
     head[i] = (i == 0 || label[i] != label[i - 1] || tdc[i] != tdc[i - 1] + zs) ? 1 : 0;
 }
 
-__global__ void k_wf_fill(long long nd, const long long* __restrict__ label, const long long* __restrict__ tdc, int zs,
-                          const int32_t* __restrict__ head, const long long* __restrict__ gidx, const long long* n_dev,
-                          CrvChannels ch, long long* __restrict__ w_label, long long* __restrict__ w_off,
-                          int32_t* __restrict__ w_n, long long* __restrict__ w_start, double* __restrict__ w_ped,
-                          double* __restrict__ w_area, double* __restrict__ w_height, double* __restrict__ w_toff) {
-  long long G = *n_dev;
+__global__ void k_wf_fill(long long nd, const long long* __restrict__ nd_dev, const long long* __restrict__ label,
+                          const long long* __restrict__ tdc, int zs, const int32_t* __restrict__ head,
+                          const long long* __restrict__ gidx, CrvChannels ch, long long* __restrict__ w_label,
+                          long long* __restrict__ w_off, int32_t* __restrict__ w_n, long long* __restrict__ w_start,
+                          double* __restrict__ w_ped, double* __restrict__ w_area, double* __restrict__ w_height,
+                          double* __restrict__ w_toff) {
+  nd = bounded_count(nd, nd_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nd; i += (long long)gridDim.x * blockDim.x) {
     if (!head[i]) continue;
     long long g = gidx[i];
@@ -1057,12 +1107,13 @@ __global__ void k_wf_fill(long long nd, const long long* __restrict__ label, con
     w_area[g] = ch.pulsearea[c];
     w_height[g] = ch.pulseheight[c];
     w_toff[g] = ch.timeoffset[c];
-    (void)G;
   }
 }
 
 __global__ void k_hit_keep(const CrvParams p, const int32_t* __restrict__ status, const long long* __restrict__ w_label,
-                           long long np, const long long* __restrict__ p_wf, int32_t* __restrict__ keep) {
+                           long long np, const long long* __restrict__ np_dev, const long long* __restrict__ p_wf,
+                           int32_t* __restrict__ keep) {
+  np = bounded_count(np, np_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
     int c = int(w_label[p_wf[i]] % 32768);
     keep[i] = (p.ignore_channels && (status[c] & 0b010)) ? 0 : 1;
@@ -1070,12 +1121,13 @@ __global__ void k_hit_keep(const CrvParams p, const int32_t* __restrict__ status
 }
 
 __global__ void k_hit_fill(const CrvParams p, const long long* __restrict__ w_label, const double* __restrict__ w_toff,
-                           const double* __restrict__ event_t0, long long np, const long long* __restrict__ p_wf,
-                           const long long* __restrict__ p_seq, const double* __restrict__ p_time,
-                           const double* __restrict__ p_pe, const int32_t* __restrict__ keep,
-                           const long long* __restrict__ kidx, int32_t* __restrict__ bar, int32_t* __restrict__ sipm,
-                           int32_t* __restrict__ seq, double* __restrict__ time, double* __restrict__ pe,
-                           long long* __restrict__ hev) {
+                           const double* __restrict__ event_t0, long long np, const long long* __restrict__ np_dev,
+                           const long long* __restrict__ p_wf, const long long* __restrict__ p_seq,
+                           const double* __restrict__ p_time, const double* __restrict__ p_pe,
+                           const int32_t* __restrict__ keep, const long long* __restrict__ kidx,
+                           int32_t* __restrict__ bar, int32_t* __restrict__ sipm, int32_t* __restrict__ seq,
+                           double* __restrict__ time, double* __restrict__ pe, long long* __restrict__ hev) {
+  np = bounded_count(np, np_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += (long long)gridDim.x * blockDim.x) {
     if (!keep[i]) continue;
     long long k = kidx[i];
@@ -1128,11 +1180,11 @@ extern "C" int64_t crv_reco_waveforms_workspace(int64_t nd) {
   return (int64_t)(c.off + 256);
 }
 
-extern "C" int crv_reco_waveforms(const CrvParams* p, const CrvChannels* ch, int64_t nd, const int64_t* label,
-                                  const int64_t* starttdc, int64_t* w_label, int64_t* w_off, int32_t* w_n,
-                                  int64_t* w_start, double* w_ped, double* w_area, double* w_height, double* w_toff,
-                                  int64_t* n_w_dev, void* workspace, int64_t workspace_bytes, void* stream,
-                                  CrvStatus* status_dev) {
+static int reco_waveforms_run(const CrvParams* p, const CrvChannels* ch, int64_t nd, const long long* nd_dev,
+                              const int64_t* label, const int64_t* starttdc, int64_t* w_label, int64_t* w_off,
+                              int32_t* w_n, int64_t* w_start, double* w_ped, double* w_area, double* w_height,
+                              double* w_toff, int64_t* n_w_dev, void* workspace, int64_t workspace_bytes, void* stream,
+                              CrvStatus* status_dev) {
   if (!p || !ch || !n_w_dev || !status_dev || nd < 0) return CRV_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (nd == 0) {
@@ -1151,12 +1203,12 @@ extern "C" int crv_reco_waveforms(const CrvParams* p, const CrvChannels* ch, int
   unsigned g = grid_for(nd, 256, 8);
   {
     crv::Mark mark_("k_wf_heads", s);
-    k_wf_heads<<<g, 256, 0, s>>>(nd, lab, tdc, p->samples_zs, head);
+    k_wf_heads<<<g, 256, 0, s>>>(nd, nd_dev, lab, tdc, p->samples_zs, head);
   }
-  CK(exclusive_scan(head, nd, Identity(), gidx, &totals[0], parts, s));
+  CK(exclusive_scan(head, nd, Identity(), gidx, &totals[0], parts, s, nd_dev));
   {
     crv::Mark mark_("k_wf_fill", s);
-    k_wf_fill<<<g, 256, 0, s>>>(nd, lab, tdc, p->samples_zs, head, gidx, &totals[0], *ch,
+    k_wf_fill<<<g, 256, 0, s>>>(nd, nd_dev, lab, tdc, p->samples_zs, head, gidx, *ch,
                                 reinterpret_cast<long long*>(w_label), reinterpret_cast<long long*>(w_off), w_n,
                                 reinterpret_cast<long long*>(w_start), w_ped, w_area, w_height, w_toff);
   }
@@ -1166,6 +1218,15 @@ extern "C" int crv_reco_waveforms(const CrvParams* p, const CrvChannels* ch, int
   }
   CK(cudaGetLastError());
   return CRV_OK;
+}
+
+extern "C" int crv_reco_waveforms(const CrvParams* p, const CrvChannels* ch, int64_t nd, const int64_t* label,
+                                  const int64_t* starttdc, int64_t* w_label, int64_t* w_off, int32_t* w_n,
+                                  int64_t* w_start, double* w_ped, double* w_area, double* w_height, double* w_toff,
+                                  int64_t* n_w_dev, void* workspace, int64_t workspace_bytes, void* stream,
+                                  CrvStatus* status_dev) {
+  return reco_waveforms_run(p, ch, nd, nullptr, label, starttdc, w_label, w_off, w_n, w_start, w_ped, w_area, w_height,
+                            w_toff, n_w_dev, workspace, workspace_bytes, stream, status_dev);
 }
 
 extern "C" int64_t crv_pulse_hits_workspace(int64_t np) {
@@ -1181,12 +1242,12 @@ extern "C" int64_t crv_pulse_hits_workspace(int64_t np) {
   return (int64_t)(c.off + 256);
 }
 
-extern "C" int crv_pulse_hits(const CrvParams* p, const int32_t* status, int64_t nw, const int64_t* w_label,
-                              const double* w_toff, const double* event_t0, int64_t np, const int64_t* p_wf,
-                              const int64_t* p_seq, const double* p_time, const double* p_pe, int64_t* ev_start,
-                              int32_t* ev_count, int64_t* ev_key, int32_t* bar, int32_t* sipm, int32_t* seq,
-                              double* time, double* pe, int64_t* n_ev_dev, int64_t* n_hit_dev, void* workspace,
-                              int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+static int pulse_hits_run(const CrvParams* p, const int32_t* status, int64_t nw, const int64_t* w_label,
+                          const double* w_toff, const double* event_t0, int64_t np, const long long* np_dev,
+                          const int64_t* p_wf, const int64_t* p_seq, const double* p_time, const double* p_pe,
+                          int64_t* ev_start, int32_t* ev_count, int64_t* ev_key, int32_t* bar, int32_t* sipm,
+                          int32_t* seq, double* time, double* pe, int64_t* n_ev_dev, int64_t* n_hit_dev,
+                          void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
   if (!p || !status || !n_ev_dev || !n_hit_dev || !status_dev || np < 0 || nw < 0) return CRV_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (np == 0) {
@@ -1208,12 +1269,12 @@ extern "C" int crv_pulse_hits(const CrvParams* p, const int32_t* status, int64_t
   const long long* wl = reinterpret_cast<const long long*>(w_label);
   {
     crv::Mark mark_("k_hit_keep", s);
-    k_hit_keep<<<g, 256, 0, s>>>(*p, status, wl, np, reinterpret_cast<const long long*>(p_wf), keep);
+    k_hit_keep<<<g, 256, 0, s>>>(*p, status, wl, np, np_dev, reinterpret_cast<const long long*>(p_wf), keep);
   }
-  CK(exclusive_scan(keep, np, Identity(), kidx, &totals[0], parts, s));
+  CK(exclusive_scan(keep, np, Identity(), kidx, &totals[0], parts, s, np_dev));
   {
     crv::Mark mark_("k_hit_fill", s);
-    k_hit_fill<<<g, 256, 0, s>>>(*p, wl, w_toff, event_t0, np, reinterpret_cast<const long long*>(p_wf),
+    k_hit_fill<<<g, 256, 0, s>>>(*p, wl, w_toff, event_t0, np, np_dev, reinterpret_cast<const long long*>(p_wf),
                                  reinterpret_cast<const long long*>(p_seq), p_time, p_pe, keep, kidx, bar, sipm, seq,
                                  time, pe, hev);
   }
@@ -1238,5 +1299,186 @@ extern "C" int crv_pulse_hits(const CrvParams* p, const int32_t* status, int64_t
     k_copy_i64<<<1, 1, 0, s>>>(&totals[0], reinterpret_cast<long long*>(n_hit_dev));
   }
   CK(cudaGetLastError());
+  return CRV_OK;
+}
+
+extern "C" int crv_pulse_hits(const CrvParams* p, const int32_t* status, int64_t nw, const int64_t* w_label,
+                              const double* w_toff, const double* event_t0, int64_t np, const int64_t* p_wf,
+                              const int64_t* p_seq, const double* p_time, const double* p_pe, int64_t* ev_start,
+                              int32_t* ev_count, int64_t* ev_key, int32_t* bar, int32_t* sipm, int32_t* seq,
+                              double* time, double* pe, int64_t* n_ev_dev, int64_t* n_hit_dev, void* workspace,
+                              int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  return pulse_hits_run(p, status, nw, w_label, w_toff, event_t0, np, nullptr, p_wf, p_seq, p_time, p_pe, ev_start,
+                        ev_count, ev_key, bar, sipm, seq, time, pe, n_ev_dev, n_hit_dev, workspace, workspace_bytes,
+                        stream, status_dev);
+}
+
+// ---- the resident chain: steps -> clusters in one call with fixed capacities ----------------------------------------
+
+namespace crv {
+struct ChainWs {
+  long long* counts;             // 0-9 raw stage counts (CRV_CHAIN_*), 16-25 the counts passed downstream
+  CrvCharges Q;
+  CrvDigis D;
+  int64_t *w_label, *w_off, *w_start;
+  int32_t* w_n;
+  double *w_ped, *w_area, *w_height, *w_toff;
+  CrvPulses P;
+  uint8_t* near;
+  int64_t *h_ev_start, *h_ev_key;
+  int32_t *h_ev_count, *h_bar, *h_sipm, *h_seq;
+  double *h_time, *h_pe;
+  char* scratch;
+  long long scratch_bytes;
+};
+
+static long long chain_scratch_bytes(const CrvParams& p, const CrvChainCaps& c) {
+  long long zs = p.samples_zs;
+  long long b = 0;
+  auto up = [&](long long v) { if (v > b) b = v; };
+  size_t r = 0;
+  resp_layout(nullptr, p, c.events, c.steps, c.photons, &r);
+  up((long long)r);
+  digi_layout(nullptr, c.charges, c.slots, p.samples_zs, &r);
+  up((long long)r);
+  up(crv_reco_waveforms_workspace(c.digis));
+  pulse_layout(nullptr, c.digis, c.digis * zs, &r);
+  up((long long)r);
+  up(crv_pulse_hits_workspace(c.pulses));
+  coinc_layout(nullptr, c.events, c.pulses, &r);
+  up((long long)r);
+  return b;
+}
+
+static ChainWs chain_layout(char* base, const CrvParams& p, const CrvChainCaps& c, size_t* bytes) {
+  Carve k{base};
+  ChainWs w;
+  const long long zs = p.samples_zs, nq = c.charges, nd = c.digis, np = c.pulses, ne = c.events;
+  w.counts = k.take<long long>(32);
+  w.Q.label = k.take<int64_t>(nq);
+  w.Q.time = k.take<double>(nq);
+  w.Q.charge = k.take<double>(nq);
+  w.Q.pe = k.take<double>(nq);
+  w.Q.photon = k.take<int64_t>(nq);
+  w.D.chan = k.take<int64_t>(nd);
+  w.D.start = k.take<double>(nd);
+  w.D.tdc0 = k.take<double>(nd);
+  w.D.starttdc = k.take<int64_t>(nd);
+  w.D.volt = k.take<double>(nd * zs);
+  w.D.adc = k.take<int16_t>(nd * zs);
+  w.w_label = k.take<int64_t>(nd);
+  w.w_off = k.take<int64_t>(nd);
+  w.w_start = k.take<int64_t>(nd);
+  w.w_n = k.take<int32_t>(nd);
+  w.w_ped = k.take<double>(nd);
+  w.w_area = k.take<double>(nd);
+  w.w_height = k.take<double>(nd);
+  w.w_toff = k.take<double>(nd);
+  int64_t** pi[2] = {&w.P.wf, &w.P.seq};
+  for (auto q : pi) *q = k.take<int64_t>(np);
+  double** pf[11] = {&w.P.pe, &w.P.peph, &w.P.time, &w.P.height, &w.P.beta, &w.P.chi2, &w.P.letime, &w.P.ped,
+                     &w.P.fit_A, &w.P.fit_mu, &w.P.fit_b};
+  for (auto q : pf) *q = k.take<double>(np);
+  uint8_t** pb[3] = {&w.P.failed, &w.P.zerondf, &w.P.pedfromdb};
+  for (auto q : pb) *q = k.take<uint8_t>(np);
+  w.near = k.take<uint8_t>(nd);
+  w.h_ev_start = k.take<int64_t>(ne);
+  w.h_ev_key = k.take<int64_t>(ne);
+  w.h_ev_count = k.take<int32_t>(ne);
+  w.h_bar = k.take<int32_t>(np);
+  w.h_sipm = k.take<int32_t>(np);
+  w.h_seq = k.take<int32_t>(np);
+  w.h_time = k.take<double>(np);
+  w.h_pe = k.take<double>(np);
+  w.scratch_bytes = chain_scratch_bytes(p, c);
+  w.scratch = k.take<char>(w.scratch_bytes);
+  *bytes = k.off + 256;
+  return w;
+}
+
+static bool chain_caps_ok(const CrvParams* p, const CrvChainCaps* c) {
+  return p && c && c->events > 0 && c->steps > 0 && c->photons > 0 && c->charges > 0 && c->slots > 0 &&
+         c->digis > 0 && c->pulses > 0 && c->max_steps_per_event > 0 && p->samples_zs > 0 && p->samples_zs <= 32;
+}
+}  // namespace crv
+
+extern "C" int64_t crv_chain_workspace(const CrvParams* p, const CrvChainCaps* caps) {
+  if (!chain_caps_ok(p, caps)) return -1;
+  size_t b = 0;
+  chain_layout(nullptr, *p, *caps, &b);
+  return (int64_t)b;
+}
+
+extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev, const int64_t* ev_keys,
+                         const uint32_t* ev_runs, const CrvSteps* st, const int64_t* nsteps_dev, const CrvBars* bars,
+                         const CrvChannels* ch, const CrvPixels* px, const double* tmpl, int32_t tlen,
+                         const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem, int64_t* counts_dev,
+                         void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!chain_caps_ok(p, caps) || !ev || !ev_keys || !ev_runs || !st || !nsteps_dev || !bars || !ch || !px || !tmpl ||
+      tlen <= 0 || !g || !out || !mem || !counts_dev || !status_dev)
+    return CRV_ERR_ARG;
+  size_t need = 0;
+  chain_layout(nullptr, *p, *caps, &need);
+  if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t dummy;
+  ChainWs w = chain_layout(base, *p, *caps, &dummy);
+  const CrvChainCaps& c = *caps;
+  long long* n = w.counts;                 // raw counts
+  long long* m = w.counts + 16;            // counts passed on: 0 when the stage overflowed its capacity
+  const long long zs = p->samples_zs;
+  CK(cudaMemsetAsync(w.counts, 0, 32 * sizeof(long long), s));
+  // the stage totals that size the photon and slot capacities, from the stage workspaces (scratch is 256-aligned)
+  auto keep_total = [&](const long long* total, int k) -> cudaError_t {
+    crv::Mark mark_("k_copy_i64", s);
+    k_copy_i64<<<1, 1, 0, s>>>(total, &n[k]);
+    return cudaGetLastError();
+  };
+  auto N = [&](int k) { return reinterpret_cast<int64_t*>(&n[k]); };
+  auto guard = [&](int k, long long cap) -> cudaError_t {
+    crv::Mark mark_("k_guard_groups", s);
+    k_guard_groups<<<1, 32, 0, s>>>(&n[k], cap, &n[k], &m[k]);
+    return cudaGetLastError();
+  };
+  int rc = response_run(p, ev, c.events, st, c.steps, reinterpret_cast<const long long*>(nsteps_dev),
+                        c.max_steps_per_event, bars, ch, px, c.photons, &w.Q, c.charges, N(CRV_CHAIN_CHARGES),
+                        nullptr, nullptr, nullptr, 0, nullptr, w.scratch, w.scratch_bytes, stream, status_dev);
+  if (rc != CRV_OK) return rc;
+  {
+    size_t b;
+    CK(keep_total(&resp_layout(w.scratch, *p, c.events, c.steps, c.photons, &b).totals[1], CRV_CHAIN_PHOTONS));
+  }
+  CK(guard(CRV_CHAIN_CHARGES, c.charges));
+  rc = digis_run(p, ch, c.charges, &m[CRV_CHAIN_CHARGES], w.Q.label, w.Q.time, w.Q.charge, tmpl, tlen, ev_keys,
+                 ev_runs, c.events, c.slots, &w.D, c.digis, N(CRV_CHAIN_DIGIS), w.scratch, w.scratch_bytes, stream,
+                 status_dev);
+  if (rc != CRV_OK) return rc;
+  {
+    size_t b;
+    CK(keep_total(&digi_layout(w.scratch, c.charges, c.slots, p->samples_zs, &b).totals[1], CRV_CHAIN_SLOTS));
+  }
+  CK(guard(CRV_CHAIN_DIGIS, c.digis));
+  rc = reco_waveforms_run(p, ch, c.digis, &m[CRV_CHAIN_DIGIS], w.D.chan, w.D.starttdc, w.w_label, w.w_off, w.w_n,
+                          w.w_start, w.w_ped, w.w_area, w.w_height, w.w_toff, N(CRV_CHAIN_WAVEFORMS), w.scratch,
+                          w.scratch_bytes, stream, status_dev);
+  if (rc != CRV_OK) return rc;
+  CK(guard(CRV_CHAIN_WAVEFORMS, c.digis));
+  rc = pulses_run(p, c.digis, &m[CRV_CHAIN_WAVEFORMS], c.digis * zs, w.w_off, w.w_n, w.w_start, w.w_ped, w.w_area,
+                  w.w_height, w.D.adc, nullptr, 0x7FFFFFFF, &w.P, c.pulses, N(CRV_CHAIN_PULSES), w.near, w.scratch,
+                  w.scratch_bytes, stream, status_dev);
+  if (rc != CRV_OK) return rc;
+  CK(guard(CRV_CHAIN_PULSES, c.pulses));
+  rc = pulse_hits_run(p, ch->status, c.digis, w.w_label, w.w_toff, nullptr, c.pulses, &m[CRV_CHAIN_PULSES], w.P.wf,
+                      w.P.seq, w.P.time, w.P.pe, w.h_ev_start, w.h_ev_count, w.h_ev_key, w.h_bar, w.h_sipm, w.h_seq,
+                      w.h_time, w.h_pe, N(CRV_CHAIN_EVENTS), N(CRV_CHAIN_HITS), w.scratch, w.scratch_bytes, stream,
+                      status_dev);
+  if (rc != CRV_OK) return rc;
+  CK(guard(CRV_CHAIN_EVENTS, c.events));
+  rc = coinc_run(p, g, c.events, &m[CRV_CHAIN_EVENTS], w.h_ev_start, w.h_ev_count, w.h_ev_key, c.pulses, w.h_bar,
+                 w.h_sipm, w.h_seq, w.h_time, w.h_pe, ch->status, out, c.pulses, N(CRV_CHAIN_CLUSTERS), mem, c.pulses,
+                 N(CRV_CHAIN_MEMBERS), w.scratch, w.scratch_bytes, stream, status_dev);
+  if (rc != CRV_OK) return rc;
+  CK(cudaMemcpyAsync(counts_dev, n, 10 * sizeof(long long), cudaMemcpyDeviceToDevice, s));
   return CRV_OK;
 }

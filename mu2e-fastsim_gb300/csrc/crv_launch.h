@@ -43,8 +43,9 @@ struct Mark {
 
 template <typename R>
 cudaError_t launch_photon_count(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,
-                                const CrvChannels& ch, const int32_t* step_event, long long nsteps, int masked,
-                                int32_t* count, Status* status, cudaStream_t s);
+                                const CrvChannels& ch, const int32_t* step_event, long long nsteps,
+                                const long long* nsteps_dev, int masked, int32_t* count, Status* status,
+                                cudaStream_t s);
 
 template <typename R>
 cudaError_t launch_photon_emit(const CrvParams& p, const CrvEvents& ev, const CrvSteps& st, const CrvBars& bars,

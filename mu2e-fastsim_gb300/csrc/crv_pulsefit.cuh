@@ -27,7 +27,8 @@ struct PulseRec {            // one reconstructed pulse (shared-memory staging)
 };
 
 struct WaveIn {
-  long long nw;              // waveforms
+  long long nw;              // waveforms (an upper bound when nw_dev is set)
+  const long long* nw_dev;   // device count of waveforms, or null
   const long long* off;      // first sample of waveform w in the sample array
   const int32_t* n;          // valid samples
   const long long* start_tdc;
@@ -759,11 +760,12 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_pf_begin(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
                                                  PulseSlots S, PfQueue Q, Status* status) {
   const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; base < W.nw;
+  const long long nw = bounded_count(W.nw, W.nw_dev);
+  for (long long base = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; base < nw;
        base += nwarps * 32) {
     const long long w = base + lane_id();
     bool pend = false;
-    if (w < W.nw) {
+    if (w < nw) {
       PfState st;
       pend = pf_begin<R>(p, W, yscr, max_pulses, w, st);
       if (pend) Q.st[w] = st;

@@ -192,8 +192,10 @@ __device__ __forceinline__ int draw_count(R avg, const U4& w) {
 // count[4 * i + s]: photons of step i on SiPM s (masked channels 0 when `masked`)
 template <typename R>
 __global__ void k_photon_count(CrvParams p, CrvEvents ev, CrvSteps st, CrvBars bars, CrvChannels ch,
-                               const int32_t* __restrict__ step_event, long long nsteps, int masked,
-                               int32_t* __restrict__ count, Status* status) {
+                               const int32_t* __restrict__ step_event, long long nsteps,
+                               const long long* __restrict__ nsteps_dev, int masked, int32_t* __restrict__ count,
+                               Status* status) {
+  nsteps = bounded_count(nsteps, nsteps_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nsteps;
        i += (long long)gridDim.x * blockDim.x) {
     int e = step_event[i];

@@ -12,11 +12,7 @@ constexpr int SCAN_ITEMS = 8;                        // items per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 // effective length: the host bound n, or the device count *n_dev when it is smaller (arrays sized by an upper bound)
-__device__ __forceinline__ long long scan_len(long long n, const long long* n_dev) {
-  if (!n_dev) return n;
-  long long m = *n_dev;
-  return m < n ? m : n;
-}
+__device__ __forceinline__ long long scan_len(long long n, const long long* n_dev) { return bounded_count(n, n_dev); }
 
 template <typename T, typename F>
 __global__ void k_scan_reduce(const T* __restrict__ in, long long n, const long long* __restrict__ n_dev, F f,

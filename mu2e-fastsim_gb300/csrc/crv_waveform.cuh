@@ -498,14 +498,17 @@ __global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D
 }
 
 // Segments of equal labels in a label-sorted array: heads, then group start/label/count.
-__global__ void k_label_heads(long long n, const long long* __restrict__ label, int32_t* __restrict__ head) {
+__global__ void k_label_heads(long long n, const long long* __restrict__ n_dev, const long long* __restrict__ label,
+                              int32_t* __restrict__ head) {
+  n = bounded_count(n, n_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     head[i] = (i == 0 || label[i] != label[i - 1]) ? 1 : 0;
 }
 
-__global__ void k_label_groups(long long n, const long long* __restrict__ label, const int32_t* __restrict__ head,
-                               const long long* __restrict__ gidx, long long* __restrict__ gstart,
-                               long long* __restrict__ glabel) {
+__global__ void k_label_groups(long long n, const long long* __restrict__ n_dev, const long long* __restrict__ label,
+                               const int32_t* __restrict__ head, const long long* __restrict__ gidx,
+                               long long* __restrict__ gstart, long long* __restrict__ glabel) {
+  n = bounded_count(n, n_dev);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     if (head[i]) {
       long long g = gidx[i];
@@ -515,11 +518,13 @@ __global__ void k_label_groups(long long n, const long long* __restrict__ label,
 }
 
 // counts from consecutive starts; run per group from a sorted (event key -> run) table (run 0 if absent)
-__global__ void k_group_counts(const long long* __restrict__ ng_dev, long long n, const long long* __restrict__ gstart,
-                               const long long* __restrict__ glabel, int32_t* __restrict__ gcount,
-                               const long long* __restrict__ ev_keys, const uint32_t* __restrict__ ev_runs,
-                               long long n_ev, uint32_t* __restrict__ grun, Status* status) {
+__global__ void k_group_counts(const long long* __restrict__ ng_dev, long long n, const long long* __restrict__ n_dev,
+                               const long long* __restrict__ gstart, const long long* __restrict__ glabel,
+                               int32_t* __restrict__ gcount, const long long* __restrict__ ev_keys,
+                               const uint32_t* __restrict__ ev_runs, long long n_ev, uint32_t* __restrict__ grun,
+                               Status* status) {
   long long ng = *ng_dev;
+  n = bounded_count(n, n_dev);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
     long long e = (g + 1 < ng ? gstart[g + 1] : n) - gstart[g];
     gcount[g] = int32_t(e);

@@ -1,0 +1,112 @@
+"""The resident chain (one crv_chain call per batch, replayed as a CUDA graph) gives the same clusters, bit for bit, as
+the per-stage ChainEngine on the same steps and seed; batches of other sizes replay the same graph; a batch that
+overflows a capacity is rejected with the sizes it needed, and with growth enabled it is re-run to the same result."""
+import numpy as np
+import pytest
+
+from tests.helpers import workload
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    from crvgpu import chain as CH
+    from crvgpu.config import ChainConfig
+    from crvgpu.response import upload_steps
+    from dataclasses import replace
+    geom, cond, cfg, steps = workload(600, seed=31)
+    cond.status[[5, 41, 90]] = [2, 1, 4]
+    cfg32 = replace(cfg, precision="fp32")
+    ds = upload_steps(steps, nbars=geom.nbars)
+    assert isinstance(cfg32, ChainConfig)
+    return geom, cond, cfg32, ds, CH
+
+
+def _trial_caps(eng, ds):
+    """Capacities from a trial batch run with ample capacities."""
+    from crvgpu.resident import ChainCaps, ResidentChain
+    big = ChainCaps(events=ds.nevents, steps=ds.nsteps, photons=400 * ds.nsteps + 4096, charges=200 * ds.nsteps + 4096,
+                    slots=100 * ds.nsteps + 4096, digis=100 * ds.nsteps + 4096, pulses=100 * ds.nsteps + 4096,
+                    max_steps_per_event=max(1, ds.max_steps))
+    rc = ResidentChain(eng, big, graph=False)
+    rc.run(ds, 7)
+    return ChainCaps.from_counts(rc.last_counts, ds.nevents, ds.nsteps, ds.max_steps, margin=1.3)
+
+
+def _same(res, ref):
+    import torch
+    assert res.counts["clusters"] == ref.n_clusters and res.counts["members"] == ref.n_members
+    for k, v in ref.clusters.items():
+        assert torch.equal(res.clusters[k], v), k
+    for k, v in ref.members.items():
+        assert torch.equal(res.members[k], v), k
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_resident_chain_matches_the_stage_engine(setup, graph):
+    geom, cond, cfg, ds, CH = setup
+    from crvgpu.resident import ResidentChain
+    eng = CH.ChainEngine(geom, cond, cfg)
+    ref = eng.run(ds, 2024)
+    rc = ResidentChain(eng, _trial_caps(eng, ds), graph=graph)
+    res = rc.run(ds, 2024)
+    assert ref.n_clusters > 0
+    c = res.counts
+    assert (c["charges"], c["digis"], c["waveforms"], c["pulses"], c["hits"]) == \
+        (ref.n_charges, ref.n_digis, ref.n_waveforms, ref.n_pulses, ref.n_hits)
+    _same(res, ref)
+    assert rc.launches_per_run > 20
+    # a second batch through the same graph (replay) and another seed (captured again)
+    _same(rc.run(ds, 2024), ref)
+    _same(rc.run(ds, 99), eng.run(ds, 99))
+
+
+def test_smaller_batches_replay_the_same_graph(setup):
+    geom, cond, cfg, ds, CH = setup
+    from crvgpu.resident import ResidentChain
+    from crvgpu.serve import slice_events
+    eng = CH.ChainEngine(geom, cond, cfg)
+    rc = ResidentChain(eng, _trial_caps(eng, ds), graph=True)
+    rc.run(ds, 5)
+    g = rc._graph
+    for a, b in ((0, 250), (250, 600), (100, 101), (37, 400)):
+        part = slice_events(ds, a, b)
+        _same(rc.run(part, 5), eng.run(part, 5))
+    assert rc._graph is g                                       # no capture after the first batch
+
+
+def test_capacity_overflow_rejects_the_batch_and_growth_recovers(setup):
+    geom, cond, cfg, ds, CH = setup
+    from dataclasses import replace
+    from crvgpu import _capi
+    from crvgpu.resident import BatchRejected, ResidentChain
+    eng = CH.ChainEngine(geom, cond, cfg)
+    ref = eng.run(ds, 3)
+    caps = _trial_caps(eng, ds)
+    for field, need in (("pulses", "PULSES_OUT"), ("digis", "DIGIS_OUT"), ("charges", "CHARGES_OUT"),
+                        ("photons", "PHOTONS_TOTAL"), ("slots", "DIGIS")):
+        small = replace(caps, **{field: 64})
+        rc = ResidentChain(eng, small, graph=True)
+        with pytest.raises(BatchRejected) as ei:
+            rc.run(ds, 3)
+        assert ei.value.flags == _capi.ST_CAPACITY
+        assert ei.value.need[_capi.NEED[need]] > 64, field
+        grown = ResidentChain(eng, small, graph=True, grow=True)
+        _same(grown.run(ds, 3), ref)
+        assert getattr(grown.caps, field) > 64
+    # more steps per event than the capacity: rejected on the host before any launch
+    rc = ResidentChain(eng, replace(caps, max_steps_per_event=1), graph=True)
+    with pytest.raises(ValueError):
+        rc.run(ds, 3)
+
+
+def test_fp64_resident_chain_matches(setup):
+    geom, cond, cfg, ds, CH = setup
+    from dataclasses import replace
+    from crvgpu.resident import ResidentChain
+    from crvgpu.serve import slice_events
+    eng = CH.ChainEngine(geom, cond, replace(cfg, precision="fp64"))
+    part = slice_events(ds, 0, 200)
+    rc = ResidentChain(eng, _trial_caps(eng, part), graph=True)
+    _same(rc.run(part, 11), eng.run(part, 11))
