@@ -263,7 +263,7 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
     return out
 
 
-def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=2048):
+def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=2048, resident=True):
     """Serving loop over a resident step pool: isolated run time model, saturated capacity, then Poisson arrivals at
     `load` of capacity (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
     import torch
@@ -272,7 +272,8 @@ def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=20
     from crvgpu.serve import Job, ServeEngine, latency_stats, random_jobs
     pool = upload_steps(GM.synthetic_steps(pool_events, geom, seed=77), nbars=geom.nbars)
     free, _ = torch.cuda.mem_get_info()
-    srv = ServeEngine(geom, cond, pool, hbm_budget=int(0.6 * free), max_slots=max_slots, chunk_events=chunk)
+    srv = ServeEngine(geom, cond, pool, hbm_budget=int(0.6 * free), max_slots=max_slots, chunk_events=chunk,
+                      resident=resident)
     # isolated run time: alone on an idle device, a small and a large job
     iso = []
     for n in (4096, min(131072, pool_events)):
@@ -290,10 +291,15 @@ def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=20
     jobs = random_jobs(n_jobs, np.random.default_rng(seed + 1), max_events=pool_events, pool_events=pool_events,
                        rate=load * cap / mean_ev)
     st = latency_stats(srv.run(jobs, realtime=True), rate, overhead)
+    st_edf = latency_stats(srv.run(jobs, realtime=True, policy="edf", iso_rate=rate, iso_overhead=overhead), rate,
+                           overhead)
     return {"jobs": n_jobs, "slots": len(srv.slots), "slot_footprint_gb": srv.footprint / 1e9,
+            "slot_engine": "resident chain (one host read per chunk)" if resident else "per-stage chain",
             "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",
             "isolated_events_per_s": rate, "isolated_overhead_s": overhead, "capacity_events_per_s": cap,
-            "offered_load": load, **{k: v for k, v in st.items() if k != "jobs"}}
+            "offered_load": load, "policy": "srpt", **{k: v for k, v in st.items() if k != "jobs"},
+            "edf": {"policy": "earliest deadline, arrival + 2 x isolated time",
+                    **{k: v for k, v in st_edf.items() if k != "jobs"}}}
 
 
 def fullscale(n_events, batch, seed=13):
@@ -460,21 +466,28 @@ def main():
     # batch (batches that need more grow them during the warm-up)
     from crvgpu.resident import ChainCaps, ResidentChain, caps_for
     from crvgpu.serve import slice_events
-    sample = slice_events(batches[0], 0, min(8192, batches[0].nevents))
-    trial = ResidentChain(eng32, caps_for(eng32, [sample]), graph=False, grow=True, max_grow=8)
-    trial.run(sample, 5)
-    scale = max(b.nevents for b in batches) / sample.nevents
-    res_caps = ChainCaps.from_counts({k: v * scale for k, v in trial.last_counts.items()},
-                                     events=max(b.nevents for b in batches), steps=max(b.nsteps for b in batches),
-                                     max_steps_per_event=max(b.max_steps for b in batches), margin=1.1)
-    trial = None
-    torch.cuda.empty_cache()
-    rchain = ResidentChain(eng32, res_caps, graph=True, grow=True)
-    ms32, tot32, clk, launches = timed(rchain, args.steps, args.warmup, pass_fn=resident_pass)
+    try:
+        sample = slice_events(batches[0], 0, min(8192, batches[0].nevents))
+        trial = ResidentChain(eng32, caps_for(eng32, [sample]), graph=False, grow=True, max_grow=8)
+        trial.run(sample, 5)
+        scale = max(b.nevents for b in batches) / sample.nevents
+        res_caps = ChainCaps.from_counts({k: v * scale for k, v in trial.last_counts.items()},
+                                         events=max(b.nevents for b in batches), steps=max(b.nsteps for b in batches),
+                                         max_steps_per_event=max(b.max_steps for b in batches), margin=1.1)
+        trial = None
+        torch.cuda.empty_cache()
+        rchain = ResidentChain(eng32, res_caps, graph=True, grow=True)
+        ms32, tot32, clk, launches = timed(rchain, args.steps, args.warmup, pass_fn=resident_pass)
+        resident = {"engine": "resident (graph replay per batch)", "caps": rchain.caps.as_dict(),
+                    "launches_per_batch": rchain.launches_per_run, "device_bytes": rchain.nbytes,
+                    "clusters_per_pass": tot32["clusters"], "stage_engine_clusters_per_pass": tot_st["clusters"]}
+    except Exception as exc:          # the line then carries the per-stage engine's figures, and says so
+        trial = rchain = None
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        ms32, tot32, clk, launches = ms_st, tot_st, clk_st, launches_st
+        resident = {"engine": "per-stage (the resident engine failed)", "error": str(exc)[:300]}
     value = ev_total / (ms32 / 1000.0)
-    resident = {"caps": rchain.caps.as_dict(), "launches_per_batch": rchain.launches_per_run,
-                "device_bytes": rchain.nbytes, "clusters_per_pass": tot32["clusters"],
-                "stage_engine_clusters_per_pass": tot_st["clusters"]}
 
     # e2e: step tables in pinned host memory -> device (asynchronous copies on a second stream, the next batch while
     # the current one computes) -> chain -> cluster table back to the host, one pass
@@ -498,7 +511,7 @@ def main():
             h2d += pinned[i].nbytes
             if i + 1 < len(pinned):
                 nxt = prefetch(i + 1)
-            r_ = rchain.run(cur, 5, copy=False)
+            r_ = rchain.run(cur, 5, copy=False) if rchain is not None else eng32.run(cur, 5)
             host_cl = {k: v.cpu().numpy() for k, v in r_.clusters.items()}
             d2h += sum(a.nbytes for a in host_cl.values())
         return h2d, d2h

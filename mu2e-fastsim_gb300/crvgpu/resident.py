@@ -18,6 +18,7 @@ on the same data, only the sizes come from the device.
 from __future__ import annotations
 
 import ctypes
+import threading
 from dataclasses import dataclass, fields, replace
 
 import numpy as np
@@ -26,6 +27,10 @@ from . import _capi
 from .response import DeviceSteps, EngineError, _stream, _torch
 
 INT64_MAX = (1 << 63) - 1
+
+# one stream capture at a time in the process: entering a capture synchronises the device, which another thread's
+# capture in progress does not permit
+_CAPTURE_LOCK = threading.Lock()
 
 
 @dataclass(frozen=True)
@@ -122,7 +127,9 @@ class ResidentResult:
 
 class ResidentChain:
     """Steps -> clusters on one device with explicit capacities; graph=True replays one captured CUDA graph per batch
-    (captured on the first batch of a seed; again after configure or a capacity change)."""
+    (captured on the first batch of a seed; again after configure or a capacity change).  Graph mode wants one host
+    thread issuing CUDA work in the process while it captures: CUDA work from other threads meanwhile has invalidated
+    captures (cudaErrorStreamCaptureInvalidated); the eager mode (graph=False) has no such restriction."""
 
     def __init__(self, engine, caps: ChainCaps, real_dtype=None, graph=True, grow=False, max_grow=4):
         """engine: a ChainEngine (its tables, finder, template and configuration are used)."""
@@ -137,6 +144,7 @@ class ResidentChain:
         self.launches_per_run = 0
         self.replays = 0                # graph replays (kernel launches of a replay: launches_per_run)
         self._graph, self._graph_key = None, None
+        self._warm = False
         self._alloc(caps)
 
     # -- buffers ----------------------------------------------------------------------------------------------------
@@ -195,7 +203,13 @@ class ResidentChain:
     def load(self, ds: DeviceSteps):
         """Copy a batch into the static buffers (device copies on the current stream)."""
         c = self.caps
-        if ds.nevents > c.events or ds.nsteps > c.steps or ds.max_steps > c.max_steps_per_event:
+        over = ds.nevents > c.events or ds.nsteps > c.steps or ds.max_steps > c.max_steps_per_event
+        if over and self.grow and ds.max_steps <= 32768:
+            up = lambda cur, v: max(cur, int(np.ceil(1.25 * v)))  # noqa: E731
+            self._alloc(replace(c, events=up(c.events, ds.nevents), steps=up(c.steps, ds.nsteps),
+                                max_steps_per_event=min(32768, up(c.max_steps_per_event, ds.max_steps))))
+            c, over = self.caps, False
+        if over:
             raise ValueError(f"batch of {ds.nevents} events / {ds.nsteps} steps / {ds.max_steps} steps per event "
                              f"exceeds the chain capacities {c.events} / {c.steps} / {c.max_steps_per_event}")
         if ds.x.dtype != self.real_dtype:
@@ -236,12 +250,15 @@ class ResidentChain:
         cur = torch.cuda.current_stream()
         side = torch.cuda.Stream()
         side.wait_stream(cur)
-        with torch.cuda.stream(side):
-            self.status.reset()
-            self._call(P)                                       # eager warm-up outside the capture
+        with _CAPTURE_LOCK, torch.cuda.stream(side):
+            if not self._warm:                                  # first capture: one eager call outside it
+                self.status.reset()
+                self._call(P)
+                self._warm = True
             g = torch.cuda.CUDAGraph()
             n0 = _capi.launch_count()
-            with torch.cuda.graph(g, stream=side):
+            # thread-local capture: other host threads (serving slots) keep launching and reading meanwhile
+            with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
                 self.status.t.zero_()
                 self._call(P)
             self.launches_per_run = _capi.launch_count() - n0

@@ -1,8 +1,9 @@
 """Serving loop: design-point jobs through the device-resident chain with continuous batching.
 
 The reference runs one design-point job per process (a knob set over a step sample).  Here jobs arrive as a
-stream and are served by slots: a slot is a ChainEngine with its own CUDA stream, workspaces and host thread, and the
-number of slots follows from the HBM budget (the footprint of one slot, measured on a chunk).  Jobs are cut into chunks
+stream and are served by slots: a slot is a resident chain (ResidentChain: one crv_chain call per chunk with explicit
+capacities, one host read per chunk) with its own CUDA stream, buffers and host thread, and the number of slots
+follows from the HBM budget (the footprint of one slot, measured on a chunk).  Jobs are cut into chunks
 of events; free slots take the next chunk of the arrived job with the least work left, so a job that arrives while
 others run joins the mix at the next chunk boundary and its chunks overlap with theirs on the device.  Step tables
 stay resident: a job names a range of events of a device step pool, which it reads through views.
@@ -94,10 +95,11 @@ def slice_events(ds: DeviceSteps, a: int, b: int) -> DeviceSteps:
 @dataclass
 class _Slot:
     index: int
-    engine: object
+    engine: object                   # ChainEngine (tables of the design point)
     stream: object
     footprint: int = 0
     job_id: object = None            # design point the engine is configured for
+    chain: object = None             # ResidentChain over the engine (resident mode)
 
 
 class ServeEngine:
@@ -108,10 +110,15 @@ class ServeEngine:
     footprint and the granularity at which jobs interleave)."""
 
     def __init__(self, geom, cond, pool: DeviceSteps, hbm_budget: int, max_slots=8, chunk_events=4096,
-                 precision="fp32", device="cuda"):
+                 precision="fp32", device="cuda", resident=True):
+        """resident: slots run the resident chain (one host read per chunk) instead of the per-stage engine (a read per
+        stage).  The slots call it without graph replay: a stream capture on one slot thread is invalidated by CUDA
+        work that the other slot threads issue meanwhile (cudaErrorStreamCaptureInvalidated in a two-slot burst)."""
         from .chain import ChainEngine
         from .geometry import sector_geom
+        from .resident import ChainCaps, ResidentChain, caps_for
         torch = _torch()
+        self.resident = bool(resident)
         self.geom, self.cond, self.pool = geom, cond, pool
         self.G = sector_geom(geom)
         self.sector = str(self.G.sector_names[0])
@@ -128,36 +135,78 @@ class ServeEngine:
         torch.cuda.reset_peak_memory_stats()
         m0 = torch.cuda.memory_allocated()
         s0 = _Slot(0, ChainEngine(geom, cond, base, G=self.G, device=device), torch.cuda.Stream())
+        first = slice_events(pool, 0, min(self.chunk, pool.nevents))
         with torch.cuda.stream(s0.stream):
             s0.engine.configure(heavy)
-            s0.engine.run(slice_events(pool, 0, min(self.chunk, pool.nevents)), 1)
+            s0.engine.run(first, 1)
+            if self.resident:
+                # capacities of a chunk at the heavy design point (a trial run of the resident chain), with a margin
+                # for the event-to-event spread of later chunks; chunks that need more grow them
+                trial = ResidentChain(s0.engine, caps_for(s0.engine, [first]), graph=False, grow=True, max_grow=8)
+                trial.run(first, 1)
+                counts = trial.last_counts
+                trial = None
+                torch.cuda.synchronize()
+                torch.cuda.empty_cache()
+                self.caps = ChainCaps.from_counts(counts, events=self.chunk, steps=int(1.2 * first.nsteps) + 1024,
+                                                  max_steps_per_event=min(32768, 2 * max(1, first.max_steps)),
+                                                  margin=1.3)
+                s0.engine = ChainEngine(geom, cond, base, G=self.G, device=device)
+                s0.chain = ResidentChain(s0.engine, self.caps, graph=False, grow=True)
         torch.cuda.synchronize()
-        s0.footprint = int(1.25 * max(1, torch.cuda.max_memory_allocated() - m0))
+        if self.resident:
+            s0.footprint = int(s0.chain.nbytes * 1.05)
+        else:
+            s0.footprint = int(1.25 * max(1, torch.cuda.max_memory_allocated() - m0))
         n = int(max(1, min(max_slots, hbm_budget // s0.footprint)))
-        self.slots = [s0] + [_Slot(i, ChainEngine(geom, cond, base, G=self.G, device=device), torch.cuda.Stream(),
-                                   s0.footprint) for i in range(1, n)]
+        self.slots = [s0]
+        for i in range(1, n):
+            eng = ChainEngine(geom, cond, base, G=self.G, device=device)
+            sl = _Slot(i, eng, torch.cuda.Stream(), s0.footprint)
+            if self.resident:
+                sl.chain = ResidentChain(eng, self.caps, graph=False, grow=True)
+            self.slots.append(sl)
         self.footprint = s0.footprint
 
     def _run_chunk(self, slot: _Slot, job: Job, a: int, b: int) -> dict:
         torch = _torch()
-        eng = slot.engine
-        if slot.job_id != job.id:
-            eng.configure(job_config(job, self.precision, self.sector))
-            slot.job_id = job.id
         with torch.cuda.stream(slot.stream):
-            r = eng.run(slice_events(self.pool, a, b), job.seed)
-            out = {k: v.clone() for k, v in r.clusters.items()}
+            if slot.job_id != job.id:
+                cfg = job_config(job, self.precision, self.sector)
+                if slot.chain is not None:
+                    slot.chain.configure(cfg)
+                else:
+                    slot.engine.configure(cfg)
+                slot.job_id = job.id
+            if slot.chain is not None:
+                out = slot.chain.run(slice_events(self.pool, a, b), job.seed).clusters
+            else:
+                r = slot.engine.run(slice_events(self.pool, a, b), job.seed)
+                out = {k: v.clone() for k, v in r.clusters.items()}
             slot.stream.synchronize()
         return out
 
-    def run(self, jobs, realtime=True):
+    def run(self, jobs, realtime=True, policy="srpt", iso_rate=None, iso_overhead=0.0, slack=2.0):
         """Serve `jobs` (arrival times in seconds from now when realtime, else all at once).  Returns JobResults in
         job order.
 
-        Scheduling: a job is split into chunks of chunk_events events; whenever a slot is free it takes the next
-        chunk of the arrived job with the fewest events left (shortest remaining work first), so small jobs that
-        arrive during large ones are not queued behind them, and an otherwise idle device works on one job's chunks
-        on every slot.  Chunk results are kept per job and joined in event order when its last chunk is done."""
+        Scheduling: a job is split into chunks of chunk_events events; whenever a slot is free it takes the next chunk
+        of an arrived job, so jobs that arrive during others join at the next chunk boundary, and an otherwise idle
+        device works on one job's chunks on every slot.  Which job:
+          "srpt": the one with the fewest events left (shortest remaining work first: small jobs are not queued behind
+                  large ones; large jobs wait longest under load);
+          "edf":  the one with the earliest deadline, arrival + slack * its isolated run time (iso_overhead +
+                  events / iso_rate), which bounds the largest latency / isolated-time ratio instead.
+        Chunk results are kept per job and joined in event order when its last chunk is done."""
+        if policy not in ("srpt", "edf"):
+            raise ValueError(f"unknown scheduling policy {policy!r}")
+        if policy == "edf" and not (iso_rate and iso_rate > 0):
+            raise ValueError("edf scheduling needs the isolated rate (events/s)")
+        if policy == "edf":
+            prio = lambda j: (info[j]["job"].arrival + slack * (iso_overhead + info[j]["job"].n_events / iso_rate),  # noqa: E731
+                              j)
+        else:
+            prio = lambda j: (info[j]["left"], info[j]["job"].arrival, j)  # noqa: E731
         torch = _torch()
         t0 = time.perf_counter()
         cv = threading.Condition()
@@ -195,7 +244,7 @@ class ServeEngine:
                         admit_arrived(time.perf_counter() - t0)
                         cand = [jid for jid in state["active"] if info[jid]["next"] < len(info[jid]["bounds"])]
                         if cand:
-                            jid = min(cand, key=lambda j: (info[j]["left"], info[j]["job"].arrival, j))
+                            jid = min(cand, key=prio)
                             rec = info[jid]
                             k = rec["next"]
                             rec["next"] += 1
