@@ -302,6 +302,85 @@ def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=20
                     **{k: v for k, v in st_edf.items() if k != "jobs"}}}
 
 
+def lookup_inputs(n_rows, seed=41, prob=0.0015, yield_per_mev=28610.0, edep=3.4, length=20.0):
+    """Synthetic inputs of the lookup-table photon model with the shape of a 3200 mm table (10 x 41 x 56 position
+    bins, 5 beta bins, 150 delay bins of random weights, 8 emission bins, arrival probability `prob`, no fibre decay)
+    and rows of muon crossings: 20 mm through the thickness at random width and length positions (200 substeps),
+    photons per substep from yield x edep and the Cherenkov rate of beta 0.999."""
+    from types import SimpleNamespace
+    rng = np.random.default_rng(seed)
+    edges = {"x": np.linspace(0, 9.89, 11), "y": np.linspace(-25.67, 25.67, 42), "z": np.linspace(-1600, 1600, 57),
+             "beta": np.linspace(0.455, 1.0, 6), "theta": np.linspace(0, np.pi, 12), "phi": np.linspace(0, np.pi, 6),
+             "r": np.linspace(0, 0.616, 6)}
+    nb = {k: len(v) - 1 for k, v in edges.items()}
+
+    def table(n):
+        d = rng.integers(0, 4, (n, 150)).astype(np.uint8)
+        e = rng.integers(0, 40, (n, 8)).astype(np.uint8)
+        return SimpleNamespace(prob=np.full(n, prob, np.float32), delays=d, delay_sum=d.sum(1, dtype=np.int32),
+                               emis=e, emis_sum=e.sum(1, dtype=np.int32))
+
+    ns = nb["x"] * nb["y"] * nb["z"]
+    L = SimpleNamespace(name="synthetic_3200", half_thickness=9.64, half_width=25.42, half_length=1600.0,
+                        fiber_separation=26.0, hole_radius_x=2.0, hole_radius_y=1.0, fiber_radius=0.7,
+                        corner_radius=1.75, fiber_decay_time=0.0, edges=edges,
+                        tables={"scint": table(ns), "ckscint": table(ns * nb["beta"]),
+                                "ckfiber": table(nb["beta"] * nb["theta"] * nb["phi"] * nb["r"] * nb["z"])})
+    a = np.c_[np.full(n_rows, -length / 2), rng.uniform(-24, 24, n_rows), rng.uniform(-1500, 1500, n_rows)]
+    d = np.c_[np.full(n_rows, length), rng.normal(0, 2, n_rows), rng.normal(0, 2, n_rows)]
+    dl = np.linalg.norm(d, axis=1)
+    nsub = np.maximum((dl / 0.1).astype(np.int64), 1)
+    t0 = rng.uniform(0, 1e5, n_rows)
+
+    def per_substep(avg):
+        x = np.where(avg > 10, rng.normal(avg, np.sqrt(avg)), rng.poisson(avg))
+        return np.maximum(np.rint(x / nsub), 0).astype(np.int64)
+
+    ck = 266.0 * (0.999 - 0.474) / (1.0 - 0.474) * length      # Cherenkov photons of the crossing (linear map)
+    rows = {"s": a, "d": d, "t0": t0, "t1": t0 + 0.07, "nsub": nsub, "beta": np.full(n_rows, 0.999),
+            "theta": np.arccos(np.clip(d[:, 2] / dl, -1, 1)), "dev": np.full(n_rows, 0.94),
+            "step": np.arange(n_rows, dtype=np.int64), "chan": (np.arange(n_rows, dtype=np.int64) % 8192) * 4,
+            "n_scint": per_substep(np.full(n_rows, yield_per_mev * edep)), "n_ck_s": per_substep(np.full(n_rows, ck)),
+            "n_ck_f": per_substep(np.full(n_rows, ck))}
+    return L, rows
+
+
+def lookup_substeps(n_rows, reps=3, cpu_rows=20000):
+    """Lookup-table photon model: (step, SiPM) rows/s of crv_substep_photons on device-resident rows (device time of
+    the launches, CUDA events), and the oracle's rate on one core over a bounded sample of the same rows."""
+    import torch
+    from crvgpu import lookup as LK
+    L, rows = lookup_inputs(n_rows)
+    DL, R = LK.DeviceLookup(L), LK.DeviceRows(rows)
+    eng = LK.SubstepEngine()
+    st, _, _ = eng.run(DL, R, 1)                          # warm-up, output capacity
+    n_ph = int(st.numel())
+    st = None
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for r in range(reps):
+        eng.run(DL, R, 2 + r)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out = {"rows": n_rows, "rows_per_s": n_rows / (ms / 1000.0), "ms_per_call": ms, "photons_per_row": n_ph / n_rows,
+           "substeps_per_row": float(np.mean(rows["nsub"])), "table": "synthetic 3200 mm: 10x41x56 position bins, "
+           "5 beta, 150 delay bins, prob 0.0015", "precision": "fp64 (bit-exact with the oracle)",
+           "published_context": "reference JAX substep kernel ~300k rows/s on A100 (its own bench)"}
+    try:
+        from oracle import oracle as O
+        sub = {k: v[:cpu_rows] for k, v in rows.items()}
+        t0 = time.perf_counter()
+        O.substep_photons(L, sub, 2)
+        out["cpu_oracle_rows_per_s"] = cpu_rows / (time.perf_counter() - t0)
+        out["cpu_oracle_sample"] = f"{cpu_rows} rows on 1 core"
+    except Exception as exc:                              # reported baseline only
+        out["cpu_oracle_error"] = str(exc)[:200]
+    DL = R = eng = None
+    return out
+
+
 def fullscale(n_events, batch, seed=13):
     """Full-scale detector (86 modules of 4 x 16 counters, bar lengths over {230, 300, 450, 560, 660} cm, Poisson(60)
     steps plus 0.5 noise steps per counter per event): events/s of the chain on a resident subset, FP32-mixed and
@@ -354,6 +433,8 @@ def main():
     ap.add_argument("--fullscale-events", type=int, default=2048, help="events of the full-scale measurement (0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
     ap.add_argument("--serve-load", type=float, default=0.8)
+    ap.add_argument("--lookup-rows", type=int, default=1 << 20,
+                    help="(step, SiPM) rows of the lookup-table photon model measurement (0: skip)")
     ap.add_argument("--uneven-waveforms", type=int, default=1 << 22,
                     help="waveforms of the uneven batched pulse-fit measurement (0: skip)")
     args = ap.parse_args()
@@ -645,6 +726,11 @@ def main():
         uneven = uneven_pulse_fit(args.uneven_waveforms, 1 << 19)
         torch.cuda.empty_cache()
 
+    lookup = None
+    if rank == 0 and args.lookup_rows > 0:
+        lookup = lookup_substeps(args.lookup_rows)
+        torch.cuda.empty_cache()
+
     full = None
     if rank == 0 and args.fullscale_events > 0:
         full = fullscale(args.fullscale_events, 1024)
@@ -680,6 +766,7 @@ def main():
                 "roofline_pulse_fit": roofline_of("pulse fit"),
                 "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
                 "uneven_pulse_fit": uneven,
+                "lookup_photons": lookup,
                 "serving": serve,
                 "fullscale": full,
                 "cpu_baseline": cpu}

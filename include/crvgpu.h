@@ -19,6 +19,7 @@
  *   crv_coincidences                 <- crvfastsim.reco.coinc.find_event over every event, as chain.clusters
  *                                                                                     (crv/crvfastsim/reco/coinc.py:289,
  *                                                                                      crv/crvfastsim/chain.py:296-362)
+ *   crv_substep_photons              <- crvfastsim.response.photons._substep_photons   (crv/crvfastsim/response/photons.py:163)
  *   crv_chain                        <- the chain above in one resident call with explicit capacities, as the
  *                                       mixing adapter's resident CRV chain (mixing/device_crv.py:127-573,
  *                                       mixing/DEVICE_CRV.md "Explicit capacities")
@@ -67,6 +68,7 @@ extern "C" {
 #define CRV_NEED_WAVEFORMS 12
 #define CRV_NEED_PULSES_OUT 13
 #define CRV_NEED_MEMBERS 14
+#define CRV_NEED_PHOTONS_OUT 15      /* crv_substep_photons output */
 
 typedef struct CrvStatus {
     int32_t flags;
@@ -388,6 +390,51 @@ int crv_chain(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev,
               const CrvChannels *ch, const CrvPixels *px, const double *tmpl, int32_t tlen, const CrvFinderGeom *g,
               CrvClusters *out, CrvMembers *mem, int64_t *counts_dev, void *workspace, int64_t workspace_bytes,
               void *stream, CrvStatus *status_dev);
+
+/*
+ * Lookup-table photon model (crvfastsim.response.photons._substep_photons, crv/crvfastsim/response/photons.py:163-224,
+ * tables as crv/crvfastsim/response/lookup.py:70-98): every (step, SiPM) row is cut into nsub substeps along its step
+ * vector; at each substep the position selects a bin of the scintillation table (inside the scintillator), of the
+ * Cherenkov-in-scintillator table (also by beta) and of the Cherenkov-in-fibre table (inside a fibre hole, by beta,
+ * theta, phi, r); the arrivals of each are Binomial(photons per substep, min(prob * dev * exp(-mu z), 1)), each
+ * delayed by a draw from the bin's delay weights (1 ns bins) and, with a fibre decay time, by a Gamma(emissions, decay
+ * time) whose emission count is drawn from the bin's emission weights.  Draws are keyed Philox blocks (key = (seed, 0);
+ * counter = (step low, step high, stage 7 | table | call | channel, substep << 12 | arrival)), so results do not depend
+ * on batching.  Limits (CRV_ST_LIMIT): 2^20 substeps per row, 4096 arrivals per (substep, table), 128 emissions.
+ */
+typedef struct CrvLookupTable {
+    const float *prob;           /* [nbins] arrival probability */
+    const uint8_t *delays;       /* [nbins][ndelay] delay weights (1 ns bins) */
+    const int32_t *delay_sum;    /* [nbins] */
+    const uint8_t *emis;         /* [nbins][nemis] emission-count weights */
+    const int32_t *emis_sum;     /* [nbins] */
+    int32_t nbins, ndelay, nemis, pad;
+} CrvLookupTable;
+
+typedef struct CrvLookup {
+    double half_thickness, half_width, half_length, fiber_separation, hole_radius_x, hole_radius_y, fiber_radius,
+        corner_radius, fiber_decay_time;
+    const double *edges[7];      /* ascending bin edges of x, y, z, beta, theta, phi, r */
+    int32_t nedges[7];
+    int32_t pad;
+    const double *cos_phi_edges; /* cos of the phi edges: phi bins are found on cos phi (no arccos per substep) */
+    CrvLookupTable table[3];     /* scintillation, Cherenkov in scintillator, Cherenkov in fibre */
+} CrvLookup;
+
+/* Rows: local start s[3] and step vector d[3] (thickness, width, length; mm), start/end time, beta, theta, yield
+ * deviation factor, optional extra attenuation per mm (NULL: none), substeps, step index, channel, and the photons per
+ * substep of the three tables. */
+typedef struct CrvSubstepRows {
+    const double *s, *d, *t0, *t1, *beta, *theta, *dev, *mu;
+    const int64_t *nsub, *step, *chan, *n_scint, *n_ck_s, *n_ck_f;
+} CrvSubstepRows;
+
+int64_t crv_substeps_workspace(int64_t nrows);
+/* Photons of every row, in (row, substep, table, arrival) order: step index, channel, arrival time (capacity cap;
+ * *n_out_dev receives the count). */
+int crv_substep_photons(const CrvLookup *L, uint32_t seed, const CrvSubstepRows *rows, int64_t nrows,
+                        int64_t *o_step, int64_t *o_chan, double *o_time, int64_t cap, int64_t *n_out_dev,
+                        void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
 
 #ifdef __cplusplus
 }

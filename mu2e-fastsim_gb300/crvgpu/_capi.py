@@ -19,7 +19,7 @@ PULSES_STATIC_MAX_BYTES = 64 << 20
 ST_CAPACITY, ST_LIMIT, ST_NONFINITE, ST_ORDER = 1, 2, 4, 8
 NEED = dict(STEPS_PER_EVENT=0, PHOTONS_PER_SIPM=1, CHARGE_FACTOR=2, DIGIS=3, SAMPLES=4, PULSES=5, HITS_PER_EVENT=6,
             CLUSTERS=7, PHOTONS_TOTAL=8, SLOTS_TOTAL=9, CHARGES_OUT=10, DIGIS_OUT=11, WAVEFORMS=12, PULSES_OUT=13,
-            MEMBERS=14)
+            MEMBERS=14, PHOTONS_OUT=15)
 
 
 class CrvStatus(ctypes.Structure):
@@ -106,6 +106,23 @@ class CrvMembers(ctypes.Structure):
     _fields_ = [("cl", c_p), ("idx", c_p), ("event", c_p)]
 
 
+class CrvLookupTable(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("prob", "delays", "delay_sum", "emis", "emis_sum")] + \
+        [(k, c_i32) for k in ("nbins", "ndelay", "nemis", "pad")]
+
+
+class CrvLookup(ctypes.Structure):
+    _fields_ = [(k, c_f64) for k in ("half_thickness", "half_width", "half_length", "fiber_separation", "hole_radius_x",
+                                     "hole_radius_y", "fiber_radius", "corner_radius", "fiber_decay_time")] + \
+        [("edges", c_p * 7), ("nedges", c_i32 * 7), ("pad", c_i32), ("cos_phi_edges", c_p),
+         ("table", CrvLookupTable * 3)]
+
+
+class CrvSubstepRows(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("s", "d", "t0", "t1", "beta", "theta", "dev", "mu", "nsub", "step", "chan",
+                                   "n_scint", "n_ck_s", "n_ck_f")]
+
+
 CHAIN_CAPS = ("events", "steps", "photons", "charges", "slots", "digis", "pulses", "max_steps_per_event")
 CHAIN_COUNTS = ("charges", "digis", "waveforms", "pulses", "events", "hits", "clusters", "members", "photons",
                 "slots")
@@ -153,6 +170,9 @@ _SIGS = {
     "crv_sipm": (c_i32, [P(CrvParams), P(CrvPixels), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, P(CrvCharges),
                          c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_chain_workspace": (c_i64, [P(CrvParams), P(CrvChainCaps)]),
+    "crv_substeps_workspace": (c_i64, [c_i64]),
+    "crv_substep_photons": (c_i32, [P(CrvLookup), c_u32, P(CrvSubstepRows), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p,
+                                    c_i64, c_p, c_p]),
     "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
                           P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters), P(CrvMembers),
                           c_p, c_p, c_i64, c_p, c_p]),

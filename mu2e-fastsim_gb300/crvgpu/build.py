@@ -1,7 +1,8 @@
 """Build the engine library (libcrvgpu.so) in-tree with nvcc for sm_103a.
 
-Three translation units compile in parallel: the engine/C-ABI unit, the FP64 kernels (built with -fmad=false so
-every FP64 operation rounds exactly as written: bit-exact with the CPU oracle) and the FP32-mixed kernels.
+The translation units compile in parallel: the engine/C-ABI unit, the FP64 kernels and the lookup-table substep unit
+(both built with -fmad=false so every FP64 operation rounds exactly as written: bit-exact with the CPU oracle), the
+FP32-mixed kernels and the allocation-free pulse-fit entry point.
 """
 from __future__ import annotations
 
@@ -23,6 +24,7 @@ UNITS = {
     "crv_kernels_f64.cu": ["-fmad=false"],
     "crv_kernels_f32.cu": [],
     "crv_static.cu": [],
+    "crv_lookup.cu": ["-fmad=false"],
 }
 
 

@@ -623,3 +623,229 @@ void orc_counts_from_mean(uint32_t seed, int64_t n, const double *avg, int64_t *
         count[i] = draw_count(avg[i], w);
     }
 }
+
+/* ------------------------------------------------------------------------------------------------------------ */
+/* Lookup-table photon model: photons._substep_photons (crv/crvfastsim/response/photons.py:139-224) over (step,   */
+/* SiPM) rows with keyed draws: Binomial arrivals per (substep, table), delay and emission counts from the bin's  */
+/* weights, Gamma(emissions) fibre decay as a sum of exponentials.                                              */
+
+enum { ST_SUBSTEP = 7, SUB_CALL_BINOMIAL = 0, SUB_CALL_PHOTON = 1, SUB_CALL_GAMMA = 2 };
+#define SUB_MAX_SUBSTEPS (1ll << 20)
+#define SUB_MAX_ARRIVALS 4096
+#define SUB_MAX_EMISSIONS 128
+
+typedef struct {
+    const float *prob;
+    const uint8_t *delays;
+    const int32_t *delay_sum;
+    const uint8_t *emis;
+    const int32_t *emis_sum;
+    int32_t nbins, ndelay, nemis, pad;
+} OrcLookupTable;
+
+typedef struct {
+    double half_thickness, half_width, half_length, fiber_separation, hole_radius_x, hole_radius_y, fiber_radius,
+        corner_radius, fiber_decay_time;
+    const double *edges[7];
+    int32_t nedges[7];
+    int32_t pad;
+    const double *cos_phi_edges;
+    OrcLookupTable table[3];
+} OrcLookup;
+
+typedef struct {
+    const double *s, *d, *t0, *t1, *beta, *theta, *dev, *mu;
+    const int64_t *nsub, *step, *chan, *n_scint, *n_ck_s, *n_ck_f;
+} OrcSubstepRows;
+
+static inline void sub_block(uint32_t seed, int64_t step, int64_t chan, int tb, int call, int idx, int64_t k, int j,
+                             uint32_t out[4]) {
+    uint32_t c[4] = {(uint32_t)step, (uint32_t)((uint64_t)step >> 32), w2_of(ST_SUBSTEP, tb, idx, call, (int)chan),
+                     ((uint32_t)k << 12) | (uint32_t)j};
+    uint32_t key[2] = {seed, 0u};
+    orc_philox(c, key, out);
+}
+
+/* Binomial(n, p): inversion on min(p, 1 - p) while the mean is at most 256 (Kachitvichyanukul & Schmeiser's BINV),
+ * else the normal approximation, clipped to [0, n]. */
+static int64_t sub_binomial(int64_t n, double p, const uint32_t w[4]) {
+    if (n <= 0 || !(p > 0.0)) return 0;
+    if (p >= 1.0) return n;
+    int flip = p > 0.5;
+    double q = flip ? 1.0 - p : p;
+    double mean = (double)n * q;
+    int64_t k;
+    if (mean > 256.0) {
+        double z0, z1;
+        normal_pair(w, &z0, &z1);
+        double x = rint(mean + sqrt(mean * (1.0 - q)) * z0);
+        k = x < 0.0 ? 0 : (x > (double)n ? n : (int64_t)x);
+    } else {
+        double u = u01(w[0], w[1]);
+        double s = q / (1.0 - q);
+        double a = (double)(n + 1) * s;
+        double r = orc_exp((double)n * orc_log(1.0 - q));
+        k = 0;
+        while (u > r && k < n) {
+            u = u - r;
+            k += 1;
+            r = r * (a / (double)k - s);
+        }
+    }
+    return flip ? n - k : k;
+}
+
+static int sub_find_bin(const double *e, int ne, double v) {
+    if (!(v >= e[0]) || !(v <= e[ne - 1])) return -1;
+    if (v == e[0]) return 0;
+    int lo = 0, hi = ne;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (e[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo - 1;
+}
+
+static int sub_find_bin_cos(const double *ce, int ne, double c) {
+    if (!(c <= ce[0]) || !(c >= ce[ne - 1])) return -1;
+    if (c == ce[0]) return 0;
+    int lo = 0, hi = ne;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (ce[mid] > c) lo = mid + 1; else hi = mid;
+    }
+    return lo - 1;
+}
+
+static int sub_first_reaching(const uint8_t *wts, int n, double thr) {
+    int cum = 0;
+    for (int j = 0; j < n; ++j) {
+        cum += wts[j];
+        if (!((double)cum < thr)) return j;
+    }
+    return n;
+}
+
+static void sub_bins(const OrcLookup *L, const OrcSubstepRows *R, int64_t r, int64_t k, int64_t nsub, int bb, int bth,
+                     int bin[3], double *t_out, double *z_out) {
+    double frac = ((double)k + 0.5) / (double)nsub;
+    double x = R->s[3 * r] + R->d[3 * r] * frac;
+    double y = R->s[3 * r + 1] + R->d[3 * r + 1] * frac;
+    double z = R->s[3 * r + 2] + R->d[3 * r + 2] * frac;
+    double t = R->t0[r] + (R->t1[r] - R->t0[r]) * frac;
+    double half_sep = L->fiber_separation / 2.0;
+    double ax = fabs(x), ay = fabs(y);
+    int insc = ax < L->half_thickness && ay < L->half_width && fabs(z) < L->half_length;
+    double ex = ax / L->hole_radius_x, ey = (ay - half_sep) / L->hole_radius_y;
+    insc = insc && (ex * ex + ey * ey >= 1.0);
+    double cx = L->half_thickness - L->corner_radius, cy = L->half_width - L->corner_radius;
+    if (ax > cx && ay > cy) {
+        double qx = ax - cx, qy = ay - cy;
+        if (sqrt(qx * qx + qy * qy) > L->corner_radius) insc = 0;
+    }
+    double y0 = y + half_sep, y1 = y - half_sep;
+    double r0 = sqrt(x * x + y0 * y0), r1 = sqrt(x * x + y1 * y1);
+    int in0 = r0 <= L->fiber_radius, in1 = r1 <= L->fiber_radius;
+    double ry = in1 ? y1 : y0, rr = in1 ? r1 : r0;
+    double dx = R->d[3 * r], dy = R->d[3 * r + 1];
+    double norm = sqrt(dx * dx + dy * dy) * rr;
+    double c = 1.0;
+    if (norm > 0.0) {
+        c = (dx * x + dy * ry) / norm;
+        c = c < -1.0 ? -1.0 : (c > 1.0 ? 1.0 : c);
+    }
+    int infb = fabs(z) < L->half_length && (in0 || in1) && !insc;
+    int ny = L->nedges[1] - 1, nz = L->nedges[2] - 1, nb = L->nedges[3] - 1;
+    int nth = L->nedges[4] - 1, nph = L->nedges[5] - 1, nr = L->nedges[6] - 1;
+    int bx = sub_find_bin(L->edges[0], L->nedges[0], ax), by = sub_find_bin(L->edges[1], L->nedges[1], y);
+    int bz = sub_find_bin(L->edges[2], L->nedges[2], z);
+    int geo = bx >= 0 && by >= 0 && bz >= 0;
+    bin[0] = (insc && geo) ? bz + by * nz + bx * ny * nz : -1;
+    bin[1] = (insc && geo && bb >= 0) ? bb + bz * nb + by * nz * nb + bx * ny * nz * nb : -1;
+    bin[2] = -1;
+    if (infb && bb >= 0 && bth >= 0 && bz >= 0) {
+        int bph = sub_find_bin_cos(L->cos_phi_edges, L->nedges[5], c);
+        int br = sub_find_bin(L->edges[6], L->nedges[6], rr);
+        if (bph >= 0 && br >= 0) bin[2] = bz + br * nz + bph * nr * nz + bth * nph * nr * nz + bb * nth * nph * nr * nz;
+    }
+    *t_out = t;
+    *z_out = z;
+}
+
+static int64_t sub_arrivals(const OrcLookup *L, const OrcSubstepRows *R, uint32_t seed, int64_t r, int64_t k, int tb,
+                            int bin, double z) {
+    double pr = (double)L->table[tb].prob[bin] * R->dev[r];
+    if (R->mu) pr = pr * orc_exp(-R->mu[r] * z);
+    pr = pr < 1.0 ? pr : 1.0;
+    int64_t n = tb == 0 ? R->n_scint[r] : (tb == 1 ? R->n_ck_s[r] : R->n_ck_f[r]);
+    uint32_t w[4];
+    sub_block(seed, R->step[r], R->chan[r], tb, SUB_CALL_BINOMIAL, 0, k, 0, w);
+    return sub_binomial(n, pr, w);
+}
+
+static double sub_time(const OrcLookup *L, uint32_t seed, int64_t step, int64_t chan, int64_t k, int tb, int bin,
+                       int j, double t, int *limit) {
+    const OrcLookupTable *T = &L->table[tb];
+    uint32_t w[4];
+    sub_block(seed, step, chan, tb, SUB_CALL_PHOTON, 0, k, j, w);
+    double thr = u01(w[0], w[1]) * (double)T->delay_sum[bin];
+    double tt = t + (double)sub_first_reaching(T->delays + (int64_t)bin * T->ndelay, T->ndelay, thr);
+    if (L->fiber_decay_time > 0.0) {
+        double thr2 = u01(w[2], w[3]) * (double)T->emis_sum[bin];
+        int ne = sub_first_reaching(T->emis + (int64_t)bin * T->nemis, T->nemis, thr2);
+        if (ne > SUB_MAX_EMISSIONS) {
+            *limit = 1;
+        } else if (ne > 0) {
+            double g = 0.0;
+            for (int i = 0; i < ne; i += 2) {
+                uint32_t v[4];
+                sub_block(seed, step, chan, tb, SUB_CALL_GAMMA, i >> 1, k, j, v);
+                g = g - orc_log(u01_open(v[0], v[1]));
+                if (i + 1 < ne) g = g - orc_log(u01_open(v[2], v[3]));
+            }
+            tt = tt + g * L->fiber_decay_time;
+        }
+    }
+    return tt;
+}
+
+/* Photons of every row in (row, substep, table, arrival) order.  Pass o_time = NULL to count only.  Returns the
+ * photon count; *limit is set when a key limit was exceeded (those arrivals are dropped, as on the device). */
+int64_t orc_substep_photons(const OrcLookup *L, uint32_t seed, const OrcSubstepRows *R, int64_t nrows, int64_t *o_step,
+                            int64_t *o_chan, double *o_time, int *limit) {
+    int64_t o = 0;
+    *limit = 0;
+    for (int64_t r = 0; r < nrows; ++r) {
+        int64_t nsub = R->nsub[r];
+        if (nsub > SUB_MAX_SUBSTEPS) { *limit = 1; continue; }
+        if (nsub <= 0) continue;
+        int bb = sub_find_bin(L->edges[3], L->nedges[3], R->beta[r]);
+        int bth = sub_find_bin(L->edges[4], L->nedges[4], R->theta[r]);
+        for (int64_t k = 0; k < nsub; ++k) {
+            int bin[3];
+            double t, z;
+            sub_bins(L, R, r, k, nsub, bb, bth, bin, &t, &z);
+            for (int tb = 0; tb < 3; ++tb) {
+                if (bin[tb] < 0) continue;
+                int64_t a = sub_arrivals(L, R, seed, r, k, tb, bin[tb], z);
+                if (a >= SUB_MAX_ARRIVALS) { *limit = 1; continue; }
+                for (int j = 0; j < (int)a; ++j, ++o) {
+                    if (!o_time) continue;
+                    o_step[o] = R->step[r];
+                    o_chan[o] = R->chan[r];
+                    o_time[o] = sub_time(L, seed, R->step[r], R->chan[r], k, tb, bin[tb], j, t, limit);
+                }
+            }
+        }
+    }
+    return o;
+}
+
+/* Binomial draws of the substep sampler for tests: n[i], p[i] with the block keyed by (step i, chan 0, table 0, k 0). */
+void orc_binomial_v(uint32_t seed, int64_t cnt, const int64_t *n, const double *p, int64_t *out) {
+    for (int64_t i = 0; i < cnt; ++i) {
+        uint32_t w[4];
+        sub_block(seed, i, 0, 0, SUB_CALL_BINOMIAL, 0, 0, 0, w);
+        out[i] = sub_binomial(n[i], p[i], w);
+    }
+}

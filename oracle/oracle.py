@@ -1028,3 +1028,79 @@ def pulses_from_waveforms(W, cond, rcfg, period):
     if "event_t0" in W:
         P["time"] = P["time"] + W["event_t0"][P["wf"]]
     return P
+
+
+# ---- lookup-table photon model (photons._substep_photons) ---------------------------------------------------------
+
+LOOKUP_EDGES = ("x", "y", "z", "beta", "theta", "phi", "r")
+LOOKUP_TABLES = ("scint", "ckscint", "ckfiber")
+
+
+class _OrcLookupTable(ctypes.Structure):
+    _fields_ = [("prob", ctypes.c_void_p), ("delays", ctypes.c_void_p), ("delay_sum", ctypes.c_void_p),
+                ("emis", ctypes.c_void_p), ("emis_sum", ctypes.c_void_p), ("nbins", ctypes.c_int32),
+                ("ndelay", ctypes.c_int32), ("nemis", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+class _OrcLookup(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("half_thickness", "half_width", "half_length", "fiber_separation",
+                                               "hole_radius_x", "hole_radius_y", "fiber_radius", "corner_radius",
+                                               "fiber_decay_time")] + \
+        [("edges", ctypes.c_void_p * 7), ("nedges", ctypes.c_int32 * 7), ("pad", ctypes.c_int32),
+         ("cos_phi_edges", ctypes.c_void_p), ("table", _OrcLookupTable * 3)]
+
+
+class _OrcRows(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("s", "d", "t0", "t1", "beta", "theta", "dev", "mu", "nsub", "step",
+                                               "chan", "n_scint", "n_ck_s", "n_ck_f")]
+
+
+def _lookup_struct(L, k):
+    """OrcLookup of a lookup table object with the reference's fields (lookup.LookupTable), arrays kept alive by k."""
+    S = _OrcLookup(*[float(getattr(L, f)) for f in ("half_thickness", "half_width", "half_length",
+                                                    "fiber_separation", "hole_radius_x", "hole_radius_y",
+                                                    "fiber_radius", "corner_radius", "fiber_decay_time")])
+    for i, e in enumerate(LOOKUP_EDGES):
+        S.edges[i] = k(L.edges[e], np.float64)
+        S.nedges[i] = len(L.edges[e])
+    S.cos_phi_edges = k(np.cos(np.asarray(L.edges["phi"], np.float64)), np.float64)
+    for i, name in enumerate(LOOKUP_TABLES):
+        T = L.tables[name]
+        d, e = np.asarray(T.delays, np.uint8), np.asarray(T.emis, np.uint8)
+        S.table[i] = _OrcLookupTable(k(T.prob, np.float32), k(d, np.uint8), k(T.delay_sum, np.int32),
+                                     k(e, np.uint8), k(T.emis_sum, np.int32), len(T.prob), d.shape[1], e.shape[1], 0)
+    return S
+
+
+def substep_photons(L, rows, seed):
+    """(step index, channel, time) of the photons of (step, SiPM) rows through lookup table L, keyed by seed, in
+    (row, substep, table, arrival) order; rows as the reference's substep rows (photons.py:163-224).  Returns
+    (step, chan, time, limit_flag)."""
+    k = _Keep()
+    S = _lookup_struct(L, k)
+    n = len(rows["nsub"])
+    mu = rows.get("mu")
+    R = _OrcRows(k(rows["s"], np.float64), k(rows["d"], np.float64), k(rows["t0"], np.float64),
+                 k(rows["t1"], np.float64), k(rows["beta"], np.float64), k(rows["theta"], np.float64),
+                 k(rows["dev"], np.float64), None if mu is None else k(mu, np.float64), k(rows["nsub"], np.int64),
+                 k(rows["step"], np.int64), k(rows["chan"], np.int64), k(rows["n_scint"], np.int64),
+                 k(rows["n_ck_s"], np.int64), k(rows["n_ck_f"], np.int64))
+    f = lib().orc_substep_photons
+    f.restype = ctypes.c_int64
+    lim = ctypes.c_int(0)
+    m = f(ctypes.byref(S), ctypes.c_uint32(seed), ctypes.byref(R), ctypes.c_int64(n), None, None, None,
+          ctypes.byref(lim))
+    st, ch, tm = np.zeros(m, np.int64), np.zeros(m, np.int64), np.zeros(m)
+    if m:
+        f(ctypes.byref(S), ctypes.c_uint32(seed), ctypes.byref(R), ctypes.c_int64(n), _p(st), _p(ch), _p(tm),
+          ctypes.byref(lim))
+    return st, ch, tm, bool(lim.value)
+
+
+def binomial(seed, n, p):
+    """The substep sampler's Binomial(n[i], p[i]) draws (block keyed by i)."""
+    n = np.ascontiguousarray(n, np.int64)
+    p = np.ascontiguousarray(p, np.float64)
+    out = np.zeros(len(n), np.int64)
+    lib().orc_binomial_v(ctypes.c_uint32(seed), ctypes.c_int64(len(n)), _p(n), _p(p), _p(out))
+    return out

@@ -1,6 +1,7 @@
 """Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
 
-Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR]
+Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
+(NAME: pulsefit, concat, waveform, coinc, stats, lookup; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -14,6 +15,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   coinc.npz      find_event clusters on three geometries, scalar and vectorised combination checks
                  (crv/crvfastsim/reco/coinc.py:289-392, coinc_cpu.py:11-51)
   stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
+  lookup.npz     a synthetic lookup table and (step, SiPM) rows with the statistics of the reference substep kernel
+                 (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
+                 delay histogram
 """
 import os
 import sys
@@ -24,7 +28,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference/crv")
+ARGS = sys.argv[1:]
+REF = Path(ARGS.pop(0)) if ARGS and os.path.isdir(ARGS[0]) else Path("/root/reference/crv")
+ONLY = set(ARGS)
 sys.path.insert(0, str(HERE.parent / "refshim"))
 sys.path.insert(0, str(REF))
 os.environ["CRVFS_CPU_ATTACHMENT"] = "numpy"
@@ -380,11 +386,80 @@ def make_stats():
     np.savez_compressed(HERE / "stats.npz", **out)
 
 
+def synthetic_lookup(rng, decay_time=7.4):
+    """A small lookup table with the reference's layout (lookup.py:70-98): bin edges, arrival probabilities, delay and
+    emission weights; geometry of a 2 cm x 5 cm counter with two fibre holes."""
+    edges = {"x": np.linspace(0.0, 10.0, 6), "y": np.linspace(-26.0, 26.0, 11), "z": np.linspace(-1000.0, 1000.0, 9),
+             "beta": np.linspace(0.4, 1.0, 4), "theta": np.linspace(0.0, np.pi, 5), "phi": np.linspace(0.0, np.pi, 4),
+             "r": np.linspace(0.0, 0.7, 4)}
+    nb = {k: len(v) - 1 for k, v in edges.items()}
+
+    def table(n, D=24, E=4, pmax=0.02):
+        d = rng.integers(0, 30, (n, D)).astype(np.uint8)
+        e = rng.integers(0, 30, (n, E)).astype(np.uint8)
+        return dict(prob=rng.uniform(0.0, pmax, n).astype(np.float32), delays=d, delay_sum=d.sum(1, dtype=np.int32),
+                    emis=e, emis_sum=e.sum(1, dtype=np.int32))
+
+    ns = nb["x"] * nb["y"] * nb["z"]
+    tabs = {"scint": table(ns), "ckscint": table(ns * nb["beta"]),
+            "ckfiber": table(nb["beta"] * nb["theta"] * nb["phi"] * nb["r"] * nb["z"], pmax=0.2)}
+    geo = dict(half_thickness=9.64, half_width=25.42, half_length=1000.0, fiber_separation=26.0, hole_radius_x=2.0,
+               hole_radius_y=1.0, fiber_radius=0.7, corner_radius=1.75, fiber_decay_time=decay_time)
+    return edges, tabs, geo
+
+
+def synthetic_rows(rng, R=1500):
+    """(step, SiPM) rows of tracks through the counter: local start, step vector, times, photons per substep."""
+    a = np.c_[rng.uniform(-9.5, 9.5, R), rng.uniform(-25, 25, R), rng.uniform(-950, 950, R)]
+    d = np.c_[rng.normal(0, 4, R), rng.normal(0, 4, R), rng.normal(0, 20, R)]
+    # a fifth of the rows cross the fibre holes' neighbourhood, so the fibre table is exercised
+    f = rng.random(R) < 0.2
+    a[f, 0] = rng.uniform(-0.6, 0.6, f.sum())
+    a[f, 1] = np.where(rng.random(f.sum()) < 0.5, -13.0, 13.0) + rng.uniform(-0.5, 0.5, f.sum())
+    d[f, 0] = rng.normal(0, 0.3, f.sum())
+    d[f, 1] = rng.normal(0, 0.3, f.sum())
+    t0 = rng.uniform(0, 1e3, R)
+    dl = np.linalg.norm(d, axis=1)
+    return {"s": a, "d": d, "t0": t0, "t1": t0 + rng.uniform(0.0, 0.2, R),
+            "nsub": np.maximum((dl / 0.1).astype(np.int64), 1), "beta": rng.uniform(0.5, 1.0, R),
+            "theta": np.arccos(np.clip(d[:, 2] / np.where(dl > 0, dl, 1.0), -1, 1)), "dev": rng.uniform(0.8, 1.2, R),
+            "mu": rng.uniform(0.0, 2e-4, R), "step": np.arange(R, dtype=np.int64) * 7 + 3,
+            "chan": (np.arange(R, dtype=np.int64) % 5000) * 4 + 1, "n_scint": rng.integers(0, 40, R),
+            "n_ck_s": rng.integers(0, 4, R), "n_ck_f": rng.integers(0, 30, R)}
+
+
+def make_lookup(seeds=16):
+    from types import SimpleNamespace
+    rng = np.random.default_rng(73)
+    edges, tabs, geo = synthetic_lookup(rng)
+    rows = synthetic_rows(rng)
+    L = SimpleNamespace(edges=edges, tables={k: SimpleNamespace(**v) for k, v in tabs.items()}, **geo)
+    R = len(rows["nsub"])
+    counts = np.zeros(R)
+    H = 64
+    hist = np.zeros(H)
+    total = 0
+    for s in range(seeds):
+        st, ch, tm = PH._substep_photons(L, rows, np.random.default_rng(1000 + s))
+        ri = (st - 3) // 7
+        counts += np.bincount(ri, minlength=R)
+        dt = tm - rows["t0"][ri]
+        hist += np.bincount(np.clip(dt.astype(np.int64), 0, H - 1), minlength=H)
+        total += len(st)
+    out = {f"edge_{k}": v for k, v in edges.items()}
+    for k, T in tabs.items():
+        out.update({f"{k}_{f}": v for f, v in T.items()})
+    out.update({f"geo_{k}": np.float64(v) for k, v in geo.items()})
+    out.update({f"row_{k}": v for k, v in rows.items()})
+    out.update(ref_seeds=np.int64(seeds), ref_counts=counts / seeds, ref_delay_hist=hist / seeds,
+               ref_total=np.int64(total))
+    np.savez_compressed(HERE / "lookup.npz", **out)
+
+
 if __name__ == "__main__":
-    make_pulsefit()
-    make_concat()
-    make_waveform()
-    make_coinc()
-    make_stats()
+    for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
+                     ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup)):
+        if not ONLY or name in ONLY:
+            fn()
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -1,0 +1,73 @@
+"""Oracle of the lookup-table photon model (photons._substep_photons, crv/crvfastsim/response/photons.py:163-224)
+against the reference's own outputs: a synthetic table and rows with the reference's statistics over 16 generator
+seeds (tests/golden/lookup.npz, made by tests/golden/make_golden.py).  The reference draws from a sequential
+generator and the oracle from keyed Philox blocks, so the comparison is statistical: photons per row (chi-square per
+degree of freedom), total photons, and the distribution of arrival delays (Kolmogorov-Smirnov distance)."""
+import os
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "lookup.npz")
+
+
+def lookup_fixture():
+    z = np.load(GOLDEN)
+    edges = {k: z[f"edge_{k}"] for k in O.LOOKUP_EDGES}
+    tabs = {k: SimpleNamespace(**{f: z[f"{k}_{f}"] for f in ("prob", "delays", "delay_sum", "emis", "emis_sum")})
+            for k in O.LOOKUP_TABLES}
+    geo = {k[4:]: float(z[k]) for k in z.files if k.startswith("geo_")}
+    rows = {k[4:]: z[k] for k in z.files if k.startswith("row_")}
+    return SimpleNamespace(edges=edges, tables=tabs, **geo), rows, z
+
+
+def test_substep_oracle_matches_the_reference_statistically():
+    L, rows, z = lookup_fixture()
+    R, S = len(rows["nsub"]), int(z["ref_seeds"])
+    counts, hist, total = np.zeros(R), np.zeros(64), 0
+    for s in range(S):
+        st, ch, tm, lim = O.substep_photons(L, rows, 500 + s)
+        assert not lim
+        ri = (st - 3) // 7
+        assert np.array_equal(ch, rows["chan"][ri])
+        counts += np.bincount(ri, minlength=R)
+        hist += np.bincount(np.clip((tm - rows["t0"][ri]).astype(np.int64), 0, 63), minlength=64)
+        total += len(st)
+    counts, hist = counts / S, hist / S
+    ref_counts, ref_hist, ref_total = z["ref_counts"], z["ref_delay_hist"], float(z["ref_total"]) / S
+    assert ref_total > 50000
+    assert abs(total / S / ref_total - 1) < 0.01
+    m = (ref_counts + counts) > 2
+    chi2 = np.mean((counts[m] - ref_counts[m]) ** 2 / ((counts[m] + ref_counts[m]) / S))
+    assert 0.8 < chi2 < 1.25
+    ks = np.max(np.abs(np.cumsum(hist) / hist.sum() - np.cumsum(ref_hist) / ref_hist.sum()))
+    assert ks < 0.01
+
+
+def test_substep_oracle_is_keyed():
+    """Rows give the same photons alone and in a batch (draws keyed by step, channel, substep, arrival)."""
+    L, rows, _ = lookup_fixture()
+    st, ch, tm, _ = O.substep_photons(L, rows, 9)
+    part = {k: v[100:140] for k, v in rows.items()}
+    st2, ch2, tm2, _ = O.substep_photons(L, part, 9)
+    sel = np.isin(st, part["step"])
+    assert sel.sum() == len(st2) > 0
+    assert np.array_equal(st[sel], st2) and np.array_equal(tm[sel], tm2)
+    st3, _, tm3, _ = O.substep_photons(L, rows, 10)
+    assert len(st3) != len(st) or not np.array_equal(tm3, tm)
+
+
+@pytest.mark.parametrize("n,p", [(10, 0.3), (1000, 0.002), (5000, 0.7), (100000, 0.01), (50, 0.999), (7, 1.0),
+                                 (0, 0.5), (12, 0.0)])
+def test_substep_binomial_moments(n, p):
+    x = O.binomial(17, np.full(40000, n), np.full(40000, p))
+    assert x.min() >= 0 and x.max() <= n
+    mean, var = n * p, n * p * (1 - p)
+    if var == 0:
+        assert np.all(x == mean)
+        return
+    assert abs(x.mean() - mean) < 5 * np.sqrt(var / len(x))
+    assert abs(x.var() / var - 1) < 0.05
