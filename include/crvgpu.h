@@ -20,6 +20,7 @@
  *                                                                                     (crv/crvfastsim/reco/coinc.py:289,
  *                                                                                      crv/crvfastsim/chain.py:296-362)
  *   crv_substep_photons              <- crvfastsim.response.photons._substep_photons   (crv/crvfastsim/response/photons.py:163)
+ *   crv_lookup_rows                  <- crvfastsim.response.photons.iter_rows          (crv/crvfastsim/response/photons.py:305)
  *   crv_chain                        <- the chain above in one resident call with explicit capacities, as the
  *                                       mixing adapter's resident CRV chain (mixing/device_crv.py:127-573,
  *                                       mixing/DEVICE_CRV.md "Explicit capacities")
@@ -419,15 +420,58 @@ typedef struct CrvLookup {
     int32_t pad;
     const double *cos_phi_edges; /* cos of the phi edges: phi bins are found on cos phi (no arccos per substep) */
     CrvLookupTable table[3];     /* scintillation, Cherenkov in scintillator, Cherenkov in fibre */
+    const double *cos_theta_edges; /* cos of the theta edges (rows that carry cos theta instead of theta) */
 } CrvLookup;
 
 /* Rows: local start s[3] and step vector d[3] (thickness, width, length; mm), start/end time, beta, theta, yield
  * deviation factor, optional extra attenuation per mm (NULL: none), substeps, step index, channel, and the photons per
- * substep of the three tables. */
+ * substep of the three tables; theta may be NULL when cos_theta is given (bins on the cos of the theta edges). */
 typedef struct CrvSubstepRows {
     const double *s, *d, *t0, *t1, *beta, *theta, *dev, *mu;
     const int64_t *nsub, *step, *chan, *n_scint, *n_ck_s, *n_ck_f;
+    const double *cos_theta;
 } CrvSubstepRows;
+
+/*
+ * Row preparation of the lookup-table model (photons.iter_rows, crv/crvfastsim/response/photons.py:292-356) for one
+ * (lookup table, reflector) group of sectors: per step of a bar in the group with finite start and end times, for each
+ * simulated SiPM (0..3 with reflector 0, else 0 and 2) a row: local start and step vector (z mirrored for reflector
+ * -1 and SiPMs 1, 3; y for SiPMs 2, 3), times with the extra delay k (z + half length), substeps of 0.1 mm, beta from
+ * the mean energy (stock), cos theta, the yield factor of channel 4 bar + s, the bar's extra attenuation, the output
+ * channel (4 bar + s, + 1 for reflector -1) and the photons per substep: rint(draw / nsub) of Gauss(avg, sqrt avg) for
+ * avg > 10 else Poisson(avg), avg = yield x edep (scintillation) and Cherenkov photons per mm x length, keyed by (seed,
+ * step, count type, channel).  Rows are written SiPM block by SiPM block, steps in order inside a block.
+ */
+typedef struct CrvLookupSteps {
+    const double *x0, *y0, *z0, *x1, *y1, *z1, *px0, *py0, *pz0, *p1, *t0, *t1, *edep, *len;
+    const int32_t *bar;
+    const int64_t *pdg;
+} CrvLookupSteps;
+
+typedef struct CrvLookupGroup {
+    const double *center;        /* [nbars][3] bar centre (Mu2e frame, mm) */
+    const int8_t *l2w;           /* [nbars][3] world axis of the local thickness, width and length axes */
+    const int32_t *in_group;     /* [nbars] 1 when the bar's sector is simulated with this group */
+    const double *yield;         /* [nbars] photons per MeV of the bar's sector */
+    const double *speed_k;       /* [nbars] extra delay per mm to the SiPM end (ns/mm) */
+    const double *mu;            /* [nbars] extra attenuation (1/mm) */
+    const double *dev;           /* [4 nbars] photon-yield factor per channel */
+    const double *ck_scint, *ck_fiber; /* [n][2] (beta, photons per mm), beta ascending */
+    const int64_t *pdg_code;     /* [npdg] ascending particle codes; ions (|code| >= 1e9) are decoded */
+    const double *pdg_mass, *pdg_charge;
+    double half_length;          /* of the group's table (mm) */
+    int32_t reflector, nbars, nck_scint, nck_fiber, npdg, pad;
+} CrvLookupGroup;
+
+typedef struct CrvSubstepRowsOut {
+    double *s, *d, *t0, *t1, *beta, *cos_theta, *dev, *mu;
+    int64_t *nsub, *step, *chan, *n_scint, *n_ck_s, *n_ck_f;
+} CrvSubstepRowsOut;
+
+int64_t crv_lookup_rows_workspace(int64_t nsteps);
+int crv_lookup_rows(const CrvLookupGroup *G, uint32_t seed, const CrvLookupSteps *st, int64_t nsteps,
+                    CrvSubstepRowsOut *out, int64_t cap, int64_t *n_rows_dev, void *workspace, int64_t workspace_bytes,
+                    void *stream, CrvStatus *status_dev);
 
 int64_t crv_substeps_workspace(int64_t nrows);
 /* Photons of every row, in (row, substep, table, arrival) order: step index, channel, arrival time (capacity cap;

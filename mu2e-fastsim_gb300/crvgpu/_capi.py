@@ -115,12 +115,31 @@ class CrvLookup(ctypes.Structure):
     _fields_ = [(k, c_f64) for k in ("half_thickness", "half_width", "half_length", "fiber_separation", "hole_radius_x",
                                      "hole_radius_y", "fiber_radius", "corner_radius", "fiber_decay_time")] + \
         [("edges", c_p * 7), ("nedges", c_i32 * 7), ("pad", c_i32), ("cos_phi_edges", c_p),
-         ("table", CrvLookupTable * 3)]
+         ("table", CrvLookupTable * 3), ("cos_theta_edges", c_p)]
 
 
 class CrvSubstepRows(ctypes.Structure):
     _fields_ = [(k, c_p) for k in ("s", "d", "t0", "t1", "beta", "theta", "dev", "mu", "nsub", "step", "chan",
-                                   "n_scint", "n_ck_s", "n_ck_f")]
+                                   "n_scint", "n_ck_s", "n_ck_f", "cos_theta")]
+
+
+LOOKUP_STEP_COLS = ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0", "p1", "t0", "t1", "edep", "len")
+LOOKUP_ROW_COLS = ("s", "d", "t0", "t1", "beta", "cos_theta", "dev", "mu", "nsub", "step", "chan", "n_scint", "n_ck_s",
+                   "n_ck_f")
+
+
+class CrvLookupSteps(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in LOOKUP_STEP_COLS + ("bar", "pdg")]
+
+
+class CrvLookupGroup(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("center", "l2w", "in_group", "yield_", "speed_k", "mu", "dev", "ck_scint",
+                                   "ck_fiber", "pdg_code", "pdg_mass", "pdg_charge")] + \
+        [("half_length", c_f64)] + [(k, c_i32) for k in ("reflector", "nbars", "nck_scint", "nck_fiber", "npdg", "pad")]
+
+
+class CrvSubstepRowsOut(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in LOOKUP_ROW_COLS]
 
 
 CHAIN_CAPS = ("events", "steps", "photons", "charges", "slots", "digis", "pulses", "max_steps_per_event")
@@ -171,6 +190,9 @@ _SIGS = {
                          c_i64, c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "crv_chain_workspace": (c_i64, [P(CrvParams), P(CrvChainCaps)]),
     "crv_substeps_workspace": (c_i64, [c_i64]),
+    "crv_lookup_rows_workspace": (c_i64, [c_i64]),
+    "crv_lookup_rows": (c_i32, [P(CrvLookupGroup), c_u32, P(CrvLookupSteps), c_i64, P(CrvSubstepRowsOut), c_i64, c_p,
+                                c_p, c_i64, c_p, c_p]),
     "crv_substep_photons": (c_i32, [P(CrvLookup), c_u32, P(CrvSubstepRows), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p,
                                     c_i64, c_p, c_p]),
     "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),

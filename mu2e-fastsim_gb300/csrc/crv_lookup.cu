@@ -187,6 +187,12 @@ __device__ __forceinline__ double arrival_time(const CrvLookup& L, uint32_t seed
   return tt;
 }
 
+// theta bin of a row: from theta, or from cos theta against the cos of the edges
+__device__ __forceinline__ int theta_bin(const CrvLookup& L, const CrvSubstepRows& R, long long r) {
+  return R.theta ? find_bin(L.edges[4], L.nedges[4], R.theta[r])
+                 : find_bin_cos(L.cos_theta_edges, L.nedges[4], R.cos_theta[r]);
+}
+
 __device__ __forceinline__ bool row_ok(const CrvSubstepRows& R, long long r, long long* nsub, Status* status) {
   *nsub = R.nsub[r];
   if (*nsub > SUB_MAX_SUBSTEPS) {
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count(CrvLo
     if (row_ok(R, r, &nsub, status)) {
       const long long step = R.step[r], chan = R.chan[r];
       const int bb = find_bin(L.edges[3], L.nedges[3], R.beta[r]);
-      const int bth = find_bin(L.edges[4], L.nedges[4], R.theta[r]);
+      const int bth = theta_bin(L, R, r);
       for (long long k = lane_id(); k < nsub; k += 32) {
         const SubBins S = substep_bins(L, R, r, k, nsub, bb, bth);
         for (int tb = 0; tb < 3; ++tb)
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLoo
     if (!row_ok(R, r, &nsub, status)) continue;               // warp-uniform
     const long long step = R.step[r], chan = R.chan[r];
     const int bb = find_bin(L.edges[3], L.nedges[3], R.beta[r]);
-    const int bth = find_bin(L.edges[4], L.nedges[4], R.theta[r]);
+    const int bth = theta_bin(L, R, r);
     long long o = offset[r];
     for (long long k0 = 0; k0 < nsub; k0 += 32) {
       const long long k = k0 + lane_id();
@@ -329,9 +335,10 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
     if (cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s) != cudaSuccess) return CRV_ERR_CUDA;
     return CRV_OK;
   }
-  if (!rows->s || !rows->d || !rows->t0 || !rows->t1 || !rows->beta || !rows->theta || !rows->dev || !rows->nsub ||
-      !rows->step || !rows->chan || !rows->n_scint || !rows->n_ck_s || !rows->n_ck_f)
+  if (!rows->s || !rows->d || !rows->t0 || !rows->t1 || !rows->beta || !rows->dev || !rows->nsub || !rows->step ||
+      !rows->chan || !rows->n_scint || !rows->n_ck_s || !rows->n_ck_f)
     return CRV_ERR_ARG;
+  if (!rows->theta && (!rows->cos_theta || !L->cos_theta_edges)) return CRV_ERR_ARG;
   size_t need = 0;
   sub_layout(nullptr, nrows, &need);
   if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
@@ -359,4 +366,218 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
   }
   if (cudaGetLastError() != cudaSuccess) return CRV_ERR_CUDA;
   return CRV_OK;
+}
+
+// ---- row preparation (photons.iter_rows) -----------------------------------------------------------------------------
+
+namespace crv {
+
+constexpr uint32_t ST_LROWS = 8;
+constexpr double LROW_PRECISION_MM = 0.1;
+constexpr double AMU_MEV = 931.49410242;       // atomic mass unit (CODATA 2018)
+
+// mass [MeV] and charge [e] of a particle code: table lookup, ions 100ZZZAAAI decoded, unknown (0, 0)
+__device__ __forceinline__ void particle(const CrvLookupGroup& G, long long pdg, double* m, double* q) {
+  int lo = 0, hi = G.npdg;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (G.pdg_code[mid] < pdg) lo = mid + 1; else hi = mid;
+  }
+  if (lo < G.npdg && G.pdg_code[lo] == pdg) {
+    *m = G.pdg_mass[lo];
+    *q = G.pdg_charge[lo];
+    return;
+  }
+  const long long a = pdg < 0 ? -pdg : pdg;
+  if (a >= 1000000000ll) {
+    *m = double((a / 10) % 1000) * AMU_MEV;
+    *q = double((a / 10000) % 1000) * (pdg < 0 ? -1.0 : 1.0);
+  } else {
+    *m = 0.0;
+    *q = 0.0;
+  }
+}
+
+// Cherenkov photons per mm: linear in beta from (0, 0) through the map, flat beyond its end, times |charge|
+__device__ __forceinline__ double cerenkov_per_mm(const double* __restrict__ map, int n, double beta, double q) {
+  double x0 = 0.0, y0 = 0.0, v;
+  int j = 0;
+  while (j < n && map[2 * j] <= beta) { x0 = map[2 * j]; y0 = map[2 * j + 1]; ++j; }
+  if (beta < 0.0) v = 0.0;
+  else if (j == n) v = n > 0 ? map[2 * (n - 1) + 1] : 0.0;
+  else v = (map[2 * j + 1] - y0) / (map[2 * j] - x0) * (beta - x0) + y0;
+  return v * fabs(q);
+}
+
+// photons per substep: rint(draw / nsub) of Gauss(avg, sqrt avg) for avg > 10, else Poisson(avg) by inversion
+__device__ __forceinline__ long long per_substep(double avg, long long nsub, const U4& w) {
+  double x;
+  if (avg > 10.0) {
+    double z0, z1;
+    Math<double>::normal_pair(w, &z0, &z1);
+    x = avg + sqrt(avg) * z0;
+  } else {
+    const double lam = avg > 0.0 ? avg : 0.0;
+    const double u = u01(w.x, w.y);
+    double p = dexp(-lam), F = p;
+    int k = 0;
+    while (u >= F && k < 200) {
+      k += 1;
+      p = p * lam / double(k);
+      F = F + p;
+    }
+    x = double(k);
+  }
+  const double n = rint(x / double(nsub));
+  return n > 0.0 ? (long long)n : 0;
+}
+
+__device__ __forceinline__ bool in_lgroup(const CrvLookupGroup& G, const CrvLookupSteps& S, long long i) {
+  const int b = S.bar[i];
+  return b >= 0 && b < G.nbars && G.in_group[b] && isfinite(S.t0[i]) && isfinite(S.t1[i]);
+}
+
+__global__ void k_lrows_flag(CrvLookupGroup G, CrvLookupSteps S, long long n, int32_t* __restrict__ flag) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    flag[i] = in_lgroup(G, S, i) ? 1 : 0;
+}
+
+__global__ void k_lrows_fill(CrvLookupGroup G, CrvLookupSteps S, uint32_t seed, long long n,
+                             const long long* __restrict__ rank, const long long* __restrict__ total,
+                             CrvSubstepRowsOut O) {
+  const long long ng = *total;
+  const int nsim = G.reflector == 0 ? 4 : 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (!in_lgroup(G, S, i)) continue;
+    const int b = S.bar[i];
+    const double* c = G.center + 3 * b;
+    const double ws[3] = {S.x0[i] - c[0], S.y0[i] - c[1], S.z0[i] - c[2]};
+    const double we[3] = {S.x1[i] - c[0], S.y1[i] - c[1], S.z1[i] - c[2]};
+    double sl[3], el[3];
+    for (int k = 0; k < 3; ++k) {
+      const int ax = G.l2w[3 * b + k];
+      sl[k] = ws[ax];
+      el[k] = we[ax];
+    }
+    if (G.reflector < 0) { sl[2] = -sl[2]; el[2] = -el[2]; }
+    double m, q;
+    particle(G, S.pdg[i], &m, &q);
+    const double p0 = sqrt(S.px0[i] * S.px0[i] + S.py0[i] * S.py0[i] + S.pz0[i] * S.pz0[i]);
+    const double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(S.p1[i] * S.p1[i] + m * m));
+    double beta = 1.0;
+    if (m > 0.0) {
+      const double g = e / m;
+      double b2 = 1.0 - 1.0 / (g * g);
+      b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
+      beta = sqrt(b2);
+    }
+    const double avg_s = G.yield[b] * S.edep[i];
+    const double avg_cs = cerenkov_per_mm(G.ck_scint, G.nck_scint, beta, q) * S.len[i];
+    const double avg_cf = cerenkov_per_mm(G.ck_fiber, G.nck_fiber, beta, q) * S.len[i];
+    const double k = G.speed_k[b];
+    const long long r0 = rank[i];
+    for (int si = 0; si < nsim; ++si) {
+      const int s = G.reflector == 0 ? si : 2 * si;
+      double a[3] = {sl[0], sl[1], sl[2]}, bb[3] = {el[0], el[1], el[2]};
+      if (s == 1 || s == 3) { a[2] = -a[2]; bb[2] = -bb[2]; }
+      if (s == 2 || s == 3) { a[1] = -a[1]; bb[1] = -bb[1]; }
+      const double d[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
+      const double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      double ct = 1.0;
+      if (dl > 0.0) {
+        ct = d[2] / dl;
+        ct = ct < -1.0 ? -1.0 : (ct > 1.0 ? 1.0 : ct);
+      }
+      long long nsub = (long long)(dl / LROW_PRECISION_MM);
+      nsub = nsub > 1 ? nsub : 1;
+      const long long chan_dev = 4ll * b + s;
+      const long long o = (long long)si * ng + r0;
+      for (int x = 0; x < 3; ++x) {
+        O.s[3 * o + x] = a[x];
+        O.d[3 * o + x] = d[x];
+      }
+      O.t0[o] = S.t0[i] + k * (a[2] + G.half_length);
+      O.t1[o] = S.t1[i] + k * (bb[2] + G.half_length);
+      O.nsub[o] = nsub;
+      O.beta[o] = beta;
+      O.cos_theta[o] = ct;
+      O.dev[o] = G.dev[chan_dev];
+      O.mu[o] = G.mu[b];
+      O.step[o] = i;
+      O.chan[o] = 4ll * b + (G.reflector < 0 ? s + 1 : s);
+      const uint32_t lo = uint32_t(i), hi = uint32_t((unsigned long long)i >> 32);
+      O.n_scint[o] = per_substep(avg_s, nsub, philox(lo, hi, w2_of(ST_LROWS, 0, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+      O.n_ck_s[o] = per_substep(avg_cs, nsub, philox(lo, hi, w2_of(ST_LROWS, 1, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+      O.n_ck_f[o] = per_substep(avg_cf, nsub, philox(lo, hi, w2_of(ST_LROWS, 2, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+    }
+  }
+}
+
+__global__ void k_lrows_count(const long long* __restrict__ total, int nsim, long long* __restrict__ n_rows) {
+  *n_rows = *total * nsim;
+}
+
+}  // namespace crv
+
+extern "C" int64_t crv_lookup_rows_workspace(int64_t nsteps) {
+  if (nsteps < 0) return -1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { off = ((off + 255) & ~size_t(255)) + (bytes ? bytes : 1); };
+  take(sizeof(int32_t) * nsteps);
+  take(sizeof(long long) * nsteps);
+  take(sizeof(long long) * (scan_parts_len(nsteps) + 1));
+  take(sizeof(long long));
+  return (int64_t)(off + 512);
+}
+
+extern "C" int crv_lookup_rows(const CrvLookupGroup* G, uint32_t seed, const CrvLookupSteps* st, int64_t nsteps,
+                               CrvSubstepRowsOut* out, int64_t cap, int64_t* n_rows_dev, void* workspace,
+                               int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (!G || !st || !out || !n_rows_dev || !status_dev || nsteps < 0) return CRV_ERR_ARG;
+  if (G->reflector < -1 || G->reflector > 1 || G->nbars < 1 || G->npdg < 0 || G->nck_scint < 0 || G->nck_fiber < 0)
+    return CRV_ERR_ARG;
+  if (!G->center || !G->l2w || !G->in_group || !G->yield || !G->speed_k || !G->mu || !G->dev ||
+      (G->nck_scint && !G->ck_scint) || (G->nck_fiber && !G->ck_fiber) ||
+      (G->npdg && (!G->pdg_code || !G->pdg_mass || !G->pdg_charge)))
+    return CRV_ERR_ARG;
+  const int nsim = G->reflector == 0 ? 4 : 2;
+  if (cap < nsim * nsteps) return CRV_ERR_ARG;                 // every step of the group gives nsim rows
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nsteps == 0) return cudaMemsetAsync(n_rows_dev, 0, sizeof(long long), s) == cudaSuccess ? CRV_OK : CRV_ERR_CUDA;
+  if (!st->x0 || !st->y0 || !st->z0 || !st->x1 || !st->y1 || !st->z1 || !st->px0 || !st->py0 || !st->pz0 ||
+      !st->p1 || !st->t0 || !st->t1 || !st->edep || !st->len || !st->bar || !st->pdg)
+    return CRV_ERR_ARG;
+  if (!out->s || !out->d || !out->t0 || !out->t1 || !out->beta || !out->cos_theta || !out->dev || !out->mu ||
+      !out->nsub || !out->step || !out->chan || !out->n_scint || !out->n_ck_s || !out->n_ck_f)
+    return CRV_ERR_ARG;
+  if (crv_lookup_rows_workspace(nsteps) > workspace_bytes || !workspace) return CRV_ERR_ARG;
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    off = (off + 255) & ~size_t(255);
+    char* p = base + off;
+    off += bytes ? bytes : 1;
+    return p;
+  };
+  int32_t* flag = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * nsteps));
+  long long* rank = reinterpret_cast<long long*>(take(sizeof(long long) * nsteps));
+  long long* parts = reinterpret_cast<long long*>(take(sizeof(long long) * (scan_parts_len(nsteps) + 1)));
+  long long* total = reinterpret_cast<long long*>(take(sizeof(long long)));
+  const long long blocks = (nsteps + 255) / 256, maxb = (long long)device_info().sms * 8;
+  const unsigned grid = (unsigned)(blocks < maxb ? blocks : maxb);
+  {
+    crv::Mark mark_("k_lrows_flag", s);
+    k_lrows_flag<<<grid, 256, 0, s>>>(*G, *st, nsteps, flag);
+  }
+  if (exclusive_scan(flag, nsteps, Identity(), rank, total, parts, s) != cudaSuccess) return CRV_ERR_CUDA;
+  {
+    crv::Mark mark_("k_lrows_fill", s);
+    k_lrows_fill<<<grid, 256, 0, s>>>(*G, *st, seed, nsteps, rank, total, *out);
+  }
+  {
+    crv::Mark mark_("k_lrows_count", s);
+    k_lrows_count<<<1, 1, 0, s>>>(total, nsim, reinterpret_cast<long long*>(n_rows_dev));
+  }
+  (void)status_dev;
+  return cudaGetLastError() == cudaSuccess ? CRV_OK : CRV_ERR_CUDA;
 }

@@ -651,11 +651,13 @@ typedef struct {
     int32_t pad;
     const double *cos_phi_edges;
     OrcLookupTable table[3];
+    const double *cos_theta_edges;
 } OrcLookup;
 
 typedef struct {
     const double *s, *d, *t0, *t1, *beta, *theta, *dev, *mu;
     const int64_t *nsub, *step, *chan, *n_scint, *n_ck_s, *n_ck_f;
+    const double *cos_theta;
 } OrcSubstepRows;
 
 static inline void sub_block(uint32_t seed, int64_t step, int64_t chan, int tb, int call, int idx, int64_t k, int j,
@@ -820,7 +822,8 @@ int64_t orc_substep_photons(const OrcLookup *L, uint32_t seed, const OrcSubstepR
         if (nsub > SUB_MAX_SUBSTEPS) { *limit = 1; continue; }
         if (nsub <= 0) continue;
         int bb = sub_find_bin(L->edges[3], L->nedges[3], R->beta[r]);
-        int bth = sub_find_bin(L->edges[4], L->nedges[4], R->theta[r]);
+        int bth = R->theta ? sub_find_bin(L->edges[4], L->nedges[4], R->theta[r])
+                           : sub_find_bin_cos(L->cos_theta_edges, L->nedges[4], R->cos_theta[r]);
         for (int64_t k = 0; k < nsub; ++k) {
             int bin[3];
             double t, z;
@@ -848,4 +851,140 @@ void orc_binomial_v(uint32_t seed, int64_t cnt, const int64_t *n, const double *
         sub_block(seed, i, 0, 0, SUB_CALL_BINOMIAL, 0, 0, 0, w);
         out[i] = sub_binomial(n[i], p[i], w);
     }
+}
+
+/* Row preparation of the lookup-table model (photons.iter_rows, crv/crvfastsim/response/photons.py:292-356) for one
+ * (table, reflector) group, with keyed per-substep counts; rows SiPM block by SiPM block, steps in order. */
+enum { ST_LROWS = 8 };
+#define AMU_MEV 931.49410242
+
+typedef struct {
+    const double *x0, *y0, *z0, *x1, *y1, *z1, *px0, *py0, *pz0, *p1, *t0, *t1, *edep, *len;
+    const int32_t *bar;
+    const int64_t *pdg;
+} OrcLookupSteps;
+
+typedef struct {
+    const double *center;
+    const int8_t *l2w;
+    const int32_t *in_group;
+    const double *yield, *speed_k, *mu, *dev, *ck_scint, *ck_fiber;
+    const int64_t *pdg_code;
+    const double *pdg_mass, *pdg_charge;
+    double half_length;
+    int32_t reflector, nbars, nck_scint, nck_fiber, npdg, pad;
+} OrcLookupGroup;
+
+static void lrow_particle(const OrcLookupGroup *G, int64_t pdg, double *m, double *q) {
+    int lo = 0, hi = G->npdg;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (G->pdg_code[mid] < pdg) lo = mid + 1; else hi = mid;
+    }
+    if (lo < G->npdg && G->pdg_code[lo] == pdg) { *m = G->pdg_mass[lo]; *q = G->pdg_charge[lo]; return; }
+    int64_t a = pdg < 0 ? -pdg : pdg;
+    if (a >= 1000000000ll) {
+        *m = (double)((a / 10) % 1000) * AMU_MEV;
+        *q = (double)((a / 10000) % 1000) * (pdg < 0 ? -1.0 : 1.0);
+    } else {
+        *m = 0.0;
+        *q = 0.0;
+    }
+}
+
+static double lrow_cerenkov(const double *map, int n, double beta, double q) {
+    double x0 = 0.0, y0 = 0.0, v;
+    int j = 0;
+    while (j < n && map[2 * j] <= beta) { x0 = map[2 * j]; y0 = map[2 * j + 1]; ++j; }
+    if (beta < 0.0) v = 0.0;
+    else if (j == n) v = n > 0 ? map[2 * (n - 1) + 1] : 0.0;
+    else v = (map[2 * j + 1] - y0) / (map[2 * j] - x0) * (beta - x0) + y0;
+    return v * fabs(q);
+}
+
+static int64_t lrow_per_substep(double avg, int64_t nsub, const uint32_t w[4]) {
+    double x;
+    if (avg > 10.0) {
+        double z0, z1;
+        normal_pair(w, &z0, &z1);
+        x = avg + sqrt(avg) * z0;
+    } else {
+        x = (double)poisson_inv(avg > 0.0 ? avg : 0.0, u01(w[0], w[1]));
+    }
+    double n = rint(x / (double)nsub);
+    return n > 0.0 ? (int64_t)n : 0;
+}
+
+/* Returns the number of rows written (nsim x steps of the group). */
+int64_t orc_lookup_rows(const OrcLookupGroup *G, uint32_t seed, const OrcLookupSteps *S, int64_t nsteps, double *o_s,
+                        double *o_d, double *o_t0, double *o_t1, double *o_beta, double *o_ct, double *o_dev,
+                        double *o_mu, int64_t *o_nsub, int64_t *o_step, int64_t *o_chan, int64_t *o_ns,
+                        int64_t *o_ncs, int64_t *o_ncf) {
+    int nsim = G->reflector == 0 ? 4 : 2;
+    int64_t ng = 0;
+    for (int64_t i = 0; i < nsteps; ++i) {
+        int b = S->bar[i];
+        if (b >= 0 && b < G->nbars && G->in_group[b] && isfinite(S->t0[i]) && isfinite(S->t1[i])) ++ng;
+    }
+    int64_t r0 = 0;
+    for (int64_t i = 0; i < nsteps; ++i) {
+        int b = S->bar[i];
+        if (!(b >= 0 && b < G->nbars && G->in_group[b] && isfinite(S->t0[i]) && isfinite(S->t1[i]))) continue;
+        const double *c = G->center + 3 * b;
+        double ws[3] = {S->x0[i] - c[0], S->y0[i] - c[1], S->z0[i] - c[2]};
+        double we[3] = {S->x1[i] - c[0], S->y1[i] - c[1], S->z1[i] - c[2]};
+        double sl[3], el[3];
+        for (int k = 0; k < 3; ++k) { int ax = G->l2w[3 * b + k]; sl[k] = ws[ax]; el[k] = we[ax]; }
+        if (G->reflector < 0) { sl[2] = -sl[2]; el[2] = -el[2]; }
+        double m, q;
+        lrow_particle(G, S->pdg[i], &m, &q);
+        double p0 = sqrt(S->px0[i] * S->px0[i] + S->py0[i] * S->py0[i] + S->pz0[i] * S->pz0[i]);
+        double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(S->p1[i] * S->p1[i] + m * m));
+        double beta = 1.0;
+        if (m > 0.0) {
+            double g = e / m;
+            double b2 = 1.0 - 1.0 / (g * g);
+            b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
+            beta = sqrt(b2);
+        }
+        double avg_s = G->yield[b] * S->edep[i];
+        double avg_cs = lrow_cerenkov(G->ck_scint, G->nck_scint, beta, q) * S->len[i];
+        double avg_cf = lrow_cerenkov(G->ck_fiber, G->nck_fiber, beta, q) * S->len[i];
+        double k = G->speed_k[b];
+        for (int si = 0; si < nsim; ++si) {
+            int s = G->reflector == 0 ? si : 2 * si;
+            double a[3] = {sl[0], sl[1], sl[2]}, bb[3] = {el[0], el[1], el[2]};
+            if (s == 1 || s == 3) { a[2] = -a[2]; bb[2] = -bb[2]; }
+            if (s == 2 || s == 3) { a[1] = -a[1]; bb[1] = -bb[1]; }
+            double d[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
+            double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            double ct = 1.0;
+            if (dl > 0.0) { ct = d[2] / dl; ct = ct < -1.0 ? -1.0 : (ct > 1.0 ? 1.0 : ct); }
+            int64_t nsub = (int64_t)(dl / 0.1);
+            nsub = nsub > 1 ? nsub : 1;
+            int64_t chan_dev = 4ll * b + s;
+            int64_t o = (int64_t)si * ng + r0;
+            for (int x = 0; x < 3; ++x) { o_s[3 * o + x] = a[x]; o_d[3 * o + x] = d[x]; }
+            o_t0[o] = S->t0[i] + k * (a[2] + G->half_length);
+            o_t1[o] = S->t1[i] + k * (bb[2] + G->half_length);
+            o_nsub[o] = nsub;
+            o_beta[o] = beta;
+            o_ct[o] = ct;
+            o_dev[o] = G->dev[chan_dev];
+            o_mu[o] = G->mu[b];
+            o_step[o] = i;
+            o_chan[o] = 4ll * b + (G->reflector < 0 ? s + 1 : s);
+            uint32_t w[4];
+            uint32_t ctr[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0, 0};
+            uint32_t key[2] = {seed, 0u};
+            ctr[2] = w2_of(ST_LROWS, 0, 0, 0, (int)chan_dev); orc_philox(ctr, key, w);
+            o_ns[o] = lrow_per_substep(avg_s, nsub, w);
+            ctr[2] = w2_of(ST_LROWS, 1, 0, 0, (int)chan_dev); orc_philox(ctr, key, w);
+            o_ncs[o] = lrow_per_substep(avg_cs, nsub, w);
+            ctr[2] = w2_of(ST_LROWS, 2, 0, 0, (int)chan_dev); orc_philox(ctr, key, w);
+            o_ncf[o] = lrow_per_substep(avg_cf, nsub, w);
+        }
+        ++r0;
+    }
+    return nsim * ng;
 }

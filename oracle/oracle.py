@@ -1047,12 +1047,12 @@ class _OrcLookup(ctypes.Structure):
                                                "hole_radius_x", "hole_radius_y", "fiber_radius", "corner_radius",
                                                "fiber_decay_time")] + \
         [("edges", ctypes.c_void_p * 7), ("nedges", ctypes.c_int32 * 7), ("pad", ctypes.c_int32),
-         ("cos_phi_edges", ctypes.c_void_p), ("table", _OrcLookupTable * 3)]
+         ("cos_phi_edges", ctypes.c_void_p), ("table", _OrcLookupTable * 3), ("cos_theta_edges", ctypes.c_void_p)]
 
 
 class _OrcRows(ctypes.Structure):
     _fields_ = [(k, ctypes.c_void_p) for k in ("s", "d", "t0", "t1", "beta", "theta", "dev", "mu", "nsub", "step",
-                                               "chan", "n_scint", "n_ck_s", "n_ck_f")]
+                                               "chan", "n_scint", "n_ck_s", "n_ck_f", "cos_theta")]
 
 
 def _lookup_struct(L, k):
@@ -1064,6 +1064,7 @@ def _lookup_struct(L, k):
         S.edges[i] = k(L.edges[e], np.float64)
         S.nedges[i] = len(L.edges[e])
     S.cos_phi_edges = k(np.cos(np.asarray(L.edges["phi"], np.float64)), np.float64)
+    S.cos_theta_edges = k(np.cos(np.asarray(L.edges["theta"], np.float64)), np.float64)
     for i, name in enumerate(LOOKUP_TABLES):
         T = L.tables[name]
         d, e = np.asarray(T.delays, np.uint8), np.asarray(T.emis, np.uint8)
@@ -1080,11 +1081,13 @@ def substep_photons(L, rows, seed):
     S = _lookup_struct(L, k)
     n = len(rows["nsub"])
     mu = rows.get("mu")
+    th = rows.get("theta")
     R = _OrcRows(k(rows["s"], np.float64), k(rows["d"], np.float64), k(rows["t0"], np.float64),
-                 k(rows["t1"], np.float64), k(rows["beta"], np.float64), k(rows["theta"], np.float64),
+                 k(rows["t1"], np.float64), k(rows["beta"], np.float64), None if th is None else k(th, np.float64),
                  k(rows["dev"], np.float64), None if mu is None else k(mu, np.float64), k(rows["nsub"], np.int64),
                  k(rows["step"], np.int64), k(rows["chan"], np.int64), k(rows["n_scint"], np.int64),
-                 k(rows["n_ck_s"], np.int64), k(rows["n_ck_f"], np.int64))
+                 k(rows["n_ck_s"], np.int64), k(rows["n_ck_f"], np.int64),
+                 None if th is not None else k(rows["cos_theta"], np.float64))
     f = lib().orc_substep_photons
     f.restype = ctypes.c_int64
     lim = ctypes.c_int(0)
@@ -1104,3 +1107,144 @@ def binomial(seed, n, p):
     out = np.zeros(len(n), np.int64)
     lib().orc_binomial_v(ctypes.c_uint32(seed), ctypes.c_int64(len(n)), _p(n), _p(p), _p(out))
     return out
+
+
+class _OrcLookupSteps(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0", "p1", "t0",
+                                               "t1", "edep", "len", "bar", "pdg")]
+
+
+class _OrcLookupGroup(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("center", "l2w", "in_group", "yield_", "speed_k", "mu", "dev",
+                                               "ck_scint", "ck_fiber", "pdg_code", "pdg_mass", "pdg_charge")] + \
+        [("half_length", ctypes.c_double)] + [(k, ctypes.c_int32) for k in ("reflector", "nbars", "nck_scint",
+                                                                             "nck_fiber", "npdg", "pad")]
+
+
+ROW_KEYS = ("s", "d", "t0", "t1", "beta", "cos_theta", "dev", "mu", "nsub", "step", "chan", "n_scint", "n_ck_s",
+            "n_ck_f")
+
+
+def lookup_rows(group, steps, seed):
+    """Rows of one (table, reflector) group (photons.iter_rows with keyed per-substep counts).  group: dict of the
+    group arrays (center [nb, 3], l2w [nb, 3], in_group, yield, speed_k, mu, dev [4 nb], ck_scint [n, 2], ck_fiber,
+    pdg_code, pdg_mass, pdg_charge, half_length, reflector); steps: dict of the step columns (x0 .. z1, px0, py0, pz0,
+    p1, t0, t1, edep, len, bar, pdg).  Returns the row dict (cos_theta in place of theta)."""
+    k = _Keep()
+    G = _OrcLookupGroup(k(group["center"], np.float64), k(group["l2w"], np.int8), k(group["in_group"], np.int32),
+                        k(group["yield"], np.float64), k(group["speed_k"], np.float64), k(group["mu"], np.float64),
+                        k(group["dev"], np.float64), k(group["ck_scint"], np.float64), k(group["ck_fiber"], np.float64),
+                        k(group["pdg_code"], np.int64), k(group["pdg_mass"], np.float64),
+                        k(group["pdg_charge"], np.float64), float(group["half_length"]), int(group["reflector"]),
+                        len(group["in_group"]), len(group["ck_scint"]), len(group["ck_fiber"]), len(group["pdg_code"]),
+                        0)
+    n = len(steps["bar"])
+    cols = [k(steps[c], np.float64) for c in ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0", "p1", "t0",
+                                              "t1", "edep", "len")]
+    S = _OrcLookupSteps(*cols, k(steps["bar"], np.int32), k(steps["pdg"], np.int64))
+    cap = (4 if int(group["reflector"]) == 0 else 2) * n
+    out = {key: np.zeros((cap, 3) if key in ("s", "d") else cap,
+                         np.int64 if key in ("nsub", "step", "chan", "n_scint", "n_ck_s", "n_ck_f") else np.float64)
+           for key in ROW_KEYS}
+    f = lib().orc_lookup_rows
+    f.restype = ctypes.c_int64
+    m = f(ctypes.byref(G), ctypes.c_uint32(seed), ctypes.byref(S), ctypes.c_int64(n), *[_p(out[key]) for key in ROW_KEYS])
+    return {key: v[:m] for key, v in out.items()}
+
+
+# photons.make_photons with lookup tables: host part of photons.iter_rows (crv/crvfastsim/response/photons.py:230-356)
+
+_PARTICLES = {11: (0.51099895, -1), -11: (0.51099895, 1), 13: (105.6583755, -1), -13: (105.6583755, 1),
+              22: (0.0, 0), 211: (139.57039, 1), -211: (139.57039, -1), 111: (134.9768, 0), 321: (493.677, 1),
+              -321: (493.677, -1), 130: (497.611, 0), 310: (497.611, 0), 2212: (938.272088, 1),
+              -2212: (938.272088, -1), 2112: (939.565420, 0), -2112: (939.565420, 0), 12: (0.0, 0), -12: (0.0, 0),
+              14: (0.0, 0), -14: (0.0, 0), 3122: (1115.683, 0), 3222: (1189.37, 1), 3112: (1197.449, -1)}
+
+
+def table_propagation(L):
+    """photons.table_propagation (photons.py:230-254): inverse signal speed from the 10 % delay quantile against the
+    distance to the SiPM end, attenuation length from the log of the summed probability."""
+    E, T = L.edges, L.tables["scint"]
+    nx, ny, nz = len(E["x"]) - 1, len(E["y"]) - 1, len(E["z"]) - 1
+    p = np.asarray(T.prob, np.float64)[:nx * ny * nz].reshape(nx, ny, nz)
+    ds = np.asarray(T.delay_sum, np.float64)[:nx * ny * nz].reshape(nx, ny, nz)
+    w = np.where(ds > 0, p / np.where(ds > 0, ds, 1.0), 0.0)
+    h = np.einsum("xyz,xyzj->zj", w, np.asarray(T.delays, np.float64)[:nx * ny * nz].reshape(nx, ny, nz, -1))
+    d = 0.5 * (np.asarray(E["z"])[1:] + np.asarray(E["z"])[:-1]) + L.half_length
+    tot = h.sum(1)
+    ok = tot > 0
+    q = np.argmax(np.cumsum(h, 1) >= 0.1 * tot[:, None], axis=1)
+    inv_v = np.polyfit(d[ok], q[ok].astype(float), 1)[0]
+    P = p.sum((0, 1))
+    a = (P > 0) & (d > 0.2 * L.half_length) & (d < 1.8 * L.half_length)
+    return float(inv_v), float(-1.0 / np.polyfit(d[a], np.log(P[a]), 1)[0])
+
+
+def bar_ratios(values, geom):
+    """photons.bar_ratios (photons.py:257-289)."""
+    out = np.ones(geom.nbars)
+    if not values:
+        return out
+    names = np.array(geom.sector_names, dtype=object)
+    nmod = np.zeros(len(names), np.int64)
+    np.maximum.at(nmod, np.asarray(geom.sector), np.asarray(geom.module) + 1)
+    sk = names[np.asarray(geom.sector)]
+    mk = np.where(nmod[np.asarray(geom.sector)] > 1, sk + np.asarray(geom.module).astype(str).astype(object), sk)
+    tag = np.array([str(n).startswith("M") for n in sk])
+    for k, v in values.items():
+        if k == "TAG":
+            out[tag] = v
+    for k, v in values.items():
+        if k != "TAG" and k in set(sk):
+            out[sk == k] = v
+    for k, v in values.items():
+        if k in set(mk) and k not in set(sk):
+            out[mk == k] = v
+    return out
+
+
+def lookup_groups(geom, cfg, tables, deviation):
+    """[(table, group arrays)] in photons.iter_rows' order (table names sorted, reflectors sorted)."""
+    names = list(geom.sector_names)
+    sec = np.asarray(geom.sector)
+    nb = int(geom.nbars)
+    r_speed, r_atten = bar_ratios(cfg.speed_ratio, geom), bar_ratios(cfg.atten_ratio, geom)
+    dev = (np.asarray(deviation, np.float64) * cfg.photon_yield_variation_scale + 1.0) * cfg.photon_yield_scale
+    codes = np.array(sorted(_PARTICLES), np.int64)
+    yields = np.array([float(cfg.sectors[n].yield_per_mev) for n in names])
+    out = []
+    for tname in sorted({cfg.sectors[n].table for n in names}):
+        L = tables[tname]
+        inv_v, att = table_propagation(L)
+        for refl in sorted({int(cfg.sectors[n].reflector) for n in names if cfg.sectors[n].table == tname}):
+            sids = [i for i, n in enumerate(names) if cfg.sectors[n].table == tname
+                    and int(cfg.sectors[n].reflector) == refl]
+            g = dict(center=np.asarray(geom.center, np.float64).reshape(nb, 3),
+                     l2w=np.asarray(geom.local_to_world, np.int8).reshape(nb, 3),
+                     in_group=np.isin(sec, sids).astype(np.int32), yield_=yields[sec],
+                     speed_k=inv_v * (1.0 / r_speed - 1.0), mu=(1.0 / r_atten - 1.0) / att, dev=dev,
+                     ck_scint=np.asarray(L.ck_scint, np.float64).reshape(-1, 2),
+                     ck_fiber=np.asarray(L.ck_fiber, np.float64).reshape(-1, 2), pdg_code=codes,
+                     pdg_mass=np.array([_PARTICLES[c][0] for c in codes]),
+                     pdg_charge=np.array([_PARTICLES[c][1] for c in codes], np.float64),
+                     half_length=float(L.half_length), reflector=refl)
+            g["yield"] = g.pop("yield_")
+            out.append((L, g))
+    return out
+
+
+def make_photons_lookup(steps, pdg, geom, cfg, tables, deviation, seed):
+    """(step, channel, time) of photons.make_photons with lookup tables and keyed draws: rows per group, then the
+    substep photons of each group's rows."""
+    cols = {k: np.asarray(steps[k], np.float64) for k in ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0",
+                                                          "p1", "t0", "t1", "edep", "len")}
+    cols["bar"] = np.asarray(steps["bar"], np.int32)
+    cols["pdg"] = np.asarray(pdg, np.int64)
+    outs = []
+    for L, g in lookup_groups(geom, cfg, tables, deviation):
+        rows = lookup_rows(g, cols, seed)
+        if len(rows["nsub"]):
+            outs.append(substep_photons(L, rows, seed)[:3])
+    if not outs:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0)
+    return tuple(np.concatenate([o[i] for o in outs]) for i in range(3))

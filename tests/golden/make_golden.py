@@ -18,6 +18,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   lookup.npz     a synthetic lookup table and (step, SiPM) rows with the statistics of the reference substep kernel
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram
+  lookup_chain.npz  make_photons with two synthetic tables (reflector 0 and 1) on a two-sector geometry
+                 (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, and over 16 seeds
+                 the mean photons per (step, channel) and the arrival-delay histogram
 """
 import os
 import sys
@@ -408,6 +411,24 @@ def synthetic_lookup(rng, decay_time=7.4):
     return edges, tabs, geo
 
 
+def shaped_lookup(rng, decay_time=3.0):
+    """synthetic_lookup with light propagation built in: arrival probabilities fall off as exp(-d / 1500 mm) and the
+    delay weights peak 6 ns/m later with the distance d to the SiPM end (so the reference's propagation fits apply)."""
+    edges, tabs, geo = synthetic_lookup(rng, decay_time)
+    zc = 0.5 * (edges["z"][1:] + edges["z"][:-1]) + geo["half_length"]
+    for name, T in tabs.items():
+        n, D = T["delays"].shape
+        nz = len(zc)
+        zi = np.arange(n) % nz if name != "ckfiber" else np.arange(n) % nz
+        T["prob"] = (T["prob"] * np.exp(-zc[zi] / 1500.0)).astype(np.float32)
+        peak = np.clip(np.rint(2 + 0.006 * zc[zi]).astype(np.int64), 0, D - 1)
+        w = rng.integers(0, 4, (n, D))
+        w[np.arange(n), peak] += 60
+        T["delays"] = w.astype(np.uint8)
+        T["delay_sum"] = T["delays"].sum(1, dtype=np.int32)
+    return edges, tabs, geo
+
+
 def synthetic_rows(rng, R=1500):
     """(step, SiPM) rows of tracks through the counter: local start, step vector, times, photons per substep."""
     a = np.c_[rng.uniform(-9.5, 9.5, R), rng.uniform(-25, 25, R), rng.uniform(-950, 950, R)]
@@ -456,9 +477,109 @@ def make_lookup(seeds=16):
     np.savez_compressed(HERE / "lookup.npz", **out)
 
 
+class _Col(np.ndarray):
+    """A step-table column with pandas' to_numpy (the reference reads columns that way)."""
+
+    def to_numpy(self):
+        return np.asarray(self)
+
+
+class _Steps:
+    def __init__(self, cols):
+        self.cols = {k: np.asarray(v).view(_Col) for k, v in cols.items()}
+
+    def __getattr__(self, k):
+        try:
+            return self.__dict__["cols"][k]
+        except KeyError:
+            raise AttributeError(k)
+
+    def __getitem__(self, k):
+        return self.cols[k]
+
+
+def lookup_chain_inputs(rng, n_steps=400):
+    """Two tables (reflector 0 and 1), a geometry of two sectors (EX: 2 modules x 4 bars, reflector 0; T1: 4 bars,
+    reflector -1), muon / electron / proton / photon / ion steps inside the bars."""
+    from types import SimpleNamespace
+    tabs = {}
+    for name, refl, seed in (("tabA", 0, 5), ("tabB", 1, 6)):
+        e, t, g = shaped_lookup(np.random.default_rng(seed), decay_time=3.0)
+        tabs[name] = (e, t, g, refl)
+    nb = 12
+    sector = np.r_[np.zeros(8, np.int64), np.ones(4, np.int64)]
+    module = np.r_[np.repeat([0, 1], 4), np.zeros(4, np.int64)]
+    l2w = np.array([[0, 1, 2]] * 8 + [[1, 0, 2]] * 4, np.int8)
+    center = np.c_[np.arange(nb) * 30.0, np.arange(nb) * 55.0 - 300.0, np.full(nb, 100.0)]
+    geom = SimpleNamespace(nbars=nb, sector=sector, module=module, local_to_world=l2w, center=center,
+                           sector_names=["EX", "T1"])
+    bar = rng.integers(0, nb, n_steps)
+    loc0 = np.c_[rng.uniform(-9, 9, n_steps), rng.uniform(-24, 24, n_steps), rng.uniform(-900, 900, n_steps)]
+    dirn = rng.normal(0, 1, (n_steps, 3))
+    dirn /= np.linalg.norm(dirn, axis=1)[:, None]
+    length = rng.uniform(2.0, 25.0, n_steps)
+    loc1 = loc0 + dirn * length[:, None]
+    w0, w1 = np.zeros((n_steps, 3)), np.zeros((n_steps, 3))
+    for k in range(3):
+        ax = l2w[bar, k]
+        w0[np.arange(n_steps), ax] = center[bar, ax] + loc0[:, k]
+        w1[np.arange(n_steps), ax] = center[bar, ax] + loc1[:, k]
+    p0 = rng.uniform(50, 2000, n_steps)
+    t0 = rng.uniform(0, 1000, n_steps)
+    t1 = t0 + length / 299.8
+    t0[::37] = np.nan                                  # skipped, as CrvPhotonGenerator skips them
+    cols = dict(bar=bar, x0=w0[:, 0], y0=w0[:, 1], z0=w0[:, 2], x1=w1[:, 0], y1=w1[:, 1], z1=w1[:, 2],
+                px0=dirn[:, 0] * p0, py0=dirn[:, 1] * p0, pz0=dirn[:, 2] * p0, p1=p0 * 0.99, t0=t0, t1=t1,
+                edep=rng.uniform(0.2, 3.0, n_steps), len=length)
+    pdg = rng.choice(np.array([13, -13, 11, 2212, 22, 211, 1000060120], np.int64), n_steps)
+    deviation = rng.normal(0, 0.05, 4 * nb)
+    return tabs, geom, cols, pdg, deviation
+
+
+def make_lookup_chain(seeds=16):
+    from types import SimpleNamespace
+    rng = np.random.default_rng(91)
+    tabs, geom, cols, pdg, deviation = lookup_chain_inputs(rng)
+    ck = np.array([[0.474, 0.0], [1.0, 2.6]])
+    tables = {}
+    for name, (e, t, g, refl) in tabs.items():
+        tables[name] = SimpleNamespace(name=name, reflector=refl, edges=e, ck_scint=ck, ck_fiber=ck * 0.5,
+                                       tables={k: SimpleNamespace(**v) for k, v in t.items()}, **g)
+    cfg = PH.ResponseConfig(sectors={"EX": PH.SectorConfig("tabA", 0, 1500.0),
+                                     "T1": PH.SectorConfig("tabB", -1, 1200.0)},
+                            photon_yield_scale=0.94, photon_yield_variation_scale=1.0, speed_ratio={"EX": 1.1},
+                            atten_ratio={"T1": 0.9, "EX1": 1.2})
+    steps = _Steps(cols)
+    n = len(pdg)
+    key = {}
+    sums, hist, total = {}, np.zeros(96), 0
+    for s in range(seeds):
+        st, ch, tm = PH.make_photons(steps, pdg, geom, cfg, tables, deviation, np.random.default_rng(2000 + s))
+        for a, b in zip(st, ch):
+            sums[(a, b)] = sums.get((a, b), 0) + 1
+        hist += np.bincount(np.clip((tm - cols["t0"][st]).astype(np.int64), 0, 95), minlength=96)
+        total += len(st)
+    pairs = np.array(sorted(sums), np.int64).reshape(-1, 2)
+    out = {f"step_{k}": np.asarray(v) for k, v in cols.items()}
+    out["pdg"] = pdg
+    out["deviation"] = deviation
+    for name, (e, t, g, refl) in tabs.items():
+        out.update({f"{name}_edge_{k}": v for k, v in e.items()})
+        for tk, T in t.items():
+            out.update({f"{name}_{tk}_{f}": v for f, v in T.items()})
+        out.update({f"{name}_geo_{k}": np.float64(v) for k, v in g.items()})
+        out[f"{name}_reflector"] = np.int64(refl)
+        out[f"{name}_propagation"] = np.array(PH.table_propagation(tables[name]))
+    out.update(ck=ck, speed_ratio=PH.bar_ratios(cfg.speed_ratio, geom), atten_ratio=PH.bar_ratios(cfg.atten_ratio, geom),
+               ref_pairs=pairs, ref_pair_mean=np.array([sums[tuple(p)] for p in pairs], float) / seeds,
+               ref_delay_hist=hist / seeds, ref_total=np.int64(total), ref_seeds=np.int64(seeds))
+    np.savez_compressed(HERE / "lookup_chain.npz", **out)
+
+
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
-                     ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup)):
+                     ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup),
+                     ("lookup_chain", make_lookup_chain)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

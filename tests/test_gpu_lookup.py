@@ -43,3 +43,30 @@ def test_substeps_are_keyed_and_capacity_grows():
     sel = np.isin(st, part["step"])
     assert np.array_equal(st[sel], s2) and np.array_equal(tm[sel], t2)
     assert eng.per_row > 0.01
+
+
+def test_lookup_rows_and_make_photons_match_the_oracle():
+    """Row preparation (every row field) and the whole lookup-table make_photons: bit for bit as the oracle, with two
+    tables (reflector 0 and -1), speed and attenuation ratios, skipped non-finite steps, ions and neutral particles."""
+    import torch
+    from crvgpu import lookup as LK
+    from tests.test_oracle_lookup import lookup_chain_fixture
+    tables, geom, cfg, steps, z = lookup_chain_fixture()
+    model = LK.LookupModel(geom, cfg, tables, z["deviation"])
+    cols = model.upload_steps(steps, z["pdg"])
+    ogroups = O.lookup_groups(geom, cfg, tables, z["deviation"])
+    assert len(ogroups) == len(model.groups) == 2
+    ocols = {k: np.asarray(steps[k], np.float64) for k in ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0",
+                                                           "p1", "t0", "t1", "edep", "len")}
+    ocols["bar"], ocols["pdg"] = np.asarray(steps["bar"], np.int32), z["pdg"]
+    for g, (_, og) in zip(model.groups, ogroups):
+        out, m = model.rows(g, cols, len(z["pdg"]), 11)
+        ref = O.lookup_rows(og, ocols, 11)
+        assert m == len(ref["nsub"]) > 0
+        for k, v in ref.items():
+            assert np.array_equal(out[k][:m].cpu().numpy(), v), k
+    st, ch, tm = (x.cpu().numpy() for x in model.make_photons(steps, z["pdg"], 11))
+    ost, och, otm = O.make_photons_lookup(steps, z["pdg"], geom, cfg, tables, z["deviation"], 11)
+    assert len(st) > 5000
+    assert np.array_equal(st, ost) and np.array_equal(ch, och) and np.array_equal(tm, otm)
+    torch.cuda.synchronize()

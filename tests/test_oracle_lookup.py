@@ -71,3 +71,74 @@ def test_substep_binomial_moments(n, p):
         return
     assert abs(x.mean() - mean) < 5 * np.sqrt(var / len(x))
     assert abs(x.var() / var - 1) < 0.05
+
+
+def lookup_chain_fixture():
+    """Tables, geometry, configuration, steps and reference statistics of tests/golden/lookup_chain.npz."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "lookup_chain.npz"))
+    tables = {}
+    for name in ("tabA", "tabB"):
+        geo = {k[len(name) + 5:]: float(z[k]) for k in z.files if k.startswith(f"{name}_geo_")}
+        tables[name] = SimpleNamespace(
+            name=name, reflector=int(z[f"{name}_reflector"]), ck_scint=z["ck"], ck_fiber=z["ck"] * 0.5,
+            edges={k: z[f"{name}_edge_{k}"] for k in O.LOOKUP_EDGES},
+            tables={t: SimpleNamespace(**{f: z[f"{name}_{t}_{f}"] for f in ("prob", "delays", "delay_sum", "emis",
+                                                                              "emis_sum")}) for t in O.LOOKUP_TABLES},
+            **geo)
+    nb = 12
+    geom = SimpleNamespace(nbars=nb, sector=np.r_[np.zeros(8, np.int64), np.ones(4, np.int64)],
+                           module=np.r_[np.repeat([0, 1], 4), np.zeros(4, np.int64)],
+                           local_to_world=np.array([[0, 1, 2]] * 8 + [[1, 0, 2]] * 4, np.int8),
+                           center=np.c_[np.arange(nb) * 30.0, np.arange(nb) * 55.0 - 300.0, np.full(nb, 100.0)],
+                           sector_names=["EX", "T1"])
+    sector = lambda t, r, y: SimpleNamespace(table=t, reflector=r, yield_per_mev=y)  # noqa: E731
+    cfg = SimpleNamespace(sectors={"EX": sector("tabA", 0, 1500.0), "T1": sector("tabB", -1, 1200.0)},
+                          photon_yield_scale=0.94, photon_yield_variation_scale=1.0, speed_ratio={"EX": 1.1},
+                          atten_ratio={"T1": 0.9, "EX1": 1.2})
+    steps = {k[5:]: z[k] for k in z.files if k.startswith("step_")}
+    return tables, geom, cfg, steps, z
+
+
+def test_lookup_setup_matches_the_reference():
+    """Table propagation fits and per-bar ratios: the oracle's and the engine's host setup give the reference's
+    values."""
+    from crvgpu import lookup as LK
+    tables, geom, cfg, _, z = lookup_chain_fixture()
+    for name, L in tables.items():
+        assert np.allclose(O.table_propagation(L), z[f"{name}_propagation"], rtol=1e-12, atol=0)
+        assert np.allclose(LK.table_propagation(L), z[f"{name}_propagation"], rtol=1e-12, atol=0)
+    for impl in (O.bar_ratios, LK.bar_ratios):
+        assert np.array_equal(impl(cfg.speed_ratio, geom), z["speed_ratio"])
+        assert np.array_equal(impl(cfg.atten_ratio, geom), z["atten_ratio"])
+    with pytest.raises(KeyError):
+        LK.bar_ratios({"XX": 1.1}, geom)
+
+
+def test_lookup_make_photons_oracle_matches_the_reference_statistically():
+    tables, geom, cfg, steps, z = lookup_chain_fixture()
+    S = int(z["ref_seeds"])
+    pairs = {tuple(p): i for i, p in enumerate(z["ref_pairs"])}
+    ref_mean = z["ref_pair_mean"]
+    got = np.zeros(len(pairs))
+    extra = 0
+    hist, total = np.zeros(96), 0
+    for s in range(S):
+        st, ch, tm = O.make_photons_lookup(steps, z["pdg"], geom, cfg, tables, z["deviation"], 700 + s)
+        for a, b in zip(st, ch):
+            i = pairs.get((a, b))
+            if i is None:
+                extra += 1
+            else:
+                got[i] += 1
+        hist += np.bincount(np.clip((tm - steps["t0"][st]).astype(np.int64), 0, 95), minlength=96)
+        total += len(st)
+    got /= S
+    ref_total = float(z["ref_total"]) / S
+    assert ref_total > 5000
+    assert abs(total / S / ref_total - 1) < 0.02
+    assert extra / S < 0.01 * ref_total                  # (step, channel) pairs the reference never lit are rare
+    m = (ref_mean + got) > 2
+    chi2 = np.mean((got[m] - ref_mean[m]) ** 2 / ((got[m] + ref_mean[m]) / S))
+    assert 0.7 < chi2 < 1.4
+    ks = np.max(np.abs(np.cumsum(hist) / hist.sum() - np.cumsum(z["ref_delay_hist"]) / z["ref_delay_hist"].sum()))
+    assert ks < 0.02
