@@ -345,7 +345,7 @@ def lookup_inputs(n_rows, seed=41, prob=0.0015, yield_per_mev=28610.0, edep=3.4,
     return L, rows
 
 
-def lookup_substeps(n_rows, reps=3, cpu_rows=20000):
+def lookup_substeps(n_rows, reps=3, cpu_rows=20000, precision="fp64"):
     """Lookup-table photon model: (step, SiPM) rows/s of crv_substep_photons on device-resident rows (device time of
     the launches, CUDA events), and the oracle's rate on one core over a bounded sample of the same rows."""
     import torch
@@ -353,22 +353,27 @@ def lookup_substeps(n_rows, reps=3, cpu_rows=20000):
     L, rows = lookup_inputs(n_rows)
     DL, R = LK.DeviceLookup(L), LK.DeviceRows(rows)
     eng = LK.SubstepEngine()
-    st, _, _ = eng.run(DL, R, 1)                          # warm-up, output capacity
+    st, _, _ = eng.run(DL, R, 1, precision=precision)     # warm-up, output capacity
     n_ph = int(st.numel())
     st = None
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for r in range(reps):
-        eng.run(DL, R, 2 + r)
+        eng.run(DL, R, 2 + r, precision=precision)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     out = {"rows": n_rows, "rows_per_s": n_rows / (ms / 1000.0), "ms_per_call": ms, "photons_per_row": n_ph / n_rows,
            "substeps_per_row": float(np.mean(rows["nsub"])), "table": "synthetic 3200 mm: 10x41x56 position bins, "
-           "5 beta, 150 delay bins, prob 0.0015", "precision": "fp64 (bit-exact with the oracle)",
+           "5 beta, 150 delay bins, prob 0.0015",
+           "precision": "fp64 (bit-exact with the oracle)" if precision == "fp64" else "fp32-mixed (FP64 times)",
            "published_context": "reference JAX substep kernel ~300k rows/s on A100 (its own bench)"}
+    if precision != "fp64":
+        cpu_rows = 0
     try:
+        if not cpu_rows:
+            raise RuntimeError("CPU sample with the FP64 leg")
         from oracle import oracle as O
         sub = {k: v[:cpu_rows] for k, v in rows.items()}
         t0 = time.perf_counter()
@@ -712,7 +717,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         procs = 1
-        v, ev, busy, wall = cpu_reference(48, procs)
+        v, ev, busy, wall = cpu_reference(960, procs)
         cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"{ev} events of the same workload through the oracle chain on 1 core ({busy:.1f} s)"}
 
@@ -729,6 +734,9 @@ def main():
     lookup = None
     if rank == 0 and args.lookup_rows > 0:
         lookup = lookup_substeps(args.lookup_rows)
+        torch.cuda.empty_cache()
+        lookup["fp32_mixed"] = {k: v for k, v in lookup_substeps(args.lookup_rows, precision="fp32").items()
+                                if k in ("rows_per_s", "ms_per_call", "photons_per_row", "precision")}
         torch.cuda.empty_cache()
 
     full = None

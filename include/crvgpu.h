@@ -417,7 +417,8 @@ typedef struct CrvLookup {
         corner_radius, fiber_decay_time;
     const double *edges[7];      /* ascending bin edges of x, y, z, beta, theta, phi, r */
     int32_t nedges[7];
-    int32_t pad;
+    int32_t precision;           /* 0: FP64 (bit-exact with the CPU oracle); 1: FP32-mixed (geometry, arrival draws
+                                    and delays in FP32 with 24-bit uniforms, absolute photon times FP64) */
     const double *cos_phi_edges; /* cos of the phi edges: phi bins are found on cos phi (no arccos per substep) */
     CrvLookupTable table[3];     /* scintillation, Cherenkov in scintillator, Cherenkov in fibre */
     const double *cos_theta_edges; /* cos of the theta edges (rows that carry cos theta instead of theta) */

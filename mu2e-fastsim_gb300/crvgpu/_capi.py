@@ -114,7 +114,7 @@ class CrvLookupTable(ctypes.Structure):
 class CrvLookup(ctypes.Structure):
     _fields_ = [(k, c_f64) for k in ("half_thickness", "half_width", "half_length", "fiber_separation", "hole_radius_x",
                                      "hole_radius_y", "fiber_radius", "corner_radius", "fiber_decay_time")] + \
-        [("edges", c_p * 7), ("nedges", c_i32 * 7), ("pad", c_i32), ("cos_phi_edges", c_p),
+        [("edges", c_p * 7), ("nedges", c_i32 * 7), ("precision", c_i32), ("cos_phi_edges", c_p),
          ("table", CrvLookupTable * 3), ("cos_theta_edges", c_p)]
 
 

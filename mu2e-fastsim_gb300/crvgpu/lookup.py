@@ -24,6 +24,12 @@ ROW_REAL = ("t0", "t1", "beta", "dev")
 ROW_INT = ("nsub", "step", "chan", "n_scint", "n_ck_s", "n_ck_f")
 
 
+def _precision_code(precision):
+    if precision not in ("fp64", "fp32"):
+        raise ValueError(f"precision must be 'fp64' or 'fp32', got {precision!r}")
+    return 0 if precision == "fp64" else 1
+
+
 class DeviceLookup:
     """A lookup table on the device (CrvLookup)."""
 
@@ -68,8 +74,9 @@ class DeviceLookup:
             self.tables.append(t)
         self.nbytes = sum(int(v.numel() * v.element_size()) for t in self.tables for k, v in t.items() if k != "shape")
 
-    def c(self):
+    def c(self, precision="fp64"):
         S = _capi.CrvLookup(*[self.geometry[k] for k in GEOMETRY])
+        S.precision = _precision_code(precision)
         for i, e in enumerate(self.edges):
             S.edges[i] = e.data_ptr()
             S.nedges[i] = int(e.numel())
@@ -133,14 +140,15 @@ class SubstepEngine:
         self.per_row = 64.0
         self.status = _capi.DeviceStatus(device)
 
-    def run(self, DL: DeviceLookup, R: DeviceRows, seed, max_tries=3):
+    def run(self, DL: DeviceLookup, R: DeviceRows, seed, max_tries=3, precision="fp64"):
+        """precision "fp64": bit-exact with the oracle; "fp32": FP32-mixed (same statistics, absolute times FP64)."""
         torch = _torch()
         L = _capi.load()
         dev = self.device
         wsb = L.crv_substeps_workspace(R.n)
         if self.ws is None or self.ws.numel() < wsb:
             self.ws = torch.empty(int(wsb) + 1024, dtype=torch.uint8, device=dev)
-        S, C = DL.c(), R.c()
+        S, C = DL.c(precision), R.c()
         for _ in range(max_tries):
             cap = int(max(1024, self.per_row * R.n))
             o_step = torch.empty(cap, dtype=torch.int64, device=dev)
@@ -166,14 +174,14 @@ class SubstepEngine:
 _ENGINE = {}
 
 
-def substep_photons(L, rows, seed, device="cuda"):
+def substep_photons(L, rows, seed, device="cuda", precision="fp64"):
     """photons._substep_photons(L, rows, rng) with keyed draws: (step index, channel, arrival time) host arrays in
     (row, substep, table, arrival) order.  L: a lookup table object (or a DeviceLookup); rows: the reference's row
     dict (s, d, t0, t1, nsub, beta, theta, dev, optional mu, step, chan, n_scint, n_ck_s, n_ck_f)."""
     DL = L if isinstance(L, DeviceLookup) else DeviceLookup(L, device)
     if device not in _ENGINE:
         _ENGINE[device] = SubstepEngine(device)
-    st, ch, tm = _ENGINE[device].run(DL, DeviceRows(rows, device), seed)
+    st, ch, tm = _ENGINE[device].run(DL, DeviceRows(rows, device), seed, precision=precision)
     return st.cpu().numpy(), ch.cpu().numpy(), tm.cpu().numpy()
 
 
@@ -254,9 +262,11 @@ class LookupModel:
     atten_ratio) with its tables on the device: one (table, reflector) group per combination the sectors use, as
     photons.iter_rows iterates them (table names sorted, reflectors sorted)."""
 
-    def __init__(self, geom, cfg, tables, deviation, device="cuda"):
+    def __init__(self, geom, cfg, tables, deviation, device="cuda", precision="fp64"):
         torch = _torch()
         self.device = device
+        _precision_code(precision)
+        self.precision = precision
         names = list(geom.sector_names)
         sec = np.asarray(geom.sector)
         nb = int(geom.nbars)
@@ -357,7 +367,7 @@ class LookupModel:
             out, m = self.rows(g, cols, n, seed)
             if m == 0:
                 continue
-            st, ch, tm = self.substeps.run(g["DL"], DeviceRows.from_columns(out, m), seed)
+            st, ch, tm = self.substeps.run(g["DL"], DeviceRows.from_columns(out, m), seed, precision=self.precision)
             parts.append((st, ch, tm))
         if not parts:
             z = torch.zeros(0, dtype=torch.int64, device=self.device)
@@ -365,8 +375,8 @@ class LookupModel:
         return tuple(torch.cat([p[i] for p in parts]) for i in range(3))
 
 
-def make_photons(steps, pdg, geom, cfg, tables, deviation, seed, device="cuda"):
+def make_photons(steps, pdg, geom, cfg, tables, deviation, seed, device="cuda", precision="fp64"):
     """photons.make_photons(steps, pdg, geom, cfg, tables, deviation, rng) with the lookup-table model on the device and
     keyed draws (seed in place of rng): (step index, channel = 4 bar + SiPM, arrival time) host arrays."""
-    st, ch, tm = LookupModel(geom, cfg, tables, deviation, device).make_photons(steps, pdg, seed)
+    st, ch, tm = LookupModel(geom, cfg, tables, deviation, device, precision).make_photons(steps, pdg, seed)
     return st.cpu().numpy(), ch.cpu().numpy(), tm.cpu().numpy()

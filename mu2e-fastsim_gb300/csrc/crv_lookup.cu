@@ -273,6 +273,273 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLoo
   }
 }
 
+// ---- FP32-mixed variant: geometry, arrival draws and delays in FP32 (24-bit uniforms), edges staged as FP32 in
+// shared memory, absolute photon times FP64 (row start time + FP32 offset).  Same keyed counters as the FP64 path,
+// different numbers from them; the results agree with the FP64 path statistically.
+
+struct EdgesF {
+  const float* e[7];
+  const float* cphi;
+  const float* cth;
+  int n[7];
+};
+
+// stage the edges (and cos of the phi / theta edges) of L as FP32 in shared memory; returns the views
+__device__ __forceinline__ EdgesF stage_edges_f(const CrvLookup& L, float* sm) {
+  EdgesF E;
+  int o = 0;
+  for (int i = 0; i < 7; ++i) {
+    E.n[i] = L.nedges[i];
+    for (int j = threadIdx.x; j < L.nedges[i]; j += blockDim.x) sm[o + j] = float(L.edges[i][j]);
+    E.e[i] = sm + o;
+    o += L.nedges[i];
+  }
+  for (int j = threadIdx.x; j < L.nedges[5]; j += blockDim.x) sm[o + j] = float(L.cos_phi_edges[j]);
+  E.cphi = sm + o;
+  o += L.nedges[5];
+  for (int j = threadIdx.x; j < L.nedges[4]; j += blockDim.x) sm[o + j] = L.cos_theta_edges ? float(L.cos_theta_edges[j]) : 0.f;
+  E.cth = sm + o;
+  __syncthreads();
+  return E;
+}
+
+__device__ __forceinline__ int find_bin_f(const float* e, int ne, float v) {
+  if (!(v >= e[0]) || !(v <= e[ne - 1])) return -1;
+  if (v == e[0]) return 0;
+  int lo = 0, hi = ne;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (e[mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return lo - 1;
+}
+
+__device__ __forceinline__ int find_bin_cos_f(const float* ce, int ne, float c) {
+  if (!(c <= ce[0]) || !(c >= ce[ne - 1])) return -1;
+  if (c == ce[0]) return 0;
+  int lo = 0, hi = ne;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ce[mid] > c) lo = mid + 1; else hi = mid;
+  }
+  return lo - 1;
+}
+
+__device__ __forceinline__ long long binomial_f(long long n, float p, const U4& w) {
+  if (n <= 0 || !(p > 0.f)) return 0;
+  if (p >= 1.f) return n;
+  const bool flip = p > 0.5f;
+  const float q = flip ? 1.f - p : p;
+  const float mean = float(n) * q;
+  long long k;
+  if (mean > 256.f) {
+    float z0, z1;
+    Math<float>::normal_pair(w, &z0, &z1);
+    const float x = rintf(mean + sqrtf(mean * (1.f - q)) * z0);
+    k = x < 0.f ? 0 : (x > float(n) ? n : (long long)x);
+  } else {
+    float u = f01(w.x);
+    const float s = q / (1.f - q);
+    const float a = float(n + 1) * s;
+    float r = __expf(float(n) * log1pf(-q));
+    k = 0;
+    while (u > r && k < n) {
+      u = u - r;
+      k += 1;
+      r = r * (a / float(k) - s);
+    }
+  }
+  return flip ? n - k : k;
+}
+
+// a row in FP32: local start, step vector, and per-row constants
+struct RowF {
+  float s[3], d[3], dev, mu, dt;
+  double t0;
+  long long nsub, step, chan;
+  int bb, bth;
+};
+
+__device__ __forceinline__ RowF load_row_f(const CrvSubstepRows& R, const EdgesF& E, long long r) {
+  RowF w;
+  for (int x = 0; x < 3; ++x) {
+    w.s[x] = float(R.s[3 * r + x]);
+    w.d[x] = float(R.d[3 * r + x]);
+  }
+  w.dev = float(R.dev[r]);
+  w.mu = R.mu ? float(R.mu[r]) : 0.f;
+  w.t0 = R.t0[r];
+  w.dt = float(R.t1[r] - R.t0[r]);
+  w.nsub = R.nsub[r];
+  w.step = R.step[r];
+  w.chan = R.chan[r];
+  w.bb = find_bin_f(E.e[3], E.n[3], float(R.beta[r]));
+  w.bth = R.theta ? find_bin_f(E.e[4], E.n[4], float(R.theta[r])) : find_bin_cos_f(E.cth, E.n[4], float(R.cos_theta[r]));
+  return w;
+}
+
+struct GeoF {
+  float ht, hw, hl, half_sep, hrx, hry, fr, cr;
+};
+
+__device__ __forceinline__ GeoF geo_f(const CrvLookup& L) {
+  return {float(L.half_thickness), float(L.half_width), float(L.half_length), float(L.fiber_separation / 2.0),
+          float(L.hole_radius_x), float(L.hole_radius_y), float(L.fiber_radius), float(L.corner_radius)};
+}
+
+__device__ __forceinline__ void substep_bins_f(const GeoF& g, const EdgesF& E, const RowF& w, long long k, int bin[3],
+                                               float* z_out, float* frac_out) {
+  const float frac = (float(k) + 0.5f) / float(w.nsub);
+  const float x = fmaf(w.d[0], frac, w.s[0]), y = fmaf(w.d[1], frac, w.s[1]), z = fmaf(w.d[2], frac, w.s[2]);
+  const float ax = fabsf(x), ay = fabsf(y);
+  bool insc = ax < g.ht && ay < g.hw && fabsf(z) < g.hl;
+  const float ex = ax / g.hrx, ey = (ay - g.half_sep) / g.hry;
+  insc = insc && (ex * ex + ey * ey >= 1.f);
+  const float cx = g.ht - g.cr, cy = g.hw - g.cr;
+  if (ax > cx && ay > cy) {
+    const float qx = ax - cx, qy = ay - cy;
+    if (sqrtf(qx * qx + qy * qy) > g.cr) insc = false;
+  }
+  const float y0 = y + g.half_sep, y1 = y - g.half_sep;
+  const float r0 = sqrtf(x * x + y0 * y0), r1 = sqrtf(x * x + y1 * y1);
+  const bool in0 = r0 <= g.fr, in1 = r1 <= g.fr;
+  const float ry = in1 ? y1 : y0, rr = in1 ? r1 : r0;
+  const float norm = sqrtf(w.d[0] * w.d[0] + w.d[1] * w.d[1]) * rr;
+  float c = 1.f;
+  if (norm > 0.f) c = fminf(1.f, fmaxf(-1.f, (w.d[0] * x + w.d[1] * ry) / norm));
+  const bool infb = fabsf(z) < g.hl && (in0 || in1) && !insc;
+  const int ny = E.n[1] - 1, nz = E.n[2] - 1, nb = E.n[3] - 1, nth = E.n[4] - 1, nph = E.n[5] - 1, nr = E.n[6] - 1;
+  const int bx = find_bin_f(E.e[0], E.n[0], ax), by = find_bin_f(E.e[1], E.n[1], y), bz = find_bin_f(E.e[2], E.n[2], z);
+  const bool geo = bx >= 0 && by >= 0 && bz >= 0;
+  bin[0] = (insc && geo) ? bz + by * nz + bx * ny * nz : -1;
+  bin[1] = (insc && geo && w.bb >= 0) ? w.bb + bz * nb + by * nz * nb + bx * ny * nz * nb : -1;
+  bin[2] = -1;
+  if (infb && w.bb >= 0 && w.bth >= 0 && bz >= 0) {
+    const int bph = find_bin_cos_f(E.cphi, E.n[5], c), br = find_bin_f(E.e[6], E.n[6], rr);
+    if (bph >= 0 && br >= 0) bin[2] = bz + br * nz + bph * nr * nz + w.bth * nph * nr * nz + w.bb * nth * nph * nr * nz;
+  }
+  *z_out = z;
+  *frac_out = frac;
+}
+
+__device__ __forceinline__ long long arrivals_f(const CrvLookup& L, const CrvSubstepRows& R, const RowF& w,
+                                                uint32_t seed, long long r, long long k, int tb, int bin, float z) {
+  float pr = L.table[tb].prob[bin] * w.dev;
+  if (R.mu) pr = pr * __expf(-w.mu * z);
+  pr = fminf(pr, 1.f);
+  return binomial_f(photons_per_substep(R, tb, r), pr, sub_block(seed, w.step, w.chan, tb, SUB_CALL_BINOMIAL, 0, k, 0));
+}
+
+__device__ __forceinline__ int first_reaching_f(const uint8_t* __restrict__ wts, int n, float thr) {
+  int cum = 0;
+  for (int j = 0; j < n; ++j) {
+    cum += wts[j];
+    if (!(float(cum) < thr)) return j;
+  }
+  return n;
+}
+
+// offset of arrival j from the row start time (FP32: substep time, delay, fibre decay)
+__device__ __forceinline__ float arrival_offset_f(const CrvLookup& L, float decay, uint32_t seed, const RowF& w,
+                                                  long long k, int tb, int bin, int j, float frac, Status* status) {
+  const CrvLookupTable& T = L.table[tb];
+  const U4 v = sub_block(seed, w.step, w.chan, tb, SUB_CALL_PHOTON, 0, k, j);
+  float off = w.dt * frac + float(first_reaching_f(T.delays + (long long)bin * T.ndelay, T.ndelay,
+                                                   f01(v.x) * float(T.delay_sum[bin])));
+  if (decay > 0.f) {
+    const int ne = first_reaching_f(T.emis + (long long)bin * T.nemis, T.nemis, f01(v.z) * float(T.emis_sum[bin]));
+    if (ne > SUB_MAX_EMISSIONS) {
+      set_flag(status, CRV_ST_LIMIT);
+    } else if (ne > 0) {
+      float g = 0.f;
+      for (int i = 0; i < ne; i += 2) {
+        const U4 q = sub_block(seed, w.step, w.chan, tb, SUB_CALL_GAMMA, i >> 1, k, j);
+        g -= __logf(f01_open(q.x));
+        if (i + 1 < ne) g -= __logf(f01_open(q.z));
+      }
+      off += g * decay;
+    }
+  }
+  return off;
+}
+
+__global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count_f32(CrvLookup L, CrvSubstepRows R,
+                                                                               uint32_t seed, long long nrows,
+                                                                               long long* __restrict__ count,
+                                                                               Status* status) {
+  extern __shared__ float edges_sm[];
+  const EdgesF E = stage_edges_f(L, edges_sm);
+  const GeoF g = geo_f(L);
+  const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
+  for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    long long nsub;
+    long long tot = 0;
+    if (row_ok(R, r, &nsub, status)) {
+      const RowF w = load_row_f(R, E, r);
+      for (long long k = lane_id(); k < nsub; k += 32) {
+        int bin[3];
+        float z, frac;
+        substep_bins_f(g, E, w, k, bin, &z, &frac);
+        for (int tb = 0; tb < 3; ++tb)
+          if (bin[tb] >= 0) {
+            long long a = arrivals_f(L, R, w, seed, r, k, tb, bin[tb], z);
+            if (a >= SUB_MAX_ARRIVALS) { set_flag(status, CRV_ST_LIMIT); a = 0; }
+            tot += a;
+          }
+      }
+    }
+    tot = warp_sum(tot);
+    if (lane_id() == 0) count[r] = tot;
+  }
+}
+
+__global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit_f32(CrvLookup L, CrvSubstepRows R,
+                                                                              uint32_t seed, long long nrows,
+                                                                              const long long* __restrict__ offset,
+                                                                              const long long* __restrict__ total,
+                                                                              long long cap,
+                                                                              int64_t* __restrict__ o_step,
+                                                                              int64_t* __restrict__ o_chan,
+                                                                              double* __restrict__ o_time,
+                                                                              Status* status) {
+  extern __shared__ float edges_sm[];
+  if (*total > cap) return;                                    // block-uniform, before the staging barrier
+  const EdgesF E = stage_edges_f(L, edges_sm);
+  const GeoF g = geo_f(L);
+  const float decay = float(L.fiber_decay_time);
+  const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
+  for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    long long nsub;
+    if (!row_ok(R, r, &nsub, status)) continue;
+    const RowF w = load_row_f(R, E, r);
+    long long o = offset[r];
+    for (long long k0 = 0; k0 < nsub; k0 += 32) {
+      const long long k = k0 + lane_id();
+      int bin[3] = {-1, -1, -1};
+      float z = 0.f, frac = 0.f;
+      long long a[3] = {0, 0, 0};
+      if (k < nsub) {
+        substep_bins_f(g, E, w, k, bin, &z, &frac);
+        for (int tb = 0; tb < 3; ++tb)
+          if (bin[tb] >= 0) {
+            a[tb] = arrivals_f(L, R, w, seed, r, k, tb, bin[tb], z);
+            if (a[tb] >= SUB_MAX_ARRIVALS) a[tb] = 0;
+          }
+      }
+      long long sum;
+      long long q = o + warp_excl_ll(a[0] + a[1] + a[2], &sum);
+      if (k < nsub)
+        for (int tb = 0; tb < 3; ++tb)
+          for (int j = 0; j < int(a[tb]); ++j, ++q) {
+            o_step[q] = w.step;
+            o_chan[q] = w.chan;
+            o_time[q] = w.t0 + double(arrival_offset_f(L, decay, seed, w, k, tb, bin[tb], j, frac, status));
+          }
+      o += sum;
+    }
+  }
+}
+
 __global__ void k_substep_check(const long long* __restrict__ total, long long cap, long long* __restrict__ n_out,
                                 Status* status) {
   if (*total > cap) {
@@ -320,7 +587,7 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
   if (!L || !rows || !n_out_dev || !status_dev || nrows < 0 || cap < 0) return CRV_ERR_ARG;
   for (int i = 0; i < 7; ++i)
     if (!L->edges[i] || L->nedges[i] < 2) return CRV_ERR_ARG;
-  if (!L->cos_phi_edges) return CRV_ERR_ARG;
+  if (!L->cos_phi_edges || L->precision < 0 || L->precision > 1) return CRV_ERR_ARG;
   for (int t = 0; t < 3; ++t) {
     const CrvLookupTable& T = L->table[t];
     if (!T.prob || !T.delays || !T.delay_sum || !T.emis || !T.emis_sum || T.ndelay < 1 || T.nemis < 1) return CRV_ERR_ARG;
@@ -349,7 +616,15 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
   const long long blocks = (nrows + SUB_ROWS_PER_BLOCK - 1) / SUB_ROWS_PER_BLOCK;
   const long long maxb = (long long)device_info().sms * 8;
   const unsigned grid = (unsigned)(blocks < maxb ? blocks : maxb);
-  {
+  const bool f32 = L->precision == 1;
+  int nedge = 0;
+  for (int i = 0; i < 7; ++i) nedge += L->nedges[i];
+  const size_t esm = sizeof(float) * size_t(nedge + L->nedges[5] + L->nedges[4]);
+  if (f32 && esm > 48 * 1024) return CRV_ERR_ARG;
+  if (f32) {
+    crv::Mark mark_("k_substep_count", s);
+    k_substep_count_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, w.count, S);
+  } else {
     crv::Mark mark_("k_substep_count", s);
     k_substep_count<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, w.count, S);
   }
@@ -359,7 +634,11 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
     crv::Mark mark_("k_substep_check", s);
     k_substep_check<<<1, 1, 0, s>>>(w.total, cap, reinterpret_cast<long long*>(n_out_dev), S);
   }
-  {
+  if (f32) {
+    crv::Mark mark_("k_substep_emit", s);
+    k_substep_emit_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, w.offset, w.total, cap,
+                                                                 o_step, o_chan, o_time, S);
+  } else {
     crv::Mark mark_("k_substep_emit", s);
     k_substep_emit<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, w.offset, w.total, cap, o_step,
                                                             o_chan, o_time, S);

@@ -70,3 +70,26 @@ def test_lookup_rows_and_make_photons_match_the_oracle():
     assert len(st) > 5000
     assert np.array_equal(st, ost) and np.array_equal(ch, och) and np.array_equal(tm, otm)
     torch.cuda.synchronize()
+
+
+def test_fp32_substeps_match_fp64():
+    """FP32-mixed substeps against the FP64 path on the same keys: the 24-bit uniforms are the top bits of the FP64
+    path's words, so arrivals and delays differ only where a draw lands within 2^-24 of a threshold or FP32 geometry
+    moves a substep across a bin edge; photon times differ by the FP32 rounding of their offsets."""
+    from crvgpu import lookup as LK
+    L, rows, _ = lookup_fixture()
+    R = len(rows["nsub"])
+    s64, _, t64 = LK.substep_photons(L, rows, 40)
+    s32, _, t32 = LK.substep_photons(L, rows, 40, precision="fp32")
+    c64 = np.bincount((s64 - 3) // 7, minlength=R)
+    c32 = np.bincount((s32 - 3) // 7, minlength=R)
+    assert abs(len(s32) / len(s64) - 1) < 1e-3
+    same = c32 == c64
+    assert same.mean() > 0.99
+    # photons of rows with equal counts, in the same order: times within the FP32 offset rounding, rarely a delay bin
+    keep64 = same[(s64 - 3) // 7]
+    keep32 = same[(s32 - 3) // 7]
+    dt = np.abs(t32[keep32] - t64[keep64])
+    assert np.median(dt) < 1e-4 and np.mean(dt < 1e-3) > 0.99
+    with pytest.raises(ValueError):
+        LK.substep_photons(L, rows, 1, precision="fp16")
