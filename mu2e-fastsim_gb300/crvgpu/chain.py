@@ -173,6 +173,13 @@ class ChainEngine:
             self.tlen = len(tm)
         self.cfg, self.ccfg, self.wcfg, self.rcfg, self.fcfg = cfg, ccfg, wcfg, rcfg, fcfg
 
+    def release(self):
+        """Drop the stage workspaces (tables, configuration and the sizes learned so far stay; the next run allocates
+        again)."""
+        for e in (self.resp, self.dig, self.pul, self.coi):
+            e.ws = None
+        self.ws_w.t = self.ws_h.t = None
+
     def params(self, seed):
         P = make_params(self.ccfg, seed, template_len=self.tlen, uniform_map=self.tabs.uniform_map)
         P.period = self.wcfg.period

@@ -1024,7 +1024,9 @@ static int coinc_run(const CrvParams* p, const CrvFinderGeom* g, int64_t nevents
     size_t smem = per * passes[k].warps;
     if (smem > di.smem_optin - 1024) return CRV_ERR_CUDA;
     long long blocks = (nevents + passes[k].warps - 1) / passes[k].warps;
-    long long maxb = (long long)di.sms * (k == 0 ? 16 : (k == 1 ? 2 : 8));
+    // the global pass (118 registers: 16 one-warp blocks per SM) sees the few large events of a batch, or every event
+    // at full scale (~11,000 hits each)
+    long long maxb = (long long)di.sms * (k == 0 ? 16 : (k == 1 ? 2 : 16));
     const unsigned grid = (unsigned)(blocks < maxb ? blocks : maxb);
     if (k < 2) {
       CK(allow_dynamic_smem(k_coinc<false>));
