@@ -54,3 +54,32 @@ def test_pulse_launch_shape_is_validated():
         with pytest.raises(ValueError):
             set_shape(bad)
     set_shape(DEFAULT_SHAPE)
+
+
+def test_chain_and_lookup_workspace_queries_without_gpu():
+    import ctypes
+    from crvgpu.params import make_params
+    from crvgpu.resident import ChainCaps
+    L = _capi.load()
+    P = make_params()
+    caps = ChainCaps(events=64, steps=2600, photons=10 ** 6, charges=10 ** 5, slots=10 ** 4, digis=10 ** 4,
+                     pulses=10 ** 4, max_steps_per_event=80)
+    small = L.crv_chain_workspace(ctypes.byref(P), ctypes.byref(caps.c()))
+    big = L.crv_chain_workspace(ctypes.byref(P), ctypes.byref(ChainCaps(**{**caps.as_dict(), "pulses": 10 ** 6}).c()))
+    assert 0 < small < big
+    bad = caps.c()
+    bad.digis = 0                                          # every capacity must be positive
+    assert L.crv_chain_workspace(ctypes.byref(P), ctypes.byref(bad)) == -1
+    assert L.crv_substeps_workspace(1000) > L.crv_substeps_workspace(10) > 0
+    assert L.crv_substeps_workspace(-1) == -1
+    assert L.crv_lookup_rows_workspace(1000) > 0 and L.crv_lookup_rows_workspace(-5) == -1
+
+
+def test_lookup_struct_layouts():
+    import ctypes
+    # CrvLookup: 9 doubles, 7 edge pointers, 7 + 1 ints, cos phi pointer, 3 tables of 5 pointers + 4 ints, cos theta
+    assert ctypes.sizeof(_capi.CrvLookupTable) == 5 * 8 + 4 * 4
+    assert ctypes.sizeof(_capi.CrvLookup) == 9 * 8 + 7 * 8 + 8 * 4 + 8 + 3 * (5 * 8 + 4 * 4) + 8
+    assert ctypes.sizeof(_capi.CrvSubstepRows) == 15 * 8
+    assert ctypes.sizeof(_capi.CrvLookupGroup) == 12 * 8 + 8 + 6 * 4
+    assert ctypes.sizeof(_capi.CrvChainCaps) == 7 * 8 + 2 * 4
