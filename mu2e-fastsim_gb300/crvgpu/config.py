@@ -187,6 +187,9 @@ class ChainConfig:
     feb_phase_key: str = "roc_feb"
     backend: str = "cuda"
     precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (FP64 LM solve and absolute times)
+    # the reference's lookup-table response block (sectors {name: (table, reflector, yield_per_mev)}, yield scales,
+    # speed / attenuation ratios): charges() runs the lookup-table photon model with it when given lookup tables
+    lookup: object = None
 
 
 def _fields_of(cls, obj, **over):
@@ -207,7 +210,7 @@ def from_reference(cfg, precision="fp64"):
     resp = getattr(cfg, "response", None)
     rc = ResponseConfig(**{k: getattr(resp, k) for k in ("photon_yield_scale", "photon_yield_variation_scale")
                            if hasattr(resp, k)})
-    kw = dict(response=rc, precision=precision,
+    kw = dict(response=rc, precision=precision, lookup=resp if hasattr(resp, "sectors") else None,
               sipm=_fields_of(SiPMConfig, getattr(cfg, "sipm", None)) or SiPMConfig(),
               waveform=_fields_of(WaveformConfig, getattr(cfg, "waveform", None)),
               pulse_reco=_fields_of(RecoConfig, getattr(cfg, "pulse_reco", None)),

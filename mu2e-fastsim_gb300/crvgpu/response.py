@@ -319,15 +319,55 @@ def engine(device="cuda"):
     return _ENGINE[device]
 
 
+def _is_lookup(tabs):
+    return isinstance(tabs, dict) and bool(tabs) and all(hasattr(t, "edges") and hasattr(t, "tables")
+                                                         for t in tabs.values())
+
+
+def lookup_charges(steps, pdg, geom, cond, cfg: ChainConfig, tables, seed, pmap=None, timers=None):
+    """chain.charges with the lookup-table photon model (crv/crvfastsim/chain.py:197-213): photons of every (step,
+    SiPM) row on the device (crvgpu.lookup), SiPMs with status bit 0 or 2 dropped, labels event key * CHAN_MULT +
+    channel, then the SiPM stage (simulate) up to the readout window's end.  cfg.lookup: the sector configuration."""
+    from . import lookup as LK
+    from .geometry import event_key
+    timers = timers if timers is not None else {}
+    if cfg.lookup is None:
+        raise ValueError("the lookup-table photon model needs ChainConfig.lookup (the reference's response block)")
+    if pdg is None:
+        raise ValueError("the lookup-table photon model needs the particle code of every step (pdg)")
+    t0 = _time.perf_counter()
+    model = LK.LookupModel(geom, cfg.lookup, tables, cond.deviation, precision=cfg.precision)
+    s, c, t = (x.cpu().numpy() for x in model.make_photons(steps, pdg, seed))
+    timers["photons_s"] = timers.get("photons_s", 0.0) + _time.perf_counter() - t0
+    status = effective_status(cond)
+    keep = (status[c] & 0b101) == 0
+    s, c, t = s[keep], c[keep], t[keep]
+    if len(c) and int(c.max()) >= CHAN_MULT:
+        raise ValueError(f"channel {int(c.max())} >= CHAN_MULT {CHAN_MULT}: SiPM labels would overlap the next event")
+    col = lambda k: np.asarray(steps[k].to_numpy() if hasattr(steps[k], "to_numpy") else steps[k])  # noqa: E731
+    label = event_key({"subrun": col("subrun"), "event": col("event")})[s] * CHAN_MULT + c
+    run = col("run")[s] if "run" in getattr(steps, "columns", steps) else None
+    t0 = _time.perf_counter()
+    Q = simulate(label, t, s, pmap, cfg.sipm, None, t_end=cfg.window[1], key=seed, run=run, precision=cfg.precision)
+    timers["sipm_s"] = timers.get("sipm_s", 0.0) + _time.perf_counter() - t0
+    timers["photons"] = timers.get("photons", 0) + len(s)
+    timers["charges"] = timers.get("charges", 0) + len(Q["time"])
+    return {k: Q[k] for k in ("chan", "time", "charge", "pe", "photon")}
+
+
 def charges(steps, parts, geom, cond, cfg: ChainConfig, rng, key=None, tabs=None, pmap=None, timers=None, pdg=None,
             caps=None):
-    """chain.charges: CrvSteps -> SiPM charges (dict chan (label), time, charge, pe, photon; sorted by label, time)."""
+    """chain.charges: CrvSteps -> SiPM charges (dict chan (label), time, charge, pe, photon; sorted by label, time).
+    With lookup tables in `tabs` ({name: lookup table}) and cfg.lookup set, the lookup-table photon model
+    (lookup_charges); otherwise the analytic model."""
     if caps is not None:
         raise ValueError("capacities are managed by the engine (fail-closed re-runs)")
     validate_sipm(cfg.sipm)
     validate_window(cfg.window)
     timers = timers if timers is not None else {}
     seed = seed_of(rng, key)
+    if _is_lookup(tabs):
+        return lookup_charges(steps, pdg, geom, cond, cfg, tabs, seed, pmap=pmap, timers=timers)
     t0 = _time.perf_counter()
     ds = upload_steps(steps, nbars=geom.nbars)
     T = tabs if isinstance(tabs, DeviceTables) else DeviceTables(geom, cond, cfg, pmap=pmap)

@@ -93,3 +93,34 @@ def test_fp32_substeps_match_fp64():
     assert np.median(dt) < 1e-4 and np.mean(dt < 1e-3) > 0.99
     with pytest.raises(ValueError):
         LK.substep_photons(L, rows, 1, precision="fp16")
+
+
+def test_charges_with_lookup_tables_match_the_oracle():
+    """chain.charges with lookup tables (the reference's production path, crv/crvfastsim/chain.py:197-213): lookup
+    photons, status-masked SiPMs dropped, labels by event, SiPM stage up to the window's end: bit for bit as the
+    oracle's photons through the oracle's SiPM stage."""
+    from crvgpu import chain as CH
+    from crvgpu.config import ChainConfig
+    from tests.test_oracle_lookup import lookup_chain_fixture
+    tables, geom, lcfg, steps, z = lookup_chain_fixture()
+    n = len(z["pdg"])
+    steps = dict(steps, event=np.arange(n) // 40, subrun=np.ones(n, np.int64), run=np.full(n, 3, np.int64))
+    status = np.zeros(4 * geom.nbars, np.int64)
+    status[[5, 18, 33]] = [1, 4, 2]                        # absent, no data (dropped) and compensated (kept)
+    cond = SimpleNamespace(status=status, deviation=z["deviation"])
+    cfg = ChainConfig(lookup=lcfg)
+    Q = CH.charges(steps, None, geom, cond, cfg, None, key=21, tabs=tables, pdg=z["pdg"])
+    s, c, t = O.make_photons_lookup(steps, z["pdg"], geom, lcfg, tables, z["deviation"], 21)
+    keep = (status[c] & 0b101) == 0
+    s, c, t = s[keep], c[keep], t[keep]
+    label = ((steps["subrun"][s] << 20) | steps["event"][s]) * 32768 + c
+    o = np.argsort(label, kind="stable")
+    u, start, cnt = np.unique(label[o], return_index=True, return_counts=True)
+    key = np.empty(len(label), np.int64)
+    key[o] = np.arange(len(label)) - np.repeat(start, cnt)  # index of the photon within its SiPM, input order
+    Qo, _, _, _, st = O.sipm_groups(label, t, s, key, lambda L: np.full(len(L), 3), cfg.sipm, 21, cfg.window[1])
+    assert st == 0 and len(Qo["time"]) > 1000
+    for k in ("chan", "time", "charge", "pe", "photon"):
+        assert np.array_equal(Q[k], Qo[k]), k
+    with pytest.raises(ValueError):
+        CH.charges(steps, None, geom, cond, ChainConfig(), None, key=21, tabs=tables, pdg=z["pdg"])
