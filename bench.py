@@ -474,6 +474,8 @@ def main():
     ap.add_argument("--serve-load", type=float, default=0.8)
     ap.add_argument("--lookup-rows", type=int, default=1 << 20,
                     help="(step, SiPM) rows of the lookup-table photon model measurement (0: skip)")
+    ap.add_argument("--lookup-precision", default="both", choices=["both", "fp64", "fp32"],
+                    help="precision of the lookup-table measurement")
     ap.add_argument("--uneven-waveforms", type=int, default=1 << 22,
                     help="waveforms of the uneven batched pulse-fit measurement (0: skip)")
     args = ap.parse_args()
@@ -767,10 +769,14 @@ def main():
 
     lookup = None
     if rank == 0 and args.lookup_rows > 0:
-        lookup = lookup_substeps(args.lookup_rows)
-        torch.cuda.empty_cache()
-        lookup["fp32_mixed"] = {k: v for k, v in lookup_substeps(args.lookup_rows, precision="fp32").items()
-                                if k in ("rows_per_s", "ms_per_call", "photons_per_row", "precision")}
+        if args.lookup_precision == "fp32":
+            lookup = lookup_substeps(args.lookup_rows, precision="fp32")
+        else:
+            lookup = lookup_substeps(args.lookup_rows)
+            torch.cuda.empty_cache()
+            if args.lookup_precision == "both":
+                lookup["fp32_mixed"] = {k: v for k, v in lookup_substeps(args.lookup_rows, precision="fp32").items()
+                                        if k in ("rows_per_s", "ms_per_call", "photons_per_row", "precision")}
         torch.cuda.empty_cache()
 
     full = None

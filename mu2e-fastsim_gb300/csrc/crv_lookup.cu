@@ -249,25 +249,43 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLoo
     for (long long k0 = 0; k0 < nsub; k0 += 32) {
       const long long k = k0 + lane_id();
       SubBins S;
-      long long a[3] = {0, 0, 0};
+      S.bin[0] = S.bin[1] = S.bin[2] = -1;
+      S.t = 0.0;
+      int a[3] = {0, 0, 0};
       if (k < nsub) {
         S = substep_bins(L, R, r, k, nsub, bb, bth);
         for (int tb = 0; tb < 3; ++tb)
           if (S.bin[tb] >= 0) {
-            a[tb] = arrivals(L, R, seed, r, step, chan, k, tb, S.bin[tb], S.z);
-            if (a[tb] >= SUB_MAX_ARRIVALS) a[tb] = 0;
+            long long x = arrivals(L, R, seed, r, step, chan, k, tb, S.bin[tb], S.z);
+            a[tb] = x >= SUB_MAX_ARRIVALS ? 0 : int(x);
           }
       }
-      long long sum;
-      long long mine = warp_excl_ll(a[0] + a[1] + a[2], &sum);
-      long long q = o + mine;
-      if (k < nsub)
-        for (int tb = 0; tb < 3; ++tb)
-          for (int j = 0; j < int(a[tb]); ++j, ++q) {
-            o_step[q] = step;
-            o_chan[q] = chan;
-            o_time[q] = arrival_time(L, seed, step, chan, k, tb, S.bin[tb], j, S.t, status);
-          }
+      // arrivals spread over the lanes in (substep, table, arrival) order, as in the FP32-mixed pass
+      int sum;
+      const int pre = warp_excl(a[0] + a[1] + a[2], &sum);
+      for (int base = 0; base < sum; base += 32) {
+        const int p = base + lane_id();
+        int owner = 0;
+#pragma unroll
+        for (int step_ = 16; step_ > 0; step_ >>= 1) {
+          const int cand = owner + step_;
+          const int pc = __shfl_sync(0xffffffffu, pre, cand);
+          if (pc <= p) owner = cand;
+        }
+        const int opre = __shfl_sync(0xffffffffu, pre, owner);
+        const int a0 = __shfl_sync(0xffffffffu, a[0], owner), a1 = __shfl_sync(0xffffffffu, a[1], owner);
+        const int b0 = __shfl_sync(0xffffffffu, S.bin[0], owner), b1 = __shfl_sync(0xffffffffu, S.bin[1], owner);
+        const int b2 = __shfl_sync(0xffffffffu, S.bin[2], owner);
+        const double ot = __shfl_sync(0xffffffffu, S.t, owner);
+        if (p < sum) {
+          int j = p - opre, tb = 0, bn = b0;
+          if (j >= a0) { j -= a0; tb = 1; bn = b1; if (j >= a1) { j -= a1; tb = 2; bn = b2; } }
+          const long long q = o + p;
+          o_step[q] = step;
+          o_chan[q] = chan;
+          o_time[q] = arrival_time(L, seed, step, chan, k0 + owner, tb, bn, j, ot, status);
+        }
+      }
       o += sum;
     }
   }
@@ -325,18 +343,19 @@ __device__ __forceinline__ int find_bin_cos_f(const float* ce, int ne, float c) 
   return lo - 1;
 }
 
-__device__ __forceinline__ long long binomial_f(long long n, float p, const U4& w) {
+// 32-bit counts throughout: conversions between 64-bit integers and floats run on the FP64 pipe
+__device__ __forceinline__ int binomial_f(int n, float p, const U4& w) {
   if (n <= 0 || !(p > 0.f)) return 0;
   if (p >= 1.f) return n;
   const bool flip = p > 0.5f;
   const float q = flip ? 1.f - p : p;
   const float mean = float(n) * q;
-  long long k;
+  int k;
   if (mean > 256.f) {
     float z0, z1;
     Math<float>::normal_pair(w, &z0, &z1);
     const float x = rintf(mean + sqrtf(mean * (1.f - q)) * z0);
-    k = x < 0.f ? 0 : (x > float(n) ? n : (long long)x);
+    k = x < 0.f ? 0 : (x > float(n) ? n : int(x));
   } else {
     float u = f01(w.x);
     const float s = q / (1.f - q);
@@ -354,27 +373,38 @@ __device__ __forceinline__ long long binomial_f(long long n, float p, const U4& 
 
 // a row in FP32: local start, step vector, and per-row constants
 struct RowF {
-  float s[3], d[3], dev, mu, dt;
+  float s[3], d[3], dev, mu, dt, inv_nsub;
   double t0;
-  long long nsub, step, chan;
-  int bb, bth;
+  long long step, chan;
+  int nsub, bb, bth, n[3];
 };
+
+// double -> float on the integer pipe (truncating; zeros by their bits): every lane of the warp converts the same
+// row values, and an FP64-pipe conversion costs a whole warp slot of GB300's FP64 pipe
+__device__ __forceinline__ float to_f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if ((b << 1) == 0ull) return __uint_as_float(uint32_t(b >> 32));
+  return d2f_trunc(x);
+}
 
 __device__ __forceinline__ RowF load_row_f(const CrvSubstepRows& R, const EdgesF& E, long long r) {
   RowF w;
   for (int x = 0; x < 3; ++x) {
-    w.s[x] = float(R.s[3 * r + x]);
-    w.d[x] = float(R.d[3 * r + x]);
+    w.s[x] = to_f(R.s[3 * r + x]);
+    w.d[x] = to_f(R.d[3 * r + x]);
   }
-  w.dev = float(R.dev[r]);
-  w.mu = R.mu ? float(R.mu[r]) : 0.f;
+  w.dev = to_f(R.dev[r]);
+  w.mu = R.mu ? to_f(R.mu[r]) : 0.f;
   w.t0 = R.t0[r];
-  w.dt = float(R.t1[r] - R.t0[r]);
-  w.nsub = R.nsub[r];
+  w.dt = to_f(R.t1[r] - R.t0[r]);
+  w.nsub = int(R.nsub[r]);                                     // at most 2^20 (checked by row_ok)
+  w.inv_nsub = 1.f / float(w.nsub);
   w.step = R.step[r];
   w.chan = R.chan[r];
-  w.bb = find_bin_f(E.e[3], E.n[3], float(R.beta[r]));
-  w.bth = R.theta ? find_bin_f(E.e[4], E.n[4], float(R.theta[r])) : find_bin_cos_f(E.cth, E.n[4], float(R.cos_theta[r]));
+  const long long n3[3] = {R.n_scint[r], R.n_ck_s[r], R.n_ck_f[r]};
+  for (int t = 0; t < 3; ++t) w.n[t] = n3[t] < 0 ? 0 : (n3[t] > 0x7FFFFFFFll ? 0x7FFFFFFF : int(n3[t]));
+  w.bb = find_bin_f(E.e[3], E.n[3], to_f(R.beta[r]));
+  w.bth = R.theta ? find_bin_f(E.e[4], E.n[4], to_f(R.theta[r])) : find_bin_cos_f(E.cth, E.n[4], to_f(R.cos_theta[r]));
   return w;
 }
 
@@ -387,9 +417,9 @@ __device__ __forceinline__ GeoF geo_f(const CrvLookup& L) {
           float(L.hole_radius_x), float(L.hole_radius_y), float(L.fiber_radius), float(L.corner_radius)};
 }
 
-__device__ __forceinline__ void substep_bins_f(const GeoF& g, const EdgesF& E, const RowF& w, long long k, int bin[3],
+__device__ __forceinline__ void substep_bins_f(const GeoF& g, const EdgesF& E, const RowF& w, int k, int bin[3],
                                                float* z_out, float* frac_out) {
-  const float frac = (float(k) + 0.5f) / float(w.nsub);
+  const float frac = (float(k) + 0.5f) * w.inv_nsub;
   const float x = fmaf(w.d[0], frac, w.s[0]), y = fmaf(w.d[1], frac, w.s[1]), z = fmaf(w.d[2], frac, w.s[2]);
   const float ax = fabsf(x), ay = fabsf(y);
   bool insc = ax < g.ht && ay < g.hw && fabsf(z) < g.hl;
@@ -422,12 +452,12 @@ __device__ __forceinline__ void substep_bins_f(const GeoF& g, const EdgesF& E, c
   *frac_out = frac;
 }
 
-__device__ __forceinline__ long long arrivals_f(const CrvLookup& L, const CrvSubstepRows& R, const RowF& w,
-                                                uint32_t seed, long long r, long long k, int tb, int bin, float z) {
+__device__ __forceinline__ int arrivals_f(const CrvLookup& L, const CrvSubstepRows& R, const RowF& w, uint32_t seed,
+                                          int k, int tb, int bin, float z) {
   float pr = L.table[tb].prob[bin] * w.dev;
   if (R.mu) pr = pr * __expf(-w.mu * z);
   pr = fminf(pr, 1.f);
-  return binomial_f(photons_per_substep(R, tb, r), pr, sub_block(seed, w.step, w.chan, tb, SUB_CALL_BINOMIAL, 0, k, 0));
+  return binomial_f(w.n[tb], pr, sub_block(seed, w.step, w.chan, tb, SUB_CALL_BINOMIAL, 0, k, 0));
 }
 
 __device__ __forceinline__ int first_reaching_f(const uint8_t* __restrict__ wts, int n, float thr) {
@@ -441,7 +471,7 @@ __device__ __forceinline__ int first_reaching_f(const uint8_t* __restrict__ wts,
 
 // offset of arrival j from the row start time (FP32: substep time, delay, fibre decay)
 __device__ __forceinline__ float arrival_offset_f(const CrvLookup& L, float decay, uint32_t seed, const RowF& w,
-                                                  long long k, int tb, int bin, int j, float frac, Status* status) {
+                                                  int k, int tb, int bin, int j, float frac, Status* status) {
   const CrvLookupTable& T = L.table[tb];
   const U4 v = sub_block(seed, w.step, w.chan, tb, SUB_CALL_PHOTON, 0, k, j);
   float off = w.dt * frac + float(first_reaching_f(T.delays + (long long)bin * T.ndelay, T.ndelay,
@@ -476,17 +506,19 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count_f32(C
     long long tot = 0;
     if (row_ok(R, r, &nsub, status)) {
       const RowF w = load_row_f(R, E, r);
-      for (long long k = lane_id(); k < nsub; k += 32) {
+      int sum = 0;
+      for (int k = lane_id(); k < w.nsub; k += 32) {
         int bin[3];
         float z, frac;
         substep_bins_f(g, E, w, k, bin, &z, &frac);
         for (int tb = 0; tb < 3; ++tb)
           if (bin[tb] >= 0) {
-            long long a = arrivals_f(L, R, w, seed, r, k, tb, bin[tb], z);
+            int a = arrivals_f(L, R, w, seed, k, tb, bin[tb], z);
             if (a >= SUB_MAX_ARRIVALS) { set_flag(status, CRV_ST_LIMIT); a = 0; }
-            tot += a;
+            sum += a;
           }
       }
+      tot = sum;
     }
     tot = warp_sum(tot);
     if (lane_id() == 0) count[r] = tot;
@@ -513,28 +545,46 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit_f32(Cr
     if (!row_ok(R, r, &nsub, status)) continue;
     const RowF w = load_row_f(R, E, r);
     long long o = offset[r];
-    for (long long k0 = 0; k0 < nsub; k0 += 32) {
-      const long long k = k0 + lane_id();
+    for (int k0 = 0; k0 < w.nsub; k0 += 32) {
+      const int k = k0 + lane_id();
       int bin[3] = {-1, -1, -1};
       float z = 0.f, frac = 0.f;
-      long long a[3] = {0, 0, 0};
-      if (k < nsub) {
+      int a[3] = {0, 0, 0};
+      if (k < w.nsub) {
         substep_bins_f(g, E, w, k, bin, &z, &frac);
         for (int tb = 0; tb < 3; ++tb)
           if (bin[tb] >= 0) {
-            a[tb] = arrivals_f(L, R, w, seed, r, k, tb, bin[tb], z);
+            a[tb] = arrivals_f(L, R, w, seed, k, tb, bin[tb], z);
             if (a[tb] >= SUB_MAX_ARRIVALS) a[tb] = 0;
           }
       }
-      long long sum;
-      long long q = o + warp_excl_ll(a[0] + a[1] + a[2], &sum);
-      if (k < nsub)
-        for (int tb = 0; tb < 3; ++tb)
-          for (int j = 0; j < int(a[tb]); ++j, ++q) {
-            o_step[q] = w.step;
-            o_chan[q] = w.chan;
-            o_time[q] = w.t0 + double(arrival_offset_f(L, decay, seed, w, k, tb, bin[tb], j, frac, status));
-          }
+      // the chunk's arrivals in (substep, table, arrival) order, spread over the lanes: arrival p belongs to the last
+      // lane whose prefix is at most p (found by a shuffle binary search), so every lane has work
+      int sum;
+      const int pre = warp_excl(a[0] + a[1] + a[2], &sum);
+      for (int base = 0; base < sum; base += 32) {
+        const int p = base + lane_id();
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int cand = owner + step;
+          const int pc = __shfl_sync(0xffffffffu, pre, cand);
+          if (pc <= p) owner = cand;
+        }
+        const int opre = __shfl_sync(0xffffffffu, pre, owner);
+        const int a0 = __shfl_sync(0xffffffffu, a[0], owner), a1 = __shfl_sync(0xffffffffu, a[1], owner);
+        const int b0 = __shfl_sync(0xffffffffu, bin[0], owner), b1 = __shfl_sync(0xffffffffu, bin[1], owner);
+        const int b2 = __shfl_sync(0xffffffffu, bin[2], owner);
+        const float ofrac = __shfl_sync(0xffffffffu, frac, owner);
+        if (p < sum) {
+          int j = p - opre, tb = 0, bn = b0;
+          if (j >= a0) { j -= a0; tb = 1; bn = b1; if (j >= a1) { j -= a1; tb = 2; bn = b2; } }
+          const long long q = o + p;
+          o_step[q] = w.step;
+          o_chan[q] = w.chan;
+          o_time[q] = w.t0 + double(arrival_offset_f(L, decay, seed, w, k0 + owner, tb, bn, j, ofrac, status));
+        }
+      }
       o += sum;
     }
   }
