@@ -124,3 +124,28 @@ def test_charges_with_lookup_tables_match_the_oracle():
         assert np.array_equal(Q[k], Qo[k]), k
     with pytest.raises(ValueError):
         CH.charges(steps, None, geom, cond, ChainConfig(), None, key=21, tabs=tables, pdg=z["pdg"])
+
+
+def test_lookup_edge_cases():
+    """Empty rows, rows without photons, a row beyond the substep key limit (rejected, not truncated), and steps whose
+    times are not finite (skipped, as the reference skips them)."""
+    from crvgpu import lookup as LK
+    from crvgpu.response import EngineError
+    from tests.test_oracle_lookup import lookup_chain_fixture
+    L, rows, _ = lookup_fixture()
+    empty = {k: v[:0] for k, v in rows.items()}
+    st, ch, tm = LK.substep_photons(L, empty, 1)
+    assert len(st) == len(ch) == len(tm) == 0
+    quiet = dict(rows, n_scint=np.zeros_like(rows["n_scint"]), n_ck_s=np.zeros_like(rows["n_ck_s"]),
+                 n_ck_f=np.zeros_like(rows["n_ck_f"]))
+    assert len(LK.substep_photons(L, quiet, 1)[0]) == 0
+    assert len(LK.substep_photons(L, quiet, 1, precision="fp32")[0]) == 0
+    long_row = {k: v[:4].copy() for k, v in rows.items()}
+    long_row["nsub"][2] = (1 << 20) + 1
+    with pytest.raises(EngineError):
+        LK.substep_photons(L, long_row, 1)
+    tables, geom, lcfg, steps, z = lookup_chain_fixture()
+    nan_steps = dict(steps, t0=np.full(len(z["pdg"]), np.nan))
+    model = LK.LookupModel(geom, lcfg, tables, z["deviation"])
+    s, c, t = model.make_photons(nan_steps, z["pdg"], 3)
+    assert s.numel() == c.numel() == t.numel() == 0

@@ -110,3 +110,24 @@ def test_fp64_resident_chain_matches(setup):
     part = slice_events(ds, 0, 200)
     rc = ResidentChain(eng, _trial_caps(eng, part), graph=True)
     _same(rc.run(part, 11), eng.run(part, 11))
+
+
+def test_empty_batch_and_step_capacity_growth(setup):
+    """A batch without events gives no clusters through the same graph; a batch with more steps than the capacity
+    grows it on the host when growth is on (and is refused otherwise) before anything runs."""
+    geom, cond, cfg, ds, CH = setup
+    from dataclasses import replace
+    from crvgpu.resident import ResidentChain
+    from crvgpu.serve import slice_events
+    eng = CH.ChainEngine(geom, cond, cfg)
+    caps = _trial_caps(eng, ds)
+    rc = ResidentChain(eng, caps, graph=True)
+    r = rc.run(slice_events(ds, 5, 5), 4)
+    assert r.n_events == 0 and all(v == 0 for v in r.counts.values())
+    _same(rc.run(ds, 4), eng.run(ds, 4))                  # the graph is still good after the empty batch
+    small = replace(caps, steps=ds.nsteps // 2)
+    with pytest.raises(ValueError):
+        ResidentChain(eng, small, graph=True).run(ds, 4)
+    grown = ResidentChain(eng, small, graph=True, grow=True)
+    _same(grown.run(ds, 4), eng.run(ds, 4))
+    assert grown.caps.steps >= ds.nsteps
