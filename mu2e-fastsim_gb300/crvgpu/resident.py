@@ -154,6 +154,8 @@ class ResidentChain:
         dev, c = self.device, caps
         self.caps = caps
         self._graph = None
+        # the previous buffers go first (called between batches, nothing in flight): growth does not need both sets
+        self.ws = self.st = self.cl = self.mem = self.ev = None
         i32, i64, f64, rd = torch.int32, torch.int64, torch.float64, self.real_dtype
         self.ev = dict(event=torch.zeros(c.events, dtype=i32, device=dev),
                        subrun=torch.zeros(c.events, dtype=i32, device=dev),
@@ -180,7 +182,6 @@ class ResidentChain:
         wsb = L.crv_chain_workspace(ctypes.byref(P), ctypes.byref(caps.c()))
         if wsb < 0:
             raise ValueError("crv_chain_workspace: invalid capacities")
-        self.ws = None
         self.ws = torch.empty(int(wsb) + 1024, dtype=torch.uint8, device=dev)
         self._C = _capi.CrvClusters(*[_capi.ptr(self.cl[k]) for k in ("event", "type", "pe", "start", "end", "slope",
                                                                       "avgtime", "poscalc", "pos", "sidepe",
