@@ -1,5 +1,6 @@
 """Serving loop host logic (CPU): the job generator draws the workload's knob ranges and Poisson arrivals; design
-points map onto the engine configuration; latency statistics."""
+points map onto the engine configuration; latency statistics; the scheduler (chunking, shortest-remaining-first and
+earliest-deadline picks, late arrivals joining at the next chunk, results joined in event order) over simulated slots."""
 import numpy as np
 import pytest
 
@@ -38,3 +39,76 @@ def test_latency_stats():
     assert st["jobs"] == 10 and st["p50_s"] == pytest.approx(np.percentile([0.5 * (i + 1) for i in range(10)], 50))
     assert st["p99_over_isolated"] == pytest.approx(2.0)
     assert st["events_per_s"] == pytest.approx(55000 / 14.0)
+
+
+@pytest.fixture
+def host_torch(monkeypatch):
+    """The serving loop's torch handle without the engine's CUDA-device gate (the fake slots below run no kernels)."""
+    import torch
+    from crvgpu import serve
+    monkeypatch.setattr(serve, "_torch", lambda: torch)
+
+
+class _FakeServe:
+    """ServeEngine's scheduler and result assembly over slots whose chunk work is simulated on the host: a chunk of
+    events [a, b) takes `per_event` seconds per event and yields a cluster column with one entry per event."""
+
+    def __new__(cls, n_slots, chunk, per_event=2e-6):
+        import time
+        import torch
+        from crvgpu.serve import ServeEngine, _Slot
+
+        class Fake(ServeEngine):
+            def _run_chunk(self, slot, job, a, b):
+                time.sleep(per_event * (b - a))
+                self.log.append((job.id, a, b, slot.index, time.perf_counter()))
+                return {"pe": torch.arange(a, b, dtype=torch.float64), "event": torch.full((b - a,), job.id)}
+
+        eng = object.__new__(Fake)
+        eng.chunk = chunk
+        eng.slots = [_Slot(i, None, None) for i in range(n_slots)]
+        eng.log = []
+        return eng
+
+
+def test_serving_results_join_chunks_in_event_order(host_torch):
+    from crvgpu.serve import Job
+    srv = _FakeServe(3, 100)
+    jobs = [Job(0, 950, first=10), Job(1, 40, first=5000), Job(2, 301, first=700)]
+    res = srv.run(jobs, realtime=False)
+    assert [r.id for r in res] == [0, 1, 2]
+    for j, r in zip(jobs, res):
+        assert np.array_equal(r.clusters["pe"], np.arange(j.first, j.first + j.n_events))
+        assert r.n_clusters == j.n_events and r.finish >= r.start
+    assert len(srv.log) == 10 + 1 + 4                          # chunks of at most 100 events
+    assert len({s for *_, s, _ in srv.log}) > 1                # the burst ran on several slots
+
+
+def test_srpt_serves_small_jobs_first_and_late_arrivals_at_the_next_chunk(host_torch):
+    from crvgpu.serve import Job
+    srv = _FakeServe(1, 50, per_event=1e-4)                    # 5 ms per 50-event chunk, 200 ms for the big job
+    big, small = Job(0, 2000, first=0), Job(1, 100, first=5000, arrival=0.05)
+    res = srv.run([big, small], realtime=True)
+    # the small job arrives while the big one runs and is served at the next chunk boundary, before the big one ends
+    assert res[1].finish < res[0].finish
+    assert res[1].start - res[1].arrival < 0.04
+    order = [jid for jid, *_ in srv.log]
+    first_small = order.index(1)
+    assert 0 < first_small < order.count(0) and order[first_small:first_small + 2] == [1, 1]
+
+
+def test_deadline_scheduling_orders_by_deadline(host_torch):
+    from crvgpu.serve import Job
+    srv = _FakeServe(1, 50, per_event=1e-6)
+    # all at once: earliest deadline = arrival + 2 x isolated time, so the smallest job first, as SRPT
+    jobs = [Job(0, 400), Job(1, 50), Job(2, 200)]
+    srv.run(jobs, realtime=False, policy="edf", iso_rate=1e6)
+    firsts = []
+    for jid, *_ in srv.log:
+        if jid not in firsts:
+            firsts.append(jid)
+    assert firsts == [1, 2, 0]
+    with pytest.raises(ValueError):
+        srv.run(jobs, realtime=False, policy="fifo")
+    with pytest.raises(ValueError):
+        srv.run(jobs, realtime=False, policy="edf")             # needs the isolated rate
