@@ -10,10 +10,14 @@ It restates the reference algorithm stage by stage:
   * digi grouping into reco waveforms (crv/crvfastsim/reco/pulsefit.py:319-345, crv/crvfastsim/chain.py:273-286);
   * pulse reconstruction with the bounded Levenberg-Marquardt Gumbel fit (pulsefit.py:49-316), vectorised NumPy;
   * the coincidence finder (crv/crvfastsim/reco/coinc.py:112-392, crv/crvfastsim/reco/coinc_cpu.py:11-51);
-  * the chain glue (crv/crvfastsim/chain.py:151-362).
+  * the chain glue (crv/crvfastsim/chain.py:151-362);
+  * the lookup-table photon model: row preparation and substeps in the C library with keyed draws
+    (crv/crvfastsim/response/photons.py:163-224, :292-356), its host setup here (table propagation fits and per-bar
+    ratios, photons.py:230-289) and make_photons over the (table, reflector) groups (photons.py:305-371).
 
 The deterministic NumPy stages are pinned bit for bit against fixtures generated from the reference itself
-(tests/golden/make_golden.py); the stochastic stages against the reference's known-answer tests and statistics.
+(tests/golden/make_golden.py); the stochastic stages, the lookup-table model included, against the reference's
+known-answer tests and statistics of its own outputs.
 Configuration objects are duck-typed: any object with the reference's field names works.
 """
 from __future__ import annotations
