@@ -2,6 +2,11 @@
 
 Host code is Python over PyTorch device memory; every stage runs in hand-written sm_103a CUDA behind the C ABI in
 include/crvgpu.h (libcrvgpu.so, loaded through ctypes).  There is no CPU fallback.
+
+Modules: chain (the reference's chain entry points and ChainEngine, stage by stage), resident (the whole chain in one
+call with explicit capacities, replayed as a CUDA graph), serve (continuous batching of design-point jobs), response /
+waveform / pulsefit / coinc (the stages), lookup (the lookup-table photon model), shard (event partition across ranks),
+config / params / geometry (configuration, launch parameters, geometry and synthetic workloads).
 """
 from . import config  # noqa: F401
 

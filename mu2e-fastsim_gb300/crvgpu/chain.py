@@ -1,6 +1,7 @@
 """Chain glue with the reference's entry points (crv/crvfastsim/chain.py): charges (:151), digis (:234),
 reco_waveforms (:273), clusters (:296); plus ChainEngine, the device-resident chain steps -> coincidence clusters
-used by the benchmark (every stage a CUDA launch sequence behind the C ABI; host syncs only to read sizes).
+stage by stage (every stage a CUDA launch sequence behind the C ABI; host reads only of the stage sizes).  The
+resident engine (crvgpu.resident, crv_chain) runs the same kernels in one call without those reads.
 
 Event key = (subrun << 20) | event; SiPM label = event key * CHAN_MULT + channel (CHAN_MULT 32768).
 """
