@@ -892,6 +892,19 @@ static void lrow_particle(const OrcLookupGroup *G, int64_t pdg, double *m, doubl
     }
 }
 
+/* stock beta from the mean of the start and end energies (massless: 1) */
+static double lrow_beta(double m, double p0, double p1) {
+    double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(p1 * p1 + m * m));
+    double beta = 1.0;
+    if (m > 0.0) {
+        double g = e / m;
+        double b2 = 1.0 - 1.0 / (g * g);
+        b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
+        beta = sqrt(b2);
+    }
+    return beta;
+}
+
 static double lrow_cerenkov(const double *map, int n, double beta, double q) {
     double x0 = 0.0, y0 = 0.0, v;
     int j = 0;
@@ -939,14 +952,7 @@ int64_t orc_lookup_rows(const OrcLookupGroup *G, uint32_t seed, const OrcLookupS
         double m, q;
         lrow_particle(G, S->pdg[i], &m, &q);
         double p0 = sqrt(S->px0[i] * S->px0[i] + S->py0[i] * S->py0[i] + S->pz0[i] * S->pz0[i]);
-        double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(S->p1[i] * S->p1[i] + m * m));
-        double beta = 1.0;
-        if (m > 0.0) {
-            double g = e / m;
-            double b2 = 1.0 - 1.0 / (g * g);
-            b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
-            beta = sqrt(b2);
-        }
+        double beta = lrow_beta(m, p0, S->p1[i]);
         double avg_s = G->yield[b] * S->edep[i];
         double avg_cs = lrow_cerenkov(G->ck_scint, G->nck_scint, beta, q) * S->len[i];
         double avg_cf = lrow_cerenkov(G->ck_fiber, G->nck_fiber, beta, q) * S->len[i];
@@ -987,4 +993,33 @@ int64_t orc_lookup_rows(const OrcLookupGroup *G, uint32_t seed, const OrcLookupS
         ++r0;
     }
     return nsim * ng;
+}
+
+/* Test hooks for the lookup model's helpers (the reference's own helper tests: crv/tests/test_photons.py:13-29). */
+void orc_find_bin_v(const double *e, int ne, int64_t n, const double *v, int32_t *out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = sub_find_bin(e, ne, v[i]);
+}
+void orc_find_bin_cos_v(const double *ce, int ne, int64_t n, const double *c, int32_t *out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = sub_find_bin_cos(ce, ne, c[i]);
+}
+void orc_cerenkov_v(const double *map, int nmap, int64_t n, const double *beta, const double *q, double *out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = lrow_cerenkov(map, nmap, beta[i], q[i]);
+}
+/* mass, charge and stock beta (mean of start and end energies) of particle codes with momenta p0, p1 */
+void orc_particle_beta_v(const int64_t *code, int ncode, const double *mass, const double *charge, int64_t n,
+                         const int64_t *pdg, const double *p0, const double *p1, double *m_out, double *q_out,
+                         double *beta_out) {
+    OrcLookupGroup G;
+    memset(&G, 0, sizeof(G));
+    G.pdg_code = code;
+    G.pdg_mass = mass;
+    G.pdg_charge = charge;
+    G.npdg = ncode;
+    for (int64_t i = 0; i < n; ++i) {
+        double m, q;
+        lrow_particle(&G, pdg[i], &m, &q);
+        m_out[i] = m;
+        q_out[i] = q;
+        beta_out[i] = lrow_beta(m, p0[i], p1[i]);
+    }
 }

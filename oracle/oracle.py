@@ -1252,3 +1252,46 @@ def make_photons_lookup(steps, pdg, geom, cfg, tables, deviation, seed):
     if not outs:
         return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0)
     return tuple(np.concatenate([o[i] for o in outs]) for i in range(3))
+
+
+def find_bin(edges, v):
+    """The lookup model's bin search (the stock findBin: the first i with e[i] <= v <= e[i+1]; -1 outside)."""
+    e = np.ascontiguousarray(edges, np.float64)
+    v = np.ascontiguousarray(v, np.float64)
+    out = np.zeros(len(v), np.int32)
+    lib().orc_find_bin_v(_p(e), ctypes.c_int(len(e)), ctypes.c_int64(len(v)), _p(v), _p(out))
+    return out
+
+
+def find_bin_cos(edges, c):
+    """The phi / theta bins found on cos: bins of arccos(c) over angle edges in [0, pi]."""
+    ce = np.ascontiguousarray(np.cos(np.asarray(edges, np.float64)))
+    c = np.ascontiguousarray(c, np.float64)
+    out = np.zeros(len(c), np.int32)
+    lib().orc_find_bin_cos_v(_p(ce), ctypes.c_int(len(ce)), ctypes.c_int64(len(c)), _p(c), _p(out))
+    return out
+
+
+def cerenkov_per_mm(beta, charge, cmap):
+    """Cherenkov photons per mm: linear in beta from (0, 0) through the map, flat beyond its end, times |charge|."""
+    m = np.ascontiguousarray(cmap, np.float64).reshape(-1, 2)
+    b = np.ascontiguousarray(beta, np.float64)
+    q = np.ascontiguousarray(charge, np.float64)
+    out = np.zeros(len(b))
+    lib().orc_cerenkov_v(_p(m), ctypes.c_int(len(m)), ctypes.c_int64(len(b)), _p(b), _p(q), _p(out))
+    return out
+
+
+def particle_beta(pdg, p0, p1):
+    """(mass, charge, stock beta) of particle codes with start / end momenta, as the row preparation uses them."""
+    codes = np.array(sorted(_PARTICLES), np.int64)
+    mass = np.array([_PARTICLES[c][0] for c in codes])
+    charge = np.array([_PARTICLES[c][1] for c in codes], np.float64)
+    pdg = np.ascontiguousarray(pdg, np.int64)
+    p0 = np.ascontiguousarray(p0, np.float64)
+    p1 = np.ascontiguousarray(p1, np.float64)
+    n = len(pdg)
+    m, q, b = np.zeros(n), np.zeros(n), np.zeros(n)
+    lib().orc_particle_beta_v(_p(codes), ctypes.c_int(len(codes)), _p(mass), _p(charge), ctypes.c_int64(n), _p(pdg),
+                              _p(p0), _p(p1), _p(m), _p(q), _p(b))
+    return m, q, b

@@ -142,3 +142,22 @@ def test_lookup_make_photons_oracle_matches_the_reference_statistically():
     assert 0.7 < chi2 < 1.4
     ks = np.max(np.abs(np.cumsum(hist) / hist.sum() - np.cumsum(z["ref_delay_hist"]) / z["ref_delay_hist"].sum()))
     assert ks < 0.02
+
+
+def test_lookup_helpers_pass_the_references_known_answers():
+    """The reference's own helper tests (crv/tests/test_photons.py:13-29): findBin's inclusive edges, Cherenkov
+    interpolation with the charge, particle charges (ions decoded) and the stock beta; plus the cos-space phi bins
+    against arccos."""
+    e = np.array([0.0, 1.0, 2.0, 3.0])
+    assert O.find_bin(e, [-0.1, 0.0, 0.5, 1.0, 2.999, 3.0, 3.1]).tolist() == [-1, 0, 0, 0, 2, 2, -1]
+    cmap = np.array([[0.5, 0.0], [0.6, 10.0], [1.0, 50.0]])
+    assert np.allclose(O.cerenkov_per_mm([0.25, 0.55, 0.8, 1.2], [1, 1, -2, 1], cmap), [0.0, 5.0, 60.0, 50.0])
+    m, q, b = O.particle_beta([13, -11, 22, 2212, 1000020040, 999], [105.66] * 6, [105.66] * 6)
+    assert q.tolist() == [-1, 1, 0, 1, 2, 0]
+    assert m[4] == pytest.approx(4 * 931.49410242) and m[5] == 0.0
+    _, _, b2 = O.particle_beta([13, 22], [105.6583755, 0.0], [105.6583755, 0.0])
+    assert b2[0] == pytest.approx(1 / np.sqrt(2)) and b2[1] == 1.0
+    phi_edges = np.linspace(0.0, np.pi, 6)
+    ang = np.r_[0.0, np.pi, np.random.default_rng(1).uniform(0, np.pi, 2000)]
+    assert np.array_equal(O.find_bin_cos(phi_edges, np.cos(ang)), O.find_bin(phi_edges, ang)) or \
+        np.mean(O.find_bin_cos(phi_edges, np.cos(ang)) == O.find_bin(phi_edges, ang)) > 0.999
