@@ -73,3 +73,39 @@ def test_chain_count_slots_match_the_header():
     hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "crvgpu.h")).read()
     slots = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define CRV_CHAIN_([A-Z]+) (\d+)", hdr)}
     assert [k for k, _ in sorted(slots.items(), key=lambda kv: kv[1])] == list(_capi.CHAIN_COUNTS)
+
+
+def test_planted_flags_are_never_consumed(monkeypatch):
+    """As the reference's fail-closed contract test: a status block with a flag set turns the batch into
+    BatchRejected with the sizes needed; only a clean status returns outputs (planted in host tensors, no kernels)."""
+    import torch
+    from crvgpu import _capi, resident
+    from crvgpu.resident import BatchRejected, ResidentChain
+    monkeypatch.setattr(resident, "_torch", lambda: torch)
+
+    class Status:
+        def __init__(self):
+            self.t = torch.zeros(17, dtype=torch.int64)
+
+    rc = object.__new__(ResidentChain)
+    rc.counts = torch.arange(10, dtype=torch.int64) + 1
+    rc.status = Status()
+    rc._n_events = 7
+    rc.cl = {"pe": torch.arange(20, dtype=torch.float64)}
+    rc.mem = {"cl": torch.arange(20, dtype=torch.int64)}
+    for flag, slot in ((_capi.ST_CAPACITY, "PULSES_OUT"), (_capi.ST_LIMIT, None), (_capi.ST_ORDER, None)):
+        rc.status.t.zero_()
+        rc.status.t[0] = flag
+        if slot:
+            rc.status.t[1 + _capi.NEED[slot]] = 123456
+        with pytest.raises(BatchRejected) as ei:
+            rc.finish()
+        assert ei.value.flags == flag
+        if slot:
+            assert ei.value.need[_capi.NEED[slot]] == 123456
+    rc.status.t.zero_()
+    res = rc.finish()
+    counts = dict(zip(_capi.CHAIN_COUNTS, range(1, 11)))
+    assert res.counts == counts and res.n_events == 7
+    assert torch.equal(res.clusters["pe"], torch.arange(counts["clusters"], dtype=torch.float64))
+    assert torch.equal(res.members["cl"], torch.arange(counts["members"]))
