@@ -161,3 +161,27 @@ def test_lookup_helpers_pass_the_references_known_answers():
     ang = np.r_[0.0, np.pi, np.random.default_rng(1).uniform(0, np.pi, 2000)]
     assert np.array_equal(O.find_bin_cos(phi_edges, np.cos(ang)), O.find_bin(phi_edges, ang)) or \
         np.mean(O.find_bin_cos(phi_edges, np.cos(ang)) == O.find_bin(phi_edges, ang)) > 0.999
+
+
+def test_engine_lookup_groups_match_the_oracle_setup(monkeypatch):
+    """The engine's host setup of the lookup model (groups in the reference's order, per-bar yield, extra delay and
+    attenuation, channel yield factors, Cherenkov maps) equals the oracle's restatement (tables built as host tensors:
+    no kernels run)."""
+    import torch
+    from crvgpu import lookup as LK
+    monkeypatch.setattr(LK, "_torch", lambda: torch)
+    tables, geom, cfg, _, z = lookup_chain_fixture()
+    model = LK.LookupModel(geom, cfg, tables, z["deviation"], device="cpu")
+    ref = O.lookup_groups(geom, cfg, tables, z["deviation"])
+    assert [(g["table"], g["reflector"]) for g in model.groups] == [(L.name, g["reflector"]) for L, g in ref]
+    for g, (L, og) in zip(model.groups, ref):
+        assert np.array_equal(g["in_group"].numpy(), og["in_group"])
+        for k, ok in (("yield_", "yield"), ("speed_k", "speed_k"), ("mu", "mu"), ("ck_scint", "ck_scint"),
+                      ("ck_fiber", "ck_fiber")):
+            assert np.array_equal(g[k].numpy().reshape(np.shape(og[ok])), og[ok]), k
+        assert g["DL"].half_length == og["half_length"]
+    assert np.array_equal(model.dev.numpy(), ref[0][1]["dev"])
+    with pytest.raises(ValueError):
+        bad = type(cfg)(**{**vars(cfg), "sectors": {**cfg.sectors, "T1": type(cfg.sectors["T1"])(
+            table="tabB", reflector=0, yield_per_mev=1.0)}})
+        LK.LookupModel(geom, bad, tables, z["deviation"], device="cpu")   # reflector 0 on a reflector-1 table
