@@ -19,8 +19,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram
   lookup_chain.npz  make_photons with two synthetic tables (reflector 0 and 1) on a two-sector geometry
-                 (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, and over 16 seeds
-                 the mean photons per (step, channel) and the arrival-delay histogram
+                 (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, the rows of
+                 iter_rows (every field but the drawn photon counts), and over 16 seeds the mean photons per (step,
+                 channel) and the arrival-delay histogram
 """
 import os
 import sys
@@ -550,8 +551,8 @@ def make_lookup_chain(seeds=16):
                             photon_yield_scale=0.94, photon_yield_variation_scale=1.0, speed_ratio={"EX": 1.1},
                             atten_ratio={"T1": 0.9, "EX1": 1.2})
     steps = _Steps(cols)
-    n = len(pdg)
-    key = {}
+    rows = list(PH.iter_rows(steps, pdg, geom, cfg, tables, deviation, np.random.default_rng(1)))
+    row_keys = ("s", "d", "t0", "t1", "nsub", "beta", "theta", "dev", "mu", "step", "chan")
     sums, hist, total = {}, np.zeros(96), 0
     for s in range(seeds):
         st, ch, tm = PH.make_photons(steps, pdg, geom, cfg, tables, deviation, np.random.default_rng(2000 + s))
@@ -573,6 +574,9 @@ def make_lookup_chain(seeds=16):
     out.update(ck=ck, speed_ratio=PH.bar_ratios(cfg.speed_ratio, geom), atten_ratio=PH.bar_ratios(cfg.atten_ratio, geom),
                ref_pairs=pairs, ref_pair_mean=np.array([sums[tuple(p)] for p in pairs], float) / seeds,
                ref_delay_hist=hist / seeds, ref_total=np.int64(total), ref_seeds=np.int64(seeds))
+    out["rows_groups"] = np.array([[L.name == "tabB", len(r["nsub"])] for L, r in rows], np.int64)
+    for k in row_keys:
+        out[f"rows_{k}"] = np.concatenate([np.asarray(r[k]) for _, r in rows])
     np.savez_compressed(HERE / "lookup_chain.npz", **out)
 
 

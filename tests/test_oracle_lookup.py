@@ -185,3 +185,21 @@ def test_engine_lookup_groups_match_the_oracle_setup(monkeypatch):
         bad = type(cfg)(**{**vars(cfg), "sectors": {**cfg.sectors, "T1": type(cfg.sectors["T1"])(
             table="tabB", reflector=0, yield_per_mev=1.0)}})
         LK.LookupModel(geom, bad, tables, z["deviation"], device="cpu")   # reflector 0 on a reflector-1 table
+
+
+def test_lookup_rows_match_the_references_rows():
+    """Row preparation against the reference's own iter_rows (photons.py:305-356): every field but the drawn photon
+    counts is deterministic, so the oracle's rows must equal the reference's (cos theta against the cosine of its
+    theta: arccos then cos, so within 1e-12)."""
+    tables, geom, cfg, steps, z = lookup_chain_fixture()
+    cols = {k: np.asarray(steps[k], np.float64) for k in ("x0", "y0", "z0", "x1", "y1", "z1", "px0", "py0", "pz0",
+                                                          "p1", "t0", "t1", "edep", "len")}
+    cols["bar"], cols["pdg"] = np.asarray(steps["bar"], np.int32), z["pdg"]
+    got = [O.lookup_rows(g, cols, 5) for _, g in O.lookup_groups(geom, cfg, tables, z["deviation"])]
+    # the reference yields a block per (table, reflector, SiPM); a group here holds its SiPM blocks in that order
+    blocks = z["rows_groups"]
+    assert [len(r["nsub"]) for r in got] == [int(blocks[blocks[:, 0] == t, 1].sum()) for t in (0, 1)]
+    cat = {k: np.concatenate([r[k] for r in got]) for k in got[0]}
+    for k in ("s", "d", "t0", "t1", "nsub", "beta", "dev", "mu", "step", "chan"):
+        assert np.array_equal(cat[k], z[f"rows_{k}"]), k
+    assert np.allclose(cat["cos_theta"], np.cos(z["rows_theta"]), rtol=0, atol=1e-12)
