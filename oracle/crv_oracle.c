@@ -1023,3 +1023,20 @@ void orc_particle_beta_v(const int64_t *code, int ncode, const double *mass, con
         beta_out[i] = lrow_beta(m, p0[i], p1[i]);
     }
 }
+
+/* Bins of every substep of every row (row-major; -1: none): out[3 * s + table]. */
+void orc_substep_bins(const OrcLookup *L, const OrcSubstepRows *R, int64_t nrows, int32_t *out) {
+    int64_t o = 0;
+    for (int64_t r = 0; r < nrows; ++r) {
+        int64_t nsub = R->nsub[r];
+        int bb = sub_find_bin(L->edges[3], L->nedges[3], R->beta[r]);
+        int bth = R->theta ? sub_find_bin(L->edges[4], L->nedges[4], R->theta[r])
+                           : sub_find_bin_cos(L->cos_theta_edges, L->nedges[4], R->cos_theta[r]);
+        for (int64_t k = 0; k < nsub; ++k, ++o) {
+            int bin[3];
+            double t, z;
+            sub_bins(L, R, r, k, nsub, bb, bth, bin, &t, &z);
+            for (int tb = 0; tb < 3; ++tb) out[3 * o + tb] = bin[tb];
+        }
+    }
+}

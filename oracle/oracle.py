@@ -1104,6 +1104,24 @@ def substep_photons(L, rows, seed):
     return st, ch, tm, bool(lim.value)
 
 
+def substep_bins(L, rows):
+    """[substeps, 3] bins of the scintillation, Cherenkov-in-scintillator and Cherenkov-in-fibre tables of every
+    substep of every row (row-major; -1 where the substep selects none)."""
+    k = _Keep()
+    S = _lookup_struct(L, k)
+    th = rows.get("theta")
+    mu = rows.get("mu")
+    R = _OrcRows(k(rows["s"], np.float64), k(rows["d"], np.float64), k(rows["t0"], np.float64),
+                 k(rows["t1"], np.float64), k(rows["beta"], np.float64), None if th is None else k(th, np.float64),
+                 k(rows["dev"], np.float64), None if mu is None else k(mu, np.float64), k(rows["nsub"], np.int64),
+                 k(rows["step"], np.int64), k(rows["chan"], np.int64), k(rows["n_scint"], np.int64),
+                 k(rows["n_ck_s"], np.int64), k(rows["n_ck_f"], np.int64),
+                 None if th is not None else k(rows["cos_theta"], np.float64))
+    out = np.zeros((int(np.sum(rows["nsub"])), 3), np.int32)
+    lib().orc_substep_bins(ctypes.byref(S), ctypes.byref(R), ctypes.c_int64(len(rows["nsub"])), _p(out))
+    return out
+
+
 def binomial(seed, n, p):
     """The substep sampler's Binomial(n[i], p[i]) draws (block keyed by i)."""
     n = np.ascontiguousarray(n, np.int64)

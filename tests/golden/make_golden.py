@@ -17,7 +17,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
   lookup.npz     a synthetic lookup table and (step, SiPM) rows with the statistics of the reference substep kernel
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
-                 delay histogram
+                 delay histogram; and, for the first 120 rows, the table bins the reference reads (its probability
+                 lookups recorded in substep order)
   lookup_chain.npz  make_photons with two synthetic tables (reflector 0 and 1) on a two-sector geometry
                  (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, the rows of
                  iter_rows (every field but the drawn photon counts), and over 16 seeds the mean photons per (step,
@@ -450,6 +451,29 @@ def synthetic_rows(rng, R=1500):
             "n_ck_s": rng.integers(0, 4, R), "n_ck_f": rng.integers(0, 30, R)}
 
 
+class _RecordingTable(np.ndarray):
+    """A probability column that logs the index arrays it is read with (the bins a substep kernel selects)."""
+
+    def __getitem__(self, idx):
+        if isinstance(idx, np.ndarray) and idx.dtype.kind in "iu":
+            _RecordingTable.log.append(np.asarray(idx).copy())
+        return np.asarray(self).__getitem__(idx)
+
+
+def reference_bins(L, rows):
+    """Per table, the bins the reference's substep kernel reads for these rows, in its substep order."""
+    from types import SimpleNamespace
+    out = {}
+    for name in ("scint", "ckscint", "ckfiber"):
+        tabs = {k: SimpleNamespace(**vars(t)) for k, t in L.tables.items()}
+        tabs[name].prob = np.asarray(L.tables[name].prob).view(_RecordingTable)
+        _RecordingTable.log = []
+        Lr = SimpleNamespace(**{**vars(L), "tables": tabs})
+        PH._substep_photons(Lr, rows, np.random.default_rng(0))
+        out[name] = np.concatenate(_RecordingTable.log) if _RecordingTable.log else np.zeros(0, np.int64)
+    return out
+
+
 def make_lookup(seeds=16):
     from types import SimpleNamespace
     rng = np.random.default_rng(73)
@@ -475,6 +499,9 @@ def make_lookup(seeds=16):
     out.update({f"row_{k}": v for k, v in rows.items()})
     out.update(ref_seeds=np.int64(seeds), ref_counts=counts / seeds, ref_delay_hist=hist / seeds,
                ref_total=np.int64(total))
+    sub = {k: v[:120] for k, v in rows.items()}
+    for name, b in reference_bins(L, sub).items():
+        out[f"ref_bins_{name}"] = b.astype(np.int32)
     np.savez_compressed(HERE / "lookup.npz", **out)
 
 

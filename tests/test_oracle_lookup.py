@@ -203,3 +203,17 @@ def test_lookup_rows_match_the_references_rows():
     for k in ("s", "d", "t0", "t1", "nsub", "beta", "dev", "mu", "step", "chan"):
         assert np.array_equal(cat[k], z[f"rows_{k}"]), k
     assert np.allclose(cat["cos_theta"], np.cos(z["rows_theta"]), rtol=0, atol=1e-12)
+
+
+def test_substep_bins_match_the_references_bins():
+    """Geometry and binning of every substep against the reference's own substep kernel: the bins it read from each
+    table (recorded by the fixture generator, in substep order) are the bins the oracle (and, bit-exact with it, the
+    GPU) selects."""
+    L, rows, z = lookup_fixture()
+    sub = {k: v[:120] for k, v in rows.items()}
+    bins = O.substep_bins(L, sub)
+    for t, name in enumerate(O.LOOKUP_TABLES):
+        ours = bins[:, t][bins[:, t] >= 0]
+        ref = z[f"ref_bins_{name}"]
+        assert len(ref) > 1000 or name == "ckfiber" and len(ref) > 1000 // 4
+        assert np.array_equal(ours, ref), name
