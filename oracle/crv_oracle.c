@@ -1040,3 +1040,9 @@ void orc_substep_bins(const OrcLookup *L, const OrcSubstepRows *R, int64_t nrows
         }
     }
 }
+
+/* The delay / emission index search for given bins and thresholds (test hook): out[i] = first j of row bins[i] of
+ * wts (n per row) whose running sum reaches thr[i]. */
+void orc_first_reaching_v(const uint8_t *wts, int n, int64_t m, const int64_t *bins, const double *thr, int32_t *out) {
+    for (int64_t i = 0; i < m; ++i) out[i] = sub_first_reaching(wts + bins[i] * (int64_t)n, n, thr[i]);
+}

@@ -1122,6 +1122,16 @@ def substep_bins(L, rows):
     return out
 
 
+def first_reaching(wts, bins, thr):
+    """Delay / emission index for bins and thresholds: the first j whose running sum of wts[bin] reaches thr."""
+    w = np.ascontiguousarray(wts, np.uint8)
+    b = np.ascontiguousarray(bins, np.int64)
+    t = np.ascontiguousarray(thr, np.float64)
+    out = np.zeros(len(b), np.int32)
+    lib().orc_first_reaching_v(_p(w), ctypes.c_int(w.shape[1]), ctypes.c_int64(len(b)), _p(b), _p(t), _p(out))
+    return out
+
+
 def binomial(seed, n, p):
     """The substep sampler's Binomial(n[i], p[i]) draws (block keyed by i)."""
     n = np.ascontiguousarray(n, np.int64)

@@ -17,8 +17,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
   lookup.npz     a synthetic lookup table and (step, SiPM) rows with the statistics of the reference substep kernel
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
-                 delay histogram; and, for the first 120 rows, the table bins the reference reads (its probability
-                 lookups recorded in substep order)
+                 delay histogram; for the first 120 rows, the table bins the reference reads (its probability
+                 lookups recorded in substep order); the delay / emission index search on random thresholds
   lookup_chain.npz  make_photons with two synthetic tables (reflector 0 and 1) on a two-sector geometry
                  (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, the rows of
                  iter_rows (every field but the drawn photon counts), and over 16 seeds the mean photons per (step,
@@ -502,6 +502,15 @@ def make_lookup(seeds=16):
     sub = {k: v[:120] for k, v in rows.items()}
     for name, b in reference_bins(L, sub).items():
         out[f"ref_bins_{name}"] = b.astype(np.int32)
+    # the delay / emission index search on random bins and thresholds (u x the bin's sum, u in [0, 1))
+    qrng = np.random.default_rng(17)
+    T = L.tables["scint"]
+    qb = qrng.integers(0, len(T.prob), 4000)
+    qd = qrng.random(4000) * T.delay_sum[qb]
+    qe = qrng.random(4000) * T.emis_sum[qb]
+    out.update(ref_search_bins=qb, ref_search_dthr=qd, ref_search_ethr=qe,
+               ref_search_delay=PH._first_above(T.delays, qb, qd).astype(np.int32),
+               ref_search_emis=PH._first_above(T.emis, qb, qe).astype(np.int32))
     np.savez_compressed(HERE / "lookup.npz", **out)
 
 

@@ -217,3 +217,12 @@ def test_substep_bins_match_the_references_bins():
         ref = z[f"ref_bins_{name}"]
         assert len(ref) > 1000 or name == "ckfiber" and len(ref) > 1000 // 4
         assert np.array_equal(ours, ref), name
+
+
+def test_delay_and_emission_search_match_the_reference():
+    """The index search of the delay and emission draws against the reference's _first_above (photons.py:118-137) on
+    4,000 random bins and thresholds: identical indices."""
+    L, _, z = lookup_fixture()
+    T = L.tables["scint"]
+    assert np.array_equal(O.first_reaching(T.delays, z["ref_search_bins"], z["ref_search_dthr"]), z["ref_search_delay"])
+    assert np.array_equal(O.first_reaching(T.emis, z["ref_search_bins"], z["ref_search_ethr"]), z["ref_search_emis"])
