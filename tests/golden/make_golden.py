@@ -19,6 +19,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram; for the first 120 rows, the table bins the reference reads (its probability
                  lookups recorded in substep order); the delay / emission index search on random thresholds
+  attach.npz     every find_event call of the reference's own attachment boundary tests
+                 (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
+                 pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
   lookup_chain.npz  make_photons with two synthetic tables (reflector 0 and 1) on a two-sector geometry
                  (photons.py:292-371): table propagation fits, per-bar speed / attenuation ratios, the rows of
                  iter_rows (every field but the drawn photon counts), and over 16 seeds the mean photons per (step,
@@ -616,10 +619,57 @@ def make_lookup_chain(seeds=16):
     np.savez_compressed(HERE / "lookup_chain.npz", **out)
 
 
+def make_attach():
+    import json
+    import pytest
+    records = []
+    orig = C.find_event
+
+    def recorded(p, G, status, cfg=None, vectorized=False):
+        out = orig(p, G, status, cfg if cfg is not None else C.FinderConfig(), vectorized=vectorized)
+        if not vectorized:
+            records.append(({k: np.asarray(v).copy() for k, v in p.items()}, G, np.asarray(status).copy(),
+                            cfg if cfg is not None else C.FinderConfig(), out))
+        return out
+
+    C.find_event = recorded
+    try:
+        # the config-schema test needs the reference's core library (not part of the finder); the rest run
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "not test_config_schema",
+                          str(REF / "tests" / "test_coinc_attachment_cpu.py")])
+    finally:
+        C.find_event = orig
+    assert rc == 0, f"the reference's attachment tests failed here ({rc})"
+    out = {"n": np.int64(len(records))}
+    for i, (p, G, status, cfg, rows) in enumerate(records):
+        tag = f"a{i}"
+        n = len(p["idx"])
+        P = {"ev": np.zeros(n, np.int64), **{k: np.asarray(p[k]) for k in ("idx", "bar", "sipm", "time", "pe", "seq")}}
+        fl = flatten_clusters([(0, rows)])
+        for k, v in fl.items():
+            out[f"{tag}_scalar_{k}"] = v
+        for k in ("ev", "idx", "bar", "sipm", "time", "pe", "seq"):
+            out[f"{tag}_in_{k}"] = P[k]
+        out[f"{tag}_status"] = status
+        for k in ("sector", "layer", "counter_in_type", "x", "y", "pos", "length_dir", "sector_type", "pos_side0",
+                  "pos_side1", "sipms_side0", "sipms_side1"):
+            out[f"{tag}_G_{k}"] = np.asarray(getattr(G, k))
+        out[f"{tag}_G_sector_names"] = np.array(G.sector_names)
+        names = [n_ for n_ in G.sector_names if n_ in cfg.cuts]
+        out[f"{tag}_cut_names"] = np.array(names)
+        out[f"{tag}_cuts"] = cuts_array(cfg, names)
+        flags = {k: getattr(cfg, k) for k in ("fiber_signal_speed", "max_time_interval", "time_offset",
+                                             "compensate_status_bits", "ignore_secondary_pulses",
+                                             "big_cluster_threshold", "add_opposite_side_pulses")}
+        flags["compensate_status_bits"] = list(flags["compensate_status_bits"])
+        out[f"{tag}_flags"] = np.array(json.dumps(flags))
+    np.savez_compressed(HERE / "attach.npz", **out)
+
+
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup),
-                     ("lookup_chain", make_lookup_chain)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

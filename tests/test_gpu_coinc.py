@@ -64,3 +64,21 @@ def test_find_event_single_event_signature(golden):
     first = np.flatnonzero(sel)
     for r, i in zip(rows, first):
         assert r["pulses"] == list(g["eight_scalar_mem_idx"][g["eight_scalar_mem_cl"] == i])
+
+
+def test_coincidences_match_the_reference_attachment_cases(golden):
+    """The reference's own attachment boundary cases (every find_event call of crv/tests/test_coinc_attachment_cpu.py:
+    strict windows, ties, order, configuration flags) on the GPU: same clusters and members, properties within 1e-12."""
+    from crvgpu import coinc as CO
+    from tests.test_oracle_golden import attach_case
+    g = golden("attach.npz")
+    for i in range(int(g["n"])):
+        G, cfg, status, P = attach_case(g, i)
+        rows = CO.find_event(P, G, status, cfg)
+        tag = f"a{i}_scalar_"
+        assert len(rows) == len(g[tag + "pe"]), i
+        for c, r in enumerate(rows):
+            assert list(r["pulses"]) == list(g[tag + "mem_idx"][g[tag + "mem_cl"] == c]), i
+            for k in ("pe", "start", "end", "slope", "avgtime"):
+                np.testing.assert_allclose(r[k], g[tag + k][c], rtol=1e-12, atol=1e-9, err_msg=f"a{i}.{k}")
+            assert list(r["sidehits"]) == list(g[tag + "sidehits"][c]), i

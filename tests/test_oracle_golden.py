@@ -114,3 +114,34 @@ def test_coincidences_match_reference(golden, tag):
     assert_same(mem_cl, g[f"{tag}_scalar_mem_cl"], "mem_cl")
     assert_same(mem_idx, g[f"{tag}_scalar_mem_idx"], "mem_idx")
     assert len(got["ev"]) > 0
+
+
+def attach_case(g, i):
+    """Geometry, finder configuration, status and pulses of case i of the reference's attachment tests."""
+    import json
+    tag = f"a{i}"
+    G = _geom(g, tag)
+    cuts = {str(n): CF.SectorCuts(*[int(v) if j == 6 else float(v) for j, v in enumerate(row)])
+            for n, row in zip(g[f"{tag}_cut_names"], g[f"{tag}_cuts"])}
+    flags = json.loads(str(g[f"{tag}_flags"]))
+    flags["compensate_status_bits"] = tuple(flags["compensate_status_bits"])
+    P = {k: g[f"{tag}_in_{k}"] for k in ("idx", "bar", "sipm", "time", "pe", "seq")}
+    return G, CF.FinderConfig(cuts=cuts, **flags), g[f"{tag}_status"], P
+
+
+def test_coincidences_match_the_reference_attachment_cases(golden):
+    """The reference's own boundary cases (strict windows, ties, order, flags; every find_event call of
+    crv/tests/test_coinc_attachment_cpu.py): same clusters, members and properties."""
+    g = golden("attach.npz")
+    n = int(g["n"])
+    assert n >= 20
+    for i in range(n):
+        G, cfg, status, P = attach_case(g, i)
+        rows = O.find_event(P, G, status, cfg)
+        tag = f"a{i}_scalar_"
+        assert len(rows) == len(g[tag + "pe"]), i
+        for c, r in enumerate(rows):
+            assert list(r["pulses"]) == list(g[tag + "mem_idx"][g[tag + "mem_cl"] == c]), i
+            for k in ("pe", "start", "end", "slope", "avgtime"):
+                assert_same(np.asarray(r[k]), g[tag + k][c], f"a{i}.{k}")
+            assert list(r["sidehits"]) == list(g[tag + "sidehits"][c]), i
