@@ -19,6 +19,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram; for the first 120 rows, the table bins the reference reads (its probability
                  lookups recorded in substep order); the delay / emission index search on random thresholds
+  pulsetests.npz every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py:
+                 injected-parameter recovery, below threshold, pedestal undershoot; at its stock 12.5 ns period), with
+                 the reference's outputs
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -619,6 +622,37 @@ def make_lookup_chain(seeds=16):
     np.savez_compressed(HERE / "lookup_chain.npz", **out)
 
 
+def make_pulsetests():
+    import pytest
+    records = []
+    orig = PF.reconstruct
+
+    def recorded(adc, n, start_tdc, pedestal_db, calib_area, calib_height, cfg=None, *a, **k):
+        out = orig(adc, n, start_tdc, pedestal_db, calib_area, calib_height,
+                   cfg if cfg is not None else PF.RecoConfig(), *a, **k)
+        records.append(((adc, n, start_tdc, pedestal_db, calib_area, calib_height), out))
+        return out
+
+    set_period(12.5)                                # the tests are written for the stock period
+    PF.reconstruct = recorded
+    try:
+        # the two waveform tests need the Mu2e single-PE template file (absent); the rest run
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "not waveform_linear and not roundtrip",
+                          str(REF / "tests" / "test_reco_pulsefit.py")])
+    finally:
+        PF.reconstruct = orig
+        set_period(PERIOD)
+    assert rc == 0, f"the reference's pulse-fit tests failed here ({rc})"
+    out = {"n": np.int64(len(records)), "period": np.array([12.5])}
+    for i, (args, r) in enumerate(records):
+        tag = f"r{i}"
+        for k, v in zip(("adc", "n", "start", "ped", "area", "height"), args):
+            out[f"{tag}_{k}"] = np.asarray(v)
+        for k, v in r.items():
+            out[f"{tag}_out_{k}"] = np.asarray(v)
+    np.savez_compressed(HERE / "pulsetests.npz", **out)
+
+
 def make_attach():
     import json
     import pytest
@@ -669,7 +703,7 @@ def make_attach():
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

@@ -107,3 +107,17 @@ def test_graph_fitter_and_launch_shapes_match_the_engine():
             assert torch.equal(other[k], ref[k]), (prec, k)
             assert torch.equal(got[k], ref[k]), (prec, k)
             assert torch.equal(got2[k], ref[k]), (prec, k)
+
+
+def test_pulsefit_matches_the_references_own_tests(golden):
+    """The reference's own pulse-fit test calls (injected single pulses, below threshold, pedestal undershoot; 12.5
+    ns) on the GPU: integer outputs identical, parameters as the reference within the fit's 1e-8."""
+    from crvgpu import pulsefit as PF
+    g = golden("pulsetests.npz")
+    period = float(g["period"][0])
+    for i in range(int(g["n"])):
+        tag = f"r{i}"
+        args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
+        r = PF.reconstruct(*args, CF.RecoConfig(period=period))
+        ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f"{tag}_out_")}
+        compare(r, ref, tag)

@@ -145,3 +145,19 @@ def test_coincidences_match_the_reference_attachment_cases(golden):
             for k in ("pe", "start", "end", "slope", "avgtime"):
                 assert_same(np.asarray(r[k]), g[tag + k][c], f"a{i}.{k}")
             assert list(r["sidehits"]) == list(g[tag + "sidehits"][c]), i
+
+
+def test_pulsefit_matches_the_references_own_tests(golden):
+    """Every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py: 200 injected
+    single pulses, a pulse below threshold, a pedestal undershoot; 12.5 ns), replayed: the reference's outputs."""
+    g = golden("pulsetests.npz")
+    period = float(g["period"][0])
+    assert int(g["n"]) == 3
+    for i in range(int(g["n"])):
+        tag = f"r{i}"
+        args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
+        r = O.reconstruct(*args, CF.RecoConfig(period=period), period)
+        keys = [k[len(tag) + 5:] for k in g.files if k.startswith(f"{tag}_out_")]
+        assert set(keys) == set(r)
+        for k in keys:
+            assert_same(r[k], g[f"{tag}_out_{k}"], f"{tag}.{k}")
