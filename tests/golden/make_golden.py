@@ -1,7 +1,8 @@
 """Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
-(NAME: pulsefit, concat, waveform, coinc, stats, lookup; default all)
+(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, lookup, lookup_chain, attach, pulsetests;
+default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -12,6 +13,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   concat.npz     concat_waveforms grouping (pulsefit.py:319-345)
   waveform.npz   _synthesize digis with and without injected noise (crv/crvfastsim/reco/waveform.py:96-172) and the
                  resampled Gumbel single-PE template (waveform.py:46-62)
+  waveform_gate.npz  _synthesize digis under eight digitisation windows cut from the ungated starts (exact and
+                 one-ulp-inside edges, single-start windows, lower edges inside long pulse trains)
   coinc.npz      find_event clusters on three geometries, scalar and vectorised combination checks
                  (crv/crvfastsim/reco/coinc.py:289-392, coinc_cpu.py:11-51)
   stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
@@ -240,6 +243,58 @@ def make_waveform():
     for k, v in b.items():
         out[f"noisy_{k}"] = v
     np.savez_compressed(HERE / "waveform.npz", **out)
+
+
+def make_waveform_gate():
+    """The digitisation window gate of the ZS scan (waveform.py:150-160): a start outside the window neither makes a
+    digi nor moves the scan on, so a trigger before the gate does not hide an in-gate continuation, and both bounds
+    are inclusive.  Windows are cut from the ungated starts themselves (exact edges, one ulp inside, one-start
+    windows, mid-train lower edges) on a sample with long pulse trains (many consecutive 12-sample digis)."""
+    set_period(PERIOD)
+    rng = np.random.default_rng(21)
+    tmpdir = tempfile.mkdtemp()
+    path = os.path.join(tmpdir, "gumbel_spe.txt")
+    gumbel_template_file(path)
+    cfg = WF.WaveformConfig(single_pe_file=path, single_pe_stretch=1.0, min_voltage=5 * 0.0055)
+    tmpl = WF.single_pe_template(cfg.single_pe_file, cfg.single_pe_precision, cfg.single_pe_stretch,
+                                 cfg.single_pe_max_time)
+    chan, time, charge = charges_sample(rng, nchan=60)
+    qref = 2.652e-13
+    trains = []
+    for c in range(12):                                                  # steady trains of 20-90 samples
+        t0 = rng.uniform(-60.0, 1200.0)
+        tt = t0 + np.arange(0.0, rng.uniform(250.0, 1100.0), rng.uniform(1.0, 2.5))
+        trains.append((np.full(len(tt), 50000 + 3 * c), tt, np.full(len(tt), 1.5 * qref)))
+    chan = np.concatenate([chan] + [t[0] for t in trains])
+    time = np.concatenate([time] + [t[1] for t in trains])
+    charge = np.concatenate([charge] + [t[2] for t in trains])
+    uch = np.unique(chan)
+    tdc0_tab = rng.uniform(0, PERIOD, len(uch))
+    lut = lambda lab: tdc0_tab[np.searchsorted(uch, lab)]              # noqa: E731
+    base = WF._synthesize(chan, time, charge, lut, cfg, (-1e5, 1e5), None)
+    S = np.unique(base["start"])
+    up, dn = np.inf, -np.inf
+    tr = base["chan"] >= 50000
+    first_train = np.array([base["start"][tr & (base["chan"] == c)].min() for c in np.unique(base["chan"][tr])])
+    q = lambda f: S[int(f * (len(S) - 1))]                               # noqa: E731
+    windows = [
+        (q(0.2), q(0.8)),                                                # exact inclusive edges
+        (np.nextafter(q(0.2), up), np.nextafter(q(0.8), dn)),            # one ulp inside: both edge starts drop
+        (q(0.5), np.nextafter(q(0.5), up)),                              # a single start
+        (np.nextafter(q(0.5), dn), q(0.5)),
+        (float(np.median(first_train)) + 5.5 * PERIOD, 1500.0),          # lower edge inside the trains
+        (float(first_train.min()) + 13.0 * PERIOD, float(first_train.max()) + 30.25 * PERIOD),
+        (200.0, 1500.0),
+        (-1e5, 1e5),
+    ]
+    out = dict(template=tmpl, chan=chan, time=time, charge=charge, uch=uch, tdc0_tab=tdc0_tab,
+               windows=np.array(windows), min_voltage=np.array([cfg.min_voltage]),
+               stretch=np.array([cfg.single_pe_stretch]))
+    for i, w in enumerate(windows):
+        r = WF._synthesize(chan, time, charge, lut, cfg, w, None)
+        for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc"):
+            out[f"w{i}_{k}"] = r[k]
+    np.savez_compressed(HERE / "waveform_gate.npz", **out)
 
 
 # ---------------------------------------------------------------------------------------------------------------------
@@ -702,6 +757,7 @@ def make_attach():
 
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
+                     ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup),
                      ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:

@@ -74,6 +74,20 @@ def test_waveform_matches_reference(golden, mode):
         assert tuple(g["noise_shape"]) == (len(r["cluster_chan"]), g["noise_Z"].shape[1])
 
 
+@pytest.mark.parametrize("i", range(8))
+def test_waveform_window_gate_matches_reference(golden, i):
+    """Digitisation windows cut from the ungated starts: exact and one-ulp-inside edges, single-start windows, lower
+    edges inside long pulse trains (an excluded start does not move the scan on)."""
+    g = golden("waveform_gate.npz")
+    cfg = _wf_cfg(g)
+    uch, tab = g["uch"], g["tdc0_tab"]
+    lut = lambda lab: tab[np.searchsorted(uch, lab)]                     # noqa: E731
+    r = O.synthesize(g["chan"], g["time"], g["charge"], lut, g["template"], cfg, 12.55, tuple(g["windows"][i]), None)
+    for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc"):
+        assert_same(r[k], g[f"w{i}_{k}"], f"w{i}.{k}")
+    assert len(r["chan"]) > 0
+
+
 def _geom(g, tag):
     G = SimpleNamespace(**{k: g[f"{tag}_G_{k}"] for k in ("sector", "layer", "counter_in_type", "x", "y", "pos",
                                                            "length_dir", "sector_type", "pos_side0", "pos_side1",
