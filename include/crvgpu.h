@@ -93,7 +93,8 @@ typedef struct CrvParams {
     double period, spe_precision, spe_max_time, spe_ref_charge, min_voltage, noise_sigma, adc_conversion;
     double window_lo, window_hi, feb_phase_width;
     int32_t samples_zs, adc_pedestal, min_adc, max_adc, template_len, feb_key_mode; /* 0 roc*1000+feb, 1 feb */
-    int32_t noise_on, pad1;
+    int32_t noise_on;
+    int32_t pixel_lrint;         /* SiPM pixel id of a photon-map point: 0 "truncate" (the bin), 1 "lrint" (rounded) */
     /* pulse reconstruction */
     double min_adc_difference, default_beta, min_beta, max_beta, max_time_difference, min_height_ratio;
     double max_height_ratio, le_time_factor, pedestal_undershoot, time_offset_scale, limit_tolerance, knife_edge_adc;
@@ -136,7 +137,8 @@ typedef struct CrvChannels {
     int32_t pad;
 } CrvChannels;
 
-/* SiPM pixel model tables: photon-map running sums (1,600 bins x * 40 + y) and the dead-pixel bitmap (50 words). */
+/* SiPM pixel model tables: photon-map running sums (1,600 bins x * 40 + y) and the dead-pixel bitmap over pixel ids
+ * x * 41 + y, x and y in 0..40 (53 words; crv/crvfastsim/response/sipm.py:22 NPIX = 41). */
 typedef struct CrvPixels {
     const double *cum;
     const uint32_t *dead_bits;

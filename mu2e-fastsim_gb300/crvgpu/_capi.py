@@ -36,7 +36,7 @@ _PARAM_FIELDS = [
     *[(n, c_f64) for n in ("period", "spe_precision", "spe_max_time", "spe_ref_charge", "min_voltage", "noise_sigma",
                            "adc_conversion", "window_lo", "window_hi", "feb_phase_width")],
     *[(n, c_i32) for n in ("samples_zs", "adc_pedestal", "min_adc", "max_adc", "template_len", "feb_key_mode",
-                           "noise_on", "pad1")],
+                           "noise_on", "pixel_lrint")],
     *[(n, c_f64) for n in ("min_adc_difference", "default_beta", "min_beta", "max_beta", "max_time_difference",
                            "min_height_ratio", "max_height_ratio", "le_time_factor", "pedestal_undershoot",
                            "time_offset_scale", "limit_tolerance", "knife_edge_adc")],

@@ -43,7 +43,7 @@ class ResponseConfig:
     photon_yield_variation_scale: float = 1.0
 
 
-PIXEL_IDS = ("truncate",)
+PIXEL_IDS = ("lrint", "truncate")          # crv/crvfastsim/response/sipm.py:23
 
 
 @dataclass

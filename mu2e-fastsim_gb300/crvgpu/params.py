@@ -4,7 +4,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _capi
-from .config import (PERIOD, ChainConfig, FinderConfig, RecoConfig, ResponseConfig, SiPMConfig, WaveformConfig)
+from .config import (PERIOD, PIXEL_IDS, ChainConfig, FinderConfig, RecoConfig, ResponseConfig, SiPMConfig, WaveformConfig)
 
 
 def p_fire(sc, v):
@@ -16,8 +16,8 @@ def validate_sipm(sc):
     (the reference's contract refuses it as well, crv/crvfastsim/response/contract.py:5-12)."""
     if sc.thermal_rate != 0:
         raise ValueError("CRV response: unsupported SiPM processes: ['thermal_rate']")
-    if getattr(sc, "pixel_id", "truncate") != "truncate":
-        raise ValueError(f"CRV response: SiPM pixel_id must be 'truncate', got {sc.pixel_id!r}")
+    if getattr(sc, "pixel_id", "truncate") not in PIXEL_IDS:
+        raise ValueError(f"CRV response: SiPM pixel_id must be one of {PIXEL_IDS}, got {sc.pixel_id!r}")
     if sc.n_pixels_x != 40 or sc.n_pixels_y != 40:
         raise ValueError("CRV response: the pixel grid is 40 x 40")
 
@@ -61,6 +61,7 @@ def make_params(cfg: ChainConfig = None, seed: int = 0, *, response: ResponseCon
     P.t_end = float(t_end if t_end is not None else win[1])
     P.n_pixels_x, P.n_pixels_y = sc.n_pixels_x, sc.n_pixels_y
     P.uniform_map = 1 if uniform_map else 0
+    P.pixel_lrint = 1 if getattr(sc, "pixel_id", "truncate") == "lrint" else 0
     P.charge_factor = int(charge_factor)
     period = getattr(wc, "period", PERIOD)
     P.period = period

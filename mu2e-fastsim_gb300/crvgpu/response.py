@@ -165,11 +165,12 @@ class PixelTables:
             raise ValueError("photon map must be 40 x 40")
         self.uniform_map = bool(np.all(pm == pm.flat[0]))
         self.cum = torch.from_numpy(np.cumsum(pm.ravel())).to(device)
-        words = np.zeros(50, np.uint32)
+        words = np.zeros(64, np.uint32)                  # pixel ids x * 41 + y over the 41 x 41 state (53 words used)
         for x, y in sc.inactive:
-            if 0 <= x < 40 and 0 <= y < 40:
-                q = x * 40 + y
-                words[q >> 5] |= np.uint32(1) << np.uint32(q & 31)
+            if not (0 <= x < 41 and 0 <= y < 41):
+                raise ValueError(f"SiPM inactive pixel ({x}, {y}) is outside the 41 x 41 pixel state")
+            q = x * 41 + y
+            words[q >> 5] |= np.uint32(1) << np.uint32(q & 31)
         self.dead_bits = torch.from_numpy(words.view(np.int32)).to(device)
 
     def c_pixels(self):

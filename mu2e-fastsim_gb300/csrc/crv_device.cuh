@@ -12,7 +12,13 @@
 
 namespace crv {
 
-constexpr int NPX = 1600;          // 40 x 40 pixels, id = x * 40 + y
+constexpr int NPX = 1600;          // photon-map bins: 40 x 40, bin = x * 40 + y
+// Pixel ids x * 41 + y over a 41 x 41 state (crv/crvfastsim/response/sipm.py:22 NPIX = 41): "lrint" rounds a
+// photon-map point to pixel 40 at the far edge of bin 39
+constexpr int PXS = 41;
+constexpr int NPS = PXS * PXS;     // 1,681 pixel states
+constexpr int NPS_ALLOC = 1688;    // NPS rounded up to 8 (keeps the following shared arrays 16-byte aligned)
+constexpr int DEAD_WORDS = 53;     // dead-pixel bitmap words over the 1,681 ids
 constexpr int MAX_GEN = 15;        // cross-talk generations per photon
 constexpr int MAX_IDX = 63;        // nodes per generation
 constexpr uint32_t ST_COUNT = 1, ST_PHOTON = 2, ST_SIPM = 3, ST_TDC0 = 4, ST_NOISE = 5, ST_STEPS = 6;

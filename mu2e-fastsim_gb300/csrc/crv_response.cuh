@@ -346,8 +346,8 @@ template <typename R>
 __host__ __device__ inline size_t sipm_smem_per_warp(int cap) {
   size_t b = 0;
   b += size_t(cap) * (sizeof(R) + 8);          // ph_t, ph_key, ph_loc
-  b += NPX * sizeof(R);                        // last
-  b += 64 * 4;                                 // bm (50 used)
+  b += NPS_ALLOC * sizeof(R);                  // last
+  b += 64 * 4;                                 // bm (53 used)
   b += size_t(sipm_tcap(cap)) * (2 * sizeof(R) + 8 + 2);   // traps
   b += 64 * 2 + 64 * 2 + 256 * 2 + 16;         // frontier, candidates, misc
   return (b + 15) & ~size_t(15);
@@ -357,7 +357,7 @@ template <typename R>
 __device__ SipmShared<R> carve(char* base, int cap) {
   SipmShared<R> S;
   char* q = base;
-  S.last = reinterpret_cast<R*>(q); q += NPX * sizeof(R);
+  S.last = reinterpret_cast<R*>(q); q += NPS_ALLOC * sizeof(R);
   S.ph_t = reinterpret_cast<R*>(q); q += size_t(cap) * sizeof(R);
   const int tcap = sipm_tcap(cap);
   S.tcap = tcap;
@@ -378,8 +378,12 @@ __device__ SipmShared<R> carve(char* base, int cap) {
 __device__ __forceinline__ bool bm_test(const uint32_t* bm, int p) { return (bm[p >> 5] >> (p & 31)) & 1u; }
 __device__ __forceinline__ void bm_set(uint32_t* bm, int p) { atomicOr(&bm[p >> 5], 1u << (p & 31)); }
 
+// Photon-map bin by the CDF (GetRandom2), then the pixel id of the point: "truncate" keeps the bin, "lrint" rounds
+// the point, i.e. moves to the next pixel in x and in y each with probability 1/2 (crv/crvfastsim/response/sipm.py:
+// 80-91).  The two halves are bits 0 and 1 of the draw word whose low bits the bin uniform does not use.
 template <typename R>
-__device__ __forceinline__ int draw_pixel(const CrvParams& p, const CrvPixels& px, const uint32_t* dead, R u) {
+__device__ __forceinline__ int draw_pixel(const CrvParams& p, const CrvPixels& px, const uint32_t* dead, R u,
+                                          uint32_t half) {
   int b;
   if (p.uniform_map) {
     b = int(floor(u * R(NPX)));
@@ -394,7 +398,10 @@ __device__ __forceinline__ int draw_pixel(const CrvParams& p, const CrvPixels& p
   }
   if (b > NPX - 1) b = NPX - 1;
   if (b < 0) b = 0;
-  return ((dead[b >> 5] >> (b & 31)) & 1u) ? -1 : b;
+  int x = b / 40, y = b - 40 * (b / 40);
+  if (p.pixel_lrint) { x += int(half & 1u); y += int((half >> 1) & 1u); }
+  const int q = x * PXS + y;
+  return ((dead[q >> 5] >> (q & 31)) & 1u) ? -1 : q;
 }
 
 // SiPM constants in the compute type, converted once per block (held in shared memory: in the FP32 kernels a
@@ -486,7 +493,7 @@ __device__ __forceinline__ unsigned node_crosstalk(const CrvParams& p, const Sip
   if (!K.ct_on) return 0;
   U4 a = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 2, C.chan), key);
   U4 b = keyed(p.seed, C.ek, w2_of(ST_SIPM, gen, idx, 3, C.chan), key);
-  int x = pix / 40, y = pix % 40;
+  int x = pix / PXS, y = pix - PXS * (pix / PXS);
   const R q = K.q_ct;
   unsigned m = 0;
   if (x > 0 && M::uni(a, 0) < q) m |= 1u;
@@ -497,7 +504,7 @@ __device__ __forceinline__ unsigned node_crosstalk(const CrvParams& p, const Sip
 }
 
 __device__ __forceinline__ int neighbour(int pix, int q) {
-  return q == 0 ? pix - 40 : (q == 1 ? pix + 40 : (q == 2 ? pix - 1 : pix + 1));
+  return q == 0 ? pix - PXS : (q == 1 ? pix + PXS : (q == 2 ? pix - 1 : pix + 1));
 }
 
 // Append a charge record (lane-ordered position pos relative to C.nq) if it fits.
@@ -639,7 +646,7 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
     U4 w0{0, 0, 0, 0};
     if (has) {
       w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), key);
-      pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0));
+      pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0), w0.y);
     }
     bool live = pix >= 0;
     unsigned same = __match_any_sync(FULL, live ? pix : -1 - lane_id());
@@ -793,7 +800,7 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
   extern __shared__ __align__(16) char smem[];
   __shared__ uint32_t dead[64];
   __shared__ SipmK<R> K;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) dead[i] = i < 50 ? px.dead_bits[i] : 0u;
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) dead[i] = i < DEAD_WORDS ? px.dead_bits[i] : 0u;
   if (threadIdx.x == 0) K = sipm_consts<R>(p);
   __syncthreads();
   SipmShared<R> S = carve<R>(smem + size_t(warp_in_block()) * sipm_smem_per_warp<R>(cap), cap);
@@ -847,7 +854,7 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
     simulate_sipm<R>(p, K, px, S, dead, C, O, n, G.photon_id, a, idb);
     int nap = run_afterpulses<R>(K, S, C, O);
     int fired = 0;
-    for (int w = lane_id(); w < 50; w += 32) fired += __popc(S.bm[w]);
+    for (int w = lane_id(); w < DEAD_WORDS; w += 32) fired += __popc(S.bm[w]);
     fired = warp_sum(fired);
     if (lane_id() == 0) {
       O.nmain[g] = C.nq;

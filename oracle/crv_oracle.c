@@ -9,7 +9,8 @@
  *     at zero  (crv/crvfastsim/response/photons.py:102-112, _draw_counts/_per_substep with one substep);
  *   - per-SiPM mirroring of the readout end (photons.py:333-356): SiPMs 0 and 2 read the -length end, 1 and 3 the
  *     +length end; the lookup-table probabilities are replaced by the analytic yield x two-exponential attenuation;
- *   - SiPM pixel draw from the photon-map CDF (crv/crvfastsim/response/sipm.py:80-91, "truncate" pixel ids);
+ *   - SiPM pixel draw from the photon-map CDF (crv/crvfastsim/response/sipm.py:80-91; "truncate" or "lrint" pixel
+ *     ids over the 41 x 41 pixel state);
  *   - the serial SiPM model (sipm.py:141-198): per SiPM, photons in time order; a pixel fires with
  *     p1 (1 - exp(-v/p2)), v = Vov (1 - exp(-(t - t_last)/tau)); cross-talk breadth-first to the 4 neighbours with
  *     multiplicity merging 1 - (1 - p)^m; trap afterpulses scheduled per firing and processed after all photons in
@@ -258,6 +259,7 @@ typedef struct {
     double trap0_lifetime, trap1_lifetime;
     double t_end;
     int32_t n_pixels_x, n_pixels_y;
+    int32_t pixel_lrint, pad1;            /* pixel id: 0 "truncate", 1 "lrint" */
 } OrcParams;
 
 static inline double p_fire(const OrcParams *P, double v) { return P->p1 * (1.0 - orc_exp(-v / P->p2)); }
@@ -333,7 +335,9 @@ void orc_photon_emit(const OrcParams *P, int64_t nrows, const int64_t *row_step,
 /* ------------------------------------------------------------------------------------------------------------ */
 /* SiPM stage                                                                                                     */
 
-#define NPX 1600
+#define NPX 1600                          /* photon-map bins, x * 40 + y */
+#define PXS 41                            /* pixel ids x * 41 + y over the 41 x 41 state (sipm.py:22 NPIX = 41) */
+#define NPS (PXS * PXS)
 #define MAX_GEN 15
 #define MAX_IDX 63
 
@@ -383,8 +387,11 @@ static void push_charge(ChargeBuf *C, double t, double v, int64_t photon) {
     C->n++;
 }
 
-/* Pixel of a photon from the photon-map CDF (cum: 1600 running sums over bins x * 40 + y); returns -1 for dead. */
-static inline int draw_pixel(const double *cum, const uint8_t *dead, double u) {
+/* Pixel of a photon (crv/crvfastsim/response/sipm.py:80-91): the photon-map bin by the CDF (cum: 1600 running sums
+ * over bins x * 40 + y), then its pixel id x * 41 + y: "truncate" keeps the bin, "lrint" rounds the point in it, i.e.
+ * adds 1 to x and to y each with probability 1/2 (bits 0 and 1 of `half`, the draw word whose low 11 bits the bin
+ * uniform drops).  Returns -1 for a dead pixel. */
+static inline int draw_pixel(const double *cum, const uint8_t *dead, double u, int lrint, uint32_t half) {
     double v = u * cum[NPX - 1];
     int lo = 0, hi = NPX;                        /* first index with cum > v (searchsorted side="right") */
     while (lo < hi) {
@@ -392,14 +399,17 @@ static inline int draw_pixel(const double *cum, const uint8_t *dead, double u) {
         if (cum[mid] <= v) lo = mid + 1; else hi = mid;
     }
     if (lo >= NPX) lo = NPX - 1;
-    return dead[lo] ? -1 : lo;
+    int x = lo / 40, y = lo % 40;
+    if (lrint) { x += (int)(half & 1u); y += (int)((half >> 1) & 1u); }
+    int q = x * PXS + y;
+    return dead[q] ? -1 : q;
 }
 
 /* Simulate one SiPM.  photons sorted by (t, key) already, t <= t_end.  Returns status (0 ok, 2 limit). */
 static int sipm_one(const OrcParams *P, const double *cum, const uint8_t *dead, uint32_t run, uint32_t ev,
                     uint32_t sub, int chan, const Ph *ph, int64_t n, ChargeBuf *out, int64_t *n_fired_pix) {
-    double last[NPX];
-    for (int i = 0; i < NPX; ++i) last[i] = -INFINITY;
+    double last[NPS];
+    for (int i = 0; i < NPS; ++i) last[i] = -INFINITY;
     Trap *traps = NULL;
     int64_t ntr = 0, captr = 0;
     int status = 0;
@@ -408,7 +418,7 @@ static int sipm_one(const OrcParams *P, const double *cum, const uint8_t *dead, 
         uint32_t w3 = (uint32_t)ph[k].key;
         uint32_t w[4];
         keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, 0, 0, 0, chan), w3, w);
-        int pix = draw_pixel(cum, dead, u01(w[0], w[1]));
+        int pix = draw_pixel(cum, dead, u01(w[0], w[1]), P->pixel_lrint, w[1]);
         if (pix < 0) continue;
         double t = ph[k].t;
         Node fr[MAX_IDX + 1], nx[4 * (MAX_IDX + 1)];
@@ -470,12 +480,12 @@ static int sipm_one(const OrcParams *P, const double *cum, const uint8_t *dead, 
             int nn = 0;
             for (int a = 0; a < nf; ++a) {
                 int i = fired[a];
-                int p = fr[i].pix, x = p / 40, y = p % 40;
+                int p = fr[i].pix, x = p / PXS, y = p % PXS;
                 uint32_t c2[4], c3[4];
                 keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 2, chan), w3, c2);
                 keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, gen, i, 3, chan), w3, c3);
                 double u[4] = {u01(c2[0], c2[1]), u01(c2[2], c2[3]), u01(c3[0], c3[1]), u01(c3[2], c3[3])};
-                int nxp[4] = {(x - 1) * 40 + y, (x + 1) * 40 + y, x * 40 + y - 1, x * 40 + y + 1};
+                int nxp[4] = {(x - 1) * PXS + y, (x + 1) * PXS + y, x * PXS + y - 1, x * PXS + y + 1};
                 int ok[4] = {x > 0, x + 1 < NX, y > 0, y + 1 < NY};
                 for (int q = 0; q < 4; ++q)
                     if (ok[q] && u[q] < P->q_ct) { nx[nn].pix = nxp[q]; nn++; }
@@ -514,7 +524,7 @@ static int sipm_one(const OrcParams *P, const double *cum, const uint8_t *dead, 
     }
     free(traps);
     int64_t nfp = 0;
-    for (int i = 0; i < NPX; ++i) nfp += (last[i] > -INFINITY);
+    for (int i = 0; i < NPS; ++i) nfp += (last[i] > -INFINITY);
     if (n_fired_pix) *n_fired_pix = nfp;
     return status;
 }
@@ -536,6 +546,17 @@ static void stable_time_sort(ChargeBuf *C, int64_t a0) {
     memcpy(C->v + a0, v, n * sizeof(double));
     memcpy(C->photon + a0, ph, n * sizeof(int64_t));
     free(k); free(t); free(v); free(ph);
+}
+
+/* Test hook: the pixel ids (x * 41 + y, -1 for a dead pixel) drawn for photons with the given draw keys on one SiPM
+ * (channel chan of event (run, subrun, event)), as the SiPM stage draws them. */
+void orc_sipm_pixels(const OrcParams *P, const double *cum, const uint8_t *dead, uint32_t run, uint32_t ev,
+                     uint32_t sub, int chan, const int64_t *key, int64_t n, int32_t *out) {
+    for (int64_t k = 0; k < n; ++k) {
+        uint32_t w[4];
+        keyed(P->seed, run, ev, sub, w2_of(ST_SIPM, 0, 0, 0, chan), (uint32_t)key[k], w);
+        out[k] = draw_pixel(cum, dead, u01(w[0], w[1]), P->pixel_lrint, w[1]);
+    }
 }
 
 /* SiPM stage over photons grouped by SiPM: groups [gstart[g], gstart[g] + gcount[g]) of the photon arrays, each

@@ -32,7 +32,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 CHAN_MULT = 32768
-NPX = 1600
+NPX = 1600                      # photon-map bins (x * 40 + y)
+NPS = 41 * 41                   # SiPM pixel ids x * 41 + y (sipm.py:22 NPIX = 41)
 
 
 def build(force=False):
@@ -91,7 +92,8 @@ class OrcParams(ctypes.Structure):
                 ("capacitance", ctypes.c_double), ("p1", ctypes.c_double), ("p2", ctypes.c_double),
                 ("q_ct", ctypes.c_double), ("q_t0", ctypes.c_double), ("q_t1", ctypes.c_double),
                 ("trap0_lifetime", ctypes.c_double), ("trap1_lifetime", ctypes.c_double), ("t_end", ctypes.c_double),
-                ("n_pixels_x", ctypes.c_int32), ("n_pixels_y", ctypes.c_int32)]
+                ("n_pixels_x", ctypes.c_int32), ("n_pixels_y", ctypes.c_int32),
+                ("pixel_lrint", ctypes.c_int32), ("pad1", ctypes.c_int32)]
 
 
 def p_fire(sc, v):
@@ -119,6 +121,7 @@ def params(rc, sc, seed, t_end):
     P.trap0_lifetime, P.trap1_lifetime = sc.trap0_lifetime, sc.trap1_lifetime
     P.t_end = float(t_end)
     P.n_pixels_x, P.n_pixels_y = sc.n_pixels_x, sc.n_pixels_y
+    P.pixel_lrint = 1 if getattr(sc, "pixel_id", "truncate") == "lrint" else 0
     return P
 
 
@@ -129,10 +132,10 @@ def photon_map_cdf(pmap=None):
 
 
 def dead_table(sc):
-    d = np.zeros(NPX, np.uint8)
+    """Dead pixels over the pixel ids x * 41 + y of the 41 x 41 state (sipm.py:125-127, NPIX = 41 at sipm.py:22)."""
+    d = np.zeros(NPS, np.uint8)
     for x, y in sc.inactive:
-        if 0 <= x < 40 and 0 <= y < 40:
-            d[x * 40 + y] = 1
+        d[x * 41 + y] = 1
     return d
 
 
@@ -233,6 +236,18 @@ def make_photons(steps, geom, rc, deviation, seed):
                           k(half, np.float64), k(ev, np.uint32), k(sub, np.uint32), k(run, np.uint32),
                           k(sie, np.int32), *[k(x) for x in o])
     return o[0], o[1], o[2], o[3]
+
+
+def sipm_pixels(keys, sc, seed, pmap=None, chan=0, event=1, subrun=0, run=0):
+    """Pixel ids (x * 41 + y; -1 dead) that the SiPM stage draws for photons with these draw keys on one SiPM."""
+    P = params(_NullResponse, sc, seed, 0.0)
+    keys = np.ascontiguousarray(np.asarray(keys, np.int64))
+    out = np.empty(len(keys), np.int32)
+    k = _Keep()
+    lib().orc_sipm_pixels(ctypes.byref(P), k(np.ascontiguousarray(photon_map_cdf(pmap))), k(dead_table(sc)),
+                          ctypes.c_uint32(run), ctypes.c_uint32(event), ctypes.c_uint32(subrun), ctypes.c_int(chan),
+                          k(keys, np.int64), ctypes.c_int64(len(keys)), out.ctypes.data_as(ctypes.c_void_p))
+    return out
 
 
 def sipm_groups(label, time, photon, key, run_of_label, sc, seed, t_end, pmap=None):

@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
-(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, lookup, lookup_chain, attach, pulsetests;
+(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_chain, attach, pulsetests;
 default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
@@ -18,6 +18,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   coinc.npz      find_event clusters on three geometries, scalar and vectorised combination checks
                  (crv/crvfastsim/reco/coinc.py:289-392, coinc_cpu.py:11-51)
   stats.npz      statistics of the reference SiPM stage (sipm.py:102-198) and photon-count rule (photons.py:102-112)
+  pixelid.npz    SiPM pixel ids by rule (sipm.py:80-91): pixel histograms of "truncate" and "lrint", PE per SiPM on
+                 crowded SiPMs, and charge statistics with cross-talk and afterpulses under "lrint"
   lookup.npz     a synthetic lookup table and (step, SiPM) rows with the statistics of the reference substep kernel
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram; for the first 120 rows, the table bins the reference reads (its probability
@@ -452,6 +454,37 @@ def make_stats():
     np.savez_compressed(HERE / "stats.npz", **out)
 
 
+def make_pixelid():
+    """SiPM pixel ids (sipm.py:80-91): the reference's pixel histograms over the 41 x 41 ids for both rules on a map with
+    content in bins 6-33 and in the last bin (39, 39) (lrint reaches pixel 40 only from there); PE per SiPM on crowded
+    SiPMs (saturation differs between the rules, no cross-talk); and charge statistics with cross-talk and afterpulses
+    under lrint."""
+    rng = np.random.default_rng(41)
+    pmap = np.zeros((40, 40))
+    pmap[6:34, 6:34] = rng.uniform(0.0, 1.0, (28, 28))
+    pmap[39, 39] = 20.0
+    out = {"pmap": pmap}
+    for pid in SI.PIXEL_IDS:
+        x, y = SI.draw_pixels(pmap, 400_000, np.random.default_rng(42), pid)
+        out[f"hist_{pid}"] = np.bincount(x * 41 + y, minlength=41 * 41)
+        cfg = replace(SI.SiPMConfig(pixel_id=pid), cross_talk=0.0, trap0_prob=0.0)
+        chan = np.repeat(np.arange(400), 400)
+        r = SI.simulate(chan, np.zeros(len(chan)), np.arange(len(chan)), pmap, cfg, np.random.default_rng(43))
+        out[f"crowded_pe_{pid}"] = np.array([r["pe"].sum() / 400])
+    cfg = replace(SI.SiPMConfig(pixel_id="lrint"), cross_talk=0.05, trap0_prob=0.02)
+    S = 4000
+    trng = np.random.default_rng(45)                                     # photon counts and times: from the seed
+    n = trng.poisson(80, S)
+    chan = np.repeat(np.arange(S), n)
+    t = np.repeat(trng.uniform(0, 1500, S), n) + trng.exponential(7.4, len(chan))
+    r = SI.simulate(chan, t, np.arange(len(chan)), pmap, cfg, np.random.default_rng(44), t_end=1606.4)
+    out["lrint_seed"], out["lrint_S"] = np.array([45]), np.array([S])
+    out["lrint_charges"] = np.array([len(r["pe"])])
+    out["lrint_pe_sum"] = np.array([r["pe"].sum()])
+    out["lrint_frac_low"] = np.array([(r["pe"] < 0.99).mean()])
+    np.savez_compressed(HERE / "pixelid.npz", **out)
+
+
 def synthetic_lookup(rng, decay_time=7.4):
     """A small lookup table with the reference's layout (lookup.py:70-98): bin edges, arrival probabilities, delay and
     emission weights; geometry of a 2 cm x 5 cm counter with two fibre holes."""
@@ -758,7 +791,7 @@ def make_attach():
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
-                     ("coinc", make_coinc), ("stats", make_stats), ("lookup", make_lookup),
+                     ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup),
                      ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()

@@ -20,6 +20,15 @@ def test_unsupported_pixel_layouts_are_refused(kw):
         validate_sipm(C.SiPMConfig(**kw))
 
 
+@pytest.mark.parametrize("pid, flag", [("truncate", 0), ("lrint", 1)])
+def test_both_reference_pixel_id_rules_are_accepted(pid, flag):
+    """crv/crvfastsim/response/sipm.py:23 PIXEL_IDS; the rule reaches the kernels as CrvParams.pixel_lrint."""
+    sc = C.SiPMConfig(pixel_id=pid)
+    validate_sipm(sc)
+    assert make_params(C.ChainConfig(sipm=sc), 1).pixel_lrint == flag
+    assert set(C.PIXEL_IDS) == {"lrint", "truncate"}
+
+
 @pytest.mark.parametrize("w", [(10.0, 5.0), (0.0, float("inf")), (0.0,), (float("nan"), 1.0)])
 def test_bad_windows_are_refused(w):
     with pytest.raises(ValueError):

@@ -79,3 +79,49 @@ def test_large_photon_counts_take_the_second_pass(R):
     assert counts.max() > 512
     for k in ("chan", "time", "charge", "pe", "photon"):
         assert np.array_equal(Q[k], Qo[k]), k
+
+
+def _lrint_photons(S=600, seed=12):
+    """Photons on S SiPMs (Poisson 60 each, spread over 1.5 us) with draw keys = index within the SiPM."""
+    rng = np.random.default_rng(seed)
+    n = rng.poisson(60, S)
+    label = np.repeat((1 << 20 | 3) * 32768 + np.arange(S, dtype=np.int64), n)
+    t = np.repeat(rng.uniform(0, 1500, S), n) + rng.exponential(7.4, len(label))
+    key = np.arange(len(label)) - np.repeat(np.cumsum(n) - n, n)
+    return label, t, np.arange(len(label)), key
+
+
+@pytest.mark.parametrize("edge", [False, True])
+def test_sipm_lrint_bit_exact_and_fired_pixels(R, golden, edge):
+    """pixel_id "lrint" on a photon map with content in bins 6-33 and (39, 39) (pixel 40 reached, cross-talk from
+    it), or with content only at (39, 39); cross-talk and afterpulses on: GPU == oracle, fired pixels included."""
+    from dataclasses import replace
+    from crvgpu.config import SiPMConfig
+    pmap = golden("pixelid.npz")["pmap"].copy()
+    if edge:
+        pmap[:] = 0.0
+        pmap[39, 39] = 1.0
+    sc = replace(SiPMConfig(pixel_id="lrint"), cross_talk=0.05, trap0_prob=0.02)
+    label, t, photon, key = _lrint_photons()
+    G = R.simulate(label, t, photon, pmap, sc, None, t_end=1606.4, key=21, draw_key=key)
+    Qo, u, nq, nfp, st = O.sipm_groups(label, t, photon, key, lambda L: np.zeros(len(L), np.int64), sc, 21, 1606.4,
+                                       pmap)
+    assert st == 0 and len(Qo["pe"]) > 5000
+    for k in ("chan", "time", "charge", "pe", "photon"):
+        assert np.array_equal(G[k], Qo[k]), k
+    assert np.array_equal(G["_group_fired"], nfp) and np.array_equal(G["_group_charges"], nq)
+
+
+def test_charges_lrint_bit_exact(R):
+    """The chain's charges under pixel_id "lrint" (uniform photon map): GPU == oracle."""
+    from dataclasses import replace
+    geom, cond, cfg, steps = workload(48, seed=5)
+    cfg.sipm = replace(cfg.sipm, pixel_id="lrint")
+    Q = R.charges(steps, None, geom, cond, cfg, None, key=4321)
+    Qo, diag = O.charges(steps, geom, cond, cfg.response, cfg.sipm, 4321, cfg.window[1])
+    assert diag["status"] == 0 and len(Q["time"]) > 1000
+    for k in ("chan", "time", "charge", "pe", "photon"):
+        assert np.array_equal(Q[k], Qo[k]), k
+    cfg.sipm = replace(cfg.sipm, pixel_id="truncate")
+    Qt = R.charges(steps, None, geom, cond, cfg, None, key=4321)
+    assert len(Qt["time"]) != len(Q["time"]) or not np.array_equal(Qt["pe"], Q["pe"])
