@@ -1,7 +1,8 @@
 /*
  * crvgpu: C ABI of the GB300 CRV response engine (CrvSteps -> SiPM charges -> digis -> reco pulses -> coincidence
  * clusters).  Plain pointers and sizes only; every array argument is a DEVICE pointer owned by the caller (the
- * Python host allocates it with PyTorch); `stream` is a cudaStream_t; no call synchronises the host.
+ * Python host allocates it with PyTorch), except in the lookup-table file reader (host memory, marked below);
+ * `stream` is a cudaStream_t; no call synchronises the host.
  *
  * Each entry point replaces one stage function of the reference's Python API (RobMina/mu2e-fastsim, CRV package):
  *
@@ -24,6 +25,7 @@
  *   crv_chain                        <- the chain above in one resident call with explicit capacities, as the
  *                                       mixing adapter's resident CRV chain (mixing/device_crv.py:127-573,
  *                                       mixing/DEVICE_CRV.md "Explicit capacities")
+ *   crv_lookup_file_info / _read     <- crvfastsim.response.lookup.load (host memory; crv/crvfastsim/response/lookup.py:149)
  *
  * Error convention: the return value is a host error code (CRV_OK, CRV_ERR_ARG for invalid arguments, CRV_ERR_CUDA
  * for a failed launch).  Data-dependent conditions are reported in the device status block (CrvStatus): capacity
@@ -482,6 +484,49 @@ int64_t crv_substeps_workspace(int64_t nrows);
 int crv_substep_photons(const CrvLookup *L, uint32_t seed, const CrvSubstepRows *rows, int64_t nrows,
                         int64_t *o_step, int64_t *o_chan, double *o_time, int64_t cap, int64_t *n_out_dev,
                         void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
+
+/* ---- Lookup-table files (HOST memory, no device work) ------------------------------------------------------------
+ * The Mu2e CRV photon lookup table, format version 6 (Offline CRVResponse MakeCrvPhotons), parsed from a file image:
+ * replaces the reference's reader crvfastsim.response.lookup.load / _read_bins (crv/crvfastsim/response/lookup.py:
+ * 108-179).  crv_lookup_file_info validates the whole image and fills the sizes; crv_lookup_file_read copies the
+ * content into caller-allocated host arrays sized from them.  A malformed image returns CRV_ERR_ARG with
+ * info->error set: */
+#define CRV_LUTF_VERSION 1     /* error_a.error_b = the file's version (6.x expected) */
+#define CRV_LUTF_BIN_NUMBER 2  /* bin number error_a found at position error_b */
+#define CRV_LUTF_TRAILING 3    /* error_a bytes after the last bin */
+#define CRV_LUTF_TRUNCATED 4   /* the image ends inside a record (at byte error_a) */
+#define CRV_LUTF_SIZE 5        /* an empty bin-edge vector (error_a = its index) or table sizes beyond the image */
+
+typedef struct CrvLookupFileInfo {
+    int32_t version_major, version_minor, reflector;
+    int32_t error;
+    int64_t error_a, error_b;
+    double constants[10];        /* half_thickness, half_width, half_length, fiber_separation, hole_radius_x,
+                                    hole_radius_y, fiber_radius, corner_radius, birks, fiber_decay_time */
+    int64_t n_ck[2];             /* Cerenkov map entries: scintillator, fibre */
+    int64_t n_edges[7];          /* bin edges: x, y, z, beta, theta, phi, r */
+    int64_t n_bins[3];           /* scint [x,y,z], ckscint [x,y,z,beta], ckfiber [beta,theta,phi,r,z] */
+    int64_t delay_width[3];      /* longest delay-weight vector of each table (at least 1) */
+    int64_t emis_width[3];       /* longest emission-weight vector of each table (at least 1) */
+} CrvLookupFileInfo;
+
+typedef struct CrvLookupFileTable {
+    float *prob;                 /* [n_bins] arrival probability */
+    uint8_t *delays;             /* [n_bins][delay_width] weights, zero-padded */
+    int32_t *delay_sum;          /* [n_bins] */
+    uint8_t *emis;               /* [n_bins][emis_width] weights, zero-padded */
+    int32_t *emis_sum;           /* [n_bins] */
+} CrvLookupFileTable;
+
+typedef struct CrvLookupFileOut {
+    double *ck[2];               /* [n_ck][2] (beta, photons per mm) */
+    double *edges[7];            /* [n_edges] */
+    CrvLookupFileTable tables[3];
+} CrvLookupFileOut;
+
+int crv_lookup_file_info(const uint8_t *image, int64_t size, CrvLookupFileInfo *info);
+int crv_lookup_file_read(const uint8_t *image, int64_t size, const CrvLookupFileInfo *info,
+                         const CrvLookupFileOut *out);
 
 #ifdef __cplusplus
 }

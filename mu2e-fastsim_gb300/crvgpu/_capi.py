@@ -142,6 +142,24 @@ class CrvSubstepRowsOut(ctypes.Structure):
     _fields_ = [(k, c_p) for k in LOOKUP_ROW_COLS]
 
 
+# lookup-table file reader (host memory)
+LUTF_VERSION, LUTF_BIN_NUMBER, LUTF_TRAILING, LUTF_TRUNCATED, LUTF_SIZE = 1, 2, 3, 4, 5
+
+
+class CrvLookupFileInfo(ctypes.Structure):
+    _fields_ = [("version_major", c_i32), ("version_minor", c_i32), ("reflector", c_i32), ("error", c_i32),
+                ("error_a", c_i64), ("error_b", c_i64), ("constants", c_f64 * 10), ("n_ck", c_i64 * 2),
+                ("n_edges", c_i64 * 7), ("n_bins", c_i64 * 3), ("delay_width", c_i64 * 3), ("emis_width", c_i64 * 3)]
+
+
+class CrvLookupFileTable(ctypes.Structure):
+    _fields_ = [(k, c_p) for k in ("prob", "delays", "delay_sum", "emis", "emis_sum")]
+
+
+class CrvLookupFileOut(ctypes.Structure):
+    _fields_ = [("ck", c_p * 2), ("edges", c_p * 7), ("tables", CrvLookupFileTable * 3)]
+
+
 CHAIN_CAPS = ("events", "steps", "photons", "charges", "slots", "digis", "pulses", "max_steps_per_event")
 CHAIN_COUNTS = ("charges", "digis", "waveforms", "pulses", "events", "hits", "clusters", "members", "photons",
                 "slots")
@@ -195,6 +213,8 @@ _SIGS = {
                                 c_p, c_i64, c_p, c_p]),
     "crv_substep_photons": (c_i32, [P(CrvLookup), c_u32, P(CrvSubstepRows), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p,
                                     c_i64, c_p, c_p]),
+    "crv_lookup_file_info": (c_i32, [c_p, c_i64, P(CrvLookupFileInfo)]),
+    "crv_lookup_file_read": (c_i32, [c_p, c_i64, P(CrvLookupFileInfo), P(CrvLookupFileOut)]),
     "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
                           P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters), P(CrvMembers),
                           c_p, c_p, c_i64, c_p, c_p]),

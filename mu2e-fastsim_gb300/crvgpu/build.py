@@ -25,6 +25,7 @@ UNITS = {
     "crv_kernels_f32.cu": [],
     "crv_static.cu": [],
     "crv_lookup.cu": ["-fmad=false"],
+    "crv_tables.cpp": [],                 # host code (lookup-table file reader)
 }
 
 
@@ -39,7 +40,7 @@ def sources():
     out = []
     for d in (CSRC, INCLUDE):
         for f in sorted(os.listdir(d)):
-            if f.endswith((".cu", ".cuh", ".h", ".inc")):
+            if f.endswith((".cu", ".cpp", ".cuh", ".h", ".inc")):
                 out.append(os.path.join(d, f))
     return out
 
@@ -63,7 +64,7 @@ def build(force=False, verbose=False, extra=None):
 
     def one(item):
         src, flags = item
-        obj = os.path.join(obj_dir, src.replace(".cu", ".o"))
+        obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
         cmd = common + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -1,8 +1,8 @@
 """Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
-(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_chain, attach, pulsetests;
-default all)
+(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
+pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -24,6 +24,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
                  (crv/crvfastsim/response/photons.py:163-224) over 16 generator seeds: mean photons per row, arrival
                  delay histogram; for the first 120 rows, the table bins the reference reads (its probability
                  lookups recorded in substep order); the delay / emission index search on random thresholds
+  lookup_file.npz  two version-6 lookup-table files (one from the reference's own test double, one with edge cases:
+                 reflector 1, minor version, a table without bins, empty and 255-long weight vectors) and the
+                 reference's decoded arrays of each (lookup.py:149-192)
   pulsetests.npz every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py:
                  injected-parameter recovery, below threshold, pedestal undershoot; at its stock 12.5 ns period), with
                  the reference's outputs
@@ -485,6 +488,53 @@ def make_pixelid():
     np.savez_compressed(HERE / "pixelid.npz", **out)
 
 
+def write_v6(rng, reflector=1, minor=2, theta_edges=1):
+    """A version-6 lookup-table image in the documented layout (crv/crvfastsim/response/lookup.py:3-11) with the edge
+    cases: reflector 1, a minor version, a table without bins (one theta edge), empty and 255-long weight vectors."""
+    import struct
+    edges = {"x": np.linspace(0, 8, 4), "y": np.linspace(-20, 20, 3), "z": np.linspace(-500, 500, 5),
+             "beta": np.linspace(0.5, 1, 3), "theta": np.linspace(0, np.pi, theta_edges), "phi": np.linspace(0, 1, 3),
+             "r": np.linspace(0, 0.7, 2)}
+    b = bytearray(struct.pack("<3i4x", 6, minor, reflector))
+    b += rng.uniform(0.1, 30.0, 10).astype("<f8").tobytes()
+    for n in (3, 0):
+        cm = np.c_[np.linspace(0.5, 1.0, n), rng.uniform(0, 200, n)]
+        b += struct.pack("<Q", n) + cm.astype("<f8").tobytes()
+    for k in ("x", "y", "z", "beta", "theta", "phi", "r"):
+        b += struct.pack("<Q", len(edges[k])) + edges[k].astype("<f8").tobytes()
+    nb = {k: len(v) - 1 for k, v in edges.items()}
+    ns = nb["x"] * nb["y"] * nb["z"]
+    for n in (ns, ns * nb["beta"], nb["beta"] * nb["theta"] * nb["phi"] * nb["r"] * nb["z"]):
+        for i in range(n):
+            nd = int(rng.choice([0, 1, 5, 30, 255]))
+            ne = int(rng.choice([0, 2, 7]))
+            d = rng.integers(0, 256, nd).astype(np.uint8)
+            e = rng.integers(0, 256, ne).astype(np.uint8)
+            b += struct.pack("<If", i, float(rng.uniform(0, 0.05)))
+            b += struct.pack("<Q", nd) + d.tobytes() + struct.pack("<Q", ne) + e.tobytes()
+    return bytes(b)
+
+
+def make_lookup_file():
+    """Version-6 lookup-table files decoded by the reference's load (lookup.py:149-179): one written by the
+    reference's own test double (crv/tests/test_lookup_library.py _write_table), one by write_v6 (edge cases)."""
+    import importlib.util
+    from crvfastsim.response import lookup as LK
+    spec = importlib.util.spec_from_file_location("ref_lookup_tests", REF / "tests" / "test_lookup_library.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        mod._write_table(d / "LookupTable_6000_0", np.random.default_rng(1))
+        (d / "LookupTable_2370_1").write_bytes(write_v6(np.random.default_rng(2)))
+        for tag, name in (("a", "6000_0"), ("b", "2370_1")):
+            out[f"{tag}_image"] = np.frombuffer((d / f"LookupTable_{name}").read_bytes(), np.uint8)
+            for k, v in LK.arrays(LK.load(name, str(d))).items():
+                out[f"{tag}_{k}"] = np.asarray(v)
+    np.savez_compressed(HERE / "lookup_file.npz", **out)
+
+
 def synthetic_lookup(rng, decay_time=7.4):
     """A small lookup table with the reference's layout (lookup.py:70-98): bin edges, arrival probabilities, delay and
     emission weights; geometry of a 2 cm x 5 cm counter with two fibre holes."""
@@ -791,7 +841,7 @@ def make_attach():
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
-                     ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup),
+                     ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
                      ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()

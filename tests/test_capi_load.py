@@ -83,3 +83,44 @@ def test_lookup_struct_layouts():
     assert ctypes.sizeof(_capi.CrvSubstepRows) == 15 * 8
     assert ctypes.sizeof(_capi.CrvLookupGroup) == 12 * 8 + 8 + 6 * 4
     assert ctypes.sizeof(_capi.CrvChainCaps) == 7 * 8 + 2 * 4
+
+
+def test_lookup_file_struct_layouts():
+    import ctypes
+    assert ctypes.sizeof(_capi.CrvLookupFileInfo) == 4 * 4 + 2 * 8 + 10 * 8 + 2 * 8 + 7 * 8 + 3 * 3 * 8
+    assert ctypes.sizeof(_capi.CrvLookupFileTable) == 5 * 8
+    assert ctypes.sizeof(_capi.CrvLookupFileOut) == 2 * 8 + 7 * 8 + 3 * 5 * 8
+
+
+def test_every_struct_matches_the_compiled_header():
+    """sizeof and offsetof of every field of every ctypes mirror against the header compiled by the C compiler."""
+    import ctypes
+    import shutil
+    import subprocess
+    import tempfile
+    import pytest
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {n: getattr(_capi, n) for n in dir(_capi)
+               if n.startswith("Crv") and isinstance(getattr(_capi, n), type)
+               and issubclass(getattr(_capi, n), ctypes.Structure)}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "crvgpu.h"', "int main(void) {"]
+    expect = []
+    for name, S in sorted(structs.items()):
+        lines.append(f'  printf("%zu\\n", sizeof({name}));')
+        expect.append((name, "sizeof", ctypes.sizeof(S)))
+        for f, _ in S._fields_:
+            c_name = f[:-1] if f.endswith("_") else f                  # ctypes spelling of a Python keyword
+            lines.append(f'  printf("%zu\\n", offsetof({name}, {c_name}));')
+            expect.append((name, f, getattr(S, f).offset))
+    lines += ["  return 0;", "}"]
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "layout.c"), os.path.join(d, "layout")
+        open(src, "w").write("\n".join(lines))
+        subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        got = [int(v) for v in subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()]
+    assert len(got) == len(expect)
+    bad = [(e, g) for e, g in zip(expect, got) if e[2] != g]
+    assert not bad, bad[:10]
+    assert len(structs) >= 15
