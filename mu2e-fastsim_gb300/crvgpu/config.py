@@ -27,7 +27,9 @@ import numpy as np
 
 CHAN_MULT = 32768          # SiPM label = event key * CHAN_MULT + channel (crv/crvfastsim/chain.py:25)
 PERIOD = 12.55             # digitisation period [ns] of the workload (the reference module constant is 12.5)
-NPIX = 1600                # 40 x 40 pixel grid; the inactive 4 x 4 centre leaves 1,584 live pixels
+NPIX = 41                  # pixels per side of the SiPM pixel state (crv/crvfastsim/response/sipm.py:22): ids
+                           # x * 41 + y; the 40 x 40 grid minus the inactive 4 x 4 centre leaves 1,584 live pixels,
+                           # the 41st row and column are reached by the "lrint" rule only
 SPE_PEAK_VOLT = 0.0055     # single-PE peak voltage of the Gumbel template [V]
 
 

@@ -18,7 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _capi
-from .config import CHAN_MULT, NPIX, ChainConfig
+from .config import CHAN_MULT, ChainConfig
 from .params import make_params, validate_sipm, validate_window
 
 

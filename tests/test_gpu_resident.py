@@ -1,7 +1,6 @@
 """The resident chain (one crv_chain call per batch, replayed as a CUDA graph) gives the same clusters, bit for bit, as
 the per-stage ChainEngine on the same steps and seed; batches of other sizes replay the same graph; a batch that
 overflows a capacity is rejected with the sizes it needed, and with growth enabled it is re-run to the same result."""
-import numpy as np
 import pytest
 
 from tests.helpers import workload
