@@ -206,9 +206,10 @@ def _fields_of(cls, obj, **over):
 
 def from_reference(cfg, precision="fp64"):
     """ChainConfig of this engine from a reference ChainConfig (crv/crvfastsim/chain.py:62-84) or any object with its
-    field names: same-named fields of the chain, SiPM, waveform, reco and finder blocks are carried over; the reference's
-    lookup-table response block contributes its yield scales only (the photon model here is the analytic one); JAX
-    switches have no meaning here and are dropped."""
+    field names: same-named fields of the chain, SiPM (pixel-id rule included), waveform, reco and finder blocks are
+    carried over; the reference's lookup-table response block (sectors with table, reflector and yield) is kept as
+    `lookup` and selects the lookup-table photon model when tables are passed, its yield scales also set the analytic
+    model's; JAX switches have no meaning here and are dropped."""
     resp = getattr(cfg, "response", None)
     rc = ResponseConfig(**{k: getattr(resp, k) for k in ("photon_yield_scale", "photon_yield_variation_scale")
                            if hasattr(resp, k)})

@@ -58,3 +58,14 @@ def test_from_reference_carries_same_named_fields():
     assert c.waveform.noise == 1e-3 and c.waveform.samples_zs == 10 and c.waveform.period == 12.55
     assert c.pulse_reco.max_pulses == 4 and c.pulse_reco.min_beta == 4.0
     assert c.finder is None and c.response.photon_yield_scale == 1.2 and c.precision == "fp32"
+
+
+def test_from_reference_carries_the_pixel_id_rule():
+    """The reference's SiPMConfig defaults to "lrint" (crv/crvfastsim/response/sipm.py:42): carried over, accepted,
+    and passed to the kernels."""
+    ref = types.SimpleNamespace(sipm=types.SimpleNamespace(pixel_id="lrint", cross_talk=0.05), window=(0.0, 1e5))
+    c = from_reference(ref)
+    assert c.sipm.pixel_id == "lrint"
+    validate_sipm(c.sipm)
+    assert make_params(c, 3).pixel_lrint == 1
+    assert make_params(from_reference(types.SimpleNamespace(window=(0.0, 1e5))), 3).pixel_lrint == 0
