@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
-pulsetests; default all)
+chaintests, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -30,6 +30,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   pulsetests.npz every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py:
                  injected-parameter recovery, below threshold, pedestal undershoot; at its stock 12.5 ns period), with
                  the reference's outputs
+  chaintests.npz every chain.reco_waveforms and chain.tdc0_per_feb call of the reference's own chain-glue tests
+                 (crv/tests/test_chain.py), and both on a multi-event digi sample (chain.py:219-231, 273-286)
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -791,6 +793,69 @@ def make_pulsetests():
     np.savez_compressed(HERE / "pulsetests.npz", **out)
 
 
+def make_chaintests():
+    """The reference's chain-glue tests (crv/tests/test_chain.py: one TDC0 per (event, FEB), digi concatenation into
+    reco waveforms) run under pytest with chain.reco_waveforms and chain.tdc0_per_feb recorded; then both on a
+    multi-event sample (chain.py:219-231, 273-286)."""
+    import pytest
+    from crvfastsim import chain as CH
+    rec_w, rec_t = [], []
+    orig_w, orig_t = CH.reco_waveforms, CH.tdc0_per_feb
+
+    def rw(D, cond):
+        out = orig_w(D, cond)
+        rec_w.append(({k: np.asarray(v).copy() for k, v in D.items()}, cond, out))
+        return out
+
+    def rt(labels, cond, rng, width=CH.PERIOD, key="roc_feb"):
+        out = orig_t(labels, cond, rng, width, key)
+        rec_t.append((np.asarray(labels).copy(), cond, width, key, out))
+        return out
+
+    CH.reco_waveforms, CH.tdc0_per_feb = rw, rt
+    try:
+        # the channel-label test needs JAX (skipped); the other two run
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", str(REF / "tests" / "test_chain.py")])
+        rng = np.random.default_rng(61)
+        nch = 512
+        z = np.zeros(nch)
+        cond = CH.Conditions(rng.uniform(90, 110, nch), rng.uniform(300, 500, nch), rng.uniform(20, 40, nch),
+                             rng.uniform(-2, 2, nch), np.zeros(nch, np.int64), np.arange(nch) // 256,
+                             (np.arange(nch) % 256) // 64, z)
+        chan, st = [], []
+        for ev in (1, 2, 7, (3 << 20) | 4):
+            for c in rng.choice(nch, 40, replace=False):
+                t = int(rng.integers(0, 50))
+                for _ in range(int(rng.integers(1, 6))):
+                    chan.append(ev * CH.CHAN_MULT + c)
+                    st.append(t)
+                    t += 12 if rng.random() < 0.6 else int(rng.integers(13, 40))   # continuation or a gap
+        perm = rng.permutation(len(chan))
+        D = {"chan": np.array(chan, np.int64)[perm], "starttdc": np.array(st, np.int64)[perm],
+             "adc": rng.integers(80, 4000, (len(chan), 12))}
+        CH.reco_waveforms(D, cond)
+        for key in CH.FEB_PHASE_KEYS:
+            CH.tdc0_per_feb(np.unique(D["chan"]), cond, np.random.default_rng(62), CH.PERIOD, key)
+    finally:
+        CH.reco_waveforms, CH.tdc0_per_feb = orig_w, orig_t
+    assert rc == 0, f"the reference's chain tests failed here ({rc})"
+    out = {"nw": np.int64(len(rec_w)), "nt": np.int64(len(rec_t))}
+    cf = ("pedestal", "pulsearea", "pulseheight", "timeoffset", "roc", "feb")
+    for i, (D, cond, W) in enumerate(rec_w):
+        for k in ("chan", "starttdc", "adc"):
+            out[f"w{i}_{k}"] = D[k]
+        for k in cf:
+            out[f"w{i}_cond_{k}"] = np.asarray(getattr(cond, k))
+        for k, v in W.items():
+            out[f"w{i}_out_{k}"] = np.asarray(v)
+    for i, (labels, cond, width, key, t) in enumerate(rec_t):
+        out[f"t{i}_labels"], out[f"t{i}_out"] = labels, np.asarray(t)
+        out[f"t{i}_width"], out[f"t{i}_key"] = np.array([float(width)]), np.array(key)
+        for k in ("roc", "feb"):
+            out[f"t{i}_cond_{k}"] = np.asarray(getattr(cond, k))
+    np.savez_compressed(HERE / "chaintests.npz", **out)
+
+
 def make_attach():
     import json
     import pytest
@@ -842,7 +907,7 @@ if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("pulsetests", make_pulsetests)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

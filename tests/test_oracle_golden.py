@@ -175,3 +175,29 @@ def test_pulsefit_matches_the_references_own_tests(golden):
         assert set(keys) == set(r)
         for k in keys:
             assert_same(r[k], g[f"{tag}_out_{k}"], f"{tag}.{k}")
+
+
+def test_chain_glue_matches_the_references_own_tests(golden):
+    """crv/tests/test_chain.py replayed (make_golden.py chaintests): reco waveforms from digis are identical
+    (concatenation of continuing digis, (event, channel, start) order, calibration per channel); TDC0 is one draw per
+    (event, FEB) in both FEB-key modes: the keyed draws partition the labels exactly as the reference's draws do."""
+    g = golden("chaintests.npz")
+    for i in range(int(g["nw"])):
+        D = {k: g[f"w{i}_{k}"] for k in ("chan", "starttdc", "adc")}
+        cond = SimpleNamespace(**{k: g[f"w{i}_cond_{k}"] for k in ("pedestal", "pulsearea", "pulseheight",
+                                                                    "timeoffset", "roc", "feb")})
+        W = O.reco_waveforms(D, cond)
+        keys = [k[len(f"w{i}_out_"):] for k in g.files if k.startswith(f"w{i}_out_")]
+        assert set(W) == set(keys)
+        for k in keys:
+            assert_same(W[k], g[f"w{i}_out_{k}"], f"w{i}.{k}")
+    for i in range(int(g["nt"])):
+        labels, ref = g[f"t{i}_labels"], g[f"t{i}_out"]
+        cond = SimpleNamespace(roc=g[f"t{i}_cond_roc"], feb=g[f"t{i}_cond_feb"])
+        width, key = float(g[f"t{i}_width"][0]), str(g[f"t{i}_key"])
+        t = O.tdc0_of_labels(labels, cond, 9, width, key, lambda e: np.zeros(len(e), np.int64))
+        _, a = np.unique(t, return_inverse=True)
+        _, b = np.unique(ref, return_inverse=True)
+        pairs = set(zip(a.ravel().tolist(), b.ravel().tolist()))
+        assert len(pairs) == len(set(a.ravel().tolist())) == len(set(b.ravel().tolist())), (i, key)
+        assert np.all((t >= 0) & (t < width))
