@@ -6,7 +6,8 @@ include/crvgpu.h (libcrvgpu.so, loaded through ctypes).  There is no CPU fallbac
 Modules: chain (the reference's chain entry points and ChainEngine, stage by stage), resident (the whole chain in one
 call with explicit capacities, replayed as a CUDA graph), serve (continuous batching of design-point jobs), response /
 waveform / pulsefit / coinc (the stages), lookup (the lookup-table photon model), lookup_file (the native reader of the
-version-6 lookup-table files, host only), shard (event partition across ranks),
+version-6 lookup-table files, host only), readout (the mask of physically present SiPMs), shard (event partition
+across ranks),
 config / params / geometry (configuration, launch parameters, geometry and synthetic workloads).
 """
 from . import config  # noqa: F401

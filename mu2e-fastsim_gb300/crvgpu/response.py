@@ -17,7 +17,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import _capi
+from . import _capi, readout
 from .config import CHAN_MULT, ChainConfig
 from .params import make_params, validate_sipm, validate_window
 
@@ -221,14 +221,9 @@ class DeviceTables:
 
 
 def effective_status(cond):
-    """Status with bit 0 set for physically absent sensors (crv/crvfastsim/readout.py:168-182)."""
-    st = np.asarray(cond.status)
-    mask = getattr(cond, "readout_mask", None)
-    if mask is None:
-        return st
-    st = st.copy()
-    st[~np.asarray(mask, bool)] |= 1
-    return st
+    """Status with bit 0 set for physically absent sensors (crvgpu.readout.effective_status; the reference's
+    crv/crvfastsim/readout.py:58-72), as an array."""
+    return np.asarray(readout.effective_status(cond))
 
 
 class EngineError(RuntimeError):

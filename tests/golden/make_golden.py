@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
-chaintests, pulsetests; default all)
+chaintests, readout, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -32,6 +32,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
                  the reference's outputs
   chaintests.npz every chain.reco_waveforms and chain.tdc0_per_feb call of the reference's own chain-glue tests
                  (crv/tests/test_chain.py), and both on a multi-event digi sample (chain.py:219-231, 273-286)
+  readout_calls.json  every readout.sensor_mask / apply / effective_status call of the reference's own readout-mask
+                 tests (crv/tests/test_readout_mask.py; crv/crvfastsim/readout.py:9-72): tagged-JSON arguments and
+                 the output or the exception raised
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -856,6 +859,72 @@ def make_chaintests():
     np.savez_compressed(HERE / "chaintests.npz", **out)
 
 
+def encode(v):
+    """Tagged JSON of a recorded argument: arrays keep dtype and shape, objects their readout attributes (a property
+    that raises keeps its exception), mappings their items, NumPy scalars their type; decoded by tests/test_readout.py."""
+    if isinstance(v, np.ndarray):
+        return {"nd": v.dtype.str, "shape": list(v.shape), "data": v.ravel().tolist()}
+    if isinstance(v, np.bool_):
+        return {"npbool": bool(v)}
+    if isinstance(v, np.integer):
+        return {"npint": int(v)}
+    if isinstance(v, float) and v != v:
+        return {"nan": True}
+    if v is None or isinstance(v, (bool, int, float, str)):
+        return v
+    if isinstance(v, (list, tuple)):
+        return {"list" if isinstance(v, list) else "tuple": [encode(x) for x in v]}
+    if isinstance(v, dict):
+        return {"map": [[k, encode(x)] for k, x in v.items()]}
+    attrs = ("sector_names", "sector", "nbars", "status", "readout_mask", "pedestal", "pulsearea", "pulseheight",
+             "timeoffset", "roc", "feb", "deviation")
+    out = {}
+    for a in attrs:
+        try:
+            out[a] = encode(getattr(v, a))
+        except AttributeError:
+            continue
+        except Exception as e:                                       # noqa: BLE001 (a property that raises)
+            out[a] = {"raises": [type(e).__name__, str(e)]}
+    return {"obj": out}
+
+
+def make_readout():
+    """The reference's readout-mask tests (crv/tests/test_readout_mask.py) run under pytest with readout.sensor_mask,
+    readout.apply and readout.effective_status recorded (crv/crvfastsim/readout.py:9-72): arguments, and the output
+    or the exception type and message of every call."""
+    import json
+    import pytest
+    from crvfastsim import readout as RO
+    calls = []
+    orig = {n: getattr(RO, n) for n in ("sensor_mask", "apply", "effective_status")}
+
+    def recorder(name):
+        def f(*args):
+            enc = [encode(a) for a in args]
+            try:
+                out = orig[name](*args)
+            except Exception as e:                                   # noqa: BLE001 (recorded, then re-raised)
+                calls.append({"fn": name, "args": enc, "error": [type(e).__name__, str(e)]})
+                raise
+            calls.append({"fn": name, "args": enc,
+                          "out": encode(out if name != "apply" else out.readout_mask)})
+            return out
+        return f
+
+    for n in orig:
+        setattr(RO, n, recorder(n))
+    try:
+        # the CSV-loading and charge-boundary tests need pandas / JAX (absent here); the rest run
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "not csv_loading and not charge_boundary",
+                          str(REF / "tests" / "test_readout_mask.py")])
+    finally:
+        for n, f in orig.items():
+            setattr(RO, n, f)
+    assert rc == 0, f"the reference's readout tests failed here ({rc})"
+    (HERE / "readout_calls.json").write_text(json.dumps(calls, allow_nan=False, separators=(",", ":")))
+
+
 def make_attach():
     import json
     import pytest
@@ -907,7 +976,7 @@ if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("pulsetests", make_pulsetests)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):
