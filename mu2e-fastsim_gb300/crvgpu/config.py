@@ -45,6 +45,8 @@ class ResponseConfig:
     photon_yield_variation_scale: float = 1.0
 
 
+# TDC0 phase per (event, ROC, FEB) or per (event, FEB number) across ROCs (crv/crvfastsim/chain.py:216-231)
+FEB_PHASE_KEYS = ("roc_feb", "feb")
 PIXEL_IDS = ("lrint", "truncate")          # crv/crvfastsim/response/sipm.py:23
 
 
@@ -186,7 +188,7 @@ class ChainConfig:
     waveform: object = None
     pulse_reco: object = None
     feb_phase_width: Optional[float] = None    # None = one digitisation period
-    feb_phase_key: str = "roc_feb"
+    feb_phase_key: str = "roc_feb"            # FEB_PHASE_KEYS
     backend: str = "cuda"
     precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (FP64 LM solve and absolute times)
     # the reference's lookup-table response block (sectors {name: (table, reflector, yield_per_mev)}, yield scales,

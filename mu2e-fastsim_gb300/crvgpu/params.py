@@ -4,7 +4,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _capi
-from .config import (PERIOD, PIXEL_IDS, ChainConfig, FinderConfig, RecoConfig, ResponseConfig, SiPMConfig, WaveformConfig)
+from .config import (FEB_PHASE_KEYS, PERIOD, PIXEL_IDS, ChainConfig, FinderConfig, RecoConfig, ResponseConfig, SiPMConfig, WaveformConfig)
 
 
 def p_fire(sc, v):
@@ -20,6 +20,14 @@ def validate_sipm(sc):
         raise ValueError(f"CRV response: SiPM pixel_id must be one of {PIXEL_IDS}, got {sc.pixel_id!r}")
     if sc.n_pixels_x != 40 or sc.n_pixels_y != 40:
         raise ValueError("CRV response: the pixel grid is 40 x 40")
+
+
+def validate_feb_phase(width, key, period):
+    """The TDC0 phase settings (crv/crvfastsim/chain.py:223-226): width finite in [0, period], a known key."""
+    if not np.isfinite(width) or not 0 <= width <= period:
+        raise ValueError(f"FEB phase width must be finite and in [0, {period}] ns, got {width}")
+    if key not in FEB_PHASE_KEYS:
+        raise ValueError(f"FEB phase key must be one of {FEB_PHASE_KEYS}, got {key!r}")
 
 
 def validate_window(window):
@@ -73,6 +81,7 @@ def make_params(cfg: ChainConfig = None, seed: int = 0, *, response: ResponseCon
     P.adc_conversion = wc.adc_conversion
     P.window_lo, P.window_hi = float(win[0]), float(win[1])
     P.feb_phase_width = period if cfg.feb_phase_width is None else float(cfg.feb_phase_width)
+    validate_feb_phase(P.feb_phase_width, cfg.feb_phase_key, period)
     P.samples_zs, P.adc_pedestal, P.min_adc, P.max_adc = wc.samples_zs, wc.pedestal, wc.min_adc, wc.max_adc
     P.template_len = int(template_len)
     P.feb_key_mode = 1 if cfg.feb_phase_key == "feb" else 0

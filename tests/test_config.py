@@ -69,3 +69,15 @@ def test_from_reference_carries_the_pixel_id_rule():
     validate_sipm(c.sipm)
     assert make_params(c, 3).pixel_lrint == 1
     assert make_params(from_reference(types.SimpleNamespace(window=(0.0, 1e5))), 3).pixel_lrint == 0
+
+
+@pytest.mark.parametrize("kw, match", [(dict(feb_phase_key="roc"), "phase key"),
+                                       (dict(feb_phase_width=13.0), "phase width"),
+                                       (dict(feb_phase_width=-0.1), "phase width"),
+                                       (dict(feb_phase_width=float("nan")), "phase width")])
+def test_bad_feb_phase_settings_are_refused(kw, match):
+    """crv/crvfastsim/chain.py:223-226: an unknown phase key or a width outside [0, period] is a ValueError."""
+    with pytest.raises(ValueError, match=match):
+        make_params(C.ChainConfig(**kw), 1)
+    assert make_params(C.ChainConfig(feb_phase_key="feb", feb_phase_width=0.0), 1).feb_key_mode == 1
+    assert make_params(C.ChainConfig(), 1).feb_phase_width == C.WaveformConfig().period
