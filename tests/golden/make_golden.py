@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
-chaintests, readout, pulsetests; default all)
+chaintests, readout, wiring, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -35,6 +35,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   readout_calls.json  every readout.sensor_mask / apply / effective_status call of the reference's own readout-mask
                  tests (crv/tests/test_readout_mask.py; crv/crvfastsim/readout.py:9-72): tagged-JSON arguments and
                  the output or the exception raised
+  wiring.npz     every chain.clusters call of the reference's pulse-configuration wiring tests
+                 (crv/tests/test_chain_config_wiring.py, NumPy backend): waveforms, status and time offsets, the pulse
+                 configuration and the flat pulse table (chain.py:296-362; stock 12.5 ns)
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -925,6 +928,45 @@ def make_readout():
     (HERE / "readout_calls.json").write_text(json.dumps(calls, allow_nan=False, separators=(",", ":")))
 
 
+def make_wiring():
+    """The reference's pulse-configuration wiring tests (crv/tests/test_chain_config_wiring.py, NumPy backend: default,
+    custom and no-offset RecoConfig, 12- and 36-sample waveforms; stock 12.5 ns) run under pytest with chain.clusters
+    recorded: reco waveforms, conditions, the pulse configuration and the flat pulse table (chain.py:296-362)."""
+    import dataclasses
+    import json
+    import pytest
+    from crvfastsim import chain as CH
+    rec = []
+    orig = CH.clusters
+
+    def recorded(W, cond, geom, counters_cfg, cfg, *a, **k):
+        outs, timers = orig(W, cond, geom, counters_cfg, cfg, *a, **k)
+        rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else PF.RecoConfig()
+        rec.append(({kk: np.asarray(v).copy() for kk, v in W.items()}, cond, dataclasses.asdict(rcfg),
+                    {kk: np.asarray(v) for kk, v in outs[0]["pulses"].items()}))
+        return outs, timers
+
+    set_period(12.5)
+    CH.clusters = recorded
+    try:
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "pulse_config",
+                          str(REF / "tests" / "test_chain_config_wiring.py")])
+    finally:
+        CH.clusters = orig
+        set_period(PERIOD)
+    assert rc == 0, f"the reference's wiring tests failed here ({rc})"
+    out = {"n": np.int64(len(rec)), "period": np.array([12.5])}
+    for i, (W, cond, rcfg, P) in enumerate(rec):
+        for k, v in W.items():
+            out[f"r{i}_W_{k}"] = v
+        for k in ("status", "timeoffset"):
+            out[f"r{i}_cond_{k}"] = np.asarray(getattr(cond, k))
+        out[f"r{i}_reco"] = np.array(json.dumps(rcfg))
+        for k, v in P.items():
+            out[f"r{i}_P_{k}"] = v
+    np.savez_compressed(HERE / "wiring.npz", **out)
+
+
 def make_attach():
     import json
     import pytest
@@ -976,7 +1018,7 @@ if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("pulsetests", make_pulsetests)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

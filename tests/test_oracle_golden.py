@@ -201,3 +201,30 @@ def test_chain_glue_matches_the_references_own_tests(golden):
         pairs = set(zip(a.ravel().tolist(), b.ravel().tolist()))
         assert len(pairs) == len(set(a.ravel().tolist())) == len(set(b.ravel().tolist())), (i, key)
         assert np.all((t >= 0) & (t < width))
+
+
+def test_pulse_configuration_wiring_matches_the_references_own_tests(golden):
+    """crv/tests/test_chain_config_wiring.py replayed (make_golden.py wiring): with the default, a custom and a
+    no-offset RecoConfig, 12- and 36-sample waveforms, the oracle's pulses (reconstruct_full + filter_channels + DB
+    offsets x scale, chain.py:317-323) sorted as chain.clusters sorts them equal the reference's pulse table."""
+    import json
+    from dataclasses import fields
+    g = golden("wiring.npz")
+    period = float(g["period"][0])
+    ours = {f.name for f in fields(CF.RecoConfig)}
+    for i in range(int(g["n"])):
+        ref_cfg = json.loads(str(g[f"r{i}_reco"]))
+        assert set(ref_cfg) <= ours, set(ref_cfg) - ours
+        rcfg = CF.RecoConfig(**{**ref_cfg, "period": period})
+        W = {k[len(f"r{i}_W_"):]: g[k] for k in g.files if k.startswith(f"r{i}_W_")}
+        cond = SimpleNamespace(status=g[f"r{i}_cond_status"], timeoffset=g[f"r{i}_cond_timeoffset"])
+        if "toff" not in W:
+            W["toff"] = cond.timeoffset[W["bar"] * 4 + W["sipm"]]
+        P = O.pulses_from_waveforms(W, cond, rcfg, period)
+        o = np.lexsort((P["seq"], P["wf"], W["ev"][P["wf"]]))
+        wf = P["wf"][o]
+        got = dict(ev=W["ev"][wf], bar=W["bar"][wf], sipm=W["sipm"][wf], seq=P["seq"][o], pe=P["pe"][o],
+                   time=P["time"][o])
+        for k, v in got.items():
+            assert_same(v, g[f"r{i}_P_{k}"], f"r{i}.{k}")
+        assert len(wf) > 0
