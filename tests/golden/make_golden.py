@@ -35,9 +35,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   readout_calls.json  every readout.sensor_mask / apply / effective_status call of the reference's own readout-mask
                  tests (crv/tests/test_readout_mask.py; crv/crvfastsim/readout.py:9-72): tagged-JSON arguments and
                  the output or the exception raised
-  wiring.npz     every chain.clusters call of the reference's pulse-configuration wiring tests
-                 (crv/tests/test_chain_config_wiring.py, NumPy backend): waveforms, status and time offsets, the pulse
-                 configuration and the flat pulse table (chain.py:296-362; stock 12.5 ns)
+  wiring.npz     every chain.clusters call of the reference's pulse-configuration wiring and chain-contract tests
+                 (crv/tests/test_chain_config_wiring.py, test_chain_reco_contract.py; NumPy backend): waveforms,
+                 status and time offsets, the pulse configuration and the flat pulse table (chain.py:296-362; 12.5 ns)
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -930,8 +930,10 @@ def make_readout():
 
 def make_wiring():
     """The reference's pulse-configuration wiring tests (crv/tests/test_chain_config_wiring.py, NumPy backend: default,
-    custom and no-offset RecoConfig, 12- and 36-sample waveforms; stock 12.5 ns) run under pytest with chain.clusters
-    recorded: reco waveforms, conditions, the pulse configuration and the flat pulse table (chain.py:296-362)."""
+    custom and no-offset RecoConfig, 12- and 36-sample waveforms) and chain contracts (crv/tests/
+    test_chain_reco_contract.py: status masking before the finder, explicit offsets, more than eight pulses in a
+    waveform, no waveforms) run under pytest at the stock 12.5 ns with chain.clusters recorded: reco waveforms,
+    conditions, the pulse configuration and the flat pulse table (chain.py:296-362)."""
     import dataclasses
     import json
     import pytest
@@ -949,8 +951,11 @@ def make_wiring():
     set_period(12.5)
     CH.clusters = recorded
     try:
-        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "pulse_config",
-                          str(REF / "tests" / "test_chain_config_wiring.py")])
+        # NumPy-backend cases of both files (the JAX ones skip; the table-reco ones need the DQM tools, absent)
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k",
+                          "pulse_config or chain_conditions or cap_at_eight or empty_chain",
+                          str(REF / "tests" / "test_chain_config_wiring.py"),
+                          str(REF / "tests" / "test_chain_reco_contract.py")])
     finally:
         CH.clusters = orig
         set_period(PERIOD)
