@@ -155,14 +155,21 @@ def pin_steps(steps, nbars=None) -> PinnedSteps:
     return PinnedSteps(cols, ds.nsteps, ds.nevents, ds.max_steps)
 
 
+def check_photon_map(pm):
+    """The photon map's capability rule (crv/crvfastsim/response_config.py:288-290): finite, non-negative 40 x 40
+    weights with a positive, finite sum (the pixel draw samples bins by their running sums)."""
+    p = np.asarray(pm, float)
+    if p.shape != (40, 40) or not np.isfinite(p).all() or np.any(p < 0) or not np.isfinite(p.sum()) or p.sum() <= 0:
+        raise ValueError("photon_map: require finite nonnegative 40x40 weights with positive sum")
+
+
 class PixelTables:
     """Photon-map running sums and dead-pixel bitmap of a SiPM configuration on the device."""
 
     def __init__(self, sc, pmap=None, device="cuda"):
         torch = _torch()
         pm = np.ones((40, 40)) if pmap is None else np.asarray(pmap, float)
-        if pm.shape != (40, 40):
-            raise ValueError("photon map must be 40 x 40")
+        check_photon_map(pm)
         self.uniform_map = bool(np.all(pm == pm.flat[0]))
         self.cum = torch.from_numpy(np.cumsum(pm.ravel())).to(device)
         words = np.zeros(64, np.uint32)                  # pixel ids x * 41 + y over the 41 x 41 state (53 words used)

@@ -2,6 +2,7 @@
 refused before any work) and the reference-config converter.  CPU only."""
 import types
 
+import numpy as np
 import pytest
 
 from crvgpu import config as C
@@ -81,3 +82,16 @@ def test_bad_feb_phase_settings_are_refused(kw, match):
         make_params(C.ChainConfig(**kw), 1)
     assert make_params(C.ChainConfig(feb_phase_key="feb", feb_phase_width=0.0), 1).feb_key_mode == 1
     assert make_params(C.ChainConfig(), 1).feb_phase_width == C.WaveformConfig().period
+
+
+@pytest.mark.parametrize("weights", [np.zeros((40, 40)), np.ones((41, 41)), -np.ones((40, 40)),
+                                     np.full((40, 40), np.nan), np.full((40, 40), np.inf)])
+def test_photon_maps_outside_the_capability_are_refused(weights):
+    """crv/crvfastsim/response_config.py:288-290: finite, non-negative 40 x 40 weights with a positive sum."""
+    from crvgpu.response import check_photon_map
+    with pytest.raises(ValueError, match="photon_map"):
+        check_photon_map(weights)
+    check_photon_map(np.ones((40, 40)))
+    one = np.zeros((40, 40))
+    one[39, 39] = 1.0
+    check_photon_map(one)
