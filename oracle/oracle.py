@@ -1237,6 +1237,10 @@ def bar_ratios(values, geom):
     np.maximum.at(nmod, np.asarray(geom.sector), np.asarray(geom.module) + 1)
     sk = names[np.asarray(geom.sector)]
     mk = np.where(nmod[np.asarray(geom.sector)] > 1, sk + np.asarray(geom.module).astype(str).astype(object), sk)
+    known = set(sk) | set(mk) | {"TAG"}
+    bad = sorted(set(values) - known)
+    if bad:
+        raise KeyError(f"unknown propagation keys {bad}; known: {sorted(known)}")
     tag = np.array([str(n).startswith("M") for n in sk])
     for k, v in values.items():
         if k == "TAG":
@@ -1247,6 +1251,8 @@ def bar_ratios(values, geom):
     for k, v in values.items():
         if k in set(mk) and k not in set(sk):
             out[mk == k] = v
+    if not np.all(out > 0):
+        raise ValueError("propagation ratios must be positive")
     return out
 
 

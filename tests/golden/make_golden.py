@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
-chaintests, readout, wiring, pulsetests; default all)
+chaintests, readout, wiring, propagation, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -38,6 +38,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   wiring.npz     every chain.clusters call of the reference's pulse-configuration wiring and chain-contract tests
                  (crv/tests/test_chain_config_wiring.py, test_chain_reco_contract.py; NumPy backend): waveforms,
                  status and time offsets, the pulse configuration and the flat pulse table (chain.py:296-362; 12.5 ns)
+  propagation.npz  every photons.table_propagation and photons.bar_ratios call of the reference's propagation tests
+                 (crv/tests/test_propagation.py): the known-value table and its fit, geometries, ratio maps and the
+                 per-bar ratios or the KeyError raised (photons.py:229-289)
   attach.npz     every find_event call of the reference's own attachment boundary tests
                  (crv/tests/test_coinc_attachment_cpu.py: strict windows, ties, order, configuration flags), run under
                  pytest with find_event recorded: inputs, geometry, cuts, finder flags and the reference's clusters
@@ -972,6 +975,57 @@ def make_wiring():
     np.savez_compressed(HERE / "wiring.npz", **out)
 
 
+def make_propagation():
+    """The reference's light-propagation tests (crv/tests/test_propagation.py: the known-value table fit, bar keys and
+    ratios) run under pytest with photons.table_propagation and photons.bar_ratios recorded (photons.py:229-289): the
+    table's decoded arrays and the fitted (inverse speed, attenuation length); the geometry, the ratio map and the
+    per-bar ratios or the KeyError raised."""
+    import json
+    import pytest
+    from crvfastsim.response import lookup as LK
+    tp, br = [], []
+    o_tp, o_br = PH.table_propagation, PH.bar_ratios
+
+    def rec_tp(L):
+        out = o_tp(L)
+        tp.append((L.name, {k: np.asarray(v) for k, v in LK.arrays(L).items()}, out))
+        return out
+
+    def rec_br(values, geom):
+        G = {k: np.asarray(getattr(geom, k)) for k in ("sector", "module")}
+        G["nbars"], G["sector_names"] = np.int64(geom.nbars), np.array(list(geom.sector_names))
+        try:
+            out = o_br(values, geom)
+        except KeyError as e:
+            br.append((dict(values), G, None, str(e.args[0])))
+            raise
+        br.append((dict(values), G, np.asarray(out), None))
+        return out
+
+    PH.table_propagation, PH.bar_ratios = rec_tp, rec_br
+    try:
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "recovers_known_values or bar_keys_and_ratios",
+                          str(REF / "tests" / "test_propagation.py")])
+    finally:
+        PH.table_propagation, PH.bar_ratios = o_tp, o_br
+    assert rc == 0, f"the reference's propagation tests failed here ({rc})"
+    out = {"n_tp": np.int64(len(tp)), "n_br": np.int64(len(br))}
+    for i, (name, arrs, fit) in enumerate(tp):
+        out[f"tp{i}_name"] = np.array(name)
+        out[f"tp{i}_fit"] = np.array(fit)
+        for k, v in arrs.items():
+            out[f"tp{i}_{k}"] = v
+    for i, (values, G, ratios, err) in enumerate(br):
+        out[f"br{i}_values"] = np.array(json.dumps(values))
+        for k, v in G.items():
+            out[f"br{i}_G_{k}"] = v
+        if ratios is not None:
+            out[f"br{i}_out"] = ratios
+        else:
+            out[f"br{i}_error"] = np.array(err)
+    np.savez_compressed(HERE / "propagation.npz", **out)
+
+
 def make_attach():
     import json
     import pytest
@@ -1023,7 +1077,7 @@ if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("pulsetests", make_pulsetests)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("propagation", make_propagation), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

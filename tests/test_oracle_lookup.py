@@ -226,3 +226,33 @@ def test_delay_and_emission_search_match_the_reference():
     T = L.tables["scint"]
     assert np.array_equal(O.first_reaching(T.delays, z["ref_search_bins"], z["ref_search_dthr"]), z["ref_search_delay"])
     assert np.array_equal(O.first_reaching(T.emis, z["ref_search_bins"], z["ref_search_ethr"]), z["ref_search_emis"])
+
+
+def test_propagation_helpers_match_the_references_own_tests(golden):
+    """crv/tests/test_propagation.py replayed (make_golden.py propagation): the fit on its known-value table (speed
+    160 mm/ns, attenuation 6000 mm) and the per-bar ratios on its 11-sector geometry equal the reference's, in the
+    engine's host setup and in the oracle; an unknown module key raises the same KeyError."""
+    import json
+    from types import SimpleNamespace
+    from crvgpu import lookup as LK
+    from crvgpu import lookup_file as LF
+    g = golden("propagation.npz")
+    for i in range(int(g["n_tp"])):
+        a = lambda k: g[f"tp{i}_{k}"]                                            # noqa: E731
+        L = LF.LookupTable(str(a("name")), tuple(a("version")), int(a("reflector")), *a("constants"), a("ck_scint"),
+                           a("ck_fiber"), {k: a(f"edges_{k}") for k in LF.EDGES},
+                           {t: LF.Table(*(a(f"{t}_{f}") for f in ("prob", "delays", "delay_sum", "emis", "emis_sum")))
+                            for t in LF.TABLES})
+        for fit in (LK.table_propagation(L), O.table_propagation(L)):
+            assert np.array_equal(np.asarray(fit), a("fit")), (fit, a("fit"))
+    for i in range(int(g["n_br"])):
+        G = SimpleNamespace(sector=g[f"br{i}_G_sector"], module=g[f"br{i}_G_module"], nbars=int(g[f"br{i}_G_nbars"]),
+                            sector_names=[str(s) for s in g[f"br{i}_G_sector_names"]])
+        values = json.loads(str(g[f"br{i}_values"]))
+        for fn in (LK.bar_ratios, O.bar_ratios):
+            if f"br{i}_error" in g.files:
+                with pytest.raises(KeyError) as e:
+                    fn(values, G)
+                assert e.value.args[0] == str(g[f"br{i}_error"])
+            else:
+                assert np.array_equal(fn(values, G), g[f"br{i}_out"])
