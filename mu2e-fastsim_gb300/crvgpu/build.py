@@ -73,15 +73,19 @@ def build(force=False, verbose=False, extra=None):
             print(r.stderr, file=sys.stderr)
         return obj
 
-    with ThreadPoolExecutor(len(UNITS)) as ex:
-        objs = list(ex.map(one, UNITS.items()))
     tmp = LIB + f".{os.getpid()}.tmp"
-    r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"], capture_output=True,
-                       text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    shutil.rmtree(obj_dir, ignore_errors=True)
+    try:
+        with ThreadPoolExecutor(len(UNITS)) as ex:
+            objs = list(ex.map(one, UNITS.items()))
+        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+        os.replace(tmp, LIB)
+    finally:                                    # objects and a partial link never outlive the call
+        shutil.rmtree(obj_dir, ignore_errors=True)
+        if os.path.exists(tmp):
+            os.remove(tmp)
     return LIB
 
 
