@@ -1,8 +1,8 @@
 """Generate the golden fixtures of the CRV response chain by running the reference NumPy stages.
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
-(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_chain, attach,
-chaintests, readout, wiring, propagation, pulsetests; default all)
+(NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_fuzz, lookup_chain,
+attach, chaintests, readout, wiring, propagation, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -27,6 +27,9 @@ Fixtures (compressed .npz, a few hundred kB in total):
   lookup_file.npz  two version-6 lookup-table files (one from the reference's own test double, one with edge cases:
                  reflector 1, minor version, a table without bins, empty and 255-long weight vectors) and the
                  reference's decoded arrays of each (lookup.py:149-192)
+  lookup_fuzz.json  600 mutated images of the two lookup_file.npz files (byte flips, corrupted 8-byte fields,
+                 truncations, inserted / deleted bytes) as recipes, with the reference's verdict on each: the hash of its
+                 decoded arrays, or the exception its load raised
   pulsetests.npz every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py:
                  injected-parameter recovery, below threshold, pedestal undershoot; at its stock 12.5 ns period), with
                  the reference's outputs
@@ -544,6 +547,72 @@ def make_lookup_file():
             for k, v in LK.arrays(LK.load(name, str(d))).items():
                 out[f"{tag}_{k}"] = np.asarray(v)
     np.savez_compressed(HERE / "lookup_file.npz", **out)
+
+
+def mutate(image, recipe):
+    """Apply a mutation recipe to a file image: ("set", offset, bytes), ("cut", length), ("ins", offset, bytes),
+    ("del", offset, count).  tests/test_lookup_file.py applies the same recipes."""
+    b = bytearray(image)
+    for op in recipe:
+        if op[0] == "set":
+            b[op[1]:op[1] + len(op[2])] = bytes(op[2])
+        elif op[0] == "cut":
+            b = b[:op[1]]
+        elif op[0] == "ins":
+            b = b[:op[1]] + bytes(op[2]) + b[op[1]:]
+        else:
+            b = b[:op[1]] + b[op[1] + op[2]:]
+    return bytes(b)
+
+
+def decoded_hash(arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(arrays):
+        a = np.ascontiguousarray(arrays[k])
+        h.update(f"{k}|{a.dtype.str}|{a.shape}|".encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def make_lookup_fuzz():
+    """Mutated version-6 images (byte flips, corrupted 8-byte fields, truncations, inserted / deleted bytes) of the two
+    lookup_file.npz images, each decoded by the reference's load: the recipe, whether it loaded, and the hash of its
+    decoded arrays (lookup.py:149-192).  Requires lookup_file.npz."""
+    import json
+    import struct
+    from crvfastsim.response import lookup as LK
+    g = np.load(HERE / "lookup_file.npz")
+    rng = np.random.default_rng(6)
+    cases = []
+    with tempfile.TemporaryDirectory() as d:
+        for tag in ("a", "b"):
+            img = g[f"{tag}_image"].tobytes()
+            for it in range(300):
+                kind = it % 4
+                if kind == 0:
+                    rec = [("set", int(rng.integers(0, len(img))), [int(rng.integers(0, 256))])
+                           for _ in range(int(rng.integers(1, 8)))]
+                elif kind == 1:
+                    vals = [2 ** 63 - 1, 2 ** 64 - 1, 2 ** 40, 1 << 20, 255, 0]
+                    rec = [("set", int(rng.integers(0, len(img) - 8)),
+                            list(struct.pack("<Q", vals[int(rng.integers(0, 6))])))]
+                elif kind == 2:
+                    rec = [("cut", int(rng.integers(0, len(img))))]
+                elif rng.random() < 0.5:
+                    rec = [("ins", int(rng.integers(0, len(img))),
+                            [int(x) for x in rng.integers(0, 256, int(rng.integers(1, 5)))])]
+                else:
+                    rec = [("del", int(rng.integers(0, len(img))), int(rng.integers(1, 5)))]
+                p = os.path.join(d, "LookupTable_9_9")
+                with open(p, "wb") as f:
+                    f.write(mutate(img, rec))
+                try:
+                    verdict = decoded_hash(LK.arrays(LK.load("9_9", d)))
+                except Exception as e:                           # noqa: BLE001 (the reference's failure, recorded)
+                    verdict = "error:" + type(e).__name__
+                cases.append({"image": tag, "recipe": rec, "verdict": verdict})
+    (HERE / "lookup_fuzz.json").write_text(json.dumps(cases, separators=(",", ":")))
 
 
 def synthetic_lookup(rng, decay_time=7.4):
@@ -1076,7 +1145,7 @@ def make_attach():
 if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
-                     ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file),
+                     ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file), ("lookup_fuzz", make_lookup_fuzz),
                      ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("propagation", make_propagation), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()

@@ -89,3 +89,50 @@ def test_a_read_table_drives_the_propagation_fits_like_the_references(golden):
                        {t: LF.Table(*(ref[f"{t}_{f}"] for f in ("prob", "delays", "delay_sum", "emis", "emis_sum")))
                         for t in LF.TABLES})
     assert np.array_equal(np.asarray(table_propagation(L)), np.asarray(table_propagation(R)))
+
+
+def _mutate(image, recipe):
+    """The recipes of make_golden.py lookup_fuzz: set bytes, cut, insert, delete."""
+    b = bytearray(image)
+    for op in recipe:
+        if op[0] == "set":
+            b[op[1]:op[1] + len(op[2])] = bytes(op[2])
+        elif op[0] == "cut":
+            b = b[:op[1]]
+        elif op[0] == "ins":
+            b = b[:op[1]] + bytes(op[2]) + b[op[1]:]
+        else:
+            b = b[:op[1]] + b[op[1] + op[2]:]
+    return bytes(b)
+
+
+def _decoded_hash(arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(arrays):
+        a = np.ascontiguousarray(arrays[k])
+        h.update(f"{k}|{a.dtype.str}|{a.shape}|".encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def test_mutated_files_get_the_references_verdict(golden):
+    """600 mutated images (make_golden.py lookup_fuzz): where the reference's load decodes one, this reader decodes the
+    same arrays (same content hash); where it fails (ValueError, or OverflowError / IndexError / MemoryError from
+    absurd length fields), this reader raises ValueError.  No image crashes the native parser."""
+    import json
+    import os
+    g = golden("lookup_file.npz")
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lookup_fuzz.json")) as f:
+        cases = json.load(f)
+    assert len(cases) == 600
+    decoded = 0
+    for i, c in enumerate(cases):
+        image = _mutate(g[f"{c['image']}_image"].tobytes(), c["recipe"])
+        if c["verdict"].startswith("error:"):
+            with pytest.raises(ValueError):
+                LF.parse(image)
+        else:
+            assert _decoded_hash(LF.arrays(LF.parse(image))) == c["verdict"], i
+            decoded += 1
+    assert decoded >= 50
