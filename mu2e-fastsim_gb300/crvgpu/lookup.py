@@ -226,18 +226,25 @@ def table_propagation(L):
     return _PROPAGATION[key]
 
 
+def bar_keys(geom):
+    """Per bar: (sector key, module key), the module key being the sector name + module index when the sector has
+    several modules (photons.bar_keys, photons.py:257-264)."""
+    names = np.array(geom.sector_names, dtype=object)
+    sector, module = np.asarray(geom.sector), np.asarray(geom.module)
+    nmod = np.zeros(len(names), np.int64)
+    np.maximum.at(nmod, sector, module + 1)
+    sk = names[sector]
+    return sk, np.where(nmod[sector] > 1, sk + module.astype(str).astype(object), sk)
+
+
 def bar_ratios(values, geom):
-    """Per-bar propagation ratios from {key: ratio} (photons.bar_ratios, photons.py:257-289): key = sector name, "TAG"
+    """Per-bar propagation ratios from {key: ratio} (photons.bar_ratios, photons.py:267-289): key = sector name, "TAG"
     (every sector whose name starts with M) or sector name + module index for sectors with several modules; a module
     key wins over its sector, a sector over TAG; unlisted bars 1."""
     out = np.ones(geom.nbars)
     if not values:
         return out
-    names = np.array(geom.sector_names, dtype=object)
-    nmod = np.zeros(len(names), np.int64)
-    np.maximum.at(nmod, np.asarray(geom.sector), np.asarray(geom.module) + 1)
-    sk = names[np.asarray(geom.sector)]
-    mk = np.where(nmod[np.asarray(geom.sector)] > 1, sk + np.asarray(geom.module).astype(str).astype(object), sk)
+    sk, mk = bar_keys(geom)
     sset, mset = set(sk), set(mk)
     bad = sorted(set(values) - sset - mset - {"TAG"})
     if bad:

@@ -1046,14 +1046,21 @@ def make_wiring():
 
 def make_propagation():
     """The reference's light-propagation tests (crv/tests/test_propagation.py: the known-value table fit, bar keys and
-    ratios) run under pytest with photons.table_propagation and photons.bar_ratios recorded (photons.py:229-289): the
-    table's decoded arrays and the fitted (inverse speed, attenuation length); the geometry, the ratio map and the
-    per-bar ratios or the KeyError raised."""
+    ratios) run under pytest with photons.table_propagation, bar_keys and bar_ratios recorded (photons.py:229-289): the
+    table's decoded arrays and the fitted (inverse speed, attenuation length); the geometry and its per-bar sector and
+    module keys; the ratio map and the per-bar ratios or the KeyError raised."""
     import json
     import pytest
     from crvfastsim.response import lookup as LK
-    tp, br = [], []
-    o_tp, o_br = PH.table_propagation, PH.bar_ratios
+    tp, br, bk = [], [], []
+    o_tp, o_br, o_bk = PH.table_propagation, PH.bar_ratios, PH.bar_keys
+
+    def rec_bk(geom):
+        sk, mk = o_bk(geom)
+        G = {k: np.asarray(getattr(geom, k)) for k in ("sector", "module")}
+        G["nbars"], G["sector_names"] = np.int64(geom.nbars), np.array(list(geom.sector_names))
+        bk.append((G, np.asarray(sk).astype(str), np.asarray(mk).astype(str)))
+        return sk, mk
 
     def rec_tp(L):
         out = o_tp(L)
@@ -1071,14 +1078,18 @@ def make_propagation():
         br.append((dict(values), G, np.asarray(out), None))
         return out
 
-    PH.table_propagation, PH.bar_ratios = rec_tp, rec_br
+    PH.table_propagation, PH.bar_ratios, PH.bar_keys = rec_tp, rec_br, rec_bk
     try:
         rc = pytest.main(["-q", "-p", "no:cacheprovider", "-k", "recovers_known_values or bar_keys_and_ratios",
                           str(REF / "tests" / "test_propagation.py")])
     finally:
-        PH.table_propagation, PH.bar_ratios = o_tp, o_br
+        PH.table_propagation, PH.bar_ratios, PH.bar_keys = o_tp, o_br, o_bk
     assert rc == 0, f"the reference's propagation tests failed here ({rc})"
-    out = {"n_tp": np.int64(len(tp)), "n_br": np.int64(len(br))}
+    out = {"n_tp": np.int64(len(tp)), "n_br": np.int64(len(br)), "n_bk": np.int64(len(bk))}
+    for i, (G, sk, mk) in enumerate(bk):
+        for k, v in G.items():
+            out[f"bk{i}_G_{k}"] = v
+        out[f"bk{i}_sector_keys"], out[f"bk{i}_module_keys"] = sk, mk
     for i, (name, arrs, fit) in enumerate(tp):
         out[f"tp{i}_name"] = np.array(name)
         out[f"tp{i}_fit"] = np.array(fit)

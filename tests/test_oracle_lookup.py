@@ -245,6 +245,12 @@ def test_propagation_helpers_match_the_references_own_tests(golden):
                             for t in LF.TABLES})
         for fit in (LK.table_propagation(L), O.table_propagation(L)):
             assert np.array_equal(np.asarray(fit), a("fit")), (fit, a("fit"))
+    for i in range(int(g["n_bk"])):
+        G = SimpleNamespace(sector=g[f"bk{i}_G_sector"], module=g[f"bk{i}_G_module"], nbars=int(g[f"bk{i}_G_nbars"]),
+                            sector_names=[str(s) for s in g[f"bk{i}_G_sector_names"]])
+        sk, mk = LK.bar_keys(G)
+        assert sk.astype(str).tolist() == g[f"bk{i}_sector_keys"].tolist()
+        assert mk.astype(str).tolist() == g[f"bk{i}_module_keys"].tolist()
     for i in range(int(g["n_br"])):
         G = SimpleNamespace(sector=g[f"br{i}_G_sector"], module=g[f"br{i}_G_module"], nbars=int(g[f"br{i}_G_nbars"]),
                             sector_names=[str(s) for s in g[f"br{i}_G_sector_names"]])
