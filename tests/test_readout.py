@@ -15,6 +15,13 @@ from crvgpu import readout as RO
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "readout_calls.json")
 
 
+def _raising(exc, msg):
+    """A property that raises exc(msg) when read (a recorded geometry attribute whose read failed)."""
+    def get(self):
+        raise exc(msg)
+    return property(get)
+
+
 def decode(v):
     if isinstance(v, list):
         raise TypeError("bare lists are tagged")
@@ -38,8 +45,7 @@ def decode(v):
         attrs, props = {}, {}
         for k, x in v["obj"].items():
             if isinstance(x, dict) and "raises" in x:
-                exc = getattr(builtins, x["raises"][0])
-                props[k] = property(lambda self, exc=exc, msg=x["raises"][1]: (_ for _ in ()).throw(exc(msg)))
+                props[k] = _raising(getattr(builtins, x["raises"][0]), x["raises"][1])
             else:
                 attrs[k] = decode(x)
         cls = type("Recorded", (), props)
