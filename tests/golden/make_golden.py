@@ -2,7 +2,7 @@
 
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_fuzz, lookup_chain,
-attach, chaintests, readout, wiring, propagation, pulsetests; default all)
+attach, chaintests, readout, wiring, propagation, pulsecache, pulsetests; default all)
 The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
@@ -30,6 +30,8 @@ Fixtures (compressed .npz, a few hundred kB in total):
   lookup_fuzz.json  600 mutated images of the two lookup_file.npz files (byte flips, corrupted 8-byte fields,
                  truncations, inserted / deleted bytes) as recipes, with the reference's verdict on each: the hash of its
                  decoded arrays, or the exception its load raised
+  pulsecache.npz the distinct reconstruct_full calls of the reference's normal-equation-cache tests
+                 (crv/tests/test_pulsefit_normal_cache.py: an edge batch and a synthetic batch; 12.5 ns) with outputs
   pulsetests.npz every reconstruct call of the reference's own pulse-fit tests (crv/tests/test_reco_pulsefit.py:
                  injected-parameter recovery, below threshold, pedestal undershoot; at its stock 12.5 ns period), with
                  the reference's outputs
@@ -1106,6 +1108,42 @@ def make_propagation():
     np.savez_compressed(HERE / "propagation.npz", **out)
 
 
+def make_pulsecache():
+    """The reference's normal-equation-cache tests (crv/tests/test_pulsefit_normal_cache.py: an edge batch with a flat
+    waveform, an 11-sample saturated prefix, a pedestal undershoot and a 12-of-36 valid length, and a synthetic batch;
+    stock 12.5 ns) run under pytest with reconstruct_full recorded; identical calls (cache on and off) kept once."""
+    import hashlib
+    import pytest
+    records, seen = [], set()
+    orig = PF.reconstruct_full
+
+    def recorded(adc, n, start_tdc, pedestal_db, calib_area, calib_height, cfg=None, *a, **k):
+        out = orig(adc, n, start_tdc, pedestal_db, calib_area, calib_height,
+                   cfg if cfg is not None else PF.RecoConfig(), *a, **k)
+        args = tuple(np.asarray(x).copy() for x in (adc, n, start_tdc, pedestal_db, calib_area, calib_height))
+        h = hashlib.sha256(b"".join(x.tobytes() for x in args)).hexdigest()
+        if h not in seen and cfg is None:
+            seen.add(h)
+            records.append((args, out))
+        return out
+
+    set_period(12.5)
+    PF.reconstruct_full = recorded
+    try:
+        rc = pytest.main(["-q", "-p", "no:cacheprovider", str(REF / "tests" / "test_pulsefit_normal_cache.py")])
+    finally:
+        PF.reconstruct_full = orig
+        set_period(PERIOD)
+    assert rc == 0, f"the reference's normal-cache tests failed here ({rc})"
+    out = {"n": np.int64(len(records)), "period": np.array([12.5])}
+    for i, (args, r) in enumerate(records):
+        for k, v in zip(("adc", "n", "start", "ped", "area", "height"), args):
+            out[f"r{i}_{k}"] = v
+        for k, v in r.items():
+            out[f"r{i}_out_{k}"] = np.asarray(v)
+    np.savez_compressed(HERE / "pulsecache.npz", **out)
+
+
 def make_attach():
     import json
     import pytest
@@ -1157,7 +1195,7 @@ if __name__ == "__main__":
     for name, fn in (("pulsefit", make_pulsefit), ("concat", make_concat), ("waveform", make_waveform),
                      ("waveform_gate", make_waveform_gate),
                      ("coinc", make_coinc), ("stats", make_stats), ("pixelid", make_pixelid), ("lookup", make_lookup), ("lookup_file", make_lookup_file), ("lookup_fuzz", make_lookup_fuzz),
-                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("propagation", make_propagation), ("pulsetests", make_pulsetests)):
+                     ("lookup_chain", make_lookup_chain), ("attach", make_attach), ("chaintests", make_chaintests), ("readout", make_readout), ("wiring", make_wiring), ("propagation", make_propagation), ("pulsecache", make_pulsecache), ("pulsetests", make_pulsetests)):
         if not ONLY or name in ONLY:
             fn()
     for f in sorted(HERE.glob("*.npz")):

@@ -232,3 +232,19 @@ def test_pulse_configuration_wiring_matches_the_references_own_tests(golden):
             assert_same(v, g[f"r{i}_P_{k}"], f"r{i}.{k}")
         total += len(wf)
     assert total > 20
+
+
+def test_pulsefit_matches_the_references_normal_cache_batches(golden):
+    """crv/tests/test_pulsefit_normal_cache.py replayed (make_golden.py pulsecache; 12.5 ns): its edge batch (flat
+    waveform, saturated prefix, pedestal undershoot, short valid length) and synthetic batch give the reference's
+    reconstruct_full outputs."""
+    g = golden("pulsecache.npz")
+    period = float(g["period"][0])
+    cfg = CF.RecoConfig(period=period)
+    for i in range(int(g["n"])):
+        args = [g[f"r{i}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
+        r = O.reconstruct_full(*args, cfg, period)
+        keys = [k[len(f"r{i}_out_"):] for k in g.files if k.startswith(f"r{i}_out_")]
+        assert set(keys) == set(r)
+        for k in keys:
+            assert_same(r[k], g[f"r{i}_out_{k}"], f"r{i}.{k}")
