@@ -199,6 +199,7 @@ class DeviceTables:
         self.nbars = nb
         rc = cfg.response
         status = effective_status(cond)
+        check_readout_mask(cond, nb)
         dev = (np.asarray(cond.deviation, float) * rc.photon_yield_variation_scale + 1.0) * rc.photon_yield_scale
         f64 = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float64))).to(device)  # noqa: E731
         i32 = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.int32))).to(device)    # noqa: E731
@@ -225,6 +226,21 @@ class DeviceTables:
 
     def c_pixels(self):
         return self.pixels.c_pixels()
+
+
+def check_readout_mask(cond, nbars):
+    """The engine keeps one status table per channel: the readout-masked status (readout.effective_status), which the
+    response needs to drop absent SiPMs.  The reference's reco stages read the unmasked status, and the finder reads it
+    for a pulse's same-side partner SiPM (PE compensation, crv/crvfastsim/reco/coinc.py:312-314).  With masks that
+    cover whole bar sides, as readout.sensor_mask builds them, the two agree wherever a pulse can exist; a mask that
+    splits a side (SiPM 0 without 2, or 1 without 3) would not, and is refused."""
+    mask = getattr(cond, "readout_mask", None)
+    if mask is None:
+        return
+    m = np.asarray(mask, bool)[:4 * nbars].reshape(-1, 4)
+    if np.any(m[:, 0] != m[:, 2]) or np.any(m[:, 1] != m[:, 3]):
+        raise NotImplementedError("readout masks must cover whole bar sides (SiPMs 0 and 2, 1 and 3 together), "
+                                  "as readout.sensor_mask builds them")
 
 
 def effective_status(cond):

@@ -106,3 +106,19 @@ def test_the_chain_uses_the_readout_status():
     assert effective_status(cond).tolist() == [0, 3, 4, 1]
     with pytest.raises(ValueError, match="boolean numpy array"):
         effective_status(_Cond(np.zeros(4, np.int64), np.ones(4, int)))
+
+
+def test_the_engine_refuses_masks_that_split_a_bar_side():
+    """Masks built by sensor_mask cover whole sides and pass; one that masks SiPM 2 but not SiPM 0 of a bar is refused
+    (the finder reads a pulse's same-side partner in the unmasked status)."""
+    from crvgpu.response import check_readout_mask
+    geom = type("G", (), {})()
+    geom.sector_names, geom.sector, geom.nbars = ["A", "B"], np.array([0, 1, 0]), 3
+    cfg = {"crs.sipmsAtSide0A": True, "crs.sipmsAtSide1A": False, "crs.sipmsAtSide0B": False,
+           "crs.sipmsAtSide1B": True}
+    check_readout_mask(RO.apply(_Cond(np.zeros(12, np.int64)), geom, cfg), 3)
+    check_readout_mask(_Cond(np.zeros(12, np.int64)), 3)
+    split = np.ones(12, bool)
+    split[4 * 1 + 2] = False
+    with pytest.raises(NotImplementedError, match="whole bar sides"):
+        check_readout_mask(_Cond(np.zeros(12, np.int64), split), 3)
