@@ -9,9 +9,9 @@
  *   crv_photon_counts / crv_photons  <- crvfastsim.response.photons.make_photons      (crv/crvfastsim/response/photons.py:359)
  *   crv_sipm                         <- crvfastsim.response.sipm.simulate             (crv/crvfastsim/response/sipm.py:102)
  *   crv_response                     <- crvfastsim.chain.charges                      (crv/crvfastsim/chain.py:151)
- *   crv_digis                        <- crvfastsim.chain.digis + reco.waveform.synthesize
- *                                                                                     (crv/crvfastsim/chain.py:234,
- *                                                                                      crv/crvfastsim/reco/waveform.py:74)
+ *   crv_digis                        <- crvfastsim.chain.digis                        (crv/crvfastsim/chain.py:234)
+ *   crv_synthesize                   <- crvfastsim.reco.waveform.synthesize           (crv/crvfastsim/reco/waveform.py:74)
+ *   crv_tdc0_per_feb                 <- crvfastsim.chain.tdc0_per_feb                 (crv/crvfastsim/chain.py:219)
  *   crv_reco_waveforms               <- crvfastsim.chain.reco_waveforms + reco.pulsefit.concat_waveforms
  *                                                                                     (crv/crvfastsim/chain.py:273,
  *                                                                                      crv/crvfastsim/reco/pulsefit.py:319)
@@ -54,6 +54,8 @@ extern "C" {
                                   16 cross-talk generations, 64 nodes per generation) */
 #define CRV_ST_NONFINITE 4     /* a non-finite input where a finite one is required */
 #define CRV_ST_ORDER 8         /* input not grouped/sorted as the entry point requires */
+#define CRV_ST_BOUNDS 16       /* crv_pulses: a waveform's samples [off, off + n) outside the sample array (or its
+                                  record slots outside the workspace); that waveform is skipped, nothing is read */
 
 /* need[] slots */
 #define CRV_NEED_STEPS_PER_EVENT 0
@@ -275,6 +277,27 @@ int crv_digis(const CrvParams *p, const CrvChannels *ch, int64_t ncharges, const
               int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
 
 /*
+ * waveform.synthesize with the caller's TDC0 (crv/crvfastsim/reco/waveform.py:74-172, whose tdc0_of_chan gives one
+ * TDC0 per charge cluster): as crv_digis, but tdc0_rows[q] is the TDC0 (ns) of the cluster that charge row q belongs
+ * to (read at the first charge of every cluster; the host broadcasts the caller's per-cluster values), and no run
+ * table is needed (the TDC0 draw is the caller's).  Workspace: crv_digis_workspace.
+ */
+int crv_synthesize(const CrvParams *p, const CrvChannels *ch, int64_t ncharges, const int64_t *label, const double *time,
+                   const double *charge, const double *tdc0_rows, const double *tmpl, int32_t tlen, int64_t slot_cap,
+                   CrvDigis *out, int64_t out_cap, int64_t *n_out_dev, void *workspace, int64_t workspace_bytes,
+                   void *stream, CrvStatus *status_dev);
+
+/*
+ * chain.tdc0_per_feb (crv/crvfastsim/chain.py:219-231): TDC0 (ns) of every SiPM label, one keyed uniform x
+ * feb_phase_width per (event, FEB key) (feb_key_mode 0: ROC * 1000 + FEB, 1: FEB), the draw crv_digis makes.
+ * ev_keys / ev_runs (optional, n_events sorted event keys and their runs) give the run of each label's event (run 0
+ * without them; a label whose event is missing, or whose channel is outside the channel table, sets CRV_ST_ORDER).
+ */
+int crv_tdc0_per_feb(const CrvParams *p, const CrvChannels *ch, int64_t nlabels, const int64_t *labels,
+                     const int64_t *ev_keys, const uint32_t *ev_runs, int64_t n_events, double *tdc0, void *stream,
+                     CrvStatus *status_dev);
+
+/*
  * pulsefit.reconstruct: nw waveforms; waveform w has n[w] valid samples at sample rows [off[w], off[w] + n[w]) of
  * adc16 (int16) or adc64 (int64; exactly one is non-null), start TDC, DB pedestal, calibration area and height;
  * nsamples: rows of the sample array.  max_pulses: rounds per waveform (reconstruct_full passes max(cfg max, longest
@@ -300,9 +323,12 @@ int crv_pulses_shape(int32_t threads, int32_t blocks_per_sm, int32_t rounds);
  * CRV_PULSES_STATIC_MAX_BYTES per device, so the call allocates nothing (launch profiler off).  For callers that must
  * not allocate once running: cudaMalloc/cudaFree synchronise the device and stall other streams sharing it, and plain
  * C FFI hosts have no caching allocator.  Limits: crv_pulses_workspace(p, nw, nsamples) must not exceed the maximum
- * (else CRV_ERR_TOO_LARGE, nothing launched); the first call on a device (that device current) sets up the scratch
- * address and should precede any stream capture; the scratch needs no zeroing; calls overlapping in time on one
- * device share the scratch and race, so serialise them.  Arguments and results as crv_pulses.
+ * (else CRV_ERR_TOO_LARGE, nothing launched).  Every call looks up the array's address on the current device (so a
+ * device reset does not leave a stale address); the first call on a device loads the library's device code there,
+ * which is when the array is reserved under lazy module loading (the CUDA default since 12.2; with
+ * CUDA_MODULE_LOADING=EAGER every device the library touches reserves it at load), and should precede any stream
+ * capture.  The scratch needs no zeroing; calls overlapping in time on one device share the scratch and race, so
+ * serialise them.  Arguments and results as crv_pulses.
  */
 #define CRV_PULSES_STATIC_MAX_BYTES (64ll << 20)
 int crv_pulses_static(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *off, const int32_t *n,

@@ -16,7 +16,7 @@ c_i32, c_i64, c_u32, c_f64, c_p = ctypes.c_int32, ctypes.c_int64, ctypes.c_uint3
 
 CRV_OK, CRV_ERR_ARG, CRV_ERR_CUDA, CRV_ERR_TOO_LARGE = 0, 1, 2, 3
 PULSES_STATIC_MAX_BYTES = 64 << 20
-ST_CAPACITY, ST_LIMIT, ST_NONFINITE, ST_ORDER = 1, 2, 4, 8
+ST_CAPACITY, ST_LIMIT, ST_NONFINITE, ST_ORDER, ST_BOUNDS = 1, 2, 4, 8, 16
 NEED = dict(STEPS_PER_EVENT=0, PHOTONS_PER_SIPM=1, CHARGE_FACTOR=2, DIGIS=3, SAMPLES=4, PULSES=5, HITS_PER_EVENT=6,
             CLUSTERS=7, PHOTONS_TOTAL=8, SLOTS_TOTAL=9, CHARGES_OUT=10, DIGIS_OUT=11, WAVEFORMS=12, PULSES_OUT=13,
             MEMBERS=14, PHOTONS_OUT=15)
@@ -189,6 +189,9 @@ _SIGS = {
     "crv_digis_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
     "crv_digis": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_p, c_i32, c_p, c_p, c_i64, c_i64,
                           P(CrvDigis), c_i64, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_synthesize": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_p, c_p, c_i32, c_i64, P(CrvDigis),
+                               c_i64, c_p, c_p, c_i64, c_p, c_p]),
+    "crv_tdc0_per_feb": (c_i32, [P(CrvParams), P(CrvChannels), c_i64, c_p, c_p, c_p, c_i64, c_p, c_p, c_p]),
     "crv_pulses_workspace": (c_i64, [P(CrvParams), c_i64, c_i64]),
     "crv_pulses": (c_i32, [P(CrvParams), c_i64, c_i64, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_p, c_i32, P(CrvPulses),
                            c_i64, c_p, c_p, c_p, c_i64, c_p, c_p]),

@@ -1,0 +1,176 @@
+"""Error report of an FP32-mixed chain run against the FP64-plain run of the same events and keys.
+
+Both runs draw the same keyed random numbers, so their outputs describe the same physics and differ only through
+arithmetic precision; where a quantity crosses a decision boundary (a sample on an ADC integer, a fit near a failure
+test, a pulse near a zero-suppression threshold) the two runs can differ in a discrete way.  Nothing here requires
+equal counts: digis are matched by (SiPM label, start TDC), pulses by SiPM label and nearest time, finder hits the
+same way, and clusters by (event, sector type, member set), so the report is complete whatever the two runs produced.
+
+Reported per quantity:
+  charges      counts, mean PE relative error;
+  digis        matched fraction, ADC mismatch rate over the matched samples, the fraction of those mismatches that
+               sit at a quantisation boundary (the FP64 value lies closer to an ADC integer than the FP32-vs-FP64
+               voltage difference, so rounding alone explains the flip), the largest |dADC|, |dV| quantiles;
+  pulses       counts, mean PE relative error (all pulses, and matched well-fitted pairs), |dt| p50 / p99 / max on
+               matched well-fitted pairs, matched fraction;
+  clusters     counts, the fraction of FP64 clusters with an FP32 cluster of the same event, sector type and member
+               pulses, and PE / start-time differences of those pairs.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+PULSE_MATCH_NS = 2.0      # pulses of one SiPM are several samples (12.55 ns) apart; a match is within 2 ns
+
+
+def _np(x):
+    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+
+
+def _q(a, qs=(0.5, 0.99, 1.0)):
+    a = np.asarray(a, float)
+    return [float(v) for v in np.quantile(a, qs)] if len(a) else [None] * len(qs)
+
+
+def match_nearest(key_a, t_a, key_b, t_b, tol):
+    """For every item of a, the index of the item of b with the same key and the nearest time (within tol), else -1.
+    One-to-one: when two a items want one b item, the nearer one gets it and the other takes its next-nearest free
+    neighbour within tol."""
+    key_a, t_a, key_b, t_b = (np.asarray(v) for v in (key_a, t_a, key_b, t_b))
+    if len(key_a) == 0 or len(key_b) == 0:
+        return np.full(len(key_a), -1, np.int64)
+    ob = np.lexsort((t_b, key_b))
+    kb, tb = key_b[ob], t_b[ob]
+    # position of each a item in b's (key, time) order
+    oa = np.lexsort((t_a, key_a))
+    ka, ta = key_a[oa], t_a[oa]
+    allk = np.concatenate([kb, ka])
+    allt = np.concatenate([tb, ta])
+    src = np.concatenate([np.zeros(len(kb), np.int8), np.ones(len(ka), np.int8)])
+    o = np.lexsort((src, allt, allk))
+    isb = src[o] == 0
+    nb_before = np.cumsum(isb) - isb                     # b items strictly before each position
+    pos_sorted = nb_before[~isb]                         # for a items in (key, time) order
+    pos = np.empty(len(ka), np.int64)
+    pos[:] = pos_sorted
+    lo = np.searchsorted(kb, ka, "left")
+    hi = np.searchsorted(kb, ka, "right")
+    cands = []
+    for d in (-1, 0):
+        j = pos + d
+        ok = (j >= lo) & (j < hi)
+        jj = np.clip(j, 0, len(tb) - 1)
+        cands.append((np.where(ok, np.abs(tb[jj] - ta), np.inf), jj))
+    best = np.where(cands[0][0] <= cands[1][0], cands[0][1], cands[1][1])
+    dist = np.minimum(cands[0][0], cands[1][0])
+    res = np.full(len(ka), -1, np.int64)
+    used = np.zeros(len(tb), bool)
+    order = np.argsort(dist, kind="stable")
+    order = order[dist[order] <= tol]
+    # greedy one-to-one claim: in distance order, a b item goes to the first a item that wants it
+    first = np.unique(best[order], return_index=True)[1]
+    take = order[np.sort(first)]
+    used[best[take]] = True
+    res[take] = ob[best[take]]
+    rest = np.setdiff1d(order, take)
+    for i in rest:                                      # rare: two a items nearest to one b item
+        for d in (-1, 0, 1, -2, 2):
+            j = pos[i] + d
+            if lo[i] <= j < hi[i] and not used[j] and abs(tb[j] - ta[i]) <= tol:
+                used[j] = True
+                res[i] = ob[j]
+                break
+    out = np.full(len(key_a), -1, np.int64)
+    out[oa] = res
+    return out
+
+
+def error_table(r64, r32, adc_conversion, adc_pedestal):
+    """FP32-mixed vs FP64 report of two ChainResults of the same batch and seed (both run with keep=True)."""
+    out = {}
+    # ---- charges
+    q64, q32 = _np(r64.charges.pe), _np(r32.charges.pe)
+    out["charges"] = {"fp64": int(len(q64)), "fp32": int(len(q32)),
+                      "mean_pe_rel": float(q32.mean() / q64.mean() - 1) if len(q64) and len(q32) else None}
+    # ---- digis by (label, start TDC)
+    D64 = {k: _np(v) for k, v in r64.digis.items()}
+    D32 = {k: _np(v) for k, v in r32.digis.items()}
+    k64 = D64["chan"].astype(np.int64) * (1 << 24) + (D64["starttdc"].astype(np.int64) + (1 << 23))
+    k32 = D32["chan"].astype(np.int64) * (1 << 24) + (D32["starttdc"].astype(np.int64) + (1 << 23))
+    com, i64, i32 = np.intersect1d(k64, k32, assume_unique=False, return_indices=True)
+    a64, a32 = D64["adc"][i64].astype(np.int64), D32["adc"][i32].astype(np.int64)
+    v64, v32 = D64["volt"][i64], D32["volt"][i32]
+    mis = a64 != a32
+    nmis = int(mis.sum())
+    x64 = v64 * adc_conversion + adc_pedestal + 0.5
+    dx = np.abs(v32 - v64) * adc_conversion
+    at_boundary = np.abs(x64 - np.rint(x64)) <= dx + 1e-9
+    dv = np.abs(v32 - v64)
+    out["digis"] = {"fp64": int(len(k64)), "fp32": int(len(k32)), "matched": int(len(com)),
+                    "matched_frac": float(len(com) / max(len(k64), 1)),
+                    "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(nmis / max(a64.size, 1)),
+                    "adc_mismatch_at_boundary_frac": float(at_boundary[mis].mean()) if nmis else 1.0,
+                    "adc_mismatch_max_abs": int(np.abs(a64 - a32).max()) if a64.size else 0,
+                    "volt_abs_err_mV_p50_p99_max": [None if v is None else 1e3 * v for v in _q(dv.ravel())]}
+    # ---- pulses by (SiPM label, nearest time)
+    W64 = {k: _np(v) for k, v in r64.waveforms.items()}
+    W32 = {k: _np(v) for k, v in r32.waveforms.items()}
+    P64 = {k: _np(v) for k, v in r64.pulses.items()}
+    P32 = {k: _np(v) for k, v in r32.pulses.items()}
+    lab64, lab32 = W64["label"][P64["wf"]], W32["label"][P32["wf"]]
+    m = match_nearest(lab64, P64["time"], lab32, P32["time"], PULSE_MATCH_NS)
+    ok = m >= 0
+    good = ok.copy()
+    good[ok] = ~P64["failed"][ok].astype(bool) & ~P32["failed"][m[ok]].astype(bool)
+    dt = np.abs(P32["time"][m[good]] - P64["time"][good])
+    pe_pairs = (P32["pe"][m[good]].mean() / P64["pe"][good].mean() - 1) if good.any() else None
+    out["pulses"] = {"fp64": int(len(lab64)), "fp32": int(len(lab32)), "matched": int(ok.sum()),
+                     "matched_frac": float(ok.mean()) if len(ok) else 1.0,
+                     "failed_flag_differs": int((P64["failed"][ok].astype(bool)
+                                                 != P32["failed"][m[ok]].astype(bool)).sum()),
+                     "mean_pe_rel": float(P32["pe"].mean() / P64["pe"].mean() - 1) if len(lab64) and len(lab32)
+                     else None,
+                     "mean_pe_rel_matched_good": None if pe_pairs is None else float(pe_pairs),
+                     "time_abs_err_ns_p50_p99_max": _q(dt)}
+    # ---- finder hits and clusters
+    H64 = {k: _np(v) for k, v in r64.hits.items()}
+    H32 = {k: _np(v) for k, v in r32.hits.items()}
+
+    def hit_keys(H):
+        n = len(H["bar"])
+        ev = np.repeat(H["ev_key"], H["ev_count"])[:n]
+        return ev, ev * 32768 + H["bar"].astype(np.int64) * 4 + H["sipm"]
+
+    ev64, hk64 = hit_keys(H64)
+    ev32, hk32 = hit_keys(H32)
+    hm = match_nearest(hk32, H32["time"], hk64, H64["time"], PULSE_MATCH_NS)   # FP32 hit -> FP64 hit
+
+    def member_sets(r, H, hit_map):
+        C = {k: _np(v) for k, v in r.clusters.items()}
+        M = {k: _np(v) for k, v in r.members.items()}
+        row0 = H["ev_start"][np.searchsorted(H["ev_key"], M["event"])] if len(M["event"]) else np.zeros(0, np.int64)
+        rows = row0 + M["idx"]
+        ids = hit_map(rows)
+        sets = {}
+        for c, h in zip(M["cl"], ids):
+            sets.setdefault(int(c), []).append(int(h))
+        keys = {}
+        for c in range(len(C["pe"])):
+            keys[(int(C["event"][c]), int(C["type"][c]), tuple(sorted(sets.get(c, []))))] = c
+        return C, keys
+
+    C64, s64 = member_sets(r64, H64, lambda rows: rows)
+    unmatched = iter(range(-1, -10 ** 9, -1))
+    C32, s32 = member_sets(r32, H32, lambda rows: np.array([hm[r] if hm[r] >= 0 else next(unmatched)
+                                                             for r in rows], np.int64))
+    same = [(s64[k], s32[k]) for k in s64 if k in s32]
+    if same:
+        a, b = np.array(same).T
+        dpe = np.abs(C32["pe"][b] / C64["pe"][a] - 1)
+        dst = np.abs(C32["start"][b] - C64["start"][a])
+    else:
+        dpe = dst = np.zeros(0)
+    out["clusters"] = {"fp64": int(len(C64["pe"])), "fp32": int(len(C32["pe"])),
+                       "same_members_frac": float(len(same) / max(len(s64), 1)),
+                       "pe_rel_err_p50_p99_max": _q(dpe), "start_abs_err_ns_p50_p99_max": _q(dst)}
+    return out

@@ -25,6 +25,32 @@ from .response import (DeviceSteps, DeviceTables, ResponseEngine, _stream, _torc
 from .waveform import DigiEngine, digis, single_pe_template  # noqa: F401
 
 
+def tdc0_per_feb(labels, cond, rng, width=PERIOD, key="roc_feb", *, seed=None, runs=None, geom=None):
+    """chain.tdc0_per_feb (crv/crvfastsim/chain.py:219-231): TDC0 [ns] of every SiPM label, one uniform x width per
+    (event, ROC, FEB) (key "roc_feb") or per (event, FEB) (key "feb").  The draw is the engine's keyed one (seed, run,
+    subrun, event, FEB key), the TDC0 chain.digis uses, so it does not depend on which labels are asked for or in which
+    order; seed = `seed`, else a draw from rng (the reference draws sequentially from rng in sorted-key order).
+    runs: optional {event key: run}.  Same ValueErrors as the reference for the width and the key."""
+    from .params import validate_feb_phase
+    from .waveform import _dev, _geometry_for, _tdc0_device
+    validate_feb_phase(width, key, PERIOD)
+    labels = np.asarray(labels, np.int64)
+    if len(labels) == 0:
+        return np.zeros(0)
+    if int(labels.min()) < 0 or int((labels % CHAN_MULT).max()) >= len(np.asarray(cond.status)):
+        raise ValueError("labels must be event key * 32768 + a channel of the conditions' channel table")
+    cfg = ChainConfig(feb_phase_width=float(width), feb_phase_key=key)
+    geom = geom if geom is not None else _geometry_for(cond)
+    tabs = DeviceTables(geom, cond, cfg)
+    P = make_params(cfg, seed_of(rng, seed))
+    ek = er = None
+    if runs:
+        keys = np.array(sorted(runs), np.int64)
+        ek = _dev(keys, np.int64)
+        er = _dev(np.array([runs[int(k)] for k in keys], np.int64).astype(np.uint32).view(np.int32), np.int32)
+    return _tdc0_device(P, tabs, _dev(labels, np.int64), ek, er)
+
+
 def reco_waveforms(D, cond):
     """Digis -> reco waveform rows with calibration, sorted by (event, channel, start) (pulsefit.concat_waveforms'
     grouping; host glue as in the reference)."""

@@ -269,8 +269,8 @@ const char* crv_status_string(int32_t flags) {
   static thread_local char buf[256];
   if (flags == 0) return "ok";
   buf[0] = 0;
-  const char* names[] = {"capacity", "limit", "nonfinite", "order"};
-  for (int i = 0; i < 4; ++i)
+  const char* names[] = {"capacity", "limit", "nonfinite", "order", "bounds"};
+  for (int i = 0; i < 5; ++i)
     if (flags & (1 << i)) {
       if (buf[0]) strncat(buf, "|", sizeof(buf) - strlen(buf) - 1);
       strncat(buf, names[i], sizeof(buf) - strlen(buf) - 1);
@@ -658,7 +658,8 @@ extern "C" int64_t crv_digis_workspace(const CrvParams* p, int64_t ncharges, int
 }
 
 static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const long long* nq_dev,
-                     const int64_t* label, const double* time, const double* charge, const double* tmpl, int32_t tlen,
+                     const int64_t* label, const double* time, const double* charge, const double* tdc0_rows,
+                     const double* tmpl, int32_t tlen,
                      const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
                      CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
                      void* stream, CrvStatus* status_dev) {
@@ -700,11 +701,11 @@ static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges
   CK(cudaGetLastError());
   WfGroups G{&w.totals[0], w.gstart, w.gcount, w.glabel, w.grun};
   if (p->precision == 1)
-    CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen,
-                                w.g_nkept, w.cl, s));
+    CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_bound,
+                                w.g_maxlen, w.g_nkept, w.cl, s));
   else
-    CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, w.g_tdc0, w.g_bound, w.g_maxlen,
-                                 w.g_nkept, w.cl, s));
+    CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_bound,
+                                 w.g_maxlen, w.g_nkept, w.cl, s));
   CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s, &w.totals[0]));
   {
     crv::Mark mark_("k_check_caps", s);
@@ -718,11 +719,11 @@ static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges
   CK(cudaGetLastError());
   G.n = &w.totals[2];
   if (p->precision == 1)
-    CK(launch_wf_synth<float>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.g_nkept, w.cl,
-                              w.D, S, s));
+    CK(launch_wf_synth<float>(*p, G, ncharges, time, charge, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_maxlen,
+                              w.g_nkept, w.cl, w.D, S, s));
   else
-    CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, w.g_tdc0, w.g_maxlen, w.g_nkept, w.cl,
-                               w.D, S, s));
+    CK(launch_wf_synth<double>(*p, G, ncharges, time, charge, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_maxlen,
+                               w.g_nkept, w.cl, w.D, S, s));
   CK(exclusive_scan(w.dn, ncharges, Identity(), w.out_off, &w.totals[3], w.parts, s, &w.totals[2]));
   {
     crv::Mark mark_("k_check_caps", s);
@@ -747,8 +748,62 @@ extern "C" int crv_digis(const CrvParams* p, const CrvChannels* ch, int64_t ncha
                          const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, int64_t slot_cap,
                          CrvDigis* out, int64_t out_cap, int64_t* n_out_dev, void* workspace, int64_t workspace_bytes,
                          void* stream, CrvStatus* status_dev) {
-  return digis_run(p, ch, ncharges, nullptr, label, time, charge, tmpl, tlen, ev_keys, ev_runs, n_events, slot_cap,
-                   out, out_cap, n_out_dev, workspace, workspace_bytes, stream, status_dev);
+  return digis_run(p, ch, ncharges, nullptr, label, time, charge, nullptr, tmpl, tlen, ev_keys, ev_runs, n_events,
+                   slot_cap, out, out_cap, n_out_dev, workspace, workspace_bytes, stream, status_dev);
+}
+
+extern "C" int crv_synthesize(const CrvParams* p, const CrvChannels* ch, int64_t ncharges, const int64_t* label,
+                              const double* time, const double* charge, const double* tdc0_rows, const double* tmpl,
+                              int32_t tlen, int64_t slot_cap, CrvDigis* out, int64_t out_cap, int64_t* n_out_dev,
+                              void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  if (ncharges > 0 && !tdc0_rows) return CRV_ERR_ARG;
+  return digis_run(p, ch, ncharges, nullptr, label, time, charge, tdc0_rows, tmpl, tlen, nullptr, nullptr, 0,
+                   slot_cap, out, out_cap, n_out_dev, workspace, workspace_bytes, stream, status_dev);
+}
+
+namespace crv {
+__global__ void k_tdc0_labels(CrvParams p, CrvChannels ch, long long n, const long long* __restrict__ label,
+                              const long long* __restrict__ ev_keys, const uint32_t* __restrict__ ev_runs,
+                              long long n_ev, double* __restrict__ out, Status* status) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long lab = label[i];
+    const long long c = lab % 32768;
+    if (lab < 0 || c >= ch.nchan) {
+      set_flag(status, CRV_ST_ORDER);
+      out[i] = 0.0;
+      continue;
+    }
+    uint32_t r = 0;
+    if (ev_keys && n_ev > 0) {
+      const long long k = lab / 32768;
+      long long lo = 0, hi = n_ev;
+      while (lo < hi) {
+        long long m = (lo + hi) >> 1;
+        if (ev_keys[m] < k) lo = m + 1; else hi = m;
+      }
+      if (lo < n_ev && ev_keys[lo] == k) r = ev_runs[lo];
+      else set_flag(status, CRV_ST_ORDER);
+    }
+    out[i] = tdc0_of(p, ch, lab, r);
+  }
+}
+}  // namespace crv
+
+extern "C" int crv_tdc0_per_feb(const CrvParams* p, const CrvChannels* ch, int64_t nlabels, const int64_t* labels,
+                                const int64_t* ev_keys, const uint32_t* ev_runs, int64_t n_events, double* tdc0,
+                                void* stream, CrvStatus* status_dev) {
+  if (!p || !ch || !status_dev || nlabels < 0 || n_events < 0) return CRV_ERR_ARG;
+  if (nlabels == 0) return CRV_OK;
+  if (!labels || !tdc0 || (n_events > 0 && (!ev_keys || !ev_runs))) return CRV_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  {
+    crv::Mark mark_("k_tdc0_labels", s);
+    k_tdc0_labels<<<grid_for(nlabels, 256, 8), 256, 0, s>>>(*p, *ch, nlabels, reinterpret_cast<const long long*>(labels),
+                                                           reinterpret_cast<const long long*>(ev_keys), ev_runs,
+                                                           n_events, tdc0, reinterpret_cast<Status*>(status_dev));
+  }
+  CK(cudaGetLastError());
+  return CRV_OK;
 }
 
 // ---- pulsefit.reconstruct -----------------------------------------------------------------------------------------
@@ -799,10 +854,15 @@ static PulseWs pulse_layout(char* base, long long nw, long long nsamples, size_t
   return w;
 }
 
-__global__ void k_pulse_caps(long long nw, const long long* __restrict__ nw_dev, const int32_t* __restrict__ n,
-                             int max_pulses, int32_t* __restrict__ cap) {
+__global__ void k_pulse_caps(long long nw, const long long* __restrict__ nw_dev, const long long* __restrict__ off,
+                             const int32_t* __restrict__ n, long long nsamples, int max_pulses,
+                             int32_t* __restrict__ cap) {
   nw = bounded_count(nw, nw_dev);
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+    if (!wave_in_bounds(off[w], n[w], nsamples)) {     // no slots: the fit skips it and reports CRV_ST_BOUNDS
+      cap[w] = 0;
+      continue;
+    }
     int b = n[w] / 2 + 1;
     cap[w] = b < max_pulses ? b : max_pulses;
   }
@@ -873,12 +933,13 @@ static int pulses_run(const CrvParams* p, int64_t nw, const long long* nw_dev, i
   unsigned g = grid_for(nw, 256, 8);
   {
     crv::Mark mark_("k_pulse_caps", s);
-    k_pulse_caps<<<g, 256, 0, s>>>(nw, nw_dev, n, max_pulses, w.cap);
+    k_pulse_caps<<<g, 256, 0, s>>>(nw, nw_dev, reinterpret_cast<const long long*>(off), n, nsamples, max_pulses,
+                                   w.cap);
   }
   CK(exclusive_scan(w.cap, nw, Identity(), w.slot_off, &w.totals[0], w.parts, s, nw_dev));
   WaveIn W{nw, nw_dev, reinterpret_cast<const long long*>(off), n, reinterpret_cast<const long long*>(start_tdc), ped_db,
-           area, height, adc16, reinterpret_cast<const long long*>(adc64)};
-  PulseSlots PS{w.slot_off, w.cap, w.count, wf_near, w.rec};
+           area, height, adc16, reinterpret_cast<const long long*>(adc64), nsamples};
+  PulseSlots PS{w.slot_off, w.cap, w.count, wf_near, w.rec, w.rc};
   if (p->precision == 1)
     CK(launch_pulsefit<float>(*p, W, w.yscr, max_pulses, PS, w.q, S, s));
   else
@@ -1452,7 +1513,7 @@ extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const Crv
     CK(keep_total(&resp_layout(w.scratch, *p, c.events, c.steps, c.photons, &b).totals[1], CRV_CHAIN_PHOTONS));
   }
   CK(guard(CRV_CHAIN_CHARGES, c.charges));
-  rc = digis_run(p, ch, c.charges, &m[CRV_CHAIN_CHARGES], w.Q.label, w.Q.time, w.Q.charge, tmpl, tlen, ev_keys,
+  rc = digis_run(p, ch, c.charges, &m[CRV_CHAIN_CHARGES], w.Q.label, w.Q.time, w.Q.charge, nullptr, tmpl, tlen, ev_keys,
                  ev_runs, c.events, c.slots, &w.D, c.digis, N(CRV_CHAIN_DIGIS), w.scratch, w.scratch_bytes, stream,
                  status_dev);
   if (rc != CRV_OK) return rc;

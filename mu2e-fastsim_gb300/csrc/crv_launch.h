@@ -67,14 +67,15 @@ cudaError_t launch_sipm(const CrvParams& p, const CrvPixels& px, const SipmGroup
 
 template <typename R>
 cudaError_t launch_wf_prepass(const CrvParams& p, const CrvChannels& ch, const WfGroups& G, long long ng_bound,
-                              const double* time, const double* tmpl, int tlen, double* g_tdc0, int32_t* g_bound,
-                              int32_t* g_maxlen, int32_t* g_nkept, WfCluster* cl, cudaStream_t s);
+                              const double* time, const double* tmpl, int tlen, const double* tdc0_rows,
+                              double* g_tdc0, int32_t* g_bound, int32_t* g_maxlen, int32_t* g_nkept, WfCluster* cl,
+                              cudaStream_t s);
 
 template <typename R>
 cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_bound, const double* time,
-                            const double* charge, const double* tmpl, int tlen, const double* g_tdc0,
-                            const int32_t* g_maxlen, const int32_t* g_nkept, const WfCluster* cl, const DigiSlots& D,
-                            Status* status, cudaStream_t s);
+                            const double* charge, const double* tmpl, int tlen, const double* tdc0_rows,
+                            const double* g_tdc0, const int32_t* g_maxlen, const int32_t* g_nkept,
+                            const WfCluster* cl, const DigiSlots& D, Status* status, cudaStream_t s);
 
 template <typename R>
 cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses, const PulseSlots& S,

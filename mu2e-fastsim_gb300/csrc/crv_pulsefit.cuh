@@ -37,6 +37,7 @@ struct WaveIn {
   const double* height;
   const int16_t* adc16;      // samples (one of adc16 / adc64)
   const long long* adc64;
+  long long nsamples;        // rows of the sample array: every waveform must lie inside it
 };
 
 __device__ __forceinline__ double round_half_away(double x) {
@@ -334,7 +335,14 @@ struct PulseSlots {
   int32_t* count;            // per waveform: pulses
   uint8_t* near;             // per waveform: wf_near_threshold
   PulseRec* rec;
+  long long rc;              // record slots of the workspace: every waveform's slots must lie inside it
 };
+
+// A waveform's samples [off, off + n) lie in the sample array and its record slots in the workspace.  Waveforms that
+// break this (inconsistent offsets or lengths from the caller) are not read; the status reports CRV_ST_BOUNDS.
+__device__ __forceinline__ bool wave_in_bounds(long long off, int n, long long nsamples) {
+  return off >= 0 && n >= 0 && off <= nsamples && (long long)n <= nsamples - off;
+}
 
 __device__ __forceinline__ float round_half_away_f(float x) {
   float a = floorf(fabsf(x) + 0.5f);
@@ -765,7 +773,12 @@ __global__ void __launch_bounds__(128) k_pf_begin(CrvParams p, WaveIn W, double*
        base += nwarps * 32) {
     const long long w = base + lane_id();
     bool pend = false;
-    if (w < nw) {
+    if (w < nw && !(wave_in_bounds(W.off[w], W.n[w], W.nsamples) && S.off[w] >= 0 && S.cap[w] >= 0 &&
+                    S.off[w] + S.cap[w] <= S.rc)) {
+      set_flag(status, CRV_ST_BOUNDS);
+      S.count[w] = 0;
+      S.near[w] = 0;
+    } else if (w < nw) {
       PfState st;
       pend = pf_begin<R>(p, W, yscr, max_pulses, w, st);
       if (pend) Q.st[w] = st;

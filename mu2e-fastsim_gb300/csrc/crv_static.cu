@@ -9,9 +9,12 @@
 // Rules of use:
 //  * The scratch holds at most CRV_PULSES_STATIC_MAX_BYTES (64 MiB).  A call whose workspace need
 //    (crv_pulses_workspace(p, nw, nsamples)) is larger returns CRV_ERR_TOO_LARGE and launches nothing.
-//  * The first call on a device (with that device current) looks up the array's device address
-//    (cudaGetSymbolAddress, which also loads this module on that device); later calls reuse the cached address.
-//    Make that first call before any stream capture.
+//  * Every call looks up the array's device address for the current device (cudaGetSymbolAddress, a host-side
+//    lookup that launches nothing).  The first lookup on a device also loads this module there (under lazy module
+//    loading, the default since CUDA 12.2, that is when the 64 MiB are reserved; with eager loading every device the
+//    library is used on reserves them when the library loads), so make the first call on each device before any
+//    stream capture.  Looking the address up per call, instead of caching it, keeps the entry point correct after a
+//    device reset or a re-created primary context, where the module is loaded again and the array may move.
 //  * Nothing in the scratch has to start at zero: every word a call reads is written earlier by the same call, and
 //    the call clears its own counters.  The status block must start at zero, as for every entry point.
 //  * One scratch per device: two calls in flight on the same device at once (different streams or host threads)
@@ -20,31 +23,17 @@
 //  * No allocation happens inside the call as long as the launch profiler (crv_profile) is off.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "../../include/crvgpu.h"
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-
 __device__ __align__(256) unsigned char g_pulse_scratch[CRV_PULSES_STATIC_MAX_BYTES];
 
-std::mutex g_setup_mu;
-void* g_scratch_of[kMaxDevices] = {};
-
-// Device address of this device's scratch; set up once per device with that device current.
+// Device address of the scratch on the current device (looked up on every call; see above).
 int scratch_for_current_device(void** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return CRV_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return CRV_ERR_ARG;
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_of[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_pulse_scratch) != cudaSuccess || !p) return CRV_ERR_CUDA;
-    g_scratch_of[dev] = p;
-  }
-  *out = g_scratch_of[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_pulse_scratch) != cudaSuccess || !p) return CRV_ERR_CUDA;
+  *out = p;
   return CRV_OK;
 }
 

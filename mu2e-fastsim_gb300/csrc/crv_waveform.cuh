@@ -171,7 +171,8 @@ __device__ __forceinline__ int cluster_length_serial(const CrvParams& p, const d
 template <typename R>
 __global__ void __launch_bounds__(256) k_wf_prepass(CrvParams p, CrvChannels ch, WfGroups G,
                                                     const double* __restrict__ time, const double* __restrict__ tmpl,
-                                                    int tlen, double* __restrict__ g_tdc0, int32_t* __restrict__ g_bound,
+                                                    int tlen, const double* __restrict__ tdc0_rows,
+                                                    double* __restrict__ g_tdc0, int32_t* __restrict__ g_bound,
                                                     int32_t* __restrict__ g_maxlen, int32_t* __restrict__ g_nkept,
                                                     WfCluster* __restrict__ cl) {
   __shared__ double vmax_s;
@@ -192,15 +193,17 @@ __global__ void __launch_bounds__(256) k_wf_prepass(CrvParams p, CrvChannels ch,
     const int n = G.count[g];
     const long long q0 = G.start[g];
     const double* t = time + q0;
-    const double tdc0 = tdc0_of(p, ch, G.label[g], G.run ? G.run[g] : 0u);
+    // keyed TDC0 of the group, unless the caller gives one per cluster (then the channel tables are not read)
+    const double tdc0 = tdc0_rows ? 0.0 : tdc0_of(p, ch, G.label[g], G.run ? G.run[g] : 0u);
     long long bound = 0;
     int maxlen = 0, nk = 0;
     for (int a = 0; a < n;) {
       int b = a + 1;
       while (b < n && !(t[b] - t[b - 1] > gap)) ++b;
       if (double(b - a) * vmax >= p.min_voltage) {
-        const long long k0 = (long long)ceil((t[a] - p.period - tdc0) / p.period);
-        const double ts = cluster_ts(k0, p.period, tdc0);
+        const double tdc0c = tdc0_rows ? tdc0_rows[q0 + a] : tdc0;
+        const long long k0 = (long long)ceil((t[a] - p.period - tdc0c) / p.period);
+        const double ts = cluster_ts(k0, p.period, tdc0c);
         const int L = cluster_length_serial<R>(p, t, a, b, ts, tlen, nr, ip);
         bound += (L + zs - 1) / zs;
         maxlen = L > maxlen ? L : maxlen;
@@ -256,7 +259,8 @@ __device__ __forceinline__ int16_t adc_of_f(const CrvParams& p, float v, float c
 template <typename R>
 __global__ void __launch_bounds__(256, 3) k_wf_synth(CrvParams p, WfGroups G, const double* __restrict__ time,
                                                   const double* __restrict__ charge, const double* __restrict__ tmpl,
-                                                  int tlen, const double* __restrict__ g_tdc0,
+                                                  int tlen, const double* __restrict__ tdc0_rows,
+                                                  const double* __restrict__ g_tdc0,
                                                   const int32_t* __restrict__ g_maxlen,
                                                   const int32_t* __restrict__ g_nkept,
                                                   const WfCluster* __restrict__ cl, int lo, int cap, int last_pass,
@@ -308,6 +312,7 @@ __global__ void __launch_bounds__(256, 3) k_wf_synth(CrvParams p, WfGroups G, co
       const int a = C.a, b = C.b, L = C.L;
       const long long k0 = C.k0;
       const double ts = C.ts;
+      const double tdc0c = tdc0_rows ? tdc0_rows[q0 + a] : tdc0;
       // stage each charge's first reached sample and normalised charge (once per charge, not per sample)
       const bool staged = (b - a) <= WF_QSTAGE;
       if (staged) {
@@ -415,7 +420,7 @@ __global__ void __launch_bounds__(256, 3) k_wf_synth(CrvParams p, WfGroups G, co
             if (lane_id() == 0) {
               D.chan[o] = lab;
               D.start[o] = __dadd_rn(ts, __dmul_rn(double(i0), p.period));
-              D.tdc0[o] = tdc0;
+              D.tdc0[o] = tdc0c;
               D.starttdc[o] = k0 + i0;
             }
           }

@@ -44,3 +44,71 @@ def uneven_waveforms(rng, W=120, period=12.55, area=400.0):
             y += gumbel(t, pe * area / b, mu, b)
         adc[w, :n] = np.clip(np.round(y + 100.0 + rng.normal(0, 2.0, n)), 0, 4095)
     return adc, lens, start, np.full(W, 100.0), np.full(W, area), np.full(W, area / 15.0)
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# Conditioning of the reference's pulse fit: how far its own results move under last-bit changes of its arithmetic
+
+FIT_KEYS = ("pe", "peph", "time", "height", "beta", "chi2", "letime", "ped", "fit_A", "fit_mu", "fit_b")
+
+
+def _perturbed_exp(mode):
+    def f(x, *a, **k):
+        v = np.exp(x)
+        if mode == "up":
+            return np.nextafter(v, np.inf)
+        if mode == "down":
+            return np.nextafter(v, -np.inf)
+        bits = np.asarray(v).view(np.uint64)
+        up = ((bits * np.uint64(0x9E3779B97F4A7C15)) >> np.uint64(63)).astype(bool)
+        return np.where(up, np.nextafter(v, np.inf), np.nextafter(v, -np.inf))
+    return f
+
+
+def fit_sensitivity(args, cfg, period, full, ref=None):
+    """Per-pulse relative movement of the oracle's pulse fit (the reference's LM schedule, pulsefit.py:125-216) under
+    changes that leave the mathematics unchanged: every exp of the fit model one ulp up, one ulp down, or up/down by a
+    hash of its value, and the fit points summed in reverse order.  These are the differences between NumPy's and
+    CUDA's exp (each within about one ulp) and between two reduction orders.  Returns ({key: per-pulse max relative
+    movement}, the unperturbed oracle result); ref (the reference's own outputs) adds |oracle - ref| as one more
+    sample, so a platform whose NumPy exp differs from the fixture generator's is covered too.  Perturbations that
+    change the pulse list or a failure flag are left out (none do on the committed fixtures)."""
+    import types
+    from oracle import oracle as O
+    fit0 = O.fit_gumbel
+
+    def reverse(t, y, mask, p0, lo, hi, iterations=40):
+        return fit0(t[:, ::-1], y[:, ::-1], mask[:, ::-1], p0, lo, hi, iterations)
+
+    def call():
+        if full:
+            return O.reconstruct_full(*args, cfg, period)
+        return O.reconstruct(*args, cfg, period)
+
+    base = call()
+    sens = {k: np.zeros(len(base["pe"])) for k in FIT_KEYS}
+    variants = []
+    for mode in ("up", "down", "hash", "reverse"):
+        if mode == "reverse":
+            O.fit_gumbel = reverse
+        else:
+            fake = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("__")})
+            fake.exp = _perturbed_exp(mode)
+            O.fit_gumbel = types.FunctionType(fit0.__code__, {**fit0.__globals__, "np": fake}, "fit_gumbel",
+                                              fit0.__defaults__)
+        try:
+            variants.append(call())
+        finally:
+            O.fit_gumbel = fit0
+    if ref is not None:
+        variants.append(ref)
+    ok = ~np.asarray(base["failed"], bool)
+    for r in variants:
+        if len(r["pe"]) != len(base["pe"]) or not np.array_equal(np.asarray(r["failed"], bool), ~ok):
+            continue
+        for k in FIT_KEYS:
+            a, b = np.asarray(r[k], float), np.asarray(base[k], float)
+            rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+            rel[a == b] = 0.0
+            sens[k] = np.maximum(sens[k], rel)
+    return sens, base

@@ -1,40 +1,40 @@
 """GPU pulse reconstruction against the reference's own outputs (golden fixtures) and the oracle.
 
-FP64: pulse counts, sequence numbers and flags identical.  Fitted parameters: every pulse within 1e-8 relative, and
-at least 95 % of the pulses' PE and time within 1e-9.  exp and the reduction order differ in the last bit between NumPy and CUDA;
-at the minimum chi2 is flat to ~1e-16 relative, which leaves the minimiser defined only to ~1e-9..1e-8 relative, so
-a few ill-conditioned fits land 1e-9..3e-9 apart.  FP32-mixed: mean PE within 0.3 % and time within 0.05 ns of FP64
-on the non-failed fits.
+FP64: pulse counts, sequence numbers and flags identical.  Fitted parameters: each pulse's relative deviation from the
+reference is at most 1e-9, or, for a pulse the reference's own fit does not define to 1e-9, at most SENS_FACTOR times
+the movement of that pulse under one-ulp changes of the fit's exp and a reversed summation order
+(tests/helpers.py fit_sensitivity; tests/test_pulsefit_conditioning.py shows such pulses exist).  CUDA's exp and the
+GPU's summation order differ from NumPy's in those ways only.  FP32-mixed: mean PE within 0.3 % and the 99th
+percentile of |time - FP64 time| within 0.05 ns on the non-failed fits.
 """
 import numpy as np
 import pytest
 
 from crvgpu import config as CF
+from tests.helpers import FIT_KEYS, fit_sensitivity
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-9          # for at least FRAC of the pulses (PE and time)
-FRAC = 0.95
-RMAX = 1e-8          # for every pulse and parameter
+RTOL = 1e-9          # the workload's contract for fitted PE and time
+SENS_FACTOR = 4.0    # allowance over the measured last-bit movement (exp within ~1 ulp on either side, any order)
 EXACT = ("wf", "seq", "failed", "zerondf", "pedfromdb", "wf_near_threshold")
-CLOSE = ("pe", "peph", "time", "height", "beta", "chi2", "letime", "ped", "fit_A", "fit_mu", "fit_b")
 
 
-def compare(got, ref, tag):
+def compare(got, ref, tag, sens):
     for k in EXACT:
         assert np.array_equal(np.asarray(got[k]).astype(np.int64), np.asarray(ref[k]).astype(np.int64)), (tag, k)
     worst = {}
     ok_fit = ~np.asarray(ref["failed"], bool)
-    for k in CLOSE:
+    for k in FIT_KEYS:
         a, b = np.asarray(got[k], float), np.asarray(ref[k], float)
+        bound = np.maximum(RTOL, SENS_FACTOR * sens[k])
         if k.startswith("fit_"):          # raw fit values of a failed (non-converged) fit are diagnostics only
-            a, b = a[ok_fit], b[ok_fit]
+            a, b, bound = a[ok_fit], b[ok_fit], bound[ok_fit]
         rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
         rel[(a == b)] = 0.0
+        bad = np.flatnonzero(rel > bound)
         worst[k] = (float(rel.max()) if len(rel) else 0.0, float((rel <= RTOL).mean()) if len(rel) else 1.0)
-        assert worst[k][0] <= RMAX, (tag, k, worst[k])
-        if k in ("pe", "time"):
-            assert worst[k][1] >= FRAC, (tag, k, worst[k])
+        assert len(bad) == 0, (tag, k, [(int(i), float(rel[i]), float(bound[i])) for i in bad[:5]])
     return worst
 
 
@@ -45,10 +45,12 @@ def test_pulsefit_matches_reference_fixtures(golden, tag):
     period = 12.5 if tag == "p125" else float(g["period"][0])
     cfg = CF.RecoConfig(period=period)
     args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
-    f = PF.reconstruct_full if tag in ("uneven", "edge") else PF.reconstruct
+    full = tag in ("uneven", "edge")
+    f = PF.reconstruct_full if full else PF.reconstruct
     r = f(*args, cfg)
     ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f"{tag}_out_")}
-    worst = compare(r, ref, tag)
+    sens, _ = fit_sensitivity(args, cfg, period, full, ref)
+    worst = compare(r, ref, tag, sens)
     print(tag, "max rel diff / fraction within 1e-9",
           {k: f"{v[0]:.1e}/{v[1]:.4f}" for k, v in worst.items()})
 
@@ -75,7 +77,7 @@ def test_pulsefit_fp32_mixed_accuracy():
     pe64, pe32 = r64["pe"][i64][good], r32["pe"][i32][good]
     assert abs(pe32.mean() / pe64.mean() - 1) < 3e-3
     dt = np.abs(r32["time"][i32][good] - r64["time"][i64][good])
-    assert np.median(dt) < 0.05
+    assert np.quantile(dt, 0.99) < 0.05, np.quantile(dt, [0.5, 0.99, 1.0])
 
 
 def test_graph_fitter_and_launch_shapes_match_the_engine():
@@ -111,13 +113,65 @@ def test_graph_fitter_and_launch_shapes_match_the_engine():
 
 def test_pulsefit_matches_the_references_own_tests(golden):
     """The reference's own pulse-fit test calls (injected single pulses, below threshold, pedestal undershoot; 12.5
-    ns) on the GPU: integer outputs identical, parameters as the reference within the fit's 1e-8."""
+    ns) on the GPU: integer outputs identical, parameters within 1e-9 or the fit's own last-bit movement."""
     from crvgpu import pulsefit as PF
     g = golden("pulsetests.npz")
     period = float(g["period"][0])
     for i in range(int(g["n"])):
         tag = f"r{i}"
         args = [g[f"{tag}_{k}"] for k in ("adc", "n", "start", "ped", "area", "height")]
-        r = PF.reconstruct(*args, CF.RecoConfig(period=period))
+        cfg = CF.RecoConfig(period=period)
+        r = PF.reconstruct(*args, cfg)
         ref = {k[len(tag) + 5:]: g[k] for k in g.files if k.startswith(f"{tag}_out_")}
-        compare(r, ref, tag)
+        sens, _ = fit_sensitivity(args, cfg, period, False, ref)
+        compare(r, ref, tag, sens)
+
+
+def test_waveform_outside_the_sample_array_is_skipped_and_reported():
+    """A waveform whose samples [off, off + n) do not lie in the sample array is not read: crv_pulses reports
+    CRV_ST_BOUNDS and fits the other waveforms as if it were absent (checked on the device before any sample read)."""
+    import ctypes
+    import torch
+    from crvgpu import _capi
+    from crvgpu.params import make_params
+    from tests.helpers import uneven_waveforms
+    adc, n, start, ped, area, height = uneven_waveforms(np.random.default_rng(4), 6)
+    W, L = adc.shape
+    off = np.arange(W) * L
+    d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a).astype(dt))).cuda()  # noqa: E731
+    lib = _capi.load()
+    P = make_params(reco=CF.RecoConfig(), precision="fp64")
+
+    def run(off_, n_):
+        cap = 16 * W + 64
+        out = {k: torch.zeros(cap, dtype=torch.int64, device="cuda") for k in _capi.PULSE_INT}
+        out.update({k: torch.zeros(cap, dtype=torch.float64, device="cuda") for k in _capi.PULSE_FLOAT})
+        out.update({k: torch.zeros(cap, dtype=torch.uint8, device="cuda") for k in _capi.PULSE_BOOL})
+        near = torch.zeros(W, dtype=torch.uint8, device="cuda")
+        n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
+        st = _capi.DeviceStatus("cuda")
+        st.reset()
+        ws = torch.empty(lib.crv_pulses_workspace(ctypes.byref(P), W, W * L), dtype=torch.uint8, device="cuda")
+        O = _capi.CrvPulses(*[_capi.ptr(out[k]) for k in _capi.PULSE_INT + _capi.PULSE_FLOAT + _capi.PULSE_BOOL])
+        o_d, n_d = d(off_, np.int64), d(n_, np.int32)
+        rc = lib.crv_pulses(ctypes.byref(P), W, W * L, _capi.ptr(o_d), _capi.ptr(n_d), _capi.ptr(d(start, np.int64)),
+                            _capi.ptr(d(ped, np.float64)), _capi.ptr(d(area, np.float64)),
+                            _capi.ptr(d(height, np.float64)), _capi.ptr(d(adc, np.int16)), None, 64, ctypes.byref(O),
+                            cap, _capi.ptr(n_out), _capi.ptr(near), _capi.ptr(ws), ws.numel(),
+                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), st.ptr)
+        _capi.check(rc, "crv_pulses")
+        flags, _ = st.read()
+        m = int(n_out.item())
+        return flags, {k: v[:m].cpu().numpy() for k, v in out.items()}
+
+    f0, ref = run(off, n)
+    assert f0 == 0 and len(ref["wf"]) > 0
+    bad_off, bad_n = off.copy(), n.copy()
+    bad_off[2] = W * L - n[2] + 1          # one sample past the end of the array
+    bad_n[4] = -3                          # a negative length
+    f1, got = run(bad_off, bad_n)
+    assert f1 & _capi.ST_BOUNDS
+    keep = (ref["wf"] != 2) & (ref["wf"] != 4)
+    assert not np.isin(got["wf"], [2, 4]).any()
+    for k in ("wf", "seq", "pe", "time"):
+        assert np.array_equal(got[k], ref[k][keep]), k

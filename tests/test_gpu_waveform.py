@@ -38,7 +38,7 @@ def test_digis_fp64_bit_exact(charges, noise):
     D = W.digis(Q, cond, cfg, None, key=55, geom=geom, runs=runs)
     Do = oracle_digis(Q, cond, cfg, 55, runs, noise)
     assert len(D["chan"]) == len(Do["chan"]) > 100
-    for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc"):
+    for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc", "cluster_chan", "cluster_tstart", "cluster_keep"):
         assert np.array_equal(D[k], Do[k]), k
 
 
@@ -99,3 +99,61 @@ def test_digis_window_gate_bit_exact(golden):
         assert len(Do["chan"]) > 0
         for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc"):
             assert np.array_equal(D[k], Do[k]), (w, k)
+
+
+@pytest.mark.parametrize("form", ["callable", "array", "batched"])
+def test_synthesize_dropin_equals_the_references_outputs(golden, tmp_path, form):
+    """waveform.synthesize with the caller's TDC0 (callable or array over labels, and batches of whole clusters) on the
+    reference's own fixture: every digi field and the per-cluster outputs equal the reference's bit for bit."""
+    from crvgpu import waveform as W
+    from crvgpu.config import WaveformConfig
+    g = golden("waveform.npz")
+    spe = tmp_path / "spe.txt"
+    np.savetxt(spe, np.c_[g["traw"], g["vraw"]], fmt="%.17g")
+    cfg = WaveformConfig(min_voltage=float(g["min_voltage"][0]), single_pe_stretch=float(g["stretch"][0]),
+                         single_pe_file=str(spe))
+    assert np.array_equal(W.single_pe_template(cfg), g["template"])
+    uch, tab = g["uch"], g["tdc0_tab"]
+    calls = []
+
+    def lut(lab):
+        calls.append(len(lab))
+        return tab[np.searchsorted(uch, lab)]
+    if form == "array":
+        dense = np.full(int(uch.max()) + 1, np.nan)
+        dense[uch] = tab
+        tdc0 = dense
+    else:
+        tdc0 = lut
+    kw = {"max_charges": 1000} if form == "batched" else {}
+    r = W.synthesize(g["chan"], g["time"], g["charge"], tdc0, cfg, tuple(g["window"]), None, **kw)
+    for k in ("chan", "start", "tdc0", "starttdc", "volt", "adc", "cluster_chan", "cluster_tstart", "cluster_keep"):
+        a, b = np.asarray(r[k]), np.asarray(g[f"clean_{k}"])
+        assert a.shape == b.shape and a.dtype.kind == b.dtype.kind, (k, a.shape, b.shape, a.dtype, b.dtype)
+        assert np.array_equal(a, b), k
+    if form == "batched":
+        assert len(calls) > 5 and sum(calls) == len(g["clean_cluster_chan"])
+
+
+def test_tdc0_per_feb_is_the_digis_draw_and_groups_by_feb():
+    """chain.tdc0_per_feb: the keyed TDC0 the digis use (oracle bit for bit), one value per (event, ROC, FEB) or
+    (event, FEB), in [0, width); the reference's ValueErrors for a bad width or key."""
+    from crvgpu import chain as CH
+    geom, cond, cfg, steps = workload(16, seed=3)
+    ev = np.unique((np.asarray(steps["subrun"], np.int64) << 20) | np.asarray(steps["event"], np.int64))
+    labels = (ev[:, None] * 32768 + np.arange(0, 4 * geom.nbars, 3)[None, :]).ravel()
+    runs = {int(k): 1 for k in ev}
+    run_of = lambda keys: np.ones(len(np.asarray(keys).ravel()), np.int64)  # noqa: E731
+    for key, width in (("roc_feb", 12.55), ("feb", 6.0)):
+        t = CH.tdc0_per_feb(labels, cond, None, width, key, seed=77, runs=runs)
+        to = O.tdc0_of_labels(labels, cond, 77, width, key, run_of)
+        assert np.array_equal(t, to)
+        assert np.all((t >= 0) & (t < width))
+        ch = labels % 32768
+        feb = cond.feb[ch] if key == "feb" else cond.roc[ch] * 1000 + cond.feb[ch]
+        grp = (labels // 32768) * 1_000_000 + feb
+        for gk in np.unique(grp)[:50]:
+            assert len(np.unique(t[grp == gk])) == 1
+    for bad in (dict(width=13.0), dict(width=float("nan")), dict(key="roc")):
+        with pytest.raises(ValueError):
+            CH.tdc0_per_feb(labels, cond, None, **{"width": 12.0, "key": "roc_feb", **bad}, seed=1)

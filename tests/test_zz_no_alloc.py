@@ -2,7 +2,9 @@
 
 Two calls in a row on different inputs (FP64 with 64-bit samples, then FP32-mixed with 16-bit samples): each must equal
 crv_pulses on the same input bit for bit, so nothing left in the shared scratch by the first call leaks into the second.
-A request larger than the static maximum is refused with CRV_ERR_TOO_LARGE before anything is launched.
+A request larger than the static maximum is refused with CRV_ERR_TOO_LARGE before anything is launched.  Around a
+later static call with every buffer allocated beforehand, neither the device's free memory nor torch's allocator
+changes: the call itself allocates nothing.
 The file is collected last so the test also runs after every other GPU test in one process.
 """
 import ctypes
@@ -26,7 +28,7 @@ def _inputs(seed, n_wf, adc16):
                 max_pulses=int(max(8, int(np.max(n)))))
 
 
-def _call(P, x, static):
+def _buffers(P, x, static):
     import torch
     from crvgpu import _capi
     L = _capi.load()
@@ -43,19 +45,36 @@ def _call(P, x, static):
             _capi.ptr(x["ped"]), _capi.ptr(x["area"]), _capi.ptr(x["height"]), _capi.ptr(x["adc16"]),
             _capi.ptr(x["adc64"]), x["max_pulses"], ctypes.byref(O), cap, _capi.ptr(n_out), _capi.ptr(near)]
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    if static:
-        rc = L.crv_pulses_static(*args, stream, status.ptr)
-    else:
+    ws = None
+    if not static:
         ws = torch.empty(L.crv_pulses_workspace(ctypes.byref(P), nw, x["ns"]), dtype=torch.uint8, device="cuda")
-        rc = L.crv_pulses(*args, _capi.ptr(ws), ws.numel(), stream, status.ptr)
+    return dict(L=L, args=args, stream=stream, status=status, ws=ws, out=out, near=near, n_out=n_out, O=O)
+
+
+def _launch(b, static):
+    from crvgpu import _capi
+    if static:
+        rc = b["L"].crv_pulses_static(*b["args"], b["stream"], b["status"].ptr)
+    else:
+        rc = b["L"].crv_pulses(*b["args"], _capi.ptr(b["ws"]), b["ws"].numel(), b["stream"], b["status"].ptr)
     _capi.check(rc, "crv_pulses_static" if static else "crv_pulses")
+
+
+def _results(b, static):
+    import torch
     torch.cuda.synchronize()
-    flags, need = status.read()
+    flags, need = b["status"].read()
     assert flags == 0, (static, flags, need)
-    m = int(n_out.item())
-    res = {k: v[:m].cpu().numpy() for k, v in out.items()}
-    res["wf_near_threshold"] = near.cpu().numpy()
+    m = int(b["n_out"].item())
+    res = {k: v[:m].cpu().numpy() for k, v in b["out"].items()}
+    res["wf_near_threshold"] = b["near"].cpu().numpy()
     return res
+
+
+def _call(P, x, static):
+    b = _buffers(P, x, static)
+    _launch(b, static)
+    return _results(b, static)
 
 
 def test_static_scratch_matches_workspace_entry_point_on_two_calls():
@@ -93,3 +112,25 @@ def test_static_scratch_refuses_requests_above_its_maximum():
     assert rc == _capi.CRV_ERR_TOO_LARGE
     with pytest.raises(ValueError, match="static maximum"):
         _capi.check(rc, "crv_pulses_static")
+
+
+def test_static_call_allocates_nothing():
+    """With its inputs, outputs and status block allocated beforehand, a static call changes neither the device's
+    free memory (cudaMemGetInfo) nor torch's allocator: the entry point itself allocates nothing."""
+    import torch
+    from crvgpu import _capi
+    from crvgpu.params import make_params
+    _capi.profile(False)
+    P = make_params(precision="fp32")
+    x = _inputs(13, 700, adc16=True)
+    first = _call(P, x, static=True)                       # warm-up: module loaded, scratch address known
+    b = _buffers(P, x, static=True)
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    _launch(b, static=True)
+    torch.cuda.synchronize()
+    free1, alloc1 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    assert (free1, alloc1) == (free0, alloc0), (free0 - free1, alloc1 - alloc0)
+    again = _results(b, static=True)
+    for k in first:
+        assert np.array_equal(again[k], first[k], equal_nan=True), k
