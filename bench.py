@@ -684,7 +684,7 @@ def main():
     #   k_coinc:    per hit 28 B in (bar, SiPM, sequence, time, PE) + per event 20 B in (first hit, count, key)
     #               + per cluster 120 B out (event, type, PE, start, end, slope, average time, position, flags) + 4 B
     #               per member index
-    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth",), "k_coinc": ("k_coinc", "k_coinc_global"),
+    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth", "k_wf_synth32"), "k_coinc": ("k_coinc", "k_coinc_global"),
               "k_sipm_sim": ("k_sipm_sim",)}
 
     def alg_bytes(group):

@@ -7,10 +7,12 @@ equal counts: digis are matched by (SiPM label, start TDC), pulses by SiPM label
 same way, and clusters by (event, sector type, member set), so the report is complete whatever the two runs produced.
 
 Reported per quantity:
-  charges      counts, mean PE relative error;
-  digis        matched fraction, ADC mismatch rate over the matched samples, the fraction of those mismatches that
-               sit at a quantisation boundary (the FP64 value lies closer to an ADC integer than the FP32-vs-FP64
-               voltage difference, so rounding alone explains the flip), the largest |dADC|, |dV| quantiles;
+  charges      counts, mean PE relative error, and the SiPMs whose charge list differs (an FP32 recovery or firing
+               decision at its threshold: a different charge, not an arithmetic error downstream);
+  digis        matched fraction; ADC mismatch rate over the matched samples, split into digis of SiPMs whose charges
+               agree (waveform arithmetic alone: the fraction of mismatches at a quantisation boundary, i.e. one count
+               apart with the FP64 value closer to the ADC step than the FP32-vs-FP64 difference, the largest |dADC|,
+               |dV| quantiles) and digis of SiPMs whose charges differ;
   pulses       counts, mean PE relative error (all pulses, and matched well-fitted pairs), |dt| p50 / p99 / max on
                matched well-fitted pairs, matched fraction;
   clusters     counts, the fraction of FP64 clusters with an FP32 cluster of the same event, sector type and member
@@ -85,14 +87,43 @@ def match_nearest(key_a, t_a, key_b, t_b, tol):
     return out
 
 
+def changed_labels(l64, t64, q64, l32, t32, q32, t_tol=0.01, pe_rtol=1e-3):
+    """SiPM labels whose charge lists differ between the two runs (inputs sorted by label, then time): a label present
+    in one run only, a different charge count, or a charge whose time differs by more than t_tol ns or whose PE
+    differs by more than pe_rtol relative."""
+    u64, s64, c64 = np.unique(l64, return_index=True, return_counts=True)
+    u32, s32, c32 = np.unique(l32, return_index=True, return_counts=True)
+    both, j64, j32 = np.intersect1d(u64, u32, return_indices=True)
+    eq = c64[j64] == c32[j32]
+    changed = [np.setxor1d(u64, u32), both[~eq]]
+    lab = both[eq]
+    if len(lab):
+        n = c64[j64][eq]
+        rows64 = np.repeat(s64[j64][eq], n) + (np.arange(n.sum()) - np.repeat(np.cumsum(n) - n, n))
+        rows32 = np.repeat(s32[j32][eq], n) + (np.arange(n.sum()) - np.repeat(np.cumsum(n) - n, n))
+        bad = (np.abs(t64[rows64] - t32[rows32]) > t_tol) | \
+              (np.abs(q64[rows64] - q32[rows32]) > pe_rtol * np.maximum(np.abs(q64[rows64]), 1e-300))
+        per = np.add.reduceat(bad.astype(np.int64), np.cumsum(n) - n) > 0
+        changed.append(lab[per])
+    return np.unique(np.concatenate(changed)).astype(np.int64)
+
+
 def error_table(r64, r32, adc_conversion, adc_pedestal):
     """FP32-mixed vs FP64 report of two ChainResults of the same batch and seed (both run with keep=True)."""
     out = {}
-    # ---- charges
-    q64, q32 = _np(r64.charges.pe), _np(r32.charges.pe)
+    # ---- charges: the SiPM stage's FP32 recovery / firing decisions can differ from FP64 at a threshold, which
+    # changes a SiPM's charge list; digis of such SiPMs differ for that reason, not through waveform arithmetic
+    R64, R32 = r64.charges, r32.charges
+    l64, l32 = _np(R64.label), _np(R32.label)
+    t64, t32 = _np(R64.time), _np(R32.time)
+    q64, q32 = _np(R64.pe), _np(R32.pe)
+    changed = changed_labels(l64, t64, q64, l32, t32, q32)
+    nlab = len(np.union1d(np.unique(l64), np.unique(l32)))
     out["charges"] = {"fp64": int(len(q64)), "fp32": int(len(q32)),
-                      "mean_pe_rel": float(q32.mean() / q64.mean() - 1) if len(q64) and len(q32) else None}
-    # ---- digis by (label, start TDC)
+                      "mean_pe_rel": float(q32.mean() / q64.mean() - 1) if len(q64) and len(q32) else None,
+                      "sipms": int(nlab), "sipms_with_different_charges": int(len(changed)),
+                      "sipms_with_different_charges_frac": float(len(changed) / max(nlab, 1))}
+    # ---- digis by (label, start TDC); ADC mismatches split by whether the SiPM's charges agree
     D64 = {k: _np(v) for k, v in r64.digis.items()}
     D32 = {k: _np(v) for k, v in r32.digis.items()}
     k64 = D64["chan"].astype(np.int64) * (1 << 24) + (D64["starttdc"].astype(np.int64) + (1 << 23))
@@ -100,18 +131,28 @@ def error_table(r64, r32, adc_conversion, adc_pedestal):
     com, i64, i32 = np.intersect1d(k64, k32, assume_unique=False, return_indices=True)
     a64, a32 = D64["adc"][i64].astype(np.int64), D32["adc"][i32].astype(np.int64)
     v64, v32 = D64["volt"][i64], D32["volt"][i32]
+    same_in = ~np.isin(D64["chan"][i64], changed)
     mis = a64 != a32
-    nmis = int(mis.sum())
     x64 = v64 * adc_conversion + adc_pedestal + 0.5
-    dx = np.abs(v32 - v64) * adc_conversion
-    at_boundary = np.abs(x64 - np.rint(x64)) <= dx + 1e-9
+    x32 = v32 * adc_conversion + adc_pedestal + 0.5
+    # a flip at a quantisation boundary: one count apart, with the integer between the two values closer to the FP64
+    # value than the FP32-vs-FP64 difference itself (so rounding of a near-integer value explains it)
+    edge = np.maximum(np.floor(x64), np.floor(x32))
+    at_boundary = (np.abs(a64 - a32) == 1) & (np.abs(x64 - edge) <= np.abs(x32 - x64) + 1e-9)
+    ms, mc = mis[same_in], mis[~same_in]
     dv = np.abs(v32 - v64)
     out["digis"] = {"fp64": int(len(k64)), "fp32": int(len(k32)), "matched": int(len(com)),
                     "matched_frac": float(len(com) / max(len(k64), 1)),
-                    "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(nmis / max(a64.size, 1)),
-                    "adc_mismatch_at_boundary_frac": float(at_boundary[mis].mean()) if nmis else 1.0,
-                    "adc_mismatch_max_abs": int(np.abs(a64 - a32).max()) if a64.size else 0,
-                    "volt_abs_err_mV_p50_p99_max": [None if v is None else 1e3 * v for v in _q(dv.ravel())]}
+                    "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(mis.sum() / max(a64.size, 1)),
+                    "same_charges": {
+                        "adc_samples": int(ms.size), "adc_mismatch_rate": float(ms.sum() / max(ms.size, 1)),
+                        "adc_mismatch_at_boundary_frac": float(at_boundary[same_in][ms].mean()) if ms.any() else 1.0,
+                        "adc_mismatch_max_abs": int(np.abs(a64 - a32)[same_in].max()) if ms.size else 0,
+                        "volt_abs_err_mV_p50_p99_max": [None if v is None else 1e3 * v
+                                                        for v in _q(dv[same_in].ravel())]},
+                    "different_charges": {
+                        "adc_samples": int(mc.size), "adc_mismatch_rate": float(mc.sum() / max(mc.size, 1)),
+                        "adc_mismatch_max_abs": int(np.abs(a64 - a32)[~same_in].max()) if mc.size else 0}}
     # ---- pulses by (SiPM label, nearest time)
     W64 = {k: _np(v) for k, v in r64.waveforms.items()}
     W32 = {k: _np(v) for k, v in r32.waveforms.items()}

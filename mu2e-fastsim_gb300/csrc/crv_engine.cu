@@ -665,6 +665,7 @@ static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges
                      void* stream, CrvStatus* status_dev) {
   if (!p || !ch || !out || !n_out_dev || !status_dev || ncharges < 0 || slot_cap < 0 || out_cap < 0) return CRV_ERR_ARG;
   if (p->samples_zs <= 0 || p->samples_zs > 32 || tlen <= 0 || !tmpl) return CRV_ERR_ARG;
+  if (p->precision == 1 && tlen > 1024) return CRV_ERR_ARG;      // FP32-mixed: template copy in shared memory
   if (ncharges > 0 && (!label || !time || !charge)) return CRV_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (ncharges == 0) {
@@ -702,10 +703,10 @@ static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges
   WfGroups G{&w.totals[0], w.gstart, w.gcount, w.glabel, w.grun};
   if (p->precision == 1)
     CK(launch_wf_prepass<float>(*p, *ch, G, ncharges, time, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_bound,
-                                w.g_maxlen, w.g_nkept, w.cl, s));
+                                w.g_maxlen, w.g_nkept, w.cl, w.head, S, s));
   else
     CK(launch_wf_prepass<double>(*p, *ch, G, ncharges, time, tmpl, tlen, tdc0_rows, w.g_tdc0, w.g_bound,
-                                 w.g_maxlen, w.g_nkept, w.cl, s));
+                                 w.g_maxlen, w.g_nkept, w.cl, w.head, S, s));
   CK(exclusive_scan(w.g_bound, ncharges, Identity(), w.slot_off, &w.totals[1], w.parts, s, &w.totals[0]));
   {
     crv::Mark mark_("k_check_caps", s);

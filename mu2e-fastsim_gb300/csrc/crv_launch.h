@@ -69,7 +69,7 @@ template <typename R>
 cudaError_t launch_wf_prepass(const CrvParams& p, const CrvChannels& ch, const WfGroups& G, long long ng_bound,
                               const double* time, const double* tmpl, int tlen, const double* tdc0_rows,
                               double* g_tdc0, int32_t* g_bound, int32_t* g_maxlen, int32_t* g_nkept, WfCluster* cl,
-                              cudaStream_t s);
+                              int32_t* row_scratch, Status* status, cudaStream_t s);
 
 template <typename R>
 cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_bound, const double* time,

@@ -36,3 +36,17 @@ def test_match_nearest_equals_greedy_brute_force():
 def test_match_nearest_empty_sides():
     assert match_nearest(np.zeros(0), np.zeros(0), np.arange(3), np.arange(3.0), 1).shape == (0,)
     assert (match_nearest(np.arange(3), np.arange(3.0), np.zeros(0), np.zeros(0), 1) == -1).all()
+
+
+def test_changed_labels_finds_every_kind_of_difference():
+    from crvgpu.accuracy import changed_labels
+    l64 = np.array([1, 1, 2, 3, 3, 3, 5])
+    t64 = np.array([1.0, 2.0, 5.0, 1.0, 2.0, 3.0, 9.0])
+    q64 = np.ones(7)
+    l32 = np.array([1, 1, 2, 3, 3, 4])            # 3 lost a charge, 4 new, 5 missing
+    t32 = np.array([1.0, 2.0005, 5.5, 1.0, 2.0, 7.0])   # 1 within tolerance, 2 moved by 0.5 ns
+    q32 = np.ones(6)
+    assert changed_labels(l64, t64, q64, l32, t32, q32).tolist() == [2, 3, 4, 5]
+    q32b = q32.copy()
+    q32b[0] = 1.01
+    assert 1 in changed_labels(l64, t64, q64, l32, t32, q32b)
