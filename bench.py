@@ -69,7 +69,7 @@ def _cpu_worker(args):
     W = O.reco_waveforms(D, cond)
     rc = CF.RecoConfig()
     P = O.pulses_from_waveforms(W, cond, rc, rc.period)
-    out = O.clusters_from_pulses(W, P, G, cond.status, CF.FinderConfig())
+    out = O.clusters_from_pulses(W, P, G, cond.status, CF.workload_finder(G.sector_names))
     return time.perf_counter() - t0, n_events, len(out["cl_event"])
 
 
@@ -254,7 +254,7 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
     out["fp32_tuned_graph"] = {"waveforms_per_s": total / (ms / 1000.0), "ms": ms, "pulses": found,
                                "shape": {"threads": shape[0], "blocks_per_sm": shape[1], "rounds": shape[2]},
                                "tuning_ms": {f"{a}/{b}/{c}": round(v, 3) for (a, b, c), v in
-                                             tuner.best[tuner.bucket(int(chunks[0]['n'].numel()))][1].items()},
+                                             next(iter(tuner.best.values()))[1].items()},
                                "matches_plain": bool(same)}
     set_shape(DEFAULT_SHAPE)
     gf = None
@@ -386,12 +386,12 @@ def lookup_substeps(n_rows, reps=3, cpu_rows=20000, precision="fp64"):
     return out
 
 
-def fullscale(n_events, batch, seed=13, resident_batch=2048):
+def fullscale(n_events, batch, seed=13, resident_batch=2048, stage_events=4096):
     """Full-scale detector (86 modules of 4 x 16 counters, bar lengths over {230, 300, 450, 560, 660} cm, Poisson(60)
     steps plus 0.5 noise steps per counter per event): events/s of the chain on a resident subset, device time over
     the batches.  FP32-mixed through the resident engine (one CUDA graph replay per `resident_batch`-event batch) and
     per stage, FP64 plain per stage (`batch`-event batches: the per-stage workspaces of this geometry take ~150 GB
-    per 1,024 events)."""
+    per 1,024 events).  The per-stage legs run on the first `stage_events` events, the resident FP32 leg on all."""
     import torch
     from crvgpu import chain as CH, config as CF, geometry as GM
     from crvgpu.resident import ChainCaps, ResidentChain, caps_for
@@ -419,15 +419,18 @@ def fullscale(n_events, batch, seed=13, resident_batch=2048):
         return e0.elapsed_time(e1), ncl
 
     rb, nsteps = make(resident_batch)                  # the events, generated once; per-stage batches are views
+    stage_events = min(stage_events, n_events)
     batches = [slice_events(r, a, min(a + batch, r.nevents)) for r in rb for a in range(0, r.nevents, batch)]
-    out = {"events": n_events, "batch": batch, "resident_batch": resident_batch, "steps": nsteps,
-           "counters": geom.nbars}
+    batches = batches[:max(1, stage_events // batch)]
+    out = {"events": n_events, "stage_events": sum(b.nevents for b in batches), "batch": batch,
+           "resident_batch": resident_batch, "resident_batches": len(rb), "steps": nsteps, "counters": geom.nbars}
     for prec in ("fp32", "fp64"):
         eng = CH.ChainEngine(geom, cond, CF.ChainConfig(precision=prec))
         eng.run(batches[0], 3)
         ms, ncl = device_ms(lambda ds: eng.run(ds, 3).n_clusters, batches)
-        out[prec if prec == "fp64" else "fp32_stage"] = {"events_per_s": n_events / (ms / 1000.0), "ms": ms,
-                                                         "clusters": ncl}
+        ne = sum(b.nevents for b in batches)
+        out[prec if prec == "fp64" else "fp32_stage"] = {"events_per_s": ne / (ms / 1000.0), "ms": ms,
+                                                         "clusters": ncl, "events": ne}
         if prec == "fp32":
             try:
                 eng.release()                          # the per-stage workspaces of this geometry are large
@@ -452,8 +455,110 @@ def fullscale(n_events, batch, seed=13, resident_batch=2048):
         eng = None
         torch.cuda.empty_cache()
     out["fp32_over_fp64"] = out["fp32"]["events_per_s"] / out["fp64"]["events_per_s"]
+    try:                                                 # the oracle chain on a bounded full-scale sample, one core
+        dt, ne, ncl = _cpu_full_worker((6, seed))
+        out["cpu_baseline"] = {"value": ne / dt, "unit": "events/s", "cores": 1, "kind": "port",
+                               "sample": f"{ne} full-scale events through the oracle chain on 1 core ({dt:.1f} s)"}
+    except Exception as exc:                             # reported baseline only
+        out["cpu_baseline"] = {"error": str(exc)[:200]}
     out["projected_s_16777216_events_fp32"] = 16777216 / out["fp32"]["events_per_s"]
     return out
+
+
+def e2e_dropin(geom, cond, n_events, seed=11, first_event=7_000_000, precision="fp32", reps=3):
+    """The reference-facing call sequence on host tables, as a reference user makes it through the drop-in entry
+    points (chain.charges -> chain.digis -> chain.reco_waveforms -> chain.clusters: host step table in, host arrays
+    between the stages, host cluster table out).  Wall-clock events/s, median of `reps` passes after a warm-up."""
+    import torch
+    from crvgpu import chain as CH, config as CF, geometry as GM
+    steps = GM.synthetic_steps(n_events, geom, seed=seed, first_event=first_event)
+    cfg = CF.ChainConfig(precision=precision)
+    G = GM.sector_geom(geom)
+    h2d = sum(np.asarray(steps[k]).nbytes for k in ("x", "y", "z", "t", "edep", "bar", "event", "subrun", "run"))
+
+    def once():
+        Q = CH.charges(steps, None, geom, cond, cfg, None, key=5)
+        D = CH.digis(Q, cond, cfg, None, key=5, geom=geom)
+        W = CH.reco_waveforms(D, cond)
+        cl, _ = CH.clusters(W, cond, geom, G, cfg)
+        return len(cl[0]["cl_event"]), sum(v.nbytes for v in cl[0].values())
+    once()
+    times = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ncl, d2h = once()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    dt = float(np.median(times))
+    return {"events": n_events, "events_per_s": n_events / dt, "s_per_pass": dt, "clusters": ncl,
+            "precision": precision, "h2d_bytes_per_pass": int(h2d), "d2h_bytes_per_pass": int(d2h),
+            "calls": "chain.charges -> chain.digis -> chain.reco_waveforms -> chain.clusters (host tables)"}
+
+
+def _cpu_fit_worker(args):
+    """Oracle reconstruct_full (the reference's pulse fit restated) on one length bucket of the uneven workload."""
+    length, n_wf, seed = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "mu2e-fastsim_gb300")]
+    import torch
+    from oracle import oracle as O
+    from crvgpu import config as CF
+    c = uneven_chunk(4 * n_wf, seed, "cpu")
+    n = c["n"].numpy()
+    sel = np.flatnonzero(n == length)[:n_wf]
+    off = c["off"].numpy()[sel]
+    adc = np.stack([c["adc"].numpy()[o:o + length].astype(np.int64) for o in off]) if len(sel) else \
+        np.zeros((0, length), np.int64)
+    rc = CF.RecoConfig()
+    t0 = time.perf_counter()
+    r = O.reconstruct_full(adc, n[sel], c["start"].numpy()[sel], c["ped"].numpy()[sel], c["area"].numpy()[sel],
+                           c["height"].numpy()[sel], rc, CF.PERIOD)
+    return length, len(sel), time.perf_counter() - t0, len(r["pe"])
+
+
+def cpu_fit_baseline(per_bucket=(400, 300, 200, 120, 80)):
+    """Waveforms/s of the oracle's reconstruct_full on one core per length bucket of the uneven batched-fit workload
+    (a bounded subset each), and the rate of the equal mix the workload draws (harmonic mean over the buckets)."""
+    lengths = (32, 64, 128, 256, 512)
+    out = {}
+    for L, nw in zip(lengths, per_bucket):
+        _, got, dt, npu = _cpu_fit_worker((L, nw, 77 + L))
+        out[str(L)] = {"waveforms": got, "s": dt, "waveforms_per_s": got / dt, "pulses": npu}
+    mix = len(lengths) / sum(1.0 / out[str(L)]["waveforms_per_s"] for L in lengths)
+    return {"value": mix, "unit": "waveforms/s", "cores": 1, "kind": "port",
+            "sample": "oracle reconstruct_full, " + ", ".join(f"{out[str(L)]['waveforms']} waveforms of {L}"
+                                                              for L in lengths) + " samples; equal mix",
+            "per_length": out}
+
+
+def _cpu_full_worker(args):
+    n_events, seed = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "mu2e-fastsim_gb300")]
+    from oracle import oracle as O
+    from crvgpu import config as CF
+    from crvgpu import geometry as GM
+    from crvgpu import waveform as WV
+    geom = GM.module_geometry(86)
+    cond = GM.default_conditions(geom)
+    cfg = CF.ChainConfig()
+    G = GM.sector_geom(geom)
+    steps = GM.synthetic_steps(n_events, geom, seed=seed, mean_steps=60.0, noise_per_counter=0.5)
+    t0 = time.perf_counter()
+    Q, _ = O.charges(steps, geom, cond, cfg.response, cfg.sipm, seed, cfg.window[1])
+    wc = CF.WaveformConfig()
+    run_of = lambda keys: np.ones(len(np.asarray(keys).ravel()), np.int64)  # noqa: E731
+    tdc0 = lambda labels: O.tdc0_of_labels(labels, cond, seed, wc.period, "roc_feb", run_of)  # noqa: E731
+    D = O.synthesize(Q["chan"], Q["time"], Q["charge"], tdc0, WV.single_pe_template(wc), wc, wc.period, cfg.window,
+                     O.keyed_noise(seed, run_of))
+    W = O.reco_waveforms(D, cond)
+    rc = CF.RecoConfig()
+    P = O.pulses_from_waveforms(W, cond, rc, rc.period)
+    out = O.clusters_from_pulses(W, P, G, cond.status, CF.workload_finder(G.sector_names))
+    return time.perf_counter() - t0, n_events, len(out["cl_event"])
 
 
 def main():
@@ -469,7 +574,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
-    ap.add_argument("--fullscale-events", type=int, default=4096, help="events of the full-scale measurement (0: skip)")
+    ap.add_argument("--fullscale-events", type=int, default=32768,
+                    help="events of the full-scale measurement, resident FP32 leg (0: skip)")
+    ap.add_argument("--fullscale-stage-events", type=int, default=4096,
+                    help="events of the full-scale per-stage FP32 and FP64 legs")
+    ap.add_argument("--dropin-events", type=int, default=16384,
+                    help="events of the drop-in (host tables through the stage entry points) end-to-end leg (0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
     ap.add_argument("--serve-load", type=float, default=0.8)
     ap.add_argument("--lookup-rows", type=int, default=1 << 20,
@@ -684,7 +794,7 @@ def main():
     #   k_coinc:    per hit 28 B in (bar, SiPM, sequence, time, PE) + per event 20 B in (first hit, count, key)
     #               + per cluster 120 B out (event, type, PE, start, end, slope, average time, position, flags) + 4 B
     #               per member index
-    groups = {"pulse fit": ("k_pf_begin", "k_pf_round"), "k_wf_synth": ("k_wf_synth", "k_wf_synth32"), "k_coinc": ("k_coinc", "k_coinc_global"),
+    groups = {"pulse fit": ("k_pf_begin", "k_pf_round", "k_pf_persist"), "k_wf_synth": ("k_wf_synth", "k_wf_synth32"), "k_coinc": ("k_coinc", "k_coinc_global"),
               "k_sipm_sim": ("k_sipm_sim",)}
 
     def alg_bytes(group):
@@ -752,9 +862,22 @@ def main():
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
 
+    dropin = None
+    if rank == 0 and args.dropin_events > 0:
+        try:
+            dropin = e2e_dropin(geom, cond, args.dropin_events)
+        except Exception as exc:                          # shown, not hidden
+            dropin = {"error": str(exc)[:300]}
+        torch.cuda.empty_cache()
+
     uneven = None
     if rank == 0 and args.uneven_waveforms > 0:
         uneven = uneven_pulse_fit(args.uneven_waveforms, 1 << 19)
+        if not args.no_cpu:
+            try:
+                uneven["cpu_baseline"] = cpu_fit_baseline()
+            except Exception as exc:                      # reported baseline only
+                uneven["cpu_baseline"] = {"error": str(exc)[:200]}
         torch.cuda.empty_cache()
 
     lookup = None
@@ -771,7 +894,7 @@ def main():
 
     full = None
     if rank == 0 and args.fullscale_events > 0:
-        full = fullscale(args.fullscale_events, 1024)
+        full = fullscale(args.fullscale_events, 1024, stage_events=args.fullscale_stage_events)
         torch.cuda.empty_cache()
 
     serve = None
@@ -794,6 +917,7 @@ def main():
                 "fp32_over_fp64": (value / fp64) if fp64 else None,
                 "fp32_vs_fp64": acc,
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "e2e_dropin": dropin,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}

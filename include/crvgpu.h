@@ -311,10 +311,11 @@ int crv_pulses(const CrvParams *p, int64_t nw, int64_t nsamples, const int64_t *
                CrvStatus *status_dev);
 
 /*
- * Launch shape of the pulse-fit rounds for later crv_pulses calls of this process (no counterpart in the reference;
- * chosen per size bucket by the host's autotuner): threads per block 64 or 128, blocks per SM 1..32, round
- * launches before the tail launch 1..32.  Results do not depend on the shape.  Returns CRV_ERR_ARG outside those
- * ranges.  Default 128 / 16 / 16.
+ * Launch shape of the pulse fit for later crv_pulses calls of this process (no counterpart in the reference; chosen
+ * per size bucket by the host's autotuner): threads per block 64 or 128, blocks per SM 1..32, and rounds: 0 = one
+ * persistent launch whose lanes claim waveforms from a device head as they finish (the default), 1..32 = that many
+ * round launches over a task list before a tail launch.  Results do not depend on the shape.  Returns CRV_ERR_ARG
+ * outside those ranges.  Default 128 / 16 / 0.
  */
 int crv_pulses_shape(int32_t threads, int32_t blocks_per_sm, int32_t rounds);
 

@@ -62,33 +62,38 @@ class PulseEngine:
         raise RuntimeError("crv_pulses: capacities did not converge")
 
 
-DEFAULT_SHAPE = (128, 16, 16)          # threads per block, blocks per SM, round launches before the tail
+DEFAULT_SHAPE = (128, 16, 0)           # threads per block, blocks per SM, rounds (0: one persistent launch)
 
 
 def set_shape(shape):
-    """Launch shape of the fit rounds for later calls (threads 64 or 128, blocks per SM 1..32, rounds 1..32)."""
+    """Launch shape of the pulse fit for later calls: threads 64 or 128, blocks per SM 1..32, and rounds (0: one
+    persistent launch whose lanes claim waveforms as they finish; 1..32: round launches before a tail launch)."""
     _capi.check(_capi.load().crv_pulses_shape(*[int(v) for v in shape]), "crv_pulses_shape")
 
 
-SHAPES = tuple((t, b, r) for t in (64, 128) for b in (8, 16, 32) for r in (8, 16))
+SHAPES = tuple((t, b, 0) for t in (64, 128) for b in (4, 8, 16, 32)) + ((128, 16, 8), (128, 16, 16))
 
 
 class ShapeTuner:
-    """Picks the launch shape of the fit rounds per size bucket (waveforms rounded up to a power of two) by timing
-    every candidate once on the first batch of that bucket; results do not depend on the shape."""
+    """Picks the launch shape of the pulse fit per size bucket by timing every candidate once on the first batch of
+    that bucket; results do not depend on the shape.  A bucket is (waveform count rounded up to a power of two,
+    longest waveform rounded up to a power of two): the count sets how many lanes the launch can fill, the length how
+    long a lane's waveform keeps it (pulses per waveform and the peak searches grow with it)."""
 
     def __init__(self, shapes=SHAPES):
         self.shapes = tuple(shapes)
         self.best = {}                 # bucket -> (shape, {shape: ms})
 
     @staticmethod
-    def bucket(nw):
-        return max(0, int(nw - 1).bit_length())
+    def bucket(nw, max_len=0):
+        return (max(0, int(nw - 1).bit_length()), max(0, int(max_len - 1).bit_length()))
 
-    def shape_for(self, eng, P, batch):
+    def shape_for(self, eng, P, batch, max_len=None):
         """Shape for this batch's bucket, tuning it first when unseen; batch = the keyword arguments of eng.run."""
         torch = _torch()
-        b = self.bucket(int(batch["n"].numel()))
+        if max_len is None:
+            max_len = int(batch["n"].max().item()) if batch["n"].numel() else 0
+        b = self.bucket(int(batch["n"].numel()), max_len)
         if b not in self.best:
             times = {}
             for sh in self.shapes:

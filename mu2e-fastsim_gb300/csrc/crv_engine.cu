@@ -825,7 +825,7 @@ constexpr int kPulseRoundsMax = 32;
 
 // launch shape of the fit rounds for later crv_pulses calls of this process (crv_pulses_shape)
 struct PulseShape {
-  std::atomic<int> threads{128}, blocks_per_sm{16}, rounds{16};
+  std::atomic<int> threads{128}, blocks_per_sm{16}, rounds{0};
 };
 static PulseShape g_pulse_shape;
 
@@ -892,7 +892,7 @@ __global__ void k_pulse_compact(long long nw, const long long* __restrict__ nw_d
 }  // namespace crv
 
 extern "C" int crv_pulses_shape(int32_t threads, int32_t blocks_per_sm, int32_t rounds) {
-  if ((threads != 64 && threads != 128) || blocks_per_sm < 1 || blocks_per_sm > 32 || rounds < 1 ||
+  if ((threads != 64 && threads != 128) || blocks_per_sm < 1 || blocks_per_sm > 32 || rounds < 0 ||
       rounds > kPulseRoundsMax)
     return CRV_ERR_ARG;
   g_pulse_shape.threads.store(threads);

@@ -815,4 +815,53 @@ __global__ void __launch_bounds__(128) k_pf_round(CrvParams p, WaveIn W, double*
   }
 }
 
+// One launch for every pulse of a batch.  Each lane holds one waveform and runs its rounds (fit, record, subtract,
+// next peak) back to back; a lane whose waveform is finished takes the next unclaimed waveform of the batch (one
+// warp-aggregated atomicAdd on a device head per refill), so lanes stay busy until every waveform has been claimed.
+// Nothing waits on anything: a warp exits once the waveforms are all claimed and its own lanes are done.  A
+// waveform's results depend only on the waveform, so the order of claims does not matter (same outputs as the round
+// kernels).  The head is Q.counts[0], zeroed before the launch.
+template <typename R>
+__global__ void __launch_bounds__(128) k_pf_persist(CrvParams p, WaveIn W, double* __restrict__ yscr, int max_pulses,
+                                                    PulseSlots S, PfQueue Q, Status* status) {
+  const long long nw = bounded_count(W.nw, W.nw_dev);
+  unsigned long long* head = reinterpret_cast<unsigned long long*>(&Q.counts[0]);
+  const int lane = lane_id();
+  long long w = -1;
+  PfState st;
+  bool pend = false;
+  bool exhausted = nw <= 0;
+  while (true) {
+    // refill the lanes without a pending pulse (a waveform without any pulse frees its lane again at once)
+    while (!exhausted) {
+      const unsigned need = __ballot_sync(0xffffffffu, !pend);
+      if (!need) break;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(head, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      exhausted = (long long)(base + __popc(need)) >= nw;
+      if (!pend) {
+        const long long c = (long long)base + __popc(need & ((1u << lane) - 1u));
+        if (c < nw) {
+          w = c;
+          if (!(wave_in_bounds(W.off[w], W.n[w], W.nsamples) && S.off[w] >= 0 && S.cap[w] >= 0 &&
+                S.off[w] + S.cap[w] <= S.rc)) {
+            set_flag(status, CRV_ST_BOUNDS);
+            S.count[w] = 0;
+            S.near[w] = 0;
+          } else {
+            pend = pf_begin<R>(p, W, yscr, max_pulses, w, st);
+            if (!pend) pf_finish(S, status, w, st);
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, pend)) break;
+    if (pend) {
+      pend = pf_step<R>(p, W, yscr, max_pulses, S, w, st);
+      if (!pend) pf_finish(S, status, w, st);
+    }
+  }
+}
+
 }  // namespace crv

@@ -52,24 +52,35 @@ def uneven_waveforms(rng, W=120, period=12.55, area=400.0):
 FIT_KEYS = ("pe", "peph", "time", "height", "beta", "chi2", "letime", "ped", "fit_A", "fit_mu", "fit_b")
 
 
-def _perturbed_exp(mode):
+def _perturbed_exp(mode, ulps=1):
+    """np.exp moved by `ulps` ulps: all up, all down, or up / down by a hash of the value (two hash variants)."""
     def f(x, *a, **k):
         v = np.exp(x)
-        if mode == "up":
-            return np.nextafter(v, np.inf)
-        if mode == "down":
-            return np.nextafter(v, -np.inf)
-        bits = np.asarray(v).view(np.uint64)
-        up = ((bits * np.uint64(0x9E3779B97F4A7C15)) >> np.uint64(63)).astype(bool)
-        return np.where(up, np.nextafter(v, np.inf), np.nextafter(v, -np.inf))
+        up = np.full(np.shape(v), mode == "up")
+        if mode.startswith("hash"):
+            mult = np.uint64(0x9E3779B97F4A7C15 if mode == "hash" else 0xC2B2AE3D27D4EB4F)
+            up = ((np.asarray(v).view(np.uint64) * mult) >> np.uint64(63)).astype(bool)
+        for _ in range(ulps):
+            v = np.where(up, np.nextafter(v, np.inf), np.nextafter(v, -np.inf))
+        return v
     return f
+
+
+def _perturbed_solve(a, b):
+    """np.linalg.solve with the matrix moved by one ulp per element (up / down by a hash of its bits): another
+    rounding of the same normal equations, as a different elimination order or a fused multiply-add gives."""
+    a = np.asarray(a, float)
+    up = ((a.view(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) >> np.uint64(63)).astype(bool)
+    return np.linalg.solve(np.where(up, np.nextafter(a, np.inf), np.nextafter(a, -np.inf)), b)
 
 
 def fit_sensitivity(args, cfg, period, full, ref=None):
     """Per-pulse relative movement of the oracle's pulse fit (the reference's LM schedule, pulsefit.py:125-216) under
-    changes that leave the mathematics unchanged: every exp of the fit model one ulp up, one ulp down, or up/down by a
-    hash of its value, and the fit points summed in reverse order.  These are the differences between NumPy's and
-    CUDA's exp (each within about one ulp) and between two reduction orders.  Returns ({key: per-pulse max relative
+    changes that leave the mathematics unchanged: every exp of the fit model one ulp up, one ulp down, or one or two
+    ulps up / down by a hash of its value (two hashes); the fit points summed in reverse order; the normal-equation
+    matrix moved by one ulp per element before the solve.  These are the differences between NumPy's and CUDA's exp
+    (each within about one ulp of the true value, so up to two apart), between two reduction orders and between two
+    roundings of the 3x3 solve (LAPACK's elimination with fused multiply-adds against an unfused one).  Returns ({key: per-pulse max relative
     movement}, the unperturbed oracle result); ref (the reference's own outputs) adds |oracle - ref| as one more
     sample, so a platform whose NumPy exp differs from the fixture generator's is covered too.  Perturbations that
     change the pulse list or a failure flag are left out (none do on the committed fixtures)."""
@@ -88,12 +99,18 @@ def fit_sensitivity(args, cfg, period, full, ref=None):
     base = call()
     sens = {k: np.zeros(len(base["pe"])) for k in FIT_KEYS}
     variants = []
-    for mode in ("up", "down", "hash", "reverse"):
+    modes = [("up", 1), ("down", 1), ("hash", 1), ("hash2", 1), ("hash", 2), ("hash2", 2), ("reverse", 0),
+             ("solve", 0)]
+    for mode, ulps in modes:
+        fake = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("__")})
         if mode == "reverse":
             O.fit_gumbel = reverse
         else:
-            fake = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("__")})
-            fake.exp = _perturbed_exp(mode)
+            if mode == "solve":
+                fake.linalg = types.SimpleNamespace(solve=_perturbed_solve, eigvalsh=np.linalg.eigvalsh,
+                                                    LinAlgError=np.linalg.LinAlgError)
+            else:
+                fake.exp = _perturbed_exp(mode, ulps)
             O.fit_gumbel = types.FunctionType(fit0.__code__, {**fit0.__globals__, "np": fake}, "fit_gumbel",
                                               fit0.__defaults__)
         try:

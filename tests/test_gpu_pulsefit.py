@@ -153,13 +153,15 @@ def test_waveform_outside_the_sample_array_is_skipped_and_reported():
         st.reset()
         ws = torch.empty(lib.crv_pulses_workspace(ctypes.byref(P), W, W * L), dtype=torch.uint8, device="cuda")
         O = _capi.CrvPulses(*[_capi.ptr(out[k]) for k in _capi.PULSE_INT + _capi.PULSE_FLOAT + _capi.PULSE_BOOL])
-        o_d, n_d = d(off_, np.int64), d(n_, np.int32)
-        rc = lib.crv_pulses(ctypes.byref(P), W, W * L, _capi.ptr(o_d), _capi.ptr(n_d), _capi.ptr(d(start, np.int64)),
-                            _capi.ptr(d(ped, np.float64)), _capi.ptr(d(area, np.float64)),
-                            _capi.ptr(d(height, np.float64)), _capi.ptr(d(adc, np.int16)), None, 64, ctypes.byref(O),
-                            cap, _capi.ptr(n_out), _capi.ptr(near), _capi.ptr(ws), ws.numel(),
-                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), st.ptr)
+        # every input tensor stays referenced until the call has finished on the device
+        x = dict(off=d(off_, np.int64), n=d(n_, np.int32), start=d(start, np.int64), ped=d(ped, np.float64),
+                 area=d(area, np.float64), height=d(height, np.float64), adc=d(adc, np.int16))
+        rc = lib.crv_pulses(ctypes.byref(P), W, W * L, _capi.ptr(x["off"]), _capi.ptr(x["n"]), _capi.ptr(x["start"]),
+                            _capi.ptr(x["ped"]), _capi.ptr(x["area"]), _capi.ptr(x["height"]), _capi.ptr(x["adc"]),
+                            None, 64, ctypes.byref(O), cap, _capi.ptr(n_out), _capi.ptr(near), _capi.ptr(ws),
+                            ws.numel(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), st.ptr)
         _capi.check(rc, "crv_pulses")
+        torch.cuda.synchronize()
         flags, _ = st.read()
         m = int(n_out.item())
         return flags, {k: v[:m].cpu().numpy() for k, v in out.items()}
