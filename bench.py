@@ -846,6 +846,8 @@ def main():
         r64 = eng64.run(batches[0], 5, keep=True)
         r32 = eng32.run(batches[0], 5, keep=True)
         acc = error_table(r64, r32, eng32.wcfg.adc_conversion, eng32.wcfg.pedestal)
+        from crvgpu.accuracy import waveform_only_table
+        acc["waveform_stage_alone"] = waveform_only_table(eng32, r64, eng32.wcfg.adc_conversion, eng32.wcfg.pedestal)
         acc["sample"] = f"first batch: {batches[0].nevents} events, seed 5"
     except Exception as exc:  # the report is informative; its failure is shown, not hidden
         acc["error"] = str(exc)[:300]

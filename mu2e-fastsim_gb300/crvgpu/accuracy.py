@@ -108,6 +108,55 @@ def changed_labels(l64, t64, q64, l32, t32, q32, t_tol=0.01, pe_rtol=1e-3):
     return np.unique(np.concatenate(changed)).astype(np.int64)
 
 
+def digi_table(D64, D32, adc_conversion, adc_pedestal, changed=None):
+    """Digis of two runs matched by (label, start TDC): ADC mismatch rate, and for the digis of SiPMs whose charges
+    agree (labels not in `changed`) the fraction of mismatches at a quantisation boundary (one count apart, with the
+    integer between the two values closer to the FP64 value than the FP32-vs-FP64 difference), the largest |dADC| and
+    |dV| quantiles.  Charges that agree to 0.01 ns still differ by the SiPM stage's FP32 rounding (~1e-4 ns at 1 us):
+    on the steep rise of the single-PE template that moves a charge across a 0.5 ns template step now and then, a
+    real difference of the input the digitisation then reproduces exactly."""
+    changed = np.zeros(0, np.int64) if changed is None else changed
+    k64 = D64["chan"].astype(np.int64) * (1 << 24) + (D64["starttdc"].astype(np.int64) + (1 << 23))
+    k32 = D32["chan"].astype(np.int64) * (1 << 24) + (D32["starttdc"].astype(np.int64) + (1 << 23))
+    com, i64, i32 = np.intersect1d(k64, k32, assume_unique=False, return_indices=True)
+    a64, a32 = D64["adc"][i64].astype(np.int64), D32["adc"][i32].astype(np.int64)
+    v64, v32 = D64["volt"][i64], D32["volt"][i32]
+    same_in = ~np.isin(D64["chan"][i64], changed)
+    mis = a64 != a32
+    x64 = v64 * adc_conversion + adc_pedestal + 0.5
+    x32 = v32 * adc_conversion + adc_pedestal + 0.5
+    edge = np.maximum(np.floor(x64), np.floor(x32))
+    at_boundary = (np.abs(a64 - a32) == 1) & (np.abs(x64 - edge) <= np.abs(x32 - x64) + 1e-9)
+    ms, mc = mis[same_in], mis[~same_in]
+    dv = np.abs(v32 - v64)
+    return {"fp64": int(len(k64)), "fp32": int(len(k32)), "matched": int(len(com)),
+            "matched_frac": float(len(com) / max(len(k64), 1)),
+            "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(mis.sum() / max(a64.size, 1)),
+            "adc_mismatch_at_boundary_frac": float(at_boundary[mis].mean()) if mis.any() else 1.0,
+            "adc_mismatch_max_abs": int(np.abs(a64 - a32).max()) if a64.size else 0,
+            "same_charges": {
+                "adc_samples": int(ms.size), "adc_mismatch_rate": float(ms.sum() / max(ms.size, 1)),
+                "adc_mismatch_at_boundary_frac": float(at_boundary[same_in][ms].mean()) if ms.any() else 1.0,
+                "adc_mismatch_max_abs": int(np.abs(a64 - a32)[same_in].max()) if ms.size else 0,
+                "volt_abs_err_mV_p50_p99_max": [None if v is None else 1e3 * v for v in _q(dv[same_in].ravel())]},
+            "different_charges": {
+                "adc_samples": int(mc.size), "adc_mismatch_rate": float(mc.sum() / max(mc.size, 1)),
+                "adc_mismatch_max_abs": int(np.abs(a64 - a32)[~same_in].max()) if mc.size else 0}}
+
+
+def waveform_only_table(eng32, r64, adc_conversion, adc_pedestal):
+    """The FP32-mixed waveform stage alone: it digitises the FP64 run's own charges, so the inputs are identical and
+    every ADC difference is the waveform arithmetic's."""
+    R = r64.charges
+    D = eng32.dig.run(eng32.params(r64.seed), eng32.tabs, R.label, R.time, R.charge, eng32.tmpl, r64.ev_keys,
+                      r64.ev_runs)
+    D64 = {k: _np(v) for k, v in r64.digis.items()}
+    D32 = {k: _np(v) for k, v in D.items()}
+    t = digi_table(D64, D32, adc_conversion, adc_pedestal)
+    return {k: t[k] for k in ("fp64", "fp32", "matched_frac", "adc_samples_compared", "adc_mismatch_rate",
+                              "adc_mismatch_at_boundary_frac", "adc_mismatch_max_abs")}
+
+
 def error_table(r64, r32, adc_conversion, adc_pedestal):
     """FP32-mixed vs FP64 report of two ChainResults of the same batch and seed (both run with keep=True)."""
     out = {}
@@ -126,33 +175,7 @@ def error_table(r64, r32, adc_conversion, adc_pedestal):
     # ---- digis by (label, start TDC); ADC mismatches split by whether the SiPM's charges agree
     D64 = {k: _np(v) for k, v in r64.digis.items()}
     D32 = {k: _np(v) for k, v in r32.digis.items()}
-    k64 = D64["chan"].astype(np.int64) * (1 << 24) + (D64["starttdc"].astype(np.int64) + (1 << 23))
-    k32 = D32["chan"].astype(np.int64) * (1 << 24) + (D32["starttdc"].astype(np.int64) + (1 << 23))
-    com, i64, i32 = np.intersect1d(k64, k32, assume_unique=False, return_indices=True)
-    a64, a32 = D64["adc"][i64].astype(np.int64), D32["adc"][i32].astype(np.int64)
-    v64, v32 = D64["volt"][i64], D32["volt"][i32]
-    same_in = ~np.isin(D64["chan"][i64], changed)
-    mis = a64 != a32
-    x64 = v64 * adc_conversion + adc_pedestal + 0.5
-    x32 = v32 * adc_conversion + adc_pedestal + 0.5
-    # a flip at a quantisation boundary: one count apart, with the integer between the two values closer to the FP64
-    # value than the FP32-vs-FP64 difference itself (so rounding of a near-integer value explains it)
-    edge = np.maximum(np.floor(x64), np.floor(x32))
-    at_boundary = (np.abs(a64 - a32) == 1) & (np.abs(x64 - edge) <= np.abs(x32 - x64) + 1e-9)
-    ms, mc = mis[same_in], mis[~same_in]
-    dv = np.abs(v32 - v64)
-    out["digis"] = {"fp64": int(len(k64)), "fp32": int(len(k32)), "matched": int(len(com)),
-                    "matched_frac": float(len(com) / max(len(k64), 1)),
-                    "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(mis.sum() / max(a64.size, 1)),
-                    "same_charges": {
-                        "adc_samples": int(ms.size), "adc_mismatch_rate": float(ms.sum() / max(ms.size, 1)),
-                        "adc_mismatch_at_boundary_frac": float(at_boundary[same_in][ms].mean()) if ms.any() else 1.0,
-                        "adc_mismatch_max_abs": int(np.abs(a64 - a32)[same_in].max()) if ms.size else 0,
-                        "volt_abs_err_mV_p50_p99_max": [None if v is None else 1e3 * v
-                                                        for v in _q(dv[same_in].ravel())]},
-                    "different_charges": {
-                        "adc_samples": int(mc.size), "adc_mismatch_rate": float(mc.sum() / max(mc.size, 1)),
-                        "adc_mismatch_max_abs": int(np.abs(a64 - a32)[~same_in].max()) if mc.size else 0}}
+    out["digis"] = digi_table(D64, D32, adc_conversion, adc_pedestal, changed)
     # ---- pulses by (SiPM label, nearest time)
     W64 = {k: _np(v) for k, v in r64.waveforms.items()}
     W32 = {k: _np(v) for k, v in r32.waveforms.items()}

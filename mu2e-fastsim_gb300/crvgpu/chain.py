@@ -141,6 +141,9 @@ class ChainResult:
     n_photons: int = 0
     n_sipms: int = 0
     charges: object = None
+    seed: int = 0
+    ev_keys: object = None
+    ev_runs: object = None
     digis: dict = None
     waveforms: dict = None
     pulses: dict = None
@@ -270,4 +273,5 @@ class ChainEngine:
                           R.nsipm if diagnostics else 0)
         if keep:
             res.charges, res.digis, res.waveforms, res.pulses, res.hits = R, D, W, Pu, H
+            res.seed, res.ev_keys, res.ev_runs = seed, evk, ds.ev_run
         return res

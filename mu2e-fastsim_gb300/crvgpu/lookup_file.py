@@ -31,15 +31,18 @@ def lookup_dir():
 
 @dataclass
 class Table:
-    prob: np.ndarray        # [N] float32 arrival probability at SiPM 0
-    delays: np.ndarray      # [N, Dmax] uint8 weights
-    delay_sum: np.ndarray   # [N] int32
-    emis: np.ndarray        # [N, Emax] uint8 weights
-    emis_sum: np.ndarray    # [N] int32
+    """One of a file's three tables, one row per table bin (field names as the reference's decoded table)."""
+    prob: np.ndarray        # float32 per bin: chance that a photon made in the bin reaches the first SiPM
+    delays: np.ndarray      # uint8, bins x longest delay vector: arrival-delay histogram (1 ns bins), zero padded
+    delay_sum: np.ndarray   # int32 per bin: total of the bin's delay weights
+    emis: np.ndarray        # uint8, bins x longest emission vector: fibre re-emission count histogram, zero padded
+    emis_sum: np.ndarray    # int32 per bin: total of the bin's emission weights
 
 
 @dataclass
 class LookupTable:
+    """A decoded version-6 table file: the counter and fibre geometry, the Cherenkov yield curves, the bin edges of
+    every table axis and the three tables (field names as the reference's decoded object)."""
     name: str
     version: tuple
     reflector: int
@@ -53,10 +56,10 @@ class LookupTable:
     corner_radius: float
     birks: float
     fiber_decay_time: float
-    ck_scint: np.ndarray    # [n, 2] (beta, photons per mm)
-    ck_fiber: np.ndarray
-    edges: dict             # x, y, z, beta, theta, phi, r -> float64 arrays
-    tables: dict            # scint, ckscint, ckfiber -> Table
+    ck_scint: np.ndarray    # Cherenkov yield in the scintillator: rows of (beta, photons per mm)
+    ck_fiber: np.ndarray    # the same in the fibre
+    edges: dict             # axis name (x, y, z, beta, theta, phi, r) -> float64 bin edges
+    tables: dict            # table name (scint, ckscint, ckfiber) -> Table
 
 
 def _error(info, where):

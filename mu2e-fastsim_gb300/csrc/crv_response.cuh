@@ -254,6 +254,32 @@ __global__ void k_sipm_sizes(const long long* __restrict__ nsipm_dev, const int3
 
 #endif  // CRV_ENGINE_TU
 
+// Emission delays, in decay times, of photons c0 + lane of a row of n photons (c0 a multiple of 32; every lane of the
+// warp calls it): the order statistics of n exponential delays by the Renyi representation, S_j = sum_{i <= j} X_i /
+// (n - i) with X_i = -log u_i and u_i photon i's keyed uniform.  The delays have the distribution of n independent
+// exponential delays; photon j (key j) takes the j-th smallest, so every row's photons come out in time order.  Sums:
+// an inclusive Hillis-Steele scan over the chunk's lanes (offsets 1, 2, 4, 8, 16), the earlier chunks' total (*carry,
+// updated) in front; the CPU oracle adds in the same order, so FP64 sums are identical.
+template <typename R>
+__device__ __forceinline__ R row_delay_chunk(uint32_t seed, const EvKey& ek, uint32_t chan, uint32_t sie, int n, int c0,
+                                             R* carry) {
+  using M = Math<R>;
+  const int j = c0 + lane_id();
+  R v = R(0);
+  if (j < n) {
+    U4 w = keyed(seed, ek, w2_of(ST_PHOTON, 0, 0, 0, chan), (sie << 16) | uint32_t(j >> 1));
+    v = (-M::log(M::uni_open(w, j & 1))) / R(n - j);
+  }
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const R y = __shfl_up_sync(0xffffffffu, v, off);
+    if (lane_id() >= off) v = v + y;
+  }
+  const R S = *carry + v;
+  *carry = *carry + __shfl_sync(0xffffffffu, v, 31);
+  return S;
+}
+
 // photons of each SiPM, contiguous from ph_off[g]: (time, key = step-in-event << 16 | photon)
 template <typename R>
 __global__ void k_photon_emit(CrvParams p, CrvEvents ev, CrvSteps st, CrvBars bars, long long nsipm,
@@ -262,7 +288,6 @@ __global__ void k_photon_emit(CrvParams p, CrvEvents ev, CrvSteps st, CrvBars ba
                               const int32_t* __restrict__ step_order, const int32_t* __restrict__ count,
                               const long long* __restrict__ ph_off, R* __restrict__ ph_t,
                               uint32_t* __restrict__ ph_key) {
-  using M = Math<R>;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < nsipm; g += warps) {
     int c = s_chan[g], s = c & 3, e = s_event[g];
@@ -280,11 +305,14 @@ __global__ void k_photon_emit(CrvParams p, CrvEvents ev, CrvSteps st, CrvBars ba
       R d = readout_distance(R(z), R(bars.half_l[b]), s);
       R t = R(step_real(st, st.t, i));
       R dt = d / R(p.signal_speed);
-      for (int j = lane_id(); j < n; j += 32) {
-        U4 w = keyed(p.seed, ek, w2_of(ST_PHOTON, 0, 0, 0, uint32_t(c)), (sie << 16) | uint32_t(j >> 1));
-        R u = M::uni_open(w, j & 1);
-        ph_t[o + j] = t + dt + R(p.decay_time) * (-M::log(u));
-        ph_key[o + j] = (sie << 16) | uint32_t(j);
+      R carry = R(0);
+      for (int c0 = 0; c0 < n; c0 += 32) {
+        const R S = row_delay_chunk<R>(p.seed, ek, uint32_t(c), sie, n, c0, &carry);
+        const int j = c0 + lane_id();
+        if (j < n) {
+          ph_t[o + j] = t + dt + R(p.decay_time) * S;
+          ph_key[o + j] = (sie << 16) | uint32_t(j);
+        }
       }
       o += n;
     }
@@ -629,14 +657,6 @@ __device__ void run_cascade(const CrvParams& p, const SipmK<R>& K, const SipmSha
 }
 
 // Serial-semantics simulation of one SiPM whose sorted photons (n <= cap) sit in S.ph_*.
-//
-// 32 photons at a time.  Everything a photon draws is keyed by the photon, not by the state, so its pixel, its fire
-// uniform and its cross-talk candidates are computed once.  Only the recovered overvoltage and the fire decision
-// depend on the state; they are re-evaluated for the photons still pending at every commit step, which commits the
-// longest prefix whose outcome cannot depend on an earlier pending photon: up to (not including) the first photon
-// whose pixel an earlier pending photon shares, and up to (including) the first firing photon with cross-talk
-// candidates, whose cascade then runs before the rest.  Charges, traps and cascades therefore come out in photon
-// order, exactly as the one-at-a-time loop of the reference.
 template <typename R>
 __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPixels& px, const SipmShared<R>& S,
                               const uint32_t* dead, SipmCtx& C, const SipmOut& O, int n, const long long* photon_id,
@@ -644,68 +664,66 @@ __device__ void simulate_sipm(const CrvParams& p, const SipmK<R>& K, const CrvPi
   using M = Math<R>;
   for (int w = lane_id(); w < 64; w += 32) S.bm[w] = 0u;
   __syncwarp();
-  const int lane = lane_id();
-  for (int k = 0; k < n; k += 32) {
-    const int i = k + lane;
-    const bool has = i < n;
-    const R t = has ? S.ph_t[i] : R(0);
-    const uint32_t key = has ? S.ph_key[i] : 0u;
+  int k = 0;
+  while (k < n) {
+    int i = k + lane_id();
+    bool has = i < n;
+    R t = has ? S.ph_t[i] : R(0);
+    uint32_t key = has ? S.ph_key[i] : 0u;
     int pix = -1;
     U4 w0{0, 0, 0, 0};
     if (has) {
       w0 = keyed(p.seed, C.ek, w2_of(ST_SIPM, 0, 0, 0, C.chan), key);
       pix = draw_pixel<R>(p, px, dead, M::uni(w0, 0), w0.y);
     }
-    const bool live = pix >= 0;
-    const R ufire = M::uni(w0, 1);
-    const unsigned ct = live ? node_crosstalk<R>(p, K, C, 0, 0, key, pix) : 0u;
-    long long id = 0;
-    if (live) id = photon_id ? photon_id[gstart + S.ph_loc[i]] : id_base + (long long)(key >> 16);
-    unsigned pend = __ballot_sync(FULL, live);
-    while (pend) {
-      const bool mine = (pend >> lane) & 1u;
-      const unsigned same = __match_any_sync(FULL, mine ? pix : -1 - lane);
-      const bool blocked = mine && (same & lanemask_lt()) != 0u;
-      R v = R(0);
-      bool fire = false;
-      if (mine && !blocked) {
-        v = recovered<R>(K, S, pix, t);
-        fire = ufire < pfire_m<R>(K, v, 1);
-      }
-      const unsigned bb = __ballot_sync(FULL, blocked);
-      const unsigned bc = __ballot_sync(FULL, fire && ct != 0u);
-      const int fb = bb ? __ffs(bb) - 1 : 32;
-      const int fc = bc ? __ffs(bc) - 1 : 32;
-      const int end = fc < fb ? fc + 1 : fb;
-      const bool commit = mine && lane < end && fire;
-      const unsigned fm = __ballot_sync(FULL, commit);
-      R tt[2], uf[2];
-      int ntr = 0;
-      if (commit) {
-        put_charge<R>(O, C, __popc(fm & lanemask_lt()), t, v, id);
-        S.last[pix] = t;
-        bm_set(S.bm, pix);
-        ntr = node_traps<R>(p, K, C, 0, 0, key, t, tt, uf);
-      }
-      C.nq += __popc(fm);
-      int tot;
-      const int tpos = warp_excl(ntr, &tot);
-      for (int a = 0; a < ntr; ++a) {
-        const int kk = C.ntr + tpos + a;
-        if (kk < S.tcap) { S.tr_t[kk] = tt[a]; S.tr_uf[kk] = uf[a]; S.tr_pix[kk] = uint16_t(pix); S.tr_id[kk] = id; }
-      }
-      C.ntr += tot;
-      __syncwarp();
-      if (fc < fb) {
-        const unsigned c0 = __shfl_sync(FULL, ct, fc);
-        const int p0 = __shfl_sync(FULL, pix, fc);
-        const R tg = __shfl_sync(FULL, t, fc);
-        const uint32_t kg = __shfl_sync(FULL, key, fc);
-        const long long idg = __shfl_sync(FULL, id, fc);
-        run_cascade<R>(p, K, S, dead, C, O, c0, p0, tg, kg, idg);
-      }
-      pend &= end >= 32 ? 0u : ~((1u << end) - 1u);
+    bool live = pix >= 0;
+    unsigned same = __match_any_sync(FULL, live ? pix : -1 - lane_id());
+    bool collide = live && (same & lanemask_lt()) != 0u;
+    bool fire = false;
+    unsigned ct = 0;
+    R v = R(0);
+    if (live && !collide) {
+      v = recovered<R>(K, S, pix, t);
+      R pm = pfire_m<R>(K, v, 1);
+      fire = M::uni(w0, 1) < pm;
+      if (fire) ct = node_crosstalk<R>(p, K, C, 0, 0, key, pix);
     }
+    int nv = min(n - k, 32);
+    unsigned cm = __ballot_sync(FULL, collide);
+    unsigned sm = __ballot_sync(FULL, ct != 0u);
+    int f = cm ? __ffs(cm) - 1 : 32;
+    int g = sm ? __ffs(sm) - 1 : 32;
+    int ncommit = (g < f) ? g + 1 : min(f, nv);
+    bool commit = lane_id() < ncommit && fire;
+    long long id = 0;
+    if (commit) id = photon_id ? photon_id[gstart + S.ph_loc[i]] : id_base + (long long)(key >> 16);
+    unsigned fm = __ballot_sync(FULL, commit);
+    R tt[2], uf[2];
+    int ntr = 0;
+    if (commit) {
+      put_charge<R>(O, C, __popc(fm & lanemask_lt()), t, v, id);
+      S.last[pix] = t;
+      bm_set(S.bm, pix);
+      ntr = node_traps<R>(p, K, C, 0, 0, key, t, tt, uf);
+    }
+    C.nq += __popc(fm);
+    int tot;
+    int tpos = warp_excl(ntr, &tot);
+    for (int a = 0; a < ntr; ++a) {
+      int kk = C.ntr + tpos + a;
+      if (kk < S.tcap) { S.tr_t[kk] = tt[a]; S.tr_uf[kk] = uf[a]; S.tr_pix[kk] = uint16_t(pix); S.tr_id[kk] = id; }
+    }
+    C.ntr += tot;
+    __syncwarp();
+    if (g < f) {
+      unsigned c0 = __shfl_sync(FULL, ct, g);
+      int p0 = __shfl_sync(FULL, pix, g);
+      R tg = __shfl_sync(FULL, t, g);
+      uint32_t kg = __shfl_sync(FULL, key, g);
+      long long idg = __shfl_sync(FULL, id, g);
+      run_cascade<R>(p, K, S, dead, C, O, c0, p0, tg, kg, idg);
+    }
+    k += ncommit;
   }
   if (C.ntr > S.tcap) C.limit = 1;
 }
@@ -802,71 +820,6 @@ __device__ void sort_photons(const SipmShared<R>& S, int n) {
   }
 }
 
-// Order-preserving 32-bit image of an FP32 time (-0 as +0) and its inverse.
-__device__ __forceinline__ uint32_t ord_f32(float t) {
-  uint32_t u = __float_as_uint(t);
-  if (u == 0x80000000u) u = 0u;
-  return (u >> 31) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float unord_f32(uint32_t o) { return __uint_as_float((o >> 31) ? (o & 0x7FFFFFFFu) : ~o); }
-
-constexpr int SORT_SLOTS = 8;      // register sort: up to 8 x 32 = 256 photons
-
-// Sort the staged FP32 photons by (time, key) in registers: (time, key) packed into one 64-bit word (order-preserving
-// time bits above the key; keys are unique within a SiPM), element e = slot * 32 + lane, a bitonic network whose
-// steps across lanes are shuffles and whose steps across slots stay in the lane.  The sorted photons are written back
-// to S.ph_t / S.ph_key.  n <= 256.
-__device__ __forceinline__ void sort_photons_reg(const SipmShared<float>& S, int n) {
-  const int lane = lane_id();
-  int ns = 1;
-  while (ns * 32 < n) ns <<= 1;
-  unsigned long long v[SORT_SLOTS];
-#pragma unroll
-  for (int j = 0; j < SORT_SLOTS; ++j) {
-    const int e = j * 32 + lane;
-    v[j] = e < n ? ((unsigned long long)ord_f32(S.ph_t[e]) << 32) | S.ph_key[e] : ~0ull;
-  }
-  const int P = ns * 32;
-  for (int size = 2; size <= P; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      if (stride < 32) {
-        const bool lower = (lane & stride) == 0;
-#pragma unroll
-        for (int j = 0; j < SORT_SLOTS; ++j) {
-          if (j < ns) {
-            const unsigned long long o = __shfl_xor_sync(FULL, v[j], stride);
-            const bool up = ((j * 32 + lane) & size) == 0;
-            v[j] = ((lower == up) == (v[j] < o)) ? v[j] : o;
-          }
-        }
-      } else {
-        const int js = stride >> 5;
-#pragma unroll
-        for (int j = 0; j < SORT_SLOTS; ++j) {
-#pragma unroll
-          for (int b = 1; b < SORT_SLOTS; b <<= 1) {
-            if (b == js && (j & b) == 0 && (j | b) < ns) {
-              const bool up = ((j * 32 + lane) & size) == 0;
-              const unsigned long long x = v[j], y = v[j | b];
-              if ((x > y) == up) { v[j] = y; v[j | b] = x; }
-            }
-          }
-        }
-      }
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int j = 0; j < SORT_SLOTS; ++j) {
-    const int e = j * 32 + lane;
-    if (e < n) {
-      S.ph_t[e] = unord_f32(uint32_t(v[j] >> 32));
-      S.ph_key[e] = uint32_t(v[j]);
-    }
-  }
-  __syncwarp();
-}
-
 // SiPM stage over photon groups (PT: storage type of the photon times)
 template <typename R, typename PT>
 __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, SipmGroups G,
@@ -881,11 +834,20 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
   SipmShared<R> S = carve<R>(smem + size_t(warp_in_block()) * sipm_smem_per_warp<R>(cap), cap);
   for (int q = 0; q < 2; ++q)
     if (G.guard[q] && *G.guard[q] > G.guard_cap[q]) return;
-  long long ngroups = *G.n;
-  long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ngroups; g += warps) {
-    int cnt = G.count[g];
-    if (cnt <= lo) continue;
+  const long long ngroups = *G.n;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  // groups in tiles of 32 per warp: one coalesced load of their counts and a ballot pick the groups of this pass (a
+  // later pass, which holds few groups, does not walk every group with a dependent load)
+  for (long long g0 = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; g0 < ngroups;
+       g0 += warps * 32) {
+   const long long gl = g0 + lane_id();
+   const int cl = gl < ngroups ? G.count[gl] : 0;
+   unsigned todo = __ballot_sync(FULL, gl < ngroups && cl > lo);
+   while (todo) {
+    const int bsel = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const long long g = g0 + bsel;
+    const int cnt = __shfl_sync(FULL, cl, bsel);
     long long a = G.start[g];
     long long lab = G.label[g];
     SipmCtx C;
@@ -924,12 +886,12 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
       n += __popc(km);
     }
     __syncwarp();
-    if constexpr (sizeof(R) == 4) {
-      if (!G.photon_id && n <= 32 * SORT_SLOTS) sort_photons_reg(S, n);
-      else sort_photons<R>(S, n);
-    } else {
-      sort_photons<R>(S, n);
-    }
+    // the photons of one (step, SiPM) row come out of the photon stage in (time, key) order, so a SiPM hit by one
+    // step needs no sort: check the order, sort only when it is broken
+    bool ordered = true;
+    for (int i = lane_id(); i + 1 < n; i += 32)
+      ordered = ordered && !after(S.ph_t[i], S.ph_key[i], S.ph_t[i + 1], S.ph_key[i + 1]);
+    if (!__all_sync(FULL, ordered)) sort_photons<R>(S, n);
     const long long idb = G.id_base ? G.id_base[g] : 0;
     simulate_sipm<R>(p, K, px, S, dead, C, O, n, G.photon_id, a, idb);
     int nap = run_afterpulses<R>(K, S, C, O);
@@ -948,6 +910,7 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
       if (C.limit) set_flag(status, CRV_ST_LIMIT);
     }
     __syncwarp();
+   }
   }
 }
 

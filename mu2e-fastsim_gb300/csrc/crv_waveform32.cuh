@@ -63,15 +63,16 @@ __device__ __forceinline__ double fx2d(long long v) {
   return __longlong_as_double((long long)((e << 52) | (m & 0xFFFFFFFFFFFFFull) | (v < 0 ? (1ull << 63) : 0ull)));
 }
 
-// ceil(x / d) and floor(x / d) for d > 0 on fixed-point values: FP32 estimate, exact integer correction
+// ceil(x / d) and floor(x / d) for d > 0 on fixed-point values whose quotient is below 2^30 in magnitude: FP32
+// estimate (a 32-bit conversion: the 64-bit one issues at a small fraction of the rate), exact integer correction
 __device__ __forceinline__ long long fx_ceil_div(long long x, long long d, float inv_d) {
-  long long k = (long long)ceilf(fx2f(x) * inv_d);
+  long long k = (long long)(int)ceilf(fminf(fmaxf(fx2f(x) * inv_d, -1073741824.0f), 1073741824.0f));
   while (k * d < x) ++k;
   while ((k - 1) * d >= x) --k;
   return k;
 }
 __device__ __forceinline__ long long fx_floor_div(long long x, long long d, float inv_d) {
-  long long k = (long long)floorf(fx2f(x) * inv_d);
+  long long k = (long long)(int)floorf(fminf(fmaxf(fx2f(x) * inv_d, -1073741824.0f), 1073741824.0f));
   while (k * d > x) --k;
   while ((k + 1) * d <= x) ++k;
   return k;
@@ -276,9 +277,16 @@ __global__ void __launch_bounds__(256) k_wf_synth32(CrvParams p, WfGroups G, con
   const float conv_f = float(p.adc_conversion), off_f = float(double(p.adc_pedestal) + 0.5);
   const long long ng = *G.n;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ng; g += warps) {
-    const int ml = g_maxlen[g];
-    if (ml <= lo) continue;
+  // groups in tiles of 32 per warp: one coalesced load of their longest clusters and a ballot pick this pass's groups
+  for (long long g0 = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; g0 < ng; g0 += warps * 32) {
+   const long long gl = g0 + lane;
+   const int mll = gl < ng ? g_maxlen[gl] : 0;
+   unsigned todo = __ballot_sync(0xffffffffu, gl < ng && mll > lo);
+   while (todo) {
+    const int bsel = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const long long g = g0 + bsel;
+    const int ml = __shfl_sync(0xffffffffu, mll, bsel);
     if (ml > cap) {
       if (last_pass && lane == 0) {
         set_flag(status, CRV_ST_CAPACITY);
@@ -402,6 +410,7 @@ __global__ void __launch_bounds__(256) k_wf_synth32(CrvParams p, WfGroups G, con
       D.n[g] = nd;
       if (nd > scap) set_flag(status, CRV_ST_CAPACITY);
     }
+   }
   }
 }
 

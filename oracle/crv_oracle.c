@@ -300,36 +300,66 @@ void orc_photon_counts(const OrcParams *P, int64_t nsteps, const int32_t *bar, c
     }
 }
 
-/* Arrival time of photon j of a row. */
-static inline double photon_time(const OrcParams *P, double t, double d, uint32_t seed, uint32_t run, uint32_t ev,
-                                 uint32_t sub, int chan, int32_t sie, int64_t j) {
-    uint32_t w[4];
-    keyed(seed, run, ev, sub, w2_of(ST_PHOTON, 0, 0, 0, chan), ((uint32_t)sie << 16) | (uint32_t)(j >> 1), w);
-    int h = (int)(j & 1) * 2;
-    double u = u01_open(w[h], w[h + 1]);
-    return t + d / P->signal_speed + P->decay_time * (-orc_log(u));
+/* Emission delays of a row's n photons in increasing order, in units of the decay time: the order statistics of n
+ * exponential delays by the Renyi representation, S_j = sum_{i <= j} X_i / (n - i) with X_i = -log u_i and u_i photon
+ * i's keyed uniform.  The set of delays has the distribution of n independent exponential delays (the reference's
+ * model); photon j of the row (key j) takes the j-th smallest, so a row's photons come out in time order.  The sums
+ * run in the GPU's order: chunks of 32 photons, an inclusive Hillis-Steele scan inside a chunk (offsets 1, 2, 4, 8,
+ * 16), the running total of the earlier chunks added in front. */
+static void row_delays(uint32_t seed, uint32_t run, uint32_t ev, uint32_t sub, int chan, int32_t sie, int64_t n,
+                       double *S) {
+    double carry = 0.0;
+    for (int64_t c0 = 0; c0 < n; c0 += 32) {
+        double v[32], nx[32];
+        for (int l = 0; l < 32; ++l) {
+            int64_t j = c0 + l;
+            v[l] = 0.0;
+            if (j < n) {
+                uint32_t w[4];
+                keyed(seed, run, ev, sub, w2_of(ST_PHOTON, 0, 0, 0, chan), ((uint32_t)sie << 16) | (uint32_t)(j >> 1),
+                      w);
+                int h = (int)(j & 1) * 2;
+                v[l] = (-orc_log(u01_open(w[h], w[h + 1]))) / (double)(n - j);
+            }
+        }
+        for (int off = 1; off < 32; off <<= 1) {
+            for (int l = 0; l < 32; ++l) nx[l] = l >= off ? v[l] + v[l - off] : v[l];
+            memcpy(v, nx, sizeof v);
+        }
+        for (int l = 0; l < 32 && c0 + l < n; ++l) S[c0 + l] = carry + v[l];
+        carry = carry + v[31];
+    }
 }
 
 /* Emit photons for rows with precomputed counts and offsets (row order = caller's).  Per photon: step row, channel,
- * time, key = (step-in-event << 16) | j. */
+ * time = step time + distance / signal speed + decay time x S_j (row_delays), key = (step-in-event << 16) | j. */
 void orc_photon_emit(const OrcParams *P, int64_t nrows, const int64_t *row_step, const int32_t *row_s,
                      const int64_t *row_count, const int64_t *row_off, const int32_t *bar, const double *zloc,
                      const double *t, const double *half, const uint32_t *event, const uint32_t *subrun,
                      const uint32_t *run, const int32_t *sie, int64_t *o_step, int64_t *o_chan, double *o_time,
                      int64_t *o_key) {
+    double *S = NULL;
+    int64_t scap = 0;
     for (int64_t r = 0; r < nrows; ++r) {
         int64_t i = row_step[r];
         int s = row_s[r];
         int chan = bar[i] * 4 + s;
+        int64_t n = row_count[r];
+        if (n > scap) {
+            scap = n;
+            S = realloc(S, (size_t)scap * sizeof(double));
+        }
+        row_delays(P->seed, run[i], event[i], subrun[i], chan, sie[i], n, S);
         double d = readout_distance(zloc[i], half[i], s);
-        for (int64_t j = 0; j < row_count[r]; ++j) {
+        for (int64_t j = 0; j < n; ++j) {
             int64_t o = row_off[r] + j;
             o_step[o] = i;
             o_chan[o] = chan;
-            o_time[o] = photon_time(P, t[i], d, P->seed, run[i], event[i], subrun[i], chan, sie[i], j);
+            o_time[o] = t[i] + d / P->signal_speed + P->decay_time * S[j];
             o_key[o] = ((int64_t)sie[i] << 16) | j;
         }
     }
+    free(S);
 }
 
 /* ------------------------------------------------------------------------------------------------------------ */

