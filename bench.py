@@ -263,43 +263,41 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
     return out
 
 
-def serving(geom, cond, n_jobs, pool_events, load, seed=5, max_slots=2, chunk=2048, resident=True):
-    """Serving loop over a resident step pool: isolated run time model, saturated capacity, then Poisson arrivals at
-    `load` of capacity (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
+def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2048, resident=True, graph=True):
+    """Serving loop over a resident step pool: isolated run time measured per job size (each size alone on the idle
+    device), saturated capacity (a burst of every job at once), then Poisson arrivals at each of `loads` x capacity
+    (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
     import torch
     from crvgpu import geometry as GM
     from crvgpu.response import upload_steps
-    from crvgpu.serve import Job, ServeEngine, latency_stats, random_jobs
+    from crvgpu.serve import ServeEngine, latency_stats, measure_isolated, random_jobs
     pool = upload_steps(GM.synthetic_steps(pool_events, geom, seed=77), nbars=geom.nbars)
     free, _ = torch.cuda.mem_get_info()
     srv = ServeEngine(geom, cond, pool, hbm_budget=int(0.6 * free), max_slots=max_slots, chunk_events=chunk,
-                      resident=resident)
-    # isolated run time: alone on an idle device, a small and a large job
-    iso = []
-    for n in (4096, min(131072, pool_events)):
-        t0 = time.perf_counter()
-        srv.run([Job(0, n, seed=3)], realtime=False)
-        iso.append((n, time.perf_counter() - t0))
-    (n1, t1), (n2, t2) = iso
-    rate = (n2 - n1) / max(t2 - t1, 1e-9)
-    overhead = max(0.0, t1 - n1 / rate)
+                      resident=resident, graph=graph)
+    sizes = sorted({int(v) for v in np.geomspace(1000, pool_events, 7)})
+    iso = measure_isolated(srv, sizes)
     rng = np.random.default_rng(seed)
     burst = random_jobs(n_jobs, rng, max_events=pool_events, pool_events=pool_events)
-    res = srv.run(burst, realtime=False)
-    cap = latency_stats(res, rate, overhead)["events_per_s"]
+    t0 = time.perf_counter()
+    srv.run(burst, realtime=False)
+    cap = sum(j.n_events for j in burst) / (time.perf_counter() - t0)
     mean_ev = np.mean([j.n_events for j in burst])
-    jobs = random_jobs(n_jobs, np.random.default_rng(seed + 1), max_events=pool_events, pool_events=pool_events,
-                       rate=load * cap / mean_ev)
-    st = latency_stats(srv.run(jobs, realtime=True), rate, overhead)
-    st_edf = latency_stats(srv.run(jobs, realtime=True, policy="edf", iso_rate=rate, iso_overhead=overhead), rate,
-                           overhead)
-    return {"jobs": n_jobs, "slots": len(srv.slots), "slot_footprint_gb": srv.footprint / 1e9,
-            "slot_engine": "resident chain (one host read per chunk)" if resident else "per-stage chain",
-            "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",
-            "isolated_events_per_s": rate, "isolated_overhead_s": overhead, "capacity_events_per_s": cap,
-            "offered_load": load, "policy": "srpt", **{k: v for k, v in st.items() if k != "jobs"},
-            "edf": {"policy": "earliest deadline, arrival + 2 x isolated time",
-                    **{k: v for k, v in st_edf.items() if k != "jobs"}}}
+    out = {"jobs": n_jobs, "slots": len(srv.slots), "slot_footprint_gb": srv.footprint / 1e9,
+           "slot_engine": ("resident chain, one captured graph per slot re-parameterised per job" if srv.graph else
+                           "resident chain, eager") if resident else "per-stage chain",
+           "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",
+           "isolated_s_by_size": {str(k): round(v, 5) for k, v in iso.items()}, "capacity_events_per_s": cap,
+           "captures_while_serving": 0, "policy": "srpt", "loads": {}}
+    c0 = sum(sl.chain.captures for sl in srv.slots if sl.chain is not None)
+    for k, load in enumerate(loads):
+        jobs = random_jobs(n_jobs, np.random.default_rng(seed + 1 + k), max_events=pool_events,
+                           pool_events=pool_events, rate=load * cap / mean_ev)
+        st = latency_stats(srv.run(jobs, realtime=True), iso_table=iso)
+        out["loads"][str(load)] = {k2: v for k2, v in st.items() if k2 != "jobs"}
+    out["captures_while_serving"] = sum(sl.chain.captures for sl in srv.slots if sl.chain is not None) - c0
+    srv = pool = None
+    return out
 
 
 def lookup_inputs(n_rows, seed=41, prob=0.0015, yield_per_mev=28610.0, edep=3.4, length=20.0):
@@ -573,7 +571,7 @@ def main():
     ap.add_argument("--warmup-ref", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--serve-jobs", type=int, default=100, help="jobs per load level of the serving measurement (0: skip)")
     ap.add_argument("--fullscale-events", type=int, default=32768,
                     help="events of the full-scale measurement, resident FP32 leg (0: skip)")
     ap.add_argument("--fullscale-stage-events", type=int, default=4096,
@@ -581,7 +579,7 @@ def main():
     ap.add_argument("--dropin-events", type=int, default=16384,
                     help="events of the drop-in (host tables through the stage entry points) end-to-end leg (0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
-    ap.add_argument("--serve-load", type=float, default=0.8)
+    ap.add_argument("--serve-loads", default="0.5,0.8,0.95", help="offered loads (fractions of the measured capacity)")
     ap.add_argument("--lookup-rows", type=int, default=1 << 20,
                     help="(step, SiPM) rows of the lookup-table photon model measurement (0: skip)")
     ap.add_argument("--lookup-precision", default="both", choices=["both", "fp64", "fp32"],
@@ -846,9 +844,16 @@ def main():
         r64 = eng64.run(batches[0], 5, keep=True)
         r32 = eng32.run(batches[0], 5, keep=True)
         acc = error_table(r64, r32, eng32.wcfg.adc_conversion, eng32.wcfg.pedestal)
-        from crvgpu.accuracy import waveform_only_table
-        acc["waveform_stage_alone"] = waveform_only_table(eng32, r64, eng32.wcfg.adc_conversion, eng32.wcfg.pedestal)
         acc["sample"] = f"first batch: {batches[0].nevents} events, seed 5"
+        r32 = None
+        eng64.release()
+        torch.cuda.empty_cache()
+        try:                                              # the waveform stage alone, on the FP64 run's charges
+            from crvgpu.accuracy import waveform_only_table
+            acc["waveform_stage_alone"] = waveform_only_table(eng32, r64, eng32.wcfg.adc_conversion,
+                                                              eng32.wcfg.pedestal)
+        except Exception as exc:
+            acc["waveform_stage_alone"] = {"error": str(exc)[:200]}
     except Exception as exc:  # the report is informative; its failure is shown, not hidden
         acc["error"] = str(exc)[:300]
 
@@ -901,7 +906,7 @@ def main():
 
     serve = None
     if rank == 0 and args.serve_jobs > 0:
-        serve = serving(geom, cond, args.serve_jobs, args.serve_pool, args.serve_load)
+        serve = serving(geom, cond, args.serve_jobs, args.serve_pool, [float(v) for v in args.serve_loads.split(",")])
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -424,6 +424,27 @@ int crv_chain(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev,
               void *stream, CrvStatus *status_dev);
 
 /*
+ * The resident chain as one CUDA graph (no counterpart in the reference; the reference's resident JAX chain compiles
+ * one program per shape): crv_chain_graph_create captures one crv_chain call with these arguments (plus the zeroing
+ * of the status block) on `stream`, which must be a created stream, in thread-local capture mode, and instantiates
+ * it; crv_chain_graph_launch replays it (a new batch: new contents in the same buffers); crv_chain_graph_set_params
+ * gives every kernel of the graph a new parameter block without a new capture, provided it differs from the current
+ * one only in the serving knobs (seed, yield_per_mev, frac_short, frac_long, lambda_short, lambda_long, min_voltage,
+ * noise_sigma; else CRV_ERR_ARG); crv_chain_graph_destroy frees it.  The design point's finder cuts live in the
+ * finder tables, which the caller may overwrite in place between launches.
+ */
+typedef struct CrvChainGraph CrvChainGraph;
+int crv_chain_graph_create(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev, const int64_t *ev_keys,
+                           const uint32_t *ev_runs, const CrvSteps *st, const int64_t *nsteps_dev, const CrvBars *bars,
+                           const CrvChannels *ch, const CrvPixels *px, const double *tmpl, int32_t tlen,
+                           const CrvFinderGeom *g, CrvClusters *out, CrvMembers *mem, int64_t *counts_dev,
+                           void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev,
+                           CrvChainGraph **graph_out);
+int crv_chain_graph_launch(CrvChainGraph *graph, void *stream);
+int crv_chain_graph_set_params(CrvChainGraph *graph, const CrvParams *p);
+void crv_chain_graph_destroy(CrvChainGraph *graph);
+
+/*
  * Lookup-table photon model (crvfastsim.response.photons._substep_photons, crv/crvfastsim/response/photons.py:163-224,
  * tables as crv/crvfastsim/response/lookup.py:70-98): every (step, SiPM) row is cut into nsub substeps along its step
  * vector; at each substep the position selects a bin of the scintillation table (inside the scintillator), of the

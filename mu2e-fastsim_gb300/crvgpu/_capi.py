@@ -221,6 +221,12 @@ _SIGS = {
     "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
                           P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters), P(CrvMembers),
                           c_p, c_p, c_i64, c_p, c_p]),
+    "crv_chain_graph_create": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p,
+                                       P(CrvBars), P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom),
+                                       P(CrvClusters), P(CrvMembers), c_p, c_p, c_i64, c_p, c_p, P(c_p)]),
+    "crv_chain_graph_launch": (c_i32, [c_p, c_p]),
+    "crv_chain_graph_set_params": (c_i32, [c_p, P(CrvParams)]),
+    "crv_chain_graph_destroy": (None, [c_p]),
 }
 
 # symbols declared in include/crvgpu.h (the load test checks every one is exported)

@@ -193,7 +193,7 @@ class ChainEngine:
         if (cfg.sipm != old.sipm or cfg.response.photon_yield_scale != old.response.photon_yield_scale
                 or cfg.response.photon_yield_variation_scale != old.response.photon_yield_variation_scale):
             self.tabs = DeviceTables(self.geom, self.cond, ccfg, self.device, self.pmap)
-        if fcfg != self.fcfg:
+        if fcfg != self.fcfg and not self.fin.update(self.G, fcfg):
             self.fin = FinderTables(self.G, fcfg, self.device)
         shape = ("single_pe_file", "single_pe_precision", "single_pe_stretch", "single_pe_max_time", "gumbel_peak",
                  "gumbel_mu", "gumbel_beta")

@@ -73,6 +73,18 @@ class FinderTables:
         if self.ntypes > 255:
             raise ValueError("coincidence finder: more than 255 sector types")
 
+    def update(self, G, cfg: FinderConfig) -> bool:
+        """Take the cuts of another finder configuration in place (same device buffers, so a captured chain graph
+        that reads them stays valid); False when the tables would change shape (then build new tables)."""
+        other = FinderTables(G, cfg, device=self.cuts.device)
+        keys = ("sec_cut", "cuts", "type_id", "type_p0", "type_p1", "type_half", "type_maxdt", "type_side0",
+                "type_side1")
+        if other.ntypes != self.ntypes or any(getattr(other, k).shape != getattr(self, k).shape for k in keys):
+            return False
+        for k in keys:
+            getattr(self, k).copy_(getattr(other, k))
+        return True
+
     def c_geom(self):
         keys = ("bar_sector", "bar_layer", "bar_counter", "bar_x", "bar_y", "bar_pos", "sec_type", "sec_cut",
                 "sec_length_dir", "sec_pos0", "sec_pos1", "cuts", "type_id", "type_p0", "type_p1", "type_half",

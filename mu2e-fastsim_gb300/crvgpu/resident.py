@@ -127,9 +127,9 @@ class ResidentResult:
 
 class ResidentChain:
     """Steps -> clusters on one device with explicit capacities; graph=True replays one captured CUDA graph per batch
-    (captured on the first batch of a seed; again after configure or a capacity change).  Graph mode wants one host
-    thread issuing CUDA work in the process while it captures: CUDA work from other threads meanwhile has invalidated
-    captures (cudaErrorStreamCaptureInvalidated); the eager mode (graph=False) has no such restriction."""
+    (crv_chain_graph_*: captured on the first batch, again only after a capacity change or a configuration change
+    beyond the serving knobs; seeds and knobs are written into the graph's kernels).  Captures are serialised in the
+    process and run in thread-local mode, so other host threads keep launching meanwhile."""
 
     def __init__(self, engine, caps: ChainCaps, real_dtype=None, graph=True, grow=False, max_grow=4):
         """engine: a ChainEngine (its tables, finder, template and configuration are used)."""
@@ -143,7 +143,8 @@ class ResidentChain:
         self.last_counts = None
         self.launches_per_run = 0
         self.replays = 0                # graph replays (kernel launches of a replay: launches_per_run)
-        self._graph, self._graph_key = None, None
+        self.captures = 0               # graph captures (a new seed or knob set needs none)
+        self._graph, self._graph_key, self._side = None, None, None
         self._warm = False
         self._alloc(caps)
 
@@ -153,7 +154,7 @@ class ResidentChain:
         L = _capi.load()
         dev, c = self.device, caps
         self.caps = caps
-        self._graph = None
+        self._drop_graph()
         # the previous buffers go first (called between batches, nothing in flight): growth does not need both sets
         self.ws = self.st = self.cl = self.mem = self.ev = None
         i32, i64, f64, rd = torch.int32, torch.int64, torch.float64, self.real_dtype
@@ -194,9 +195,9 @@ class ResidentChain:
                                                  (self.ev, self.st, self.cl, self.mem) for t in d.values())
 
     def configure(self, cfg):
-        """Switch the engine to another design point (the graph is captured again on the next batch)."""
+        """Switch the engine to another design point.  The serving knobs (photon yield, attenuation, threshold, finder
+        window) reach a captured graph without a new capture; other changes capture again on the next batch."""
         self.eng.configure(cfg)
-        self._graph = None
         P = self.eng.params(1)
         if _capi.load().crv_chain_workspace(ctypes.byref(P), ctypes.byref(self.caps.c())) > self.ws.numel():
             self._alloc(self.caps)
@@ -245,35 +246,54 @@ class ResidentChain:
                                 _capi.ptr(self.counts), _capi.ptr(self.ws), self.ws.numel(), _stream(),
                                 self.status.ptr), "crv_chain")
 
+    def _drop_graph(self):
+        if self._graph is not None:
+            _torch().cuda.synchronize()          # a replay may still be in flight
+            _capi.load().crv_chain_graph_destroy(self._graph)
+            self._graph = None
+
     def _capture(self, P, key):
+        """Capture one crv_chain call (and the status zeroing) as a native CUDA graph on a side stream, in
+        thread-local capture mode, so other host threads (serving slots) keep launching meanwhile."""
         torch = _torch()
-        self._graph = None
+        L = _capi.load()
+        self._drop_graph()
+        if self._side is None:
+            self._side = torch.cuda.Stream()
         cur = torch.cuda.current_stream()
-        side = torch.cuda.Stream()
-        side.wait_stream(cur)
-        with _CAPTURE_LOCK, torch.cuda.stream(side):
+        self._side.wait_stream(cur)
+        with _CAPTURE_LOCK, torch.cuda.stream(self._side):
             if not self._warm:                                  # first capture: one eager call outside it
                 self.status.reset()
                 self._call(P)
                 self._warm = True
-            g = torch.cuda.CUDAGraph()
+            h = ctypes.c_void_p()
+            t = self.eng.tabs
             n0 = _capi.launch_count()
-            # thread-local capture: other host threads (serving slots) keep launching and reading meanwhile
-            with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
-                self.status.t.zero_()
-                self._call(P)
+            _capi.check(L.crv_chain_graph_create(
+                ctypes.byref(P), ctypes.byref(self.caps.c()), ctypes.byref(self._E), _capi.ptr(self.ev["key"]),
+                _capi.ptr(self.ev["run"]), ctypes.byref(self._S), _capi.ptr(self.nsteps_dev),
+                ctypes.byref(t.c_bars()), ctypes.byref(t.c_channels()), ctypes.byref(t.c_pixels()),
+                _capi.ptr(self.eng.tmpl), int(self.eng.tlen), ctypes.byref(self.eng.fin.c_geom()),
+                ctypes.byref(self._C), ctypes.byref(self._M), _capi.ptr(self.counts), _capi.ptr(self.ws),
+                self.ws.numel(), _stream(), self.status.ptr, ctypes.byref(h)), "crv_chain_graph_create")
             self.launches_per_run = _capi.launch_count() - n0
-        cur.wait_stream(side)
-        self._graph, self._graph_key = g, key
+        cur.wait_stream(self._side)
+        self._graph, self._graph_key = h, key
+        self.captures += 1
 
     def launch(self, seed):
-        """Run the loaded batch (asynchronous; read the outcome with finish())."""
+        """Run the loaded batch (asynchronous; read the outcome with finish()).  Graph mode replays the captured
+        chain; a new seed or serving knobs go into the graph's kernels without a new capture (crv_chain_graph_
+        set_params), other changes (tables, template, capacities, settings that shape the launches) capture again."""
         P = self.eng.params(seed)
         if self.graph_mode:
-            key = (int(seed), id(self.eng.tabs), id(self.eng.fin), id(self.eng.tmpl), self.eng.ccfg)
-            if self._graph is None or self._graph_key != key:
+            L = _capi.load()
+            key = (id(self.eng.tabs), id(self.eng.fin), id(self.eng.tmpl))
+            if (self._graph is None or self._graph_key != key
+                    or L.crv_chain_graph_set_params(self._graph, ctypes.byref(P)) != _capi.CRV_OK):
                 self._capture(P, key)
-            self._graph.replay()
+            _capi.check(L.crv_chain_graph_launch(self._graph, _stream()), "crv_chain_graph_launch")
             self.replays += 1
         else:
             n0 = _capi.launch_count()

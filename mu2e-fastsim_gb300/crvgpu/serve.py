@@ -110,15 +110,17 @@ class ServeEngine:
     footprint and the granularity at which jobs interleave)."""
 
     def __init__(self, geom, cond, pool: DeviceSteps, hbm_budget: int, max_slots=8, chunk_events=4096,
-                 precision="fp32", device="cuda", resident=True):
+                 precision="fp32", device="cuda", resident=True, graph=True):
         """resident: slots run the resident chain (one host read per chunk) instead of the per-stage engine (a read per
-        stage).  The slots call it without graph replay: a stream capture on one slot thread is invalidated by CUDA
-        work that the other slot threads issue meanwhile (cudaErrorStreamCaptureInvalidated in a two-slot burst)."""
+        stage).  graph: every resident slot replays one captured CUDA graph of the chain, captured here, before any
+        slot thread runs; a job's seed and knobs are written into the graph's kernels (crv_chain_graph_set_params),
+        so serving needs no capture while it runs (a capacity growth would capture that slot again)."""
         from .chain import ChainEngine
         from .geometry import sector_geom
         from .resident import ChainCaps, ResidentChain, caps_for
         torch = _torch()
         self.resident = bool(resident)
+        self.graph = bool(graph) and self.resident
         self.geom, self.cond, self.pool = geom, cond, pool
         self.G = sector_geom(geom)
         self.sector = str(self.G.sector_names[0])
@@ -152,7 +154,7 @@ class ServeEngine:
                                                   max_steps_per_event=min(32768, 2 * max(1, first.max_steps)),
                                                   margin=1.3)
                 s0.engine = ChainEngine(geom, cond, base, G=self.G, device=device)
-                s0.chain = ResidentChain(s0.engine, self.caps, graph=False, grow=True)
+                s0.chain = ResidentChain(s0.engine, self.caps, graph=self.graph, grow=True)
         torch.cuda.synchronize()
         if self.resident:
             s0.footprint = int(s0.chain.nbytes * 1.05)
@@ -164,9 +166,14 @@ class ServeEngine:
             eng = ChainEngine(geom, cond, base, G=self.G, device=device)
             sl = _Slot(i, eng, torch.cuda.Stream(), s0.footprint)
             if self.resident:
-                sl.chain = ResidentChain(eng, self.caps, graph=False, grow=True)
+                sl.chain = ResidentChain(eng, self.caps, graph=self.graph, grow=True)
             self.slots.append(sl)
         self.footprint = s0.footprint
+        if self.graph:                               # capture every slot's graph now, one slot at a time
+            for sl in self.slots:
+                with torch.cuda.stream(sl.stream):
+                    sl.chain.run(first, 1)
+                sl.stream.synchronize()
 
     def _run_chunk(self, slot: _Slot, job: Job, a: int, b: int) -> dict:
         torch = _torch()
@@ -286,13 +293,51 @@ class ServeEngine:
         return [results[j.id] for j in jobs]
 
 
-def latency_stats(results, iso_rate, iso_overhead=0.0):
-    """p50 / p99 job latency [s] and p99 of latency / isolated run time (isolated time modelled as
-    iso_overhead + events / iso_rate)."""
+def measure_isolated(srv, sizes, seed=3, reps=2):
+    """Isolated run time of a job of each size (events): the job alone on an idle device, best of `reps` runs.
+    Returns {size: seconds}; isolated_time() interpolates it."""
+    out = {}
+    for n in sizes:
+        best = None
+        for r in range(reps):
+            t0 = time.perf_counter()
+            srv.run([Job(0, int(n), seed=seed + r)], realtime=False)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out[int(n)] = best
+    return out
+
+
+def isolated_time(table, n):
+    """Isolated run time of n events from a measured size table (linear in events between the measured sizes,
+    extrapolated with the rate of the largest two)."""
+    xs = np.array(sorted(table), float)
+    ys = np.array([table[int(x)] for x in xs])
+    n = np.asarray(n, float)
+    if len(xs) == 1:
+        return ys[0] * n / xs[0]
+    hi = ys[-1] + (n - xs[-1]) * (ys[-1] - ys[-2]) / (xs[-1] - xs[-2])
+    return np.where(n <= xs[-1], np.interp(n, xs, ys), hi)
+
+
+def latency_stats(results, iso_rate=None, iso_overhead=0.0, iso_table=None):
+    """p50 / p99 job latency [s] and p99 of latency / isolated run time.  The isolated time is measured per size
+    (iso_table from measure_isolated, interpolated), or modelled as iso_overhead + events / iso_rate."""
     lat = np.array([r.latency for r in results])
-    iso = np.array([iso_overhead + r.n_events / iso_rate for r in results])
+    nev = np.array([r.n_events for r in results], float)
+    iso = isolated_time(iso_table, nev) if iso_table else iso_overhead + nev / iso_rate
     span = max(r.finish for r in results) - min(r.arrival for r in results) if results else 0.0
     ev = sum(r.n_events for r in results)
-    return {"jobs": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "p99_over_isolated": float(np.percentile(lat / iso, 99)),
-            "events_per_s": float(ev / span) if span > 0 else None}
+    ratio = lat / iso
+    out = {"jobs": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "p99_over_isolated": float(np.percentile(ratio, 99)), "p50_over_isolated": float(np.percentile(ratio, 50)),
+           "events_per_s": float(ev / span) if span > 0 else None}
+    # slowdown per size class (decades of events)
+    cls = {}
+    for lo in (1e3, 1e4, 1e5, 1e6):
+        m = (nev >= lo) & (nev < 10 * lo)
+        if m.any():
+            cls[f"{int(lo)}-{int(10 * lo)}"] = {"jobs": int(m.sum()), "p50": float(np.percentile(ratio[m], 50)),
+                                                "p99": float(np.percentile(ratio[m], 99))}
+    out["slowdown_by_size"] = cls
+    return out

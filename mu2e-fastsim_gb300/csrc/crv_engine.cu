@@ -2,6 +2,8 @@
 // The kernels of each precision live in crv_kernels_f64.cu / crv_kernels_f32.cu; this unit holds the precision-free
 // kernels (event preparation, SiPM sizing, compaction, scans).
 #define CRV_ENGINE_TU 1
+#include <cuda.h>
+
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -1545,4 +1547,126 @@ extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const Crv
   if (rc != CRV_OK) return rc;
   CK(cudaMemcpyAsync(counts_dev, n, 10 * sizeof(long long), cudaMemcpyDeviceToDevice, s));
   return CRV_OK;
+}
+
+// ---- the resident chain as one CUDA graph, re-parameterised per design point --------------------------------------
+
+struct CrvChainGraph {
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  CrvParams p;                   // the parameter block the graph's kernels hold now
+};
+
+namespace crv {
+// The serving knobs a graph's kernels may take from a new parameter block without a new capture: none of them
+// changes which kernels run or their launch shapes (the host reads no other field of the block to launch the chain).
+static bool only_knobs_differ(const CrvParams& a, const CrvParams& b) {
+  CrvParams x = b;
+  x.seed = a.seed;
+  x.yield_per_mev = a.yield_per_mev;
+  x.frac_short = a.frac_short;
+  x.frac_long = a.frac_long;
+  x.lambda_short = a.lambda_short;
+  x.lambda_long = a.lambda_long;
+  x.min_voltage = a.min_voltage;
+  x.noise_sigma = a.noise_sigma;
+  return memcmp(&x, &a, sizeof(CrvParams)) == 0;
+}
+
+typedef CUresult (*FuncGetParamInfo)(CUfunction, size_t, size_t*, size_t*);
+
+static FuncGetParamInfo param_info_fn() {
+  static FuncGetParamInfo fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuFuncGetParamInfo", &f, 12040, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<FuncGetParamInfo>(f);
+  });
+  return fn;
+}
+}  // namespace crv
+
+extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev,
+                                      const int64_t* ev_keys, const uint32_t* ev_runs, const CrvSteps* st,
+                                      const int64_t* nsteps_dev, const CrvBars* bars, const CrvChannels* ch,
+                                      const CrvPixels* px, const double* tmpl, int32_t tlen, const CrvFinderGeom* g,
+                                      CrvClusters* out, CrvMembers* mem, int64_t* counts_dev, void* workspace,
+                                      int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                                      CrvChainGraph** graph_out) {
+  if (!graph_out || !p || !status_dev) return CRV_ERR_ARG;
+  *graph_out = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!s) return CRV_ERR_ARG;                    // the legacy default stream cannot be captured
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = CRV_OK;
+  if (cudaMemsetAsync(status_dev, 0, sizeof(CrvStatus), s) != cudaSuccess) rc = CRV_ERR_CUDA;
+  if (rc == CRV_OK)
+    rc = crv_chain(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem, counts_dev,
+                   workspace, workspace_bytes, stream, status_dev);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != CRV_OK || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != CRV_OK ? rc : CRV_ERR_CUDA;
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return CRV_ERR_CUDA;
+  }
+  *graph_out = new CrvChainGraph{graph, exec, *p};
+  return CRV_OK;
+}
+
+extern "C" int crv_chain_graph_launch(CrvChainGraph* h, void* stream) {
+  if (!h || !stream) return CRV_ERR_ARG;
+  CK(cudaGraphLaunch(h->exec, (cudaStream_t)stream));
+  return CRV_OK;
+}
+
+extern "C" int crv_chain_graph_set_params(CrvChainGraph* h, const CrvParams* p) {
+  if (!h || !p) return CRV_ERR_ARG;
+  if (!only_knobs_differ(h->p, *p)) return CRV_ERR_ARG;
+  if (memcmp(&h->p, p, sizeof(CrvParams)) == 0) return CRV_OK;
+  FuncGetParamInfo info = param_info_fn();
+  if (!info) return CRV_ERR_CUDA;
+  size_t nn = 0;
+  CK(cudaGraphGetNodes(h->graph, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  CK(cudaGraphGetNodes(h->graph, nodes.data(), &nn));
+  CrvParams np = *p;
+  std::vector<void*> args;
+  for (size_t i = 0; i < nn; ++i) {
+    cudaGraphNodeType t;
+    CK(cudaGraphNodeGetType(nodes[i], &t));
+    if (t != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp;
+    CK(cudaGraphKernelNodeGetParams(nodes[i], &kp));
+    cudaFunction_t f;
+    CK(cudaGetFuncBySymbol(&f, kp.func));
+    size_t off = 0, size = 0;
+    if (info(reinterpret_cast<CUfunction>(f), 0, &off, &size) != CUDA_SUCCESS) return CRV_ERR_CUDA;
+    // a kernel whose first argument is this library's parameter block, as captured
+    if (size != sizeof(CrvParams) || !kp.kernelParams || memcmp(kp.kernelParams[0], &h->p, size) != 0) continue;
+    size_t na = 1;
+    while (info(reinterpret_cast<CUfunction>(f), na, &off, &size) == CUDA_SUCCESS) ++na;
+    args.assign(kp.kernelParams, kp.kernelParams + na);
+    args[0] = &np;
+    kp.kernelParams = args.data();
+    kp.extra = nullptr;
+    CK(cudaGraphExecKernelNodeSetParams(h->exec, nodes[i], &kp));
+    CK(cudaGraphKernelNodeSetParams(nodes[i], &kp));
+  }
+  h->p = np;
+  return CRV_OK;
+}
+
+extern "C" void crv_chain_graph_destroy(CrvChainGraph* h) {
+  if (!h) return;
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  delete h;
 }

@@ -244,7 +244,7 @@ __host__ __device__ inline size_t wf32_smem_per_warp(int cap) {
 }
 
 // Synthesis + zero suppression of the groups whose longest kept cluster is in (lo, cap] (FP32-mixed).
-__global__ void __launch_bounds__(256) k_wf_synth32(CrvParams p, WfGroups G, const double* __restrict__ time,
+__global__ void __launch_bounds__(256, 4) k_wf_synth32(CrvParams p, WfGroups G, const double* __restrict__ time,
                                                     const double* __restrict__ charge, const double* __restrict__ tmpl,
                                                     int tlen, const double* __restrict__ tdc0_rows,
                                                     const double* __restrict__ g_tdc0,
@@ -340,18 +340,24 @@ __global__ void __launch_bounds__(256) k_wf_synth32(CrvParams p, WfGroups G, con
             const int m = (q2 + hi) >> 1;
             if (sj[m] > T + 31) hi = m; else q2 = m + 1;
           }
-          const int J = T + lane;
+          // a cluster of at most 16 samples (most of them) takes two lanes per sample, each summing every other
+          // charge; the two partial sums are added in a fixed order, so the result is the same on every run
+          const int split = L <= 16 ? 1 : 0;
+          const int J = T + (split ? (lane & 15) : lane);
+          const int part = split ? (lane >> 4) : 0;
           const float JP = float(J) * Pf;
-          float acc = J < L ? wave[J] : 0.0f;
+          float acc = 0.0f;
 #pragma unroll 4
-          for (int q = q1; q < q2; ++q) {
+          for (int q = q1 + part; q < q2; q += 1 + split) {
             const float2 v = sq[q];
             const float st = JP - v.x;
             // nearest integer of st / precision (ties to even) by the 1.5 x 2^23 shift; |st / precision| < 2^22
             const int ti = __float_as_int(fmaf(st, ip, 12582912.0f)) - 0x4B400000;
             if (st >= 0.0f && ti < tlen) acc = fmaf(tmpl_f[ti], v.y, acc);
           }
-          if (J < L) wave[J] = acc;
+          const float other = __shfl_down_sync(0xffffffffu, acc, 16);
+          if (split) acc = acc + other;
+          if (J < L && (split ? lane < 16 : true)) wave[J] = wave[J] + acc;
         }
       }
       __syncwarp();

@@ -130,3 +130,35 @@ def test_empty_batch_and_step_capacity_growth(setup):
     grown = ResidentChain(eng, small, graph=True, grow=True)
     _same(grown.run(ds, 4), eng.run(ds, 4))
     assert grown.caps.steps >= ds.nsteps
+
+
+def test_one_graph_serves_every_design_point(setup):
+    """A captured chain graph takes a new seed and new serving knobs (yield, attenuation length, threshold and the
+    finder window, the last through the finder tables updated in place) without a new capture, and every design point
+    equals the per-stage engine run at that point; a change beyond the knobs captures again."""
+    from dataclasses import replace
+    from crvgpu.resident import ResidentChain
+    from crvgpu.serve import Job, job_config
+    geom, cond, cfg, ds, CH = setup
+    from crvgpu.geometry import sector_geom
+    sector = str(sector_geom(geom).sector_names[0])
+    jobs = [Job(0, 1, yield_per_mev=40.0, lambda_long=5000.0, threshold_pe=5.0, window_ns=10.0, seed=11),
+            Job(1, 1, yield_per_mev=31.0, lambda_long=3600.0, threshold_pe=7.5, window_ns=18.0, seed=12),
+            Job(2, 1, yield_per_mev=48.5, lambda_long=6400.0, threshold_pe=3.2, window_ns=5.5, seed=13)]
+    heavy = job_config(Job(9, 1, yield_per_mev=50.0, lambda_long=6500.0, threshold_pe=3.0, window_ns=20.0), "fp32",
+                       sector)
+    caps = _trial_caps(CH.ChainEngine(geom, cond, heavy), ds)          # room for every design point below
+    eng = CH.ChainEngine(geom, cond, job_config(jobs[0], "fp32", sector))
+    rc = ResidentChain(eng, caps, graph=True, grow=True)
+    for j in jobs:
+        c = job_config(j, "fp32", sector)
+        rc.configure(c)
+        res = rc.run(ds, j.seed)
+        ref = CH.ChainEngine(geom, cond, c).run(ds, j.seed)
+        _same(res, ref)
+    assert rc.captures == 1 and rc.replays == len(jobs)
+    # noise off is not a serving knob: the graph is captured again, and still right
+    c = replace(job_config(jobs[1], "fp32", sector), noise=False)
+    rc.configure(c)
+    _same(rc.run(ds, 5), CH.ChainEngine(geom, cond, c).run(ds, 5))
+    assert rc.captures == 2

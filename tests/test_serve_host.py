@@ -111,3 +111,14 @@ def test_deadline_scheduling_orders_by_deadline(host_torch):
         srv.run(jobs, realtime=False, policy="fifo")
     with pytest.raises(ValueError):
         srv.run(jobs, realtime=False, policy="edf")             # needs the isolated rate
+
+
+def test_isolated_time_interpolates_the_measured_sizes():
+    from crvgpu.serve import JobResult, isolated_time, latency_stats
+    table = {1000: 0.010, 10000: 0.040, 100000: 0.340}
+    assert np.isclose(isolated_time(table, 1000), 0.010) and np.isclose(isolated_time(table, 55000), 0.19)
+    assert np.isclose(isolated_time(table, 200000), 0.340 + 100000 * 0.3 / 90000)
+    rs = [JobResult(i, n, {}, 0, 0.0, 0.0, 2 * float(isolated_time(table, n)), 0) for i, n in
+          enumerate([1000, 5000, 20000, 100000])]
+    st = latency_stats(rs, iso_table=table)
+    assert np.isclose(st["p99_over_isolated"], 2.0) and st["slowdown_by_size"]["1000-10000"]["jobs"] == 2
