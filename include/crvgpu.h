@@ -427,7 +427,8 @@ int crv_chain(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev,
  * The resident chain as one CUDA graph (no counterpart in the reference; the reference's resident JAX chain compiles
  * one program per shape): crv_chain_graph_create captures one crv_chain call with these arguments (plus the zeroing
  * of the status block) on `stream`, which must be a created stream, in thread-local capture mode, and instantiates
- * it; crv_chain_graph_launch replays it (a new batch: new contents in the same buffers); crv_chain_graph_set_params
+ * it; crv_chain_graph_launch replays it on any stream, the default one included (a new batch: new contents in the
+ * same buffers); crv_chain_graph_set_params
  * gives every kernel of the graph a new parameter block without a new capture, provided it differs from the current
  * one only in the serving knobs (seed, yield_per_mev, frac_short, frac_long, lambda_short, lambda_long, min_voltage,
  * noise_sigma; else CRV_ERR_ARG); crv_chain_graph_destroy frees it.  The design point's finder cuts live in the

@@ -1622,7 +1622,7 @@ extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* ca
 }
 
 extern "C" int crv_chain_graph_launch(CrvChainGraph* h, void* stream) {
-  if (!h || !stream) return CRV_ERR_ARG;
+  if (!h) return CRV_ERR_ARG;
   CK(cudaGraphLaunch(h->exec, (cudaStream_t)stream));
   return CRV_OK;
 }
