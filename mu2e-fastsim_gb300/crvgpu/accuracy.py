@@ -133,6 +133,8 @@ def digi_table(D64, D32, adc_conversion, adc_pedestal, changed=None):
             "matched_frac": float(len(com) / max(len(k64), 1)),
             "adc_samples_compared": int(a64.size), "adc_mismatch_rate": float(mis.sum() / max(a64.size, 1)),
             "adc_mismatch_at_boundary_frac": float(at_boundary[mis].mean()) if mis.any() else 1.0,
+            # the rest: an FP32 time offset that moves a charge across a 0.5 ns step of the single-PE template
+            "adc_mismatch_template_step_frac": float(1.0 - at_boundary[mis].mean()) if mis.any() else 0.0,
             "adc_mismatch_max_abs": int(np.abs(a64 - a32).max()) if a64.size else 0,
             "same_charges": {
                 "adc_samples": int(ms.size), "adc_mismatch_rate": float(ms.sum() / max(ms.size, 1)),
@@ -154,7 +156,8 @@ def waveform_only_table(eng32, r64, adc_conversion, adc_pedestal):
     D32 = {k: _np(v) for k, v in D.items()}
     t = digi_table(D64, D32, adc_conversion, adc_pedestal)
     return {k: t[k] for k in ("fp64", "fp32", "matched_frac", "adc_samples_compared", "adc_mismatch_rate",
-                              "adc_mismatch_at_boundary_frac", "adc_mismatch_max_abs")}
+                              "adc_mismatch_at_boundary_frac", "adc_mismatch_template_step_frac",
+                              "adc_mismatch_max_abs")}
 
 
 def error_table(r64, r32, adc_conversion, adc_pedestal):

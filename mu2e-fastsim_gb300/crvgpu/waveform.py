@@ -188,8 +188,8 @@ def digis(Q, cond, cfg: ChainConfig, rng, key=None, timers=None, *, stock_scan=F
     D = engine().run(P, tabs, lab_d, _dev(Q["time"], np.float64), _dev(Q["charge"], np.float64),
                      _dev(tmpl, np.float64), ek, er)
     out = _host(D)
-    # per-cluster outputs: the keyed TDC0 of each cluster's label
-    labels = np.unique(lab)
+    # per-cluster outputs: the keyed TDC0 of each cluster's label (labels are sorted: their distinct values by a scan)
+    labels = lab[np.r_[True, lab[1:] != lab[:-1]]] if len(lab) else lab
     tdc0_lab = _tdc0_device(P, tabs, _dev(labels, np.int64), ek, er)
     cid, first = charge_clusters(lab, Q["time"], wcfg)
     out.update(cluster_table(lab, Q["time"], tdc0_lab[np.searchsorted(labels, lab[first])], wcfg, tmpl))
