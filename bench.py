@@ -288,13 +288,16 @@ def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2
                            "resident chain, eager") if resident else "per-stage chain",
            "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",
            "isolated_s_by_size": {str(k): round(v, 5) for k, v in iso.items()}, "capacity_events_per_s": cap,
-           "captures_while_serving": 0, "policy": "srpt", "loads": {}}
+           "captures_while_serving": 0, "policy": "srpt (and the slowdown-balancing policy)", "loads": {}}
     c0 = sum(sl.chain.captures for sl in srv.slots if sl.chain is not None)
     for k, load in enumerate(loads):
         jobs = random_jobs(n_jobs, np.random.default_rng(seed + 1 + k), max_events=pool_events,
                            pool_events=pool_events, rate=load * cap / mean_ev)
         st = latency_stats(srv.run(jobs, realtime=True), iso_table=iso)
         out["loads"][str(load)] = {k2: v for k2, v in st.items() if k2 != "jobs"}
+        # the same arrivals, scheduled to even out the slowdown of small and large jobs
+        sl = latency_stats(srv.run(jobs, realtime=True, policy="slowdown", iso_table=iso), iso_table=iso)
+        out["loads"][str(load)]["slowdown_policy"] = {k2: v for k2, v in sl.items() if k2 != "jobs"}
     out["captures_while_serving"] = sum(sl.chain.captures for sl in srv.slots if sl.chain is not None) - c0
     srv = pool = None
     return out

@@ -193,25 +193,36 @@ class ServeEngine:
             slot.stream.synchronize()
         return out
 
-    def run(self, jobs, realtime=True, policy="srpt", iso_rate=None, iso_overhead=0.0, slack=2.0):
+    def run(self, jobs, realtime=True, policy="srpt", iso_rate=None, iso_overhead=0.0, slack=2.0, iso_table=None):
         """Serve `jobs` (arrival times in seconds from now when realtime, else all at once).  Returns JobResults in
         job order.
 
         Scheduling: a job is split into chunks of chunk_events events; whenever a slot is free it takes the next chunk
         of an arrived job, so jobs that arrive during others join at the next chunk boundary, and an otherwise idle
         device works on one job's chunks on every slot.  Which job:
-          "srpt": the one with the fewest events left (shortest remaining work first: small jobs are not queued behind
-                  large ones; large jobs wait longest under load);
-          "edf":  the one with the earliest deadline, arrival + slack * its isolated run time (iso_overhead +
-                  events / iso_rate), which bounds the largest latency / isolated-time ratio instead.
+          "srpt":     the one with the fewest events left (shortest remaining work first: small jobs are not queued
+                      behind large ones; large jobs wait longest under load);
+          "edf":      the one with the earliest deadline, arrival + slack * its isolated run time;
+          "slowdown": the one whose latency / isolated time would be largest if it were served now (time waited plus
+                      its remaining isolated time, over its isolated time): it evens out the slowdown of small and
+                      large jobs instead of favouring either.
+        The isolated run time is iso_table (measured sizes, see measure_isolated) or iso_overhead + events / iso_rate.
         Chunk results are kept per job and joined in event order when its last chunk is done."""
-        if policy not in ("srpt", "edf"):
+        if policy not in ("srpt", "edf", "slowdown"):
             raise ValueError(f"unknown scheduling policy {policy!r}")
-        if policy == "edf" and not (iso_rate and iso_rate > 0):
-            raise ValueError("edf scheduling needs the isolated rate (events/s)")
+        if policy != "srpt" and not iso_table and not (iso_rate and iso_rate > 0):
+            raise ValueError(f"{policy} scheduling needs the isolated run times (iso_table or iso_rate)")
+
+        def iso_of(n):
+            return float(isolated_time(iso_table, n)) if iso_table else iso_overhead + n / iso_rate
         if policy == "edf":
-            prio = lambda j: (info[j]["job"].arrival + slack * (iso_overhead + info[j]["job"].n_events / iso_rate),  # noqa: E731
-                              j)
+            prio = lambda j: (info[j]["job"].arrival + slack * info[j]["iso"], j)  # noqa: E731
+        elif policy == "slowdown":
+            def prio(j):
+                rec = info[j]
+                now = time.perf_counter() - t0
+                left = rec["iso"] * rec["left"] / max(rec["job"].n_events, 1)
+                return (-((now - rec["job"].arrival) + left) / rec["iso"], j)
         else:
             prio = lambda j: (info[j]["left"], info[j]["job"].arrival, j)  # noqa: E731
         torch = _torch()
@@ -230,7 +241,8 @@ class ServeEngine:
                 bounds = [(a, min(a + self.chunk, job.first + job.n_events))
                           for a in range(job.first, job.first + job.n_events, self.chunk)]
                 info[job.id] = {"job": job, "next": 0, "bounds": bounds, "parts": [None] * len(bounds),
-                                "left": job.n_events, "ndone": 0, "start": None}
+                                "left": job.n_events, "ndone": 0, "start": None,
+                                "iso": iso_of(job.n_events) if policy != "srpt" else 0.0}
                 state["active"].append(job.id)
 
         def finish(jid):

@@ -71,6 +71,7 @@ def test_serving_modes_agree():
         outs.append(srv.run(jobs, realtime=False))
     # deadline scheduling changes the order chunks run in, not the results
     outs.append(srv.run(jobs, realtime=False, policy="edf", iso_rate=1e5))
+    outs.append(srv.run(jobs, realtime=False, policy="slowdown", iso_table={1000: 0.01, 100000: 0.5}))
     with pytest.raises(ValueError):
         srv.run(jobs, realtime=False, policy="edf")
     for other in outs[1:]:

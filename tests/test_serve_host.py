@@ -122,3 +122,25 @@ def test_isolated_time_interpolates_the_measured_sizes():
           enumerate([1000, 5000, 20000, 100000])]
     st = latency_stats(rs, iso_table=table)
     assert np.isclose(st["p99_over_isolated"], 2.0) and st["slowdown_by_size"]["1000-10000"]["jobs"] == 2
+
+
+def test_slowdown_policy_needs_isolated_times():
+    from crvgpu.serve import ServeEngine
+    srv = ServeEngine.__new__(ServeEngine)
+    with pytest.raises(ValueError, match="isolated run times"):
+        srv.run([], policy="slowdown")
+    with pytest.raises(ValueError, match="unknown scheduling policy"):
+        srv.run([], policy="fifo")
+
+
+def test_slowdown_policy_serves_a_small_late_job_before_a_long_wait_grows(host_torch):
+    from crvgpu.serve import Job
+    srv = _FakeServe(1, 50, per_event=1e-6)
+    jobs = [Job(0, 400), Job(1, 50), Job(2, 200)]
+    res = srv.run(jobs, realtime=False, policy="slowdown", iso_table={50: 50e-6, 400: 400e-6})
+    assert [r.id for r in res] == [0, 1, 2] and all(r.finish >= r.start for r in res)
+    firsts = []
+    for jid, *_ in srv.log:
+        if jid not in firsts:
+            firsts.append(jid)
+    assert sorted(firsts) == [0, 1, 2]
