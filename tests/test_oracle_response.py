@@ -93,6 +93,29 @@ def test_keyed_draws_do_not_depend_on_batching():
         assert np.array_equal(Q[k][m], Q1[k])
 
 
+def test_photon_delays_are_sorted_exponential_order_statistics():
+    """Each (step, SiPM) row's emission delays come out in key order, and the normalised spacings
+    (t_j - t_(j-1)) * (n - j) / decay_time of every row are i.i.d. Exp(1) (Renyi's representation), so the row holds
+    the same distribution as the reference's n independent exponential delays (photons.py:163-224) sorted."""
+    from scipy import stats
+    from tests.helpers import workload
+    geom, cond, cfg, steps = workload(40, seed=5)
+    step, chan, t, key = O.make_photons(steps, geom, cfg.response, np.zeros(len(steps["event"])), 17)
+    row = step * 8 + (chan % 4)
+    o = np.lexsort((key, row))
+    row, t, key = row[o], t[o], key[o]
+    first = np.r_[True, row[1:] != row[:-1]]
+    start = np.maximum.accumulate(np.where(first, np.arange(len(row)), 0))
+    j = np.arange(len(row)) - start
+    assert np.array_equal(j, key & 0xFFFF)
+    n = np.bincount(np.cumsum(first) - 1)[np.cumsum(first) - 1]
+    dt = np.diff(t)[~first[1:]]
+    assert (dt >= 0).all()
+    x = dt * (n[1:][~first[1:]] - j[1:][~first[1:]]) / cfg.response.decay_time
+    assert len(x) > 20_000
+    assert stats.kstest(x, "expon").pvalue > 1e-3
+
+
 def _pix_cfg(pid, **kw):
     return replace(CF.SiPMConfig(pixel_id=pid), **kw)
 
