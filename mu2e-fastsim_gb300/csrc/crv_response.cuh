@@ -867,23 +867,32 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
       }
       continue;
     }
-    // stage photons with t <= t_end
+    // stage photons with t <= t_end, four chunks of 32 per step (their loads in flight together)
     int n = 0;
-    for (int base = 0; base < cnt; base += 32) {
-      int i = base + lane_id();
-      bool in = i < cnt;
-      R t = in ? R(ph_time[a + i]) : R(0);
-      bool keep;
-      if constexpr (sizeof(PT) == 4) keep = in && (float(ph_time[a + i]) <= K.t_end_dn);
-      else keep = in && (double(ph_time[a + i]) <= p.t_end);
-      unsigned km = __ballot_sync(FULL, keep);
-      if (keep) {
-        int o = n + __popc(km & lanemask_lt());
-        S.ph_t[o] = t;
-        S.ph_key[o] = G.key32 ? G.key32[a + i] : uint32_t(G.key64[a + i]);
-        S.ph_loc[o] = uint32_t(i);
+    for (int base = 0; base < cnt; base += 128) {
+      PT tv[4];
+      uint32_t kv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = base + 32 * u + lane_id();
+        tv[u] = i < cnt ? ph_time[a + i] : PT(0);
+        kv[u] = i < cnt ? (G.key32 ? G.key32[a + i] : uint32_t(G.key64[a + i])) : 0u;
       }
-      n += __popc(km);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = base + 32 * u + lane_id();
+        bool keep;
+        if constexpr (sizeof(PT) == 4) keep = i < cnt && (float(tv[u]) <= K.t_end_dn);
+        else keep = i < cnt && (double(tv[u]) <= p.t_end);
+        const unsigned km = __ballot_sync(FULL, keep);
+        if (keep) {
+          const int o = n + __popc(km & lanemask_lt());
+          S.ph_t[o] = R(tv[u]);
+          S.ph_key[o] = kv[u];
+          S.ph_loc[o] = uint32_t(i);
+        }
+        n += __popc(km);
+      }
     }
     __syncwarp();
     // the photons of one (step, SiPM) row come out of the photon stage in (time, key) order, so a SiPM hit by one

@@ -96,14 +96,41 @@ struct WfFx {                   // per-launch constants of the fixed-point forms
   bool ok;
 };
 
-__device__ __forceinline__ WfFx wf_fx_consts(const CrvParams& p, const double* tmpl, int tlen) {
+// order-preserving unsigned key of a double's bits (larger key = larger value), so a maximum over a table is
+// integer work: a warp-wide FP64 instruction costs ~60-70 FP32 issue slots on this GPU
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_value(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
+// the template's maximum (NaN entries ignored, as fmax does) by every thread of the block; call from all threads
+__device__ __forceinline__ double block_tmpl_max(const double* tmpl, int tlen, unsigned long long* slot) {
+  if (threadIdx.x == 0) *slot = dkey(-1e300);
+  __syncthreads();
+  unsigned long long m = dkey(-1e300);
+  for (int i = threadIdx.x; i < tlen; i += blockDim.x) {
+    const double v = tmpl[i];
+    const unsigned long long k = dkey(v);
+    if (v == v && k > m) m = k;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+    if (x > m) m = x;
+  }
+  if (lane_id() == 0) atomicMax(slot, m);
+  __syncthreads();
+  return dkey_value(*slot);
+}
+
+__device__ __forceinline__ WfFx wf_fx_consts(const CrvParams& p, double vmax) {
   WfFx f;
   f.ok = d2fx(p.period, &f.P) && d2fx(p.spe_max_time + 4.0 * p.period, &f.gap) && d2fx(p.spe_max_time, &f.maxt) &&
          d2fx(fmax(fmin(p.window_lo, 5e8), -5e8), &f.wlo) && d2fx(fmax(fmin(p.window_hi, 5e8), -5e8), &f.whi) &&
          d2fx(p.feb_phase_width, &f.width) && f.P > 0;
   f.invP = float(1.0 / p.period);              // fx_ceil_div / fx_floor_div estimate on times in ns
-  double vmax = -1e300;
-  for (int i = 0; i < tlen; ++i) vmax = fmax(vmax, tmpl[i]);
   // keep rule n * vmax >= min_voltage (n integer, monotone in n): the smallest such n
   int n = vmax > 0.0 ? int(fmin(ceil(p.min_voltage / vmax), 2e9)) : 2000000000;
   if (n < 0) n = 0;
@@ -130,16 +157,25 @@ __global__ void __launch_bounds__(256) k_wf_prep32(CrvParams p, CrvChannels ch, 
                                                    int32_t* __restrict__ cstart, WfCluster32* __restrict__ cl,
                                                    Status* status) {
   __shared__ WfFx fx_s;
-  if (threadIdx.x == 0) fx_s = wf_fx_consts(p, tmpl, tlen);
+  __shared__ unsigned long long vmax_s;
+  __shared__ float ip_s, pf_s;
+  __shared__ int nr_s;
+  const double vmax = block_tmpl_max(tmpl, tlen, &vmax_s);
+  if (threadIdx.x == 0) {                      // FP64 scalars once per block, in one thread
+    fx_s = wf_fx_consts(p, vmax);
+    ip_s = float(1.0 / p.spe_precision);
+    pf_s = float(p.period);
+    nr_s = reach_samples(p);
+  }
   __syncthreads();
   const WfFx F = fx_s;
   if (!F.ok || tlen > 1024) {
     if (threadIdx.x == 0 && blockIdx.x == 0) set_flag(status, CRV_ST_LIMIT);
     return;
   }
-  const int nr = reach_samples(p);
+  const int nr = nr_s;
   const int zs = p.samples_zs;
-  const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
+  const float Pf = pf_s, ip = ip_s;
   const int lane = lane_id();
   const long long ng = *G.n;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
@@ -259,22 +295,32 @@ __global__ void __launch_bounds__(256, 4) k_wf_synth32(CrvParams p, WfGroups G, 
   float* wave = reinterpret_cast<float*>(wbase);
   float2* sq = reinterpret_cast<float2*>(wbase + size_t(cap) * 4);              // (dt, normalised charge)
   int* sj = reinterpret_cast<int*>(wbase + size_t(cap) * 4 + size_t(WF32_QS) * 8);  // first sample reached
+  __shared__ float cf_s[7];
+  __shared__ int nr_s;
   if (tlen > 1024) return;                     // refused by the host; the table must fit the shared copy
   for (int i = threadIdx.x; i < tlen; i += blockDim.x) tmpl_f[i] = float(tmpl[i]);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0) {                      // FP64 scalars once per block, in one thread
     long long P;
     P_fx_s = d2fx(p.period, &P) ? P : 0;
+    cf_s[0] = float(p.period);
+    cf_s[1] = float(1.0 / p.spe_precision);
+    cf_s[2] = float(1.0 / p.spe_ref_charge);
+    cf_s[3] = float(p.min_voltage);
+    cf_s[4] = float(p.noise_sigma);
+    cf_s[5] = float(p.adc_conversion);
+    cf_s[6] = float(double(p.adc_pedestal) + 0.5);
+    nr_s = reach_samples(p);
   }
   __syncthreads();
   const long long P_fx = P_fx_s;
-  const int nr = reach_samples(p);
+  const int nr = nr_s;
   const int zs = p.samples_zs;
   const int lane = lane_id();
-  const float Pf = float(p.period), ip = float(1.0 / p.spe_precision);
-  const float inv_q = float(1.0 / p.spe_ref_charge);
-  const float vthr = float(p.min_voltage);
-  const float sigma = float(p.noise_sigma);
-  const float conv_f = float(p.adc_conversion), off_f = float(double(p.adc_pedestal) + 0.5);
+  const float Pf = cf_s[0], ip = cf_s[1];
+  const float inv_q = cf_s[2];
+  const float vthr = cf_s[3];
+  const float sigma = cf_s[4];
+  const float conv_f = cf_s[5], off_f = cf_s[6];
   const long long ng = *G.n;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   // groups in tiles of 32 per warp: one coalesced load of their longest clusters and a ballot pick this pass's groups
