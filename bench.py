@@ -263,7 +263,8 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
     return out
 
 
-def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2048, resident=True, graph=True):
+def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2048, resident=True, graph=True,
+            express=False):
     """Serving loop over a resident step pool: isolated run time measured per job size (each size alone on the idle
     device), saturated capacity (a burst of every job at once), then Poisson arrivals at each of `loads` x capacity
     (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
@@ -274,7 +275,7 @@ def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2
     pool = upload_steps(GM.synthetic_steps(pool_events, geom, seed=77), nbars=geom.nbars)
     free, _ = torch.cuda.mem_get_info()
     srv = ServeEngine(geom, cond, pool, hbm_budget=int(0.6 * free), max_slots=max_slots, chunk_events=chunk,
-                      resident=resident, graph=graph)
+                      resident=resident, graph=graph, express=express)
     sizes = sorted({int(v) for v in np.geomspace(1000, pool_events, 7)})
     iso = measure_isolated(srv, sizes)
     rng = np.random.default_rng(seed)
@@ -283,7 +284,7 @@ def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2
     srv.run(burst, realtime=False)
     cap = sum(j.n_events for j in burst) / (time.perf_counter() - t0)
     mean_ev = np.mean([j.n_events for j in burst])
-    out = {"jobs": n_jobs, "slots": len(srv.slots), "slot_footprint_gb": srv.footprint / 1e9,
+    out = {"jobs": n_jobs, "slots": len(srv.slots), "express_slot": srv.express, "slot_footprint_gb": srv.footprint / 1e9,
            "slot_engine": ("resident chain, one captured graph per slot re-parameterised per job" if srv.graph else
                            "resident chain, eager") if resident else "per-stage chain",
            "chunk_events": srv.chunk, "pool_events": pool_events, "job_events": f"log-uniform 1e3..{pool_events}",

@@ -100,6 +100,8 @@ class _Slot:
     footprint: int = 0
     job_id: object = None            # design point the engine is configured for
     chain: object = None             # ResidentChain over the engine (resident mode)
+    express: bool = False            # serves only jobs of at most one chunk, on a high-priority stream
+    busy: bool = False
 
 
 class ServeEngine:
@@ -110,11 +112,14 @@ class ServeEngine:
     footprint and the granularity at which jobs interleave)."""
 
     def __init__(self, geom, cond, pool: DeviceSteps, hbm_budget: int, max_slots=8, chunk_events=4096,
-                 precision="fp32", device="cuda", resident=True, graph=True):
+                 precision="fp32", device="cuda", resident=True, graph=True, express=False):
         """resident: slots run the resident chain (one host read per chunk) instead of the per-stage engine (a read per
         stage).  graph: every resident slot replays one captured CUDA graph of the chain, captured here, before any
         slot thread runs; a job's seed and knobs are written into the graph's kernels (crv_chain_graph_set_params),
-        so serving needs no capture while it runs (a capacity growth would capture that slot again)."""
+        so serving needs no capture while it runs (a capacity growth would capture that slot again).
+        express: one more slot (within the HBM budget) that takes only jobs of at most one chunk, on a stream of the
+        highest priority: a small job that arrives while the other slots run chunks of large jobs starts at once, and
+        the block scheduler gives its kernels the SMs that free up before those of the other streams."""
         from .chain import ChainEngine
         from .geometry import sector_geom
         from .resident import ChainCaps, ResidentChain, caps_for
@@ -161,10 +166,13 @@ class ServeEngine:
         else:
             s0.footprint = int(1.25 * max(1, torch.cuda.max_memory_allocated() - m0))
         n = int(max(1, min(max_slots, hbm_budget // s0.footprint)))
+        self.express = bool(express) and hbm_budget // s0.footprint > n
         self.slots = [s0]
-        for i in range(1, n):
+        for i in range(1, n + int(self.express)):
             eng = ChainEngine(geom, cond, base, G=self.G, device=device)
-            sl = _Slot(i, eng, torch.cuda.Stream(), s0.footprint)
+            ex = i == n
+            sl = _Slot(i, eng, torch.cuda.Stream(priority=-8) if ex else torch.cuda.Stream(), s0.footprint,
+                       express=ex)
             if self.resident:
                 sl.chain = ResidentChain(eng, self.caps, graph=self.graph, grow=True)
             self.slots.append(sl)
@@ -262,6 +270,11 @@ class ServeEngine:
                             return
                         admit_arrived(time.perf_counter() - t0)
                         cand = [jid for jid in state["active"] if info[jid]["next"] < len(info[jid]["bounds"])]
+                        if slot.express:                      # one-chunk jobs only
+                            cand = [jid for jid in cand if len(info[jid]["bounds"]) == 1]
+                        elif express is not None and not express.busy:
+                            # one-chunk jobs go to the idle express slot
+                            cand = [jid for jid in cand if len(info[jid]["bounds"]) > 1]
                         if cand:
                             jid = min(cand, key=prio)
                             rec = info[jid]
@@ -272,6 +285,7 @@ class ServeEngine:
                             if rec["start"] is None:
                                 rec["start"] = time.perf_counter() - t0
                                 rec["slot"] = slot.index
+                            slot.busy = True
                             break
                         wait = None
                         if realtime and state["pending"]:
@@ -285,6 +299,7 @@ class ServeEngine:
                         cv.notify_all()
                     return
                 with cv:
+                    slot.busy = False
                     rec["parts"][k] = out
                     rec["ndone"] += 1
                     if rec["ndone"] == len(rec["bounds"]):
@@ -293,8 +308,10 @@ class ServeEngine:
                         state["done"] += 1
                     cv.notify_all()
 
+        express = next((s_ for s_ in self.slots if s_.express), None)
         for s_ in self.slots:
             s_.job_id = None
+            s_.busy = False
         threads = [threading.Thread(target=worker, args=(s_,), daemon=True) for s_ in self.slots]
         for th in threads:
             th.start()

@@ -53,7 +53,7 @@ class _FakeServe:
     """ServeEngine's scheduler and result assembly over slots whose chunk work is simulated on the host: a chunk of
     events [a, b) takes `per_event` seconds per event and yields a cluster column with one entry per event."""
 
-    def __new__(cls, n_slots, chunk, per_event=2e-6):
+    def __new__(cls, n_slots, chunk, per_event=2e-6, express=False):
         import time
         import torch
         from crvgpu.serve import ServeEngine, _Slot
@@ -67,6 +67,8 @@ class _FakeServe:
         eng = object.__new__(Fake)
         eng.chunk = chunk
         eng.slots = [_Slot(i, None, None) for i in range(n_slots)]
+        if express:
+            eng.slots.append(_Slot(n_slots, None, None, express=True))
         eng.log = []
         return eng
 
@@ -144,3 +146,19 @@ def test_slowdown_policy_serves_a_small_late_job_before_a_long_wait_grows(host_t
         if jid not in firsts:
             firsts.append(jid)
     assert sorted(firsts) == [0, 1, 2]
+
+
+def test_express_slot_takes_one_chunk_jobs_and_nothing_else(host_torch):
+    from crvgpu.serve import Job
+    srv = _FakeServe(2, 50, per_event=1e-4, express=True)       # 5 ms per 50-event chunk
+    big = Job(0, 2000, first=0)
+    small = [Job(1 + i, 30, first=5000 + 100 * i, arrival=0.01 + 0.015 * i) for i in range(4)]
+    res = srv.run([big] + small, realtime=True)
+    for jid, a, b, slot, _ in srv.log:
+        if jid == 0:
+            assert slot in (0, 1)                                # multi-chunk work stays on the normal slots
+        else:
+            assert slot == 2                                     # one-chunk jobs on the idle express slot
+    assert all(r.finish < res[0].finish for r in res[1:])
+    for j, r in zip([big] + small, res):
+        assert np.array_equal(r.clusters["pe"], np.arange(j.first, j.first + j.n_events))
