@@ -819,10 +819,11 @@ def main():
         by_group[group_of(name)] = by_group.get(group_of(name), 0.0) + ms_k
     top_group = max(by_group.items(), key=lambda kv: kv[1])[0]
 
-    # DRAM bytes (read + write) per launch over algorithmic bytes, from one ncu capture of a 16,384-event chain batch
-    # (k_sipm_sim: 3.51 GB over 2.98 GB; k_wf_synth: 1.80 GB over 1.40 GB); the traffic of a stage grows with the events
-    # processed, so the ratio scales it to this run's batch
-    traffic_ratio = {"k_sipm_sim": 1.178, "k_wf_synth": 1.283}
+    # DRAM bytes (read + write) over algorithmic bytes of one 16,384-event chain batch, from single-kernel ncu captures
+    # of every launch of the stage in that batch (k_sipm_sim, 3 launches: 3.419 GB over 2.978 GB; k_wf_synth32,
+    # 3 launches: 1.823 GB over 1.405 GB; k_pf_persist, 1 launch: 0.765 GB over 0.396 GB); the traffic of a stage grows
+    # with the events processed, so the ratio scales it to this run's batch
+    traffic_ratio = {"k_sipm_sim": 1.148, "k_wf_synth": 1.298, "pulse fit": 1.931}
 
     def roofline_of(group):
         ks = groups.get(group, (group,))
