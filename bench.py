@@ -264,7 +264,7 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
 
 
 def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2048, resident=True, graph=True,
-            express=False):
+            express=True):
     """Serving loop over a resident step pool: isolated run time measured per job size (each size alone on the idle
     device), saturated capacity (a burst of every job at once), then Poisson arrivals at each of `loads` x capacity
     (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""

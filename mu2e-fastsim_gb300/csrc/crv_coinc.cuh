@@ -516,10 +516,12 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
                 if (kq > K + 1) break;
                 const int a = S.tmp[uint32_t(w)];
                 if (fabs(S.t[a] - S.t[h]) > dadj) continue;
+                // each entry goes to the one sum its counter offset names (the other two would add +0.0, which
+                // leaves a sum that starts at +0.0 unchanged: FP64 work saved, the same sums)
                 const int d = int(kq) - int(K);
-                same += d == 0 ? S.pe[a] : 0.0;
-                a1 += d == -1 ? S.pe[a] : 0.0;
-                a2 += d == 1 ? S.pe[a] : 0.0;
+                if (d == 0) same += S.pe[a];
+                else if (d == -1) a1 += S.pe[a];
+                else a2 += S.pe[a];
               }
               const double thr = cutv(G, S.cut[h], CUT_PE);
               pass_ = (same + a1 >= thr) || (same + a2 >= thr);
@@ -539,11 +541,15 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
               double dadj = cutv(G, S.cut[h], CUT_DTADJ);
               for (int q = 0; q < nt; ++q) {
                 int a = S.list[q];
-                if (S.side[a] != side || S.layer[a] != S.layer[h] || fabs(S.t[a] - S.t[h]) > dadj) continue;
-                int d = int(S.counter[a]) - int(S.counter[h]);
-                same += d == 0 ? S.pe[a] : 0.0;
-                a1 += d == -1 ? S.pe[a] : 0.0;
-                a2 += d == 1 ? S.pe[a] : 0.0;
+                // integer tests first: only hits of this side and layer on this or an adjacent counter enter a sum
+                // (a hit elsewhere would add +0.0 to every sum, which changes none of them), so the FP64 time test
+                // and addition run for those alone
+                if (S.side[a] != side || S.layer[a] != S.layer[h]) continue;
+                const int d = int(S.counter[a]) - int(S.counter[h]);
+                if (d < -1 || d > 1 || fabs(S.t[a] - S.t[h]) > dadj) continue;
+                if (d == 0) same += S.pe[a];
+                else if (d == -1) a1 += S.pe[a];
+                else a2 += S.pe[a];
               }
               double thr = cutv(G, S.cut[h], CUT_PE);
               pass = (same + a1 >= thr) || (same + a2 >= thr);
