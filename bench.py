@@ -467,6 +467,56 @@ def fullscale(n_events, batch, seed=13, resident_batch=2048, stage_events=4096):
     return out
 
 
+def lookup_chain(n_events, precision="fp32", seed=4, reps=3):
+    """The lookup-table photon model inside the resident chain (crv_chain_lookup, one graph replay per batch) on the
+    workload's module with a synthetic lookup table of its bars (crvgpu.lookup.synthetic_module_lookup: muons crossing
+    the thickness), against the stage path on the same events and seed: chain.charges with the lookup tables (host
+    tables in and out), then the per-stage engine from those charges.  Wall-clock per batch after warm-up; the two give
+    the same clusters."""
+    import torch
+    from crvgpu import chain as CH
+    from crvgpu.config import ChainConfig
+    from crvgpu.lookup import LookupModel, synthetic_module_lookup
+    from crvgpu.resident import ChainCaps, ResidentChain
+    from crvgpu.response import upload_steps
+    geom, cond, tables, lcfg, steps, pdg = synthetic_module_lookup(n_events, seed=seed)
+    cfg = ChainConfig(lookup=lcfg, precision=precision)
+    ds = upload_steps(steps, nbars=geom.nbars)
+    model = LookupModel(geom, lcfg, tables, cond.deviation, precision=precision)
+    cols = model.upload_steps(steps, pdg)
+    eng = CH.ChainEngine(geom, cond, cfg)
+    caps = ChainCaps(events=ds.nevents, steps=ds.nsteps, photons=1024, charges=1024, slots=1024, digis=1024,
+                     pulses=1024, max_steps_per_event=max(1, ds.max_steps))
+    rc = ResidentChain(eng, caps, real_dtype=torch.float64, graph=True, grow=True, max_grow=8, lookup=model)
+    rc.run(ds, seed, lookup_steps=cols)
+    rc.run(ds, seed + 1, lookup_steps=cols)
+    torch.cuda.synchronize()
+    best = None
+    for k in range(reps):
+        t0 = time.perf_counter()
+        r = rc.run(ds, seed + 2 + k, lookup_steps=cols)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+
+    def stage(sd):
+        Q = CH.charges(steps, None, geom, cond, cfg, None, key=sd, tabs=tables, pdg=pdg)
+        dq = {"label": torch.from_numpy(np.asarray(Q["chan"], np.int64)).cuda(),
+              **{k: torch.from_numpy(np.ascontiguousarray(Q[k])).cuda() for k in ("time", "charge", "pe", "photon")}}
+        return eng.run(ds, sd, charges=dq)
+    stage(seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = stage(seed + 2 + reps - 1)
+    torch.cuda.synchronize()
+    t_st = time.perf_counter() - t0
+    same = ref.n_clusters == r.counts["clusters"] and all(torch.equal(r.clusters[k], v) for k, v in ref.clusters.items())
+    return {"events": ds.nevents, "steps": ds.nsteps, "precision": precision, "tables": "synthetic, one 450 cm table",
+            "resident_events_per_s": ds.nevents / best, "stage_path_events_per_s": ds.nevents / t_st,
+            "resident_over_stage": t_st / best, "same_clusters": bool(same), "counts": r.counts,
+            "launches_per_batch": rc.launches_per_run}
+
+
 def e2e_dropin(geom, cond, n_events, seed=11, first_event=7_000_000, precision="fp32", reps=3):
     """The reference-facing call sequence on host tables, as a reference user makes it through the drop-in entry
     points (chain.charges -> chain.digis -> chain.reco_waveforms -> chain.clusters: host step table in, host arrays
@@ -583,6 +633,8 @@ def main():
     ap.add_argument("--dropin-events", type=int, default=16384,
                     help="events of the drop-in (host tables through the stage entry points) end-to-end leg (0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
+    ap.add_argument("--lookup-chain-events", type=int, default=16384,
+                    help="events of the resident chain with the lookup-table model (0: skip)")
     ap.add_argument("--serve-loads", default="0.5,0.8,0.95", help="offered loads (fractions of the measured capacity)")
     ap.add_argument("--lookup-rows", type=int, default=1 << 20,
                     help="(step, SiPM) rows of the lookup-table photon model measurement (0: skip)")
@@ -882,6 +934,14 @@ def main():
             dropin = {"error": str(exc)[:300]}
         torch.cuda.empty_cache()
 
+    lkchain = None
+    if rank == 0 and args.lookup_chain_events > 0:
+        try:
+            lkchain = lookup_chain(args.lookup_chain_events)
+        except Exception as exc:                          # shown, not hidden
+            lkchain = {"error": str(exc)[:300]}
+        torch.cuda.empty_cache()
+
     uneven = None
     if rank == 0 and args.uneven_waveforms > 0:
         uneven = uneven_pulse_fit(args.uneven_waveforms, 1 << 19)
@@ -929,7 +989,7 @@ def main():
                 "fp32_over_fp64": (value / fp64) if fp64 else None,
                 "fp32_vs_fp64": acc,
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-                "e2e_dropin": dropin,
+                "e2e_dropin": dropin, "lookup_chain": lkchain,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}

@@ -534,6 +534,40 @@ int crv_substep_photons(const CrvLookup *L, uint32_t seed, const CrvSubstepRows 
                         int64_t *o_step, int64_t *o_chan, double *o_time, int64_t cap, int64_t *n_out_dev,
                         void *workspace, int64_t workspace_bytes, void *stream, CrvStatus *status_dev);
 
+/*
+ * The resident chain with the lookup-table photon model: chain.charges with lookup tables (crv/crvfastsim/chain.py:
+ * 197-213) inside crv_chain.  The photons of every (step, SiPM) row come from the lookup model instead of the analytic
+ * one: rows as crv_lookup_rows makes them (keyed by the step's row in the batch), photons as crv_substep_photons draws
+ * them; SiPMs with status bit 0 or 2 get none; a SiPM's photons are in (step, substep, table, arrival) order, with
+ * draw key = their index in the SiPM and photon id = the step's row, as chain.charges with lookup tables gives them to
+ * sipm.simulate.  lk: the model's (table, reflector) groups (at most CRV_LOOKUP_CHAIN_GROUPS) with the table of each,
+ * and the batch's steps in the model's form (row i of lk->steps is row i of st, whose bar column the chain groups
+ * by).  The workspace holds 4 rows per step of caps->steps and the photons' times and ids (crv_chain_lookup_workspace).
+ * crv_chain_graph_create_lookup captures a crv_chain_lookup call as crv_chain_graph_create captures crv_chain; the
+ * lookup kernels read the seed from the graph's parameter block, so crv_chain_graph_set_params covers them too.
+ */
+#define CRV_LOOKUP_CHAIN_GROUPS 8
+typedef struct CrvLookupChain {
+    CrvLookupSteps steps;
+    int32_t ngroups, pad;
+    CrvLookupGroup group[CRV_LOOKUP_CHAIN_GROUPS];
+    CrvLookup table[CRV_LOOKUP_CHAIN_GROUPS];   /* the lookup table of group g */
+} CrvLookupChain;
+
+int64_t crv_chain_lookup_workspace(const CrvParams *p, const CrvChainCaps *caps);
+int crv_chain_lookup(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev, const int64_t *ev_keys,
+                     const uint32_t *ev_runs, const CrvSteps *st, const int64_t *nsteps_dev, const CrvBars *bars,
+                     const CrvChannels *ch, const CrvPixels *px, const double *tmpl, int32_t tlen,
+                     const CrvFinderGeom *g, CrvClusters *out, CrvMembers *mem, int64_t *counts_dev, void *workspace,
+                     int64_t workspace_bytes, void *stream, CrvStatus *status_dev, const CrvLookupChain *lk);
+int crv_chain_graph_create_lookup(const CrvParams *p, const CrvChainCaps *caps, const CrvEvents *ev,
+                                  const int64_t *ev_keys, const uint32_t *ev_runs, const CrvSteps *st,
+                                  const int64_t *nsteps_dev, const CrvBars *bars, const CrvChannels *ch,
+                                  const CrvPixels *px, const double *tmpl, int32_t tlen, const CrvFinderGeom *g,
+                                  CrvClusters *out, CrvMembers *mem, int64_t *counts_dev, void *workspace,
+                                  int64_t workspace_bytes, void *stream, CrvStatus *status_dev,
+                                  const CrvLookupChain *lk, CrvChainGraph **graph_out);
+
 /* ---- Lookup-table files (HOST memory, no device work) ------------------------------------------------------------
  * The Mu2e CRV photon lookup table, format version 6 (Offline CRVResponse MakeCrvPhotons), parsed from a file image:
  * replaces the reference's reader crvfastsim.response.lookup.load / _read_bins (crv/crvfastsim/response/lookup.py:

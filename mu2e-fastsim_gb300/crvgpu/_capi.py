@@ -142,6 +142,14 @@ class CrvSubstepRowsOut(ctypes.Structure):
     _fields_ = [(k, c_p) for k in LOOKUP_ROW_COLS]
 
 
+LOOKUP_CHAIN_GROUPS = 8
+
+
+class CrvLookupChain(ctypes.Structure):
+    _fields_ = [("steps", CrvLookupSteps), ("ngroups", c_i32), ("pad", c_i32),
+                ("group", CrvLookupGroup * LOOKUP_CHAIN_GROUPS), ("table", CrvLookup * LOOKUP_CHAIN_GROUPS)]
+
+
 # lookup-table file reader (host memory)
 LUTF_VERSION, LUTF_BIN_NUMBER, LUTF_TRAILING, LUTF_TRUNCATED, LUTF_SIZE = 1, 2, 3, 4, 5
 
@@ -224,6 +232,14 @@ _SIGS = {
     "crv_chain_graph_create": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p,
                                        P(CrvBars), P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom),
                                        P(CrvClusters), P(CrvMembers), c_p, c_p, c_i64, c_p, c_p, P(c_p)]),
+    "crv_chain_lookup_workspace": (c_i64, [P(CrvParams), P(CrvChainCaps)]),
+    "crv_chain_lookup": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
+                                 P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters),
+                                 P(CrvMembers), c_p, c_p, c_i64, c_p, c_p, P(CrvLookupChain)]),
+    "crv_chain_graph_create_lookup": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p,
+                                              P(CrvBars), P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom),
+                                              P(CrvClusters), P(CrvMembers), c_p, c_p, c_i64, c_p, c_p,
+                                              P(CrvLookupChain), P(c_p)]),
     "crv_chain_graph_launch": (c_i32, [c_p, c_p]),
     "crv_chain_graph_set_params": (c_i32, [c_p, P(CrvParams)]),
     "crv_chain_graph_destroy": (None, [c_p]),

@@ -215,13 +215,21 @@ class ChainEngine:
         P.period = self.wcfg.period
         return P
 
-    def run(self, ds: DeviceSteps, seed, keep=False, diagnostics=False):
-        """One pass of the chain over ds.  diagnostics: also count photons and hit SiPMs (n_photons, n_sipms)."""
+    def run(self, ds: DeviceSteps, seed, keep=False, diagnostics=False, charges=None):
+        """One pass of the chain over ds.  diagnostics: also count photons and hit SiPMs (n_photons, n_sipms).
+        charges: the batch's SiPM charges from elsewhere (device columns label, time, charge, pe, photon in label and
+        time order, e.g. chain.charges with lookup tables), which replace the response stage."""
         torch = _torch()
         L = _capi.load()
         dev = self.device
         P = self.params(seed)
-        R = self.resp.run(P, ds, self.tabs, diagnostics=diagnostics)
+        if charges is None:
+            R = self.resp.run(P, ds, self.tabs, diagnostics=diagnostics)
+        else:
+            from types import SimpleNamespace
+            R = SimpleNamespace(**{k: charges[k] for k in ("label", "time", "charge", "pe", "photon")},
+                                n=int(charges["label"].numel()), nsipm=0, sipm_photons=None)
+            diagnostics = False
         evk = ((ds.ev_subrun.to(torch.int64) & 0xFFFFFFFF) << 20) | (ds.ev_event.to(torch.int64) & 0xFFFFFFFF)
         D = self.dig.run(P, self.tabs, R.label, R.time, R.charge, self.tmpl, evk, ds.ev_run)
         nd = int(D["chan"].numel())

@@ -387,3 +387,60 @@ def make_photons(steps, pdg, geom, cfg, tables, deviation, seed, device="cuda", 
     keyed draws (seed in place of rng): (step index, channel = 4 bar + SiPM, arrival time) host arrays."""
     st, ch, tm = LookupModel(geom, cfg, tables, deviation, device, precision).make_photons(steps, pdg, seed)
     return st.cpu().numpy(), ch.cpu().numpy(), tm.cpu().numpy()
+
+
+def synthetic_module_lookup(n_events, seed=0, yield_per_mev=20000.0):
+    """The workload's one-module geometry with a synthetic lookup table of its bars (450 cm long, 19.8 mm thick, 50 mm
+    wide; 10 x 10 x 45 position bins, arrival probability falling with the distance to the SiPM as the workload's
+    two-exponential attenuation, delay weights peaked at distance / 140 mm/ns, fibre decay 5 ns) and `n_events`
+    synthetic events of muons crossing the thickness (the workload's steps: bar, position along the bar and across
+    its width, time and energy; start and end on the two faces).  Returns (geom, cond, tables, lookup config,
+    steps, pdg)."""
+    from types import SimpleNamespace
+    from . import geometry as GM
+    rng = np.random.default_rng(1000 + seed)
+    geom = GM.module_geometry()
+    cond = GM.default_conditions(geom)
+    hl = 2250.0
+    edges = {"x": np.linspace(-9.9, 9.9, 11), "y": np.linspace(-25.0, 25.0, 11), "z": np.linspace(-hl, hl, 46),
+             "beta": np.linspace(0.455, 1.0, 6), "theta": np.linspace(0, np.pi, 12), "phi": np.linspace(0, np.pi, 6),
+             "r": np.linspace(0, 0.616, 6)}
+    nb = {k: len(v) - 1 for k, v in edges.items()}
+    zc = 0.5 * (edges["z"][1:] + edges["z"][:-1])
+    d = zc + hl                                              # distance to the SiPM end at -half length
+
+    def table(n_per_z, z_of, scale):
+        zi = z_of(np.arange(n_per_z * nb["z"]))
+        dist = d[zi]
+        prob = (scale * (0.3 * np.exp(-dist / 1000.0) + 0.7 * np.exp(-dist / 5000.0))).astype(np.float32)
+        j = np.arange(150)[None, :]
+        peak = 3.0 + dist[:, None] / 140.0
+        delays = np.rint(12.0 * np.exp(-0.5 * ((j - peak) / 2.5) ** 2)).astype(np.uint8)
+        delays[:, 0] |= (delays.sum(1) == 0).astype(np.uint8)
+        emis = rng.integers(1, 20, (len(prob), 8)).astype(np.uint8)
+        return SimpleNamespace(prob=prob, delays=delays, delay_sum=delays.sum(1, dtype=np.int32), emis=emis,
+                               emis_sum=emis.sum(1, dtype=np.int32))
+
+    # bin index layouts: scint (x, y, z) and ckscint (x, y, z, beta) with z before beta; ckfiber z last
+    nxy = nb["x"] * nb["y"]
+    L = SimpleNamespace(name="module450", reflector=0, half_thickness=9.9, half_width=25.0, half_length=hl,
+                        fiber_separation=26.0, hole_radius_x=2.0, hole_radius_y=1.0, fiber_radius=0.7,
+                        corner_radius=1.75, fiber_decay_time=5.0, edges=edges,
+                        ck_scint=np.array([[0.6, 0.0], [1.0, 12.0]]), ck_fiber=np.array([[0.6, 0.0], [1.0, 6.0]]),
+                        tables={"scint": table(nxy, lambda i: i % nb["z"], 2.5e-3),
+                                "ckscint": table(nxy * nb["beta"], lambda i: (i // nb["beta"]) % nb["z"], 1e-3),
+                                "ckfiber": table(nb["beta"] * nb["theta"] * nb["phi"] * nb["r"],
+                                                 lambda i: i % nb["z"], 1e-3)})
+    lcfg = SimpleNamespace(sectors={"EX": SimpleNamespace(table="module450", reflector=0, yield_per_mev=yield_per_mev)},
+                           photon_yield_scale=1.0, photon_yield_variation_scale=1.0, speed_ratio={}, atten_ratio={})
+    st = GM.synthetic_steps(n_events, geom, seed=seed, dtype=np.float64)
+    bar = np.asarray(st["bar"])
+    n = len(bar)
+    cy = geom.center[bar, 1]
+    half = geom.halflen[bar, 1]
+    x, z, t = (np.asarray(st[k], np.float64) for k in ("x", "z", "t"))
+    steps = {"x0": x, "x1": x.copy(), "y0": cy - half, "y1": cy + half, "z0": z, "z1": z.copy(),
+             "px0": np.zeros(n), "py0": np.full(n, 1000.0), "pz0": np.zeros(n), "p1": np.full(n, 999.0),
+             "t0": t, "t1": t + 0.08, "edep": np.asarray(st["edep"], np.float64), "len": 2.0 * half, "bar": bar,
+             "event": np.asarray(st["event"]), "subrun": np.asarray(st["subrun"]), "run": np.asarray(st["run"])}
+    return geom, cond, {"module450": L}, lcfg, steps, np.full(n, 13, np.int64)

@@ -131,10 +131,16 @@ class ResidentChain:
     beyond the serving knobs; seeds and knobs are written into the graph's kernels).  Captures are serialised in the
     process and run in thread-local mode, so other host threads keep launching meanwhile."""
 
-    def __init__(self, engine, caps: ChainCaps, real_dtype=None, graph=True, grow=False, max_grow=4):
-        """engine: a ChainEngine (its tables, finder, template and configuration are used)."""
+    def __init__(self, engine, caps: ChainCaps, real_dtype=None, graph=True, grow=False, max_grow=4, lookup=None):
+        """engine: a ChainEngine (its tables, finder, template and configuration are used).  lookup: a LookupModel
+        (crvgpu.lookup) of the engine's geometry: the photons then come from the lookup-table model (crv_chain_lookup,
+        as chain.charges with lookup tables), and every batch also needs its steps in the model's form (run(...,
+        lookup_steps=LookupModel.upload_steps(steps, pdg)))."""
         torch = _torch()
         self.eng = engine
+        self.lookup = lookup
+        if lookup is not None and len(lookup.groups) > _capi.LOOKUP_CHAIN_GROUPS:
+            raise ValueError(f"the resident chain takes at most {_capi.LOOKUP_CHAIN_GROUPS} lookup groups")
         self.device = engine.device
         self.graph_mode, self.grow, self.max_grow = bool(graph), bool(grow), int(max_grow)
         self.real_dtype = real_dtype if real_dtype is not None else torch.float32
@@ -166,6 +172,10 @@ class ResidentChain:
                        key=torch.full((c.events,), INT64_MAX, dtype=i64, device=dev))
         self.st = {k: torch.zeros(c.steps, dtype=rd, device=dev) for k in ("x", "y", "z", "t", "edep")}
         self.st["bar"] = torch.zeros(c.steps, dtype=i32, device=dev)
+        self.lst = None
+        if self.lookup is not None:                     # the steps in the lookup model's form (bar: self.st's)
+            self.lst = {k: torch.zeros(c.steps, dtype=f64, device=dev) for k in _capi.LOOKUP_STEP_COLS}
+            self.lst["pdg"] = torch.zeros(c.steps, dtype=i64, device=dev)
         self.nsteps_dev = torch.zeros(1, dtype=i64, device=dev)
         cap = c.pulses
         self.cl = dict(event=torch.empty(cap, dtype=i64, device=dev), type=torch.empty(cap, dtype=i32, device=dev),
@@ -180,7 +190,7 @@ class ResidentChain:
         self.mem = dict(cl=torch.empty(cap, dtype=i64, device=dev), idx=torch.empty(cap, dtype=i32, device=dev),
                         event=torch.empty(cap, dtype=i64, device=dev))
         P = self.eng.params(1)
-        wsb = L.crv_chain_workspace(ctypes.byref(P), ctypes.byref(caps.c()))
+        wsb = self._workspace_bytes(P, caps)
         if wsb < 0:
             raise ValueError("crv_chain_workspace: invalid capacities")
         self.ws = torch.empty(int(wsb) + 1024, dtype=torch.uint8, device=dev)
@@ -191,19 +201,41 @@ class ResidentChain:
         rb = 4 if self.st["x"].dtype.itemsize == 4 else 8
         self._S = _capi.CrvSteps(*[_capi.ptr(self.st[k]) for k in ("x", "y", "z", "t", "edep", "bar")], rb, 0)
         self._E = _capi.CrvEvents(*[_capi.ptr(self.ev[k]) for k in ("event", "subrun", "run", "first", "nsteps")])
+        self._LK = self._lookup_c() if self.lookup is not None else None
         self.nbytes = int(self.ws.numel()) + sum(int(t.numel() * t.element_size()) for d in
-                                                 (self.ev, self.st, self.cl, self.mem) for t in d.values())
+                                                 (self.ev, self.st, self.cl, self.mem, self.lst or {})
+                                                 for t in d.values())
+
+    def _workspace_bytes(self, P, caps):
+        L = _capi.load()
+        f = L.crv_chain_lookup_workspace if self.lookup is not None else L.crv_chain_workspace
+        return f(ctypes.byref(P), ctypes.byref(caps.c()))
+
+    def _lookup_c(self):
+        """CrvLookupChain of the model over the static step buffers."""
+        m = self.lookup
+        K = _capi.CrvLookupChain()
+        K.steps = _capi.CrvLookupSteps(*[_capi.ptr(self.lst[k]) for k in _capi.LOOKUP_STEP_COLS],
+                                       _capi.ptr(self.st["bar"]), _capi.ptr(self.lst["pdg"]))
+        K.ngroups = len(m.groups)
+        for i, g in enumerate(m.groups):
+            K.group[i] = m._group_c(g)
+            K.table[i] = g["DL"].c(m.precision)
+        return K
 
     def configure(self, cfg):
         """Switch the engine to another design point.  The serving knobs (photon yield, attenuation, threshold, finder
         window) reach a captured graph without a new capture; other changes capture again on the next batch."""
         self.eng.configure(cfg)
         P = self.eng.params(1)
-        if _capi.load().crv_chain_workspace(ctypes.byref(P), ctypes.byref(self.caps.c())) > self.ws.numel():
+        if self._workspace_bytes(P, self.caps) > self.ws.numel():
             self._alloc(self.caps)
 
-    def load(self, ds: DeviceSteps):
-        """Copy a batch into the static buffers (device copies on the current stream)."""
+    def load(self, ds: DeviceSteps, lookup_steps=None):
+        """Copy a batch into the static buffers (device copies on the current stream).  lookup_steps: the batch's
+        steps in the lookup model's form (LookupModel.upload_steps), in the order of ds's rows (lookup model only)."""
+        if (self.lookup is not None) != (lookup_steps is not None):
+            raise ValueError("the lookup-table chain takes every batch's lookup_steps; the analytic chain none")
         c = self.caps
         over = ds.nevents > c.events or ds.nsteps > c.steps or ds.max_steps > c.max_steps_per_event
         if over and self.grow and ds.max_steps <= 32768:
@@ -217,6 +249,13 @@ class ResidentChain:
         if ds.x.dtype != self.real_dtype:
             raise ValueError(f"step table dtype {ds.x.dtype} differs from the chain's {self.real_dtype}")
         n, e = ds.nsteps, ds.nevents
+        if self.lookup is not None:
+            if ds.order is not None:
+                raise ValueError("the lookup-table chain needs steps grouped by event in increasing event key")
+            for k in _capi.LOOKUP_STEP_COLS + ("pdg",):
+                if int(lookup_steps[k].numel()) != n:
+                    raise ValueError(f"lookup step column {k}: {int(lookup_steps[k].numel())} rows, the batch {n}")
+                self.lst[k][:n].copy_(lookup_steps[k])
         for k in ("x", "y", "z", "t", "edep", "bar"):
             self.st[k][:n].copy_(getattr(ds, k))
         E = self.ev
@@ -235,16 +274,21 @@ class ResidentChain:
         self._n_events = e
 
     # -- the call ---------------------------------------------------------------------------------------------------
+    def _args(self, P):
+        t = self.eng.tabs
+        return (ctypes.byref(P), ctypes.byref(self.caps.c()), ctypes.byref(self._E), _capi.ptr(self.ev["key"]),
+                _capi.ptr(self.ev["run"]), ctypes.byref(self._S), _capi.ptr(self.nsteps_dev), ctypes.byref(t.c_bars()),
+                ctypes.byref(t.c_channels()), ctypes.byref(t.c_pixels()), _capi.ptr(self.eng.tmpl),
+                int(self.eng.tlen), ctypes.byref(self.eng.fin.c_geom()), ctypes.byref(self._C),
+                ctypes.byref(self._M), _capi.ptr(self.counts), _capi.ptr(self.ws), self.ws.numel(), _stream(),
+                self.status.ptr)
+
     def _call(self, P):
         L = _capi.load()
-        t = self.eng.tabs
-        _capi.check(L.crv_chain(ctypes.byref(P), ctypes.byref(self.caps.c()), ctypes.byref(self._E),
-                                _capi.ptr(self.ev["key"]), _capi.ptr(self.ev["run"]), ctypes.byref(self._S),
-                                _capi.ptr(self.nsteps_dev), ctypes.byref(t.c_bars()), ctypes.byref(t.c_channels()),
-                                ctypes.byref(t.c_pixels()), _capi.ptr(self.eng.tmpl), int(self.eng.tlen),
-                                ctypes.byref(self.eng.fin.c_geom()), ctypes.byref(self._C), ctypes.byref(self._M),
-                                _capi.ptr(self.counts), _capi.ptr(self.ws), self.ws.numel(), _stream(),
-                                self.status.ptr), "crv_chain")
+        if self.lookup is not None:
+            _capi.check(L.crv_chain_lookup(*self._args(P), ctypes.byref(self._LK)), "crv_chain_lookup")
+        else:
+            _capi.check(L.crv_chain(*self._args(P)), "crv_chain")
 
     def _drop_graph(self):
         if self._graph is not None:
@@ -268,15 +312,12 @@ class ResidentChain:
                 self._call(P)
                 self._warm = True
             h = ctypes.c_void_p()
-            t = self.eng.tabs
             n0 = _capi.launch_count()
-            _capi.check(L.crv_chain_graph_create(
-                ctypes.byref(P), ctypes.byref(self.caps.c()), ctypes.byref(self._E), _capi.ptr(self.ev["key"]),
-                _capi.ptr(self.ev["run"]), ctypes.byref(self._S), _capi.ptr(self.nsteps_dev),
-                ctypes.byref(t.c_bars()), ctypes.byref(t.c_channels()), ctypes.byref(t.c_pixels()),
-                _capi.ptr(self.eng.tmpl), int(self.eng.tlen), ctypes.byref(self.eng.fin.c_geom()),
-                ctypes.byref(self._C), ctypes.byref(self._M), _capi.ptr(self.counts), _capi.ptr(self.ws),
-                self.ws.numel(), _stream(), self.status.ptr, ctypes.byref(h)), "crv_chain_graph_create")
+            if self.lookup is not None:
+                _capi.check(L.crv_chain_graph_create_lookup(*self._args(P), ctypes.byref(self._LK), ctypes.byref(h)),
+                            "crv_chain_graph_create_lookup")
+            else:
+                _capi.check(L.crv_chain_graph_create(*self._args(P), ctypes.byref(h)), "crv_chain_graph_create")
             self.launches_per_run = _capi.launch_count() - n0
         cur.wait_stream(self._side)
         self._graph, self._graph_key = h, key
@@ -289,7 +330,7 @@ class ResidentChain:
         P = self.eng.params(seed)
         if self.graph_mode:
             L = _capi.load()
-            key = (id(self.eng.tabs), id(self.eng.fin), id(self.eng.tmpl))
+            key = (id(self.eng.tabs), id(self.eng.fin), id(self.eng.tmpl), id(self.lookup))
             if (self._graph is None or self._graph_key != key
                     or L.crv_chain_graph_set_params(self._graph, ctypes.byref(P)) != _capi.CRV_OK):
                 self._capture(P, key)
@@ -315,11 +356,11 @@ class ResidentChain:
         return ResidentResult(self._n_events, counts, {k: take(v, ncl) for k, v in self.cl.items()},
                               {k: take(v, nm) for k, v in self.mem.items()})
 
-    def run(self, ds: DeviceSteps, seed, copy=True):
+    def run(self, ds: DeviceSteps, seed, copy=True, lookup_steps=None):
         """One batch: load, launch, read.  With grow, a rejected batch for capacity alone is re-run with larger
-        capacities (captured again)."""
+        capacities (captured again).  lookup_steps: see load."""
         for attempt in range(self.max_grow + 1):
-            self.load(ds)
+            self.load(ds, lookup_steps)
             self.launch(seed)
             try:
                 return self.finish(copy)

@@ -181,15 +181,18 @@ struct RespWs {
   double *slot_t, *slot_v;
   long long* slot_id;
   long long nb, pc, sc;
+  LookupChainWs lk;              // lookup-table model (resident chain): rows, counts, offsets, photon ids
 };
 
-static RespWs resp_layout(char* base, const CrvParams& p, long long ne, long long ns, long long photon_cap, size_t* bytes) {
+// lookup: the lookup-table model's arrays too (photon times in FP64 in ph_t, whatever the precision)
+static RespWs resp_layout(char* base, const CrvParams& p, long long ne, long long ns, long long photon_cap, size_t* bytes,
+                          bool lookup = false) {
   Carve c{base};
   RespWs w;
   w.nb = 4 * ns;
   w.pc = photon_cap;
   w.sc = (long long)(p.charge_factor > 0 ? p.charge_factor : 1) * photon_cap + 16 * w.nb;
-  size_t rb = p.precision == 1 ? 4 : 8;
+  size_t rb = p.precision == 1 && !lookup ? 4 : 8;
   w.step_event = c.take<int32_t>(ns);
   w.step_order = c.take<int32_t>(ns);
   w.count = c.take<int32_t>(4 * ns);
@@ -219,6 +222,24 @@ static RespWs resp_layout(char* base, const CrvParams& p, long long ne, long lon
   w.slot_t = c.take<double>(w.sc);
   w.slot_v = c.take<double>(w.sc);
   w.slot_id = c.take<long long>(w.sc);
+  w.lk = LookupChainWs{};
+  if (lookup) {
+    const long long nr = w.nb;
+    CrvSubstepRowsOut& o = w.lk.rows;
+    o.s = c.take<double>(3 * nr);
+    o.d = c.take<double>(3 * nr);
+    double** dcols[6] = {&o.t0, &o.t1, &o.beta, &o.cos_theta, &o.dev, &o.mu};
+    for (auto q : dcols) *q = c.take<double>(nr);
+    int64_t** icols[6] = {&o.nsub, &o.step, &o.chan, &o.n_scint, &o.n_ck_s, &o.n_ck_f};
+    for (auto q : icols) *q = c.take<int64_t>(nr);
+    w.lk.row_group = c.take<int8_t>(nr);
+    w.lk.count = c.take<long long>(nr);
+    w.lk.row_off = c.take<long long>(nr);
+    w.lk.nrows = c.take<long long>(1);
+    w.lk.seed = c.take<uint32_t>(1);
+    w.lk.o_step = c.take<int64_t>(photon_cap);
+    w.lk.o_time = reinterpret_cast<double*>(w.ph_t);
+  }
   *bytes = c.off + 256;
   return w;
 }
@@ -327,23 +348,45 @@ int crv_photons(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const 
 
 // Stage bodies take an optional device count beside each host count (the host count is then a capacity), so that a
 // whole chain can run without reading sizes back: the public entry points pass null.
+// Lookup-table model in the resident chain: the output offset of every row of every SiPM, its steps in order (rows of
+// SiPMs without an entry keep -1 and are not written)
+__global__ void k_lrow_offsets(const long long* __restrict__ nsipm_dev, const int32_t* __restrict__ s_chan,
+                               const long long* __restrict__ s_seg, const int32_t* __restrict__ s_nseg,
+                               const int32_t* __restrict__ step_order, const int32_t* __restrict__ count,
+                               const long long* __restrict__ ph_off, long long* __restrict__ row_off) {
+  const long long nsipm = *nsipm_dev;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nsipm;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int sp = s_chan[g] & 3;
+    const long long a = s_seg[g];
+    long long o = ph_off[g];
+    for (int k = 0; k < s_nseg[g]; ++k) {
+      const long long r = 4 * (long long)step_order[a + k] + sp;
+      row_off[r] = o;
+      o += count[r];
+    }
+  }
+}
+
 static int response_run(const CrvParams* p, const CrvEvents* ev, int64_t nevents, const CrvSteps* st, int64_t nsteps,
                         const long long* nsteps_dev, int32_t max_steps_per_event, const CrvBars* bars,
                         const CrvChannels* ch, const CrvPixels* px, int64_t photon_cap, CrvCharges* out,
                         int64_t out_cap, int64_t* n_out_dev, int64_t* sipm_label, int32_t* sipm_photons,
                         int32_t* sipm_fired, int64_t sipm_cap, int64_t* n_sipm_dev, void* workspace,
-                        int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+                        int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                        const CrvLookupChain* lk = nullptr) {
   if (!p || !ev || !st || !bars || !ch || !px || !out || !n_out_dev || !status_dev) return CRV_ERR_ARG;
   if (st->real_bytes != 4 && st->real_bytes != 8) return CRV_ERR_ARG;
   if (nevents < 0 || nsteps < 0 || photon_cap < 0 || out_cap < 0 || max_steps_per_event < 0) return CRV_ERR_ARG;
+  if (lk && (lk->ngroups < 0 || lk->ngroups > CRV_LOOKUP_CHAIN_GROUPS || !nsteps_dev)) return CRV_ERR_ARG;
   size_t need = 0;
-  resp_layout(nullptr, *p, nevents, nsteps, photon_cap, &need);
+  resp_layout(nullptr, *p, nevents, nsteps, photon_cap, &need, lk != nullptr);
   if (!workspace || (size_t)workspace_bytes < need) return CRV_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   Status* S = reinterpret_cast<Status*>(status_dev);
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
   size_t dummy;
-  RespWs w = resp_layout(base, *p, nevents, nsteps, photon_cap, &dummy);
+  RespWs w = resp_layout(base, *p, nevents, nsteps, photon_cap, &dummy, lk != nullptr);
   CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
   if (nevents == 0 || nsteps == 0) {
     CK(cudaMemsetAsync(n_out_dev, 0, sizeof(long long), s));
@@ -377,8 +420,11 @@ static int response_run(const CrvParams* p, const CrvEvents* ev, int64_t nevents
                                                   w.sipm_off, w.s_event, w.s_chan, w.s_seg, w.s_nseg, S, 1);
   }
   CK(cudaGetLastError());
-  // 4. photon counts per (step, SiPM)
-  if (p->precision == 1)
+  // 4. photon counts per (step, SiPM): the lookup-table model's rows and arrival counts, or the analytic model's
+  if (lk) {
+    CK(lookup_chain_rows(*p, *lk, nsteps_dev, nsteps, w.lk, s));
+    CK(lookup_chain_count(*lk, w.lk, w.nb, w.count, S, s));
+  } else if (p->precision == 1)
     CK(launch_photon_count<float>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, nsteps_dev, 1, w.count, S, s));
   else
     CK(launch_photon_count<double>(*p, *ev, *st, *bars, *ch, w.step_event, nsteps, nsteps_dev, 1, w.count, S, s));
@@ -402,8 +448,17 @@ static int response_run(const CrvParams* p, const CrvEvents* ev, int64_t nevents
     k_check_caps<<<1, 32, 0, s>>>(&w.totals[2], w.sc, CRV_NEED_SLOTS_TOTAL, S);
   }
   CK(cudaGetLastError());
-  // 6. photons of every SiPM
-  if (p->precision == 1)
+  // 6. photons of every SiPM (lookup model: each row's photons at the offset of its step in its SiPM)
+  if (lk) {
+    CK(cudaMemsetAsync(w.lk.row_off, 0xFF, sizeof(long long) * size_t(w.nb), s));
+    {
+      crv::Mark mark_("k_lrow_offsets", s);
+      k_lrow_offsets<<<grid_for(w.nb, 256, 8), 256, 0, s>>>(&w.totals[0], w.s_chan, w.s_seg, w.s_nseg, w.step_order,
+                                                            w.count, w.ph_off, w.lk.row_off);
+    }
+    CK(cudaGetLastError());
+    CK(lookup_chain_emit(*lk, w.lk, w.nb, &w.totals[1], w.pc, S, s));
+  } else if (p->precision == 1)
     CK(launch_photon_emit<float>(*p, *ev, *st, *bars, w.nb, &w.totals[0], w.s_event, w.s_chan, w.s_seg, w.s_nseg,
                                  w.step_order, w.count, w.ph_off, (float*)w.ph_t, w.ph_key, &w.totals[1], w.pc, s));
   else
@@ -420,14 +475,16 @@ static int response_run(const CrvParams* p, const CrvEvents* ev, int64_t nevents
   G.count = w.nphot;
   G.label = w.label;
   G.run = w.run;
-  G.key32 = w.ph_key;
+  G.key32 = lk ? nullptr : w.ph_key;          // lookup model: draw key = index of the photon in its SiPM
   G.key64 = nullptr;
-  G.photon_id = nullptr;
+  G.photon_id = lk ? reinterpret_cast<const long long*>(w.lk.o_step) : nullptr;
   G.id_base = w.id_base;
   G.slot_off = w.slot_off;
   G.slot_cap = w.slot_cap;
   SipmOut O{w.slot_t, w.slot_v, w.slot_id, w.nmain, w.nap, w.fired};
-  if (p->precision == 1)
+  if (p->precision == 1 && lk)
+    CK((launch_sipm<float, double>(*p, *px, G, &w.totals[0], (const double*)w.ph_t, O, S, s)));
+  else if (p->precision == 1)
     CK((launch_sipm<float, float>(*p, *px, G, &w.totals[0], (const float*)w.ph_t, O, S, s)));
   else
     CK((launch_sipm<double, double>(*p, *px, G, &w.totals[0], (const double*)w.ph_t, O, S, s)));
@@ -1398,12 +1455,12 @@ struct ChainWs {
   long long scratch_bytes;
 };
 
-static long long chain_scratch_bytes(const CrvParams& p, const CrvChainCaps& c) {
+static long long chain_scratch_bytes(const CrvParams& p, const CrvChainCaps& c, bool lookup) {
   long long zs = p.samples_zs;
   long long b = 0;
   auto up = [&](long long v) { if (v > b) b = v; };
   size_t r = 0;
-  resp_layout(nullptr, p, c.events, c.steps, c.photons, &r);
+  resp_layout(nullptr, p, c.events, c.steps, c.photons, &r, lookup);
   up((long long)r);
   digi_layout(nullptr, c.charges, c.slots, p.samples_zs, &r);
   up((long long)r);
@@ -1416,7 +1473,7 @@ static long long chain_scratch_bytes(const CrvParams& p, const CrvChainCaps& c) 
   return b;
 }
 
-static ChainWs chain_layout(char* base, const CrvParams& p, const CrvChainCaps& c, size_t* bytes) {
+static ChainWs chain_layout(char* base, const CrvParams& p, const CrvChainCaps& c, size_t* bytes, bool lookup = false) {
   Carve k{base};
   ChainWs w;
   const long long zs = p.samples_zs, nq = c.charges, nd = c.digis, np = c.pulses, ne = c.events;
@@ -1456,7 +1513,7 @@ static ChainWs chain_layout(char* base, const CrvParams& p, const CrvChainCaps& 
   w.h_seq = k.take<int32_t>(np);
   w.h_time = k.take<double>(np);
   w.h_pe = k.take<double>(np);
-  w.scratch_bytes = chain_scratch_bytes(p, c);
+  w.scratch_bytes = chain_scratch_bytes(p, c, lookup);
   w.scratch = k.take<char>(w.scratch_bytes);
   *bytes = k.off + 256;
   return w;
@@ -1475,21 +1532,30 @@ extern "C" int64_t crv_chain_workspace(const CrvParams* p, const CrvChainCaps* c
   return (int64_t)b;
 }
 
-extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev, const int64_t* ev_keys,
-                         const uint32_t* ev_runs, const CrvSteps* st, const int64_t* nsteps_dev, const CrvBars* bars,
-                         const CrvChannels* ch, const CrvPixels* px, const double* tmpl, int32_t tlen,
-                         const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem, int64_t* counts_dev,
-                         void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+extern "C" int64_t crv_chain_lookup_workspace(const CrvParams* p, const CrvChainCaps* caps) {
+  if (!chain_caps_ok(p, caps)) return -1;
+  size_t b = 0;
+  chain_layout(nullptr, *p, *caps, &b, true);
+  return (int64_t)b;
+}
+
+namespace crv {
+static int chain_run(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev, const int64_t* ev_keys,
+                     const uint32_t* ev_runs, const CrvSteps* st, const int64_t* nsteps_dev, const CrvBars* bars,
+                     const CrvChannels* ch, const CrvPixels* px, const double* tmpl, int32_t tlen,
+                     const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem, int64_t* counts_dev,
+                     void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                     const CrvLookupChain* lk) {
   if (!chain_caps_ok(p, caps) || !ev || !ev_keys || !ev_runs || !st || !nsteps_dev || !bars || !ch || !px || !tmpl ||
       tlen <= 0 || !g || !out || !mem || !counts_dev || !status_dev)
     return CRV_ERR_ARG;
   size_t need = 0;
-  chain_layout(nullptr, *p, *caps, &need);
+  chain_layout(nullptr, *p, *caps, &need, lk != nullptr);
   if (!workspace || (long long)need > workspace_bytes) return CRV_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
   size_t dummy;
-  ChainWs w = chain_layout(base, *p, *caps, &dummy);
+  ChainWs w = chain_layout(base, *p, *caps, &dummy, lk != nullptr);
   const CrvChainCaps& c = *caps;
   long long* n = w.counts;                 // raw counts
   long long* m = w.counts + 16;            // counts passed on: 0 when the stage overflowed its capacity
@@ -1509,11 +1575,12 @@ extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const Crv
   };
   int rc = response_run(p, ev, c.events, st, c.steps, reinterpret_cast<const long long*>(nsteps_dev),
                         c.max_steps_per_event, bars, ch, px, c.photons, &w.Q, c.charges, N(CRV_CHAIN_CHARGES),
-                        nullptr, nullptr, nullptr, 0, nullptr, w.scratch, w.scratch_bytes, stream, status_dev);
+                        nullptr, nullptr, nullptr, 0, nullptr, w.scratch, w.scratch_bytes, stream, status_dev, lk);
   if (rc != CRV_OK) return rc;
   {
     size_t b;
-    CK(keep_total(&resp_layout(w.scratch, *p, c.events, c.steps, c.photons, &b).totals[1], CRV_CHAIN_PHOTONS));
+    CK(keep_total(&resp_layout(w.scratch, *p, c.events, c.steps, c.photons, &b, lk != nullptr).totals[1],
+                  CRV_CHAIN_PHOTONS));
   }
   CK(guard(CRV_CHAIN_CHARGES, c.charges));
   rc = digis_run(p, ch, c.charges, &m[CRV_CHAIN_CHARGES], w.Q.label, w.Q.time, w.Q.charge, nullptr, tmpl, tlen, ev_keys,
@@ -1547,6 +1614,28 @@ extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const Crv
   if (rc != CRV_OK) return rc;
   CK(cudaMemcpyAsync(counts_dev, n, 10 * sizeof(long long), cudaMemcpyDeviceToDevice, s));
   return CRV_OK;
+}
+}  // namespace crv
+
+extern "C" int crv_chain(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev, const int64_t* ev_keys,
+                         const uint32_t* ev_runs, const CrvSteps* st, const int64_t* nsteps_dev, const CrvBars* bars,
+                         const CrvChannels* ch, const CrvPixels* px, const double* tmpl, int32_t tlen,
+                         const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem, int64_t* counts_dev,
+                         void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev) {
+  return chain_run(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem, counts_dev,
+                   workspace, workspace_bytes, stream, status_dev, nullptr);
+}
+
+extern "C" int crv_chain_lookup(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev,
+                                const int64_t* ev_keys, const uint32_t* ev_runs, const CrvSteps* st,
+                                const int64_t* nsteps_dev, const CrvBars* bars, const CrvChannels* ch,
+                                const CrvPixels* px, const double* tmpl, int32_t tlen, const CrvFinderGeom* g,
+                                CrvClusters* out, CrvMembers* mem, int64_t* counts_dev, void* workspace,
+                                int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                                const CrvLookupChain* lk) {
+  if (!lk) return CRV_ERR_ARG;
+  return chain_run(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem, counts_dev,
+                   workspace, workspace_bytes, stream, status_dev, lk);
 }
 
 // ---- the resident chain as one CUDA graph, re-parameterised per design point --------------------------------------
@@ -1589,13 +1678,13 @@ static FuncGetParamInfo param_info_fn() {
 }
 }  // namespace crv
 
-extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev,
-                                      const int64_t* ev_keys, const uint32_t* ev_runs, const CrvSteps* st,
-                                      const int64_t* nsteps_dev, const CrvBars* bars, const CrvChannels* ch,
-                                      const CrvPixels* px, const double* tmpl, int32_t tlen, const CrvFinderGeom* g,
-                                      CrvClusters* out, CrvMembers* mem, int64_t* counts_dev, void* workspace,
-                                      int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
-                                      CrvChainGraph** graph_out) {
+namespace crv {
+static int graph_create(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev, const int64_t* ev_keys,
+                        const uint32_t* ev_runs, const CrvSteps* st, const int64_t* nsteps_dev, const CrvBars* bars,
+                        const CrvChannels* ch, const CrvPixels* px, const double* tmpl, int32_t tlen,
+                        const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem, int64_t* counts_dev,
+                        void* workspace, int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                        const CrvLookupChain* lk, CrvChainGraph** graph_out) {
   if (!graph_out || !p || !status_dev) return CRV_ERR_ARG;
   *graph_out = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1604,8 +1693,8 @@ extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* ca
   int rc = CRV_OK;
   if (cudaMemsetAsync(status_dev, 0, sizeof(CrvStatus), s) != cudaSuccess) rc = CRV_ERR_CUDA;
   if (rc == CRV_OK)
-    rc = crv_chain(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem, counts_dev,
-                   workspace, workspace_bytes, stream, status_dev);
+    rc = chain_run(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem, counts_dev,
+                   workspace, workspace_bytes, stream, status_dev, lk);
   cudaGraph_t graph = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s, &graph);
   if (rc != CRV_OK || e != cudaSuccess || !graph) {
@@ -1619,6 +1708,31 @@ extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* ca
   }
   *graph_out = new CrvChainGraph{graph, exec, *p};
   return CRV_OK;
+}
+}  // namespace crv
+
+extern "C" int crv_chain_graph_create(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev,
+                                      const int64_t* ev_keys, const uint32_t* ev_runs, const CrvSteps* st,
+                                      const int64_t* nsteps_dev, const CrvBars* bars, const CrvChannels* ch,
+                                      const CrvPixels* px, const double* tmpl, int32_t tlen, const CrvFinderGeom* g,
+                                      CrvClusters* out, CrvMembers* mem, int64_t* counts_dev, void* workspace,
+                                      int64_t workspace_bytes, void* stream, CrvStatus* status_dev,
+                                      CrvChainGraph** graph_out) {
+  return graph_create(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem,
+                      counts_dev, workspace, workspace_bytes, stream, status_dev, nullptr, graph_out);
+}
+
+extern "C" int crv_chain_graph_create_lookup(const CrvParams* p, const CrvChainCaps* caps, const CrvEvents* ev,
+                                             const int64_t* ev_keys, const uint32_t* ev_runs, const CrvSteps* st,
+                                             const int64_t* nsteps_dev, const CrvBars* bars, const CrvChannels* ch,
+                                             const CrvPixels* px, const double* tmpl, int32_t tlen,
+                                             const CrvFinderGeom* g, CrvClusters* out, CrvMembers* mem,
+                                             int64_t* counts_dev, void* workspace, int64_t workspace_bytes,
+                                             void* stream, CrvStatus* status_dev, const CrvLookupChain* lk,
+                                             CrvChainGraph** graph_out) {
+  if (!lk) return CRV_ERR_ARG;
+  return graph_create(p, caps, ev, ev_keys, ev_runs, st, nsteps_dev, bars, ch, px, tmpl, tlen, g, out, mem,
+                      counts_dev, workspace, workspace_bytes, stream, status_dev, lk, graph_out);
 }
 
 extern "C" int crv_chain_graph_launch(CrvChainGraph* h, void* stream) {

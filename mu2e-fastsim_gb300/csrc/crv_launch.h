@@ -77,6 +77,26 @@ cudaError_t launch_wf_synth(const CrvParams& p, const WfGroups& G, long long ng_
                             const double* g_tdc0, const int32_t* g_maxlen, const int32_t* g_nkept,
                             const WfCluster* cl, const DigiSlots& D, Status* status, cudaStream_t s);
 
+// The lookup-table photon model inside the resident chain: dense rows (row 4 step + SiPM of the output channel; a
+// row of no group has group -1), their arrival counts in the chain's per-(step, SiPM) count array, and the photons
+// written at the offsets the chain gives each row (row_off, -1: not written).
+struct LookupChainWs {
+  CrvSubstepRowsOut rows;
+  int8_t* row_group;
+  long long* count;
+  long long* row_off;
+  long long* nrows;              // device: 4 x the batch's steps
+  uint32_t* seed;                // device copy of the parameter block's seed
+  int64_t* o_step;               // per photon: the step's row (the photon id)
+  double* o_time;                // per photon: arrival time
+};
+cudaError_t lookup_chain_rows(const CrvParams& p, const CrvLookupChain& K, const long long* nsteps_dev,
+                              long long step_cap, const LookupChainWs& w, cudaStream_t s);
+cudaError_t lookup_chain_count(const CrvLookupChain& K, const LookupChainWs& w, long long row_cap, int32_t* count32,
+                               Status* status, cudaStream_t s);
+cudaError_t lookup_chain_emit(const CrvLookupChain& K, const LookupChainWs& w, long long row_cap,
+                              const long long* total, long long cap, Status* status, cudaStream_t s);
+
 template <typename R>
 cudaError_t launch_pulsefit(const CrvParams& p, const WaveIn& W, double* yscr, int max_pulses, const PulseSlots& S,
                             const PfQueue& Q, Status* status, cudaStream_t s);

@@ -202,12 +202,33 @@ __device__ __forceinline__ bool row_ok(const CrvSubstepRows& R, long long r, lon
   return *nsub > 0;
 }
 
+// Rows a launch takes.  The stage entry point takes every row; the resident chain's dense rows (row 4 step + SiPM,
+// every group's rows in one table) take [0, min(nrows, *nrows_dev)) of group gsel, and the seed from *seed_dev (a
+// device copy of the chain's parameter-block seed, so that a captured graph of the chain follows a new seed).
+struct RowSel {
+  const long long* nrows_dev;
+  const int8_t* group;
+  const uint32_t* seed_dev;
+  int gsel;
+};
+
+__device__ __forceinline__ long long sel_nrows(const RowSel& q, long long n) {
+  if (!q.nrows_dev) return n;
+  const long long m = *q.nrows_dev;
+  return m < n ? m : n;
+}
+__device__ __forceinline__ bool sel_row(const RowSel& q, long long r) { return !q.group || q.group[r] == q.gsel; }
+__device__ __forceinline__ uint32_t sel_seed(const RowSel& q, uint32_t seed) { return q.seed_dev ? *q.seed_dev : seed; }
+
 __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count(CrvLookup L, CrvSubstepRows R,
-                                                                           uint32_t seed, long long nrows,
+                                                                           uint32_t seed, long long nrows, RowSel sel,
                                                                            long long* __restrict__ count,
                                                                            Status* status) {
+  seed = sel_seed(sel, seed);
+  nrows = sel_nrows(sel, nrows);
   const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
   for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    if (!sel_row(sel, r)) continue;                          // warp-uniform
     long long nsub;
     long long tot = 0;
     if (row_ok(R, r, &nsub, status)) {
@@ -229,8 +250,9 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count(CrvLo
   }
 }
 
+// o_chan may be null (not written); a row whose offset is negative has no place in the output and is skipped
 __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLookup L, CrvSubstepRows R, uint32_t seed,
-                                                                          long long nrows,
+                                                                          long long nrows, RowSel sel,
                                                                           const long long* __restrict__ offset,
                                                                           const long long* __restrict__ total,
                                                                           long long cap, int64_t* __restrict__ o_step,
@@ -238,8 +260,11 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLoo
                                                                           double* __restrict__ o_time,
                                                                           Status* status) {
   if (*total > cap) return;                                    // reported by the capacity check
+  seed = sel_seed(sel, seed);
+  nrows = sel_nrows(sel, nrows);
   const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
   for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    if (!sel_row(sel, r) || offset[r] < 0) continue;          // warp-uniform
     long long nsub;
     if (!row_ok(R, r, &nsub, status)) continue;               // warp-uniform
     const long long step = R.step[r], chan = R.chan[r];
@@ -282,7 +307,7 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit(CrvLoo
           if (j >= a0) { j -= a0; tb = 1; bn = b1; if (j >= a1) { j -= a1; tb = 2; bn = b2; } }
           const long long q = o + p;
           o_step[q] = step;
-          o_chan[q] = chan;
+          if (o_chan) o_chan[q] = chan;
           o_time[q] = arrival_time(L, seed, step, chan, k0 + owner, tb, bn, j, ot, status);
         }
       }
@@ -495,13 +520,17 @@ __device__ __forceinline__ float arrival_offset_f(const CrvLookup& L, float deca
 
 __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count_f32(CrvLookup L, CrvSubstepRows R,
                                                                                uint32_t seed, long long nrows,
+                                                                               RowSel sel,
                                                                                long long* __restrict__ count,
                                                                                Status* status) {
   extern __shared__ float edges_sm[];
   const EdgesF E = stage_edges_f(L, edges_sm);
   const GeoF g = geo_f(L);
+  seed = sel_seed(sel, seed);
+  nrows = sel_nrows(sel, nrows);
   const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
   for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    if (!sel_row(sel, r)) continue;                          // warp-uniform
     long long nsub;
     long long tot = 0;
     if (row_ok(R, r, &nsub, status)) {
@@ -527,6 +556,7 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_count_f32(C
 
 __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit_f32(CrvLookup L, CrvSubstepRows R,
                                                                               uint32_t seed, long long nrows,
+                                                                              RowSel sel,
                                                                               const long long* __restrict__ offset,
                                                                               const long long* __restrict__ total,
                                                                               long long cap,
@@ -539,8 +569,11 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit_f32(Cr
   const EdgesF E = stage_edges_f(L, edges_sm);
   const GeoF g = geo_f(L);
   const float decay = float(L.fiber_decay_time);
+  seed = sel_seed(sel, seed);
+  nrows = sel_nrows(sel, nrows);
   const long long warps = (long long)gridDim.x * SUB_ROWS_PER_BLOCK;
   for (long long r = (long long)blockIdx.x * SUB_ROWS_PER_BLOCK + warp_in_block(); r < nrows; r += warps) {
+    if (!sel_row(sel, r) || offset[r] < 0) continue;          // warp-uniform
     long long nsub;
     if (!row_ok(R, r, &nsub, status)) continue;
     const RowF w = load_row_f(R, E, r);
@@ -581,7 +614,7 @@ __global__ void __launch_bounds__(SUB_ROWS_PER_BLOCK * 32) k_substep_emit_f32(Cr
           if (j >= a0) { j -= a0; tb = 1; bn = b1; if (j >= a1) { j -= a1; tb = 2; bn = b2; } }
           const long long q = o + p;
           o_step[q] = w.step;
-          o_chan[q] = w.chan;
+          if (o_chan) o_chan[q] = w.chan;
           o_time[q] = w.t0 + double(arrival_offset_f(L, decay, seed, w, k0 + owner, tb, bn, j, ofrac, status));
         }
       }
@@ -673,10 +706,10 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
   if (f32 && esm > 48 * 1024) return CRV_ERR_ARG;
   if (f32) {
     crv::Mark mark_("k_substep_count", s);
-    k_substep_count_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, w.count, S);
+    k_substep_count_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, RowSel{}, w.count, S);
   } else {
     crv::Mark mark_("k_substep_count", s);
-    k_substep_count<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, w.count, S);
+    k_substep_count<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, RowSel{}, w.count, S);
   }
   if (cudaGetLastError() != cudaSuccess) return CRV_ERR_CUDA;
   if (exclusive_scan(w.count, nrows, Identity(), w.offset, w.total, w.parts, s) != cudaSuccess) return CRV_ERR_CUDA;
@@ -686,11 +719,13 @@ extern "C" int crv_substep_photons(const CrvLookup* L, uint32_t seed, const CrvS
   }
   if (f32) {
     crv::Mark mark_("k_substep_emit", s);
-    k_substep_emit_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, w.offset, w.total, cap,
+    k_substep_emit_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, esm, s>>>(*L, *rows, seed, nrows, RowSel{}, w.offset,
+                                                                 w.total, cap,
                                                                  o_step, o_chan, o_time, S);
   } else {
     crv::Mark mark_("k_substep_emit", s);
-    k_substep_emit<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, w.offset, w.total, cap, o_step,
+    k_substep_emit<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(*L, *rows, seed, nrows, RowSel{}, w.offset, w.total,
+                                                            cap, o_step,
                                                             o_chan, o_time, S);
   }
   if (cudaGetLastError() != cudaSuccess) return CRV_ERR_CUDA;
@@ -771,74 +806,82 @@ __global__ void k_lrows_flag(CrvLookupGroup G, CrvLookupSteps S, long long n, in
     flag[i] = in_lgroup(G, S, i) ? 1 : 0;
 }
 
+// The rows of step i (a step of group G) for each simulated SiPM: row index(si, output channel) of O
+template <typename Index>
+__device__ __forceinline__ void lrows_of_step(const CrvLookupGroup& G, const CrvLookupSteps& S, uint32_t seed, long long i,
+                                              const CrvSubstepRowsOut& O, Index index) {
+  const int nsim = G.reflector == 0 ? 4 : 2;
+  const int b = S.bar[i];
+  const double* c = G.center + 3 * b;
+  const double ws[3] = {S.x0[i] - c[0], S.y0[i] - c[1], S.z0[i] - c[2]};
+  const double we[3] = {S.x1[i] - c[0], S.y1[i] - c[1], S.z1[i] - c[2]};
+  double sl[3], el[3];
+  for (int k = 0; k < 3; ++k) {
+    const int ax = G.l2w[3 * b + k];
+    sl[k] = ws[ax];
+    el[k] = we[ax];
+  }
+  if (G.reflector < 0) { sl[2] = -sl[2]; el[2] = -el[2]; }
+  double m, q;
+  particle(G, S.pdg[i], &m, &q);
+  const double p0 = sqrt(S.px0[i] * S.px0[i] + S.py0[i] * S.py0[i] + S.pz0[i] * S.pz0[i]);
+  const double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(S.p1[i] * S.p1[i] + m * m));
+  double beta = 1.0;
+  if (m > 0.0) {
+    const double g = e / m;
+    double b2 = 1.0 - 1.0 / (g * g);
+    b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
+    beta = sqrt(b2);
+  }
+  const double avg_s = G.yield[b] * S.edep[i];
+  const double avg_cs = cerenkov_per_mm(G.ck_scint, G.nck_scint, beta, q) * S.len[i];
+  const double avg_cf = cerenkov_per_mm(G.ck_fiber, G.nck_fiber, beta, q) * S.len[i];
+  const double k = G.speed_k[b];
+  for (int si = 0; si < nsim; ++si) {
+    const int s = G.reflector == 0 ? si : 2 * si;
+    double a[3] = {sl[0], sl[1], sl[2]}, bb[3] = {el[0], el[1], el[2]};
+    if (s == 1 || s == 3) { a[2] = -a[2]; bb[2] = -bb[2]; }
+    if (s == 2 || s == 3) { a[1] = -a[1]; bb[1] = -bb[1]; }
+    const double d[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
+    const double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    double ct = 1.0;
+    if (dl > 0.0) {
+      ct = d[2] / dl;
+      ct = ct < -1.0 ? -1.0 : (ct > 1.0 ? 1.0 : ct);
+    }
+    long long nsub = (long long)(dl / LROW_PRECISION_MM);
+    nsub = nsub > 1 ? nsub : 1;
+    const long long chan_dev = 4ll * b + s;
+    const long long chan_out = 4ll * b + (G.reflector < 0 ? s + 1 : s);
+    const long long o = index(si, chan_out);
+    for (int x = 0; x < 3; ++x) {
+      O.s[3 * o + x] = a[x];
+      O.d[3 * o + x] = d[x];
+    }
+    O.t0[o] = S.t0[i] + k * (a[2] + G.half_length);
+    O.t1[o] = S.t1[i] + k * (bb[2] + G.half_length);
+    O.nsub[o] = nsub;
+    O.beta[o] = beta;
+    O.cos_theta[o] = ct;
+    O.dev[o] = G.dev[chan_dev];
+    O.mu[o] = G.mu[b];
+    O.step[o] = i;
+    O.chan[o] = chan_out;
+    const uint32_t lo = uint32_t(i), hi = uint32_t((unsigned long long)i >> 32);
+    O.n_scint[o] = per_substep(avg_s, nsub, philox(lo, hi, w2_of(ST_LROWS, 0, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+    O.n_ck_s[o] = per_substep(avg_cs, nsub, philox(lo, hi, w2_of(ST_LROWS, 1, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+    O.n_ck_f[o] = per_substep(avg_cf, nsub, philox(lo, hi, w2_of(ST_LROWS, 2, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
+  }
+}
+
 __global__ void k_lrows_fill(CrvLookupGroup G, CrvLookupSteps S, uint32_t seed, long long n,
                              const long long* __restrict__ rank, const long long* __restrict__ total,
                              CrvSubstepRowsOut O) {
   const long long ng = *total;
-  const int nsim = G.reflector == 0 ? 4 : 2;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     if (!in_lgroup(G, S, i)) continue;
-    const int b = S.bar[i];
-    const double* c = G.center + 3 * b;
-    const double ws[3] = {S.x0[i] - c[0], S.y0[i] - c[1], S.z0[i] - c[2]};
-    const double we[3] = {S.x1[i] - c[0], S.y1[i] - c[1], S.z1[i] - c[2]};
-    double sl[3], el[3];
-    for (int k = 0; k < 3; ++k) {
-      const int ax = G.l2w[3 * b + k];
-      sl[k] = ws[ax];
-      el[k] = we[ax];
-    }
-    if (G.reflector < 0) { sl[2] = -sl[2]; el[2] = -el[2]; }
-    double m, q;
-    particle(G, S.pdg[i], &m, &q);
-    const double p0 = sqrt(S.px0[i] * S.px0[i] + S.py0[i] * S.py0[i] + S.pz0[i] * S.pz0[i]);
-    const double e = 0.5 * (sqrt(p0 * p0 + m * m) + sqrt(S.p1[i] * S.p1[i] + m * m));
-    double beta = 1.0;
-    if (m > 0.0) {
-      const double g = e / m;
-      double b2 = 1.0 - 1.0 / (g * g);
-      b2 = b2 < 0.0 ? 0.0 : (b2 > 1.0 ? 1.0 : b2);
-      beta = sqrt(b2);
-    }
-    const double avg_s = G.yield[b] * S.edep[i];
-    const double avg_cs = cerenkov_per_mm(G.ck_scint, G.nck_scint, beta, q) * S.len[i];
-    const double avg_cf = cerenkov_per_mm(G.ck_fiber, G.nck_fiber, beta, q) * S.len[i];
-    const double k = G.speed_k[b];
     const long long r0 = rank[i];
-    for (int si = 0; si < nsim; ++si) {
-      const int s = G.reflector == 0 ? si : 2 * si;
-      double a[3] = {sl[0], sl[1], sl[2]}, bb[3] = {el[0], el[1], el[2]};
-      if (s == 1 || s == 3) { a[2] = -a[2]; bb[2] = -bb[2]; }
-      if (s == 2 || s == 3) { a[1] = -a[1]; bb[1] = -bb[1]; }
-      const double d[3] = {bb[0] - a[0], bb[1] - a[1], bb[2] - a[2]};
-      const double dl = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-      double ct = 1.0;
-      if (dl > 0.0) {
-        ct = d[2] / dl;
-        ct = ct < -1.0 ? -1.0 : (ct > 1.0 ? 1.0 : ct);
-      }
-      long long nsub = (long long)(dl / LROW_PRECISION_MM);
-      nsub = nsub > 1 ? nsub : 1;
-      const long long chan_dev = 4ll * b + s;
-      const long long o = (long long)si * ng + r0;
-      for (int x = 0; x < 3; ++x) {
-        O.s[3 * o + x] = a[x];
-        O.d[3 * o + x] = d[x];
-      }
-      O.t0[o] = S.t0[i] + k * (a[2] + G.half_length);
-      O.t1[o] = S.t1[i] + k * (bb[2] + G.half_length);
-      O.nsub[o] = nsub;
-      O.beta[o] = beta;
-      O.cos_theta[o] = ct;
-      O.dev[o] = G.dev[chan_dev];
-      O.mu[o] = G.mu[b];
-      O.step[o] = i;
-      O.chan[o] = 4ll * b + (G.reflector < 0 ? s + 1 : s);
-      const uint32_t lo = uint32_t(i), hi = uint32_t((unsigned long long)i >> 32);
-      O.n_scint[o] = per_substep(avg_s, nsub, philox(lo, hi, w2_of(ST_LROWS, 0, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
-      O.n_ck_s[o] = per_substep(avg_cs, nsub, philox(lo, hi, w2_of(ST_LROWS, 1, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
-      O.n_ck_f[o] = per_substep(avg_cf, nsub, philox(lo, hi, w2_of(ST_LROWS, 2, 0, 0, uint32_t(chan_dev)), 0u, seed, 0u));
-    }
+    lrows_of_step(G, S, seed, i, O, [&](int si, long long) { return (long long)si * ng + r0; });
   }
 }
 
@@ -910,3 +953,139 @@ extern "C" int crv_lookup_rows(const CrvLookupGroup* G, uint32_t seed, const Crv
   (void)status_dev;
   return cudaGetLastError() == cudaSuccess ? CRV_OK : CRV_ERR_CUDA;
 }
+
+// ---- the lookup-table model inside the resident chain ------------------------------------------------------------
+//
+// Rows are dense: row 4 i + c for step i and output channel c = chan & 3, one table of rows for every group; a row of
+// no group (a SiPM the group does not simulate, a step of no group or with a non-finite time) has group -1.  The
+// counts and the photons then run once per group over the rows of that group (RowSel), with that group's table.
+
+namespace crv {
+
+struct LGroups {
+  CrvLookupGroup g[CRV_LOOKUP_CHAIN_GROUPS];
+  int n;
+};
+
+// rows of every step of the batch; the first thread also writes the row bound and the parameter block's seed
+__global__ void k_lrows_chain(CrvParams p, LGroups K, CrvLookupSteps S, const long long* __restrict__ nsteps_dev,
+                              long long step_cap, CrvSubstepRowsOut O, int8_t* __restrict__ row_group,
+                              long long* __restrict__ nrows, uint32_t* __restrict__ seed_dev) {
+  long long n = *nsteps_dev;
+  n = n < step_cap ? (n > 0 ? n : 0) : step_cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *nrows = 4 * n;
+    *seed_dev = p.seed;
+  }
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    for (int c = 0; c < 4; ++c) row_group[4 * i + c] = -1;
+    int gi = -1;
+    for (int k = 0; k < K.n && gi < 0; ++k)
+      if (in_lgroup(K.g[k], S, i)) gi = k;
+    if (gi < 0) continue;
+    lrows_of_step(K.g[gi], S, p.seed, i, O, [&](int, long long chan) {
+      const long long o = 4 * i + (chan & 3);
+      row_group[o] = int8_t(gi);
+      return o;
+    });
+  }
+}
+
+// per-row counts into the chain's int32 per-(step, SiPM) counts (0 for rows of no group; a row beyond the int32
+// range is reported and leaves its group, so that no pass writes its photons)
+__global__ void k_lcount_narrow(const long long* __restrict__ nrows_dev, long long cap, int8_t* __restrict__ row_group,
+                                const long long* __restrict__ c64, int32_t* __restrict__ c32, Status* status) {
+  long long n = *nrows_dev;
+  n = n < cap ? n : cap;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    long long v = row_group[r] < 0 ? 0 : c64[r];
+    if (v > 0x7FFFFFFFll) {
+      set_flag(status, CRV_ST_LIMIT);
+      row_group[r] = -1;
+      v = 0;
+    }
+    c32[r] = int32_t(v);
+  }
+}
+
+static CrvSubstepRows rows_in(const CrvSubstepRowsOut& o) {
+  CrvSubstepRows r{};
+  r.s = o.s; r.d = o.d; r.t0 = o.t0; r.t1 = o.t1; r.beta = o.beta; r.theta = nullptr; r.dev = o.dev; r.mu = o.mu;
+  r.nsub = o.nsub; r.step = o.step; r.chan = o.chan; r.n_scint = o.n_scint; r.n_ck_s = o.n_ck_s; r.n_ck_f = o.n_ck_f;
+  r.cos_theta = o.cos_theta;
+  return r;
+}
+
+static size_t edges_smem(const CrvLookup& L) {
+  int nedge = 0;
+  for (int i = 0; i < 7; ++i) nedge += L.nedges[i];
+  return sizeof(float) * size_t(nedge + L.nedges[5] + L.nedges[4]);
+}
+
+static unsigned step_grid(long long n) {
+  const long long blocks = (n + 255) / 256;
+  const long long maxb = (long long)device_info().sms * 8;
+  return (unsigned)(blocks < 1 ? 1 : (blocks < maxb ? blocks : maxb));
+}
+
+static unsigned row_grid(long long nrows) {
+  const long long blocks = (nrows + SUB_ROWS_PER_BLOCK - 1) / SUB_ROWS_PER_BLOCK;
+  const long long maxb = (long long)device_info().sms * 8;
+  return (unsigned)(blocks < 1 ? 1 : (blocks < maxb ? blocks : maxb));
+}
+
+cudaError_t lookup_chain_rows(const CrvParams& p, const CrvLookupChain& K, const long long* nsteps_dev,
+                              long long step_cap, const LookupChainWs& w, cudaStream_t s) {
+  LGroups G{};
+  G.n = K.ngroups;
+  for (int k = 0; k < K.ngroups; ++k) G.g[k] = K.group[k];
+  const unsigned grid = step_grid(step_cap);
+  crv::Mark mark_("k_lrows_chain", s);
+  k_lrows_chain<<<grid, 256, 0, s>>>(p, G, K.steps, nsteps_dev, step_cap, w.rows, w.row_group, w.nrows, w.seed);
+  return cudaGetLastError();
+}
+
+cudaError_t lookup_chain_count(const CrvLookupChain& K, const LookupChainWs& w, long long row_cap, int32_t* count32,
+                               Status* status, cudaStream_t s) {
+  const CrvSubstepRows R = rows_in(w.rows);
+  const unsigned grid = row_grid(row_cap);
+  for (int k = 0; k < K.ngroups; ++k) {
+    const CrvLookup& L = K.table[k];
+    if (L.precision == 1 && edges_smem(L) > 48 * 1024) return cudaErrorInvalidValue;
+    const RowSel sel{w.nrows, w.row_group, w.seed, k};
+    crv::Mark mark_("k_substep_count", s);
+    if (L.precision == 1)
+      k_substep_count_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, edges_smem(L), s>>>(L, R, 0u, row_cap, sel, w.count,
+                                                                              status);
+    else
+      k_substep_count<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(L, R, 0u, row_cap, sel, w.count, status);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  crv::Mark mark_("k_lcount_narrow", s);
+  k_lcount_narrow<<<step_grid(row_cap), 256, 0, s>>>(w.nrows, row_cap, w.row_group, w.count, count32, status);
+  return cudaGetLastError();
+}
+
+cudaError_t lookup_chain_emit(const CrvLookupChain& K, const LookupChainWs& w, long long row_cap,
+                              const long long* total, long long cap, Status* status, cudaStream_t s) {
+  const CrvSubstepRows R = rows_in(w.rows);
+  const unsigned grid = row_grid(row_cap);
+  for (int k = 0; k < K.ngroups; ++k) {
+    const CrvLookup& L = K.table[k];
+    const RowSel sel{w.nrows, w.row_group, w.seed, k};
+    crv::Mark mark_("k_substep_emit", s);
+    if (L.precision == 1)
+      k_substep_emit_f32<<<grid, SUB_ROWS_PER_BLOCK * 32, edges_smem(L), s>>>(L, R, 0u, row_cap, sel, w.row_off,
+                                                                             total, cap, w.o_step, nullptr,
+                                                                             w.o_time, status);
+    else
+      k_substep_emit<<<grid, SUB_ROWS_PER_BLOCK * 32, 0, s>>>(L, R, 0u, row_cap, sel, w.row_off, total, cap,
+                                                              w.o_step, nullptr, w.o_time, status);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace crv

@@ -336,7 +336,7 @@ struct SipmGroups {
   const long long* label;        // SiPM label
   const uint32_t* run;
   const uint32_t* key32;         // draw key per photon (chain) ...
-  const long long* key64;        // ... or per photon as int64 (stage API)
+  const long long* key64;        // ... or per photon as int64 (stage API); neither: the photon's index in its SiPM
   const long long* photon_id;    // photon id per photon (stage API), or null: id = id_base[g] + (key >> 16)
   const long long* id_base;
   const long long* slot_off;     // output slot region of the group
@@ -876,7 +876,7 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
       for (int u = 0; u < 4; ++u) {
         const int i = base + 32 * u + lane_id();
         tv[u] = i < cnt ? ph_time[a + i] : PT(0);
-        kv[u] = i < cnt ? (G.key32 ? G.key32[a + i] : uint32_t(G.key64[a + i])) : 0u;
+        kv[u] = i < cnt ? (G.key32 ? G.key32[a + i] : G.key64 ? uint32_t(G.key64[a + i]) : uint32_t(i)) : 0u;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {

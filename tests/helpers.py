@@ -162,3 +162,10 @@ def window_chi2(win, A, mu, b):
     t, y, m = win
     z = (t - mu) / b
     return float((((y - A * np.exp(-z - np.exp(-z))) * m) ** 2).sum())
+
+
+
+def module_lookup(n_events, seed=0, yield_per_mev=20000.0):
+    """The workload's module with a synthetic lookup table and muon-crossing steps (crvgpu.lookup.synthetic_module_lookup)."""
+    from crvgpu.lookup import synthetic_module_lookup
+    return synthetic_module_lookup(n_events, seed=seed, yield_per_mev=yield_per_mev)

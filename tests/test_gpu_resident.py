@@ -162,3 +162,46 @@ def test_one_graph_serves_every_design_point(setup):
     rc.configure(c)
     _same(rc.run(ds, 5), CH.ChainEngine(geom, cond, c).run(ds, 5))
     assert rc.captures == 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_lookup_model_inside_the_resident_chain(precision):
+    """The resident chain with the lookup-table photon model (crv_chain_lookup; chain.charges with lookup tables,
+    crv/crvfastsim/chain.py:197-213) gives, bit for bit, the clusters of the stage path: chain.charges with the same
+    tables and seed, then the per-stage engine from those charges.  One graph serves a second seed and a second batch
+    (the lookup kernels take the seed from the graph's parameter block)."""
+    import numpy as np
+    import torch
+    from crvgpu import chain as CH
+    from crvgpu.config import ChainConfig
+    from crvgpu.lookup import LookupModel
+    from crvgpu.resident import ChainCaps, ResidentChain
+    from crvgpu.response import upload_steps
+    from tests.helpers import module_lookup
+    geom, cond, tables, lcfg, steps, pdg = module_lookup(300, seed=4)
+    cond.status[[6, 44, 91]] = [1, 4, 2]                    # absent and no data (dropped), compensated (kept)
+    cfg = ChainConfig(lookup=lcfg, precision=precision)
+    ds = upload_steps(steps, nbars=geom.nbars)
+    model = LookupModel(geom, lcfg, tables, cond.deviation, precision=precision)
+    cols = model.upload_steps(steps, pdg)
+    eng = CH.ChainEngine(geom, cond, cfg)
+    caps = ChainCaps(events=ds.nevents, steps=ds.nsteps, photons=1024, charges=1024, slots=1024, digis=1024,
+                     pulses=1024, max_steps_per_event=max(1, ds.max_steps))
+    rc = ResidentChain(eng, caps, real_dtype=torch.float64, graph=True, grow=True, max_grow=8, lookup=model)
+    caps_before = None
+    for seed in (77, 78):
+        if seed == 78:
+            caps_before = rc.captures
+        Q = CH.charges(steps, None, geom, cond, cfg, None, key=seed, tabs=tables, pdg=pdg)
+        assert len(Q["time"]) > 10000
+        dq = {"label": torch.from_numpy(np.asarray(Q["chan"], np.int64)).cuda(),
+              **{k: torch.from_numpy(np.ascontiguousarray(Q[k])).cuda() for k in ("time", "charge", "pe", "photon")}}
+        ref = eng.run(ds, seed, charges=dq)
+        res = rc.run(ds, seed, lookup_steps=cols)
+        assert ref.n_clusters > 0
+        c = res.counts
+        assert (c["charges"], c["digis"], c["waveforms"], c["pulses"], c["hits"]) == \
+            (len(Q["time"]), ref.n_digis, ref.n_waveforms, ref.n_pulses, ref.n_hits)
+        _same(res, ref)
+        _same(rc.run(ds, seed, lookup_steps=cols), ref)      # the same graph again
+    assert rc.captures == caps_before                       # the second seed needed no new capture
