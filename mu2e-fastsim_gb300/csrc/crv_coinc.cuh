@@ -90,6 +90,16 @@ __device__ inline CoincShared coinc_carve(char* b, int hcap) {
 
 __device__ __forceinline__ double cutv(const CoincGeom& G, int c, int k) { return G.cuts[c * 10 + k]; }
 
+// int(v) (truncation) for |v| < 2^31, from the bits: integer instructions instead of an FP64 conversion
+__device__ __forceinline__ int trunc_int(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = int((b >> 52) & 0x7FF) - 1023;
+  if (e < 0) return 0;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+  const int r = int(m >> (52 - e));
+  return (b >> 63) ? -r : r;
+}
+
 // link test of hit/copy a and b (maxd taken from ma, mb)
 __device__ __forceinline__ bool linked(const CoincShared& S, int a, int b, double ma, double mb, double max_dt,
                                        bool opposite, double dt_opp) {
@@ -179,7 +189,7 @@ __device__ void check_coincidence(const CoincGeom& G, const CoincShared& S, cons
   for (int k = 0; k < m; ++k) {
     int h = mem[k];
     cnt[S.layer[h]]++;
-    int cl = int(cutv(G, S.cut[h], CUT_LAYERS));
+    int cl = trunc_int(cutv(G, S.cut[h], CUT_LAYERS));
     nmin = cl < nmin ? cl : nmin;
     nmax = cl > nmax ? cl : nmax;
   }
@@ -195,6 +205,9 @@ __device__ void check_coincidence(const CoincGeom& G, const CoincShared& S, cons
     __syncwarp();
     return;
   }
+  // a combination of nl layers needs nl non-empty layers, and is skipped unless one of its hits asks for at most nl
+  // layers (nmin or more): with fewer non-empty layers than nmin no combination can keep a hit
+  if (nonempty < nmin) return;
   // bucket lists: offsets
   int off[5] = {0, cnt[0], cnt[0] + cnt[1], cnt[0] + cnt[1] + cnt[2], m};
   if (lane_id() == 0) {
@@ -530,7 +543,26 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
             if (pass_) S.filt[nf + __popc(m & ((1u << lane_id()) - 1u))] = h;
             nf += __popc(m);
           }
-        } else
+        } else {
+          // the side's hits bucketed by layer in list order (S.tmp: the previous side's combination buckets are used
+          // up): a hit then scans the hits of its own side and layer only, in list order.  Only those, on this or an
+          // adjacent counter, enter a sum (a hit elsewhere would add +0.0 to every sum, which changes none of them),
+          // so the sums add the same terms in the same order as a scan of the whole list.
+          int lb0 = 0, lb1 = 0, lb2 = 0, lb3 = 0, ns = 0;
+          for (int l = 0; l < 4; ++l) {
+            if (l == 1) lb1 = ns;
+            if (l == 2) lb2 = ns;
+            if (l == 3) lb3 = ns;
+            for (int base = 0; base < nt; base += 32) {
+              const int k = base + lane_id();
+              const int h = k < nt ? S.list[k] : 0;
+              const bool on = k < nt && S.side[h] == side && S.layer[h] == l;
+              const unsigned m = __ballot_sync(0xffffffffu, on);
+              if (on) S.tmp[ns + __popc(m & ((1u << lane_id()) - 1u))] = h;
+              ns += __popc(m);
+            }
+          }
+          __syncwarp();
         for (int base = 0; base < nt; base += 32) {
           int k = base + lane_id();
           bool pass = false;
@@ -539,12 +571,11 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
             if (S.side[h] == side) {
               double same = 0.0, a1 = 0.0, a2 = 0.0;
               double dadj = cutv(G, S.cut[h], CUT_DTADJ);
-              for (int q = 0; q < nt; ++q) {
-                int a = S.list[q];
-                // integer tests first: only hits of this side and layer on this or an adjacent counter enter a sum
-                // (a hit elsewhere would add +0.0 to every sum, which changes none of them), so the FP64 time test
-                // and addition run for those alone
-                if (S.side[a] != side || S.layer[a] != S.layer[h]) continue;
+              const int l = S.layer[h];
+              const int qa = l == 0 ? lb0 : l == 1 ? lb1 : l == 2 ? lb2 : lb3;
+              const int qb = l == 0 ? lb1 : l == 1 ? lb2 : l == 2 ? lb3 : ns;
+              for (int q = qa; q < qb; ++q) {
+                int a = S.tmp[q];
                 const int d = int(S.counter[a]) - int(S.counter[h]);
                 if (d < -1 || d > 1 || fabs(S.t[a] - S.t[h]) > dadj) continue;
                 if (d == 0) same += S.pe[a];
@@ -558,6 +589,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
           unsigned m = __ballot_sync(0xffffffffu, pass);
           if (pass) S.filt[nf + __popc(m & ((1u << lane_id()) - 1u))] = S.list[k];
           nf += __popc(m);
+        }
         }
         __syncwarp();
         int nfs = nf - f0;

@@ -738,6 +738,7 @@ static int digis_run(const CrvParams* p, const CrvChannels* ch, int64_t ncharges
   char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
   size_t dummy;
   DigiWs w = digi_layout(base, ncharges, slot_cap, p->samples_zs, &dummy);
+  if (!out->volt) w.D.volt = nullptr;       // volts not asked for: the slots keep none either
   const long long* lab = reinterpret_cast<const long long*>(label);
   CK(cudaMemsetAsync(w.totals, 0, 8 * sizeof(long long), s));
   CK(cudaMemsetAsync(w.g_maxlen, 0, sizeof(int32_t) * ncharges, s));
@@ -1481,13 +1482,13 @@ static ChainWs chain_layout(char* base, const CrvParams& p, const CrvChainCaps& 
   w.Q.label = k.take<int64_t>(nq);
   w.Q.time = k.take<double>(nq);
   w.Q.charge = k.take<double>(nq);
-  w.Q.pe = k.take<double>(nq);
-  w.Q.photon = k.take<int64_t>(nq);
+  w.Q.pe = nullptr;                        // the chain's later stages read label, time and charge only
+  w.Q.photon = nullptr;
   w.D.chan = k.take<int64_t>(nd);
-  w.D.start = k.take<double>(nd);
-  w.D.tdc0 = k.take<double>(nd);
+  w.D.start = nullptr;                     // the chain's later stages read channel, start TDC and ADC only
+  w.D.tdc0 = nullptr;
   w.D.starttdc = k.take<int64_t>(nd);
-  w.D.volt = k.take<double>(nd * zs);
+  w.D.volt = nullptr;
   w.D.adc = k.take<int16_t>(nd * zs);
   w.w_label = k.take<int64_t>(nd);
   w.w_off = k.take<int64_t>(nd);

@@ -931,6 +931,7 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
                                  const long long* __restrict__ out_off, const double* __restrict__ st,
                                  const double* __restrict__ sv, const long long* __restrict__ sid, double capacitance,
                                  double overvoltage, int fp32, CrvCharges out, long long out_cap) {
+  // out.pe and out.photon may be null (the resident chain reads label, time and charge only): not written
   // FP32-mixed: voltages are FP32 values; charge and PE in FP32 (no FP64 multiply and division per charge)
   const float cap_f = float(capacitance), inv_vov_f = 1.0f / float(overvoltage);
   long long ngroups = *ngroups_dev;
@@ -966,12 +967,12 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
       if (fp32) {
         const float vf = d2f_trunc(v);
         out.charge[o] = f2d(cap_f * vf);
-        out.pe[o] = f2d(vf * inv_vov_f);
+        if (out.pe) out.pe[o] = f2d(vf * inv_vov_f);
       } else {
         out.charge[o] = capacitance * v;
-        out.pe[o] = v / overvoltage;
+        if (out.pe) out.pe[o] = v / overvoltage;
       }
-      out.photon[o] = sid[src];
+      if (out.photon) out.photon[o] = sid[src];
     }
   }
 }

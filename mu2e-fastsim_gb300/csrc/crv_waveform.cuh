@@ -37,7 +37,7 @@ struct DigiSlots {
   double* start;
   double* tdc0;
   long long* starttdc;
-  double* volt;                  // [slots, 12]
+  double* volt;                  // [slots, 12]; null: volts not kept
   int16_t* adc;                  // [slots, 12]
 };
 
@@ -409,11 +409,11 @@ __global__ void __launch_bounds__(256, 3) k_wf_synth(CrvParams p, WfGroups G, co
               int c = i0 + lane_id();
               if constexpr (sizeof(R) == 4) {
                 const float v = c < L ? float(wave[c]) : 0.0f;
-                D.volt[o * zs + lane_id()] = f2d(v);
+                if (D.volt) D.volt[o * zs + lane_id()] = f2d(v);
                 D.adc[o * zs + lane_id()] = adc_of_f(p, v, conv_f, off_f);
               } else {
                 double v = c < L ? double(wave[c]) : 0.0;
-                D.volt[o * zs + lane_id()] = v;
+                if (D.volt) D.volt[o * zs + lane_id()] = v;
                 D.adc[o * zs + lane_id()] = adc_of(p, v);
               }
             }
@@ -452,6 +452,7 @@ struct Digis {
 
 #ifdef CRV_ENGINE_TU
 // Move each group's digis from its slots to the output, ordered by start (stable) within the group.
+// O.start, O.tdc0 and O.volt may be null (the resident chain reads channel, start TDC and ADC only): not written
 __global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D, const long long* __restrict__ out_off,
                                int zs, Digis O, long long out_cap) {
   long long ng = *ng_dev;
@@ -468,12 +469,12 @@ __global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D
     if (__all_sync(0xffffffffu, sorted)) {
       for (int i = lane_id(); i < nd; i += 32) {
         O.chan[o0 + i] = D.chan[s0 + i];
-        O.start[o0 + i] = D.start[s0 + i];
-        O.tdc0[o0 + i] = D.tdc0[s0 + i];
+        if (O.start) O.start[o0 + i] = D.start[s0 + i];
+        if (O.tdc0) O.tdc0[o0 + i] = D.tdc0[s0 + i];
         O.starttdc[o0 + i] = D.starttdc[s0 + i];
       }
       for (long long f = lane_id(); f < (long long)nd * zs; f += 32) {
-        O.volt[o0 * zs + f] = D.volt[s0 * zs + f];
+        if (O.volt) O.volt[o0 * zs + f] = D.volt[s0 * zs + f];
         O.adc[o0 * zs + f] = D.adc[s0 * zs + f];
       }
       continue;
@@ -490,12 +491,12 @@ __global__ void k_digi_compact(const long long* __restrict__ ng_dev, DigiSlots D
       long long o = o0 + r, s = s0 + i;
       if (lane_id() == 0) {
         O.chan[o] = D.chan[s];
-        O.start[o] = D.start[s];
-        O.tdc0[o] = D.tdc0[s];
+        if (O.start) O.start[o] = D.start[s];
+        if (O.tdc0) O.tdc0[o] = D.tdc0[s];
         O.starttdc[o] = D.starttdc[s];
       }
       if (lane_id() < zs) {
-        O.volt[o * zs + lane_id()] = D.volt[s * zs + lane_id()];
+        if (O.volt) O.volt[o * zs + lane_id()] = D.volt[s * zs + lane_id()];
         O.adc[o * zs + lane_id()] = D.adc[s * zs + lane_id()];
       }
     }

@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_synth32(CrvParams p, WfGroups G, 
             if (lane < zs) {
               const int c = i0 + lane;
               const float v = c < L ? wave[c] : 0.0f;
-              D.volt[o * zs + lane] = f2d(v);
+              if (D.volt) D.volt[o * zs + lane] = f2d(v);
               D.adc[o * zs + lane] = adc_of_f(p, v, conv_f, off_f);
             }
             if (lane == 0) {
