@@ -108,6 +108,18 @@ __device__ __forceinline__ bool linked(const CoincShared& S, int a, int b, doubl
   return fabs(S.x[a] - S.x[b]) <= md && fabs(S.t[a] - S.t[b]) < mt;
 }
 
+// The same decision, with an FP32 rejection first: most pairs lie far apart in time, and a time difference that the
+// FP32 copies (truncated: within 2^-23 relative of the FP64 times) put beyond the window by more than four times their
+// rounding bound is beyond it in FP64 too, so only the pairs left go through the FP64 test.  tc: the FP32 copy of item
+// a's time; mt_hi: an FP32 value at least the largest window the pair can have, less 2^-23 relative.
+__device__ __forceinline__ bool linked_fast(const CoincShared& S, int a, float tc, int b, double ma, double mb,
+                                            double max_dt, float mt_hi, bool opposite, double dt_opp) {
+  const float tb = d2f_trunc(S.t[b]);
+  const float d = fabsf(tc - tb);
+  if (d > mt_hi + 4.8e-7f * (fabsf(tc) + fabsf(tb) + mt_hi)) return false;
+  return linked(S, a, b, ma, mb, max_dt, opposite, dt_opp);
+}
+
 // Greedy clustering of items 0..n-1 in list order: item k is hit ids[k] with maxd mds[k].  Writes the cluster of
 // every item into cl_of[k], the items grouped by cluster in join order into out[], and cluster starts into
 // clstart[0..ncl].  Returns the number of clusters.
@@ -122,6 +134,7 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
   const int lane = lane_id();
   for (int k = lane; k < n; k += 32) cl_of[k] = -1;
   __syncwarp();
+  const float mt_hi = d2f_trunc(max_dt + (opposite ? fabs(dt_opp) : 0.0));
   int nout = 0, ncl = 0, first = 0;
   while (true) {
     int seed = -1;
@@ -145,13 +158,15 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
         const bool cand = k < n && cl_of[k] < 0;
         int hc = 0;
         double mc = 0.0;
+        float tc = 0.0f;
         bool link = false;
         if (cand) {
           hc = ids[k];
           mc = mds[k];
+          tc = d2f_trunc(S.t[hc]);
           for (int m = c0; m < nout && !link; ++m) {
             const int it = out[m];
-            link = linked(S, hc, ids[it], mc, mds[it], max_dt, opposite, dt_opp);
+            link = linked_fast(S, hc, tc, ids[it], mc, mds[it], max_dt, mt_hi, opposite, dt_opp);
           }
         }
         unsigned L = __ballot_sync(0xffffffffu, link);
@@ -165,7 +180,7 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
           L &= L - 1u;
           bool t = false;
           if (cand && !link && lane > b) {
-            t = linked(S, hc, ids[nk], mc, mds[nk], max_dt, opposite, dt_opp);
+            t = linked_fast(S, hc, tc, ids[nk], mc, mds[nk], max_dt, mt_hi, opposite, dt_opp);
             link = t;
           }
           L |= __ballot_sync(0xffffffffu, t);
