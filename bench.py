@@ -264,7 +264,7 @@ def uneven_pulse_fit(total, chunk, device="cuda"):
 
 
 def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2048, resident=True, graph=True,
-            express=True):
+            express=True, capacity_jobs=None, policies=("srpt", "slowdown")):
     """Serving loop over a resident step pool: isolated run time measured per job size (each size alone on the idle
     device), saturated capacity (a burst of every job at once), then Poisson arrivals at each of `loads` x capacity
     (jobs log-uniform 1e3 .. pool_events events, knobs drawn per job).  Wall-clock latencies."""
@@ -279,11 +279,12 @@ def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2
     sizes = sorted({int(v) for v in np.geomspace(1000, pool_events, 7)})
     iso = measure_isolated(srv, sizes)
     rng = np.random.default_rng(seed)
-    burst = random_jobs(n_jobs, rng, max_events=pool_events, pool_events=pool_events)
+    # saturated capacity: a burst of capacity_jobs jobs (default n_jobs) of the same distribution, all at once
+    burst = random_jobs(capacity_jobs or n_jobs, rng, max_events=pool_events, pool_events=pool_events)
     t0 = time.perf_counter()
     srv.run(burst, realtime=False)
     cap = sum(j.n_events for j in burst) / (time.perf_counter() - t0)
-    mean_ev = np.mean([j.n_events for j in burst])
+    mean_ev = np.mean([j.n_events for j in random_jobs(4096, np.random.default_rng(seed), max_events=pool_events)])
     out = {"jobs": n_jobs, "slots": len(srv.slots), "express_slot": srv.express, "slot_footprint_gb": srv.footprint / 1e9,
            "slot_engine": ("resident chain, one captured graph per slot re-parameterised per job" if srv.graph else
                            "resident chain, eager") if resident else "per-stage chain",
@@ -296,9 +297,9 @@ def serving(geom, cond, n_jobs, pool_events, loads, seed=5, max_slots=2, chunk=2
                            pool_events=pool_events, rate=load * cap / mean_ev)
         st = latency_stats(srv.run(jobs, realtime=True), iso_table=iso)
         out["loads"][str(load)] = {k2: v for k2, v in st.items() if k2 != "jobs"}
-        # the same arrivals, scheduled to even out the slowdown of small and large jobs
-        sl = latency_stats(srv.run(jobs, realtime=True, policy="slowdown", iso_table=iso), iso_table=iso)
-        out["loads"][str(load)]["slowdown_policy"] = {k2: v for k2, v in sl.items() if k2 != "jobs"}
+        if "slowdown" in policies:          # the same arrivals, scheduled to even out the slowdown of small and large jobs
+            sl = latency_stats(srv.run(jobs, realtime=True, policy="slowdown", iso_table=iso), iso_table=iso)
+            out["loads"][str(load)]["slowdown_policy"] = {k2: v for k2, v in sl.items() if k2 != "jobs"}
     out["captures_while_serving"] = sum(sl.chain.captures for sl in srv.slots if sl.chain is not None) - c0
     srv = pool = None
     return out
@@ -636,6 +637,9 @@ def main():
     ap.add_argument("--lookup-chain-events", type=int, default=16384,
                     help="events of the resident chain with the lookup-table model (0: skip)")
     ap.add_argument("--serve-loads", default="0.5,0.8,0.95", help="offered loads (fractions of the measured capacity)")
+    ap.add_argument("--serve-capacity-jobs", type=int, default=0,
+                    help="jobs of the saturated burst that measures the capacity (0: as many as --serve-jobs)")
+    ap.add_argument("--serve-policies", default="srpt,slowdown", help="scheduling policies run at every load")
     ap.add_argument("--lookup-rows", type=int, default=1 << 20,
                     help="(step, SiPM) rows of the lookup-table photon model measurement (0: skip)")
     ap.add_argument("--lookup-precision", default="both", choices=["both", "fp64", "fp32"],
@@ -971,7 +975,9 @@ def main():
 
     serve = None
     if rank == 0 and args.serve_jobs > 0:
-        serve = serving(geom, cond, args.serve_jobs, args.serve_pool, [float(v) for v in args.serve_loads.split(",")])
+        serve = serving(geom, cond, args.serve_jobs, args.serve_pool, [float(v) for v in args.serve_loads.split(",")],
+                        capacity_jobs=args.serve_capacity_jobs or None,
+                        policies=tuple(args.serve_policies.split(",")))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
