@@ -112,9 +112,8 @@ __device__ __forceinline__ bool linked(const CoincShared& S, int a, int b, doubl
 // FP32 copies (truncated: within 2^-23 relative of the FP64 times) put beyond the window by more than four times their
 // rounding bound is beyond it in FP64 too, so only the pairs left go through the FP64 test.  tc: the FP32 copy of item
 // a's time; mt_hi: an FP32 value at least the largest window the pair can have, less 2^-23 relative.
-__device__ __forceinline__ bool linked_fast(const CoincShared& S, int a, float tc, int b, double ma, double mb,
-                                            double max_dt, float mt_hi, bool opposite, double dt_opp) {
-  const float tb = d2f_trunc(S.t[b]);
+__device__ __forceinline__ bool linked_fast(const CoincShared& S, int a, float tc, int b, float tb, double ma,
+                                            double mb, double max_dt, float mt_hi, bool opposite, double dt_opp) {
   const float d = fabsf(tc - tb);
   if (d > mt_hi + 4.8e-7f * (fabsf(tc) + fabsf(tb) + mt_hi)) return false;
   return linked(S, a, b, ma, mb, max_dt, opposite, dt_opp);
@@ -129,10 +128,18 @@ __device__ __forceinline__ bool linked_fast(const CoincShared& S, int a, float t
 // nothing.  Here the scan goes over 32 items at a time, one per lane: each lane tests its item against the members;
 // the lowest linked lane joins first, the lanes after it re-test against that new member, and so on, which is the
 // sequential scan's order exactly.
+//
+// tfs (n floats of scratch): the items' FP32 times.  The cluster's FP32 time range [lo, hi] rejects, with one test, a
+// candidate that linked_fast would reject against every member: its distance to the range exceeds linked_fast's bound
+// for the largest member time magnitude in the range (the FP32 operations are monotone, so every member's own test
+// would reject it too).
 __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* mds, int n, double max_dt, bool opposite,
-                      double dt_opp, int32_t* cl_of, int32_t* out, int32_t* clstart) {
+                      double dt_opp, int32_t* cl_of, int32_t* out, int32_t* clstart, float* tfs) {
   const int lane = lane_id();
-  for (int k = lane; k < n; k += 32) cl_of[k] = -1;
+  for (int k = lane; k < n; k += 32) {
+    cl_of[k] = -1;
+    tfs[k] = d2f_trunc(S.t[ids[k]]);
+  }
   __syncwarp();
   const float mt_hi = d2f_trunc(max_dt + (opposite ? fabs(dt_opp) : 0.0));
   int nout = 0, ncl = 0, first = 0;
@@ -150,6 +157,7 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
     __syncwarp();
     const int c0 = nout;
     ++nout;
+    float lo = tfs[seed], hi = lo;
     bool grew = true;
     while (grew) {
       grew = false;
@@ -163,11 +171,13 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
         if (cand) {
           hc = ids[k];
           mc = mds[k];
-          tc = d2f_trunc(S.t[hc]);
-          for (int m = c0; m < nout && !link; ++m) {
-            const int it = out[m];
-            link = linked_fast(S, hc, tc, ids[it], mc, mds[it], max_dt, mt_hi, opposite, dt_opp);
-          }
+          tc = tfs[k];
+          const float mg = mt_hi + 4.8e-7f * (fabsf(tc) + fmaxf(fabsf(lo), fabsf(hi)) + mt_hi);
+          if (!(tc - hi > mg) && !(lo - tc > mg))
+            for (int m = c0; m < nout && !link; ++m) {
+              const int it = out[m];
+              link = linked_fast(S, hc, tc, ids[it], tfs[it], mc, mds[it], max_dt, mt_hi, opposite, dt_opp);
+            }
         }
         unsigned L = __ballot_sync(0xffffffffu, link);
         while (L) {
@@ -178,9 +188,12 @@ __device__ int greedy(const CoincShared& S, const int32_t* ids, const double* md
           ++nout;
           grew = true;
           L &= L - 1u;
+          const float tn = tfs[nk];
+          lo = fminf(lo, tn);
+          hi = fmaxf(hi, tn);
           bool t = false;
           if (cand && !link && lane > b) {
-            t = linked_fast(S, hc, tc, ids[nk], mc, mds[nk], max_dt, mt_hi, opposite, dt_opp);
+            t = linked_fast(S, hc, tc, ids[nk], tn, mc, mds[nk], max_dt, mt_hi, opposite, dt_opp);
             link = t;
           }
           L |= __ballot_sync(0xffffffffu, t);
@@ -611,7 +624,8 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
         if (nfs == 0) continue;
         for (int k = lane_id(); k < nfs; k += 32) W.fmd[k] = cutv(G, S.cut[S.filt[f0 + k]], CUT_D0);
         __syncwarp();
-        int ncl1 = greedy(S, S.filt + f0, W.fmd, nfs, G.type_maxdt[ti], false, 0.0, S.cl_of, S.clus, W.clstart);
+        int ncl1 = greedy(S, S.filt + f0, W.fmd, nfs, G.type_maxdt[ti], false, 0.0, S.cl_of, S.clus, W.clstart,
+                          reinterpret_cast<float*>(S.order));
         for (int c = 0; c < ncl1; ++c) {
           int a = W.clstart[c], b = W.clstart[c + 1];
           for (int k = lane_id(); k < b - a; k += 32) S.order[k] = S.filt[f0 + S.clus[a + k]];
@@ -642,7 +656,8 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
       if (nc == 0) continue;
       bool both = G.type_side0[ti] && G.type_side1[ti];
       double dt_opp = 2.0 * G.type_half[ti] / p.fiber_signal_speed;
-      int ncl2 = greedy(S, S.coinc, W.cmd, nc, G.type_maxdt[ti], both, dt_opp, W.ccl, S.clus, W.cstart);
+      int ncl2 = greedy(S, S.coinc, W.cmd, nc, G.type_maxdt[ti], both, dt_opp, W.ccl, S.clus, W.cstart,
+                        reinterpret_cast<float*>(S.order));
       // attachment of filtered first pulses on missing opposite counter ends
       int natt = 0;
       if (both && p.add_opposite) {
