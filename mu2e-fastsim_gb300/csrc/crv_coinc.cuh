@@ -626,7 +626,26 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
         __syncwarp();
         int ncl1 = greedy(S, S.filt + f0, W.fmd, nfs, G.type_maxdt[ti], false, 0.0, S.cl_of, S.clus, W.clstart,
                           reinterpret_cast<float*>(S.order));
-        for (int c = 0; c < ncl1; ++c) {
+        // clusters one per lane first: one with fewer non-empty layers than its smallest layer cut keeps no hit (as
+        // check_coincidence finds), so only the others go through the check, in cluster order
+        for (int cb = 0; cb < ncl1; cb += 32) {
+         bool live = false;
+         if (cb + lane_id() < ncl1) {
+           const int c = cb + lane_id();
+           unsigned lmask = 0;
+           int nmin = 1 << 30;
+           for (int z = W.clstart[c]; z < W.clstart[c + 1]; ++z) {
+             const int h = S.filt[f0 + S.clus[z]];
+             lmask |= 1u << S.layer[h];
+             const int cl = trunc_int(cutv(G, S.cut[h], CUT_LAYERS));
+             nmin = cl < nmin ? cl : nmin;
+           }
+           live = __popc(lmask) >= nmin;
+         }
+         unsigned lm = __ballot_sync(0xffffffffu, live);
+         while (lm) {
+          const int c = cb + __ffs(lm) - 1;
+          lm &= lm - 1u;
           int a = W.clstart[c], b = W.clstart[c + 1];
           for (int k = lane_id(); k < b - a; k += 32) S.order[k] = S.filt[f0 + S.clus[a + k]];
           __syncwarp();
@@ -651,6 +670,7 @@ __global__ void __launch_bounds__(CO_WARPS_MAX * 32) k_coinc(CrvParams p, CoincG
           nk = warp_sum(nk);
           __syncwarp();
           nc += nk;
+         }
         }
       }
       if (nc == 0) continue;

@@ -370,10 +370,12 @@ struct SipmShared {
   int tcap;                      // afterpulse queue length
 };
 
+// loc: the photons' positions in the group are kept (ph_loc), for per-photon ids (photon_id); without them a warp
+// needs 4 bytes less per photon and more warps fit an SM
 template <typename R>
-__host__ __device__ inline size_t sipm_smem_per_warp(int cap) {
+__host__ __device__ inline size_t sipm_smem_per_warp(int cap, bool loc = true) {
   size_t b = 0;
-  b += size_t(cap) * (sizeof(R) + 8);          // ph_t, ph_key, ph_loc
+  b += size_t(cap) * (sizeof(R) + (loc ? 8 : 4));   // ph_t, ph_key, ph_loc
   b += NPS_ALLOC * sizeof(R);                  // last
   b += 64 * 4;                                 // bm (53 used)
   b += size_t(sipm_tcap(cap)) * (2 * sizeof(R) + 8 + 2);   // traps
@@ -382,7 +384,7 @@ __host__ __device__ inline size_t sipm_smem_per_warp(int cap) {
 }
 
 template <typename R>
-__device__ SipmShared<R> carve(char* base, int cap) {
+__device__ SipmShared<R> carve(char* base, int cap, bool loc) {
   SipmShared<R> S;
   char* q = base;
   S.last = reinterpret_cast<R*>(q); q += NPS_ALLOC * sizeof(R);
@@ -393,7 +395,8 @@ __device__ SipmShared<R> carve(char* base, int cap) {
   S.tr_uf = reinterpret_cast<R*>(q); q += tcap * sizeof(R);
   S.tr_id = reinterpret_cast<long long*>(q); q += tcap * 8;
   S.ph_key = reinterpret_cast<uint32_t*>(q); q += size_t(cap) * 4;
-  S.ph_loc = reinterpret_cast<uint32_t*>(q); q += size_t(cap) * 4;
+  S.ph_loc = loc ? reinterpret_cast<uint32_t*>(q) : nullptr;
+  if (loc) q += size_t(cap) * 4;
   S.bm = reinterpret_cast<uint32_t*>(q); q += 64 * 4;
   S.misc = reinterpret_cast<int*>(q); q += 16;
   S.tr_pix = reinterpret_cast<uint16_t*>(q); q += tcap * 2;
@@ -797,7 +800,7 @@ __device__ void sort_photons(const SipmShared<R>& S, int n) {
   for (int i = n + lane_id(); i < P; i += 32) {
     S.ph_t[i] = R(INFINITY);
     S.ph_key[i] = 0xFFFFFFFFu;
-    S.ph_loc[i] = 0xFFFFFFFFu;
+    if (S.ph_loc) S.ph_loc[i] = 0xFFFFFFFFu;
   }
   __syncwarp();
   for (int size = 2; size <= P; size <<= 1) {
@@ -811,8 +814,10 @@ __device__ void sort_photons(const SipmShared<R>& S, int n) {
         if (after(ta, ka, tb, kb) == up) {
           S.ph_t[lo] = tb; S.ph_t[hi] = ta;
           S.ph_key[lo] = kb; S.ph_key[hi] = ka;
-          uint32_t la = S.ph_loc[lo];
-          S.ph_loc[lo] = S.ph_loc[hi]; S.ph_loc[hi] = la;
+          if (S.ph_loc) {
+            uint32_t la = S.ph_loc[lo];
+            S.ph_loc[lo] = S.ph_loc[hi]; S.ph_loc[hi] = la;
+          }
         }
       }
       __syncwarp();
@@ -831,7 +836,8 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
   for (int i = threadIdx.x; i < 64; i += blockDim.x) dead[i] = i < DEAD_WORDS ? px.dead_bits[i] : 0u;
   if (threadIdx.x == 0) K = sipm_consts<R>(p);
   __syncthreads();
-  SipmShared<R> S = carve<R>(smem + size_t(warp_in_block()) * sipm_smem_per_warp<R>(cap), cap);
+  const bool loc = G.photon_id != nullptr;
+  SipmShared<R> S = carve<R>(smem + size_t(warp_in_block()) * sipm_smem_per_warp<R>(cap, loc), cap, loc);
   for (int q = 0; q < 2; ++q)
     if (G.guard[q] && *G.guard[q] > G.guard_cap[q]) return;
   const long long ngroups = *G.n;
@@ -889,7 +895,7 @@ __global__ void __launch_bounds__(512) k_sipm_sim(CrvParams p, CrvPixels px, Sip
           const int o = n + __popc(km & lanemask_lt());
           S.ph_t[o] = R(tv[u]);
           S.ph_key[o] = kv[u];
-          S.ph_loc[o] = uint32_t(i);
+          if (loc) S.ph_loc[o] = uint32_t(i);
         }
         n += __popc(km);
       }
