@@ -942,12 +942,29 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
   const float cap_f = float(capacitance), inv_vov_f = 1.0f / float(overvoltage);
   long long ngroups = *ngroups_dev;
   long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long g = blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block(); g < ngroups; g += warps) {
-    int nm = nmain[g], na = nap[g];
-    if (nm + na > slot_cap[g]) continue;          // overflowed group: reported through the status
-    long long s0 = slot_off[g], o0 = out_off[g];
-    if (o0 + nm + na > out_cap) continue;
-    long long lab = glabel[g];
+  // groups in tiles of 32 per warp: one coalesced load of their sizes and offsets, then the non-empty ones in order
+  for (long long g0 = (blockIdx.x * (long long)(blockDim.x >> 5) + warp_in_block()) * 32; g0 < ngroups;
+       g0 += warps * 32) {
+   const long long gl = g0 + lane_id();
+   int nm_l = 0, na_l = 0;
+   long long s0_l = 0, o0_l = 0, lab_l = 0;
+   bool ok = false;
+   if (gl < ngroups) {
+     nm_l = nmain[gl];
+     na_l = nap[gl];
+     s0_l = slot_off[gl];
+     o0_l = out_off[gl];
+     lab_l = glabel[gl];
+     // an overflowed group (reported through the status) or one beyond the output is not written
+     ok = nm_l + na_l > 0 && nm_l + na_l <= slot_cap[gl] && o0_l + nm_l + na_l <= out_cap;
+   }
+   unsigned todo = __ballot_sync(0xffffffffu, ok);
+   while (todo) {
+    const int bsel = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int nm = __shfl_sync(0xffffffffu, nm_l, bsel), na = __shfl_sync(0xffffffffu, na_l, bsel);
+    const long long s0 = __shfl_sync(0xffffffffu, s0_l, bsel), o0 = __shfl_sync(0xffffffffu, o0_l, bsel);
+    const long long lab = __shfl_sync(0xffffffffu, lab_l, bsel);
     // rank of each record in the merged order: main i -> i + #(ap with t < t_main_i);
     // ap j -> j + #(main with t <= t_ap_j)
     for (int i = lane_id(); i < nm + na; i += 32) {
@@ -980,6 +997,7 @@ __global__ void k_charge_compact(const long long* __restrict__ ngroups_dev, cons
       }
       if (out.photon) out.photon[o] = sid[src];
     }
+   }
   }
 }
 
