@@ -40,7 +40,8 @@ def test_fp32_rejection_never_drops_a_link():
         for fused in (False, True):
             reject = diff > bound(tc, tm, mt_hi, fused)
             assert not np.any(reject & linked64), (scale, fused, int(np.sum(reject & linked64)))
-            assert np.mean(reject[~linked64]) > 0.5              # and it does reject the pairs beyond the window
+            far = np.abs(ta - tb) > 1.01 * max_dt              # and it rejects the pairs clearly beyond the window
+            assert np.mean(reject[far]) > 0.999, (scale, fused)
         # the cluster range test: a candidate beyond [lo, hi] by the bound at the largest member magnitude
         lo = np.minimum(tm, tm - np.abs(rng.normal(0, 1, n)).astype(np.float32))
         hi = tm
