@@ -54,11 +54,18 @@ def tdc0_per_feb(labels, cond, rng, width=PERIOD, key="roc_feb", *, seed=None, r
 def reco_waveforms(D, cond):
     """Digis -> reco waveform rows with calibration, sorted by (event, channel, start) (pulsefit.concat_waveforms'
     grouping; host glue as in the reference)."""
-    ev, ch = D["chan"] // CHAN_MULT, D["chan"] % CHAN_MULT
-    o = np.lexsort((D["starttdc"], ch, ev))
-    ev, ch, st = ev[o], ch[o], D["starttdc"][o]
-    adc = np.asarray(D["adc"])[o]
-    lens = np.full(len(o), adc.shape[1] if adc.ndim == 2 else 12, np.int64)
+    lab, std = np.asarray(D["chan"]), np.asarray(D["starttdc"])
+    ev, ch = lab // CHAN_MULT, lab % CHAN_MULT
+    # (event, channel) order is label order; chain.digis returns (label, start) order already, which the stable sort
+    # would keep as it is
+    ordered = len(lab) < 2 or bool(np.all((lab[1:] > lab[:-1]) | ((lab[1:] == lab[:-1]) & (std[1:] >= std[:-1]))))
+    if ordered:
+        st, adc = std, np.asarray(D["adc"])
+    else:
+        o = np.lexsort((std, ch, ev))
+        ev, ch, st = ev[o], ch[o], std[o]
+        adc = np.asarray(D["adc"])[o]
+    lens = np.full(len(lab), adc.shape[1] if adc.ndim == 2 else 12, np.int64)
     gid, mat, n, start, first = concat_waveforms(ev, ch // 4, ch % 4, st, adc.ravel(), lens)
     c0 = ch[first]
     return {"ev": ev[first], "bar": c0 // 4, "sipm": c0 % 4, "chan": c0, "adc": mat, "n": n, "start": start,

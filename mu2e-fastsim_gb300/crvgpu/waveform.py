@@ -142,12 +142,12 @@ def charge_clusters(chan, time, wcfg: WaveformConfig):
     return np.cumsum(new) - 1, np.flatnonzero(new)
 
 
-def cluster_table(chan, time, tdc0_cluster, wcfg: WaveformConfig, tmpl):
+def cluster_table(chan, time, tdc0_cluster, wcfg: WaveformConfig, tmpl, clusters=None):
     """The reference's per-cluster outputs (waveform.py:118-121, 169-172): cluster_chan, cluster_tstart (the first
     FEB tick after the first charge - one period: ceil((t_first - P - TDC0) / P) P + TDC0) and cluster_keep (charges x
     template maximum >= min_voltage), for every cluster, kept or not.  The device forms the same start with the same
-    operations for the clusters it synthesises."""
-    cid, first = charge_clusters(chan, time, wcfg)
+    operations for the clusters it synthesises.  clusters: charge_clusters' result when the caller has it."""
+    cid, first = clusters if clusters is not None else charge_clusters(chan, time, wcfg)
     P = wcfg.period
     nq = np.bincount(cid, minlength=len(first)) if len(first) else np.zeros(0, np.int64)
     t_first = np.asarray(time, np.float64)[first] - P
@@ -177,22 +177,19 @@ def digis(Q, cond, cfg: ChainConfig, rng, key=None, timers=None, *, stock_scan=F
     tabs = DeviceTables(geom, cond, ccfg)
     P = make_params(ccfg, seed, template_len=len(tmpl))
     lab = np.asarray(Q["chan"], np.int64)
-    if len(lab) > 1 and np.any(np.diff(lab) < 0):
-        raise ValueError("charges must be sorted by SiPM label (as chain.charges returns them)")
     ek = er = None
     if runs:
         keys = np.array(sorted(runs), np.int64)
         ek = _dev(keys, np.int64)
         er = _dev(np.array([runs[int(k)] for k in keys], np.int64).astype(np.uint32).view(np.int32), np.int32)
     lab_d = _dev(lab, np.int64)
-    D = engine().run(P, tabs, lab_d, _dev(Q["time"], np.float64), _dev(Q["charge"], np.float64),
-                     _dev(tmpl, np.float64), ek, er)
+    if lab_d.numel() > 1 and bool((lab_d[1:] < lab_d[:-1]).any()):
+        raise ValueError("charges must be sorted by SiPM label (as chain.charges returns them)")
+    time_d = _dev(Q["time"], np.float64)
+    D = engine().run(P, tabs, lab_d, time_d, _dev(Q["charge"], np.float64), _dev(tmpl, np.float64), ek, er)
     out = _host(D)
-    # per-cluster outputs: the keyed TDC0 of each cluster's label (labels are sorted: their distinct values by a scan)
-    labels = lab[np.r_[True, lab[1:] != lab[:-1]]] if len(lab) else lab
-    tdc0_lab = _tdc0_device(P, tabs, _dev(labels, np.int64), ek, er)
-    cid, first = charge_clusters(lab, Q["time"], wcfg)
-    out.update(cluster_table(lab, Q["time"], tdc0_lab[np.searchsorted(labels, lab[first])], wcfg, tmpl))
+    # per-cluster outputs, formed on the device from the uploaded columns with cluster_table's operations
+    out.update(_cluster_table_device(P, tabs, lab_d, time_d, wcfg, tmpl, ek, er))
     timers["waveforms_s"] = timers.get("waveforms_s", 0.0) + _time.perf_counter() - t0
     timers["digis"] = timers.get("digis", 0) + len(out["chan"])
     return out
@@ -200,7 +197,30 @@ def digis(Q, cond, cfg: ChainConfig, rng, key=None, timers=None, *, stock_scan=F
 
 def _dev(a, dt):
     torch = _torch()
-    return torch.from_numpy(np.ascontiguousarray(np.asarray(a).astype(dt))).to("cuda")
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a).astype(dt, copy=False))).to("cuda")
+
+
+def _cluster_table_device(P, tabs, lab_d, time_d, wcfg: WaveformConfig, tmpl, ek=None, er=None):
+    """cluster_table on device columns (label-sorted charges): the same splits and the same FP64 operations, in
+    order, on the device; the keyed TDC0 of each cluster's label (crv_tdc0_per_feb).  Host arrays."""
+    torch = _torch()
+    n = int(lab_d.numel())
+    if n == 0:
+        return {"cluster_chan": np.zeros(0, np.int64), "cluster_tstart": np.zeros(0),
+                "cluster_keep": np.zeros(0, bool)}
+    gap = wcfg.single_pe_max_time + N_DIGI_PERIODS_GAP * wcfg.period
+    new = torch.ones(n, dtype=torch.bool, device=lab_d.device)
+    new[1:] = (lab_d[1:] != lab_d[:-1]) | ((time_d[1:] - time_d[:-1]) > gap)
+    first = torch.nonzero(new).squeeze(1)
+    nq = torch.diff(torch.cat([first, torch.tensor([n], device=first.device)]))
+    cl_lab = lab_d[first].contiguous()
+    tdc0 = _tdc0_device(P, tabs, cl_lab, ek, er, host=False)
+    Pd = float(wcfg.period)
+    t_first = time_d[first] - Pd
+    tstart = torch.ceil((t_first - tdc0) / Pd) * Pd + tdc0
+    keep = nq.to(torch.float64) * float(np.max(tmpl)) >= wcfg.min_voltage
+    return {"cluster_chan": cl_lab.cpu().numpy(), "cluster_tstart": tstart.cpu().numpy(),
+            "cluster_keep": keep.cpu().numpy()}
 
 
 def _geometry_for(cond):
@@ -209,8 +229,8 @@ def _geometry_for(cond):
     return module_geometry(n_modules=max(1, (nb + 63) // 64))
 
 
-def _tdc0_device(P, tabs, labels_d, ek=None, er=None):
-    """Keyed TDC0 of device labels (crv_tdc0_per_feb) -> host array."""
+def _tdc0_device(P, tabs, labels_d, ek=None, er=None, host=True):
+    """Keyed TDC0 of device labels (crv_tdc0_per_feb) -> host array (or the device tensor)."""
     torch = _torch()
     L = _capi.load()
     n = int(labels_d.numel())
@@ -222,7 +242,7 @@ def _tdc0_device(P, tabs, labels_d, ek=None, er=None):
                                    _capi.ptr(out), _stream(), st.ptr), "crv_tdc0_per_feb")
     flags, need = st.read()
     raise_status(flags, need, "crv_tdc0_per_feb")
-    return out[:n].cpu().numpy()
+    return out[:n].cpu().numpy() if host else out[:n]
 
 
 def _part_starts(cid, first, max_charges):
@@ -263,7 +283,7 @@ def synthesize(chan, time, charge, tdc0_of_chan, cfg=WaveformConfig(), window=(0
         ca, cb = cid[a], cid[b - 1] + 1
         cch = chan[first[ca:cb]]
         tdc0_cl[ca:cb] = tdc0_of_chan(cch) if callable(tdc0_of_chan) else np.asarray(tdc0_of_chan)[cch]
-    table = cluster_table(chan, time, tdc0_cl, cfg, tmpl)
+    table = cluster_table(chan, time, tdc0_cl, cfg, tmpl, clusters=(cid, first))
     # the device wants labels ascending: a stable sort keeps every label's time order and its clusters
     lab = chan.astype(np.int64)
     order = None
