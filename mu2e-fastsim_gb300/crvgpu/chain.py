@@ -19,6 +19,7 @@ from .config import (CHAN_MULT, PERIOD, ChainConfig, Conditions, FinderConfig, R
                      from_reference, workload_finder)
 from .params import make_params, validate_sipm, validate_window
 from .pulsefit import PulseEngine, filter_channels, concat_waveforms
+from .pulsefit import engine as _pulse_engine
 from .pulsefit import reconstruct_full as _reconstruct_full
 from .response import (DeviceSteps, DeviceTables, ResponseEngine, _stream, _torch, charges, raise_status,  # noqa: F401
                        seed_of, upload_steps)
@@ -88,6 +89,62 @@ def clusters(W, cond, geom, counters_cfg, cfg: ChainConfig, timers=None, detail=
     G = counters_cfg if counters_cfg is not None and hasattr(counters_cfg, "sector_type") else sector_geom(geom)
     fcfg = cfg.finder if cfg.finder is not None else workload_finder(G.sector_names)
     rcfg = cfg.pulse_reco if cfg.pulse_reco is not None else RecoConfig()
+    adc = np.asarray(W["adc"])
+    if adc.ndim != 2 or adc.shape[0] == 0:
+        return _clusters_host(W, cond, G, fcfg, rcfg, cfg, timers, detail)
+    torch = _torch()
+    up = lambda a, dt: torch.from_numpy(np.ascontiguousarray(  # noqa: E731
+        np.asarray(a).astype(dt, copy=False))).to("cuda")
+    t0 = _time.perf_counter()
+    # reconstruct_full (pulsefit.py:222) -> filter_channels (:228) -> DB time offsets and event t0 (chain.py:317-323),
+    # on the device: the fit returns its pulses in (waveform, sequence) order, so the reference's
+    # lexsort((seq, wf, event)) is a stable sort by event, and none when the waveforms are in event order
+    nw, L = adc.shape
+    n = np.asarray(W["n"])
+    Pp = make_params(reco=rcfg, precision=cfg.precision)
+    Pp.period = getattr(rcfg, "period", PERIOD)
+    res = _pulse_engine().run(Pp, torch.arange(nw, dtype=torch.int64, device="cuda") * L, up(n, np.int32),
+                              up(W["start"], np.int64), up(W["ped"], np.float64), up(W["area"], np.float64),
+                              up(W["height"], np.float64), adc64=up(adc, np.int64),
+                              max_pulses=max(rcfg.max_pulses, int(n.max(initial=0))))
+    wf, time, pe, seq = res["wf"], res["time"], res["pe"], res["seq"]
+    if rcfg.ignore_channels:
+        keep = (up(cond.status, np.int64)[up(W["bar"] * 4 + W["sipm"], np.int64)[wf]] & 0b010) == 0
+        wf, time, pe, seq = wf[keep], time[keep], pe[keep], seq[keep]
+    if rcfg.use_time_offset_db:
+        time = time + up(W["toff"], np.float64)[wf] * rcfg.time_offset_scale
+    if "event_t0" in W:
+        time = time + up(W["event_t0"], np.float64)[wf]
+    ev = up(W["ev"], np.int64)[wf]
+    if ev.numel() > 1 and bool((ev[1:] < ev[:-1]).any()):
+        o = torch.sort(ev, stable=True).indices
+        ev, wf, time, pe, seq = ev[o], wf[o], time[o], pe[o], seq[o]
+    torch.cuda.synchronize()
+    timers["pulses_s"] = timers.get("pulses_s", 0.0) + _time.perf_counter() - t0
+    t0 = _time.perf_counter()
+    u, cnt = torch.unique_consecutive(ev, return_counts=True)
+    start = torch.cumsum(cnt, 0) - cnt
+    status = up(cond.status, np.int32)
+    cl, mem = CO.engine().run(make_params(finder=fcfg), CO.FinderTables(G, fcfg), start, cnt.to(torch.int32), u,
+                              up(W["bar"], np.int32)[wf], up(W["sipm"], np.int32)[wf], seq.to(torch.int32), time, pe,
+                              status)
+    cl = {k: v.cpu().numpy() for k, v in cl.items()}
+    mem = {k: v.cpu().numpy() for k, v in mem.items()}
+    timers["coinc_s"] = timers.get("coinc_s", 0.0) + _time.perf_counter() - t0
+    timers["pulses"] = timers.get("pulses", 0) + int(ev.numel())
+    pulses = None
+    if detail:
+        wf_h, ev_h = wf.cpu().numpy(), ev.cpu().numpy()
+        st_h, cnt_h = start.cpu().numpy(), cnt.cpu().numpy()
+        pulses = dict(ev=ev_h, idx=np.arange(len(ev_h)) - np.repeat(st_h, cnt_h), bar=W["bar"][wf_h],
+                      sipm=W["sipm"][wf_h], seq=seq.cpu().numpy(), pe=pe.cpu().numpy(), time=time.cpu().numpy())
+    return [_cluster_out(cl, mem, detail, pulses)], timers
+
+
+def _clusters_host(W, cond, G, fcfg, rcfg, cfg, timers, detail):
+    """clusters for a batch with no reco waveforms (or a non-matrix ADC table): the host sequence of the reference's
+    calls, each on the GPU."""
+    from . import coinc as CO
     t0 = _time.perf_counter()
     P = _reconstruct_full(W["adc"], W["n"], W["start"], W["ped"], W["area"], W["height"], rcfg,
                           precision=cfg.precision)
@@ -107,14 +164,18 @@ def clusters(W, cond, geom, counters_cfg, cfg: ChainConfig, timers=None, detail=
     cl, mem = CO.find_events(ev, idx, bar, sipm, time, pe, seq, G, cond.status, fcfg)
     timers["coinc_s"] = timers.get("coinc_s", 0.0) + _time.perf_counter() - t0
     timers["pulses"] = timers.get("pulses", 0) + len(ev)
+    pulses = dict(ev=ev, idx=idx, bar=bar, sipm=sipm, seq=seq, pe=pe, time=time) if detail else None
+    return [_cluster_out(cl, mem, detail, pulses)], timers
+
+
+def _cluster_out(cl, mem, detail, pulses):
     out = {"cl_event": cl["event"], "cl_type": cl["type"].astype(np.int64), "cl_pe": cl["pe"], "cl_start": cl["start"],
            "cl_end": cl["end"], "cl_slope": cl["slope"], "cl_avgtime": cl["avgtime"],
            "cl_poscalc": cl["poscalc"].astype(bool)}
     if detail:
         out.update({"mem_cl": mem["cl"], "mem_idx": mem["idx"].astype(np.int64), "mem_event": mem["event"],
-                    "cl_pos": cl["pos"], "pulses": dict(ev=ev, idx=idx, bar=bar, sipm=sipm, seq=seq, pe=pe,
-                                                          time=time)})
-    return [out], timers
+                    "cl_pos": cl["pos"], "pulses": pulses})
+    return out
 
 
 # ---------------------------------------------------------------------------------------------------------------------

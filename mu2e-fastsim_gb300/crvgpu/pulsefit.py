@@ -235,7 +235,8 @@ def filter_channels(pulses, channels, status, cfg=RecoConfig()):
 
 def concat_waveforms(key, bar, sipm, start_tdc, adc_flat, lens):
     """Consecutive digis of one channel whose TDCs continue are one waveform: (group id per digi, padded ADC matrix,
-    valid lengths, start TDC and first digi index per group)."""
+    valid lengths, start TDC and first digi index per group).  Digis of one length L (the digitizer's fixed sample
+    count) are copied as whole rows of L samples into a (groups, digis per group, L) view of the matrix."""
     nd = len(bar)
     lens = np.asarray(lens, np.int64)
     cont = np.zeros(nd, bool)
@@ -244,8 +245,22 @@ def concat_waveforms(key, bar, sipm, start_tdc, adc_flat, lens):
                     & (start_tdc[1:] == start_tdc[:-1] + lens[:-1]))
     gid = np.cumsum(~cont) - 1
     G = int(gid[-1]) + 1 if nd else 0
-    glen = np.bincount(gid, weights=lens, minlength=G).astype(np.int64)
     first = np.flatnonzero(~cont)
+    adc_flat = np.asarray(adc_flat)
+    if nd and int(lens.min()) == int(lens.max()) and int(lens[0]) > 0 and adc_flat.size == nd * int(lens[0]):
+        L = int(lens[0])
+        ndig = np.diff(np.append(first, nd))
+        glen = ndig * L
+        rows = adc_flat.reshape(nd, L)
+        if int(ndig.max()) == 1:
+            mat = rows.astype(np.int64)
+        else:
+            pos = np.arange(nd) - np.repeat(first, ndig)
+            mat = np.zeros((G, int(ndig.max()), L), np.int64)
+            mat[gid, pos] = rows
+            mat = mat.reshape(G, -1)
+        return gid, mat, glen, start_tdc[first], first
+    glen = np.bincount(gid, weights=lens, minlength=G).astype(np.int64)
     begin = np.cumsum(lens) - lens
     offs = begin - begin[first][gid] if nd else np.zeros(0, np.int64)
     mat = np.zeros((G, int(glen.max()) if G else 0), np.int64)

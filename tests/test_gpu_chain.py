@@ -106,3 +106,38 @@ def test_chain_end_to_end_matches_oracle_chain(chain_run):
     assert np.array_equal(out["mem_idx"], host(res.members["idx"]))
     np.testing.assert_allclose(out["cl_avgtime"], host(res.clusters["avgtime"]), rtol=1e-9, atol=1e-9)
     assert res.n_events == 160 and res.n_hits == len(out["pulses"]["ev"])
+
+
+def test_dropin_clusters_device_glue_equals_host_sequence_and_oracle(chain_run):
+    """chain.clusters (crv/crvfastsim/chain.py:296-330) on reco waveforms: its device glue (fit, ignored channels,
+    DB time offsets, event t0, event order, finder input) equals the host sequence of the reference's calls
+    (reconstruct_full -> filter_channels -> lexsort -> find_events) bit for bit, with the waveform rows in event order
+    and shuffled, and the clusters equal the oracle chain's."""
+    from crvgpu import chain as CH
+    from crvgpu import config as CF
+    geom, cond, cfg, steps, eng, res, G = chain_run
+    D = {k: host(v) for k, v in res.digis.items()}
+    Wo = O.reco_waveforms(D, cond)
+    rng = np.random.default_rng(4)
+    perm = rng.permutation(len(Wo["n"]))
+    shuffled = {k: (v[perm] if isinstance(v, np.ndarray) and len(v) == len(perm) else v) for k, v in Wo.items()}
+    with_t0 = {**Wo, "event_t0": rng.uniform(-3, 3, len(Wo["n"]))}
+    fcfg = CF.FinderConfig()
+    rcfg = CF.RecoConfig()
+    ccfg = CF.ChainConfig(finder=fcfg, pulse_reco=rcfg)
+    for W in (Wo, shuffled, with_t0):
+        dev, tm = CH.clusters(W, cond, geom, G, ccfg, detail=True)
+        hst, _ = CH._clusters_host(W, cond, G, fcfg, rcfg, ccfg, {}, True)
+        dev, hst = dev[0], hst[0]
+        assert tm["pulses"] == len(hst["pulses"]["ev"]) > 100
+        for k, v in hst.items():
+            if k == "pulses":
+                for q in v:
+                    assert np.array_equal(dev[k][q], v[q]), q
+            else:
+                assert np.array_equal(dev[k], v), k
+    out = O.clusters_from_pulses(Wo, O.pulses_from_waveforms(Wo, cond, rcfg, rcfg.period), G, cond.status, fcfg)
+    got = CH.clusters(Wo, cond, geom, G, ccfg, detail=True)[0][0]
+    assert len(out["cl_event"]) > 0
+    assert np.array_equal(got["cl_event"], out["cl_event"]) and np.array_equal(got["mem_idx"], out["mem_idx"])
+    np.testing.assert_allclose(got["cl_avgtime"], out["cl_avgtime"], rtol=1e-9, atol=1e-9)
