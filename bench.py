@@ -549,6 +549,83 @@ def e2e_dropin(geom, cond, n_events, seed=11, first_event=7_000_000, precision="
             "calls": "chain.charges -> chain.digis -> chain.reco_waveforms -> chain.clusters (host tables)"}
 
 
+def dumper_steps(steps, seed=3):
+    """A synthetic step table in the CrvStepTableDumper layout (run/subrun/event unsigned, nstep/bar/sp int, t0/t1
+    double, start/end positions and the rest float), whose midpoints are the workload's steps."""
+    rng = np.random.default_rng(seed)
+    n = len(steps["bar"])
+    ev = np.asarray(steps["event"])
+    first = np.r_[True, ev[1:] != ev[:-1]] if n else np.zeros(0, bool)
+    cnt = np.diff(np.r_[np.flatnonzero(first), n])
+    d = {"run": np.asarray(steps["run"]).astype(np.uint32), "subrun": np.asarray(steps["subrun"]).astype(np.uint32),
+         "event": ev.astype(np.uint32), "nstep": np.repeat(cnt, cnt).astype(np.int32),
+         "bar": np.asarray(steps["bar"], np.int32), "sp": np.ones(n, np.int32), "sp_product_id": np.ones(n, np.uint32),
+         "t0": np.asarray(steps["t"], np.float64) - 0.25, "t1": np.asarray(steps["t"], np.float64) + 0.25,
+         "edep": np.asarray(steps["edep"], np.float32)}
+    for a in "xyz":
+        h = rng.uniform(-3, 3, n).astype(np.float32)
+        d[f"{a}0"] = np.asarray(steps[a], np.float32) - h
+        d[f"{a}1"] = np.asarray(steps[a], np.float32) + h
+    for k in ("px0", "py0", "pz0", "p1"):
+        d[k] = rng.normal(0, 300, n).astype(np.float32)
+    d["len"] = np.asarray(steps["len"], np.float32)
+    return d
+
+
+def step_tables(geom, cond, n_events, seed=11, first_event=9_000_000, precision="fp32", reps=3):
+    """Step-table files (tables.write / tables.read: the dumper layout as a ROOT TTree, zlib level 1): write and read
+    throughput on the host, and the file -> clusters sequence (tables.read, then the drop-in chain calls)."""
+    import shutil
+    import tempfile
+    import torch
+    from crvgpu import chain as CH, config as CF, geometry as GM, tables as TB
+    steps = dumper_steps(GM.synthetic_steps(n_events, geom, seed=seed, first_event=first_event))
+    rows = len(steps["bar"])
+    raw = sum(v.nbytes for v in steps.values())
+    tmp = tempfile.mkdtemp(prefix="crvsteps")
+    path = os.path.join(tmp, "crvsteps.bench.root")
+    try:
+        tw = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            TB.write(path, steps, None)
+            tw.append(time.perf_counter() - t0)
+        size = os.path.getsize(path)
+        tr = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            s = TB.read(path, "steps")
+            tr.append(time.perf_counter() - t0)
+        same = all(np.array_equal(s[k], v) for k, v in steps.items())
+        cfg = CF.ChainConfig(precision=precision)
+        G = GM.sector_geom(geom)
+
+        def once():
+            st = TB.read(path, "steps")
+            Q = CH.charges(st, None, geom, cond, cfg, None, key=5)
+            D = CH.digis(Q, cond, cfg, None, key=5, geom=geom)
+            W = CH.reco_waveforms(D, cond)
+            cl, _ = CH.clusters(W, cond, geom, G, cfg)
+            return len(cl[0]["cl_event"])
+        once()
+        te = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ncl = once()
+            torch.cuda.synchronize()
+            te.append(time.perf_counter() - t0)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    w, r, e = min(tw), float(np.median(tr)), float(np.median(te))
+    return {"events": n_events, "rows": rows, "columns": len(steps), "column_bytes": int(raw), "file_bytes": int(size),
+            "compression": "zlib level 1 (ROOT setting 101)", "write_s": w, "read_s": r,
+            "read_rows_per_s": rows / r, "read_mb_per_s": raw / r / 1e6, "write_mb_per_s": raw / w / 1e6,
+            "read_identical": bool(same), "file_to_clusters_events_per_s": n_events / e, "clusters": ncl,
+            "host_threads": min(16, os.cpu_count() or 1),
+            "calls": "tables.read -> chain.charges -> chain.digis -> chain.reco_waveforms -> chain.clusters"}
+
+
 def _cpu_fit_worker(args):
     """Oracle reconstruct_full (the reference's pulse fit restated) on one length bucket of the uneven workload."""
     length, n_wf, seed = args
@@ -633,6 +710,8 @@ def main():
                     help="events of the full-scale per-stage FP32 and FP64 legs")
     ap.add_argument("--dropin-events", type=int, default=16384,
                     help="events of the drop-in (host tables through the stage entry points) end-to-end leg (0: skip)")
+    ap.add_argument("--step-table-events", type=int, default=65536,
+                    help="events of the step-table file leg (tables.write / tables.read, file -> clusters; 0: skip)")
     ap.add_argument("--serve-pool", type=int, default=1 << 18, help="events of the resident step pool")
     ap.add_argument("--lookup-chain-events", type=int, default=16384,
                     help="events of the resident chain with the lookup-table model (0: skip)")
@@ -938,6 +1017,14 @@ def main():
             dropin = {"error": str(exc)[:300]}
         torch.cuda.empty_cache()
 
+    tables_io = None
+    if rank == 0 and args.step_table_events > 0:
+        try:
+            tables_io = step_tables(geom, cond, args.step_table_events)
+        except Exception as exc:                          # shown, not hidden
+            tables_io = {"error": str(exc)[:300]}
+        torch.cuda.empty_cache()
+
     lkchain = None
     if rank == 0 and args.lookup_chain_events > 0:
         try:
@@ -995,7 +1082,7 @@ def main():
                 "fp32_over_fp64": (value / fp64) if fp64 else None,
                 "fp32_vs_fp64": acc,
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-                "e2e_dropin": dropin, "lookup_chain": lkchain,
+                "e2e_dropin": dropin, "step_tables": tables_io, "lookup_chain": lkchain,
                 "gpu_launches": int(launches),
                 "clocks": clk,
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3), "share": round(v[1] / tot_ms, 4)}

@@ -26,6 +26,8 @@
  *                                       mixing adapter's resident CRV chain (mixing/device_crv.py:127-573,
  *                                       mixing/DEVICE_CRV.md "Explicit capacities")
  *   crv_lookup_file_info / _read     <- crvfastsim.response.lookup.load (host memory; crv/crvfastsim/response/lookup.py:149)
+ *   crv_lz4_block_decompress,        <- the "L4" baskets of the ROOT step tables that mu2efastsim.tables.read opens
+ *   crv_xxh64                           through uproot (core/mu2efastsim/tables.py:25-27)
  *
  * Error convention: the return value is a host error code (CRV_OK, CRV_ERR_ARG for invalid arguments, CRV_ERR_CUDA
  * for a failed launch).  Data-dependent conditions are reported in the device status block (CrvStatus): capacity
@@ -610,6 +612,12 @@ typedef struct CrvLookupFileOut {
 int crv_lookup_file_info(const uint8_t *image, int64_t size, CrvLookupFileInfo *info);
 int crv_lookup_file_read(const uint8_t *image, int64_t size, const CrvLookupFileInfo *info,
                          const CrvLookupFileOut *out);
+
+/* ROOT "L4" compression blocks (host code).  crv_lz4_block_decompress decodes one LZ4 block (src, n bytes) into dst
+ * (cap bytes) and returns the bytes written, or a negative status for a malformed block (nothing is read or written
+ * outside the two buffers).  crv_xxh64 is the XXH64 hash ROOT stores, big-endian, in front of each block. */
+int64_t crv_lz4_block_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap);
+uint64_t crv_xxh64(const uint8_t *data, int64_t n, uint64_t seed);
 
 #ifdef __cplusplus
 }

@@ -226,6 +226,8 @@ _SIGS = {
                                     c_i64, c_p, c_p]),
     "crv_lookup_file_info": (c_i32, [c_p, c_i64, P(CrvLookupFileInfo)]),
     "crv_lookup_file_read": (c_i32, [c_p, c_i64, P(CrvLookupFileInfo), P(CrvLookupFileOut)]),
+    "crv_lz4_block_decompress": (c_i64, [c_p, c_i64, c_p, c_i64]),
+    "crv_xxh64": (ctypes.c_uint64, [c_p, c_i64, ctypes.c_uint64]),
     "crv_chain": (c_i32, [P(CrvParams), P(CrvChainCaps), P(CrvEvents), c_p, c_p, P(CrvSteps), c_p, P(CrvBars),
                           P(CrvChannels), P(CrvPixels), c_p, c_i32, P(CrvFinderGeom), P(CrvClusters), P(CrvMembers),
                           c_p, c_p, c_i64, c_p, c_p]),

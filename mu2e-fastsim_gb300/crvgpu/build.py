@@ -26,6 +26,7 @@ UNITS = {
     "crv_static.cu": [],
     "crv_lookup.cu": ["-fmad=false"],
     "crv_tables.cpp": [],                 # host code (lookup-table file reader)
+    "crv_rootio.cpp": [],                 # host code (LZ4 / XXH64 of ROOT step-table baskets)
 }
 
 

@@ -1,0 +1,329 @@
+"""Step-table I/O (core/mu2efastsim/tables.py, crv/crvfastsim/tables.py) on the CPU: the ROOT layer (crvgpu.rootio)
+round-trips every leaf type through uncompressed, zlib, LZMA and LZ4 baskets; the file's records are consistent (the
+header's end and seeks, the key list, the basket byte counts, the tree's leaf references resolving to the branches'
+leaves); the native LZ4 and XXH64 decoders meet their published test values and refuse malformed blocks; and the
+tables helpers (read, read_many, livetime, primary_muons, all_primary_muons, primary_muon_crossings, write in both
+forms) give what the reference's pandas code gives, restated here with plain loops.
+
+Parity with uproot/ROOT themselves is not pinned: neither is installed here and the reference ships no ROOT files.
+"""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from crvgpu import rootio as R
+from crvgpu import tables as TB
+
+
+# ---- a greedy LZ4 block compressor (test side only), to make "L4" baskets the native decoder must read
+
+def _lz4_len(out, v):
+    while v >= 255:
+        out.append(255)
+        v -= 255
+    out.append(v)
+
+
+def _lz4_compress(data):
+    out, table, i, anchor, n = bytearray(), {}, 0, 0, len(data)
+
+    def seq(lit, off=None, m=0):
+        tok_l = min(len(lit), 15)
+        tok_m = 0 if off is None else min(m - 4, 15)
+        out.append((tok_l << 4) | tok_m)
+        if len(lit) >= 15:
+            _lz4_len(out, len(lit) - 15)
+        out.extend(lit)
+        if off is not None:
+            out.extend(off.to_bytes(2, "little"))
+            if m - 4 >= 15:
+                _lz4_len(out, m - 4 - 15)
+
+    while i + 4 <= n - 5:
+        key = bytes(data[i:i + 4])
+        j = table.get(key)
+        table[key] = i
+        if j is not None and i - j <= 65535:
+            m = 4
+            while i + m < n - 5 and data[j + m] == data[i + m]:
+                m += 1
+            seq(data[anchor:i], i - j, m)
+            i += m
+            anchor = i
+        else:
+            i += 1
+    seq(data[anchor:])
+    return bytes(out)
+
+
+def _l4_blocks(raw):
+    from crvgpu import _capi
+    L = _capi.load()
+    out = []
+    for a in range(0, len(raw), R.MAX_BLOCK):
+        chunk = raw[a:a + R.MAX_BLOCK]
+        body = _lz4_compress(chunk)
+        body = L.crv_xxh64(body, len(body), 0).to_bytes(8, "big") + body
+        out.append(R._block(b"L4", 1, chunk, body))
+    z = b"".join(out)
+    return z if len(z) < len(raw) else None
+
+
+def _columns(n, rng):
+    return {"run": np.full(n, 1400, np.uint32), "subrun": rng.integers(0, 9, n).astype(np.uint32),
+            "event": np.arange(n, dtype=np.uint32), "bar": rng.integers(0, 5000, n).astype(np.int32),
+            "t0": rng.uniform(0, 1e3, n), "edep": rng.uniform(0, 5, n).astype(np.float32),
+            "big": rng.integers(-2 ** 62, 2 ** 62, n), "u64": rng.integers(0, 2 ** 63, n).astype(np.uint64),
+            "flag": rng.random(n) < 0.3, "s": rng.integers(-300, 300, n).astype(np.int16),
+            "us": rng.integers(0, 60000, n).astype(np.uint16), "c": rng.integers(-100, 100, n).astype(np.int8),
+            "uc": rng.integers(0, 255, n).astype(np.uint8), "pos": rng.normal(size=(n, 3)),
+            "rep": np.repeat(np.arange(n // 50 + 1), 50)[:n].astype(np.int64)}
+
+
+@pytest.mark.parametrize("mode", ["none", "zlib", "lzma", "lz4"])
+def test_every_leaf_type_round_trips(tmp_path, mode):
+    rng = np.random.default_rng(1)
+    cols = _columns(30011, rng)
+    path = str(tmp_path / f"a_{mode}.root")
+    kw = dict(none=dict(compression=0), zlib=dict(compression=101), lzma=dict(compression=205),
+              lz4=dict(compression=404, _compressor=_l4_blocks))[mode]
+    R.write(path, {"dump/steps": cols, "dump/sub/x": {"v": np.arange(10.0)}, "top": {"k": np.arange(5, dtype=np.int32)},
+                   "dump/empty": {"e": np.zeros(0)}, "dump/none": None}, basket_bytes=16384, **kw)
+    with R.RootFile(path) as f:
+        assert f.keys() == ["top", "dump", "dump/steps", "dump/sub", "dump/sub/x"]
+        T = f["dump/steps"]
+        assert len(T) == 30011 and T.keys() == list(cols)
+        assert T.branches["bar"].write_basket > 10                 # several baskets per branch
+        got = T.arrays()
+        for k, v in cols.items():
+            assert got[k].dtype == v.dtype and got[k].shape == v.shape and np.array_equal(got[k], v), k
+        assert np.array_equal(f["dump/sub/x"].arrays()["v"], np.arange(10.0))
+        assert list(f["top"].arrays(["k"])) == ["k"]
+        assert T.branches["pos"].title == "pos[3]/D" and T.branches["us"].title == "us/s"
+        assert f.compression == (0 if mode == "none" else kw["compression"])
+        with pytest.raises(KeyError):
+            f["dump/nothing"]
+        with pytest.raises(KeyError):
+            T.arrays(["nothing"])
+
+
+def test_file_records_are_consistent(tmp_path):
+    """Header, key list, basket byte counts and the tree's leaf references, read back from the raw bytes."""
+    path = str(tmp_path / "c.root")
+    rng = np.random.default_rng(2)
+    R.write(path, {"dump/steps": _columns(5000, rng)}, basket_bytes=8192)
+    raw = open(path, "rb").read()
+    assert raw[:4] == b"root"
+    version, begin, end, seek_free, nbytes_free, nfree, nbytes_name, units, comp, seek_info, nbytes_info = \
+        struct.unpack_from(">iiiiiiiBiii", raw, 4)
+    assert version == R.ROOT_VERSION and begin == 100 and end == len(raw) and units == 4 and comp == 101
+    assert seek_free + nbytes_free == end and nfree == 1
+    with R.RootFile(path) as f:
+        k = R._key(R._Cursor(f.buf, seek_info))
+        assert (k.classname, k.name, k.nbytes) == ("TList", "StreamerInfo", nbytes_info)
+        top = R._key(R._Cursor(f.buf, begin))
+        assert top.classname == "TFile" and nbytes_name == top.keylen + 2 + len(top.name) + len(top.title)
+        T = f["dump/steps"]
+        leaves = [b.leaves[0] for b in T.branches.values()]
+        assert T.leaves is not None and len(T.leaves) == len(leaves)
+        assert all(a is b for a, b in zip(T.leaves, leaves))       # references resolve to the branches' leaves
+        for b in T.branches.values():
+            for i in range(b.write_basket):
+                bk = R._key(R._Cursor(f.buf, int(b.basket_seek[i])))
+                assert bk.classname == "TBasket" and bk.name == b.name and bk.title == "steps"
+                assert bk.nbytes == b.basket_bytes[i] and bk.seek_key == b.basket_seek[i]
+            assert b.basket_entry[b.write_basket] == 5000 and not b.basket_seek[b.write_basket]
+
+
+def test_big_file_layout_reads_back(tmp_path, monkeypatch):
+    """The 64-bit layout (file version + 1000000, key version 1004, directory version 1005), forced on a small file."""
+    monkeypatch.setattr(R, "START_BIG_FILE", 0)
+    path = str(tmp_path / "big.root")
+    rng = np.random.default_rng(3)
+    cols = _columns(3000, rng)
+    R.write(path, {"dump/steps": cols}, basket_bytes=4096)
+    raw = open(path, "rb").read()
+    assert struct.unpack_from(">i", raw, 4)[0] == R.ROOT_VERSION + 1000000
+    with R.RootFile(path) as f:
+        got = f["dump/steps"].arrays()
+        assert f.get_key("dump/steps").version == 1004
+    for k, v in cols.items():
+        assert np.array_equal(got[k], v), k
+
+
+def test_xxh64_and_lz4_decoders():
+    from crvgpu import _capi
+    L = _capi.load()
+    assert L.crv_xxh64(b"", 0, 0) == 0xEF46DB3751D8E999          # published XXH64 test values
+    assert L.crv_xxh64(b"abc", 3, 0) == 0x44BC2CF5AD770999
+    rng = np.random.default_rng(4)
+    data = bytes(rng.integers(0, 4, 40000).astype(np.uint8)) + b"abcd" * 3000 + bytes(rng.integers(0, 256, 5000)
+                                                                                    .astype(np.uint8)) + b"\0" * 70000
+    blocks = _l4_blocks(data)
+    assert blocks is not None and len(blocks) < len(data) // 2
+    assert R.decompress(blocks, len(data)) == data
+    # malformed blocks: negative status, nothing written past the output buffer
+    import ctypes
+    body = _lz4_compress(data)
+    out = ctypes.create_string_buffer(len(data) + 16)
+    assert L.crv_lz4_block_decompress(body, len(body), out, len(data)) == len(data)
+    assert L.crv_lz4_block_decompress(body, len(body), out, len(data) - 1) < 0        # output too small
+    assert L.crv_lz4_block_decompress(body[:len(body) // 2], len(body) // 2, out, len(data)) != len(data)
+    i, lit = 1, body[0] >> 4                                    # the first sequence's match offset -> 0
+    if lit == 15:
+        while body[i] == 255:
+            lit += 255
+            i += 1
+        lit += body[i]
+        i += 1
+    bad = bytearray(body)
+    bad[i + lit] = bad[i + lit + 1] = 0
+    assert L.crv_lz4_block_decompress(bytes(bad), len(bad), out, len(data)) < 0
+    # a wrong checksum is refused
+    b2 = bytearray(blocks)
+    b2[9] ^= 1
+    with pytest.raises(R.RootFormatError):
+        R.decompress(bytes(b2), len(data))
+
+
+def test_mixed_blocks_and_refusals():
+    raw = bytes(range(256)) * 400
+    z = R._block(b"ZL", 8, raw[:50000], __import__("zlib").compress(raw[:50000])) + \
+        R._block(b"XZ", 0, raw[50000:], __import__("lzma").compress(raw[50000:]))
+    assert R.decompress(z, len(raw)) == raw
+    with pytest.raises(R.RootFormatError, match="zstd"):
+        R.decompress(R._block(b"ZS", 1, b"x" * 10, b"0123"), 10)
+    with pytest.raises(R.RootFormatError):
+        R.decompress(b"ZL\x08\xff\x00\x00", 10)
+
+
+def test_not_a_root_file(tmp_path):
+    p = tmp_path / "x.root"
+    p.write_bytes(b"root")
+    with pytest.raises(R.RootFormatError):
+        R.RootFile(str(p))
+    p.write_bytes(b"notroot" * 20)
+    with pytest.raises(R.RootFormatError):
+        R.RootFile(str(p))
+
+
+def test_unsupported_columns_are_refused(tmp_path):
+    with pytest.raises(TypeError):
+        R.write(str(tmp_path / "u.root"), {"t": {"s": np.array(["a", "b"])}})
+    with pytest.raises(ValueError):
+        R.write(str(tmp_path / "u.root"), {"t": {"a": np.zeros(3), "b": np.zeros(4)}})
+
+
+# ---- the tables API against the reference's pandas semantics, restated with loops
+
+def _dumper_tables(rng, n_events=40):
+    steps, parts, gen = {k: [] for k in ("run", "subrun", "event", "nstep", "bar", "sp", "t0", "t1", "edep",
+                                         "x0", "y0", "z0", "x1", "y1", "z1", "len")}, \
+        {k: [] for k in ("run", "subrun", "event", "key", "parent", "pdg", "isprim")}, \
+        {k: [] for k in ("run", "subrun", "event", "idx", "pdg", "x")}
+    for e in range(n_events):
+        sub = 1 + e // 15
+        nmu = rng.integers(0, 3)
+        for g in range(rng.integers(1, 4)):
+            pdg = 13 if g < nmu else rng.choice([11, 22, -13])
+            for k, v in (("run", 1), ("subrun", sub), ("event", e), ("idx", 2 - g), ("pdg", pdg), ("x", rng.normal())):
+                gen[k].append(v)
+        keys = [1, 2, 5]
+        for kk in keys:
+            for k, v in (("run", 1), ("subrun", sub), ("event", e), ("key", kk), ("parent", -1 if kk == 1 else 1),
+                         ("pdg", 13 if kk == 1 else rng.choice([11, 13])), ("isprim", int(kk == 1))):
+                parts[k].append(v)
+        ns = rng.integers(0, 12)
+        for s in range(ns):
+            vals = dict(run=1, subrun=sub, event=e, nstep=ns, bar=rng.integers(0, 6), sp=rng.choice(keys),
+                        t0=rng.uniform(0, 100), edep=rng.uniform(0, 3), len=rng.uniform(1, 20))
+            vals["t1"] = vals["t0"] + 0.5
+            for a in "xyz":
+                vals[f"{a}0"], vals[f"{a}1"] = rng.normal(), rng.normal()
+            for k in steps:
+                steps[k].append(vals[k])
+    dt = dict(run=np.uint32, subrun=np.uint32, event=np.uint32, nstep=np.int32, bar=np.int32, sp=np.int32,
+              t0=np.float64, t1=np.float64, key=np.int32, parent=np.int32, pdg=np.int32, isprim=np.int32,
+              idx=np.int32, x=np.float64)
+    conv = lambda d: {k: np.asarray(v, dt.get(k, np.float32)) for k, v in d.items()}  # noqa: E731
+    return conv(steps), conv(parts), conv(gen)
+
+
+def test_tables_api_matches_the_reference_semantics(tmp_path, capsys):
+    rng = np.random.default_rng(7)
+    steps, parts, gen = _dumper_tables(rng)
+    subruns = {"run": np.array([1, 1, 1, 1], np.uint32), "subrun": np.array([1, 2, 2, 3], np.uint32),
+               "livetime": np.array([1.5, 2.0, 2.0, 0.25]), "primaries": np.array([10, 20, 20, 3], np.uint64)}
+    p1, p2 = str(tmp_path / "crvsteps.1.root"), str(tmp_path / "crvsteps.2.root")
+    TB.write(p1, steps, parts, gen=gen, subruns=subruns, as_ttree=True)        # crv form
+    TB.write(p2, {"steps": steps, "particles": parts, "subruns": subruns})      # core form
+    assert "wrote" in capsys.readouterr().out
+    s = TB.read(p1, "steps")
+    assert isinstance(s, TB.StepRows) and len(s) == len(steps["bar"]) and s.bar is s["bar"]
+    for k, v in steps.items():
+        assert s[k].dtype == v.dtype and np.array_equal(s[k], v), k
+    both = TB.read_many([str(tmp_path / "crvsteps.*.root")], "steps", ["event", "bar"])
+    assert list(both) == ["event", "bar"] and np.array_equal(both["bar"], np.r_[steps["bar"], steps["bar"]])
+    # livetime: each (run, subrun) once over both files
+    assert TB.livetime([p1, p2]) == pytest.approx(1.5 + 2.0 + 0.25)
+    # primary_muons: first |pdg| == 13 row of each event
+    pm = TB.primary_muons(gen)
+    want, seen = [], set()
+    for i in range(len(gen["pdg"])):
+        key = (gen["run"][i], gen["subrun"][i], gen["event"][i])
+        if abs(gen["pdg"][i]) == 13 and key not in seen:
+            seen.add(key)
+            want.append(i)
+    assert np.array_equal(pm["x"], gen["x"][want])
+    # all_primary_muons: ordered by (run, subrun, event, idx), mukey = 1, 2, ...
+    am = TB.all_primary_muons(gen)
+    rows = sorted([i for i in range(len(gen["pdg"])) if abs(gen["pdg"][i]) == 13],
+                  key=lambda i: (gen["run"][i], gen["subrun"][i], gen["event"][i], gen["idx"][i]))
+    assert np.array_equal(am["x"], gen["x"][rows])
+    mk, cnt = [], {}
+    for i in rows:
+        key = (gen["run"][i], gen["subrun"][i], gen["event"][i])
+        cnt[key] = cnt.get(key, 0) + 1
+        mk.append(cnt[key])
+    assert np.array_equal(am["mukey"], mk)
+    # primary_muon_crossings: inner merge on (run, subrun, event, sp = primary muon key), groups in first-seen order
+    sector_of_bar = np.array([0, 0, 1, 1, 2, 2])
+    cx = TB.primary_muon_crossings(s, TB.read(p1, "particles"), sector_of_bar)
+    prim = {(parts["run"][i], parts["subrun"][i], parts["event"][i], parts["key"][i])
+            for i in range(len(parts["key"])) if parts["isprim"][i] == 1 and abs(parts["pdg"][i]) == 13}
+    groups = {}
+    for i in range(len(steps["bar"])):
+        if (steps["run"][i], steps["subrun"][i], steps["event"][i], steps["sp"][i]) in prim:
+            g = (steps["run"][i], steps["subrun"][i], steps["event"][i], steps["bar"][i])
+            e = groups.setdefault(g, [0.0, 0.0, np.inf, 0])
+            e[0] += float(steps["edep"][i])
+            e[1] += float(steps["len"][i])
+            e[2] = min(e[2], steps["t0"][i])
+            e[3] += 1
+    assert len(groups) > 10 and len(cx) == len(groups)
+    assert [tuple(int(cx[k][j]) for k in ("run", "subrun", "event", "bar")) for j in range(len(cx))] == \
+        [tuple(int(x) for x in g) for g in groups]
+    v = np.array(list(groups.values()))
+    np.testing.assert_allclose(cx["edep"], v[:, 0], rtol=1e-6)
+    np.testing.assert_allclose(cx["len"], v[:, 1], rtol=1e-6)
+    assert np.array_equal(cx["t0"], v[:, 2]) and np.array_equal(cx["nsteps"], v[:, 3])
+    assert np.array_equal(cx["sector"], sector_of_bar[cx["bar"]])
+    assert TB.expand([str(tmp_path / "none.*.root")]) == [str(tmp_path / "none.*.root")]
+    assert os.path.getsize(p1) > 0
+
+
+def test_step_table_feeds_the_engine_host_path(tmp_path):
+    """A dumper-layout steps tree read back goes into the engine's step upload as it is: midpoints from the start/end
+    columns (as the oracle's step frame takes them) and events keyed by (subrun, event)."""
+    from crvgpu import geometry as GM
+    from crvgpu.response import _col
+    rng = np.random.default_rng(8)
+    steps, parts, gen = _dumper_tables(rng, 60)
+    p = str(tmp_path / "s.root")
+    TB.write(p, steps, parts)
+    s = TB.read(p, "steps")
+    assert np.array_equal(GM.event_key(s), (steps["subrun"].astype(np.int64) << 20) | steps["event"])
+    for a in "xyzt":
+        assert np.array_equal(_col(s, a), 0.5 * (steps[f"{a}0"].astype(float) + steps[f"{a}1"].astype(float))), a
