@@ -956,9 +956,9 @@ def main():
 
     # DRAM bytes (read + write) over algorithmic bytes of one 16,384-event chain batch, from single-kernel ncu captures
     # of every launch of the stage in that batch (k_sipm_sim, 3 launches: 3.419 GB over 2.978 GB; k_wf_synth32,
-    # 3 launches: 1.823 GB over 1.405 GB; k_pf_persist, 1 launch: 0.765 GB over 0.396 GB); the traffic of a stage grows
+    # 3 launches: 1.823 GB over 1.405 GB; k_pf_persist, 1 launch: 0.757 GB over 0.396 GB); the traffic of a stage grows
     # with the events processed, so the ratio scales it to this run's batch
-    traffic_ratio = {"k_sipm_sim": 1.148, "k_wf_synth": 1.298, "pulse fit": 1.931}
+    traffic_ratio = {"k_sipm_sim": 1.148, "k_wf_synth": 1.298, "pulse fit": 1.910}
 
     def roofline_of(group):
         ks = groups.get(group, (group,))

@@ -174,6 +174,25 @@ class Conditions:
     deviation: np.ndarray
     readout_mask: Optional[np.ndarray] = None
 
+    @staticmethod
+    def from_csv(calib_csv, photon_csv=None):
+        """Conditions.from_csv (crv/crvfastsim/chain.py:42-51): per-channel CSV rows channel, pedestal, pulsearea,
+        pulseheight, timeoffset, status, roc, feb[, febch] (e.g. dumped from crvdump/calib), dense by channel;
+        yield deviations from an optional channel, deviation CSV."""
+        a = np.loadtxt(calib_csv, delimiter=",", comments="#", ndmin=2)
+        n = int(a[:, 0].max()) + 1 if a.size else 0
+
+        def col(j, dt=float):
+            out = np.zeros(n, dt)
+            if a.size:
+                out[a[:, 0].astype(int)] = a[:, j]
+            return out
+        dev = np.zeros(n)
+        if photon_csv:
+            p = np.loadtxt(photon_csv, delimiter=",", comments="#", ndmin=2)
+            dev[p[:, 0].astype(int)] = p[:, 1]
+        return Conditions(col(1), col(2), col(3), col(4), col(5, np.int64), col(6, np.int64), col(7, np.int64), dev)
+
 
 PRECISIONS = ("fp64", "fp32")
 

@@ -1,0 +1,178 @@
+"""The CrvRecoTableDumper trees (crv/art/CrvFastSim/src/CrvRecoTableDumper_module.cc, read by
+crv/art/CrvFastSim/src/CrvRecoTable.hh): directory ``crvdump/``, rows keyed by (run, subrun, event), channel rows
+with ``idx`` (row index in its art collection), ``bar`` and ``sipm``; jagged columns (ADC samples, voltages, charges,
+waveform and member indices) as std::vector branches (the art dumper) or counted arrays n<name> (the uproot writer).
+
+The reference reads them with crvfastsim.reco.reftables (read, calib, event_key: crv/crvfastsim/reco/reftables.py:
+17-50) into awkward arrays through uproot; here they come back as Tables whose jagged columns are
+crvgpu.rootio.JaggedArray.  On top: `write` (counted arrays, the layout CrvRecoTable.hh's Jagged<T> reads),
+`conditions` (the chain's Conditions from the calib tree, as Conditions.from_csv takes the CSV dumped from it),
+`digis_table` (the engine's digis in the dumper's digis layout) and `waveforms` (dumped digis -> reco waveforms with
+their calibration, the grouping crv/crvfastsim/reco/cli.py:52-74 makes before the pulse fit), so a dumped digi table
+goes into chain.clusters / pulsefit.reconstruct_full as it is.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import rootio
+from .config import CHAN_MULT, Conditions
+from .tables import KEY, Table, expand
+
+DIR = "crvdump"
+TREES = ("events", "charges", "digimc", "digis", "pulses", "clusters", "calib")
+NCHAN_PER_BAR = 4
+
+
+def _concat(parts):
+    out = Table()
+    for k in parts[0]:
+        vs = [p[k] for p in parts]
+        if isinstance(vs[0], rootio.JaggedArray):
+            vals = np.concatenate([v.values for v in vs])
+            offs = np.concatenate([[0]] + [v.offsets[1:] + s for v, s in
+                                           zip(vs, np.cumsum([0] + [len(v.values) for v in vs[:-1]]))])
+            out[k] = rootio.JaggedArray(vals, offs)
+        else:
+            out[k] = np.concatenate(vs)
+    return out
+
+
+def read(paths, tree, columns=None, entry_stop=None):
+    """One tree concatenated over files (patterns expanded; files without it are skipped); None when no file has it."""
+    parts = []
+    for p in expand(paths if isinstance(paths, (list, tuple)) else [paths]):
+        with rootio.RootFile(p) as f:
+            try:
+                T = f[f"{DIR}/{tree}"]
+            except KeyError:
+                continue
+            cols = T.arrays(columns)
+        if entry_stop is not None:
+            cols = {k: (v.take(slice(0, entry_stop)) if isinstance(v, rootio.JaggedArray) else v[:entry_stop])
+                    for k, v in cols.items()}
+        parts.append(Table(cols))
+    return _concat(parts) if parts else None
+
+
+def calib(paths):
+    """Per-channel conditions as dense arrays indexed by offline channel (bar*4 + SiPM): pedestal, pulsearea,
+    pulseheight, timeoffset (float, 0 where absent) and status, roc, feb, febch (int64, -1 where absent)."""
+    c = read(paths, "calib")
+    if c is None:
+        raise KeyError(f"no {DIR}/calib tree in {paths}")
+    ch = np.asarray(c["channel"], np.int64)
+    n = int(ch.max()) + 1 if len(ch) else 0
+    out = {k: np.zeros(n, float) for k in ("pedestal", "pulsearea", "pulseheight", "timeoffset")}
+    for k in ("status", "roc", "feb", "febch"):
+        out[k] = np.full(n, -1, np.int64)
+    for k in out:
+        out[k][ch] = np.asarray(c[k])
+    return out
+
+
+def event_key(a):
+    """One int64 per row combining (run, subrun, event), for joins."""
+    return (np.asarray(a["run"]).astype(np.int64) << 40) | (np.asarray(a["subrun"]).astype(np.int64) << 20) | \
+        np.asarray(a["event"]).astype(np.int64)
+
+
+def conditions(paths, deviation=None):
+    """The chain's Conditions from the calib tree (the columns Conditions.from_csv reads from its CSV dump)."""
+    c = calib(paths)
+    n = len(c["pedestal"])
+    dev = np.zeros(n) if deviation is None else np.asarray(deviation, float)
+    return Conditions(c["pedestal"], c["pulsearea"], c["pulseheight"], c["timeoffset"], c["status"], c["roc"],
+                      c["feb"], dev)
+
+
+def write(path, trees):
+    """{tree name: table} into directory crvdump/ of a new ROOT file (jagged columns as counted arrays)."""
+    return rootio.write(path, {f"{DIR}/{k}": v for k, v in trees.items()})
+
+
+def calib_table(cond, febch=None):
+    """The calib tree (one row per channel) of a Conditions."""
+    n = len(cond.pedestal)
+    fc = np.full(n, -1, np.int32) if febch is None else np.asarray(febch, np.int32)
+    return {"channel": np.arange(n, dtype=np.int32), "pedestal": np.asarray(cond.pedestal, np.float32),
+            "pulsearea": np.asarray(cond.pulsearea, np.float32),
+            "pulseheight": np.asarray(cond.pulseheight, np.float32),
+            "timeoffset": np.asarray(cond.timeoffset, np.float32), "status": np.asarray(cond.status, np.int32),
+            "roc": np.asarray(cond.roc, np.int32), "feb": np.asarray(cond.feb, np.int32), "febch": fc}
+
+
+def digis_table(D, cond, run=1, febch=None):
+    """The digis tree of the engine's digis (chain.digis / waveform.synthesize output: SiPM label, start TDC, ADC
+    samples): one row per digi in the given order, idx = its index among its event's digis, nzs 0 (zero-suppressed
+    digis), roc/feb/febch of the channel (febch -1 unless given per channel).  run: one run number for every event,
+    or {event key: run}."""
+    lab = np.asarray(D["chan"], np.int64)
+    evk, ch = lab // CHAN_MULT, lab % CHAN_MULT
+    if isinstance(run, dict):
+        r = np.array([run[int(k)] for k in evk], np.int64)
+    else:
+        r = np.full(len(lab), int(run), np.int64)
+    key = (r << 40) | evk
+    o = np.argsort(key, kind="stable")
+    new = np.ones(len(lab), bool)
+    if len(lab) > 1:
+        new[1:] = key[o][1:] != key[o][:-1]
+    first = np.flatnonzero(new)
+    idx = np.empty(len(lab), np.int64)
+    idx[o] = np.arange(len(lab)) - np.repeat(first, np.diff(np.r_[first, len(lab)]))
+    adc = np.asarray(D["adc"])
+    per = adc.shape[1] if adc.ndim == 2 else 0
+    fc = np.full(len(np.asarray(cond.roc)), -1) if febch is None else np.asarray(febch)
+    return {"run": r.astype(np.uint32), "subrun": (evk >> 20).astype(np.uint32),
+            "event": (evk & ((1 << 20) - 1)).astype(np.uint32), "idx": idx.astype(np.int32),
+            "bar": (ch // NCHAN_PER_BAR).astype(np.int32), "sipm": (ch % NCHAN_PER_BAR).astype(np.int32),
+            "starttdc": np.asarray(D["starttdc"]).astype(np.int32), "nzs": np.zeros(len(lab), np.int32),
+            "roc": np.asarray(cond.roc)[ch].astype(np.int32), "feb": np.asarray(cond.feb)[ch].astype(np.int32),
+            "febch": fc[ch].astype(np.int32),
+            "adc": rootio.JaggedArray(adc.reshape(-1).astype(np.int16), np.arange(len(lab) + 1, dtype=np.int64) * per)}
+
+
+def waveforms(paths, reco_cfg=None, max_events=None, cond=None):
+    """Dumped digis -> reco waveforms: zero-suppressed digis grouped per channel into waveforms in collection order
+    (pulsefit.concat_waveforms), status-ignored channels dropped when the reco configuration ignores them,
+    calibration from the calib tree (or `cond`).  The keys of chain.reco_waveforms (ev = event_key, bar, sipm, chan,
+    adc, n, start, ped, area, height, toff) and of the reference's grouping (digi0 = the first digi's idx, mat = adc,
+    events = every event key of the digis)."""
+    from .config import RecoConfig
+    from .pulsefit import concat_waveforms
+    cfg = reco_cfg or RecoConfig()
+    d = read(paths, "digis")
+    if d is None:
+        raise KeyError(f"no {DIR}/digis tree in {paths}")
+    ev = event_key(d)
+    if max_events:
+        keep = np.isin(ev, np.unique(ev)[:max_events])
+        d = Table({k: (v.take(keep) if isinstance(v, rootio.JaggedArray) else np.asarray(v)[keep])
+                   for k, v in d.items()})
+        ev = ev[keep]
+    C = calib(paths) if cond is None else {"status": np.asarray(cond.status), "pedestal": np.asarray(cond.pedestal),
+                                           "pulsearea": np.asarray(cond.pulsearea),
+                                           "pulseheight": np.asarray(cond.pulseheight),
+                                           "timeoffset": np.asarray(cond.timeoffset)}
+    zs = np.asarray(d["nzs"]) == 0
+    adc = d["adc"]
+    lens = adc.counts[zs]
+    flat = adc.values[np.repeat(zs, adc.counts)]
+    bar, sipm = np.asarray(d["bar"])[zs], np.asarray(d["sipm"])[zs]
+    gid, mat, n, start, first = concat_waveforms(ev[zs], bar, sipm, np.asarray(d["starttdc"])[zs], flat, lens)
+    chan = bar[first] * NCHAN_PER_BAR + sipm[first]
+    ok = np.ones(len(first), bool)
+    if cfg.ignore_channels:
+        ok = ~((np.asarray(C["status"])[chan] >> 1) & 1).astype(bool)
+    c = chan[ok]
+    key = ev[zs][first][ok]
+    return {"ev": key, "bar": c // NCHAN_PER_BAR, "sipm": c % NCHAN_PER_BAR, "chan": c,
+            "digi0": np.asarray(d["idx"])[zs][first][ok], "adc": mat[ok], "mat": mat[ok], "n": n[ok],
+            "start": start[ok], "ped": np.asarray(C["pedestal"])[c], "area": np.asarray(C["pulsearea"])[c],
+            "height": np.asarray(C["pulseheight"])[c], "toff": np.asarray(C["timeoffset"])[c],
+            "events": np.unique(ev)}
+
+
+__all__ = ["DIR", "TREES", "KEY", "read", "calib", "event_key", "conditions", "write", "calib_table", "digis_table",
+           "waveforms"]

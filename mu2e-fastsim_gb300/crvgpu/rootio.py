@@ -218,6 +218,7 @@ class Leaf:
     length: int
     size: int
     unsigned: bool
+    leaf_count: object = None                    # the counter leaf of a counted array (name[nname])
 
     def dtype(self):
         t = LEAF_TYPES.get(self.cls)
@@ -239,6 +240,8 @@ class Branch:
     leaves: list
     branches: list
     embedded_baskets: int
+    entry_offset_len: int = 0
+    class_name: str = ""                         # TBranchElement: the streamed class (e.g. vector<short>)
 
 
 class _Unsupported:
@@ -253,12 +256,12 @@ def _leaf(cls, cur, ctx):
     length, size, _off = cur.i32(), cur.i32(), cur.i32()
     cur.u8()
     unsigned = bool(cur.u8())
-    _object_any(cur, ctx)                        # fLeafCount
+    count = _object_any(cur, ctx)                # fLeafCount
     if lend is not None:
         cur.pos = lend
     if end is not None:
         cur.pos = end
-    return Leaf(cls, name, title, length, size, unsigned)
+    return Leaf(cls, name, title, length, size, unsigned, count if isinstance(count, Leaf) else None)
 
 
 def _branch(cls, cur, ctx):
@@ -266,6 +269,11 @@ def _branch(cls, cur, ctx):
     if cls != "TBranch":
         b = _branch("TBranch", cur, ctx)         # base part of a derived branch class
         b.cls = cls
+        if cls == "TBranchElement":
+            try:
+                b.class_name = cur.string()      # fClassName, the first member after the base
+            except RootFormatError:
+                b.class_name = ""
         if end is not None:
             cur.pos = end
         return b
@@ -273,7 +281,8 @@ def _branch(cls, cur, ctx):
         raise RootFormatError(f"TBranch class version {v}: versions 12 and 13 are read")
     name, title = _tnamed(cur)
     _skip_versioned(cur)                         # TAttFill
-    cur.i32(), cur.i32(), cur.i32()              # fCompress, fBasketSize, fEntryOffsetLen
+    cur.i32(), cur.i32()                         # fCompress, fBasketSize
+    entry_offset_len = cur.i32()
     write_basket = cur.i32()
     cur.i64()                                    # fEntryNumber
     if v >= 13:
@@ -295,7 +304,7 @@ def _branch(cls, cur, ctx):
     emb = sum(1 for b in baskets if b is not None)
     return Branch(cls, name, title, entries, write_basket, arrs[0].astype(np.int64), arrs[1].astype(np.int64),
                   arrs[2].astype(np.int64), [x for x in leaves if x is not None],
-                  [x for x in branches if x is not None], emb)
+                  [x for x in branches if x is not None], emb, entry_offset_len)
 
 
 def _read_class(cname, cur, ctx):
@@ -444,6 +453,69 @@ def _key(cur):
                cur.string(), cur.string())
 
 
+_VECTOR = {f"vector<{k}>": v for k, v in (
+    ("char", ">i1"), ("unsignedchar", ">u1"), ("short", ">i2"), ("unsignedshort", ">u2"), ("int", ">i4"),
+    ("unsignedint", ">u4"), ("long", ">i8"), ("longlong", ">i8"), ("Long64_t", ">i8"), ("unsignedlong", ">u8"),
+    ("unsignedlonglong", ">u8"), ("ULong64_t", ">u8"), ("float", ">f4"), ("double", ">f8"), ("bool", "?"),
+    ("Short_t", ">i2"), ("Int_t", ">i4"), ("Float_t", ">f4"), ("Double_t", ">f8"))}
+
+
+_VECTOR_OF = {">i1": "vector<char>", ">u1": "vector<unsigned char>", ">i2": "vector<short>",
+              ">u2": "vector<unsigned short>", ">i4": "vector<int>", ">u4": "vector<unsigned int>",
+              ">i8": "vector<long>",
+              ">u8": "vector<unsigned long>", ">f4": "vector<float>", ">f8": "vector<double>", "|b1": "vector<bool>"}
+
+
+class JaggedArray:
+    """Variable-length rows: values (flat) and offsets (rows + 1); row i is values[offsets[i]:offsets[i + 1]]."""
+
+    def __init__(self, values, offsets):
+        self.values = np.asarray(values)
+        self.offsets = np.asarray(offsets, np.int64)
+        if self.offsets.ndim != 1 or len(self.offsets) < 1 or self.offsets[0] != 0 or \
+                self.offsets[-1] != len(self.values) or np.any(np.diff(self.offsets) < 0):
+            raise ValueError("offsets must start at 0, not decrease, and end at the number of values")
+
+    @classmethod
+    def from_rows(cls, rows, dtype=None):
+        rows = [np.asarray(r, dtype) for r in rows]
+        cnt = np.array([len(r) for r in rows], np.int64)
+        dt = dtype or (rows[0].dtype if rows else np.float64)
+        vals = np.concatenate(rows).astype(dt) if rows else np.zeros(0, dt)
+        return cls(vals, np.r_[0, np.cumsum(cnt)])
+
+    @property
+    def counts(self):
+        return np.diff(self.offsets)
+
+    @property
+    def nbytes(self):
+        return self.values.nbytes + self.offsets.nbytes
+
+    @property
+    def dtype(self):
+        return self.values.dtype
+
+    def __len__(self):
+        return len(self.offsets) - 1
+
+    def __getitem__(self, i):
+        return self.values[self.offsets[i]:self.offsets[i + 1]]
+
+    def tolist(self):
+        return [self[i].tolist() for i in range(len(self))]
+
+    def __eq__(self, other):
+        return isinstance(other, JaggedArray) and np.array_equal(self.offsets, other.offsets) and \
+            self.values.dtype == other.values.dtype and np.array_equal(self.values, other.values)
+
+    __hash__ = None
+
+    def take(self, sel):
+        sel = np.arange(len(self))[sel]
+        return JaggedArray.from_rows([self[i] for i in sel], self.values.dtype)
+
+
 class Tree:
     """One TTree: name, title, entries and branches {name: Branch}; arrays() reads fixed-size leaf columns."""
 
@@ -460,40 +532,89 @@ class Tree:
     def keys(self):
         return list(self.branches)
 
-    def _column(self, b):
+    def _layout(self, b):
+        """(dtype, values per entry, jagged header bytes or None): fixed leaves, counted arrays (header 0) and
+        std::vector<basic> element branches (10 header bytes per entry: byte count, version, size)."""
+        if b.cls == "TBranchElement" and not b.branches:
+            m = _VECTOR.get(b.class_name.replace(" ", ""))
+            if m is None:
+                raise RootFormatError(f"branch {b.name!r}: class {b.class_name!r} is not a vector of a basic type")
+            return np.dtype(m), 1, 10
         if b.branches or len(b.leaves) != 1 or not isinstance(b.leaves[0], Leaf) or b.leaves[0].dtype() is None:
-            raise RootFormatError(f"branch {b.name!r} ({b.cls}) is not a single fixed-size leaf of a basic type")
+            raise RootFormatError(f"branch {b.name!r} ({b.cls}) is not a single leaf of a basic type")
         lf = b.leaves[0]
-        per = max(1, lf.length)
-        dt = lf.dtype()
+        if lf.leaf_count is not None:
+            return lf.dtype(), max(1, lf.length), 0
+        return lf.dtype(), max(1, lf.length), None
+
+    def _column(self, b):
+        dt, per, header = self._layout(b)
         if int(b.basket_entry[b.write_basket]) < b.entries or b.embedded_baskets:
             raise RootFormatError(f"branch {b.name!r}: entries held in an unflushed (embedded) basket are not read")
-        out = np.empty(b.entries * per, dt.newbyteorder("="))
         jobs = []
         for i in range(b.write_basket):
             a, e = int(b.basket_entry[i]), int(b.basket_entry[i + 1])
             if e > a:
                 jobs.append((int(b.basket_seek[i]), int(b.basket_bytes[i]), a, e))
 
-        def one(job):
+        def basket(job):
             seek, nbytes, a, e = job
             kc = _Cursor(self.file.buf, seek)
             k = _key(kc)
             if k.nbytes != nbytes:
                 raise RootFormatError(f"branch {b.name!r}: basket at {seek} does not match the branch's byte count")
-            raw = self.file.object_bytes(k)
-            n = (e - a) * per
-            if len(raw) < n * dt.itemsize:
-                raise RootFormatError(f"branch {b.name!r}: basket at {seek} holds fewer values than its entries")
-            out[a * per:e * per] = np.frombuffer(raw, dt, n)
+            kc.i16()
+            bufsize = kc.i32()
+            if bufsize < 0:                      # extra IO-bits byte
+                kc.u8()
+            kc.i32(), kc.i32()                   # fNevBufSize, fNevBuf
+            last = kc.i32()
+            return k, last, self.file.object_bytes(k)
 
+        if header is None:
+            out = np.empty(b.entries * per, dt.newbyteorder("="))
+
+            def fixed(job):
+                k, _, raw = basket(job)
+                a, e = job[2], job[3]
+                n = (e - a) * per
+                if len(raw) < n * dt.itemsize:
+                    raise RootFormatError(f"branch {b.name!r}: basket at {job[0]} holds fewer values than its entries")
+                out[a * per:e * per] = np.frombuffer(raw, dt, n)
+            self._map(fixed, jobs)
+            return out.reshape(-1, per) if per > 1 else out
+        parts = [None] * len(jobs)
+
+        def jag(ij):
+            i, job = ij
+            k, last, raw = basket(job)
+            a, e = job[2], job[3]
+            border = last - k.keylen
+            if border < 0 or border + 4 * (e - a + 2) > len(raw):
+                raise RootFormatError(f"branch {b.name!r}: basket at {job[0]} has no entry offsets")
+            offs = np.frombuffer(raw, ">i4", e - a + 1, border + 4).astype(np.int64) - k.keylen
+            offs[-1] = border
+            starts, ends = offs[:-1] + header, offs[1:]
+            if np.any(ends < starts) or np.any((ends - starts) % dt.itemsize):
+                raise RootFormatError(f"branch {b.name!r}: basket at {job[0]} has inconsistent entry offsets")
+            cnt = (ends - starts) // dt.itemsize
+            body = np.frombuffer(raw, np.uint8, border)
+            idx = np.repeat(starts - np.r_[0, np.cumsum((ends - starts))[:-1]], ends - starts) + \
+                np.arange(int((ends - starts).sum()))
+            parts[i] = (cnt, body[idx].view(dt) if len(idx) else np.zeros(0, dt))
+        self._map(jag, list(enumerate(jobs)))
+        counts = np.concatenate([p[0] for p in parts]) if parts else np.zeros(0, np.int64)
+        values = np.concatenate([p[1] for p in parts]).astype(dt.newbyteorder("=")) if parts else \
+            np.zeros(0, dt.newbyteorder("="))
+        return JaggedArray(values, np.r_[0, np.cumsum(counts)].astype(np.int64))
+
+    def _map(self, fn, jobs):
         if len(jobs) > 1 and self.file.threads > 1:
             with ThreadPoolExecutor(self.file.threads) as ex:
-                list(ex.map(one, jobs))
+                list(ex.map(fn, jobs))
         else:
             for j in jobs:
-                one(j)
-        return out.reshape(-1, per) if per > 1 else out
+                fn(j)
 
     def arrays(self, columns=None):
         """{column: native-endian array} for `columns` (all when None), in branch order."""
@@ -722,41 +843,103 @@ def _dir_record(big, datime, nbytes_keys, nbytes_name, seek_dir, seek_parent, se
 @dataclass
 class _Col:
     name: str
-    data: np.ndarray         # (entries,) or (entries, n) native
+    data: object             # (entries,) or (entries, n) native array, or a JaggedArray
     leaf: str
     unsigned: bool
     per: int
+    counter: str = ""        # counted array: the name of its counter column
+    vector: str = ""         # std::vector element branch (tests): the vector's class name
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def variable(self):
+        return bool(self.counter or self.vector)
+
+    def raw(self, a, e, be, keylen):
+        """Big-endian bytes of entries [a, e) (variable-size rows: values, then the entry-offset block; a
+        std::vector row is preceded by its byte count, version and size)."""
+        if not self.variable:
+            return np.ascontiguousarray(self.data[a:e]).astype(be, copy=False).tobytes()
+        o = self.data.offsets
+        if self.vector:
+            rows = []
+            for i in range(a, e):
+                v = self.data.values[o[i]:o[i + 1]].astype(be, copy=False).tobytes()
+                rows.append(struct.pack(">Ihi", (6 + len(v)) | BYTECOUNT, 9, o[i + 1] - o[i]) + v)
+            starts = np.r_[0, np.cumsum([len(r) for r in rows])[:-1]].astype(np.int64) + keylen if rows else \
+                np.zeros(0, np.int64)
+            vals = b"".join(rows)
+        else:
+            vals = self.data.values[o[a]:o[e]].astype(be, copy=False).tobytes()
+            starts = (o[a:e] - o[a]) * be.itemsize + keylen
+        offs = np.r_[e - a + 1, starts, 0].astype(">i4")
+        return vals + offs.tobytes()
 
 
-def _columns(cols):
+ENTRY_OFFSET_LEN = 1000          # ROOT's default entry-offset table length for variable-size branches
+
+
+def _columns(cols, vectors=()):
     out = []
     n = None
+    names = set(cols)
     for name, a in cols.items():
-        a = np.asarray(a)
+        if not isinstance(a, JaggedArray) and isinstance(a, (list, tuple)) and a and \
+                not np.isscalar(a[0]) and np.ndim(a[0]) == 1:
+            a = JaggedArray.from_rows(a)
+        jag = isinstance(a, JaggedArray)
+        if not jag:
+            a = np.asarray(a)
         if a.dtype not in _DTYPE_LEAF:
             raise TypeError(f"column {name!r}: dtype {a.dtype} has no ROOT leaf type (basic numeric types only)")
-        if a.ndim not in (1, 2):
-            raise ValueError(f"column {name!r}: one value or a fixed-length array per entry")
+        if not jag and a.ndim not in (1, 2):
+            raise ValueError(f"column {name!r}: one value, a fixed-length array or a variable-length row per entry")
         if n is None:
             n = len(a)
         elif len(a) != n:
             raise ValueError("every column of a tree needs the same number of entries")
         leaf, uns = _DTYPE_LEAF[a.dtype]
-        out.append(_Col(name, a, leaf, uns, 1 if a.ndim == 1 else a.shape[1]))
+        if jag and name in vectors:
+            out.append(_Col(name, a, leaf, uns, 1, "", _VECTOR_OF[np.dtype(LEAF_TYPES[leaf][1 if uns else 0]).str]))
+        elif jag:
+            cname = f"n{name}"
+            cnt = a.counts.astype(np.int32)
+            if cname in names:
+                given = [c for c in out if c.name == cname]
+                if not given or not np.array_equal(given[0].data, cnt):
+                    raise ValueError(f"column {cname!r} must come before {name!r} and hold its row lengths")
+            else:
+                out.append(_Col(cname, cnt, "TLeafI", False, 1))
+            out.append(_Col(name, a, leaf, uns, 1, cname))
+        else:
+            out.append(_Col(name, a, leaf, uns, 1 if a.ndim == 1 else a.shape[1]))
     return out, (n or 0)
 
 
-def _leaf_body(c, lo, hi):
+def _leaf_body(c, lo, hi, leaf_tags):
     t = LEAF_TYPES[c.leaf]
     dt = np.dtype(t[1] if c.unsigned else t[0])
     size = dt.itemsize
 
     def body(w):
+        if c.vector:                                   # TLeafElement: TLeaf, fID, fType
+            at = w.begin(1)
+            lat = w.begin(2)
+            w.tnamed(c.name, c.name)
+            w.put(">iiiBB", 0, size, 0, 0, 0)
+            w.put(">I", 0)
+            w.end(lat)
+            w.put(">ii", -1, 0)
+            w.end(at)
+            return
         at = w.begin(1)
         lat = w.begin(2)
-        w.tnamed(c.name, c.name)
+        w.tnamed(c.name, f"{c.name}[{c.counter}]" if c.counter else c.name)
         w.put(">iiiBB", c.per, size, 0, 0, 1 if c.unsigned else 0)
-        w.put(">I", 0)                                  # fLeafCount
+        w.put(">I", leaf_tags[c.counter] if c.counter else 0)   # fLeafCount: a reference to the counter's leaf
         w.end(lat)
         w.b += np.array([lo, hi], dt).tobytes()
         w.end(at)
@@ -765,14 +948,31 @@ def _leaf_body(c, lo, hi):
 
 def _branch_body(c, lo, hi, nbk, n, bounds, seeks, nbytes, tot, zip_, fcompress, leaf_tags):
     letter = LEAF_TYPES[c.leaf][3 if c.unsigned else 2]
-    btitle = f"{c.name}[{c.per}]/{letter}" if c.per > 1 else f"{c.name}/{letter}"
+    if c.vector:
+        btitle = c.name
+    elif c.counter:
+        btitle = f"{c.name}[{c.counter}]/{letter}"
+    else:
+        btitle = f"{c.name}[{c.per}]/{letter}" if c.per > 1 else f"{c.name}/{letter}"
     mb = max(10, nbk + 1)
 
     def body(w):
+        if c.vector:                                   # TBranchElement: the TBranch base, then its own members
+            ea = w.begin(10)
+            base(w)
+            for x in (c.vector, "", ""):               # fClassName, fParentName, fClonesName
+                w.string(x)
+            w.put(">Ihiiii", 0, 6, -1, 0, -1, 0)       # fCheckSum, fClassVersion, fID, fType, fStreamerType, ..
+            w.put(">II", 0, 0)                         # fBranchCount, fBranchCount2
+            w.end(ea)
+        else:
+            base(w)
+
+    def base(w):
         at = w.begin(13)
         w.tnamed(c.name, btitle)
         w.versioned(2, ">hh", 0, 1001)                 # TAttFill
-        w.put(">iiiiq", fcompress, 32000, 0, nbk, n)   # fCompress, fBasketSize, fEntryOffsetLen, fWriteBasket, ..
+        w.put(">iiiiq", fcompress, 32000, ENTRY_OFFSET_LEN if c.variable else 0, nbk, n)
         w.versioned(1, ">B", 0)                        # fIOFeatures
         w.put(">iii", 0, mb, 0)                        # fOffset, fMaxBaskets, fSplitLevel
         w.put(">qqqq", n, 0, tot, zip_)                # fEntries, fFirstEntry, fTotBytes, fZipBytes
@@ -781,7 +981,7 @@ def _branch_body(c, lo, hi, nbk, n, bounds, seeks, nbytes, tot, zip_, fcompress,
         w.tobject()
         w.string("")
         w.put(">ii", 1, 0)
-        leaf_tags[c.name] = w.object_any(c.leaf, _leaf_body(c, lo, hi))
+        leaf_tags[c.name] = w.object_any("TLeafElement" if c.vector else c.leaf, _leaf_body(c, lo, hi, leaf_tags))
         w.end(la)
         w.objarray([])                                 # fBaskets: every basket is a key of its own
         bb, be, bs = np.zeros(mb, ">i4"), np.zeros(mb, ">i8"), np.zeros(mb, ">i8")
@@ -794,18 +994,21 @@ def _branch_body(c, lo, hi, nbk, n, bounds, seeks, nbytes, tot, zip_, fcompress,
     return body
 
 
-def write(path, trees, compression=101, basket_bytes=4 << 20, title="", threads=None, _compressor=None):
+def write(path, trees, compression=101, basket_bytes=4 << 20, title="", threads=None, _compressor=None, _vectors=()):
     """Write {"dir/.../tree": {column: array}} as TTrees (directories made from the path).  compression: ROOT
     setting (0 none, 1xx zlib level xx (the default 101 is ROOT's), 2xx LZMA; 1..9 alone mean zlib).  Every branch of
     a tree shares the basket (cluster) boundaries; a basket holds about `basket_bytes` of the tree's widest column.
-    Empty or None tables are skipped, as in the reference's write.  _compressor (tests): raw bytes -> blocks or
-    None, used instead of the setting's algorithm."""
+    Empty or None tables are skipped, as in the reference's write.  Variable-length columns (JaggedArray, or a list
+    of 1-d arrays) are written as counted arrays with a counter column n<name>, as uproot writes them.  Tests only:
+    _compressor (raw bytes -> blocks or None, instead of the setting's algorithm) and _vectors (names of variable
+    columns to write as std::vector element branches, the layout ROOT's TTree::Branch gives a vector of a basic type,
+    which this module reads from files ROOT made; these records are not checked against ROOT here)."""
     threads = threads or min(16, os.cpu_count() or 1)
     items = []
     for tpath, cols in trees.items():
         if cols is None:
             continue
-        cc, n = _columns(cols)
+        cc, n = _columns(cols, _vectors)
         if n == 0 or not cc:
             continue
         parts = [p for p in tpath.split("/") if p]
@@ -857,38 +1060,43 @@ def write(path, trees, compression=101, basket_bytes=4 << 20, title="", threads=
 
         for d, tname, cc, n in items:
             pdir = seek_dir(d)
-            widest = max(c.data.dtype.itemsize * c.per for c in cc)
-            per_basket = max(1, min(n, basket_bytes // widest))
+            def entry_bytes(c):
+                if c.variable:
+                    return c.dtype.itemsize * max(1, -(-len(c.data.values) // max(1, n))) + 4 + (10 if c.vector else 0)
+                return c.dtype.itemsize * c.per
+            per_basket = max(1, min(n, basket_bytes // max(entry_bytes(c) for c in cc)))
             bounds = list(range(0, n, per_basket)) + [n]
             nbk = len(bounds) - 1
             info = []
             for c in cc:
                 t = LEAF_TYPES[c.leaf]
                 be = np.dtype(t[1] if c.unsigned else t[0])
-                raws = [np.ascontiguousarray(c.data[bounds[i]:bounds[i + 1]]).astype(be, copy=False).tobytes()
-                        for i in range(nbk)]
+                kl = _keylen(big, "TBasket", c.name, tname) + 19
+                raws = [c.raw(bounds[i], bounds[i + 1], be, kl) for i in range(nbk)]
                 zs = [None] * nbk
                 if comp:
                     with ThreadPoolExecutor(threads) as ex:
                         zs = list(ex.map(lambda r: pack(r) if len(r) > 256 else None, raws))
                 seeks, nbytes, tot, zip_ = [], [], 0, 0
-                kl = _keylen(big, "TBasket", c.name, tname) + 19
                 for i in range(nbk):
                     raw = raws[i]
                     payload = zs[i] if zs[i] is not None else raw
                     nb = kl + len(payload)
+                    ne = bounds[i + 1] - bounds[i]
+                    data_len = len(raw) - (4 * (ne + 2) if c.variable else 0)
                     hdr = _key_header(big, nb, len(raw), kl, 1, pos, pdir, "TBasket", c.name, tname, now)
                     # TBasket header: version, fBufferSize, fNevBufSize, fNevBuf, fLast, flag
-                    bh = struct.pack(">hiiiiB", 3, kl + len(raw), be.itemsize * c.per, bounds[i + 1] - bounds[i],
-                                     kl + len(raw), 0)
+                    nevbufsize = ENTRY_OFFSET_LEN if c.variable else be.itemsize * c.per
+                    bh = struct.pack(">hiiiiB", 3, kl + len(raw), nevbufsize, ne, kl + data_len, 0)
                     seeks.append(pos)
                     nbytes.append(nb)
                     tot += kl + len(raw)
                     zip_ += nb
                     emit(hdr + bh + payload)
                 lo = hi = 0
-                if c.data.size and c.leaf != "TLeafO":
-                    lo, hi = c.data.min(), c.data.max()
+                vals = c.data.values if c.variable else c.data
+                if vals.size and c.leaf != "TLeafO":
+                    lo, hi = vals.min(), vals.max()
                 info.append((c, lo, hi, seeks, nbytes, tot, zip_))
             kl = _keylen(big, "TTree", tname, tname)
             w = _W(origin=kl)
@@ -905,8 +1113,9 @@ def write(path, trees, compression=101, basket_bytes=4 << 20, title="", threads=
             w.put(">BB", 0, 0)                          # fClusterRangeEnd, fClusterSize: none
             w.versioned(1, ">B", 0)                     # fIOFeatures
             leaf_tags = {}
-            w.objarray([("TBranch", _branch_body(c, lo, hi, nbk, n, bounds, seeks, nb_, tb, zb, fcompress,
-                                                  leaf_tags)) for c, lo, hi, seeks, nb_, tb, zb in info])
+            w.objarray([("TBranchElement" if c.vector else "TBranch",
+                         _branch_body(c, lo, hi, nbk, n, bounds, seeks, nb_, tb, zb, fcompress, leaf_tags))
+                        for c, lo, hi, seeks, nb_, tb, zb in info])
             w.objarray([("ref", leaf_tags[x[0].name]) for x in info])
             w.put(">I", 0)                              # fAliases
             w.put(">ii", 0, 0)                          # fIndexValues (TArrayD), fIndex (TArrayI): empty

@@ -327,3 +327,74 @@ def test_step_table_feeds_the_engine_host_path(tmp_path):
     assert np.array_equal(GM.event_key(s), (steps["subrun"].astype(np.int64) << 20) | steps["event"])
     for a in "xyzt":
         assert np.array_equal(_col(s, a), 0.5 * (steps[f"{a}0"].astype(float) + steps[f"{a}1"].astype(float))), a
+
+
+def test_jagged_columns_round_trip(tmp_path):
+    """Counted arrays (n<name> counter + name[n<name>], as uproot writes them) and std::vector element branches (the
+    art dumper's layout), through every basket split and compression."""
+    rng = np.random.default_rng(9)
+    n = 4001
+    adc = R.JaggedArray.from_rows([rng.integers(-50, 4000, rng.integers(0, 30)).astype(np.int16) for _ in range(n)],
+                                  np.int16)
+    volt = R.JaggedArray.from_rows([rng.normal(size=rng.integers(0, 5)) for _ in range(n)], np.float64)
+    cols = {"event": np.arange(n, dtype=np.uint32), "adc": adc, "x": rng.normal(size=n), "volt": volt,
+            "wfidx": [np.arange(i % 3, dtype=np.int32) for i in range(n)]}
+    for comp, vec in ((0, ()), (101, ()), (101, ("adc", "volt", "wfidx"))):
+        p = str(tmp_path / f"j{comp}{len(vec)}.root")
+        R.write(p, {"crvdump/digis": cols}, compression=comp, basket_bytes=2048, _vectors=vec)
+        with R.RootFile(p) as f:
+            T = f["crvdump/digis"]
+            got = T.arrays()
+            if not vec:
+                assert T.keys() == ["event", "nadc", "adc", "x", "nvolt", "volt", "nwfidx", "wfidx"]
+                b = T.branches["adc"]
+                assert b.title == "adc[nadc]/S" and b.leaves[0].leaf_count.name == "nadc"
+                assert np.array_equal(got["nadc"], adc.counts)
+            else:
+                assert T.branches["adc"].cls == "TBranchElement" and T.branches["adc"].class_name == "vector<short>"
+            assert T.branches["adc"].write_basket > 5
+        assert got["adc"] == adc and got["volt"] == volt and np.array_equal(got["x"], cols["x"])
+        assert got["wfidx"].tolist() == [list(range(i % 3)) for i in range(n)]
+
+
+def test_reco_tables_feed_the_pulse_fit_grouping(tmp_path):
+    """crvdump/digis + calib written from the oracle's digis read back through reftables (read, calib, conditions,
+    event_key) and grouped by reftables.waveforms give the oracle's reco waveforms; the art dumper's vector layout of
+    the same digis reads back the same; Conditions.from_csv reads the calib columns."""
+    from crvgpu import reftables as RT
+    from crvgpu.config import Conditions
+    from oracle import oracle as O
+    from tests.test_chain_glue_host import _digis
+    D, cond = _digis()
+    cond.status[[5, 9]] = [2, 1]
+    path = str(tmp_path / "crvdump.root")
+    dig = RT.digis_table(D, cond, run=1400)
+    RT.write(path, {"digis": dig, "calib": RT.calib_table(cond)})
+    d = RT.read([path], "digis")
+    assert np.array_equal(d["adc"].values, np.asarray(D["adc"]).reshape(-1)) and np.all(d["adc"].counts == 12)
+    assert np.array_equal(RT.event_key(d) & ((1 << 40) - 1), np.asarray(D["chan"]) // 32768)
+    c = RT.conditions(path)
+    assert np.array_equal(c.pedestal, np.asarray(cond.pedestal, np.float32)) and np.array_equal(c.status, cond.status)
+    W = RT.waveforms(path)
+    Wo = O.reco_waveforms(D, cond)
+    keep = ~((np.asarray(cond.status)[Wo["chan"]] >> 1) & 1).astype(bool)
+    assert keep.sum() < len(keep)                                  # the ignored channel's waveforms are dropped
+    for k in ("bar", "sipm", "adc", "n", "start"):
+        assert np.array_equal(np.asarray(W[k]), np.asarray(Wo[k])[keep]), k
+    assert np.array_equal(W["ev"] & ((1 << 40) - 1), np.asarray(Wo["ev"])[keep])
+    np.testing.assert_array_equal(W["ped"], np.asarray(cond.pedestal, np.float32)[W["chan"]])
+    # the art dumper's layout: std::vector ADC branches
+    vpath = str(tmp_path / "crvdump_vec.root")
+    R.write(vpath, {"crvdump/digis": dig, "crvdump/calib": RT.calib_table(cond)}, _vectors=("adc",))
+    dv = RT.read(vpath, "digis")
+    assert dv["adc"] == d["adc"] and set(d) - set(dv) == {"nadc"}
+    Wv = RT.waveforms(vpath)
+    assert all(np.array_equal(np.asarray(Wv[k]), np.asarray(W[k])) for k in W)
+    # Conditions.from_csv on the calib columns
+    csv = tmp_path / "calib.csv"
+    rows = np.c_[np.arange(len(cond.pedestal)), cond.pedestal, cond.pulsearea, cond.pulseheight, cond.timeoffset,
+                 cond.status, cond.roc, cond.feb, np.zeros(len(cond.pedestal))]
+    np.savetxt(csv, rows, delimiter=",", fmt="%.17g")
+    cc = Conditions.from_csv(str(csv))
+    for k in ("pedestal", "pulsearea", "pulseheight", "timeoffset", "status", "roc", "feb"):
+        assert np.array_equal(getattr(cc, k), np.asarray(getattr(cond, k))), k
