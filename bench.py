@@ -1074,7 +1074,7 @@ def main():
                                        f"steps/event ({nsteps_total} steps, SoA f32 resident), full chain "
                                        f"steps->coincidences in batches of {args.batch} events, resident engine "
                                        f"(one CUDA graph replay per batch)",
-                           "precision": "fp32-mixed (FP64 LM solve and absolute times)",
+                           "precision": "fp32-mixed (float-float LM solve, FP64 absolute times)",
                            "l2": f"inputs larger than L2 ({step_bytes / 1e9:.2f} GB of steps)"},
                 "stage_engine_events_per_s": stage_value,
                 "resident": resident,

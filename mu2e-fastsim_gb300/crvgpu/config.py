@@ -209,7 +209,7 @@ class ChainConfig:
     feb_phase_width: Optional[float] = None    # None = one digitisation period
     feb_phase_key: str = "roc_feb"            # FEB_PHASE_KEYS
     backend: str = "cuda"
-    precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (FP64 LM solve and absolute times)
+    precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (float-float LM solve, FP64 absolute times)
     # the reference's lookup-table response block (sectors {name: (table, reflector, yield_per_mev)}, yield scales,
     # speed / attenuation ratios): charges() runs the lookup-table photon model with it when given lookup tables
     lookup: object = None

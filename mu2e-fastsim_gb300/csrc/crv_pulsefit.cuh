@@ -14,7 +14,8 @@
 // eigenvalues (cyclic Jacobi) run in the lane; pulses go to per-waveform record slots (rounds are bounded by half the
 // samples).  R = double: every step in FP64, the solve by LU with partial pivoting.  R = float (mixed): parameter
 // mapping, residuals, Jacobians, sums and the fit state in FP32 relative to the window's first sample; the
-// normal-equation solve in FP64; absolute pulse times in FP64.
+// normal-equation solve in float-float arithmetic on the FP32 pipe (FP64 for values outside FP32's comfortable
+// range); absolute pulse times in FP64.
 #pragma once
 #include "crv_device.cuh"
 
@@ -384,7 +385,7 @@ __device__ __forceinline__ void subtract_lane(const CrvParams& p, R* y, int n, l
   *hi_o = hi;
 }
 
-// ---- FP32-mixed fit: evaluation, mapping and state in FP32, the normal-equation solve in FP64 -----------------------
+// ---- FP32-mixed fit: evaluation, mapping and state in FP32, the normal-equation solve in float-float ----------------
 //
 // The evaluation and the solves are called, not inlined: inlined at each call site they made the round kernel large
 // enough to stall on instruction fetch (1.7x faster as calls).
@@ -429,7 +430,8 @@ static __device__ __noinline__ void eval_f32(const Fit3f& F, const float u[3], c
 }
 
 // symmetric 3x3 solve M x = b (M packed 00 01 02 11 12 22): cofactors, determinant and adjugate product in FP64
-// (products of FP32 inputs are exact there), the final division by the determinant in FP32
+// (products of FP32 inputs are exact there), the final division by the determinant in FP32.  The fit calls it only
+// for values outside FP32's comfortable range (solve_sym_ff below does the rest).
 static __device__ __noinline__ bool solve_sym64(const float M[6], const float b[3], float x[3]) {
   const double m00 = f2d(M[0]), m01 = f2d(M[1]), m02 = f2d(M[2]), m11 = f2d(M[3]), m12 = f2d(M[4]), m22 = f2d(M[5]);
   const double c00 = m11 * m22 - m12 * m12;
@@ -452,6 +454,69 @@ static __device__ __noinline__ bool solve_sym64(const float M[6], const float b[
     return true;
   }
   x[0] = d2f_trunc(y0) * r; x[1] = d2f_trunc(y1) * r; x[2] = d2f_trunc(y2) * r;
+  return true;
+}
+
+// The same solve in float-float arithmetic on the FP32 pipe: every product of two FP32 values split exactly into a
+// rounded product and its error (fmaf), sums of such pairs with their rounding errors carried (Dekker's and Knuth's
+// error-free transformations), so the cofactors, the determinant and the adjugate product keep ~46 significant bits,
+// reduced to the FP32 result's 24 by the final truncation, as the FP64 solve's 53 are.  Values outside FP32's
+// comfortable range (or a non-finite or zero determinant) go to the FP64 solve.  Measured on the 9,358,230 pulses of
+// 65,536 workload events against the FP64 solve: the same pulses, flags and clusters; the sum of pulse PE moves by
+// 3e-14 relative; the fit takes 48 % less time (it was bound by the FP64 pipe: ~24 FP64 operations per solve, at
+// 1/64 of the FP32 rate, against ~350 FP32 operations for a whole window evaluation).
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return FF{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_norm(float a, float b) {       // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_mul2m(float a, float b, float c, float d) {   // a*b - c*d
+  const FF p = ff_two_prod(a, b), q = ff_two_prod(c, d);
+  const FF s = ff_two_sum(p.hi, -q.hi);
+  return ff_norm(s.hi, __fadd_rn(s.lo, __fsub_rn(p.lo, q.lo)));
+}
+__device__ __forceinline__ FF ff_mul(float x, FF y) {
+  const FF p = ff_two_prod(x, y.hi);
+  return ff_norm(p.hi, fmaf(x, y.lo, p.lo));
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_norm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ bool ff_safe(float x) { return fabsf(x) < 1e36f; }   // finite, headroom for the sums
+
+static __device__ __noinline__ bool solve_sym_ff(const float M[6], const float b[3], float x[3]) {
+  const float m00 = M[0], m01 = M[1], m02 = M[2], m11 = M[3], m12 = M[4], m22 = M[5];
+  const FF c00 = ff_mul2m(m11, m22, m12, m12);
+  const FF c01 = ff_mul2m(m12, m02, m01, m22);
+  const FF c02 = ff_mul2m(m01, m12, m11, m02);
+  const FF det = ff_add(ff_add(ff_mul(m00, c00), ff_mul(m01, c01)), ff_mul(m02, c02));
+  const FF c11 = ff_mul2m(m00, m22, m02, m02);
+  const FF c12 = ff_mul2m(m01, m02, m00, m12);
+  const FF c22 = ff_mul2m(m00, m11, m01, m01);
+  const FF y0 = ff_add(ff_add(ff_mul(b[0], c00), ff_mul(b[1], c01)), ff_mul(b[2], c02));
+  const FF y1 = ff_add(ff_add(ff_mul(b[0], c01), ff_mul(b[1], c11)), ff_mul(b[2], c12));
+  const FF y2 = ff_add(ff_add(ff_mul(b[0], c02), ff_mul(b[1], c12)), ff_mul(b[2], c22));
+  const float df = __fadd_rz(det.hi, det.lo);
+  const float r = 1.0f / df;
+  if (!(ff_safe(c00.hi) && ff_safe(c01.hi) && ff_safe(c02.hi) && ff_safe(c11.hi) && ff_safe(c12.hi) &&
+        ff_safe(c22.hi) && ff_safe(det.hi) && ff_safe(y0.hi) && ff_safe(y1.hi) && ff_safe(y2.hi)) ||
+      !(fabsf(df) > 1e-30f) || !(fabsf(r) < 1e30f) || !(fabsf(r) > 1e-30f))
+    return solve_sym64(M, b, x);
+  x[0] = __fadd_rz(y0.hi, y0.lo) * r;
+  x[1] = __fadd_rz(y1.hi, y1.lo) * r;
+  x[2] = __fadd_rz(y2.hi, y2.lo) * r;
   return true;
 }
 
@@ -494,7 +559,7 @@ __device__ inline void fit_f32(const Fit3f& F, const float p0[3], const float* y
     float M[6] = {H[0] + lam * (H[0] + 1e-12f), H[1], H[2], H[3] + lam * (H[3] + 1e-12f), H[4],
                   H[5] + lam * (H[5] + 1e-12f)};
     float du[3];
-    const bool solved = solve_sym64(M, g, du);
+    const bool solved = solve_sym_ff(M, g, du);
     if (!solved) du[0] = du[1] = du[2] = 0.0f;
     float un[3] = {u[0] + du[0], u[1] + du[1], u[2] + du[2]};
     bool better = false;
@@ -517,7 +582,7 @@ __device__ inline void fit_f32(const Fit3f& F, const float p0[3], const float* y
   for (int it = 0; it < 8; ++it) {
     float M[6] = {H[0] + 1e-12f, H[1], H[2], H[3] + 1e-12f, H[4], H[5] + 1e-12f};
     float du[3];
-    if (!solve_sym64(M, g, du)) break;
+    if (!solve_sym_ff(M, g, du)) break;
     for (int k = 0; k < 3; ++k)
       if (!isfinite(du[k])) du[k] = 0.0f;
     bool moved = false;
@@ -540,7 +605,7 @@ __device__ inline void fit_f32(const Fit3f& F, const float p0[3], const float* y
   float st[3];
   float edm;
   bool okh;
-  if (solve_sym64(M, g, st)) {
+  if (solve_sym_ff(M, g, st)) {
     edm = 0.5f * (g[0] * st[0] + g[1] * st[1] + g[2] * st[2]);
     okh = hessian_ok(H);
   } else {
