@@ -10,7 +10,9 @@ stay resident: a job names a range of events of a device step pool, which it rea
 
 Per-job knobs (the design point): photon yield [PE/MeV], long attenuation length [mm], readout threshold [PE] and
 coincidence window [ns].  Every draw is keyed by (job seed, run, subrun, event, SiPM, draw), so a job's result does not
-depend on what else runs: alone and in a mix it is the same, bit for bit.
+depend on what else runs: alone and in a mix it is the same, bit for bit.  With the lookup-table photon model (the
+production call's tables, crv/crvfastsim/chain.py:197-213) the slots run the lookup-table resident chain; the yields
+then come from the model's configuration, and a job's threshold and window are its knobs.
 """
 from __future__ import annotations
 
@@ -53,12 +55,13 @@ class JobResult:
         return self.finish - self.arrival
 
 
-def job_config(job: Job, precision="fp32", sector="EX") -> ChainConfig:
-    """ChainConfig of a design point (the serving knobs of the workload)."""
+def job_config(job: Job, precision="fp32", sector="EX", lookup=None) -> ChainConfig:
+    """ChainConfig of a design point (the serving knobs of the workload).  lookup: the lookup-table model's response
+    configuration (its yields replace the job's yield and attenuation knobs)."""
     return ChainConfig(response=ResponseConfig(yield_per_mev=job.yield_per_mev, lambda_long=job.lambda_long),
                        waveform=WaveformConfig(min_voltage=job.threshold_pe * SPE_PEAK_VOLT),
                        finder=FinderConfig(cuts={sector: replace(WORKLOAD_CUTS, max_dt=job.window_ns)}),
-                       precision=precision)
+                       precision=precision, lookup=lookup)
 
 
 def random_jobs(n, rng, min_events=1000, max_events=1_000_000, pool_events=None, rate=None):
@@ -78,18 +81,22 @@ def random_jobs(n, rng, min_events=1000, max_events=1_000_000, pool_events=None,
     return jobs
 
 
-def slice_events(ds: DeviceSteps, a: int, b: int) -> DeviceSteps:
-    """Events [a, b) of a device step table as views of its columns (event table rebased to the slice)."""
+def slice_events(ds: DeviceSteps, a: int, b: int, lookup_steps=None):
+    """Events [a, b) of a device step table as views of its columns (event table rebased to the slice).  With
+    lookup_steps (the table's steps in the lookup model's form, row for row): (the slice, views of those columns)."""
     torch = _torch()
     first = ds.ev_first[a:b]
     r0 = int(first[0].item()) if b > a else 0
     cnt = ds.ev_nsteps[a:b]
     n = int(cnt.sum().item()) if b > a else 0
     sl = slice(r0, r0 + n)
-    return DeviceSteps(x=ds.x[sl], y=ds.y[sl], z=ds.z[sl], t=ds.t[sl], edep=ds.edep[sl], bar=ds.bar[sl],
-                       ev_event=ds.ev_event[a:b], ev_subrun=ds.ev_subrun[a:b], ev_run=ds.ev_run[a:b],
-                       ev_first=(first - r0).to(torch.int64), ev_nsteps=cnt, nsteps=n, nevents=b - a,
-                       max_steps=int(cnt.max().item()) if b > a else 0)
+    out = DeviceSteps(x=ds.x[sl], y=ds.y[sl], z=ds.z[sl], t=ds.t[sl], edep=ds.edep[sl], bar=ds.bar[sl],
+                      ev_event=ds.ev_event[a:b], ev_subrun=ds.ev_subrun[a:b], ev_run=ds.ev_run[a:b],
+                      ev_first=(first - r0).to(torch.int64), ev_nsteps=cnt, nsteps=n, nevents=b - a,
+                      max_steps=int(cnt.max().item()) if b > a else 0)
+    if lookup_steps is None:
+        return out
+    return out, {k: v[sl] for k, v in lookup_steps.items()}
 
 
 @dataclass
@@ -112,14 +119,18 @@ class ServeEngine:
     footprint and the granularity at which jobs interleave)."""
 
     def __init__(self, geom, cond, pool: DeviceSteps, hbm_budget: int, max_slots=8, chunk_events=4096,
-                 precision="fp32", device="cuda", resident=True, graph=True, express=False):
+                 precision="fp32", device="cuda", resident=True, graph=True, express=False, lookup=None,
+                 lookup_config=None, lookup_steps=None):
         """resident: slots run the resident chain (one host read per chunk) instead of the per-stage engine (a read per
         stage).  graph: every resident slot replays one captured CUDA graph of the chain, captured here, before any
         slot thread runs; a job's seed and knobs are written into the graph's kernels (crv_chain_graph_set_params),
         so serving needs no capture while it runs (a capacity growth would capture that slot again).
         express: one more slot (within the HBM budget) that takes only jobs of at most one chunk, on a stream of the
         highest priority: a small job that arrives while the other slots run chunks of large jobs starts at once, and
-        the block scheduler gives its kernels the SMs that free up before those of the other streams."""
+        the block scheduler gives its kernels the SMs that free up before those of the other streams.
+        lookup: a LookupModel (crvgpu.lookup) of the geometry, with lookup_config its response configuration and
+        lookup_steps the pool's steps in its form (LookupModel.upload_steps, row for row): the slots run the
+        lookup-table resident chain (resident mode only)."""
         from .chain import ChainEngine
         from .geometry import sector_geom
         from .resident import ChainCaps, ResidentChain, caps_for
@@ -132,25 +143,34 @@ class ServeEngine:
         self.precision = precision
         self.device = device
         self.chunk = int(chunk_events)
-        base = job_config(Job(0, 1), precision, self.sector)
+        if lookup is not None:
+            if not self.resident:
+                raise ValueError("the lookup-table model serves through the resident chain (resident=True)")
+            if lookup_config is None or lookup_steps is None:
+                raise ValueError("the lookup-table model needs its response configuration and the pool's lookup steps")
+            if pool.order is not None:
+                raise ValueError("the lookup-table chain needs the pool's steps grouped by event in increasing key")
+        self.lookup, self.lookup_config, self.lookup_steps = lookup, lookup_config, lookup_steps
+        base = self._config(Job(0, 1))
         # The first slot measures its footprint on a full chunk at the most demanding design point of the knob ranges
         # (largest yield and attenuation length, lowest threshold, widest window), with a margin for the event-to-event
         # spread of later chunks.
-        heavy = job_config(Job(0, 1, yield_per_mev=50.0, lambda_long=6500.0, threshold_pe=3.0, window_ns=20.0),
-                           precision, self.sector)
+        heavy = self._config(Job(0, 1, yield_per_mev=50.0, lambda_long=6500.0, threshold_pe=3.0, window_ns=20.0))
         torch.cuda.synchronize()
         torch.cuda.reset_peak_memory_stats()
         m0 = torch.cuda.memory_allocated()
         s0 = _Slot(0, ChainEngine(geom, cond, base, G=self.G, device=device), torch.cuda.Stream())
-        first = slice_events(pool, 0, min(self.chunk, pool.nevents))
+        first, first_lk = self._slice(0, min(self.chunk, pool.nevents))
         with torch.cuda.stream(s0.stream):
             s0.engine.configure(heavy)
-            s0.engine.run(first, 1)
+            if self.lookup is None:
+                s0.engine.run(first, 1)
             if self.resident:
                 # capacities of a chunk at the heavy design point (a trial run of the resident chain), with a margin
                 # for the event-to-event spread of later chunks; chunks that need more grow them
-                trial = ResidentChain(s0.engine, caps_for(s0.engine, [first]), graph=False, grow=True, max_grow=8)
-                trial.run(first, 1)
+                trial = ResidentChain(s0.engine, caps_for(s0.engine, [first]), real_dtype=pool.x.dtype, graph=False,
+                                      grow=True, max_grow=8, lookup=self.lookup)
+                trial.run(first, 1, lookup_steps=first_lk)
                 counts = trial.last_counts
                 trial = None
                 torch.cuda.synchronize()
@@ -159,7 +179,8 @@ class ServeEngine:
                                                   max_steps_per_event=min(32768, 2 * max(1, first.max_steps)),
                                                   margin=1.3)
                 s0.engine = ChainEngine(geom, cond, base, G=self.G, device=device)
-                s0.chain = ResidentChain(s0.engine, self.caps, graph=self.graph, grow=True)
+                s0.chain = ResidentChain(s0.engine, self.caps, real_dtype=pool.x.dtype, graph=self.graph, grow=True,
+                                         lookup=self.lookup)
         torch.cuda.synchronize()
         if self.resident:
             s0.footprint = int(s0.chain.nbytes * 1.05)
@@ -174,27 +195,38 @@ class ServeEngine:
             sl = _Slot(i, eng, torch.cuda.Stream(priority=-8) if ex else torch.cuda.Stream(), s0.footprint,
                        express=ex)
             if self.resident:
-                sl.chain = ResidentChain(eng, self.caps, graph=self.graph, grow=True)
+                sl.chain = ResidentChain(eng, self.caps, real_dtype=pool.x.dtype, graph=self.graph, grow=True,
+                                         lookup=self.lookup)
             self.slots.append(sl)
         self.footprint = s0.footprint
         if self.graph:                               # capture every slot's graph now, one slot at a time
             for sl in self.slots:
                 with torch.cuda.stream(sl.stream):
-                    sl.chain.run(first, 1)
+                    sl.chain.run(first, 1, lookup_steps=first_lk)
                 sl.stream.synchronize()
+
+    def _config(self, job: Job) -> ChainConfig:
+        return job_config(job, self.precision, self.sector, self.lookup_config)
+
+    def _slice(self, a: int, b: int):
+        """Events [a, b) of the pool, and their steps in the lookup model's form (None without the model)."""
+        if self.lookup is None:
+            return slice_events(self.pool, a, b), None
+        return slice_events(self.pool, a, b, self.lookup_steps)
 
     def _run_chunk(self, slot: _Slot, job: Job, a: int, b: int) -> dict:
         torch = _torch()
         with torch.cuda.stream(slot.stream):
             if slot.job_id != job.id:
-                cfg = job_config(job, self.precision, self.sector)
+                cfg = self._config(job)
                 if slot.chain is not None:
                     slot.chain.configure(cfg)
                 else:
                     slot.engine.configure(cfg)
                 slot.job_id = job.id
             if slot.chain is not None:
-                out = slot.chain.run(slice_events(self.pool, a, b), job.seed).clusters
+                ds, lk = self._slice(a, b)
+                out = slot.chain.run(ds, job.seed, lookup_steps=lk).clusters
             else:
                 r = slot.engine.run(slice_events(self.pool, a, b), job.seed)
                 out = {k: v.clone() for k, v in r.clusters.items()}

@@ -78,3 +78,41 @@ def test_serving_modes_agree():
         for a, b in zip(outs[0], other):
             assert a.n_clusters > 0
             _same(a.clusters, b.clusters)
+
+
+def test_lookup_model_jobs_alone_in_the_mix_and_direct():
+    """Serving with the lookup-table photon model (the production call's tables, crv/crvfastsim/chain.py:197-213):
+    each job's clusters are the same alone, in the mix, and through a direct resident lookup chain of its design
+    point over the same events."""
+    import torch
+    from crvgpu import chain as CH
+    from crvgpu.lookup import LookupModel
+    from crvgpu.resident import ChainCaps, ResidentChain
+    from crvgpu.response import upload_steps
+    from crvgpu.serve import Job, ServeEngine, job_config, slice_events
+    from tests.helpers import module_lookup
+    geom, cond, tables, lcfg, steps, pdg = module_lookup(600, seed=5)
+    pool = upload_steps(steps, nbars=geom.nbars)
+    assert pool.order is None
+    model = LookupModel(geom, lcfg, tables, cond.deviation, precision="fp32")
+    cols = model.upload_steps(steps, pdg)
+    srv = ServeEngine(geom, cond, pool, hbm_budget=1 << 40, max_slots=2, chunk_events=128, lookup=model,
+                      lookup_config=lcfg, lookup_steps=cols)
+    jobs = [Job(0, 300, first=10, seed=31, threshold_pe=4.0, window_ns=12.0),
+            Job(1, 250, first=320, seed=32, threshold_pe=6.0, window_ns=8.0),
+            Job(2, 100, first=200, seed=33)]
+    alone = [srv.run([j], realtime=False)[0] for j in jobs]
+    mixed = srv.run(jobs, realtime=False)
+    for a, m in zip(alone, mixed):
+        assert a.n_clusters > 0
+        _same(a.clusters, m.clusters)
+    j = jobs[0]
+    ds, lk = slice_events(pool, j.first, j.first + j.n_events, cols)
+    eng = CH.ChainEngine(geom, cond, job_config(j, "fp32", srv.sector, lcfg), G=srv.G)
+    caps = ChainCaps(events=ds.nevents, steps=ds.nsteps, photons=4096, charges=4096, slots=4096, digis=4096,
+                     pulses=4096, max_steps_per_event=max(1, ds.max_steps))
+    rc = ResidentChain(eng, caps, real_dtype=pool.x.dtype, graph=False, grow=True, max_grow=12, lookup=model)
+    direct = {k: v.cpu().numpy() for k, v in rc.run(ds, j.seed, lookup_steps=lk).clusters.items()}
+    # the served job ran in chunks of 128 events: the same clusters, in event order
+    _same(alone[0].clusters, direct)
+    torch.cuda.synchronize()
