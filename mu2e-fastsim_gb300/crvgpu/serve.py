@@ -12,7 +12,10 @@ Per-job knobs (the design point): photon yield [PE/MeV], long attenuation length
 coincidence window [ns].  Every draw is keyed by (job seed, run, subrun, event, SiPM, draw), so a job's result does not
 depend on what else runs: alone and in a mix it is the same, bit for bit.  With the lookup-table photon model (the
 production call's tables, crv/crvfastsim/chain.py:197-213) the slots run the lookup-table resident chain; the yields
-then come from the model's configuration, and a job's threshold and window are its knobs.
+then come from the model's configuration, and a job's threshold and window are its knobs.  That model keys its draws
+by the step's row in the batch (the row the stage API's photon ids refer to), so its result depends on how a job is
+cut into chunks; a job's chunks are fixed (chunk_events from its first event), so alone and in a mix it is again the
+same.
 """
 from __future__ import annotations
 
