@@ -388,9 +388,15 @@ def decompress(buf, objlen):
         if len(block) != csize:
             raise RootFormatError("compressed block runs past the end of its key")
         if alg == b"ZL":
-            data = zlib.decompress(block)
+            try:
+                data = zlib.decompress(block)
+            except zlib.error as exc:
+                raise RootFormatError(f"corrupt zlib block: {exc}") from None
         elif alg == b"XZ":
-            data = lzma.decompress(block)
+            try:
+                data = lzma.decompress(block)
+            except lzma.LZMAError as exc:
+                raise RootFormatError(f"corrupt LZMA block: {exc}") from None
         elif alg == b"L4":
             data = _lz4(block, usize)
         elif alg == b"ZS":

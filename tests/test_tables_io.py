@@ -398,3 +398,32 @@ def test_reco_tables_feed_the_pulse_fit_grouping(tmp_path):
     cc = Conditions.from_csv(str(csv))
     for k in ("pedestal", "pulsearea", "pulseheight", "timeoffset", "status", "roc", "feb"):
         assert np.array_equal(getattr(cc, k), np.asarray(getattr(cond, k))), k
+
+
+def test_truncated_and_corrupted_files_are_refused(tmp_path):
+    """A file cut short or with a damaged basket raises RootFormatError (or KeyError for a missing tree); the reader
+    never reads outside the file."""
+    rng = np.random.default_rng(11)
+    p = str(tmp_path / "t.root")
+    R.write(p, {"dump/steps": _columns(20000, rng)}, basket_bytes=8192)
+    raw = open(p, "rb").read()
+    with R.RootFile(p) as f:
+        b = f["dump/steps"].branches["t0"]
+        seek = int(b.basket_seek[1])
+        k = R._key(R._Cursor(f.buf, seek))
+    bad = bytearray(raw)
+    for i in range(seek + k.keylen + 20, seek + k.keylen + 60):
+        bad[i] ^= 0x5A
+    q = str(tmp_path / "bad.root")
+    open(q, "wb").write(bytes(bad))
+    with R.RootFile(q) as f:
+        with pytest.raises(R.RootFormatError):
+            f["dump/steps"].arrays(["t0"])
+        with R.RootFile(p) as g:                              # other branches still read
+            assert np.array_equal(f["dump/steps"].arrays(["bar"])["bar"], g["dump/steps"].arrays(["bar"])["bar"])
+    for cut in (len(raw) // 2, len(raw) - 200, 150):
+        c = str(tmp_path / f"cut{cut}.root")
+        open(c, "wb").write(raw[:cut])
+        with pytest.raises((R.RootFormatError, KeyError)):
+            with R.RootFile(c) as f:
+                f["dump/steps"].arrays()
