@@ -174,7 +174,8 @@ def _cluster_out(cl, mem, detail, pulses):
            "cl_poscalc": cl["poscalc"].astype(bool)}
     if detail:
         out.update({"mem_cl": mem["cl"], "mem_idx": mem["idx"].astype(np.int64), "mem_event": mem["event"],
-                    "cl_pos": cl["pos"], "pulses": pulses})
+                    "cl_pos": cl["pos"], "cl_sidepe": cl["sidepe"], "cl_sidetime": cl["sidetime"],
+                    "cl_sidehits": cl["sidehits"], "cl_nlayers": cl["nlayers"], "pulses": pulses})
     return out
 
 

@@ -7,7 +7,8 @@ The reference reads them with crvfastsim.reco.reftables (read, calib, event_key:
 17-50) into awkward arrays through uproot; here they come back as Tables whose jagged columns are
 crvgpu.rootio.JaggedArray.  On top: `write` (counted arrays, the layout CrvRecoTable.hh's Jagged<T> reads),
 `conditions` (the chain's Conditions from the calib tree, as Conditions.from_csv takes the CSV dumped from it),
-`digis_table` (the engine's digis in the dumper's digis layout) and `waveforms` (dumped digis -> reco waveforms with
+`digis_table`, `clusters_table` and `events_table` (the engine's digis, clusters and per-event counts in the
+dumper's layouts) and `waveforms` (dumped digis -> reco waveforms with
 their calibration, the grouping crv/crvfastsim/reco/cli.py:52-74 makes before the pulse fit), so a dumped digi table
 goes into chain.clusters / pulsefit.reconstruct_full as it is.
 """
@@ -133,6 +134,71 @@ def digis_table(D, cond, run=1, febch=None):
             "adc": rootio.JaggedArray(adc.reshape(-1).astype(np.int16), np.arange(len(lab) + 1, dtype=np.int64) * per)}
 
 
+def _run_of(evk, run):
+    if isinstance(run, dict):
+        return np.array([run[int(k)] for k in evk], np.int64)
+    return np.full(len(evk), int(run), np.int64)
+
+
+def clusters_table(out, G, run=1):
+    """The clusters tree (crv/art/CrvFastSim/src/CrvRecoTableDumper_module.cc:155-170) of a chain.clusters(...,
+    detail=True) result: one row per cluster, in event order; idx = its index among its event's clusters; pulses = its
+    member pulses' indices in the event's pulse list, in member order; layers = the distinct layers of their counters,
+    increasing; position, side PE, side times and side hit counts as the finder gives them.  G: the SectorGeom (layer
+    per counter); run: one run number, or {event key: run}."""
+    ev = np.asarray(out["cl_event"], np.int64)
+    n = len(ev)
+    new = np.ones(n, bool)
+    if n > 1:
+        new[1:] = ev[1:] != ev[:-1]
+    first = np.flatnonzero(new)
+    idx = np.arange(n) - np.repeat(first, np.diff(np.r_[first, n]))
+    mcl = np.asarray(out["mem_cl"], np.int64)
+    o = np.argsort(mcl, kind="stable")
+    mcl, midx, mev = mcl[o], np.asarray(out["mem_idx"], np.int64)[o], np.asarray(out["mem_event"], np.int64)[o]
+    offs = np.searchsorted(mcl, np.arange(n + 1))
+    P = out["pulses"]
+    pev = np.asarray(P["ev"], np.int64)
+    pstart = np.searchsorted(pev, mev)                  # pulses are grouped by event, idx = position in the event
+    layer = np.asarray(G.layer)[np.asarray(P["bar"], np.int64)[pstart + midx]]
+    layers = [np.unique(layer[offs[c]:offs[c + 1]]).astype(np.int32) for c in range(n)]
+    pos = np.asarray(out["cl_pos"], float).reshape(-1, 3)
+    spe = np.asarray(out["cl_sidepe"], float).reshape(-1, 2)
+    stm = np.asarray(out["cl_sidetime"], float).reshape(-1, 2)
+    shi = np.asarray(out["cl_sidehits"]).reshape(-1, 2)
+    return {"run": _run_of(ev, run).astype(np.uint32), "subrun": (ev >> 20).astype(np.uint32),
+            "event": (ev & ((1 << 20) - 1)).astype(np.uint32), "idx": idx.astype(np.int32),
+            "sectortype": np.asarray(out["cl_type"]).astype(np.int32),
+            "start": np.asarray(out["cl_start"], np.float64), "end": np.asarray(out["cl_end"], np.float64),
+            "pe": np.asarray(out["cl_pe"]).astype(np.float32), "slope": np.asarray(out["cl_slope"]).astype(np.float32),
+            "layers": rootio.JaggedArray.from_rows(layers, np.int32) if n else rootio.JaggedArray(
+                np.zeros(0, np.int32), np.zeros(1, np.int64)),
+            "pulses": rootio.JaggedArray(midx.astype(np.int32), offs.astype(np.int64)),
+            "poscalc": np.asarray(out["cl_poscalc"]).astype(np.int32),
+            "avgtime": np.asarray(out["cl_avgtime"], np.float64), "x": pos[:, 0].astype(np.float32),
+            "y": pos[:, 1].astype(np.float32), "z": pos[:, 2].astype(np.float32),
+            "sidepe0": spe[:, 0].astype(np.float32), "sidepe1": spe[:, 1].astype(np.float32),
+            "sidetime0": stm[:, 0], "sidetime1": stm[:, 1], "sidehits0": shi[:, 0].astype(np.int32),
+            "sidehits1": shi[:, 1].astype(np.int32)}
+
+
+def events_table(event_keys, run=1, ndigi=None, npulse=None, ncluster=None):
+    """The events tree (one row per event; spill -1, event length and proton-bunch time 0 for the fast chain's
+    off-spill events) with the per-event digi, pulse and cluster counts ({event key: count} or arrays by event)."""
+    evk = np.asarray(event_keys, np.int64)
+
+    def per(c):
+        if c is None:
+            return np.zeros(len(evk), np.int32)
+        if isinstance(c, dict):
+            return np.array([c.get(int(k), 0) for k in evk], np.int32)
+        return np.asarray(c).astype(np.int32)
+    return {"run": _run_of(evk, run).astype(np.uint32), "subrun": (evk >> 20).astype(np.uint32),
+            "event": (evk & ((1 << 20) - 1)).astype(np.uint32), "spill": np.full(len(evk), -1, np.int32),
+            "evlen": np.zeros(len(evk)), "pbtime": np.zeros(len(evk)), "ndigi": per(ndigi), "npulse": per(npulse),
+            "ncluster": per(ncluster)}
+
+
 def waveforms(paths, reco_cfg=None, max_events=None, cond=None):
     """Dumped digis -> reco waveforms: zero-suppressed digis grouped per channel into waveforms in collection order
     (pulsefit.concat_waveforms), status-ignored channels dropped when the reco configuration ignores them,
@@ -175,4 +241,4 @@ def waveforms(paths, reco_cfg=None, max_events=None, cond=None):
 
 
 __all__ = ["DIR", "TREES", "KEY", "read", "calib", "event_key", "conditions", "write", "calib_table", "digis_table",
-           "waveforms"]
+           "clusters_table", "events_table", "waveforms"]

@@ -1017,6 +1017,7 @@ def clusters_from_pulses(W, P, G, status, fcfg, detail=False):
     cl = {k: [] for k in ("cl_event", "cl_type", "cl_pe", "cl_start", "cl_end", "cl_slope", "cl_avgtime",
                           "cl_poscalc")}
     mem = {"cl_pos": [], "mem_cl": [], "mem_idx": [], "mem_event": []}
+    side = {"cl_sidepe": [], "cl_sidetime": [], "cl_sidehits": []}
     ue, lo = np.unique(ev, return_index=True)
     hi = np.r_[lo[1:], len(ev)]
     for e, a, b in zip(ue, lo, hi):
@@ -1028,12 +1029,20 @@ def clusters_from_pulses(W, P, G, status, fcfg, detail=False):
                 cl[k].append(r[src])
             n = len(cl["cl_event"]) - 1
             mem["cl_pos"].append(np.asarray(r["pos"], float))
+            side["cl_sidepe"].append(np.asarray(r["sidepe"], float))
+            side["cl_sidetime"].append(np.asarray(r["sidetime"], float))
+            side["cl_sidehits"].append(np.asarray(r["sidehits"], np.int64))
+            side.setdefault("cl_layers", []).append(list(r["layers"]))
             mem["mem_cl"] += [n] * len(r["pulses"])
             mem["mem_idx"] += list(r["pulses"])
             mem["mem_event"] += [e] * len(r["pulses"])
     out = {k: np.asarray(v) for k, v in cl.items()}
     out.update({k: np.asarray(v, np.int64) for k, v in mem.items() if k != "cl_pos"})
     out["cl_pos"] = np.asarray(mem["cl_pos"], float).reshape(-1, 3)
+    out["cl_sidepe"] = np.asarray(side["cl_sidepe"], float).reshape(-1, 2)
+    out["cl_sidetime"] = np.asarray(side["cl_sidetime"], float).reshape(-1, 2)
+    out["cl_sidehits"] = np.asarray(side["cl_sidehits"], np.int64).reshape(-1, 2)
+    out["cl_layers"] = side.get("cl_layers", [])
     out["pulses"] = dict(ev=ev, idx=idx, bar=bar, sipm=sipm, seq=seq, pe=pe, time=time)
     return out
 

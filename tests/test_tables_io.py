@@ -427,3 +427,39 @@ def test_truncated_and_corrupted_files_are_refused(tmp_path):
         with pytest.raises((R.RootFormatError, KeyError)):
             with R.RootFile(c) as f:
                 f["dump/steps"].arrays()
+
+
+def test_cluster_and_event_trees_of_the_chain_outputs(tmp_path):
+    """reftables.clusters_table / events_table on the chain's cluster output (here the oracle's, in the same detail
+    format as chain.clusters(..., detail=True)): member pulses and layers per cluster (the reference finder's `pulses`
+    and `layers`), the per-event index, and a round trip through a crvdump file with jagged columns."""
+    from crvgpu import config as CF
+    from crvgpu import geometry as GM
+    from crvgpu import reftables as RT
+    from oracle import oracle as O
+    from tests.test_chain_glue_host import _digis
+    D, cond = _digis()
+    W = O.reco_waveforms(D, cond)
+    rcfg = CF.RecoConfig()
+    geom = GM.module_geometry()
+    G = GM.sector_geom(geom)
+    out = O.clusters_from_pulses(W, O.pulses_from_waveforms(W, cond, rcfg, rcfg.period), G, cond.status,
+                                 CF.workload_finder(G.sector_names))
+    n = len(out["cl_event"])
+    assert n >= 2
+    t = RT.clusters_table(out, G, run=1400)
+    for c in range(n):
+        assert t["pulses"][c].tolist() == list(out["mem_idx"][out["mem_cl"] == c])
+        assert t["layers"][c].tolist() == out["cl_layers"][c]
+    ev = np.asarray(out["cl_event"])
+    assert np.array_equal(t["idx"], [int(np.sum(ev[:i] == ev[i])) for i in range(n)])
+    uev, ncl = np.unique(ev, return_counts=True)
+    e = RT.events_table(uev, run=1400, ncluster=ncl, npulse={int(k): 1 for k in uev})
+    p = str(tmp_path / "crvdump_cl.root")
+    RT.write(p, {"clusters": t, "events": e})
+    r = RT.read(p, "clusters")
+    for k, v in t.items():
+        assert (r[k] == v) if isinstance(v, R.JaggedArray) else np.array_equal(r[k], v), k
+    re_ = RT.read(p, "events")
+    assert np.array_equal(re_["ncluster"], ncl) and np.all(re_["spill"] == -1) and np.all(re_["npulse"] == 1)
+    assert np.array_equal(RT.event_key(r) & ((1 << 40) - 1), ev) and np.all(np.asarray(r["run"]) == 1400)
