@@ -7,7 +7,8 @@ The reference reads them with crvfastsim.reco.reftables (read, calib, event_key:
 17-50) into awkward arrays through uproot; here they come back as Tables whose jagged columns are
 crvgpu.rootio.JaggedArray.  On top: `write` (counted arrays, the layout CrvRecoTable.hh's Jagged<T> reads),
 `conditions` (the chain's Conditions from the calib tree, as Conditions.from_csv takes the CSV dumped from it),
-`digis_table`, `clusters_table` and `events_table` (the engine's digis, clusters and per-event counts in the
+`digis_table`, `pulses_table`, `clusters_table` and `events_table` (the engine's digis, pulses, clusters and
+per-event counts in the
 dumper's layouts) and `waveforms` (dumped digis -> reco waveforms with
 their calibration, the grouping crv/crvfastsim/reco/cli.py:52-74 makes before the pulse fit), so a dumped digi table
 goes into chain.clusters / pulsefit.reconstruct_full as it is.
@@ -182,6 +183,44 @@ def clusters_table(out, G, run=1):
             "sidehits1": shi[:, 1].astype(np.int32)}
 
 
+def pulses_table(W, P, run=1, digi_len=12):
+    """The pulses tree (crv/art/CrvFastSim/src/CrvRecoTableDumper_module.cc:143-154) of reco waveforms W
+    (chain.reco_waveforms or waveforms() above) and their pulses P (pulsefit.reconstruct_full, after
+    filter_channels and the time offsets as chain.clusters applies them): one row per pulse in (event, waveform,
+    sequence) order; idx = its index among its event's pulses; flags bit 0 = failed fit (the bit the reference's reco
+    reads); wfidx = the indices of the waveform's digis in their event's digi list (W["digi0"] onwards, one per
+    digi_len samples, the digitizer's samples per digi; empty when W has no digi0)."""
+    wf = np.asarray(P["wf"], np.int64)
+    evw = np.asarray(W["ev"], np.int64)
+    ev = evw[wf] & ((1 << 40) - 1)
+    o = np.lexsort((np.asarray(P["seq"]), wf, ev))
+    wf, ev = wf[o], ev[o]
+    n = len(wf)
+    new = np.ones(n, bool)
+    if n > 1:
+        new[1:] = ev[1:] != ev[:-1]
+    first = np.flatnonzero(new)
+    idx = np.arange(n) - np.repeat(first, np.diff(np.r_[first, n]))
+    chan = np.asarray(W["bar"], np.int64)[wf] * NCHAN_PER_BAR + np.asarray(W["sipm"], np.int64)[wf]
+    if "digi0" in W:
+        L = int(digi_len)
+        nd = -(-np.asarray(W["n"], np.int64)[wf] // L)
+        d0 = np.asarray(W["digi0"], np.int64)[wf]
+        wfidx = rootio.JaggedArray((np.repeat(d0, nd) + np.arange(int(nd.sum())) -
+                                    np.repeat(np.cumsum(nd) - nd, nd)).astype(np.int32), np.r_[0, np.cumsum(nd)])
+    else:
+        wfidx = rootio.JaggedArray(np.zeros(0, np.int32), np.zeros(n + 1, np.int64))
+    col = lambda k, dt: np.asarray(P[k])[o].astype(dt)  # noqa: E731
+    return {"run": _run_of(ev, run).astype(np.uint32), "subrun": (ev >> 20).astype(np.uint32),
+            "event": (ev & ((1 << 20) - 1)).astype(np.uint32), "idx": idx.astype(np.int32),
+            "bar": (chan // NCHAN_PER_BAR).astype(np.int32), "sipm": (chan % NCHAN_PER_BAR).astype(np.int32),
+            "pe": col("pe", np.float32), "peph": col("peph", np.float32), "height": col("height", np.float32),
+            "beta": col("beta", np.float32), "chi2": col("chi2", np.float32), "ped": col("ped", np.float32),
+            "time": col("time", np.float64), "letime": col("letime", np.float64), "seq": col("seq", np.int32),
+            "flags": col("failed", bool).astype(np.int32), "pedfromdb": col("pedfromdb", bool).astype(np.int32),
+            "wfidx": wfidx}
+
+
 def events_table(event_keys, run=1, ndigi=None, npulse=None, ncluster=None):
     """The events tree (one row per event; spill -1, event length and proton-bunch time 0 for the fast chain's
     off-spill events) with the per-event digi, pulse and cluster counts ({event key: count} or arrays by event)."""
@@ -241,4 +280,4 @@ def waveforms(paths, reco_cfg=None, max_events=None, cond=None):
 
 
 __all__ = ["DIR", "TREES", "KEY", "read", "calib", "event_key", "conditions", "write", "calib_table", "digis_table",
-           "clusters_table", "events_table", "waveforms"]
+           "pulses_table", "clusters_table", "events_table", "waveforms"]

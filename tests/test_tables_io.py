@@ -463,3 +463,33 @@ def test_cluster_and_event_trees_of_the_chain_outputs(tmp_path):
     re_ = RT.read(p, "events")
     assert np.array_equal(re_["ncluster"], ncl) and np.all(re_["spill"] == -1) and np.all(re_["npulse"] == 1)
     assert np.array_equal(RT.event_key(r) & ((1 << 40) - 1), ev) and np.all(np.asarray(r["run"]) == 1400)
+
+
+def test_pulses_tree_from_dumped_digis(tmp_path):
+    """reftables.pulses_table on reco waveforms grouped from a dumped digi table and their pulses: one row per pulse in
+    (event, waveform, sequence) order, flags bit 0 = failed fit, wfidx = the waveform's digis, and the reference
+    reco's reading of it (bar, sipm, seq, pe, time, failed = flags & 1, the first wfidx) gives the pulses back."""
+    from crvgpu import config as CF
+    from crvgpu import reftables as RT
+    from oracle import oracle as O
+    from tests.test_chain_glue_host import _digis
+    D, cond = _digis()
+    path = str(tmp_path / "d.root")
+    RT.write(path, {"digis": RT.digis_table(D, cond, run=7), "calib": RT.calib_table(cond)})
+    W = RT.waveforms(path)
+    rcfg = CF.RecoConfig()
+    P = O.reconstruct_full(W["adc"], W["n"], W["start"], W["ped"], W["area"], W["height"], rcfg, rcfg.period)
+    t = RT.pulses_table(W, P, run=7)
+    assert len(t["pe"]) == len(P["pe"]) > 20
+    RT.write(str(tmp_path / "p.root"), {"pulses": t})
+    r = RT.read(str(tmp_path / "p.root"), "pulses")
+    o = np.lexsort((P["seq"], P["wf"], np.asarray(W["ev"])[P["wf"]]))
+    assert np.array_equal(r["pe"], np.asarray(P["pe"])[o].astype(np.float32))
+    assert np.array_equal(r["time"], np.asarray(P["time"])[o])
+    assert np.array_equal(r["flags"] & 1, np.asarray(P["failed"])[o].astype(np.int32))
+    wf = np.asarray(P["wf"])[o]
+    assert np.array_equal(r["bar"] * 4 + r["sipm"], np.asarray(W["chan"])[wf])
+    first = np.array([row[0] for row in r["wfidx"].tolist()])
+    assert np.array_equal(first, np.asarray(W["digi0"])[wf])
+    assert np.array_equal(r["wfidx"].counts, -(-np.asarray(W["n"])[wf] // 12))
+    assert np.array_equal(RT.event_key(r), np.asarray(W["ev"])[wf])
