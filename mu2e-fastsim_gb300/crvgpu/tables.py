@@ -2,9 +2,10 @@
 event) — the reference's core/mu2efastsim/tables.py (KEY, DIR, expand, read, read_many, livetime, primary_muons,
 all_primary_muons, write: :12-72) and crv/crvfastsim/tables.py (primary_muon_crossings :13-26, write :29-31).
 
-The reference returns pandas DataFrames read through uproot; neither is a dependency here, so tables are `Table`s:
-dicts of NumPy columns with the row count as len() and attribute access to columns (``t.bar``).  The ``steps`` tree
-comes back as a StepTable, which the engine's entry points (chain.charges, upload_steps) take as they are.  Files are
+The reference returns pandas DataFrames read through uproot; uproot is not a dependency here, and pandas is optional:
+read returns a DataFrame where pandas is importable (library="pd"), else a `Table` (library="np"): a dict of NumPy
+columns with the row count as len() and attribute access to columns (``t.bar``); the ``steps`` tree then comes back as
+a StepTable.  The engine's entry points (chain.charges, upload_steps) take either as they are.  Files are
 read and written by crvgpu.rootio (TTrees; the reference's writer makes RNTuples unless as_ttree=True, this one makes
 TTrees either way).
 """
@@ -52,8 +53,24 @@ class StepRows(StepTable):
     columns = Table.columns
 
 
-def _table(tree, cols):
+def _table(tree, cols, library="np"):
+    if library == "pd":
+        import pandas as pd
+        return pd.DataFrame(dict(cols))
     return StepRows(cols) if tree == "steps" else Table(cols)
+
+
+def _library(library):
+    """The reference returns pandas DataFrames: library None means "pd" where pandas is importable, else "np"."""
+    if library is None:
+        try:
+            import pandas  # noqa: F401
+            return "pd"
+        except ImportError:
+            return "np"
+    if library not in ("np", "pd"):
+        raise ValueError(f"library must be 'np' or 'pd', got {library!r}")
+    return library
 
 
 def expand(inputs):
@@ -64,18 +81,21 @@ def expand(inputs):
     return out
 
 
-def read(path, tree, columns=None):
-    """Tree `tree` of directory dump/ in `path` -> Table (StepRows for ``steps``)."""
+def read(path, tree, columns=None, library=None):
+    """Tree `tree` of directory dump/ in `path` -> a pandas DataFrame, as the reference returns (library "pd", the
+    default where pandas is importable), or a Table (StepRows for ``steps``; library "np", the default otherwise)."""
+    lib = _library(library)
     with rootio.RootFile(path) as f:
-        return _table(tree, f[f"{DIR}/{tree}"].arrays(columns))
+        return _table(tree, f[f"{DIR}/{tree}"].arrays(columns), lib)
 
 
-def read_many(paths, tree, columns=None):
-    """Rows of `tree` from every file (patterns expanded), concatenated in file order."""
-    parts = [read(p, tree, columns) for p in expand(paths)]
+def read_many(paths, tree, columns=None, library=None):
+    """Rows of `tree` from every file (patterns expanded), concatenated in file order (library as in read)."""
+    lib = _library(library)
+    parts = [read(p, tree, columns, "np") for p in expand(paths)]
     if not parts:
-        return _table(tree, {})
-    return _table(tree, {k: np.concatenate([t[k] for t in parts]) for k in parts[0]})
+        return _table(tree, {}, lib)
+    return _table(tree, {k: np.concatenate([t[k] for t in parts]) for k in parts[0]}, lib)
 
 
 def _first_of_groups(cols):
@@ -90,7 +110,7 @@ def _first_of_groups(cols):
 
 def livetime(paths):
     """Total CosmicLivetime [s] over the subruns of the given files (each (run, subrun) counted once)."""
-    s = read_many(paths, "subruns")
+    s = read_many(paths, "subruns", library="np")
     if len(s) == 0:
         return 0.0
     keep = _first_of_groups([s["run"], s["subrun"]])

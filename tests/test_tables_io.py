@@ -260,11 +260,11 @@ def test_tables_api_matches_the_reference_semantics(tmp_path, capsys):
     TB.write(p1, steps, parts, gen=gen, subruns=subruns, as_ttree=True)        # crv form
     TB.write(p2, {"steps": steps, "particles": parts, "subruns": subruns})      # core form
     assert "wrote" in capsys.readouterr().out
-    s = TB.read(p1, "steps")
+    s = TB.read(p1, "steps", library="np")
     assert isinstance(s, TB.StepRows) and len(s) == len(steps["bar"]) and s.bar is s["bar"]
     for k, v in steps.items():
         assert s[k].dtype == v.dtype and np.array_equal(s[k], v), k
-    both = TB.read_many([str(tmp_path / "crvsteps.*.root")], "steps", ["event", "bar"])
+    both = TB.read_many([str(tmp_path / "crvsteps.*.root")], "steps", ["event", "bar"], library="np")
     assert list(both) == ["event", "bar"] and np.array_equal(both["bar"], np.r_[steps["bar"], steps["bar"]])
     # livetime: each (run, subrun) once over both files
     assert TB.livetime([p1, p2]) == pytest.approx(1.5 + 2.0 + 0.25)
@@ -290,7 +290,10 @@ def test_tables_api_matches_the_reference_semantics(tmp_path, capsys):
     assert np.array_equal(am["mukey"], mk)
     # primary_muon_crossings: inner merge on (run, subrun, event, sp = primary muon key), groups in first-seen order
     sector_of_bar = np.array([0, 0, 1, 1, 2, 2])
-    cx = TB.primary_muon_crossings(s, TB.read(p1, "particles"), sector_of_bar)
+    cx = TB.primary_muon_crossings(s, TB.read(p1, "particles", library="np"), sector_of_bar)
+    with pytest.raises(ValueError):
+        TB.read(p1, "steps", library="arrow")
+    assert TB._library(None) in ("np", "pd")
     prim = {(parts["run"][i], parts["subrun"][i], parts["event"][i], parts["key"][i])
             for i in range(len(parts["key"])) if parts["isprim"][i] == 1 and abs(parts["pdg"][i]) == 13}
     groups = {}
@@ -323,7 +326,7 @@ def test_step_table_feeds_the_engine_host_path(tmp_path):
     steps, parts, gen = _dumper_tables(rng, 60)
     p = str(tmp_path / "s.root")
     TB.write(p, steps, parts)
-    s = TB.read(p, "steps")
+    s = TB.read(p, "steps", library="np")
     assert np.array_equal(GM.event_key(s), (steps["subrun"].astype(np.int64) << 20) | steps["event"])
     for a in "xyzt":
         assert np.array_equal(_col(s, a), 0.5 * (steps[f"{a}0"].astype(float) + steps[f"{a}1"].astype(float))), a
@@ -493,3 +496,16 @@ def test_pulses_tree_from_dumped_digis(tmp_path):
     assert np.array_equal(first, np.asarray(W["digi0"])[wf])
     assert np.array_equal(r["wfidx"].counts, -(-np.asarray(W["n"])[wf] // 12))
     assert np.array_equal(RT.event_key(r), np.asarray(W["ev"])[wf])
+
+
+def test_dataframes_where_pandas_is_installed(tmp_path):
+    """With pandas importable, read gives the reference's DataFrame (same columns and values)."""
+    pd = pytest.importorskip("pandas")
+    rng = np.random.default_rng(3)
+    steps, parts, gen = _dumper_tables(rng, 20)
+    p = str(tmp_path / "pd.root")
+    TB.write(p, steps, parts, gen=gen)
+    df = TB.read(p, "steps")
+    assert isinstance(df, pd.DataFrame) and list(df.columns) == list(steps)
+    for k, v in steps.items():
+        assert np.array_equal(df[k].to_numpy(), v), k
