@@ -78,7 +78,7 @@ class _Cursor:
         self.buf, self.pos, self.origin = buf, pos, origin
 
     def _u(self, fmt, n):
-        if self.pos + n > len(self.buf):
+        if self.pos < 0 or self.pos + n > len(self.buf):
             raise RootFormatError("record runs past the end of its buffer")
         v = struct.unpack_from(fmt, self.buf, self.pos)[0]
         self.pos += n
@@ -115,6 +115,8 @@ class _Cursor:
 
     def array(self, dtype, n):
         dt = np.dtype(dtype)
+        if n < 0 or self.pos < 0 or self.pos + n * dt.itemsize > len(self.buf):
+            raise RootFormatError("array runs past the end of its buffer")
         a = np.frombuffer(self.buf, dt, n, self.pos) if n else np.zeros(0, dt)
         self.pos += n * dt.itemsize
         return a
@@ -555,8 +557,13 @@ class Tree:
 
     def _column(self, b):
         dt, per, header = self._layout(b)
+        if not (0 <= b.write_basket < len(b.basket_entry)) or b.entries < 0:
+            raise RootFormatError(f"branch {b.name!r}: basket count outside its tables")
         if int(b.basket_entry[b.write_basket]) < b.entries or b.embedded_baskets:
             raise RootFormatError(f"branch {b.name!r}: entries held in an unflushed (embedded) basket are not read")
+        be = b.basket_entry[:b.write_basket + 1]
+        if be[0] != 0 or np.any(np.diff(be) < 0) or int(be[-1]) != b.entries:
+            raise RootFormatError(f"branch {b.name!r}: basket entry ranges do not cover its entries")
         jobs = []
         for i in range(b.write_basket):
             a, e = int(b.basket_entry[i]), int(b.basket_entry[i + 1])

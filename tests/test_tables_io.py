@@ -509,3 +509,30 @@ def test_dataframes_where_pandas_is_installed(tmp_path):
     assert isinstance(df, pd.DataFrame) and list(df.columns) == list(steps)
     for k, v in steps.items():
         assert np.array_equal(df[k].to_numpy(), v), k
+
+
+def test_mutated_files_fail_cleanly(tmp_path):
+    """300 random mutations (byte flips, 1-8 bytes anywhere, zlib and LZ4 baskets): reading either gives the
+    original columns or raises RootFormatError / KeyError / ValueError; nothing crashes the process or reads outside
+    the file (the native LZ4 decoder checks every length, and its blocks carry a checksum)."""
+    rng = np.random.default_rng(21)
+    cols = {"a": rng.integers(0, 1000, 3000).astype(np.int32), "b": rng.normal(size=3000),
+            "j": R.JaggedArray.from_rows([rng.integers(0, 9, rng.integers(0, 5)).astype(np.int16) for _ in range(3000)],
+                                         np.int16)}
+    for mode, kw in (("zlib", dict(compression=101)), ("lz4", dict(compression=404, _compressor=_l4_blocks))):
+        p = str(tmp_path / f"m_{mode}.root")
+        R.write(p, {"dump/t": cols}, basket_bytes=4096, **kw)
+        raw = open(p, "rb").read()
+        for k in range(150):
+            bad = bytearray(raw)
+            for _ in range(int(rng.integers(1, 9))):
+                bad[int(rng.integers(0, len(raw)))] ^= int(rng.integers(1, 256))
+            q = str(tmp_path / "mut.root")
+            open(q, "wb").write(bytes(bad))
+            try:
+                with R.RootFile(q) as f:
+                    got = f["dump/t"].arrays()
+            except (R.RootFormatError, KeyError, ValueError):
+                continue
+            assert got["a"].shape == cols["a"].shape and got["b"].dtype == cols["b"].dtype
+            assert len(got["j"]) == len(cols["j"])
