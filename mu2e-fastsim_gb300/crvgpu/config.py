@@ -209,10 +209,73 @@ class ChainConfig:
     feb_phase_width: Optional[float] = None    # None = one digitisation period
     feb_phase_key: str = "roc_feb"            # FEB_PHASE_KEYS
     backend: str = "cuda"
-    precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (float-float LM solve, FP64 absolute times)
+    precision: str = "fp64"                     # "fp64" plain, or "fp32" mixed (float-float LM solve, FP64 times)
     # the reference's lookup-table response block (sectors {name: (table, reflector, yield_per_mev)}, yield scales,
     # speed / attenuation ratios): charges() runs the lookup-table photon model with it when given lookup tables
     lookup: object = None
+    # the background model's rate factor (the reference's knob); inert: this engine takes no background overlays
+    background_scale: float = 1.0
+
+
+# light-propagation keys of the reference's knobs (crv/crvfastsim/chain.py:88-89): sectors, TAG = every muon tagger,
+# and modules
+PROP_KEYS = (("EX", "T1", "T2", "TAG") + tuple(f"EX{i}" for i in range(4)) + ("T10", "T11", "T20", "T21")
+             + tuple(f"M{i}" for i in range(1, 9)))
+# the reference's design-point knobs (crv/crvfastsim/chain.py:91-97): name -> (block, field) of this engine's config;
+# "response" sets the analytic model's field and the lookup-table block's; sector yields and light-propagation ratios
+# live in the lookup-table block
+KNOBS = {"photon_yield_scale": ("response", "photon_yield_scale"), "time_constant": ("sipm", "time_constant"),
+         "cross_talk": ("sipm", "cross_talk"), "min_voltage": ("waveform", "min_voltage"),
+         "wf_noise": ("waveform", "noise"), "pe_stretch": ("waveform", "single_pe_stretch"),
+         "background_scale": (None, "background_scale"),
+         **{f"yield_{n}": ("sector_yield", n) for n in ("EX", "T1", "T2", "TAG")},
+         **{f"speed_{n}": ("speed_ratio", n) for n in PROP_KEYS},
+         **{f"atten_{n}": ("atten_ratio", n) for n in PROP_KEYS}}
+
+
+def _with(obj, **kw):
+    """A copy of a dataclass or plain-attribute object with fields replaced."""
+    import dataclasses
+    import types
+    if dataclasses.is_dataclass(obj):
+        return dataclasses.replace(obj, **kw)
+    return types.SimpleNamespace(**{**vars(obj), **kw})
+
+
+def apply_knobs(cfg: "ChainConfig", knobs) -> "ChainConfig":
+    """ChainConfig with knob overrides {name: value} (KNOBS), as the reference's apply_knobs
+    (crv/crvfastsim/chain.py:117-144): unknown names raise KeyError, non-positive propagation ratios ValueError.  A
+    sector-yield or propagation knob needs the lookup-table response block (cfg.lookup), whose sectors they change
+    (yield_TAG: every muon tagger M1..M8)."""
+    if cfg.waveform is None:
+        cfg = replace(cfg, waveform=WaveformConfig())
+    for k, v in (knobs or {}).items():
+        if k not in KNOBS:
+            raise KeyError(f"unknown knob {k}; known: {sorted(KNOBS)}")
+        blk, fld = KNOBS[k]
+        if blk in ("sector_yield", "speed_ratio", "atten_ratio"):
+            if cfg.lookup is None:
+                raise ValueError(f"knob {k} acts on the lookup-table response block (ChainConfig.lookup): unset")
+            if blk == "sector_yield":
+                names = [f"M{i}" for i in range(1, 9)] if fld == "TAG" else [fld]
+                secs = dict(cfg.lookup.sectors)
+                for nm in names:
+                    secs[nm] = _with(secs[nm], yield_per_mev=float(v))
+                cfg = replace(cfg, lookup=_with(cfg.lookup, sectors=secs))
+            else:
+                if not float(v) > 0:
+                    raise ValueError(f"knob {k} must be positive, got {v}")
+                d = {**(getattr(cfg.lookup, blk, None) or {}), fld: float(v)}
+                cfg = replace(cfg, lookup=_with(cfg.lookup, **{blk: d}))
+            continue
+        if blk is None:
+            cfg = replace(cfg, **{fld: float(v)})
+        elif blk == "response":
+            cfg = replace(cfg, response=replace(cfg.response, **{fld: float(v)}),
+                          lookup=_with(cfg.lookup, **{fld: float(v)}) if cfg.lookup is not None else None)
+        else:
+            cfg = replace(cfg, **{blk: replace(getattr(cfg, blk), **{fld: float(v)})})
+    return cfg
 
 
 def _fields_of(cls, obj, **over):
@@ -239,7 +302,7 @@ def from_reference(cfg, precision="fp64"):
               waveform=_fields_of(WaveformConfig, getattr(cfg, "waveform", None)),
               pulse_reco=_fields_of(RecoConfig, getattr(cfg, "pulse_reco", None)),
               finder=_fields_of(FinderConfig, getattr(cfg, "finder", None)))
-    for k in ("window", "noise", "feb_phase_width", "feb_phase_key"):
+    for k in ("window", "noise", "feb_phase_width", "feb_phase_key", "background_scale"):
         if hasattr(cfg, k):
             kw[k] = getattr(cfg, k)
     return ChainConfig(**kw)

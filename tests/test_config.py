@@ -95,3 +95,39 @@ def test_photon_maps_outside_the_capability_are_refused(weights):
     one = np.zeros((40, 40))
     one[39, 39] = 1.0
     check_photon_map(one)
+
+
+def test_knobs_follow_the_reference_table_and_semantics():
+    """apply_knobs (crv/crvfastsim/chain.py:91-144): the reference's knob names; each sets its block's field; yield
+    knobs change the lookup-table block's sectors (yield_TAG every tagger M1..M8); propagation ratios must be positive;
+    unknown names raise KeyError."""
+    from types import SimpleNamespace
+    from crvgpu import config as CF
+    prop = ("EX", "T1", "T2", "TAG", "EX0", "EX1", "EX2", "EX3", "T10", "T11", "T20", "T21") + \
+        tuple(f"M{i}" for i in range(1, 9))
+    names = {"photon_yield_scale", "time_constant", "cross_talk", "min_voltage", "wf_noise", "pe_stretch",
+             "background_scale", "yield_EX", "yield_T1", "yield_T2", "yield_TAG"} | \
+        {f"{q}_{n}" for q in ("speed", "atten") for n in prop}
+    assert set(CF.KNOBS) == names
+    sec = lambda y: SimpleNamespace(table="t", reflector=0, yield_per_mev=y)  # noqa: E731
+    lk = SimpleNamespace(sectors={"EX": sec(1.0), "T1": sec(2.0), **{f"M{i}": sec(3.0) for i in range(1, 9)}},
+                         photon_yield_scale=1.0, speed_ratio={}, atten_ratio={"EX": 0.5})
+    base = CF.ChainConfig(lookup=lk)
+    cfg = CF.apply_knobs(base, {"photon_yield_scale": 1.2, "time_constant": 11.0, "cross_talk": 0.03,
+                                "min_voltage": 0.01, "wf_noise": 5e-4, "pe_stretch": 1.1, "background_scale": 2.0,
+                                "yield_TAG": 4.0, "yield_EX": 5.0, "speed_EX1": 0.9, "atten_EX": 1.1})
+    assert cfg.response.photon_yield_scale == 1.2 and cfg.lookup.photon_yield_scale == 1.2
+    assert cfg.sipm.time_constant == 11.0 and cfg.sipm.cross_talk == 0.03
+    assert (cfg.waveform.min_voltage, cfg.waveform.noise, cfg.waveform.single_pe_stretch) == (0.01, 5e-4, 1.1)
+    assert cfg.background_scale == 2.0
+    assert all(cfg.lookup.sectors[f"M{i}"].yield_per_mev == 4.0 for i in range(1, 9))
+    assert cfg.lookup.sectors["EX"].yield_per_mev == 5.0 and cfg.lookup.sectors["T1"].yield_per_mev == 2.0
+    assert cfg.lookup.speed_ratio == {"EX1": 0.9} and cfg.lookup.atten_ratio == {"EX": 1.1}
+    assert lk.sectors["EX"].yield_per_mev == 1.0 and base.sipm.time_constant != 11.0   # inputs untouched
+    with pytest.raises(KeyError, match="unknown knob"):
+        CF.apply_knobs(base, {"nope": 1})
+    with pytest.raises(ValueError):
+        CF.apply_knobs(base, {"speed_EX": 0.0})
+    with pytest.raises(ValueError):
+        CF.apply_knobs(CF.ChainConfig(), {"yield_EX": 3.0})
+    assert CF.apply_knobs(CF.ChainConfig(), {}).waveform == CF.WaveformConfig()
