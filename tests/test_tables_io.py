@@ -536,3 +536,34 @@ def test_mutated_files_fail_cleanly(tmp_path):
                 continue
             assert got["a"].shape == cols["a"].shape and got["b"].dtype == cols["b"].dtype
             assert len(got["j"]) == len(cols["j"])
+
+
+def test_against_uproot_where_installed(tmp_path):
+    """Parity with the reference's ROOT library where it is installed (not in this image): a file written here reads
+    the same through uproot, and TTrees uproot writes (flat columns, counted arrays) read the same here."""
+    uproot = pytest.importorskip("uproot")
+    rng = np.random.default_rng(12)
+    n = 5000
+    cols = {"run": np.full(n, 1400, np.uint32), "event": np.arange(n, dtype=np.uint32),
+            "bar": rng.integers(0, 5000, n).astype(np.int32), "t0": rng.uniform(0, 1e3, n),
+            "edep": rng.uniform(0, 5, n).astype(np.float32), "flag": rng.random(n) < 0.5}
+    ours = str(tmp_path / "ours.root")
+    R.write(ours, {"dump/steps": cols}, basket_bytes=4096)
+    with uproot.open(ours) as f:
+        got = f["dump/steps"].arrays(library="np")
+    for k, v in cols.items():
+        assert np.array_equal(got[k], v), k
+    theirs = str(tmp_path / "theirs.root")
+    counts = rng.integers(0, 6, n)
+    jag = [rng.integers(-9, 9, c).astype(np.int16) for c in counts]
+    with uproot.recreate(theirs) as f:
+        f.mktree("dump/steps", {k: v.dtype for k, v in cols.items()})
+        f["dump/steps"].extend(cols)
+        import awkward as ak
+        f["crvdump/digis"] = {"adc": ak.Array([list(a) for a in jag])}
+    with R.RootFile(theirs) as f:
+        got = f["dump/steps"].arrays()
+        adc = f["crvdump/digis"].arrays()["adc"]
+    for k, v in cols.items():
+        assert np.array_equal(got[k], v), k
+    assert adc.tolist() == [a.tolist() for a in jag]
